@@ -1,0 +1,403 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 refinement engine: pins/s per refinement pass.
+
+Workload (default "c2"): all six metrics (CN, TV, TM, MSM, MSV, MSRV), each on
+its own resident instance: K = 256, eps = 0.05 (C = (W/K) * 1.05),
+4,194,304 vertices and 4,194,304 nets, net sizes Zipf(2.1) clipped to
+[2, 10000], pins drawn by a Zipf(1.5) vertex popularity, source = first drawn
+pin, vertex weight = degree; 10 refinement passes.  Synthetic and seeded.
+
+A step is the full refinement (all passes) of the six instances, each restarted
+from its streaming initial partition.  metric = pins * passes / refinement
+seconds, summed over the six metrics (the reference's "Refinement took" span).
+
+  value   device-resident: CUDA events on the engine's stream around each
+          refinement launch
+  e2e     through the C ABI with host buffers: host -> device upload of the
+          state, the passes, device -> host copy of the part vector
+  cpu_baseline / --impl reference: the reference's own OpenMP partition_par()
+          (compiled from its sources into oracle/_ref) on the host cores
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRICS = ["CN", "TV", "TM", "MSM", "MSV", "MSRV"]
+WORKLOADS = {
+    "c2": dict(nov=4_194_304, noe=4_194_304, alpha=2.1, lo=2, hi=10000, beta=1.5, weight_rule=1, K=256,
+               eps=1.05, passes=10, seed=0),
+    "c1": dict(nov=16_384, noe=16_384, alpha=0.0, lo=2, hi=16, beta=0.0, weight_rule=0, K=8, eps=1.03,
+               passes=5, seed=0),
+}
+
+
+def spec_for(fp, w, scale=1, unit_weights=False):
+    nov, noe = max(w["nov"] // scale, 1024), max(w["noe"] // scale, 1024)
+    if w["alpha"] > 0:
+        return fp.GenSpec.zipf(nov, noe, w["alpha"], w["lo"], min(w["hi"], nov), beta=w["beta"],
+                               weight_rule=0 if unit_weights else w["weight_rule"], seed=w["seed"])
+    return fp.GenSpec.column_net(nov, noe, w["lo"], w["hi"], seed=w["seed"])
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device=0):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except FileNotFoundError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, val in zip(names, f[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def algorithmic_bytes(metric, hg, ep_len, moved_mask, K):
+    """Bytes one refinement pass must move at minimum (per-pass figure, see
+    the design doc): vertex CSR, per-pin net offset + part count, the listed parts
+    scanned, the part vector, part sizes, and the list slots a move rewrites.
+    The TM/MSM/MSV/MSRV passes also read the source and its part per pin, the
+    counts of the scanned slots, and one K-row per evaluated vertex (TM/MSM)."""
+    sizes = np.diff(hg.nptr).astype(np.int64)
+    lam = ep_len.astype(np.int64)
+    P = hg.pins
+    scanned = int(np.sum(sizes * lam))                 # sum over (v, e) of lambda_e
+    deg = np.diff(hg.vptr).astype(np.int64)
+    if metric == "CN":
+        two = lam == 2
+        return 4 * (hg.noe + 1) + 8 * hg.noe + int(np.sum(8 * sizes[two]))
+    b = 4 * (hg.nov + 1) + 4 * P + 8 * P + 4 * scanned + 4 * hg.nov + 8 * K
+    if moved_mask is not None and moved_mask.any():
+        vv = np.nonzero(moved_mask)[0]
+        net_lam = lam[hg.vnets.astype(np.int64)]
+        per_v = np.add.reduceat(net_lam, hg.vptr[:-1].astype(np.int64)) if P else np.zeros(hg.nov, np.int64)
+        per_v[deg == 0] = 0
+        b += 16 * int(per_v[vv].sum())
+    if metric != "TV":
+        b += 8 * P + 4 * scanned + 4 * K
+        if metric in ("TM", "MSM"):
+            b += 4 * K * hg.nov
+    return b
+
+
+def run_ours(args):
+    import torch
+    import fastpartitioner_gb300 as fp
+
+    dist = int(os.environ.get("WORLD_SIZE", "1")) > 1
+    rank = int(os.environ.get("RANK", "0"))
+    if dist:
+        import torch.distributed as tdist
+        local = int(os.environ.get("LOCAL_RANK", "0"))
+        torch.cuda.set_device(local)
+        tdist.init_process_group("nccl")
+        device = local
+    else:
+        device = 0
+        torch.cuda.set_device(0)
+    w = WORKLOADS[args.config]
+    passes = args.passes or w["passes"]
+    metrics = args.metrics.split(",") if args.metrics else METRICS
+    t_gen = time.time()
+    hg = fp.generate(spec_for(fp, w, args.scale))
+    t_gen = time.time() - t_gen
+    stream = torch.cuda.Stream(device=device)
+    eng = fp.Engine(device)
+    eng.set_stream(stream.cuda_stream)
+    insts = {}
+    t_init = time.time()
+    for m in metrics:
+        inst = eng.instance(hg, w["K"], m, w["eps"])
+        inst.initial_partition()
+        insts[m] = inst
+    t_init = time.time() - t_init
+
+    def one_step(timed):
+        out = {}
+        for m in metrics:
+            inst = insts[m]
+            inst.reset_state()
+            torch.cuda.synchronize()
+            if timed:
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+            inst.refine(passes)
+            if timed:
+                e1.record(stream)
+                e1.synchronize()
+                out[m] = e0.elapsed_time(e1) / 1e3
+        return out
+
+    for _ in range(args.warmup):
+        one_step(False)
+    if dist:
+        tdist.barrier()
+    torch.cuda.synchronize()
+    per_metric = {m: [] for m in metrics}
+    launches = 0
+    with Clocks(device) as clk:
+        for _ in range(args.steps):
+            r = one_step(True)
+            for m, t in r.items():
+                per_metric[m].append(t)
+            launches += len(metrics)
+    torch.cuda.synchronize()
+    total_t = sum(sum(v) for v in per_metric.values())
+    if dist:
+        tt = torch.tensor([total_t], device=f"cuda:{device}", dtype=torch.float64)
+        tdist.all_reduce(tt, op=tdist.ReduceOp.MAX)
+        total_t = float(tt.item())
+    work = hg.pins * passes * len(metrics) * args.steps
+    value = work / total_t * (int(os.environ.get("WORLD_SIZE", "1")) if dist else 1)
+
+    # e2e: host state -> device, passes, part vector -> host, wall clock.
+    e2e_t = 0.0
+    h2d = d2h = 0
+    for _ in range(args.steps):
+        for m in metrics:
+            inst = insts[m]
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            inst.reset_state()
+            inst.refine(passes)
+            pv = inst.partition()
+            t1 = time.perf_counter()
+            e2e_t += t1 - t0
+            h2d += inst.state_bytes()
+            d2h += pv.nbytes
+    e2e_value = work / e2e_t
+
+    # Roofline of the dominant kernel (the refinement launch of each metric):
+    # algorithmic bytes of the passes it runs / its average duration.
+    peak, peak_kind = peaks()
+    bytes_per_launch = {}
+    for m in metrics:
+        inst = insts[m]
+        inst.reset_state()
+        tot = 0
+        for p in range(passes):
+            ln, _, _ = inst.lists()
+            before = inst.partition()
+            inst.refine(1)
+            after = inst.partition()
+            tot += algorithmic_bytes(m, hg, ln, before != after, w["K"])
+        bytes_per_launch[m] = tot
+    avg_bytes = statistics.mean(bytes_per_launch.values())
+    avg_launch = total_t / launches
+    achieved = avg_bytes / avg_launch / 1e9
+    traffic = None
+    prof = ROOT / "profiles" / "traffic.json"
+    if prof.exists():
+        try:
+            traffic = json.loads(prof.read_text()).get(args.config)
+        except Exception:
+            traffic = None
+
+    cpu = None
+    if not args.no_cpu_baseline and rank == 0:
+        cpu = cpu_baseline(fp, w, args)
+    clocks = clk.summary()
+    line = {
+        "metric": "pins/s per refine pass (pins x passes / refinement seconds, six metrics)",
+        "value": value,
+        "unit": "pins/s",
+        "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": total_t / args.steps * 1e3,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "int32",
+        "data": "synthetic (seeded generator, fastpartitioner_gb300/csrc/fp_gen.cpp)",
+        "config": {
+            "workload": f"{args.config}: {hg.nov} vertices, {hg.noe} nets, {hg.pins} pins, K={w['K']}, "
+                        f"eps factor {w['eps']}, {passes} passes, metrics {','.join(metrics)}",
+            "weights": "degree" if w["weight_rule"] else "unit",
+            "l2": "inputs larger than L2 (per-instance state and CSRs exceed 129 MB)" if hg.pins > 8_000_000
+                  else "inputs smaller than L2",
+            "per_metric_pins_per_s": {m: hg.pins * passes * args.steps / sum(v) for m, v in per_metric.items()},
+            "per_metric_ms": {m: 1e3 * statistics.mean(v) for m, v in per_metric.items()},
+            "scale": args.scale,
+            "generate_s": round(t_gen, 2),
+            "host_initial_partition_s": round(t_init, 2),
+            "parallelism": "one instance per metric, one GPU (replicas only across GPUs)",
+        },
+        "e2e": {"value": e2e_value, "unit": "pins/s", "h2d_bytes_per_step": h2d // args.steps,
+                "d2h_bytes_per_step": d2h // args.steps},
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_kind": peak_kind, "traffic": traffic,
+                     "algorithmic_bytes_per_launch": int(avg_bytes), "avg_launch_s": avg_launch},
+        "cpu_baseline": cpu,
+        "clocks": clocks,
+    }
+    for inst in insts.values():
+        inst.close()
+    eng.close()
+    if dist:
+        tdist.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def reference_timing(w, args, scale, passes, metrics, threads):
+    """Runs the reference's partition_par (threads > 1) on a bounded sample and
+    returns (pins * passes, refinement seconds, kind)."""
+    import fastpartitioner_gb300 as fp
+    import oracle
+    hg = fp.generate(spec_for(fp, w, scale, unit_weights=True))
+    if oracle.reference_available():
+        tot_t, tot_w = 0.0, 0
+        for m in metrics:
+            r = oracle.run_reference(hg, w["K"], m, passes, threads=threads, capture=False)
+            tot_t += r["refine_seconds"]
+            tot_w += hg.pins * passes
+        return tot_w, tot_t, "reference", hg
+    tot_t, tot_w = 0.0, 0
+    for m in metrics:
+        o = oracle.run_oracle(hg, w["K"], m, passes, eps_factor=1.05)
+        tot_t += o["refine_seconds"]
+        tot_w += hg.pins * passes
+    return tot_w, tot_t, "port", hg
+
+
+def cpu_baseline(fp, w, args):
+    import oracle  # noqa: F401
+    threads = os.cpu_count() or 1
+    scale = args.cpu_scale
+    passes = args.cpu_passes
+    metrics = args.metrics.split(",") if args.metrics else METRICS
+    work, t, kind, hg = reference_timing(w, args, scale, passes, metrics, threads)
+    return {"value": work / t, "unit": "pins/s", "cores": threads if kind == "reference" else 1, "kind": kind,
+            "sample": f"{hg.nov} vertices / {hg.pins} pins ({args.config} distribution at 1/{scale} scale, unit "
+                      f"weights: the reference has none), {passes} passes of each of {','.join(metrics)}, "
+                      f"partition_par with {threads} threads" if kind == "reference" else "oracle restatement"}
+
+
+def run_reference_arm(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import oracle
+    try:
+        oracle.build()
+    except Exception:
+        pass
+    w = WORKLOADS[args.config]
+    metrics = args.metrics.split(",") if args.metrics else METRICS
+    threads = os.cpu_count() or 1
+    passes = args.cpu_passes
+    vals = []
+    kind = None
+    hg = None
+    for i in range(args.warmup + args.steps):
+        work, t, kind, hg = reference_timing(w, args, args.cpu_scale, passes, metrics, threads)
+        if i >= args.warmup:
+            vals.append((work, t))
+    tot_w = sum(a for a, _ in vals)
+    tot_t = sum(b for _, b in vals)
+    value = tot_w / tot_t
+    sample = (f"{hg.nov} vertices / {hg.pins} pins ({args.config} distribution at 1/{args.cpu_scale} scale, unit "
+              f"weights), {passes} passes of each of {','.join(metrics)}")
+    line = {
+        "metric": "pins/s per refine pass (pins x passes / refinement seconds, six metrics)",
+        "value": value, "unit": "pins/s", "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": tot_t / len(vals) * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+        "data": "synthetic (seeded generator)", "impl": "reference",
+        "config": {"workload": f"{args.config} sample: {sample}", "threads": threads},
+        "cpu_baseline": {"value": value, "unit": "pins/s", "cores": threads if kind == "reference" else 1,
+                         "kind": kind, "sample": sample},
+        "e2e": {"value": value, "unit": "pins/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="c2", choices=sorted(WORKLOADS))
+    ap.add_argument("--scale", type=int, default=1, help="divide vertex/net counts (quick runs)")
+    ap.add_argument("--passes", type=int, default=0)
+    ap.add_argument("--metrics", default="")
+    ap.add_argument("--cpu-scale", type=int, default=8)
+    ap.add_argument("--cpu-passes", type=int, default=2)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference_arm(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

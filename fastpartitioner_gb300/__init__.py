@@ -1,0 +1,432 @@
+"""GB300 refinement engine for FastPartitioner hypergraph partitions.
+
+The package is a thin host-side mirror of FastPartitioner's per-metric
+``partition_gpu()`` entry points over the C ABI in ``include/fastpart.h``.  The
+refinement passes and the metric evaluation run as CUDA kernels for sm_103a in
+``libfastpart.so``; there is no CPU fallback.  If the library is missing or no
+GPU is visible, the calls that need the device raise ``FastPartError``.
+
+Typical use::
+
+    import fastpartitioner_gb300 as fp
+    hg = fp.generate(fp.GenSpec.column_net(16384, 16384, 2, 16, seed=0))
+    with fp.Engine() as eng:
+        inst = eng.instance(hg, K=8, metric="TV")
+        inst.initial_partition()
+        before = inst.metrics()
+        inst.refine(5)
+        after = inst.metrics()
+"""
+from __future__ import annotations
+
+import ctypes as C
+import dataclasses
+from pathlib import Path
+from typing import Optional, Sequence
+
+import numpy as np
+
+_PKG = Path(__file__).resolve().parent
+_LIB_PATH = _PKG / "libfastpart.so"
+
+FP_OK = 0
+ERRORS = {
+    -1: "invalid argument or malformed hypergraph",
+    -2: "CUDA runtime error",
+    -3: "out of memory",
+    -4: "device-side wait timed out",
+    -5: "input on which the reference behaviour is undefined",
+    -6: "call out of order",
+    -7: "file error",
+}
+
+# Metric ids of the C ABI; the reference's directory / print names map onto them.
+METRICS = {"CN": 0, "TV": 1, "TM": 2, "MSM": 3, "MSV": 4, "MSRV": 5,
+           "MGM": 3, "MGV": 4, "MGAV": 5}
+METRIC_NAMES = ["CN", "TV", "TM", "MSM", "MSV", "MSRV"]
+# Order of fp_metrics() values: the order the reference prints them.
+OUTPUT_ORDER = ["TV", "CN", "TM", "MSM", "MSV", "MSRV"]
+
+
+class FastPartError(RuntimeError):
+    def __init__(self, status: int, what: str = ""):
+        self.status = status
+        super().__init__(f"{what}: {ERRORS.get(status, 'unknown status')} ({status})")
+
+
+def metric_id(metric) -> int:
+    if isinstance(metric, (int, np.integer)):
+        if not 0 <= int(metric) <= 5:
+            raise ValueError(f"unknown metric {metric}")
+        return int(metric)
+    try:
+        return METRICS[str(metric).upper()]
+    except KeyError:
+        raise ValueError(f"unknown metric {metric!r}") from None
+
+
+# ---------------------------------------------------------------- C types
+
+class _Hypergraph(C.Structure):
+    _fields_ = [("nov", C.c_int32), ("noe", C.c_int32), ("pins", C.c_int64),
+                ("vptr", C.c_void_p), ("vnets", C.c_void_p), ("nptr", C.c_void_p),
+                ("npins", C.c_void_p), ("src", C.c_void_p), ("weights", C.c_void_p),
+                ("ordering", C.c_void_p)]
+
+
+class _GenParams(C.Structure):
+    _fields_ = [("nov", C.c_int32), ("noe", C.c_int32), ("size_lo", C.c_int32),
+                ("size_hi", C.c_int32), ("size_alpha", C.c_double), ("pin_beta", C.c_double),
+                ("src_rule", C.c_int32), ("sort_pins", C.c_int32), ("weight_rule", C.c_int32),
+                ("seed", C.c_uint64)]
+
+
+_lib_handle = None
+
+
+def library_path() -> Path:
+    return _LIB_PATH
+
+
+def lib():
+    """The loaded engine library (raises FastPartError-free OSError if absent)."""
+    global _lib_handle
+    if _lib_handle is None:
+        if not _LIB_PATH.exists():
+            raise OSError(f"{_LIB_PATH} is not built; run fastpartitioner_gb300.build.build()")
+        L = C.CDLL(str(_LIB_PATH))
+        vp, i32, i64, dbl = C.c_void_p, C.c_int32, C.c_int64, C.c_double
+        pp = C.POINTER(C.c_void_p)
+        sig = {
+            "fp_validate": ([C.POINTER(_Hypergraph)], C.c_int),
+            "fp_ctx_create": ([i32, pp], C.c_int),
+            "fp_ctx_destroy": ([vp], C.c_int),
+            "fp_ctx_set_stream": ([vp, vp], C.c_int),
+            "fp_instance_create": ([vp, C.POINTER(_Hypergraph), i32, i32, dbl, pp], C.c_int),
+            "fp_instance_destroy": ([vp], C.c_int),
+            "fp_initial_partition": ([vp], C.c_int),
+            "fp_refine": ([vp, i32], C.c_int),
+            "fp_reset_state": ([vp], C.c_int),
+            "fp_metrics": ([vp, vp], C.c_int),
+            "fp_get_partition": ([vp, vp], C.c_int),
+            "fp_get_lists": ([vp, vp, vp, vp], C.c_int),
+            "fp_get_part_sizes": ([vp, vp], C.c_int),
+            "fp_get_moves": ([vp, vp, i32], C.c_int),
+            "fp_last_launches": ([vp, vp], C.c_int),
+            "fp_strerror": ([C.c_int], C.c_char_p),
+            "fp_generate": ([C.POINTER(_GenParams), pp], C.c_int),
+            "fp_graph_from_nets": ([i32, i32, vp, vp, vp, pp], C.c_int),
+            "fp_read_patohlike": ([C.c_char_p, i32, i32, pp], C.c_int),
+            "fp_write_patohlike": ([vp, C.c_char_p], C.c_int),
+            "fp_graph_view": ([vp, C.POINTER(_Hypergraph)], C.c_int),
+            "fp_graph_destroy": ([vp], C.c_int),
+            "fp_partition_gpu": ([i32, vp, vp, vp, i32, i32, i64, vp, vp, i32, vp, C.c_char_p,
+                                  i32, i32, vp, vp, vp, vp], C.c_int),
+        }
+        for name, (args, res) in sig.items():
+            f = getattr(L, name)
+            f.argtypes = args
+            f.restype = res
+        _lib_handle = L
+    return _lib_handle
+
+
+def _check(status: int, what: str):
+    if status != FP_OK:
+        raise FastPartError(status, what)
+
+
+def _ptr(a: Optional[np.ndarray]):
+    return None if a is None else a.ctypes.data
+
+
+# ---------------------------------------------------------------- hypergraphs
+
+@dataclasses.dataclass
+class Hypergraph:
+    """A hypergraph as the engine consumes it.
+
+    vptr/vnets: nets of each vertex in scan order (the reference's row_ptr /
+    col_ind); nptr/npins: pins of each net (row_ptr_inv / col_ind_inv); src: the
+    source vertex of each net; weights: vertex weights or None (unit);
+    ordering: visiting order or None (vertex ids)."""
+    nov: int
+    noe: int
+    vptr: np.ndarray
+    vnets: np.ndarray
+    nptr: np.ndarray
+    npins: np.ndarray
+    src: np.ndarray
+    weights: Optional[np.ndarray] = None
+    ordering: Optional[np.ndarray] = None
+
+    def __post_init__(self):
+        self.vptr = np.ascontiguousarray(self.vptr, dtype=np.uint32)
+        self.vnets = np.ascontiguousarray(self.vnets, dtype=np.uint32)
+        self.nptr = np.ascontiguousarray(self.nptr, dtype=np.uint32)
+        self.npins = np.ascontiguousarray(self.npins, dtype=np.uint32)
+        self.src = np.ascontiguousarray(self.src, dtype=np.int32)
+        if self.weights is not None:
+            self.weights = np.ascontiguousarray(self.weights, dtype=np.int32)
+        if self.ordering is not None:
+            self.ordering = np.ascontiguousarray(self.ordering, dtype=np.int32)
+
+    @property
+    def pins(self) -> int:
+        return int(self.vnets.size)
+
+    def validate(self) -> int:
+        """fp_validate status (0 when the engine accepts the hypergraph)."""
+        v = self.view()
+        return int(lib().fp_validate(C.byref(v)))
+
+    def view(self) -> _Hypergraph:
+        return _Hypergraph(self.nov, self.noe, self.pins, _ptr(self.vptr), _ptr(self.vnets),
+                           _ptr(self.nptr), _ptr(self.npins), _ptr(self.src),
+                           _ptr(self.weights), _ptr(self.ordering))
+
+    @staticmethod
+    def from_nets(nov: int, nptr, npins, src=None) -> "Hypergraph":
+        """Builds vertex -> nets as the transpose of net -> pins (nets ascending
+        per vertex), the orientation of the TV and CN drivers."""
+        nptr = np.ascontiguousarray(nptr, dtype=np.uint32)
+        npins = np.ascontiguousarray(npins, dtype=np.uint32)
+        noe = nptr.size - 1
+        s = None if src is None else np.ascontiguousarray(src, dtype=np.int32)
+        g = C.c_void_p()
+        _check(lib().fp_graph_from_nets(nov, noe, _ptr(nptr), _ptr(npins), _ptr(s), C.byref(g)),
+               "fp_graph_from_nets")
+        return _take_graph(g)
+
+    def save_fphg(self, path) -> None:
+        """Binary instance file read by the oracle's reference driver."""
+        with open(path, "wb") as f:
+            f.write(b"FPHG1\0\0\0")
+            f.write(np.array([self.nov, self.noe], dtype=np.int32).tobytes())
+            f.write(np.array([self.pins], dtype=np.int64).tobytes())
+            for a in (self.vptr, self.vnets, self.nptr, self.npins):
+                f.write(a.astype(np.uint32).tobytes())
+            f.write(self.src.astype(np.int32).tobytes())
+
+    @staticmethod
+    def load_fphg(path) -> "Hypergraph":
+        raw = Path(path).read_bytes()
+        if raw[:5] != b"FPHG1":
+            raise ValueError("not an FPHG1 file")
+        nov, noe = np.frombuffer(raw, np.int32, 2, 8)
+        pins = int(np.frombuffer(raw, np.int64, 1, 16)[0])
+        off = 24
+        arrs = []
+        for n, dt in ((nov + 1, np.uint32), (pins, np.uint32), (noe + 1, np.uint32), (pins, np.uint32),
+                      (noe, np.int32)):
+            arrs.append(np.frombuffer(raw, dt, int(n), off).copy())
+            off += 4 * int(n)
+        return Hypergraph(int(nov), int(noe), *arrs)
+
+
+def _take_graph(g: C.c_void_p) -> Hypergraph:
+    v = _Hypergraph()
+    try:
+        _check(lib().fp_graph_view(g, C.byref(v)), "fp_graph_view")
+        pins = v.pins
+
+        def arr(p, n, dt):
+            if n == 0:
+                return np.zeros(0, dt)
+            return np.ctypeslib.as_array(C.cast(p, C.POINTER(np.ctypeslib.as_ctypes_type(dt))), (n,)).copy()
+        hg = Hypergraph(v.nov, v.noe, arr(v.vptr, v.nov + 1, np.uint32), arr(v.vnets, pins, np.uint32),
+                        arr(v.nptr, v.noe + 1, np.uint32), arr(v.npins, pins, np.uint32),
+                        arr(v.src, v.noe, np.int32),
+                        arr(v.weights, v.nov, np.int32) if v.weights else None)
+    finally:
+        lib().fp_graph_destroy(g)
+    return hg
+
+
+@dataclasses.dataclass
+class GenSpec:
+    """Seeded synthetic hypergraph (see csrc/fp_gen.cpp)."""
+    nov: int
+    noe: int
+    size_lo: int
+    size_hi: int
+    size_alpha: float = 0.0     # > 0: Zipf(alpha) sizes clipped to [lo, hi]
+    pin_beta: float = 0.0       # > 0: Zipf(beta) pin popularity
+    src_rule: int = 0           # 0 lowest-id pin, 1 first drawn pin
+    sort_pins: int = 1
+    weight_rule: int = 0        # 0 unit, 1 degree
+    seed: int = 0
+
+    @staticmethod
+    def column_net(nov, noe, lo, hi, seed=0) -> "GenSpec":
+        """Column-net sparse pattern: uniform sizes in [lo, hi], uniform pins,
+        source = lowest-id pin, unit weights."""
+        return GenSpec(nov, noe, lo, hi, 0.0, 0.0, 0, 1, 0, seed)
+
+    @staticmethod
+    def zipf(nov, noe, alpha, lo, hi, beta=0.0, weight_rule=0, seed=0) -> "GenSpec":
+        """Zipf(alpha) net sizes clipped to [lo, hi]; pins by Zipf(beta)
+        popularity (uniform if beta == 0); source = first drawn pin."""
+        return GenSpec(nov, noe, lo, hi, alpha, beta, 1, 0, weight_rule, seed)
+
+
+def generate(spec: GenSpec) -> Hypergraph:
+    p = _GenParams(spec.nov, spec.noe, spec.size_lo, spec.size_hi, spec.size_alpha, spec.pin_beta,
+                   spec.src_rule, spec.sort_pins, spec.weight_rule, spec.seed)
+    g = C.c_void_p()
+    _check(lib().fp_generate(C.byref(p), C.byref(g)), "fp_generate")
+    return _take_graph(g)
+
+
+def read_patohlike(path, transpose: bool = True, write_cache: bool = False) -> Hypergraph:
+    """Reads a PaToH-like .hg file (and its .plbin cache, as the reference does).
+    transpose=True: file lines are nets (TV, CN drivers); False: file lines are
+    vertices (TM, MSM, MGV, MSRV drivers)."""
+    g = C.c_void_p()
+    _check(lib().fp_read_patohlike(str(path).encode(), int(transpose), int(write_cache), C.byref(g)),
+           "fp_read_patohlike")
+    return _take_graph(g)
+
+
+def write_patohlike(hg: Hypergraph, path) -> None:
+    """Writes hg's net -> pins CSR as a 0-based PaToH-like text file."""
+    lines = [f"0 {hg.nov} {hg.noe} {hg.pins}"]
+    for e in range(hg.noe):
+        lines.append(" ".join(map(str, hg.npins[hg.nptr[e]:hg.nptr[e + 1]])))
+    Path(path).write_text("\n".join(lines) + "\n")
+
+
+# ---------------------------------------------------------------- engine
+
+class Engine:
+    """One GPU and one stream (fp_ctx)."""
+
+    def __init__(self, device: int = 0):
+        self._ctx = C.c_void_p()
+        _check(lib().fp_ctx_create(device, C.byref(self._ctx)), "fp_ctx_create")
+
+    def set_stream(self, stream_handle: Optional[int]) -> None:
+        """Runs subsequent work on the given cudaStream_t (e.g. a torch stream's
+        ``cuda_stream``); None selects the engine's own stream."""
+        _check(lib().fp_ctx_set_stream(self._ctx, stream_handle), "fp_ctx_set_stream")
+
+    def instance(self, hg: Hypergraph, K: int, metric, eps_factor: float = 1.05) -> "Instance":
+        return Instance(self, hg, K, metric_id(metric), eps_factor)
+
+    def close(self):
+        if self._ctx:
+            lib().fp_ctx_destroy(self._ctx)
+            self._ctx = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Instance:
+    """A hypergraph resident on the device with its refinement state."""
+
+    def __init__(self, engine: Engine, hg: Hypergraph, K: int, metric: int, eps_factor: float):
+        self.engine = engine
+        self.hg = hg
+        self.K = K
+        self.metric = metric
+        self._h = C.c_void_p()
+        view = hg.view()
+        _check(lib().fp_instance_create(engine._ctx, C.byref(view), K, metric, eps_factor,
+                                        C.byref(self._h)), "fp_instance_create")
+
+    def initial_partition(self) -> None:
+        _check(lib().fp_initial_partition(self._h), "fp_initial_partition")
+
+    def refine(self, passes: int) -> None:
+        _check(lib().fp_refine(self._h, passes), "fp_refine")
+
+    def reset_state(self) -> None:
+        """Uploads the host-side stream result again (host -> device)."""
+        _check(lib().fp_reset_state(self._h), "fp_reset_state")
+
+    def state_bytes(self) -> int:
+        """Bytes fp_reset_state copies host -> device."""
+        K, m = self.K, self.metric
+        b = 4 * (self.hg.nov + self.hg.noe + 2 * self.hg.pins) + 4 * 5 * K
+        if m in (2, 3):
+            words = (K + 31) // 32
+            b += 4 * K * K + 2 * 4 * K * words
+        return b
+
+    def metrics(self) -> dict:
+        out = np.zeros(6, np.int64)
+        _check(lib().fp_metrics(self._h, _ptr(out)), "fp_metrics")
+        return dict(zip(OUTPUT_ORDER, map(int, out)))
+
+    def partition(self) -> np.ndarray:
+        pv = np.empty(self.hg.nov, np.int32)
+        _check(lib().fp_get_partition(self._h, _ptr(pv)), "fp_get_partition")
+        return pv
+
+    def lists(self):
+        """(ep_len, ep_part, ep_cnt): the ordered per-net part lists."""
+        ln = np.empty(self.hg.noe, np.int32)
+        pt = np.empty(self.hg.pins, np.int32)
+        ct = np.empty(self.hg.pins, np.int32)
+        _check(lib().fp_get_lists(self._h, _ptr(ln), _ptr(pt), _ptr(ct)), "fp_get_lists")
+        return ln, pt, ct
+
+    def part_sizes(self) -> np.ndarray:
+        s = np.empty(self.K, np.int32)
+        _check(lib().fp_get_part_sizes(self._h, _ptr(s)), "fp_get_part_sizes")
+        return s
+
+    def moves(self, n: int) -> np.ndarray:
+        m = np.zeros(n, np.int64)
+        _check(lib().fp_get_moves(self._h, _ptr(m), n), "fp_get_moves")
+        return m
+
+    def last_launches(self) -> int:
+        x = np.zeros(1, np.int64)
+        _check(lib().fp_last_launches(self._h, _ptr(x)), "fp_last_launches")
+        return int(x[0])
+
+    def close(self):
+        if self._h:
+            lib().fp_instance_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def partition_gpu(metric, row_ptr, col_ind, net_appearence, nov, noe, pins, edge_wgths, src_nodes, K,
+                  ordering, f_name="", REFI_OPT=1, REFI_ITER=1, row_ptr_inv=None, col_ind_inv=None):
+    """Mirror of the reference's partition_gpu(): same arguments, same stdout
+    lines.  Returns (part_vec, metrics_before, metrics_after) as numpy arrays /
+    dicts in the reference's print order."""
+    a = lambda x, dt: None if x is None else np.ascontiguousarray(x, dtype=dt)
+    row_ptr, col_ind = a(row_ptr, np.uint32), a(col_ind, np.uint32)
+    net_app, ew = a(net_appearence, np.uint32), a(edge_wgths, np.int32)
+    srcs, order = a(src_nodes, np.int32), a(ordering, np.int32)
+    rpi, cii = a(row_ptr_inv, np.uint32), a(col_ind_inv, np.uint32)
+    pv = np.empty(nov, np.int32)
+    mo = np.zeros(12, np.int64)
+    _check(lib().fp_partition_gpu(metric_id(metric), _ptr(row_ptr), _ptr(col_ind), _ptr(net_app), nov, noe,
+                                  pins, _ptr(ew), _ptr(srcs), K, _ptr(order), str(f_name).encode(), REFI_OPT,
+                                  REFI_ITER, _ptr(rpi), _ptr(cii), _ptr(pv), _ptr(mo)), "fp_partition_gpu")
+    return pv, dict(zip(OUTPUT_ORDER, map(int, mo[:6]))), dict(zip(OUTPUT_ORDER, map(int, mo[6:])))

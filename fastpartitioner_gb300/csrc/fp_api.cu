@@ -1,0 +1,413 @@
+// C ABI of the engine (include/fastpart.h): contexts, resident instances,
+// validation of the hypergraph, uploads, kernel launches, read-backs.
+
+#include "fp_internal.h"
+#include "fp_device.cuh"
+
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstring>
+#include <chrono>
+#include <new>
+#include <vector>
+#include <algorithm>
+
+namespace fp {
+size_t refine_smem_bytes(int metric, int K);
+cudaError_t launch_refine(const DevInstance& I, int passes, cudaStream_t st);
+size_t metrics_scratch_bytes(int K);
+cudaError_t launch_metrics(const DevInstance& I, void* scratch, long long* out, int num_sms, cudaStream_t st,
+                           int* launches);
+}  // namespace fp
+
+using namespace fp;
+
+struct fp_ctx {
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t own = nullptr;
+  cudaStream_t stream = nullptr;
+};
+
+struct fp_instance {
+  fp_ctx* ctx = nullptr;
+  HostGraph g;                 // host copy (validated)
+  Problem pb;
+  HostState st;
+  bool has_state = false;
+  DevInstance d{};
+  std::vector<void*> allocs;
+  void* metric_scratch = nullptr;
+  long long* metric_out = nullptr;
+  long long* h_moves = nullptr;   // pinned
+  int* h_status = nullptr;        // pinned
+  long long* h_metrics = nullptr; // pinned
+  int last_passes = 0;
+  long long last_launches = 0;
+};
+
+namespace {
+
+const int kMaxPasses = 4096;
+const int kMaxK = 4096;
+
+int cuda_status(cudaError_t e) {
+  if (e == cudaSuccess) return FP_OK;
+  if (e == cudaErrorMemoryAllocation) return FP_ERR_NOMEM;
+  return FP_ERR_CUDA;
+}
+
+template <class T>
+int dalloc(fp_instance* in, T** p, size_t n) {
+  void* q = nullptr;
+  cudaError_t e = cudaMalloc(&q, std::max<size_t>(n, 1) * sizeof(T));
+  if (e != cudaSuccess) return cuda_status(e);
+  in->allocs.push_back(q);
+  *p = static_cast<T*>(q);
+  return FP_OK;
+}
+
+// Structural checks the kernels rely on: consistent CSRs (the net -> pins CSR is
+// a permutation of the transpose of vertex -> nets), distinct pins per net,
+// every net non-empty with its source among its pins, a permutation ordering.
+int validate(const fp_hypergraph* h) {
+  if (!h || h->nov <= 0 || h->noe < 0 || h->pins < 0 || h->pins >= (1ll << 31)) return FP_ERR_INVALID;
+  if (!h->vptr || !h->nptr || !h->src || (h->pins > 0 && (!h->vnets || !h->npins))) return FP_ERR_INVALID;
+  const int nov = h->nov, noe = h->noe;
+  if (h->vptr[0] != 0 || h->nptr[0] != 0) return FP_ERR_INVALID;
+  if ((long long)h->vptr[nov] != h->pins || (long long)h->nptr[noe] != h->pins) return FP_ERR_INVALID;
+  for (int v = 0; v < nov; v++)
+    if (h->vptr[v + 1] < h->vptr[v]) return FP_ERR_INVALID;
+  for (int e = 0; e < noe; e++)
+    if (h->nptr[e + 1] <= h->nptr[e]) return FP_ERR_INVALID;  // empty nets are rejected
+  std::vector<uint32_t> cnt(noe, 0);
+  for (long long k = 0; k < h->pins; k++) {
+    if (h->vnets[k] >= (uint32_t)noe) return FP_ERR_INVALID;
+    cnt[h->vnets[k]]++;
+  }
+  for (int e = 0; e < noe; e++)
+    if (cnt[e] != h->nptr[e + 1] - h->nptr[e]) return FP_ERR_INVALID;
+  // stamp[v] = e marks v as a pin of e according to vertex -> nets.
+  std::vector<uint32_t> tptr(noe + 1, 0), tpins(h->pins);
+  for (int e = 0; e < noe; e++) tptr[e + 1] = tptr[e] + cnt[e];
+  std::vector<uint32_t> fill(tptr.begin(), tptr.end() - 1);
+  for (int v = 0; v < nov; v++)
+    for (uint32_t k = h->vptr[v]; k < h->vptr[v + 1]; k++) tpins[fill[h->vnets[k]]++] = (uint32_t)v;
+  std::vector<int> stamp(nov, -1);
+  for (int e = 0; e < noe; e++) {
+    for (uint32_t k = tptr[e]; k < tptr[e + 1]; k++) {
+      if (stamp[tpins[k]] == e) return FP_ERR_INVALID;  // vertex lists the net twice
+      stamp[tpins[k]] = e;
+    }
+    bool src_ok = false;
+    for (uint32_t k = h->nptr[e]; k < h->nptr[e + 1]; k++) {
+      const uint32_t u = h->npins[k];
+      if (u >= (uint32_t)nov || stamp[u] != e) return FP_ERR_INVALID;
+      stamp[u] = -2 - e;
+      if ((int)u == h->src[e]) src_ok = true;
+    }
+    if (!src_ok) return FP_ERR_INVALID;
+  }
+  if (h->weights) {
+    long long W = 0;
+    for (int v = 0; v < nov; v++) {
+      if (h->weights[v] < 0) return FP_ERR_INVALID;
+      W += h->weights[v];
+    }
+    if (W >= (1ll << 31)) return FP_ERR_INVALID;
+  }
+  if (h->ordering) {
+    std::vector<char> seen(nov, 0);
+    for (int z = 0; z < nov; z++) {
+      const int v = h->ordering[z];
+      if (v < 0 || v >= nov || seen[v]) return FP_ERR_INVALID;
+      seen[v] = 1;
+    }
+  }
+  return FP_OK;
+}
+
+int upload_state(fp_instance* in) {
+  const HostState& st = in->st;
+  cudaStream_t s = in->ctx->stream;
+  const DevInstance& d = in->d;
+  const int K = in->pb.K;
+  cudaError_t e = cudaSuccess;
+  auto cp = [&](void* dst, const void* src, size_t bytes) {
+    if (e == cudaSuccess && bytes) e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s);
+  };
+  cp(d.part_vec, st.part_vec.data(), sizeof(int) * st.part_vec.size());
+  cp(d.ep_len, st.ep_len.data(), sizeof(int) * st.ep_len.size());
+  cp(d.ep_part, st.ep_part.data(), sizeof(int) * st.ep_part.size());
+  cp(d.ep_cnt, st.ep_cnt.data(), sizeof(int) * st.ep_cnt.size());
+  cp(d.part_sizes, st.part_sizes.data(), sizeof(int) * K);
+  cp(d.marker, st.marker.data(), sizeof(int) * K);
+  cp(d.send, st.send.data(), sizeof(int) * K);
+  cp(d.recv, st.recv.data(), sizeof(int) * K);
+  cp(d.msgs, st.msgs.data(), sizeof(int) * K);
+  std::vector<uint32_t> zr, zc;
+  if (in->pb.metric == FP_METRIC_TM || in->pb.metric == FP_METRIC_MSM) {
+    const int words = (K + 31) / 32;
+    zr.assign((size_t)K * words, 0);
+    zc.assign((size_t)K * words, 0);
+    for (int a = 0; a < K; a++)
+      for (int b = 0; b < K; b++)
+        if (st.conn[(size_t)a * K + b] == 0) {
+          zr[(size_t)a * words + (b >> 5)] |= 1u << (b & 31);
+          zc[(size_t)b * words + (a >> 5)] |= 1u << (a & 31);
+        }
+    cp(d.conn, st.conn.data(), sizeof(int) * st.conn.size());
+    cp(d.zrow, zr.data(), sizeof(uint32_t) * zr.size());
+    cp(d.zcol, zc.data(), sizeof(uint32_t) * zc.size());
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);  // host vectors are pageable
+  return cuda_status(e);
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* fp_strerror(int status) {
+  switch (status) {
+    case FP_OK: return "ok";
+    case FP_ERR_INVALID: return "invalid argument or malformed hypergraph";
+    case FP_ERR_CUDA: return "CUDA runtime error";
+    case FP_ERR_NOMEM: return "out of memory";
+    case FP_ERR_DEVICE_TIMEOUT: return "device-side wait timed out";
+    case FP_ERR_UNSUPPORTED: return "input on which the reference behaviour is undefined";
+    case FP_ERR_STATE: return "call out of order";
+    case FP_ERR_IO: return "file error";
+    default: return "unknown status";
+  }
+}
+
+int fp_validate(const fp_hypergraph* hg) { return validate(hg); }
+
+int fp_ctx_create(int32_t device, fp_ctx** out) {
+  if (!out) return FP_ERR_INVALID;
+  *out = nullptr;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n <= 0) return FP_ERR_CUDA;
+  if (device < 0 || device >= n) return FP_ERR_INVALID;
+  cudaError_t e = cudaSetDevice(device);
+  if (e != cudaSuccess) return cuda_status(e);
+  fp_ctx* c = new (std::nothrow) fp_ctx;
+  if (!c) return FP_ERR_NOMEM;
+  c->device = device;
+  cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
+  e = cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking);
+  if (e != cudaSuccess) { delete c; return cuda_status(e); }
+  c->stream = c->own;
+  *out = c;
+  return FP_OK;
+}
+
+int fp_ctx_destroy(fp_ctx* ctx) {
+  if (!ctx) return FP_ERR_INVALID;
+  cudaSetDevice(ctx->device);
+  if (ctx->own) cudaStreamDestroy(ctx->own);
+  delete ctx;
+  return FP_OK;
+}
+
+int fp_ctx_set_stream(fp_ctx* ctx, void* stream) {
+  if (!ctx) return FP_ERR_INVALID;
+  ctx->stream = stream ? static_cast<cudaStream_t>(stream) : ctx->own;
+  return FP_OK;
+}
+
+int fp_instance_create(fp_ctx* ctx, const fp_hypergraph* h, int32_t K, int32_t metric, double eps_factor,
+                       fp_instance** out) {
+  if (!ctx || !out || metric < 0 || metric > 5 || K < 2 || K > kMaxK || !(eps_factor > 0)) return FP_ERR_INVALID;
+  *out = nullptr;
+  int rc = validate(h);
+  if (rc) return rc;
+  fp_instance* in = new (std::nothrow) fp_instance;
+  if (!in) return FP_ERR_NOMEM;
+  in->ctx = ctx;
+  HostGraph& g = in->g;
+  g.nov = h->nov;
+  g.noe = h->noe;
+  g.pins = h->pins;
+  g.vptr.assign(h->vptr, h->vptr + h->nov + 1);
+  g.vnets.assign(h->vnets, h->vnets + h->pins);
+  g.nptr.assign(h->nptr, h->nptr + h->noe + 1);
+  g.npins.assign(h->npins, h->npins + h->pins);
+  g.src.assign(h->src, h->src + h->noe);
+  Problem& pb = in->pb;
+  pb.g = &in->g;
+  pb.K = K;
+  pb.metric = metric;
+  pb.eps_factor = eps_factor;
+  pb.w.resize(g.nov);
+  long long W = 0;
+  for (int v = 0; v < g.nov; v++) { pb.w[v] = h->weights ? h->weights[v] : 1; W += pb.w[v]; }
+  if (h->weights) g.weights = pb.w;
+  pb.order.resize(g.nov);
+  for (int z = 0; z < g.nov; z++) pb.order[z] = h->ordering ? h->ordering[z] : z;
+  pb.xw = (int)(W / K);
+  if (pb.xw < 1) { delete in; return FP_ERR_INVALID; }
+  pb.C = pb.xw * eps_factor;
+
+  cudaSetDevice(ctx->device);
+  DevInstance& d = in->d;
+  d.nov = g.nov;
+  d.noe = g.noe;
+  d.pins = g.pins;
+  d.K = K;
+  d.metric = metric;
+  d.C = pb.C;
+  d.max_pw = (int)(pb.xw + (pb.xw * 0.1));
+  d.min_pw = (int)(pb.xw - (pb.xw * 0.1));
+  const size_t KK = (size_t)K * K, words = (size_t)(K + 31) / 32;
+  const bool msg = metric == FP_METRIC_TM || metric == FP_METRIC_MSM;
+  uint32_t *vptr, *vnets, *nptr, *npins;
+  int *src, *w, *order;
+  if ((rc = dalloc(in, &vptr, g.nov + 1)) || (rc = dalloc(in, &vnets, g.pins)) || (rc = dalloc(in, &nptr, g.noe + 1)) ||
+      (rc = dalloc(in, &npins, g.pins)) || (rc = dalloc(in, &src, g.noe)) || (rc = dalloc(in, &w, g.nov)) ||
+      (rc = dalloc(in, &order, g.nov)) || (rc = dalloc(in, &d.part_vec, g.nov)) || (rc = dalloc(in, &d.ep_len, g.noe)) ||
+      (rc = dalloc(in, &d.ep_part, g.pins)) || (rc = dalloc(in, &d.ep_cnt, g.pins)) ||
+      (rc = dalloc(in, &d.part_sizes, K)) || (rc = dalloc(in, &d.marker, K)) || (rc = dalloc(in, &d.send, K)) ||
+      (rc = dalloc(in, &d.recv, K)) || (rc = dalloc(in, &d.msgs, K)) || (rc = dalloc(in, &d.conn, msg ? KK : 1)) ||
+      (rc = dalloc(in, &d.zrow, msg ? K * words : 1)) || (rc = dalloc(in, &d.zcol, msg ? K * words : 1)) ||
+      (rc = dalloc(in, &d.moves, kMaxPasses)) || (rc = dalloc(in, &d.status, 1)) ||
+      (rc = dalloc(in, &in->metric_out, 8))) {
+    fp_instance_destroy(in);
+    return rc;
+  }
+  void* ms = nullptr;
+  cudaError_t e = cudaMalloc(&ms, metrics_scratch_bytes(K));
+  if (e != cudaSuccess) { fp_instance_destroy(in); return cuda_status(e); }
+  in->allocs.push_back(ms);
+  in->metric_scratch = ms;
+  if (cudaMallocHost(&in->h_moves, sizeof(long long) * kMaxPasses) != cudaSuccess ||
+      cudaMallocHost(&in->h_status, sizeof(int)) != cudaSuccess ||
+      cudaMallocHost(&in->h_metrics, sizeof(long long) * 8) != cudaSuccess) {
+    fp_instance_destroy(in);
+    return FP_ERR_NOMEM;
+  }
+  d.vptr = vptr; d.vnets = vnets; d.nptr = nptr; d.npins = npins; d.src = src; d.w = w; d.order = order;
+  cudaStream_t s = ctx->stream;
+  e = cudaMemcpyAsync(vptr, g.vptr.data(), sizeof(uint32_t) * (g.nov + 1), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess && g.pins) e = cudaMemcpyAsync(vnets, g.vnets.data(), sizeof(uint32_t) * g.pins, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(nptr, g.nptr.data(), sizeof(uint32_t) * (g.noe + 1), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess && g.pins) e = cudaMemcpyAsync(npins, g.npins.data(), sizeof(uint32_t) * g.pins, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess && g.noe) e = cudaMemcpyAsync(src, g.src.data(), sizeof(int) * g.noe, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(w, pb.w.data(), sizeof(int) * g.nov, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(order, pb.order.data(), sizeof(int) * g.nov, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(d.status, 0, sizeof(int), s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) { fp_instance_destroy(in); return cuda_status(e); }
+  *out = in;
+  return FP_OK;
+}
+
+int fp_instance_destroy(fp_instance* in) {
+  if (!in) return FP_ERR_INVALID;
+  cudaSetDevice(in->ctx->device);
+  for (void* p : in->allocs) cudaFree(p);
+  if (in->h_moves) cudaFreeHost(in->h_moves);
+  if (in->h_status) cudaFreeHost(in->h_status);
+  if (in->h_metrics) cudaFreeHost(in->h_metrics);
+  delete in;
+  return FP_OK;
+}
+
+int fp_initial_partition(fp_instance* in) {
+  if (!in) return FP_ERR_INVALID;
+  int rc = initial_partition(in->pb, in->st);
+  if (rc) return rc;
+  cudaSetDevice(in->ctx->device);
+  rc = upload_state(in);
+  if (rc) return rc;
+  in->has_state = true;
+  return FP_OK;
+}
+
+int fp_reset_state(fp_instance* in) {
+  if (!in) return FP_ERR_INVALID;
+  if (!in->has_state) return FP_ERR_STATE;
+  cudaSetDevice(in->ctx->device);
+  return upload_state(in);
+}
+
+int fp_refine(fp_instance* in, int32_t passes) {
+  if (!in || passes < 0 || passes > kMaxPasses) return FP_ERR_INVALID;
+  if (!in->has_state) return FP_ERR_STATE;
+  if (passes == 0) { in->last_passes = 0; in->last_launches = 0; return FP_OK; }
+  cudaSetDevice(in->ctx->device);
+  cudaStream_t s = in->ctx->stream;
+  cudaError_t e = cudaMemsetAsync(in->d.moves, 0, sizeof(long long) * passes, s);
+  if (e == cudaSuccess) e = launch_refine(in->d, passes, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(in->h_status, in->d.status, sizeof(int), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(in->h_moves, in->d.moves, sizeof(long long) * passes, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_status(e);
+  in->last_passes = passes;
+  in->last_launches = 1;
+  return *in->h_status;
+}
+
+int fp_metrics(fp_instance* in, int64_t out[6]) {
+  if (!in || !out) return FP_ERR_INVALID;
+  if (!in->has_state) return FP_ERR_STATE;
+  cudaSetDevice(in->ctx->device);
+  cudaStream_t s = in->ctx->stream;
+  int launches = 0;
+  cudaError_t e = launch_metrics(in->d, in->metric_scratch, in->metric_out, in->ctx->num_sms, s, &launches);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(in->h_metrics, in->metric_out, sizeof(long long) * 6, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_status(e);
+  for (int i = 0; i < 6; i++) out[i] = in->h_metrics[i];
+  in->last_launches = launches;
+  return FP_OK;
+}
+
+static int d2h(fp_instance* in, void* dst, const void* src, size_t bytes) {
+  if (!bytes) return FP_OK;
+  cudaSetDevice(in->ctx->device);
+  cudaStream_t s = in->ctx->stream;
+  cudaError_t e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  return cuda_status(e);
+}
+
+int fp_get_partition(fp_instance* in, int32_t* part_vec) {
+  if (!in || !part_vec) return FP_ERR_INVALID;
+  if (!in->has_state) return FP_ERR_STATE;
+  return d2h(in, part_vec, in->d.part_vec, sizeof(int) * in->g.nov);
+}
+
+int fp_get_lists(fp_instance* in, int32_t* ep_len, int32_t* ep_part, int32_t* ep_cnt) {
+  if (!in) return FP_ERR_INVALID;
+  if (!in->has_state) return FP_ERR_STATE;
+  int rc = FP_OK;
+  if (ep_len && (rc = d2h(in, ep_len, in->d.ep_len, sizeof(int) * in->g.noe))) return rc;
+  if (ep_part && (rc = d2h(in, ep_part, in->d.ep_part, sizeof(int) * in->g.pins))) return rc;
+  if (ep_cnt && (rc = d2h(in, ep_cnt, in->d.ep_cnt, sizeof(int) * in->g.pins))) return rc;
+  return FP_OK;
+}
+
+int fp_get_part_sizes(fp_instance* in, int32_t* sizes) {
+  if (!in || !sizes) return FP_ERR_INVALID;
+  if (!in->has_state) return FP_ERR_STATE;
+  return d2h(in, sizes, in->d.part_sizes, sizeof(int) * in->pb.K);
+}
+
+int fp_get_moves(fp_instance* in, int64_t* moves, int32_t n) {
+  if (!in || !moves || n < 0) return FP_ERR_INVALID;
+  for (int i = 0; i < n; i++) moves[i] = i < in->last_passes ? in->h_moves[i] : 0;
+  return FP_OK;
+}
+
+int fp_last_launches(fp_instance* in, int64_t* launches) {
+  if (!in || !launches) return FP_ERR_INVALID;
+  *launches = in->last_launches;
+  return FP_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,146 @@
+// Device-side data of one resident instance and small block-level helpers.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace fp {
+
+constexpr int kThreads = 512;                 // refinement CTA size
+constexpr int kWarps = kThreads / 32;
+
+// Everything the refinement kernels read or write, as device pointers.
+struct DevInstance {
+  int nov, noe;
+  long long pins;
+  int K;
+  int metric;
+  double C;          // (W / K) * eps_factor
+  int max_pw;        // TV: (W/K) + (W/K)*0.1, truncated (TV/partition.cpp:95)
+  int min_pw;        // TV: (W/K) - (W/K)*0.1, truncated (TV/partition.cpp:96)
+  // hypergraph (read-only)
+  const uint32_t* vptr;
+  const uint32_t* vnets;
+  const uint32_t* nptr;    // also the slot offset of each net's part list
+  const uint32_t* npins;
+  const int* src;
+  const int* w;
+  const int* order;
+  // refinement state
+  int* part_vec;
+  int* ep_len;
+  int* ep_part;
+  int* ep_cnt;
+  int* part_sizes;   // K
+  int* marker;       // K (TV)
+  int* send;         // K (MSV, MSRV)
+  int* recv;         // K (MSRV)
+  int* conn;         // K*K (TM, MSM)
+  int* msgs;         // K (TM, MSM)
+  uint32_t* zrow;    // K*K/32 bits: conn[k][r] == 0 (TM, MSM)
+  uint32_t* zcol;    // K*K/32 bits: conn[s][k] == 0, column-major (TM, MSM)
+  // bookkeeping
+  long long* moves;  // per pass
+  int* status;       // device status word, 0 = ok
+};
+
+// Status values a kernel can report (mirrors FP_ERR_* of the public header).
+constexpr int kDevErrInvalid = -1;
+constexpr int kDevErrUnsupported = -5;
+
+__device__ __forceinline__ void dev_fail(int* status, int code) { atomicCAS(status, 0, code); }
+
+// LDG penalty: 1 - size / C, then score * penalty, with no contraction, exactly
+// the reference's double arithmetic (TV/partition.cpp:103-104).
+__device__ __forceinline__ double ldg_score(int count, int size, double C) {
+  double pen = __dsub_rn(1.0, __ddiv_rn((double)size, C));
+  return __dmul_rn((double)count, pen);
+}
+
+// Candidate key of the LDG argmax: higher score, then smaller part, then the
+// part seen first (the reference keeps the first of equal candidates).
+struct LdgKey {
+  double score;      // <= 0 means "not a candidate"
+  int size;
+  int part;
+  unsigned long long first;
+};
+
+__device__ __forceinline__ bool ldg_better(const LdgKey& a, const LdgKey& b) {
+  if (a.score <= 0) return false;
+  if (b.score <= 0) return true;
+  if (a.score != b.score) return a.score > b.score;
+  if (a.size != b.size) return a.size < b.size;
+  return a.first < b.first;
+}
+
+__device__ __forceinline__ LdgKey shfl_key(const LdgKey& k, int off) {
+  LdgKey o;
+  o.score = __shfl_xor_sync(0xffffffffu, k.score, off);
+  o.size = __shfl_xor_sync(0xffffffffu, k.size, off);
+  o.part = __shfl_xor_sync(0xffffffffu, k.part, off);
+  o.first = __shfl_xor_sync(0xffffffffu, k.first, off);
+  return o;
+}
+
+// Block-wide LDG argmax; every thread gets the winner (part = -1 if none).
+__device__ __forceinline__ LdgKey block_ldg_argmax(LdgKey k, LdgKey* scratch) {
+  for (int off = 16; off; off >>= 1) {
+    LdgKey o = shfl_key(k, off);
+    if (ldg_better(o, k)) k = o;
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) scratch[warp] = k;
+  __syncthreads();
+  if (warp == 0) {
+    k = lane < kWarps ? scratch[lane] : LdgKey{-1.0, 0, -1, ~0ull};
+    for (int off = 16; off; off >>= 1) {
+      LdgKey o = shfl_key(k, off);
+      if (ldg_better(o, k)) k = o;
+    }
+    if (lane == 0) scratch[0] = k;
+  }
+  __syncthreads();
+  k = scratch[0];
+  __syncthreads();
+  return k;
+}
+
+// Block-wide minimum of a 64-bit key.
+__device__ __forceinline__ unsigned long long block_min_u64(unsigned long long x, unsigned long long* scratch) {
+  for (int off = 16; off; off >>= 1) {
+    unsigned long long o = __shfl_xor_sync(0xffffffffu, x, off);
+    x = o < x ? o : x;
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) scratch[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    x = lane < kWarps ? scratch[lane] : ~0ull;
+    for (int off = 16; off; off >>= 1) {
+      unsigned long long o = __shfl_xor_sync(0xffffffffu, x, off);
+      x = o < x ? o : x;
+    }
+    if (lane == 0) scratch[0] = x;
+  }
+  __syncthreads();
+  x = scratch[0];
+  __syncthreads();
+  return x;
+}
+
+// Least-loaded part, lowest index on ties (TV/partition.cpp:118-132).
+__device__ __forceinline__ int block_min_loaded(const int* sizes, int K, unsigned long long* scratch) {
+  unsigned long long best = ~0ull;
+  for (int p = threadIdx.x; p < K; p += blockDim.x) {
+    // sizes are non-negative; bias keeps signed order if one ever is not.
+    unsigned long long key = ((unsigned long long)((unsigned)sizes[p] ^ 0x80000000u) << 32) | (unsigned)p;
+    best = key < best ? key : best;
+  }
+  best = block_min_u64(best, scratch);
+  return (int)(best & 0xffffffffu);
+}
+
+}  // namespace fp

@@ -1,0 +1,313 @@
+// Host side of the C ABI that needs no GPU: generated and file-backed
+// hypergraphs, and the drop-in partition_gpu() driver.
+
+#include "fp_internal.h"
+
+#include <cstdio>
+#include <cstring>
+#include <chrono>
+#include <fstream>
+#include <sstream>
+#include <string>
+#include <new>
+#include <vector>
+#include <algorithm>
+
+namespace {
+
+using fp::HostGraph;
+
+// Net -> pins from vertex -> nets, pins in ascending vertex order per net
+// (the reference's createInverse, shared/utils.cpp:32-56).
+void build_net_csr(HostGraph& g) {
+  g.nptr.assign(g.noe + 1, 0);
+  for (long long k = 0; k < g.pins; k++) g.nptr[g.vnets[k] + 1]++;
+  for (int e = 0; e < g.noe; e++) g.nptr[e + 1] += g.nptr[e];
+  g.npins.assign(g.pins, 0);
+  std::vector<uint32_t> fill(g.nptr.begin(), g.nptr.end() - 1);
+  for (int v = 0; v < g.nov; v++)
+    for (uint32_t k = g.vptr[v]; k < g.vptr[v + 1]; k++) g.npins[fill[g.vnets[k]]++] = (uint32_t)v;
+}
+
+void choose_sources(HostGraph& g, int rule) {
+  g.src.assign(g.noe, -1);
+  for (int e = 0; e < g.noe; e++) {
+    if (g.nptr[e] == g.nptr[e + 1]) continue;
+    const uint32_t* b = &g.npins[g.nptr[e]];
+    const uint32_t* en = &g.npins[g.nptr[e + 1]];
+    g.src[e] = rule == 0 ? (int)*std::min_element(b, en) : (int)*b;
+  }
+}
+
+// PaToH-like text: "index_base nov noe pins" then one line of vertex ids per
+// file net (shared/hypergraph_rw.cpp:97-183).  Produces the file's own
+// net -> pins CSR (lines as given).
+bool parse_text(const std::string& path, int& nov, int& noe, long long& pins, std::vector<uint32_t>& lptr,
+                std::vector<uint32_t>& lids) {
+  std::ifstream in(path);
+  if (!in) return false;
+  int base = 0;
+  unsigned unov = 0, unoe = 0;
+  in >> base >> unov >> unoe >> pins;
+  if (!in || pins < 0) return false;
+  nov = (int)unov;
+  noe = (int)unoe;
+  const int salt = base == 0 ? 0 : -1;
+  std::string line;
+  std::getline(in, line);
+  lptr.assign(1, 0);
+  lids.clear();
+  lids.reserve(pins);
+  while ((int)lptr.size() - 1 < noe && std::getline(in, line)) {
+    std::istringstream iss(line);
+    long long x;
+    size_t before = lids.size();
+    while (iss >> x) {
+      long long id = x + salt;
+      if (id < 0 || id >= nov) return false;
+      lids.push_back((uint32_t)id);
+    }
+    if (lids.size() != before) lptr.push_back((uint32_t)lids.size());
+  }
+  noe = (int)lptr.size() - 1;
+  return (long long)lids.size() == pins;
+}
+
+// <path>.plbin: u32 noe, u32 nov, i64 pins, then per line its cumulative end
+// and its ids (shared/hypergraph_rw.cpp:185-240).
+bool read_plbin(const std::string& path, int& nov, int& noe, long long& pins, std::vector<uint32_t>& lptr,
+                std::vector<uint32_t>& lids) {
+  std::ifstream in(path, std::ios::binary);
+  if (!in) return false;
+  uint32_t unoe = 0, unov = 0;
+  in.read((char*)&unoe, 4);
+  in.read((char*)&unov, 4);
+  in.read((char*)&pins, 8);
+  if (!in || pins < 0) return false;
+  noe = (int)unoe;
+  nov = (int)unov;
+  lptr.assign(noe + 1, 0);
+  lids.resize(pins);
+  uint32_t prev = 0;
+  for (int e = 0; e < noe; e++) {
+    uint32_t end = 0;
+    in.read((char*)&end, 4);
+    if (!in || end < prev || end > (uint64_t)pins) return false;
+    lptr[e + 1] = end;
+    in.read((char*)&lids[prev], (std::streamsize)(end - prev) * 4);
+    if (!in) return false;
+    prev = end;
+  }
+  for (uint32_t x : lids)
+    if (x >= (uint32_t)nov) return false;
+  return prev == (uint64_t)pins;
+}
+
+bool write_plbin(const std::string& path, int nov, int noe, long long pins, const std::vector<uint32_t>& lptr,
+                 const std::vector<uint32_t>& lids) {
+  std::ofstream out(path, std::ios::binary);
+  if (!out) return false;
+  uint32_t unoe = (uint32_t)noe, unov = (uint32_t)nov;
+  out.write((const char*)&unoe, 4);
+  out.write((const char*)&unov, 4);
+  out.write((const char*)&pins, 8);
+  for (int e = 0; e < noe; e++) {
+    uint32_t end = lptr[e + 1];
+    out.write((const char*)&end, 4);
+    out.write((const char*)&lids[lptr[e]], (std::streamsize)(lptr[e + 1] - lptr[e]) * 4);
+  }
+  return (bool)out;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fp_generate(const fp_gen_params* p, fp_graph** out) {
+  if (!p || !out) return FP_ERR_INVALID;
+  *out = nullptr;
+  fp::GenParams gp;
+  gp.nov = p->nov; gp.noe = p->noe;
+  gp.size_lo = p->size_lo; gp.size_hi = p->size_hi;
+  gp.size_alpha = p->size_alpha; gp.pin_beta = p->pin_beta;
+  gp.src_rule = p->src_rule; gp.sort_pins = p->sort_pins; gp.weight_rule = p->weight_rule;
+  gp.seed = p->seed;
+  fp_graph* g = new (std::nothrow) fp_graph;
+  if (!g) return FP_ERR_NOMEM;
+  int rc = fp::generate(gp, g->g);
+  if (rc) { delete g; return rc; }
+  *out = g;
+  return FP_OK;
+}
+
+int fp_graph_from_nets(int32_t nov, int32_t noe, const uint32_t* nptr, const uint32_t* npins, const int32_t* src,
+                       fp_graph** out) {
+  if (!out || nov <= 0 || noe < 0 || !nptr || (!npins && nptr[noe] > 0)) return FP_ERR_INVALID;
+  *out = nullptr;
+  fp_graph* gg = new (std::nothrow) fp_graph;
+  if (!gg) return FP_ERR_NOMEM;
+  HostGraph& g = gg->g;
+  g.nov = nov;
+  g.noe = noe;
+  g.pins = nptr[noe];
+  g.nptr.assign(nptr, nptr + noe + 1);
+  g.npins.assign(npins, npins + g.pins);
+  for (uint32_t x : g.npins)
+    if (x >= (uint32_t)nov) { delete gg; return FP_ERR_INVALID; }
+  if (src) g.src.assign(src, src + noe);
+  else choose_sources(g, 0);
+  fp::build_vertex_csr(g);
+  *out = gg;
+  return FP_OK;
+}
+
+int fp_read_patohlike(const char* path, int32_t transpose, int32_t write_cache, fp_graph** out) {
+  if (!path || !out) return FP_ERR_INVALID;
+  *out = nullptr;
+  int nov = 0, noe = 0;
+  long long pins = 0;
+  std::vector<uint32_t> lptr, lids;
+  const std::string bin = std::string(path) + ".plbin";
+  bool ok = read_plbin(bin, nov, noe, pins, lptr, lids);
+  if (!ok) {
+    if (!parse_text(path, nov, noe, pins, lptr, lids)) return FP_ERR_IO;
+    if (write_cache) write_plbin(bin, nov, noe, pins, lptr, lids);
+  }
+  fp_graph* gg = new (std::nothrow) fp_graph;
+  if (!gg) return FP_ERR_NOMEM;
+  HostGraph& g = gg->g;
+  g.pins = pins;
+  if (transpose) {
+    // File lines are nets (TV/tv.cpp:51-80, CN/cn.cpp:154-177).
+    g.nov = nov;
+    g.noe = noe;
+    g.nptr = std::move(lptr);
+    g.npins = std::move(lids);
+    fp::build_vertex_csr(g);
+  } else {
+    // File lines are vertices, ids are nets (TM/tm.cpp:65): needs a square file.
+    if (nov != noe) { delete gg; return FP_ERR_INVALID; }
+    g.nov = noe;
+    g.noe = nov;
+    g.vptr = std::move(lptr);
+    g.vnets = std::move(lids);
+    build_net_csr(g);
+  }
+  choose_sources(g, 0);
+  *out = gg;
+  return FP_OK;
+}
+
+int fp_write_patohlike(const fp_graph* gg, const char* path) {
+  if (!gg || !path) return FP_ERR_INVALID;
+  const HostGraph& g = gg->g;
+  FILE* f = std::fopen(path, "w");
+  if (!f) return FP_ERR_IO;
+  std::fprintf(f, "0 %d %d %lld\n", g.nov, g.noe, g.pins);
+  for (int e = 0; e < g.noe; e++) {
+    for (uint32_t k = g.nptr[e]; k < g.nptr[e + 1]; k++)
+      std::fprintf(f, k + 1 < g.nptr[e + 1] ? "%u " : "%u", g.npins[k]);
+    std::fputc('\n', f);
+  }
+  return std::fclose(f) == 0 ? FP_OK : FP_ERR_IO;
+}
+
+int fp_graph_view(const fp_graph* gg, fp_hypergraph* v) {
+  if (!gg || !v) return FP_ERR_INVALID;
+  const HostGraph& g = gg->g;
+  v->nov = g.nov;
+  v->noe = g.noe;
+  v->pins = g.pins;
+  v->vptr = g.vptr.data();
+  v->vnets = g.vnets.data();
+  v->nptr = g.nptr.data();
+  v->npins = g.npins.data();
+  v->src = g.src.data();
+  v->weights = g.weights.empty() ? nullptr : g.weights.data();
+  v->ordering = nullptr;
+  return FP_OK;
+}
+
+int fp_graph_destroy(fp_graph* g) {
+  if (!g) return FP_ERR_INVALID;
+  delete g;
+  return FP_OK;
+}
+
+// Drop-in body of the reference's partition_gpu(): host stream, metric lines,
+// REFI_ITER device passes, metric lines again (e.g. TV/partition.cpp:984-1184).
+int fp_partition_gpu(int32_t metric, const uint32_t* row_ptr, const uint32_t* col_ind, const uint32_t* net_appearence,
+                     int32_t nov, int32_t noe, int64_t pins, const int32_t* edge_wgths, const int32_t* src_nodes,
+                     int32_t K, const int32_t* ordering, const char* f_name, int32_t REFI_OPT, int32_t REFI_ITER,
+                     const uint32_t* row_ptr_inv, const uint32_t* col_ind_inv, int32_t* part_vec_out,
+                     int64_t* metrics_out) {
+  (void)edge_wgths;      // unused by the reference as well
+  (void)net_appearence;  // net sizes follow from the CSR
+  (void)f_name;
+  if (!row_ptr || !col_ind || !src_nodes || nov <= 0 || noe < 0 || pins < 0) return FP_ERR_INVALID;
+  HostGraph g;
+  g.nov = nov;
+  g.noe = noe;
+  g.pins = pins;
+  g.vptr.assign(row_ptr, row_ptr + nov + 1);
+  g.vnets.assign(col_ind, col_ind + pins);
+  if (row_ptr_inv && col_ind_inv) {
+    g.nptr.assign(row_ptr_inv, row_ptr_inv + noe + 1);
+    g.npins.assign(col_ind_inv, col_ind_inv + pins);
+  } else {
+    for (long long k = 0; k < pins; k++)
+      if (g.vnets[k] >= (uint32_t)noe) return FP_ERR_INVALID;
+    build_net_csr(g);
+  }
+  g.src.assign(src_nodes, src_nodes + noe);
+  fp_hypergraph h;
+  h.nov = nov;
+  h.noe = noe;
+  h.pins = pins;
+  h.vptr = g.vptr.data();
+  h.vnets = g.vnets.data();
+  h.nptr = g.nptr.data();
+  h.npins = g.npins.data();
+  h.src = g.src.data();
+  h.weights = nullptr;
+  h.ordering = ordering;
+
+  fp_ctx* ctx = nullptr;
+  fp_instance* inst = nullptr;
+  int rc = fp_ctx_create(0, &ctx);
+  if (rc) return rc;
+  rc = fp_instance_create(ctx, &h, K, metric, 1.05, &inst);
+  if (rc) { fp_ctx_destroy(ctx); return rc; }
+  int64_t before[6] = {0}, after[6] = {-1, -1, -1, -1, -1, -1};
+  static const char* names[6] = {"TV", "CN", "TM", "MGM", "MGV", "MGAV"};
+  if ((rc = fp_initial_partition(inst)) == FP_OK && (rc = fp_metrics(inst, before)) == FP_OK) {
+    for (int i = 0; i < 6; i++) std::printf("%s : %lld\n", names[i], (long long)before[i]);
+    auto t0 = std::chrono::steady_clock::now();
+    if (REFI_OPT) rc = fp_refine(inst, REFI_ITER);
+    auto t1 = std::chrono::steady_clock::now();
+    if (rc == FP_OK) {
+      std::printf("Refinement took : %g seconds.\n", std::chrono::duration<double>(t1 - t0).count());
+      if (REFI_OPT) rc = fp_metrics(inst, after);
+    }
+    if (rc == FP_OK) {
+      for (int i = 0; i < 6; i++) std::printf("After Refinement %s : %lld\n", names[i], (long long)after[i]);
+      for (int i = 0; i < 6; i++) {
+        if (REFI_OPT)
+          std::printf("Improved Percentage %s : %g\n", names[i], 100.0 - ((double)after[i] / before[i]) * 100);
+        else
+          std::printf("Improved Percentage %s : -1\n", names[i]);
+      }
+      std::printf("Iterated for : %d times\n", REFI_OPT ? REFI_ITER : 0);
+      if (part_vec_out) rc = fp_get_partition(inst, part_vec_out);
+      if (metrics_out) {
+        for (int i = 0; i < 6; i++) { metrics_out[i] = before[i]; metrics_out[6 + i] = after[i]; }
+      }
+    }
+  }
+  std::fflush(stdout);
+  fp_instance_destroy(inst);
+  fp_ctx_destroy(ctx);
+  return rc;
+}
+
+}  // extern "C"

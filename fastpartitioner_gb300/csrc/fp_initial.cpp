@@ -1,0 +1,245 @@
+// Streaming initial partitioners (host side).
+//
+// Each metric's partition_gpu() in the reference first runs its CPU streaming
+// partitioner and then hands the resulting state to the GPU; the same split is
+// kept here.  These produce the refinement input: part vector, ordered per-net
+// part lists, part sizes, and the metric's auxiliary state.
+//
+//   LDG stream  (TV, MSV, MSRV): TV/partition.cpp:207-264, MGV/partition.cpp:122-189,
+//                                MSRV/partition.cpp:123-196
+//   CN stream   (uncut nets):    CN/partition.cpp:132-221
+//   message-greedy (TM, MSM):    TM/partition.cpp:87-250, MSM/partition.cpp:146-309
+
+#include "fp_internal.h"
+
+#include <climits>
+#include <algorithm>
+
+namespace fp {
+
+namespace {
+
+inline int list_find(const int* part, int len, int p) {
+  for (int j = 0; j < len; j++)
+    if (part[j] == p) return j;
+  return -1;
+}
+
+// Increments part p in net e, appending it when absent.  Returns the slot.
+inline int list_add(HostState& st, int e, int p) {
+  int s = st.ep_start[e];
+  int j = list_find(&st.ep_part[s], st.ep_len[e], p);
+  if (j >= 0) {
+    st.ep_cnt[s + j]++;
+    return j;
+  }
+  j = st.ep_len[e]++;
+  st.ep_part[s + j] = p;
+  st.ep_cnt[s + j] = 1;
+  return j;
+}
+
+int argmin_size(const std::vector<int>& sizes) {
+  int best = INT_MAX, idx = -1;
+  for (size_t i = 0; i < sizes.size(); i++)
+    if (sizes[i] < best) { best = sizes[i]; idx = (int)i; }
+  return idx;
+}
+
+// LDG decision over the parts seen by the current vertex, in first-seen order:
+// highest score * (1 - size / C) above zero, ties to the smaller part, then to
+// the earlier part; if no part scores, the least loaded part (lowest index).
+int ldg_decide(const Problem& pb, const HostState& st, const std::vector<int>& seen, int nseen,
+               const std::vector<int>& count) {
+  double best = 0;
+  int arg = -1;
+  for (int i = 0; i < nseen; i++) {
+    int p = seen[i];
+    double pen = 1 - (1.0 * st.part_sizes[p] / pb.C);
+    double sc = (double)count[p] * pen;
+    if (sc > 0 && (arg == -1 || sc > best || (sc == best && st.part_sizes[p] < st.part_sizes[arg]))) {
+      best = sc;
+      arg = p;
+    }
+  }
+  return arg >= 0 ? arg : argmin_size(st.part_sizes);
+}
+
+void state_alloc(const Problem& pb, HostState& st) {
+  const HostGraph& g = *pb.g;
+  st.part_vec.assign(g.nov, -1);
+  st.part_sizes.assign(pb.K, 0);
+  st.ep_start.assign(g.nptr.begin(), g.nptr.end());
+  st.ep_len.assign(g.noe, 0);
+  st.ep_part.assign(g.pins, -1);
+  st.ep_cnt.assign(g.pins, 0);
+  st.marker.assign(pb.K, -1);
+  st.send.assign(pb.K, 0);
+  st.recv.assign(pb.K, 0);
+  st.msgs.assign(pb.K, 0);
+  st.conn.clear();
+}
+
+int stream_ldg(const Problem& pb, HostState& st) {
+  const HostGraph& g = *pb.g;
+  const int K = pb.K;
+  const bool vol = pb.metric == FP_METRIC_MSV || pb.metric == FP_METRIC_MSRV;
+  const bool rv = pb.metric == FP_METRIC_MSRV;
+  const int max_pw = (int)(pb.xw + (pb.xw * 0.1));
+  std::vector<int> seen(K), count(K, 0);
+  for (int z = 0; z < g.nov; z++) {
+    const int v = pb.order[z];
+    int nseen = 0;
+    for (uint32_t i = g.vptr[v]; i < g.vptr[v + 1]; i++) {
+      const int e = (int)g.vnets[i];
+      const int s = st.ep_start[e];
+      for (int j = 0; j < st.ep_len[e]; j++) {
+        const int p = st.ep_part[s + j];
+        if (st.marker[p] != v) {
+          st.marker[p] = v;
+          count[p] = 1;
+          seen[nseen++] = p;
+        } else {
+          count[p]++;
+        }
+      }
+    }
+    const int d = ldg_decide(pb, st, seen, nseen, count);
+    // TV's LDG2 sends a part above max_pw back to the vertex's current part,
+    // which is -1 during the stream (TV/partition.cpp:135-138).
+    if (pb.metric == FP_METRIC_TV && st.part_sizes[d] > max_pw) return FP_ERR_UNSUPPORTED;
+    st.part_sizes[d] += pb.w[v];
+    st.part_vec[v] = d;
+    for (uint32_t i = g.vptr[v]; i < g.vptr[v + 1]; i++) {
+      const int e = (int)g.vnets[i];
+      if (!vol) {
+        list_add(st, e, d);
+        continue;
+      }
+      const int s = st.ep_start[e];
+      const int sv = g.src[e];
+      const int sp = st.part_vec[sv];
+      if (sv == v) {
+        for (int j = 0; j < st.ep_len[e]; j++) {
+          const int p = st.ep_part[s + j];
+          if (p != sp) {
+            st.send[sp]++;
+            if (rv) st.recv[p]++;
+          }
+        }
+      }
+      const int before = st.ep_len[e];
+      list_add(st, e, d);
+      if (st.ep_len[e] != before && sv != v && sp != -1) {
+        st.send[sp]++;
+        if (rv) st.recv[d]++;
+      }
+    }
+  }
+  return FP_OK;
+}
+
+int stream_cn(const Problem& pb, HostState& st) {
+  const HostGraph& g = *pb.g;
+  std::vector<int> seen(pb.K), count(pb.K, 0), mark(pb.K, -1);
+  for (int z = 0; z < g.nov; z++) {
+    const int v = pb.order[z];
+    int nseen = 0;
+    for (uint32_t i = g.vptr[v]; i < g.vptr[v + 1]; i++) {
+      const int e = (int)g.vnets[i];
+      if (st.ep_len[e] != 1) continue;
+      const int p = st.ep_part[st.ep_start[e]];
+      if (mark[p] != v) { mark[p] = v; count[p] = 1; seen[nseen++] = p; }
+      else count[p]++;
+    }
+    const int d = ldg_decide(pb, st, seen, nseen, count);
+    st.part_sizes[d] += pb.w[v];
+    st.part_vec[v] = d;
+    for (uint32_t i = g.vptr[v]; i < g.vptr[v + 1]; i++) list_add(st, (int)g.vnets[i], d);
+  }
+  return FP_OK;
+}
+
+int stream_msg(const Problem& pb, HostState& st) {
+  const HostGraph& g = *pb.g;
+  const int K = pb.K;
+  st.conn.assign((size_t)K * K, 0);
+  if (pb.metric == FP_METRIC_MSM)
+    for (int i = 0; i < K; i++) st.conn[(size_t)i * K + i] = -1;
+  std::vector<int> smark(K, -1), src_part(g.noe, -1);
+  std::vector<int> act_parts, act_nets, own_nets;
+  for (int z = 0; z < g.nov; z++) {
+    const int v = pb.order[z];
+    act_parts.clear();
+    act_nets.clear();
+    own_nets.clear();
+    for (uint32_t i = g.vptr[v]; i < g.vptr[v + 1]; i++) {
+      const int e = (int)g.vnets[i];
+      if (g.src[e] == v) own_nets.push_back(e);
+      const int sp = src_part[e];
+      if (sp != -1) {
+        if (smark[sp] != v) { smark[sp] = v; act_parts.push_back(sp); }
+        act_nets.push_back(e);
+      }
+    }
+    // Part saving the most messages among parts below capacity; ties to the
+    // smaller part, then the lower index.
+    int best = -1, arg = -1;
+    for (int k = 0; k < K; k++) {
+      if (!(st.part_sizes[k] < pb.C)) continue;
+      int saved = 0;
+      for (int sp : act_parts) saved += st.conn[(size_t)sp * K + k] > 0;
+      for (int e : own_nets) {
+        const int s = st.ep_start[e];
+        for (int j = 0; j < st.ep_len[e]; j++) saved += st.conn[(size_t)k * K + st.ep_part[s + j]] > 0;
+      }
+      if (saved > best || (saved == best && st.part_sizes[k] < st.part_sizes[arg])) { best = saved; arg = k; }
+    }
+    const int d = arg >= 0 ? arg : argmin_size(st.part_sizes);
+    st.part_vec[v] = d;
+    st.part_sizes[d] += pb.w[v];
+    for (uint32_t i = g.vptr[v]; i < g.vptr[v + 1]; i++) list_add(st, (int)g.vnets[i], d);
+    for (int e : act_nets) {
+      const int sp = src_part[e];
+      if (sp == d) continue;
+      int& c = st.conn[(size_t)sp * K + d];
+      if (c == 0) {
+        st.msgs[sp]++;
+        c = 1;
+      } else {
+        const int s = st.ep_start[e];
+        const int j = list_find(&st.ep_part[s], st.ep_len[e], d);
+        if (j >= 0 && st.ep_cnt[s + j] == 1) c++;
+      }
+    }
+    for (int e : own_nets) {
+      src_part[e] = d;
+      const int s = st.ep_start[e];
+      for (int j = 0; j < st.ep_len[e]; j++) {
+        const int p = st.ep_part[s + j];
+        if (p == d) continue;
+        int& c = st.conn[(size_t)d * K + p];
+        if (c == 0) { st.msgs[d]++; c = 1; }
+        else c++;
+      }
+    }
+  }
+  return FP_OK;
+}
+
+}  // namespace
+
+int initial_partition(const Problem& pb, HostState& st) {
+  state_alloc(pb, st);
+  switch (pb.metric) {
+    case FP_METRIC_TV:
+    case FP_METRIC_MSV:
+    case FP_METRIC_MSRV: return stream_ldg(pb, st);
+    case FP_METRIC_CN: return stream_cn(pb, st);
+    case FP_METRIC_TM:
+    case FP_METRIC_MSM: return stream_msg(pb, st);
+    default: return FP_ERR_INVALID;
+  }
+}
+
+}  // namespace fp

@@ -1,0 +1,182 @@
+/*
+ * fastpart.h -- C ABI of the GB300 refinement engine for FastPartitioner.
+ *
+ * The library keeps one hypergraph instance resident on one GPU and runs the
+ * per-metric refinement pass (CN, TV, TM, MSM, MSV, MSRV) and the six metric
+ * evaluators as CUDA kernels.  Results are bit-identical to the reference's
+ * single-threaded CPU refinement (`partition()` in each metric directory).
+ *
+ * Every function returns FP_OK (0) or a negative status; none of them prints,
+ * aborts or calls exit().  Plain pointers and sizes only.
+ *
+ * Reference interfaces this ABI replaces (paths inside the FastPartitioner tree):
+ *   partition_gpu_wrapper(...)   TV/partition.cpp:6-26, CN/partition.cpp:7-27,
+ *                                TM/partition.cpp:3-7, MGV/partition.cpp:4-27,
+ *                                MSRV/partition.cpp:4-25
+ *   partition_gpu(...)           TV/partition.h:19, CN/partition.h:19,
+ *                                TM/partition.h:16-20, MGV/partition.h:17,
+ *                                MSRV/partition.h:17 (MSM has none: MSM/msm.cpp:67)
+ *   metric evaluators            shared/metric.cpp:3-391
+ */
+#ifndef FASTPART_H
+#define FASTPART_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------- */
+#define FP_OK                   0
+#define FP_ERR_INVALID         -1  /* bad argument or malformed hypergraph            */
+#define FP_ERR_CUDA            -2  /* CUDA runtime error (no device, launch failure)   */
+#define FP_ERR_NOMEM           -3  /* host or device allocation failed                 */
+#define FP_ERR_DEVICE_TIMEOUT  -4  /* a bounded device-side wait ran out               */
+#define FP_ERR_UNSUPPORTED     -5  /* input on which the reference has undefined
+                                      behaviour (e.g. a part above max_pw in the TV
+                                      stream, MSRV's max-part list overflowing K)     */
+#define FP_ERR_STATE           -6  /* call out of order (e.g. refine before a state)   */
+#define FP_ERR_IO              -7  /* file could not be read or written                */
+
+/* ---- metrics (the reference's directory names) ------------------------ */
+#define FP_METRIC_CN    0   /* cut-net                         CN/   */
+#define FP_METRIC_TV    1   /* connectivity - 1                TV/   */
+#define FP_METRIC_TM    2   /* total messages                  TM/   */
+#define FP_METRIC_MSM   3   /* max send messages               MSM/  */
+#define FP_METRIC_MSV   4   /* max send volume                 MGV/  */
+#define FP_METRIC_MSRV  5   /* max send + receive volume       MSRV/ */
+
+/* Order of the six values returned by fp_metrics(); the order in which the
+ * reference prints them (TV/partition.cpp:278-283). */
+#define FP_OUT_TV   0
+#define FP_OUT_CN   1
+#define FP_OUT_TM   2
+#define FP_OUT_MSM  3
+#define FP_OUT_MSV  4
+#define FP_OUT_MSRV 5
+
+typedef struct fp_ctx fp_ctx;
+typedef struct fp_instance fp_instance;
+typedef struct fp_graph fp_graph;
+
+/* A hypergraph view.  vptr/vnets: nets of each vertex in the order the
+ * refinement scans them (the reference's row_ptr/col_ind).  nptr/npins: pins of
+ * each net (row_ptr_inv/col_ind_inv; CN moves pins in this order).  src: the
+ * source vertex of each net, which must be one of its pins (src_nodes).
+ * weights: vertex weights or NULL for unit weights (the reference counts
+ * vertices).  ordering: visiting order of the LDG-based metrics or NULL for
+ * vertex-id order (the reference's `ordering`, -o 0). */
+typedef struct {
+  int32_t nov;
+  int32_t noe;
+  int64_t pins;
+  const uint32_t* vptr;
+  const uint32_t* vnets;
+  const uint32_t* nptr;
+  const uint32_t* npins;
+  const int32_t* src;
+  const int32_t* weights;
+  const int32_t* ordering;
+} fp_hypergraph;
+
+/* ---- context: one GPU, one stream ------------------------------------- */
+int fp_ctx_create(int32_t device, fp_ctx** out);
+int fp_ctx_destroy(fp_ctx* ctx);
+/* Run all subsequent work of this context on `stream` (a cudaStream_t); NULL
+ * selects the context's own stream. */
+int fp_ctx_set_stream(fp_ctx* ctx, void* stream);
+
+/* Structural check fp_instance_create applies (no device needed): consistent
+ * CSRs, distinct pins per net, non-empty nets whose source is one of their
+ * pins, a permutation ordering, non-negative weights summing below 2^31. */
+int fp_validate(const fp_hypergraph* hg);
+
+/* ---- instance lifecycle ------------------------------------------------ */
+/* Copies the hypergraph to the device.  eps_factor is the balance factor the
+ * reference hard-codes as 1.05 (C = (nov / K) * eps, TV/partition.cpp:159-160). */
+int fp_instance_create(fp_ctx* ctx, const fp_hypergraph* hg, int32_t K, int32_t metric,
+                       double eps_factor, fp_instance** out);
+int fp_instance_destroy(fp_instance* inst);
+
+/* Streaming initial partition of the metric (host, vertex order), uploaded as
+ * the refinement state: part vector, per-net ordered part lists, part sizes and
+ * the metric's auxiliary state (TV marker, MSV/MSRV volumes, TM/MSM K x K
+ * connection counts).  Replaces the initial stream inside partition_gpu(),
+ * e.g. TV/partition.cpp:1035-1092. */
+int fp_initial_partition(fp_instance* inst);
+
+/* Copies the host-side result of the last fp_initial_partition to the device
+ * again (host -> device), discarding device-side refinement: the upload leg of
+ * the reference's partition_gpu_wrapper (TV/gpu_partition.cu:366-498). */
+int fp_reset_state(fp_instance* inst);
+
+/* `passes` refinement passes on the device (REFI_ITER; the loop inside
+ * partition_gpu_wrapper, TV/gpu_partition.cu:503-513).  Stream-ordered; returns
+ * after the work is enqueued and its status has been read back. */
+int fp_refine(fp_instance* inst, int32_t passes);
+
+/* All six metrics of the current device state, in FP_OUT_* order
+ * (shared/metric.cpp: TV_Refined, CN, TM_scratch, MGM_scratch, MGV_Scratch,
+ * MGAV_Scratch). */
+int fp_metrics(fp_instance* inst, int64_t out[6]);
+
+/* Copies of the current device state (caller-allocated host buffers). */
+int fp_get_partition(fp_instance* inst, int32_t* part_vec /* nov */);
+int fp_get_lists(fp_instance* inst, int32_t* ep_len /* noe */, int32_t* ep_part /* pins */,
+                 int32_t* ep_cnt /* pins */);
+int fp_get_part_sizes(fp_instance* inst, int32_t* sizes /* K */);
+/* Accepted moves of each of the last refine call's passes (up to n values). */
+int fp_get_moves(fp_instance* inst, int64_t* moves, int32_t n);
+/* Number of kernel launches the last fp_refine / fp_metrics call enqueued. */
+int fp_last_launches(fp_instance* inst, int64_t* launches);
+
+const char* fp_strerror(int status);
+
+/* ---- host hypergraphs: generator and file formats ---------------------- */
+typedef struct {
+  int32_t nov, noe;
+  int32_t size_lo, size_hi;   /* net size range                                   */
+  double size_alpha;          /* > 0: Zipf(alpha) sizes clipped to [lo, hi]         */
+  double pin_beta;            /* > 0: pins by Zipf(beta) popularity, else uniform   */
+  int32_t src_rule;           /* 0: lowest-id pin is the source, 1: first drawn     */
+  int32_t sort_pins;          /* 1: pins of a net sorted by id                      */
+  int32_t weight_rule;        /* 0: unit weights, 1: weight = degree                */
+  uint64_t seed;
+} fp_gen_params;
+
+int fp_generate(const fp_gen_params* p, fp_graph** out);
+/* Builds a host graph from a net -> pins CSR (the .hg orientation of the TV and
+ * CN drivers): vertex -> nets is its transpose, nets ascending per vertex. */
+int fp_graph_from_nets(int32_t nov, int32_t noe, const uint32_t* nptr, const uint32_t* npins,
+                       const int32_t* src, fp_graph** out);
+/* Reads a PaToH-like .hg file (shared/hypergraph_rw.cpp:97-242), honouring an
+ * existing `<path>.plbin` cache exactly as the reference does.  `transpose` = 1
+ * makes file lines nets (TV, CN drivers); 0 makes file lines vertices (TM, MSM,
+ * MGV, MSRV drivers, TM/tm.cpp:65).  Sources: src_rule as in fp_gen_params,
+ * applied to each net's pins. */
+int fp_read_patohlike(const char* path, int32_t transpose, int32_t write_cache, fp_graph** out);
+int fp_write_patohlike(const fp_graph* g, const char* path);
+int fp_graph_view(const fp_graph* g, fp_hypergraph* view);
+int fp_graph_destroy(fp_graph* g);
+
+/* ---- drop-in for partition_gpu() --------------------------------------- */
+/* Same arguments and the same stdout lines as the reference's partition_gpu()
+ * of the given metric: initial stream, "TV : ..." metric lines, REFI_ITER
+ * device refinement passes, "After Refinement ..." lines and "Refinement took".
+ * row_ptr_inv / col_ind_inv may be NULL (they are rebuilt from row_ptr/col_ind;
+ * CN passes them, CN/partition.h:19).  part_vec_out (nov, may be NULL) receives
+ * the refined part vector; metrics_out (12, may be NULL) the six metrics before
+ * and after refinement. */
+int fp_partition_gpu(int32_t metric, const uint32_t* row_ptr, const uint32_t* col_ind,
+                     const uint32_t* net_appearence, int32_t nov, int32_t noe, int64_t pins,
+                     const int32_t* edge_wgths, const int32_t* src_nodes, int32_t K,
+                     const int32_t* ordering, const char* f_name, int32_t REFI_OPT, int32_t REFI_ITER,
+                     const uint32_t* row_ptr_inv, const uint32_t* col_ind_inv, int32_t* part_vec_out,
+                     int64_t* metrics_out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FASTPART_H */

@@ -1,0 +1,165 @@
+"""CPU oracle for the GB300 refinement engine -- TEST INFRASTRUCTURE ONLY.
+
+Imported by tests/, __graft_entry__.smoke() and bench.py's CPU legs, never by the
+product package.  Two checkers live here:
+
+* ``run_oracle`` -- libfporacle.so, a single-threaded C++ restatement of the
+  reference's sequential partition() for the six metrics (fp_oracle.cpp).
+* ``run_reference`` -- the reference's own partition() / partition_par(),
+  compiled from its sources by oracle/Makefile into oracle/_ref/ and driven by
+  ref_harness.cpp.  Used to pin the restatement and to time the reference.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import re
+import subprocess
+import tempfile
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB = HERE / "libfporacle.so"
+REF_DIR = HERE / "_ref"
+
+METRIC_IDS = {"CN": 0, "TV": 1, "TM": 2, "MSM": 3, "MSV": 4, "MSRV": 5}
+REF_BIN = {"TV": "ref_tv", "CN": "ref_cn", "TM": "ref_tm", "MSM": "ref_msm", "MSV": "ref_mgv", "MSRV": "ref_msrv"}
+OUTPUT_ORDER = ["TV", "CN", "TM", "MSM", "MSV", "MSRV"]
+_PRINT_NAMES = {"TV": "TV", "CN": "CN", "TM": "TM", "MSM": "MGM", "MSV": "MGV", "MSRV": "MGAV"}
+
+
+class _Hg(C.Structure):
+    _fields_ = [("nov", C.c_int), ("noe", C.c_int), ("pins", C.c_longlong),
+                ("vptr", C.c_void_p), ("vnets", C.c_void_p), ("nptr", C.c_void_p),
+                ("npins", C.c_void_p), ("src", C.c_void_p), ("weights", C.c_void_p),
+                ("ordering", C.c_void_p)]
+
+
+class _Run(C.Structure):
+    _fields_ = [("metric", C.c_int), ("K", C.c_int), ("eps_factor", C.c_double),
+                ("passes", C.c_int), ("refine", C.c_int),
+                ("part_vec_init", C.c_void_p), ("ep_len_init", C.c_void_p),
+                ("ep_part_init", C.c_void_p), ("ep_cnt_init", C.c_void_p),
+                ("part_vec", C.c_void_p), ("ep_len", C.c_void_p), ("ep_part", C.c_void_p),
+                ("ep_cnt", C.c_void_p), ("metrics_init", C.c_longlong * 6),
+                ("metrics_final", C.c_longlong * 6), ("moves", C.c_longlong * 64),
+                ("refine_seconds", C.c_double), ("status", C.c_int)]
+
+
+def build(quiet: bool = True) -> None:
+    """Builds libfporacle.so and, where the reference sources are reachable, the
+    reference harness binaries."""
+    res = subprocess.run(["make", "-C", str(HERE), "-j8", "all"], capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"oracle build failed:\n{res.stdout}\n{res.stderr}")
+    if not quiet:
+        print(res.stdout)
+
+
+_lib = None
+
+
+def _oracle():
+    global _lib
+    if _lib is None:
+        if not LIB.exists():
+            build()
+        _lib = C.CDLL(str(LIB))
+        _lib.fpo_partition.argtypes = [C.POINTER(_Hg), C.POINTER(_Run)]
+        _lib.fpo_partition.restype = C.c_int
+    return _lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data
+
+
+def run_oracle(hg, K: int, metric: str, passes: int, eps_factor: float = 1.05, refine: bool = True):
+    """Runs the restated reference pipeline (stream + passes + metrics).
+    Returns a dict of numpy arrays and metric dicts."""
+    m = METRIC_IDS[metric.upper()]
+    nov, noe, pins = hg.nov, hg.noe, hg.pins
+    out = {k: np.empty(n, np.int32) for k, n in (("part_vec_init", nov), ("ep_len_init", noe),
+                                                   ("ep_part_init", pins), ("ep_cnt_init", pins),
+                                                   ("part_vec", nov), ("ep_len", noe),
+                                                   ("ep_part", pins), ("ep_cnt", pins))}
+    h = _Hg(nov, noe, pins, _p(hg.vptr), _p(hg.vnets), _p(hg.nptr), _p(hg.npins), _p(hg.src),
+            _p(hg.weights), _p(hg.ordering))
+    r = _Run()
+    r.metric, r.K, r.eps_factor, r.passes, r.refine = m, K, eps_factor, passes, int(refine)
+    for k, a in out.items():
+        setattr(r, k, a.ctypes.data)
+    rc = _oracle().fpo_partition(C.byref(h), C.byref(r))
+    out["status"] = rc
+    out["metrics_init"] = dict(zip(OUTPUT_ORDER, list(r.metrics_init)))
+    out["metrics_final"] = dict(zip(OUTPUT_ORDER, list(r.metrics_final)))
+    out["moves"] = np.array(list(r.moves)[:passes], np.int64)
+    out["refine_seconds"] = r.refine_seconds
+    return out
+
+
+def reference_available(metric: str = "TV") -> bool:
+    return (REF_DIR / REF_BIN[metric.upper()]).exists()
+
+
+def _read_capture(path: Path, nov: int, noe: int):
+    raw = np.fromfile(path, dtype=np.int32)
+    assert raw[0] == nov and raw[1] == noe, "capture header mismatch"
+    part_vec = raw[2:2 + nov].copy()
+    ep_len = raw[2 + nov:2 + nov + noe].copy()
+    flat = raw[2 + nov + noe:].copy()
+    return part_vec, ep_len, flat
+
+
+def run_reference(hg, K: int, metric: str, passes: int, threads: int = 1, capture: bool = True,
+                  timeout: float = 3600):
+    """Runs the reference's own partition() (threads == 1) or partition_par()
+    on `hg` through the harness.  Returns its printed metrics, its
+    'Refinement took' seconds and, with capture, the part vector and ordered part
+    lists after the initial stream and after refinement."""
+    metric = metric.upper()
+    exe = REF_DIR / REF_BIN[metric]
+    if not exe.exists():
+        raise FileNotFoundError(f"{exe} not built (reference sources unavailable)")
+    with tempfile.TemporaryDirectory(prefix="fpref") as td:
+        inst = Path(td) / "inst.fphg"
+        hg.save_fphg(inst)
+        prefix = str(Path(td) / "cap") if capture else "-"
+        env = dict(os.environ)
+        env.setdefault("OMP_NUM_THREADS", str(max(threads, 1)))
+        res = subprocess.run([str(exe), str(inst), str(K), str(passes), str(threads), prefix],
+                             capture_output=True, text=True, timeout=timeout, env=env, cwd=td)
+        if res.returncode != 0:
+            raise RuntimeError(f"reference run failed ({res.returncode}):\n{res.stdout[-2000:]}\n{res.stderr[-2000:]}")
+        text = res.stdout
+        out = {"stdout": text}
+        before, after = {}, {}
+        for key in OUTPUT_ORDER:
+            pn = _PRINT_NAMES[key]
+            mb = re.search(rf"^{pn} : (-?\d+)$", text, re.M)
+            ma = re.search(rf"^After Refinement {pn} : (-?\d+)$", text, re.M)
+            if mb:
+                before[key] = int(mb.group(1))
+            if ma:
+                after[key] = int(ma.group(1))
+        out["metrics_init"], out["metrics_final"] = before, after
+        mt = re.search(r"^Refinement took : ([0-9.eE+-]+) seconds", text, re.M)
+        out["refine_seconds"] = float(mt.group(1)) if mt else None
+        if capture:
+            caps = sorted((p for p in Path(td).glob("cap.*") if p.suffix[1:].isdigit() and p.name.count(".") == 1),
+                          key=lambda p: int(p.suffix[1:]))
+            if caps:
+                out["part_vec_init"], out["ep_len_init"], out["lists_init"] = _read_capture(caps[0], hg.nov, hg.noe)
+            if len(caps) > 1:
+                out["part_vec"], out["ep_len"], out["lists"] = _read_capture(caps[-1], hg.nov, hg.noe)
+        return out
+
+
+def flat_lists(hg, ep_len, ep_part):
+    """Concatenation of every net's listed parts, in list order (the form the
+    reference capture stores)."""
+    starts = hg.nptr[:-1].astype(np.int64)
+    idx = np.concatenate([np.arange(s, s + n) for s, n in zip(starts, ep_len)]) if len(ep_len) else np.zeros(0, np.int64)
+    return ep_part[idx.astype(np.int64)] if idx.size else np.zeros(0, np.int32)

@@ -1,0 +1,148 @@
+"""Parity of the GPU refinement engine, called through the C ABI.
+
+* against the reference's own outputs (committed golden fixtures): part vector
+  after the stream and after refinement, every net's ordered part list, all six
+  metric values -- bit for bit;
+* against the CPU oracle on larger seeded instances, including vertex weights,
+  a non-default balance factor and a custom visiting order (extensions the
+  oracle restates; the reference has neither).
+"""
+import numpy as np
+import pytest
+
+from conftest import METRICS, golden_cases, load_golden
+
+pytestmark = pytest.mark.gpu
+OUT = ["TV", "CN", "TM", "MSM", "MSV", "MSRV"]
+
+
+def run_gpu(eng, hg, K, metric, passes, eps=1.05):
+    with eng.instance(hg, K, metric, eps) as inst:
+        inst.initial_partition()
+        pv0 = inst.partition()
+        m0 = inst.metrics()
+        inst.refine(passes)
+        m1 = inst.metrics()
+        pv = inst.partition()
+        ln, pt, ct = inst.lists()
+        moves = inst.moves(passes)
+        sizes = inst.part_sizes()
+    return dict(part_vec_init=pv0, metrics_init=m0, metrics_final=m1, part_vec=pv, ep_len=ln, ep_part=pt,
+                ep_cnt=ct, moves=moves, sizes=sizes)
+
+
+@pytest.mark.parametrize("path", golden_cases(), ids=lambda p: p.stem)
+def test_gpu_matches_reference_fixtures(fp, orc, gpu_engine, path):
+    hg, passes, Ks, z = load_golden(path)
+    for m in METRICS:
+        for K in Ks:
+            key = f"{m}_{K}"
+            g = run_gpu(gpu_engine, hg, K, m, passes)
+            np.testing.assert_array_equal(g["part_vec_init"], z[f"{key}_part_vec_init"], err_msg=key)
+            np.testing.assert_array_equal(g["part_vec"], z[f"{key}_part_vec"], err_msg=key)
+            np.testing.assert_array_equal(g["ep_len"], z[f"{key}_ep_len"], err_msg=key)
+            np.testing.assert_array_equal(orc.flat_lists(hg, g["ep_len"], g["ep_part"]), z[f"{key}_lists"],
+                                          err_msg=key)
+            assert [g["metrics_init"][k] for k in OUT] == list(z[f"{key}_metrics_init"]), key
+            assert [g["metrics_final"][k] for k in OUT] == list(z[f"{key}_metrics_final"]), key
+
+
+def assert_same(g, o, hg, orc, tag):
+    np.testing.assert_array_equal(g["part_vec_init"], o["part_vec_init"], err_msg=tag)
+    np.testing.assert_array_equal(g["part_vec"], o["part_vec"], err_msg=tag)
+    np.testing.assert_array_equal(g["ep_len"], o["ep_len"], err_msg=tag)
+    np.testing.assert_array_equal(orc.flat_lists(hg, g["ep_len"], g["ep_part"]),
+                                  orc.flat_lists(hg, o["ep_len"], o["ep_part"]), err_msg=tag)
+    np.testing.assert_array_equal(g["ep_cnt"], o["ep_cnt"], err_msg=tag)
+    assert g["metrics_init"] == o["metrics_init"], tag
+    assert g["metrics_final"] == o["metrics_final"], tag
+    np.testing.assert_array_equal(g["moves"], o["moves"], err_msg=tag)
+
+
+CASES = [
+    ("colnet_4k_K8", lambda fp: fp.GenSpec.column_net(4096, 4096, 2, 16, seed=11), 8, 5),
+    ("zipf_6k_K64", lambda fp: fp.GenSpec.zipf(6000, 6000, 2.1, 2, 2000, beta=1.5, seed=12), 64, 4),
+    ("zipf_5k_K256", lambda fp: fp.GenSpec.zipf(5000, 5000, 2.1, 2, 1000, beta=1.5, seed=13), 256, 3),
+    ("colnet_3k_K1024", lambda fp: fp.GenSpec.column_net(3000, 3000, 2, 40, seed=14), 1024, 2),
+]
+
+
+@pytest.mark.parametrize("name,mk,K,passes", CASES, ids=[c[0] for c in CASES])
+@pytest.mark.parametrize("metric", METRICS)
+def test_gpu_matches_oracle(fp, orc, gpu_engine, name, mk, K, passes, metric):
+    hg = fp.generate(mk(fp))
+    o = orc.run_oracle(hg, K, metric, passes)
+    assert o["status"] == 0
+    g = run_gpu(gpu_engine, hg, K, metric, passes)
+    assert_same(g, o, hg, orc, f"{name} {metric}")
+
+
+@pytest.mark.parametrize("metric", METRICS)
+def test_gpu_weighted_eps_and_order(fp, orc, gpu_engine, metric):
+    """Degree weights, eps = 0.03 and a shuffled visiting order."""
+    hg = fp.generate(fp.GenSpec.zipf(3000, 3000, 2.1, 2, 500, beta=1.5, weight_rule=1, seed=21))
+    rng = np.random.default_rng(5)
+    hg.ordering = rng.permutation(hg.nov).astype(np.int32)
+    o = orc.run_oracle(hg, 16, metric, 4, eps_factor=1.03)
+    assert o["status"] == 0
+    g = run_gpu(gpu_engine, hg, 16, metric, 4, eps=1.03)
+    assert_same(g, o, hg, orc, metric)
+
+
+@pytest.mark.parametrize("metric", METRICS)
+def test_gpu_edge_cases(fp, orc, gpu_engine, metric):
+    """Isolated vertices (degree 0), single-pin nets, K = 2, and one pass."""
+    nov = 64
+    nets = [[0], [1, 2], [2, 3, 4], [5], [6, 7, 8, 9, 10], [10, 11], [12, 13, 14, 15, 16, 17, 18, 19]]
+    rng = np.random.default_rng(0)
+    for _ in range(40):
+        nets.append(sorted(rng.choice(np.arange(20, 60), size=int(rng.integers(2, 6)), replace=False).tolist()))
+    nptr = np.cumsum([0] + [len(n) for n in nets]).astype(np.uint32)
+    npins = np.concatenate([np.array(n, np.uint32) for n in nets])
+    hg = fp.Hypergraph.from_nets(nov, nptr, npins)          # vertices 60..63 have no nets
+    for K, passes in ((2, 1), (5, 3)):
+        o = orc.run_oracle(hg, K, metric, passes)
+        assert o["status"] == 0
+        g = run_gpu(gpu_engine, hg, K, metric, passes)
+        assert_same(g, o, hg, orc, f"{metric} K={K}")
+
+
+def test_gpu_state_invariants_large(fp, orc, gpu_engine):
+    """Size-independent checks on a larger instance: the ordered lists agree with
+    the part vector (checkMe, MSM/partition.cpp:2-68), part sizes agree with the
+    part vector, and the metrics agree with a recount from the part vector."""
+    hg = fp.generate(fp.GenSpec.zipf(200_000, 200_000, 2.1, 2, 10000, beta=1.5, seed=31))
+    K = 256
+    for metric in METRICS:
+        g = run_gpu(gpu_engine, hg, K, metric, 2)
+        pv, ln, pt, ct = g["part_vec"], g["ep_len"], g["ep_part"], g["ep_cnt"]
+        np.testing.assert_array_equal(np.bincount(pv, minlength=K), g["sizes"])
+        net_of_pin = np.repeat(np.arange(hg.noe), np.diff(hg.nptr).astype(np.int64))
+        key = net_of_pin.astype(np.int64) * K + pv[hg.npins]
+        uniq, cnt = np.unique(key, return_counts=True)
+        lam = np.bincount((uniq // K).astype(np.int64), minlength=hg.noe)
+        np.testing.assert_array_equal(ln, lam)
+        slot_key = []
+        slot_cnt = []
+        for arr_k, arr_c in ((pt, ct),):
+            starts = hg.nptr[:-1].astype(np.int64)
+            idx = np.concatenate([np.arange(s, s + n) for s, n in zip(starts, ln)])
+            slot_key = np.repeat(np.arange(hg.noe), ln).astype(np.int64) * K + arr_k[idx]
+            slot_cnt = arr_c[idx]
+        order = np.argsort(slot_key)
+        np.testing.assert_array_equal(slot_key[order], uniq)
+        np.testing.assert_array_equal(slot_cnt[order], cnt)
+        # recount of the six metrics from the part vector
+        tv = int(np.sum(lam - 1))
+        cn = int(np.sum(lam > 1))
+        sp = pv[hg.src]
+        send = np.bincount(sp, weights=lam - 1, minlength=K)
+        pair_src = sp[(uniq // K).astype(np.int64)]
+        tgt = (uniq % K)
+        mask = tgt != pair_src
+        pairs = np.unique(pair_src[mask].astype(np.int64) * K + tgt[mask])
+        msgs = np.bincount((pairs // K).astype(np.int64), minlength=K)
+        recv = np.bincount(tgt[mask].astype(np.int64), minlength=K)
+        want = {"TV": tv, "CN": cn, "TM": int(pairs.size), "MSM": int(msgs.max()), "MSV": int(send.max()),
+                "MSRV": int((send + recv).max())}
+        assert g["metrics_final"] == want, metric

@@ -1,0 +1,81 @@
+"""Host-side hypergraph handling: the generator and the PaToH-like file format."""
+import numpy as np
+
+from conftest import ROOT  # noqa: F401
+
+
+def test_generator_is_deterministic(fp):
+    a = fp.generate(fp.GenSpec.column_net(1000, 900, 2, 16, seed=3))
+    b = fp.generate(fp.GenSpec.column_net(1000, 900, 2, 16, seed=3))
+    c = fp.generate(fp.GenSpec.column_net(1000, 900, 2, 16, seed=4))
+    for k in ("vptr", "vnets", "nptr", "npins", "src"):
+        np.testing.assert_array_equal(getattr(a, k), getattr(b, k))
+    assert not np.array_equal(a.npins, c.npins)
+
+
+def test_column_net_distribution(fp):
+    hg = fp.generate(fp.GenSpec.column_net(5000, 4000, 2, 16, seed=0))
+    sizes = np.diff(hg.nptr)
+    assert sizes.min() >= 2 and sizes.max() <= 16
+    assert abs(sizes.mean() - 9.0) < 0.3
+    for e in range(0, hg.noe, 97):
+        pins = hg.npins[hg.nptr[e]:hg.nptr[e + 1]]
+        assert len(set(pins.tolist())) == len(pins)            # without replacement
+        assert hg.src[e] == pins.min()                          # lowest-id pin
+        assert np.all(np.diff(pins.astype(np.int64)) > 0)       # sorted pattern
+    # vertex -> nets is the transpose, nets ascending per vertex
+    for v in range(0, hg.nov, 101):
+        nets = hg.vnets[hg.vptr[v]:hg.vptr[v + 1]]
+        assert np.all(np.diff(nets.astype(np.int64)) > 0)
+        for e in nets:
+            assert v in hg.npins[hg.nptr[e]:hg.nptr[e + 1]]
+
+
+def test_zipf_distribution(fp):
+    hg = fp.generate(fp.GenSpec.zipf(20000, 20000, 2.1, 2, 10000, beta=1.5, weight_rule=1, seed=0))
+    sizes = np.diff(hg.nptr)
+    assert sizes.min() >= 2 and sizes.max() <= 10000
+    # clipped Zipf(2.1) from 1: mean about 5
+    assert 3.5 < sizes.mean() < 7.0
+    deg = np.diff(hg.vptr)
+    assert np.array_equal(hg.weights, deg)                      # weight = degree
+    assert deg.max() > 20 * deg.mean()                          # heavy-tailed popularity
+    assert hg.validate() == 0
+
+
+def test_patohlike_roundtrip(fp, tmp_path):
+    hg = fp.generate(fp.GenSpec.column_net(300, 250, 2, 9, seed=2))
+    path = tmp_path / "g.hg"
+    fp.write_patohlike(hg, path)
+    back = fp.read_patohlike(path, transpose=True)
+    assert (back.nov, back.noe) == (hg.nov, hg.noe)
+    np.testing.assert_array_equal(back.nptr, hg.nptr)
+    np.testing.assert_array_equal(back.npins, hg.npins)
+    np.testing.assert_array_equal(back.vptr, hg.vptr)
+    np.testing.assert_array_equal(back.vnets, hg.vnets)
+
+
+def test_patohlike_one_based_and_cache(fp, tmp_path):
+    path = tmp_path / "one.hg"
+    # 1-based file, 4 vertices, 3 nets
+    path.write_text("1 4 3 7\n1 2\n2 3 4\n1 4\n")
+    g = fp.read_patohlike(path, transpose=True, write_cache=True)
+    assert (g.nov, g.noe, g.pins) == (4, 3, 7)
+    np.testing.assert_array_equal(g.npins, [0, 1, 1, 2, 3, 0, 3])
+    assert (tmp_path / "one.hg.plbin").exists()
+    # the cache wins over the text, as in the reference (hypergraph_rw.cpp:102-106)
+    path.write_text("1 4 3 6\n1 2\n2 3\n1 4\n")
+    g2 = fp.read_patohlike(path, transpose=True)
+    np.testing.assert_array_equal(g2.npins, g.npins)
+
+
+def test_patohlike_lines_as_vertices(fp, tmp_path):
+    path = tmp_path / "sq.hg"
+    path.write_text("0 3 3 5\n0 1\n1 2\n0\n")
+    g = fp.read_patohlike(path, transpose=False)
+    # lines are vertices: vertex 0 has nets {0, 1}, vertex 1 {1, 2}, vertex 2 {0}
+    np.testing.assert_array_equal(g.vptr, [0, 2, 4, 5])
+    np.testing.assert_array_equal(g.vnets, [0, 1, 1, 2, 0])
+    # net -> pins is the inverse with ascending vertices
+    np.testing.assert_array_equal(g.nptr, [0, 2, 4, 5])
+    np.testing.assert_array_equal(g.npins, [0, 2, 0, 1, 1])
