@@ -83,13 +83,18 @@ __device__ void move_lists(const DevInstance& I, int v, int own, int d, uint32_t
       if (bo && jo < 0) jo = j0 + __ffs(bo) - 1;
       if (bd && jd < 0) jd = j0 + __ffs(bd) - 1;
     }
+    const int cap = (int)I.nptr[e + 1] - s;
+    if (jo < 0 || n > cap || (jd < 0 && n == cap && I.ep_cnt[s + jo] > 1)) {
+      // The list does not hold v's part, or has no free slot: the state is
+      // inconsistent.  Report it and leave the net untouched.
+      if (lane == 0) dev_fail(I.status, kDevErrInvalid);
+      continue;
+    }
     if (lane == 0) {
       const int sv = vh ? I.src[e] : -1;
       const int sp = (vh && sv != v) ? I.part_vec[sv] : d;
       if (vh && sv == v) atomicAdd(&vh->send[own], -(n - 1));
-      if (jo < 0) {
-        dev_fail(I.status, kDevErrInvalid);
-      } else {
+      {
         const int co = I.ep_cnt[s + jo] - 1;
         if (co == 0) {
           const int last = n - 1;
@@ -456,6 +461,7 @@ __global__ void __launch_bounds__(kThreads, 1) refine_msg_kernel(DevInstance I, 
         if (sv == v) {
           for (int j = lane; j < n; j += 32) {
             const int t = I.ep_part[s + j];
+            if ((unsigned)t >= (unsigned)K) { dev_fail(I.status, kDevErrInvalid); continue; }
             if (t == own) {
               if (I.ep_cnt[s + j] > 1) atomicOr(&R[own >> 5], 1u << (own & 31));
             } else {
