@@ -107,12 +107,14 @@ def lib():
             "fp_initial_partition": ([vp], C.c_int),
             "fp_refine": ([vp, i32], C.c_int),
             "fp_reset_state": ([vp], C.c_int),
+            "fp_set_engine": ([vp, i32], C.c_int),
             "fp_metrics": ([vp, vp], C.c_int),
             "fp_get_partition": ([vp, vp], C.c_int),
             "fp_get_lists": ([vp, vp, vp, vp], C.c_int),
             "fp_get_part_sizes": ([vp, vp], C.c_int),
             "fp_get_moves": ([vp, vp, i32], C.c_int),
             "fp_last_launches": ([vp, vp], C.c_int),
+            "fp_get_stats": ([vp, vp, i32], C.c_int),
             "fp_strerror": ([C.c_int], C.c_char_p),
             "fp_generate": ([C.POINTER(_GenParams), pp], C.c_int),
             "fp_graph_from_nets": ([i32, i32, vp, vp, vp, pp], C.c_int),
@@ -350,6 +352,11 @@ class Instance:
     def refine(self, passes: int) -> None:
         _check(lib().fp_refine(self._h, passes), "fp_refine")
 
+    def set_engine(self, engine: str) -> None:
+        """'auto' (speculative grid-wide engine where available) or 'sequential'
+        (single-CTA walk); both give identical results."""
+        _check(lib().fp_set_engine(self._h, {"auto": 0, "sequential": 1}[engine]), "fp_set_engine")
+
     def reset_state(self) -> None:
         """Uploads the host-side stream result again (host -> device)."""
         _check(lib().fp_reset_state(self._h), "fp_reset_state")
@@ -390,6 +397,16 @@ class Instance:
         m = np.zeros(n, np.int64)
         _check(lib().fp_get_moves(self._h, _ptr(m), n), "fp_get_moves")
         return m
+
+    def stats(self) -> dict:
+        """Round statistics of the last refine on the grid-wide engine."""
+        x = np.zeros(32, np.int64)
+        _check(lib().fp_get_stats(self._h, _ptr(x), 32), "fp_get_stats")
+        names = ["windows", "heavy_rounds", "window_moves", "cut_none", "cut_stale", "cut_size", "cut_volume",
+                 "cut_maxpart", "cut_conflict", "walked"]
+        d = {n: int(x[i]) for i, n in enumerate(names)}
+        d.update(eval_ms=x[16] / 1e6, validate_ms=x[17] / 1e6, commit_ms=x[18] / 1e6, heavy_ms=x[19] / 1e6)
+        return d
 
     def last_launches(self) -> int:
         x = np.zeros(1, np.int64)

@@ -17,6 +17,14 @@ namespace fp {
 size_t refine_smem_bytes(int metric, int K);
 cudaError_t launch_refine(const DevInstance& I, int passes, cudaStream_t st);
 size_t metrics_scratch_bytes(int K);
+cudaError_t launch_spec_ldg(const DevInstance& I, const SpecBuf& B, int passes, int num_sms, cudaStream_t st,
+                            int* grid_out);
+// Metrics the speculative grid-wide engine covers.
+static bool spec_supported(int metric) {
+  return metric == FP_METRIC_TV || metric == FP_METRIC_MSV || metric == FP_METRIC_MSRV;
+}
+constexpr int kHeavyDegHost = 256;   // must equal spec::kHeavyDeg (fp_spec_common.cuh)
+constexpr int kMaxSpecWarps = 16384;
 cudaError_t launch_metrics(const DevInstance& I, void* scratch, long long* out, int num_sms, cudaStream_t st,
                            int* launches);
 }  // namespace fp
@@ -45,12 +53,18 @@ struct fp_instance {
   long long* h_metrics = nullptr; // pinned
   int last_passes = 0;
   long long last_launches = 0;
+  int engine = FP_ENGINE_AUTO;
+  SpecBuf sb{};
+  int last_grid = 0;
+  std::vector<int> heavy_pos;     // host copy
+  int* heavy_pos_d = nullptr;
 };
 
 namespace {
 
 const int kMaxPasses = 4096;
 const int kMaxK = 4096;
+const int kSpecWindow = 16384;   // longest speculative window (vertices)
 
 int cuda_status(cudaError_t e) {
   if (e == cudaSuccess) return FP_OK;
@@ -261,6 +275,13 @@ int fp_instance_create(fp_ctx* ctx, const fp_hypergraph* h, int32_t K, int32_t m
   d.C = pb.C;
   d.max_pw = (int)(pb.xw + (pb.xw * 0.1));
   d.min_pw = (int)(pb.xw - (pb.xw * 0.1));
+  // Heavy vertices (more than kHeavyDegHost nets), by position in visiting order.
+  in->heavy_pos.clear();
+  for (int z = 0; z < g.nov; z++) {
+    const int v = pb.order[z];
+    if ((int)(g.vptr[v + 1] - g.vptr[v]) > kHeavyDegHost) in->heavy_pos.push_back(z);
+  }
+  const int nheavy = (int)in->heavy_pos.size();
   const size_t KK = (size_t)K * K, words = (size_t)(K + 31) / 32;
   const bool msg = metric == FP_METRIC_TM || metric == FP_METRIC_MSM;
   uint32_t *vptr, *vnets, *nptr, *npins;
@@ -273,6 +294,19 @@ int fp_instance_create(fp_ctx* ctx, const fp_hypergraph* h, int32_t K, int32_t m
       (rc = dalloc(in, &d.recv, K)) || (rc = dalloc(in, &d.msgs, K)) || (rc = dalloc(in, &d.conn, msg ? KK : 1)) ||
       (rc = dalloc(in, &d.zrow, msg ? K * words : 1)) || (rc = dalloc(in, &d.zcol, msg ? K * words : 1)) ||
       (rc = dalloc(in, &d.moves, kMaxPasses)) || (rc = dalloc(in, &d.status, 1)) ||
+      (rc = dalloc(in, &in->sb.ctl, 8)) || (rc = dalloc(in, &in->sb.bar, 4)) || (rc = dalloc(in, &in->sb.stats, 32)) || (rc = dalloc(in, &in->sb.dec, kSpecWindow)) ||
+      (rc = dalloc(in, &in->sb.flag, kSpecWindow)) || (rc = dalloc(in, &in->sb.slack, kSpecWindow)) ||
+      (rc = dalloc(in, &in->sb.vslack, kSpecWindow)) || (rc = dalloc(in, &in->sb.wt, kSpecWindow)) ||
+      (rc = dalloc(in, &in->sb.vd, kSpecWindow)) || (rc = dalloc(in, &in->sb.scan, (size_t)kSpecWindow * words)) ||
+      (rc = dalloc(in, &in->sb.nflag, (size_t)kSpecWindow * kHeavyDegHost)) ||
+      (rc = dalloc(in, &in->sb.cand, (size_t)kSpecWindow * K)) || (rc = dalloc(in, &in->sb.ncand, kSpecWindow)) ||
+      (rc = dalloc(in, &in->sb.pref, (size_t)kSpecWindow * K)) ||
+      (rc = dalloc(in, &in->sb.wsum, kMaxSpecWarps)) || (rc = dalloc(in, &in->sb.vsum, kMaxSpecWarps)) ||
+      (rc = dalloc(in, &in->sb.claim_m, g.noe)) || (rc = dalloc(in, &in->sb.claim_c, g.noe)) ||
+      (rc = dalloc(in, &in->sb.mask_c, g.noe)) || (rc = dalloc(in, &in->sb.hcnt, 2 * K)) ||
+      (rc = dalloc(in, &in->sb.hfirst, 2 * K)) || (rc = dalloc(in, &in->sb.hgain, 2 * K)) ||
+      (rc = dalloc(in, &in->sb.hloss, 2 * K)) || (rc = dalloc(in, &in->sb.hadelta, 2 * K)) ||
+      (rc = dalloc(in, &in->sb.hmisc, 16)) || (rc = dalloc(in, &in->heavy_pos_d, std::max(nheavy, 1))) ||
       (rc = dalloc(in, &in->metric_out, 8))) {
     fp_instance_destroy(in);
     return rc;
@@ -282,6 +316,26 @@ int fp_instance_create(fp_ctx* ctx, const fp_hypergraph* h, int32_t K, int32_t m
   if (e != cudaSuccess) { fp_instance_destroy(in); return cuda_status(e); }
   in->allocs.push_back(ms);
   in->metric_scratch = ms;
+  in->sb.wmax = kSpecWindow;
+  in->sb.max_warps = kMaxSpecWarps;
+  in->sb.heavy_pos = in->heavy_pos_d;
+  in->sb.nheavy = nheavy;
+  {
+    cudaStream_t s0 = ctx->stream;
+    e = cudaMemsetAsync(in->sb.claim_m, 0x7f, sizeof(int) * std::max(g.noe, 1), s0);
+    if (e == cudaSuccess) e = cudaMemsetAsync(in->sb.claim_c, 0x7f, sizeof(int) * std::max(g.noe, 1), s0);
+    if (e == cudaSuccess) e = cudaMemsetAsync(in->sb.mask_c, 0, sizeof(uint32_t) * std::max(g.noe, 1), s0);
+    if (e == cudaSuccess) e = cudaMemsetAsync(in->sb.hcnt, 0, sizeof(int) * 2 * K, s0);
+    if (e == cudaSuccess) e = cudaMemsetAsync(in->sb.hfirst, 0xff, sizeof(unsigned long long) * 2 * K, s0);
+    if (e == cudaSuccess) e = cudaMemsetAsync(in->sb.hgain, 0, sizeof(int) * 2 * K, s0);
+    if (e == cudaSuccess) e = cudaMemsetAsync(in->sb.hloss, 0, sizeof(int) * 2 * K, s0);
+    if (e == cudaSuccess) e = cudaMemsetAsync(in->sb.hadelta, 0, sizeof(int) * 2 * K, s0);
+    if (e == cudaSuccess) e = cudaMemsetAsync(in->sb.hmisc, 0, sizeof(int) * 16, s0);
+    if (e == cudaSuccess && nheavy)
+      e = cudaMemcpyAsync(in->heavy_pos_d, in->heavy_pos.data(), sizeof(int) * nheavy, cudaMemcpyHostToDevice, s0);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s0);
+    if (e != cudaSuccess) { fp_instance_destroy(in); return cuda_status(e); }
+  }
   if (cudaMallocHost(&in->h_moves, sizeof(long long) * kMaxPasses) != cudaSuccess ||
       cudaMallocHost(&in->h_status, sizeof(int)) != cudaSuccess ||
       cudaMallocHost(&in->h_metrics, sizeof(long long) * 8) != cudaSuccess) {
@@ -340,7 +394,18 @@ int fp_refine(fp_instance* in, int32_t passes) {
   cudaSetDevice(in->ctx->device);
   cudaStream_t s = in->ctx->stream;
   cudaError_t e = cudaMemsetAsync(in->d.moves, 0, sizeof(long long) * passes, s);
-  if (e == cudaSuccess) e = launch_refine(in->d, passes, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(in->d.status, 0, sizeof(int), s);
+  const bool spec = in->engine == FP_ENGINE_AUTO && spec_supported(in->pb.metric);
+  if (spec) {
+    static const int none[8] = {0x7fffffff, 0x7fffffff, 0x7fffffff, 0x7fffffff,
+                                0x7fffffff, 0x7fffffff, 0x7fffffff, 0x7fffffff};
+    if (e == cudaSuccess) e = cudaMemcpyAsync(in->sb.ctl, none, sizeof(none), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(in->sb.bar, 0, sizeof(unsigned) * 4, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(in->sb.stats, 0, sizeof(unsigned long long) * 32, s);
+    if (e == cudaSuccess) e = launch_spec_ldg(in->d, in->sb, passes, in->ctx->num_sms, s, &in->last_grid);
+  } else if (e == cudaSuccess) {
+    e = launch_refine(in->d, passes, s);
+  }
   if (e == cudaSuccess) e = cudaMemcpyAsync(in->h_status, in->d.status, sizeof(int), cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(in->h_moves, in->d.moves, sizeof(long long) * passes, cudaMemcpyDeviceToHost, s);
@@ -349,6 +414,12 @@ int fp_refine(fp_instance* in, int32_t passes) {
   in->last_passes = passes;
   in->last_launches = 1;
   return *in->h_status;
+}
+
+int fp_set_engine(fp_instance* in, int32_t engine) {
+  if (!in || (engine != FP_ENGINE_AUTO && engine != FP_ENGINE_SEQUENTIAL)) return FP_ERR_INVALID;
+  in->engine = engine;
+  return FP_OK;
 }
 
 int fp_metrics(fp_instance* in, int64_t out[6]) {
@@ -402,6 +473,11 @@ int fp_get_moves(fp_instance* in, int64_t* moves, int32_t n) {
   if (!in || !moves || n < 0) return FP_ERR_INVALID;
   for (int i = 0; i < n; i++) moves[i] = i < in->last_passes ? in->h_moves[i] : 0;
   return FP_OK;
+}
+
+int fp_get_stats(fp_instance* in, int64_t* out, int32_t n) {
+  if (!in || !out || n < 0 || n > 32) return FP_ERR_INVALID;
+  return d2h(in, out, in->sb.stats, sizeof(int64_t) * n);
 }
 
 int fp_last_launches(fp_instance* in, int64_t* launches) {

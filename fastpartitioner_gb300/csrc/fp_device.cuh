@@ -44,6 +44,42 @@ struct DevInstance {
   int* status;       // device status word, 0 = ok
 };
 
+// Device buffers of the speculative engine (fp_spec.cu), allocated with the
+// instance.
+struct SpecBuf {
+  unsigned* bar;         // [4] grid barrier: arrivals, generation, abort
+  int* ctl;              // [8] per-round words, double-buffered by round parity:
+                         //     [0,1] cut, [2,3] first max-touching mover
+  int* dec;              // [wmax] (own part << 16) | decision per window offset
+  unsigned char* flag;   // [wmax] bit0 mover, bit1 stale-marker risk
+  int* slack;            // [wmax] part-size drift the decision tolerates (-1: none)
+  int* vslack;           // [wmax] volume drift the accept/reject outcome tolerates
+  int* wt;               // [wmax] weight moved by a mover (0 otherwise)
+  int* vd;               // [wmax] largest volume change of one part by a mover
+  uint32_t* scan;        // [wmax * words] parts scanned per window offset (TV)
+  unsigned char* nflag;  // [wmax * 256] per mover net: bit0 loses own part, bit1 gains
+                         //     the new part, bit2 the mover is the net's source
+  unsigned long long* cand;  // [wmax * K] LDG candidates per window offset (part, count, first)
+  int* ncand;            // [wmax]
+  int* pref;             // [K * wmax] per-part prefix of the window's size changes
+  int* wsum;             // [max_warps] per-warp sums of wt
+  int* vsum;             // [max_warps] per-warp sums of vd
+  int* claim_m;          // [noe] first mover position changing the net's part set
+  int* claim_c;          // [noe] first mover position changing only counts
+  uint32_t* mask_c;      // [noe] parts (mod 32) whose counts those movers change
+  const int* heavy_pos;  // positions (in visiting order) of heavy vertices, ascending
+  int nheavy;
+  int* hcnt;             // [2*K] heavy-vertex tally (double-buffered)
+  unsigned long long* hfirst;  // [2*K]
+  int* hgain;            // [2*K]
+  int* hloss;            // [2*K]
+  int* hadelta;          // [2*K]
+  int* hmisc;            // [16]
+  unsigned long long* stats;  // [32] round statistics (see fp_get_stats)
+  int wmax;
+  int max_warps;
+};
+
 // Status values a kernel can report (mirrors FP_ERR_* of the public header).
 constexpr int kDevErrInvalid = -1;
 constexpr int kDevErrUnsupported = -5;

@@ -1,0 +1,835 @@
+// Speculative grid-wide refinement for the LDG metrics: TV (TV/partition.cpp:
+// 307-440), MSV (MGV/partition.cpp:222-477) and MSRV (MSRV/partition.cpp:240-517).
+//
+// The reference walks the vertices one by one; every decision reads the state
+// left by all earlier moves.  Here one persistent cooperative kernel runs all
+// passes as a sequence of rounds.  A round covers a window of the next vertices
+// in visiting order:
+//
+//   A  evaluate   every warp of the grid decides its vertices against the
+//                 current state, as if each were next.  A mover claims its nets
+//                 (part-set-changing or count-only), and every vertex records
+//                 how much part-size / volume drift its outcome tolerates.
+//   B  validate   a vertex keeps its outcome iff nothing it read can have
+//                 changed: no earlier mover of the window changed the part set
+//                 of one of its nets, or the count of its own part there; the
+//                 weight moved before it stays within its size slack (the LDG
+//                 argmax, its tie-breaks and TV's clamps cannot flip); the
+//                 volumes stay within its volume slack; no earlier mover touched
+//                 a max-volume part; for TV, no stale marker can apply.  The
+//                 first invalid position cuts the window.
+//   C  commit     all movers before the cut are applied at once -- on any net
+//                 they either are alone or only shift counts, which commute --
+//                 and the next window starts at the cut.
+//
+// Every committed outcome therefore equals the reference's sequential outcome.
+// Vertices with more than kHeavyDeg nets get a round of their own in which all
+// warps of the grid split the tally, the gain / loss sums and the move.
+
+#include "fp_spec_common.cuh"
+
+namespace fp {
+
+namespace {
+
+using namespace spec;
+
+constexpr int kTV = 1, kMSRV = 5;
+constexpr int kBig = 1000000000;
+
+__device__ __forceinline__ int clamp_slack(double x) {
+  if (!(x > -1.0)) return -1;
+  if (x > 1.0e9) return kBig;
+  return (int)floor(x);
+}
+
+struct RoundCtx {
+  const int* sizes;
+  const double* pen;
+  const int* marker;
+  const int* vol;
+  const int* mark;
+  int minpart, minsize, second, maxv, cc;
+};
+
+// LDG argmax over the tallied parts (TV/partition.cpp:98-145 with TV's clamps,
+// MGV/partition.cpp:28-65 without), executed by one warp, plus the part-size
+// drift under which the outcome cannot change.
+__device__ int ldg_decide(const DevInstance& I, const RoundCtx& R, const int* cnt, const unsigned long long* first,
+                          int metric, int v, int own, bool first_of_window, bool* special, int* slack_out) {
+  const int lane = threadIdx.x & 31;
+  const int K = I.K;
+  LdgKey best{-1.0, 0, -1, ~0ull};
+  bool sp = false;
+  for (int p = lane; p < K; p += 32) {
+    const int c = cnt[p];
+    if (c > 0) {
+      const bool stale = metric == kTV && R.marker[p] == v;
+      if (stale && !first_of_window) sp = true;
+      if (!stale) {
+        LdgKey k{__dmul_rn((double)(c - (p == own ? 1 : 0)), R.pen[p]), R.sizes[p], p, first[p]};
+        if (ldg_better(k, best)) best = k;
+      }
+    }
+  }
+  best = warp_ldg_argmax(best);
+  *special = __any_sync(kAll, sp);
+  const int d0 = best.part >= 0 ? best.part : R.minpart;
+  int d = d0;
+  if (metric == kTV) {
+    if (R.sizes[d] > I.max_pw) d = own;
+    if (R.sizes[d] < I.min_pw) d = own;
+  }
+  // Drift margins: every part's size may move by at most D.  All conditions are
+  // monotone in D; a 1e-12 relative and one-unit margin covers the rounding.
+  int sl = kBig;
+  const double C = I.C;
+  if (best.part >= 0) {
+    const int w = best.part;
+    const int cw = cnt[w] - (w == own ? 1 : 0);
+    const double Sw = best.score;
+    sl = min(sl, clamp_slack(Sw * C / cw * (1.0 - 1e-12)) - 1);   // stays positive
+    for (int q = lane; q < K; q += 32) {
+      const int c = cnt[q];
+      if (q == w || c <= 0) continue;
+      if (metric == kTV && R.marker[q] == v) continue;
+      const int cq = c - (q == own ? 1 : 0);
+      if (cq <= 0) continue;
+      const double diff = Sw - __dmul_rn((double)cq, R.pen[q]);
+      if (!(diff > 0)) { sl = -1; continue; }                     // tie: size / order decide
+      sl = min(sl, clamp_slack(diff * C / (double)(cw + cq) * (1.0 - 1e-12)) - 1);
+    }
+  } else {
+    for (int q = lane; q < K; q += 32) {
+      const int c = cnt[q];
+      if (c <= 0) continue;
+      if (metric == kTV && R.marker[q] == v) continue;
+      if (c - (q == own ? 1 : 0) <= 0) continue;
+      sl = min(sl, clamp_slack((double)R.sizes[q] - C) - 1);       // stays non-positive
+    }
+    sl = min(sl, (R.second - R.minsize - 1) / 2);                 // least-loaded part stays
+  }
+  if (metric == kTV) {
+    const int s0 = R.sizes[d0];
+    sl = min(sl, s0 > I.max_pw ? s0 - I.max_pw - 1 : I.max_pw - s0);
+    const int d1 = s0 > I.max_pw ? own : d0;
+    const int s1 = R.sizes[d1];
+    sl = min(sl, s1 < I.min_pw ? I.min_pw - s1 - 1 : s1 - I.min_pw);
+  }
+  sl = warp_min(sl);
+  *slack_out = max(sl, -1);
+  return d;
+}
+
+// The LDG decision of the vertex at window offset o again, from its stored
+// candidates and the exact part sizes at that position (round-start sizes plus
+// the prefix of the window's moves); one warp.
+__device__ int ldg_recheck(const DevInstance& I, const RoundCtx& R, const SpecBuf& B, int o, int v, int own,
+                           int metric) {
+  const int lane = threadIdx.x & 31;
+  const int K = I.K;
+  const unsigned long long* cl = B.cand + (size_t)o * K;
+  const int nc = lds(&B.ncand[o]);
+  LdgKey best{-1.0, 0, -1, ~0ull};
+  for (int i = lane; i < nc; i += 32) {
+    const unsigned long long ent = lds(&cl[i]);
+    const int p = (int)(ent >> 52);
+    const int c = (int)((ent >> 36) & 0xffffull);
+    const unsigned long long f = (((ent >> 20) & 0xffffull) << 32) | (ent & 0xfffffull);
+    const int sz = R.sizes[p] + lds(&B.pref[(size_t)p * B.wmax + o]);
+    const double pen = __dsub_rn(1.0, __ddiv_rn((double)sz, I.C));
+    LdgKey k{__dmul_rn((double)c, pen), sz, p, f};
+    if (ldg_better(k, best)) best = k;
+  }
+  best = warp_ldg_argmax(best);
+  int d0 = best.part;
+  if (d0 < 0) {
+    unsigned long long mk = ~0ull;
+    for (int p = lane; p < K; p += 32) {
+      const int sz = R.sizes[p] + lds(&B.pref[(size_t)p * B.wmax + o]);
+      const unsigned long long key = ((unsigned long long)((unsigned)sz ^ 0x80000000u) << 32) | (unsigned)p;
+      mk = key < mk ? key : mk;
+    }
+    for (int off = 16; off; off >>= 1) {
+      const unsigned long long x = __shfl_xor_sync(kAll, mk, off);
+      mk = x < mk ? x : mk;
+    }
+    d0 = (int)(mk & 0xffffffffu);
+  }
+  int d = d0;
+  if (metric == kTV) {
+    if (R.sizes[d] + lds(&B.pref[(size_t)d * B.wmax + o]) > I.max_pw) d = own;
+    if (R.sizes[d] + lds(&B.pref[(size_t)d * B.wmax + o]) < I.min_pw) d = own;
+  }
+  (void)v;
+  return d;
+}
+
+// Per-net pass of a vertex with d != own, one net per thread (nets k0, k0 +
+// kstep, ...): which nets lose `own` / gain `d` (nflag bit0 / bit1; bit2 = v is
+// the net's source), and for MSV / MSRV the reference's gains / losses
+// (MGV/partition.cpp:294-337, MSRV/partition.cpp:303-350) and the exact change
+// of every part's volume that commit_net will make (adelta).
+__device__ void net_pass(const DevInstance& I, int metric, int v, int own, int d, uint32_t base, int deg, int k0,
+                         int kstep, unsigned char* nflag, int* gains, int* losses, int* adelta) {
+  const bool vol = metric != kTV;
+  const bool rv = metric == kMSRV;
+  for (int k = k0; k < deg; k += kstep) {
+    const int e = (int)__ldg(&I.vnets[base + k]);
+    const int s = (int)__ldg(&I.nptr[e]);
+    const int n = lds(&I.ep_len[e]);
+    int co = 0;
+    bool fd = false;
+    for (int j = 0; j < n; j++) {
+      const int p = lds(&I.ep_part[s + j]);
+      if (p == own) co = lds(&I.ep_cnt[s + j]);
+      if (p == d) fd = true;
+    }
+    const bool rem = co == 1, add = !fd;
+    const int sv = __ldg(&I.src[e]);
+    if (nflag) nflag[k] = (unsigned char)((rem ? 1 : 0) | (add ? 2 : 0) | (sv == v ? 4 : 0));
+    if (!vol) continue;
+    const int sp = sv == v ? own : lds(&I.part_vec[sv]);
+    if (sv == v) {
+      atomicAdd(&gains[own], n - 1);
+      atomicAdd(&losses[d], n - 1);
+    }
+    if (rem) {
+      if (sv != v) {
+        atomicAdd(&gains[sp], 1);
+        if (rv) atomicAdd(&gains[own], 1);
+      } else {
+        atomicAdd(&losses[d], -1);
+      }
+    }
+    if (add) {
+      if (sv != v) {
+        atomicAdd(&losses[sp], 1);
+        if (rv) atomicAdd(&losses[d], 1);
+      } else {
+        atomicAdd(&losses[d], 1);
+      }
+    }
+    const int n1 = rem ? n - 1 : n;
+    if (sv == v) {
+      atomicAdd(&adelta[own], -(n - 1));
+      atomicAdd(&adelta[d], n1 - 1);
+    }
+    if (rem) {
+      if (sv != v) {
+        atomicAdd(&adelta[sp], -1);
+        if (rv) atomicAdd(&adelta[own], -1);
+      }
+    } else if (rv && sv == v) {
+      atomicAdd(&adelta[own], 1);
+    }
+    if (!add) {
+      if (rv && sv == v) atomicAdd(&adelta[d], -1);
+    } else {
+      atomicAdd(&adelta[sv == v ? d : sp], 1);
+      if (rv && sv != v) atomicAdd(&adelta[d], 1);
+    }
+  }
+}
+
+// Per-thread partial of the MSV / MSRV accept test (MGV/partition.cpp:339-362,
+// MSRV/partition.cpp:352-376) over parts p0, p0 + pstep, ...
+struct AcceptPart {
+  bool failM, failN, mt;
+  int fsl, msl, vd;
+};
+
+__device__ AcceptPart accept_partial(const RoundCtx& R, const int* gains, const int* losses, const int* adelta, int K,
+                                     bool rv, int p0, int pstep) {
+  AcceptPart a{false, false, false, -1, kBig, 0};
+  for (int p = p0; p < K; p += pstep) {
+    const int g = gains[p], l = losses[p];
+    const int t = R.vol[p] + l - g;
+    if (R.mark[p] == R.cc) {
+      if (rv ? (g <= l) : (g < l)) a.failM = true;
+      if (adelta[p] != 0) a.mt = true;
+    } else {
+      if (t >= R.maxv) { a.failN = true; a.fsl = max(a.fsl, t - R.maxv); }
+      a.msl = min(a.msl, R.maxv - 1 - t);
+    }
+    a.vd = max(a.vd, abs(adelta[p]));
+  }
+  return a;
+}
+
+// Outcome and volume slack: accepted -> stays accepted while no non-max part
+// rises by more than msl; rejected on a max part -> local, stays rejected;
+// rejected only on non-max parts -> stays rejected while the worst of them
+// drops by at most fsl.
+__device__ __forceinline__ void accept_final(bool failM, bool failN, int fsl, int msl, bool* good, int* vslack) {
+  *good = !failM && !failN;
+  *vslack = *good ? msl : (failM ? kBig : fsl);
+}
+
+__global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, SpecBuf B, int passes) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ unsigned long long uscr[kSWarps];
+  __shared__ int iscr[kSWarps];
+  __shared__ int s_minpart, s_minsize, s_second, s_maxv, s_cc, s_count, s_d;
+  __shared__ long long s_pre_w, s_pre_v;
+  const int metric = I.metric;
+  const bool vol = metric != kTV;
+  const bool rv = metric == kMSRV;
+  const int K = I.K;
+  const int words = (K + 31) >> 5;
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const int gw = blockIdx.x * kSWarps + wib;
+  const int nwarps = gridDim.x * kSWarps;
+  Carve cv{smem_raw};
+  int* sizes_s = cv.take<int>(K);
+  double* pen_s = cv.take<double>(K);
+  int* marker_s = cv.take<int>(K);
+  int* vol_s = cv.take<int>(K);
+  int* mark_s = cv.take<int>(K);
+  int* cnt_b = cv.take<int>((size_t)K * kSWarps);                    // per-warp arrays, warp x at x*K
+  unsigned long long* first_b = cv.take<unsigned long long>((size_t)K * kSWarps);
+  int* gains_b = cv.take<int>((size_t)K * kSWarps);
+  int* losses_b = cv.take<int>((size_t)K * kSWarps);
+  int* adelta_b = cv.take<int>((size_t)K * kSWarps);
+  int* cnt = cnt_b + (size_t)wib * K;
+  unsigned long long* first = first_b + (size_t)wib * K;
+  int* gains = gains_b + (size_t)wib * K;
+  int* losses = losses_b + (size_t)wib * K;
+  int* adelta = adelta_b + (size_t)wib * K;
+  Vol V{I.send, rv ? I.recv : nullptr};
+
+  int round = 0;
+  int heavy_round = 0;
+  unsigned long long tA = gtimer();
+  for (int it = 0; it < passes; it++) {
+    int pos = 0;
+    int W = min(nwarps, B.wmax);
+    int hidx = 0;
+    bool pass_start = true;
+    bool prev_maxtouch = false;
+    while (pos < I.nov) {
+      const int par = round & 1;
+      // ------------------------------------------------------------ round state
+      for (int p = threadIdx.x; p < K; p += blockDim.x) {
+        const int sz = lds(&I.part_sizes[p]);
+        sizes_s[p] = sz;
+        pen_s[p] = __dsub_rn(1.0, __ddiv_rn((double)sz, I.C));
+        if (metric == kTV) marker_s[p] = lds(&I.marker[p]);
+        if (vol) vol_s[p] = lds(&I.send[p]) + (rv ? lds(&I.recv[p]) : 0);
+      }
+      __syncthreads();
+      block_min_part(sizes_s, K, uscr, &s_minpart, &s_minsize, &s_second);
+      if (vol) {
+        // Max-volume parts.  MSV rescans after every move (MGV/partition.cpp:
+        // 453-472); MSRV rescans only when an old max part changed, against the
+        // old maximum, appending to its list (MSRV/partition.cpp:486-513).
+        int mx = -2147483647 - 1;
+        for (int p = threadIdx.x; p < K; p += blockDim.x) mx = max(mx, vol_s[p]);
+        mx = warp_max(mx);
+        if (lane == 0) iscr[wib] = mx;
+        __syncthreads();
+        mx = iscr[0];
+        for (int x = 1; x < kSWarps; x++) mx = max(mx, iscr[x]);
+        __syncthreads();
+        if (!rv || pass_start) {
+          int local = 0;
+          for (int p = threadIdx.x; p < K; p += blockDim.x) {
+            const bool m = vol_s[p] == mx;
+            mark_s[p] = m ? 1 : -1;
+            local += m;
+          }
+          local = warp_sum(local);
+          if (lane == 0) iscr[wib] = local;
+          __syncthreads();
+          if (threadIdx.x == 0) {
+            int c = 0;
+            for (int x = 0; x < kSWarps; x++) c += iscr[x];
+            s_maxv = mx;
+            s_cc = 1;
+            s_count = c;
+          }
+          __syncthreads();
+        } else if (prev_maxtouch) {
+          bool changed = false;
+          for (int p = threadIdx.x; p < K; p += blockDim.x)
+            if (mark_s[p] == s_cc && vol_s[p] != s_maxv) changed = true;
+          changed = __syncthreads_or(changed);
+          if (changed && mx >= s_maxv) {
+            const int ncc = mx > s_maxv ? s_cc + 1 : s_cc;
+            int local = 0;
+            for (int p = threadIdx.x; p < K; p += blockDim.x)
+              if (vol_s[p] == mx) { mark_s[p] = ncc; local++; }
+            local = warp_sum(local);
+            if (lane == 0) iscr[wib] = local;
+            __syncthreads();
+            if (threadIdx.x == 0) {
+              int c = 0;
+              for (int x = 0; x < kSWarps; x++) c += iscr[x];
+              s_count = (mx > s_maxv ? 0 : s_count) + c;
+              s_maxv = mx;
+              s_cc = ncc;
+              if (s_count > K) dev_fail(I.status, kDevErrUnsupported);  // the reference overruns max_parts
+            }
+            __syncthreads();
+          }
+        }
+      }
+      __syncthreads();
+      const RoundCtx R{sizes_s, pen_s, marker_s, vol_s, mark_s, s_minpart, s_minsize, s_second, s_maxv, s_cc};
+      pass_start = false;
+      prev_maxtouch = false;
+      while (hidx < B.nheavy && __ldg(&B.heavy_pos[hidx]) < pos) hidx++;
+      const int next_heavy = hidx < B.nheavy ? __ldg(&B.heavy_pos[hidx]) : I.nov;
+
+      if (next_heavy == pos) {
+        // ========================================================== heavy round
+        const int hp = heavy_round & 1;
+        int* hcnt = B.hcnt + hp * K;
+        unsigned long long* hfirst = B.hfirst + hp * K;
+        int* hgain = B.hgain + hp * K;
+        int* hloss = B.hloss + hp * K;
+        int* hadelta = B.hadelta + hp * K;
+        int* hmisc = B.hmisc + hp * 8;
+        const int v = __ldg(&I.order[pos]);
+        const int own = lds(&I.part_vec[v]);
+        const uint32_t base = __ldg(&I.vptr[v]);
+        const int deg = (int)(__ldg(&I.vptr[v + 1]) - base);
+        // A: every warp tallies a slice of the nets; CTAs pre-reduce.
+        for (int p = lane; p < K; p += 32) { cnt[p] = 0; first[p] = ~0ull; }
+        __syncwarp();
+        int c1 = 0;
+        for (int nb = gw * 32; nb < deg; nb += nwarps * 32) c1 += tally_batch(I, own, base, nb, deg, cnt, first);
+        c1 = warp_sum(c1);
+        __syncthreads();
+        for (int p = threadIdx.x; p < K; p += blockDim.x) {
+          int c = 0;
+          unsigned long long f = ~0ull;
+          for (int x = 0; x < kSWarps; x++) {
+            c += cnt_b[(size_t)x * K + p];
+            const unsigned long long fx = first_b[(size_t)x * K + p];
+            f = fx < f ? fx : f;
+          }
+          if (c) {
+            atomicAdd(&hcnt[p], c);
+            atomicMin(&hfirst[p], f);
+          }
+        }
+        if (lane == 0 && c1) atomicAdd(&hmisc[0], c1);
+        if (!grid_barrier(B.bar, I.status)) return;
+        // B: every CTA takes the same decision from the global tally.
+        for (int p = threadIdx.x; p < K; p += blockDim.x) {
+          cnt_b[p] = lds(&hcnt[p]);
+          first_b[p] = lds(&hfirst[p]);
+        }
+        __syncthreads();
+        if (wib == 0) {
+          bool special;
+          int slack;
+          const int d = ldg_decide(I, R, cnt_b, first_b, metric, v, own, true, &special, &slack);
+          if (lane == 0) s_d = d;
+        }
+        __syncthreads();
+        const int d = s_d;
+        const int hc1 = lds(&hmisc[0]);
+        bool mover = false;
+        if (metric == kTV) {
+          mover = d != own && hc1 >= deg - cnt_b[d];
+        } else if (d != own) {
+          for (int p = lane; p < K; p += 32) { gains[p] = 0; losses[p] = 0; adelta[p] = 0; }
+          __syncwarp();
+          net_pass(I, metric, v, own, d, base, deg, gw * 32 + lane, nwarps * 32, nullptr, gains, losses, adelta);
+          __syncthreads();
+          for (int p = threadIdx.x; p < K; p += blockDim.x) {
+            int g = 0, l = 0, a = 0;
+            for (int x = 0; x < kSWarps; x++) {
+              g += gains_b[(size_t)x * K + p];
+              l += losses_b[(size_t)x * K + p];
+              a += adelta_b[(size_t)x * K + p];
+            }
+            if (g) atomicAdd(&hgain[p], g);
+            if (l) atomicAdd(&hloss[p], l);
+            if (a) atomicAdd(&hadelta[p], a);
+          }
+        }
+        if (!grid_barrier(B.bar, I.status)) return;
+        // C: accept test (MSV/MSRV), commit, markers, clean-up.
+        if (vol && d != own) {
+          for (int p = threadIdx.x; p < K; p += blockDim.x) {
+            gains_b[p] = lds(&hgain[p]);
+            losses_b[p] = lds(&hloss[p]);
+            adelta_b[p] = lds(&hadelta[p]);
+          }
+          __syncthreads();
+          const AcceptPart a = accept_partial(R, gains_b, losses_b, adelta_b, K, rv, threadIdx.x, blockDim.x);
+          const bool fM = __syncthreads_or(a.failM);
+          const bool fN = __syncthreads_or(a.failN);
+          const bool mt = __syncthreads_or(a.mt);
+          mover = !fM && !fN;
+          prev_maxtouch = mover && mt;
+        }
+        if (mover) {
+          for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < deg; i += gridDim.x * blockDim.x)
+            commit_net(I, v, own, d, (int)__ldg(&I.vnets[base + i]), vol ? &V : nullptr);
+          if (blockIdx.x == 0 && threadIdx.x == 0) {
+            I.part_vec[v] = d;
+            const int wv = __ldg(&I.w[v]);
+            atomicAdd(&I.part_sizes[own], -wv);
+            atomicAdd(&I.part_sizes[d], wv);
+            atomicAdd((unsigned long long*)&I.moves[it], 1ull);
+          }
+        }
+        if (metric == kTV && blockIdx.x == 0)
+          for (int p = threadIdx.x; p < K; p += blockDim.x)
+            if (cnt_b[p] > 0) I.marker[p] = v;
+        {
+          const int op = hp ^ 1;   // clear the other heavy buffers for the next heavy round
+          for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < K; p += gridDim.x * blockDim.x) {
+            B.hcnt[op * K + p] = 0;
+            B.hfirst[op * K + p] = ~0ull;
+            B.hgain[op * K + p] = 0;
+            B.hloss[op * K + p] = 0;
+            B.hadelta[op * K + p] = 0;
+          }
+          if (blockIdx.x == 0 && threadIdx.x < 8) B.hmisc[op * 8 + threadIdx.x] = 0;
+        }
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+          B.ctl[par ^ 1] = kNone;
+          B.ctl[2 + (par ^ 1)] = kNone;
+        }
+        pos += 1;
+        heavy_round++;
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+          B.stats[1]++;
+          const unsigned long long tH = gtimer();
+          B.stats[19] += tH - tA;
+          tA = tH;
+        }
+        round++;
+        if (!grid_barrier(B.bar, I.status)) return;
+        continue;
+      }
+
+      // ============================================================ light round
+      const int end_w = min(min(pos + W, I.nov), next_heavy);
+      const int span = end_w - pos;
+      const int q = (span + nwarps - 1) / nwarps;
+      const int z0 = min(pos + gw * q, end_w);
+      const int z1 = min(z0 + q, end_w);
+      // ---- A: evaluate
+      int wsum = 0, vsum = 0;
+      for (int z = z0; z < z1; z++) {
+        const int o = z - pos;
+        const int v = __ldg(&I.order[z]);
+        const int own = lds(&I.part_vec[v]);
+        const uint32_t base = __ldg(&I.vptr[v]);
+        const int deg = (int)(__ldg(&I.vptr[v + 1]) - base);
+        for (int p = lane; p < K; p += 32) { cnt[p] = 0; first[p] = ~0ull; }
+        __syncwarp();
+        int c1 = 0;
+        for (int nb = 0; nb < deg; nb += 32) c1 += tally_batch(I, own, base, nb, deg, cnt, first);
+        __syncwarp();
+        c1 = warp_sum(c1);
+        bool special;
+        int slack;
+        const int d = ldg_decide(I, R, cnt, first, metric, v, own, z == pos, &special, &slack);
+        {
+          // Candidates (part, count, first sighting) for an exact re-check of the
+          // decision if the part sizes drift beyond its slack.
+          unsigned long long* cl = B.cand + (size_t)o * K;
+          int nc = 0;
+          for (int p0 = 0; p0 < K; p0 += 32) {
+            const int p = p0 + lane;
+            bool ok = false;
+            unsigned long long ent = 0;
+            if (p < K) {
+              const int c = cnt[p];
+              if (c > 0 && !(metric == kTV && R.marker[p] == v)) {
+                ok = true;
+                const unsigned long long f = first[p];
+                ent = ((unsigned long long)p << 52) | ((unsigned long long)(c - (p == own ? 1 : 0)) << 36) |
+                      (((f >> 32) & 0xffffull) << 20) | (f & 0xfffffull);
+              }
+            }
+            const unsigned m = __ballot_sync(kAll, ok);
+            if (ok) cl[nc + __popc(m & ((1u << lane) - 1u))] = ent;
+            nc += __popc(m);
+          }
+          if (lane == 0) B.ncand[o] = nc;
+        }
+        unsigned char* nflag = B.nflag + (size_t)o * kHeavyDeg;
+        bool mover = false, mt = false;
+        int vs = kBig, vdd = 0;
+        if (d != own) {
+          if (metric == kTV) {
+            mover = c1 >= deg - cnt[d];
+            if (mover) net_pass(I, metric, v, own, d, base, deg, lane, 32, nflag, nullptr, nullptr, nullptr);
+          } else {
+            for (int p = lane; p < K; p += 32) { gains[p] = 0; losses[p] = 0; adelta[p] = 0; }
+            __syncwarp();
+            net_pass(I, metric, v, own, d, base, deg, lane, 32, nflag, gains, losses, adelta);
+            __syncwarp();
+            AcceptPart a = accept_partial(R, gains, losses, adelta, K, rv, lane, 32);
+            const bool fM = __any_sync(kAll, a.failM);
+            const bool fN = __any_sync(kAll, a.failN);
+            bool good;
+            accept_final(fM, fN, warp_max(a.fsl), warp_min(a.msl), &good, &vs);
+            mover = good;
+            mt = mover && __any_sync(kAll, a.mt);
+            vdd = warp_max(a.vd);
+          }
+        }
+        __syncwarp();
+        if (mover) {
+          // claims: part-set / source changes, or count-only changes
+          for (int k = lane; k < deg; k += 32) {
+            const int e = (int)__ldg(&I.vnets[base + k]);
+            const int fl = nflag[k];
+            if ((fl & 3) || (vol && (fl & 4))) {
+              atomicMin(&B.claim_m[e], z);
+            } else {
+              atomicMin(&B.claim_c[e], z);
+              atomicOr(&B.mask_c[e], (1u << (own & 31)) | (1u << (d & 31)));
+            }
+          }
+          if (lane == 0 && mt) atomicMin(&B.ctl[2 + par], z);
+        }
+        if (metric == kTV) {
+          for (int wd = 0; wd < words; wd++) {
+            const int p = wd * 32 + lane;
+            const unsigned m = __ballot_sync(kAll, p < K && cnt[p] > 0);
+            if (lane == 0) B.scan[(size_t)o * words + wd] = m;
+          }
+        }
+        const int wv = mover ? __ldg(&I.w[v]) : 0;
+        if (lane == 0) {
+          B.dec[o] = (own << 16) | d;   // own read now: part_vec changes in the commit phase
+          B.flag[o] = (unsigned char)((mover ? 1 : 0) | (special ? 2 : 0));
+          B.slack[o] = slack;
+          B.vslack[o] = vs;
+          B.wt[o] = wv;
+          B.vd[o] = mover ? vdd : 0;
+        }
+        wsum += wv;
+        vsum += mover ? vdd : 0;
+        __syncwarp();
+      }
+      if (lane == 0) {
+        B.wsum[gw] = wsum;
+        B.vsum[gw] = vsum;
+      }
+      if (!grid_barrier(B.bar, I.status)) return;
+      if (blockIdx.x == 0 && threadIdx.x == 0) {
+        const unsigned long long tE = gtimer();
+        B.stats[16] += tE - tA;
+        tA = tE;
+      }
+      // ---- P: per-part prefix sums of the size changes of the window's movers
+      // (exact part sizes at every window position).
+      for (int p = gw; p < K; p += nwarps) {
+        int carry = 0;
+        int* pr = B.pref + (size_t)p * B.wmax;
+        for (int o0 = 0; o0 < span; o0 += 32) {
+          const int o = o0 + lane;
+          int dl = 0;
+          if (o < span && (lds(&B.flag[o]) & 1)) {
+            const int pk = lds(&B.dec[o]);
+            const int wv = lds(&B.wt[o]);
+            if ((pk & 0xffff) == p) dl += wv;
+            if ((pk >> 16) == p) dl -= wv;
+          }
+          int incl = dl;
+          for (int off = 1; off < 32; off <<= 1) {
+            const int t = __shfl_up_sync(kAll, incl, off);
+            if (lane >= off) incl += t;
+          }
+          if (o < span) pr[o] = carry + incl - dl;
+          carry += __shfl_sync(kAll, incl, 31);
+        }
+      }
+      if (!grid_barrier(B.bar, I.status)) return;
+      // ---- B: validate.  Prefix sums of moved weight and volume drift over the
+      // warps before this one (warps own consecutive position ranges).
+      {
+        long long pw = 0, pv = 0;
+        const int lim = blockIdx.x * kSWarps;
+        for (int g = threadIdx.x; g < lim; g += blockDim.x) {
+          pw += lds(&B.wsum[g]);
+          pv += lds(&B.vsum[g]);
+        }
+        pw = warp_sum64(pw);
+        pv = warp_sum64(pv);
+        if (lane == 0) uscr[wib] = (unsigned long long)pw;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+          long long a = 0;
+          for (int x = 0; x < kSWarps; x++) a += (long long)uscr[x];
+          s_pre_w = a;
+        }
+        __syncthreads();
+        if (lane == 0) uscr[wib] = (unsigned long long)pv;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+          long long a = 0;
+          for (int x = 0; x < kSWarps; x++) a += (long long)uscr[x];
+          s_pre_v = a;
+        }
+        __syncthreads();
+      }
+      long long Dw = s_pre_w, Vw = s_pre_v;
+      for (int x = 0; x < wib; x++) {
+        Dw += lds(&B.wsum[blockIdx.x * kSWarps + x]);
+        Vw += lds(&B.vsum[blockIdx.x * kSWarps + x]);
+      }
+      const int mtpos = lds(&B.ctl[2 + par]);
+      for (int z = z0; z < z1; z++) {
+        const int o = z - pos;
+        const int fl = lds(&B.flag[o]);
+        int why = ((fl & 2) && z != pos) ? 1 : 0;
+        if (!why && Dw > max(lds(&B.slack[o]), 0)) {
+          // beyond the slack: decide again with the exact sizes at this position
+          const int pk = lds(&B.dec[o]);
+          if (ldg_recheck(I, R, B, o, __ldg(&I.order[z]), pk >> 16, metric) != (pk & 0xffff)) why = 2;
+        }
+        if (!why) why = Vw > max(lds(&B.vslack[o]), 0) ? 3 : mtpos < z ? 4 : 0;
+        bool bad = why != 0;
+        if (!bad) {
+          const int v = __ldg(&I.order[z]);
+          const int own = lds(&B.dec[o]) >> 16;
+          const bool mover = fl & 1;
+          const uint32_t base = __ldg(&I.vptr[v]);
+          const int deg = (int)(__ldg(&I.vptr[v + 1]) - base);
+          const unsigned ob = 1u << (own & 31);
+          const unsigned char* nflag = B.nflag + (size_t)o * kHeavyDeg;
+          bool conf = false;
+          for (int k = lane; k < deg; k += 32) {
+            const int e = (int)__ldg(&I.vnets[base + k]);
+            if (lds(&B.claim_m[e]) < z) conf = true;
+            if (lds(&B.claim_c[e]) < z) {
+              if (lds(&B.mask_c[e]) & ob) conf = true;
+              // a mover that changes this net's part set must not run next to
+              // earlier count updates on it
+              if (mover && ((nflag[k] & 3) || (vol && (nflag[k] & 4)))) conf = true;
+            }
+          }
+          bad = __any_sync(kAll, conf);
+          why = 5;
+        }
+        if (bad) {
+          if (lane == 0) atomicMin(&B.ctl[par], (z << 3) | why);   // position, then cut reason
+          break;
+        }
+        Dw += lds(&B.wt[o]);
+        Vw += lds(&B.vd[o]);
+      }
+      if (!grid_barrier(B.bar, I.status)) return;
+      // ---- C: commit every mover before the cut.
+      const int cutw = lds(&B.ctl[par]);
+      const int cut = cutw == kNone ? end_w : min(cutw >> 3, end_w);
+      if (blockIdx.x == 0 && threadIdx.x == 0) {
+        const unsigned long long tB = gtimer();
+        B.stats[0]++;
+        B.stats[3 + (cutw == kNone ? 0 : (cutw & 7))]++;
+        B.stats[9] += cut - pos;
+        B.stats[17] += tB - tA;
+        tA = tB;
+      }
+      if (cut <= pos) {             // no progress: inconsistent claims; stop (all CTAs agree)
+        if (threadIdx.x == 0) dev_fail(I.status, kDevErrInvalid);
+        return;
+      }
+      const int mt_c = lds(&B.ctl[2 + par]);
+      for (int z = z0; z < z1; z++) {
+        const int o = z - pos;
+        const int fl = lds(&B.flag[o]);
+        if (!(fl & 1)) continue;
+        const int v = __ldg(&I.order[z]);
+        const int pk = lds(&B.dec[o]);
+        const int own = pk >> 16, d = pk & 0xffff;
+        const uint32_t base = __ldg(&I.vptr[v]);
+        const int deg = (int)(__ldg(&I.vptr[v + 1]) - base);
+        if (z < cut) {
+          for (int k = lane; k < deg; k += 32) commit_net(I, v, own, d, (int)__ldg(&I.vnets[base + k]), vol ? &V : nullptr);
+          if (lane == 0) {
+            atomicAdd(&B.stats[2], 1ull);
+            I.part_vec[v] = d;
+            const int wv = __ldg(&I.w[v]);
+            atomicAdd(&I.part_sizes[own], -wv);
+            atomicAdd(&I.part_sizes[d], wv);
+            atomicAdd((unsigned long long*)&I.moves[it], 1ull);
+          }
+        }
+        for (int k = lane; k < deg; k += 32) {
+          const int e = (int)__ldg(&I.vnets[base + k]);
+          B.claim_m[e] = kNone;
+          B.claim_c[e] = kNone;
+          B.mask_c[e] = 0;
+        }
+      }
+      if (metric == kTV) {
+        // marker = last scanner of each part among the walked positions
+        const int len = cut - pos;
+        for (int p = gw; p < K; p += nwarps) {
+          for (int o0 = len - 1; o0 >= 0; o0 -= 32) {
+            const int o = o0 - lane;
+            const bool b = o >= 0 && ((lds(&B.scan[(size_t)o * words + (p >> 5)]) >> (p & 31)) & 1u);
+            const unsigned m = __ballot_sync(kAll, b);
+            if (m) {
+              if (lane == 0) I.marker[p] = __ldg(&I.order[pos + o0 - (__ffs(m) - 1)]);
+              break;
+            }
+          }
+        }
+      }
+      if (gw == 0 && lane == 0) {
+        B.ctl[par ^ 1] = kNone;
+        B.ctl[2 + (par ^ 1)] = kNone;
+      }
+      prev_maxtouch = mt_c < cut;
+      if (cut == end_w) {
+        if (end_w == pos + W) W = min(2 * W, B.wmax);
+      } else {
+        W = max(256, min(B.wmax, 2 * (cut - pos)));
+      }
+      pos = cut;
+      round++;
+      if (!grid_barrier(B.bar, I.status)) return;
+      if (blockIdx.x == 0 && threadIdx.x == 0) {
+        const unsigned long long tC = gtimer();
+        B.stats[18] += tC - tA;
+        tA = tC;
+      }
+    }
+  }
+}
+
+}  // namespace
+
+size_t spec_ldg_smem_bytes(int K) {
+  auto a = [](size_t n) { return (n + 15) & ~size_t(15); };
+  const size_t k4 = a(sizeof(int) * K), k8 = a(sizeof(double) * K);
+  return 4 * k4 + k8 + 4 * a(sizeof(int) * (size_t)K * kSWarps) + a(sizeof(unsigned long long) * (size_t)K * kSWarps);
+}
+
+cudaError_t launch_spec_ldg(const DevInstance& I, const SpecBuf& B, int passes, int num_sms, cudaStream_t st,
+                            int* grid_out) {
+  const size_t smem = spec_ldg_smem_bytes(I.K);
+  const void* fn = (const void*)spec_ldg_kernel;
+  cudaError_t err = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (err != cudaSuccess) return err;
+  int per_sm = 0;
+  err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kSThreads, smem);
+  if (err != cudaSuccess) return err;
+  if (per_sm < 1) return cudaErrorInvalidConfiguration;
+  int grid = per_sm * num_sms;
+  if (grid * kSWarps > B.max_warps) grid = B.max_warps / kSWarps;
+  if (grid_out) *grid_out = grid;
+  DevInstance Ic = I;
+  SpecBuf Bc = B;
+  int p = passes;
+  void* args[] = {&Ic, &Bc, &p};
+  err = cudaLaunchCooperativeKernel(fn, grid, kSThreads, args, smem, st);
+  if (err != cudaSuccess) return err;
+  return cudaGetLastError();
+}
+
+}  // namespace fp

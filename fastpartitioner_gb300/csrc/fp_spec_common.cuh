@@ -1,0 +1,277 @@
+// Helpers shared by the speculative (grid-wide) refinement kernels.
+#pragma once
+
+#include "fp_device.cuh"
+
+#include <cooperative_groups.h>
+
+namespace fp {
+namespace spec {
+
+namespace cg = cooperative_groups;
+
+constexpr int kSThreads = 256;
+constexpr int kSWarps = kSThreads / 32;
+constexpr int kNone = 0x7fffffff;
+constexpr unsigned kAll = 0xffffffffu;
+// Vertices with more nets than this are "heavy": they get a round of their own
+// in which every warp of the grid tallies a slice of their nets.
+constexpr int kHeavyDeg = 256;
+
+// Global nanosecond timer (per-phase time statistics).
+__device__ __forceinline__ unsigned long long gtimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Loads of state that other SMs write (L2, not the SM's L1).
+template <class T>
+__device__ __forceinline__ T lds(const T* p) { return __ldcg(p); }
+
+// Grid-wide barrier of a co-resident (cooperatively launched) grid with a
+// bounded wait.  bar[0] = arrivals, bar[1] = generation, bar[2] = abort flag.
+// Returns false in every thread of the CTA if the wait gave up (another CTA
+// stopped arriving) or another CTA aborted; the kernel then reports
+// FP_ERR_DEVICE_TIMEOUT through `status` and returns.
+constexpr unsigned kBarrierSpins = 1u << 24;   // with 64 ns naps: about a second or more
+
+__device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ bool grid_barrier(unsigned* bar, int* status) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    __threadfence();
+    const unsigned gen = ld_acquire(&bar[1]);
+    const unsigned arrived = atomicAdd(&bar[0], 1u);
+    if (arrived == gridDim.x - 1) {
+      atomicExch(&bar[0], 0u);
+      __threadfence();
+      atomicAdd(&bar[1], 1u);
+    } else {
+      unsigned spins = 0;
+      while (ld_acquire(&bar[1]) == gen) {
+        if (ld_acquire(&bar[2]) != 0u || ++spins > kBarrierSpins) {
+          ok = 0;
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    if (ld_acquire(&bar[2]) != 0u) ok = 0;
+    if (!ok) {
+      atomicExch(&bar[2], 1u);
+      atomicCAS(status, 0, -4);   // FP_ERR_DEVICE_TIMEOUT
+    }
+    __threadfence();
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+__device__ __forceinline__ int warp_sum(int x) {
+  for (int off = 16; off; off >>= 1) x += __shfl_xor_sync(kAll, x, off);
+  return x;
+}
+__device__ __forceinline__ int warp_min(int x) {
+  for (int off = 16; off; off >>= 1) x = min(x, __shfl_xor_sync(kAll, x, off));
+  return x;
+}
+__device__ __forceinline__ int warp_max(int x) {
+  for (int off = 16; off; off >>= 1) x = max(x, __shfl_xor_sync(kAll, x, off));
+  return x;
+}
+__device__ __forceinline__ long long warp_sum64(long long x) {
+  for (int off = 16; off; off >>= 1) x += __shfl_xor_sync(kAll, x, off);
+  return x;
+}
+
+__device__ __forceinline__ LdgKey warp_ldg_argmax(LdgKey k) {
+  for (int off = 16; off; off >>= 1) {
+    LdgKey o = shfl_key(k, off);
+    if (ldg_better(o, k)) k = o;
+  }
+  return k;
+}
+
+struct Carve {
+  unsigned char* p;
+  template <class T>
+  __device__ T* take(size_t n) {
+    T* r = reinterpret_cast<T*>(p);
+    p += (n * sizeof(T) + 15) & ~size_t(15);
+    return r;
+  }
+};
+
+// Adds to the warp's part tally the nets [nb, nb + 32) of a vertex (base: its
+// offset in vnets, deg: its net count): for every listed part, the number of
+// nets listing it (cnt) and the (net index, slot) of its first sighting (first);
+// returns this lane's count of nets where `own` has exactly one pin.  Slots of
+// the 32 nets are flattened across the warp (inclusive scan of list lengths).
+__device__ __forceinline__ int tally_batch(const DevInstance& I, int own, uint32_t base, int nb, int deg, int* cnt,
+                                           unsigned long long* first) {
+  const int lane = threadIdx.x & 31;
+  const int K = I.K;
+  const int k = nb + lane;
+  int s = 0, n = 0;
+  if (k < deg) {
+    const int e = (int)__ldg(&I.vnets[base + k]);
+    s = (int)__ldg(&I.nptr[e]);
+    const int cap = (int)__ldg(&I.nptr[e + 1]) - s;
+    n = lds(&I.ep_len[e]);
+    if (n < 0 || n > cap) { dev_fail(I.status, kDevErrInvalid); n = 0; }
+  }
+  int incl = n;
+  for (int off = 1; off < 32; off <<= 1) {
+    const int t = __shfl_up_sync(kAll, incl, off);
+    if (lane >= off) incl += t;
+  }
+  const int total = __shfl_sync(kAll, incl, 31);
+  int c1 = 0;
+  // kU slots per lane per step: the loads of one step are independent, which
+  // keeps kU requests per lane in flight (the walk is latency-bound otherwise).
+  constexpr int kU = 4;
+  for (int f0 = 0; f0 < total; f0 += 32 * kU) {
+    int aa[kU], key_net[kU], key_slot[kU], pp[kU];
+#pragma unroll
+    for (int u = 0; u < kU; u++) {
+      const int f = f0 + u * 32 + lane;
+      int lo = 0, hi = 31;
+#pragma unroll
+      for (int it = 0; it < 5; it++) {
+        const int mid = (lo + hi) >> 1;
+        const int val = __shfl_sync(kAll, incl, mid);
+        if (f < val) hi = mid; else lo = mid + 1;
+      }
+      const int sl = __shfl_sync(kAll, s, lo);
+      const int nl = __shfl_sync(kAll, n, lo);
+      const int il = __shfl_sync(kAll, incl, lo);
+      const int j = f - (il - nl);              // slot within net nb + lo
+      key_net[u] = nb + lo;
+      key_slot[u] = j;
+      aa[u] = f < total ? sl + j : -1;          // slot address, -1 past the end
+    }
+#pragma unroll
+    for (int u = 0; u < kU; u++) pp[u] = aa[u] >= 0 ? lds(&I.ep_part[aa[u]]) : -1;
+#pragma unroll
+    for (int u = 0; u < kU; u++) {
+      if (aa[u] < 0) continue;
+      const int p = pp[u];
+      if ((unsigned)p >= (unsigned)K) {
+        dev_fail(I.status, kDevErrInvalid);
+        continue;
+      }
+      atomicAdd(&cnt[p], 1);
+      atomicMin(&first[p], ((unsigned long long)key_net[u] << 32) | (unsigned)key_slot[u]);
+      if (p == own && lds(&I.ep_cnt[aa[u]]) == 1) c1++;
+    }
+  }
+  return c1;
+}
+
+// Volume arrays updated while a vertex moves (MSV: send only; MSRV: both).
+struct Vol {
+  int* send;
+  int* recv;
+};
+
+// One thread applies vertex v's move own -> d to net e: the reference's
+// REMOVAL (decrement, swap-with-last when the count reaches zero) then ADDING
+// (increment or append), TV/partition.cpp:388-436, with the send / received
+// volume bookkeeping of MGV/partition.cpp:376-449 and MSRV/partition.cpp:387-483.
+__device__ __forceinline__ void commit_net(const DevInstance& I, int v, int own, int d, int e, const Vol* vol) {
+  const int s = (int)__ldg(&I.nptr[e]);
+  const int cap = (int)__ldg(&I.nptr[e + 1]) - s;
+  int n = lds(&I.ep_len[e]);
+  int jo = -1, jd = -1;
+  for (int j = 0; j < n && (jo < 0 || jd < 0); j++) {
+    const int p = lds(&I.ep_part[s + j]);
+    if (p == own) jo = j;
+    if (p == d) jd = j;
+  }
+  if (jo < 0 || n > cap || (jd < 0 && n == cap && lds(&I.ep_cnt[s + jo]) > 1)) {
+    dev_fail(I.status, kDevErrInvalid);
+    return;
+  }
+  const int sv = vol ? __ldg(&I.src[e]) : -1;
+  const int sp = (vol && sv != v) ? lds(&I.part_vec[sv]) : d;
+  if (vol && sv == v) atomicAdd(&vol->send[own], -(n - 1));
+  // Counts change atomically: movers committed in the same round may share a net
+  // on which they only shift counts (their part sets are disjoint there).
+  const int co = atomicAdd(&I.ep_cnt[s + jo], -1) - 1;
+  if (co == 0) {
+    const int last = n - 1;
+    I.ep_part[s + jo] = lds(&I.ep_part[s + last]);
+    I.ep_cnt[s + jo] = lds(&I.ep_cnt[s + last]);
+    I.ep_part[s + last] = -1;
+    I.ep_cnt[s + last] = 0;
+    if (jd == last) jd = jo;
+    n = last;
+    if (vol && sv != v) {
+      atomicAdd(&vol->send[sp], -1);
+      if (vol->recv) atomicAdd(&vol->recv[own], -1);
+    }
+  } else {
+    if (vol && vol->recv && sv == v) atomicAdd(&vol->recv[own], 1);
+  }
+  if (vol && sv == v) atomicAdd(&vol->send[d], n - 1);
+  if (jd >= 0) {
+    atomicAdd(&I.ep_cnt[s + jd], 1);
+    if (vol && vol->recv && sv == v) atomicAdd(&vol->recv[d], -1);
+  } else {
+    I.ep_part[s + n] = d;
+    I.ep_cnt[s + n] = 1;
+    n++;
+    if (vol) {
+      atomicAdd(&vol->send[sp], 1);
+      if (vol->recv && sv != v) atomicAdd(&vol->recv[d], 1);
+    }
+  }
+  I.ep_len[e] = n;
+}
+
+// Least-loaded part (lowest index on ties) and the second smallest size, for
+// the LDG fallback (TV/partition.cpp:118-132) and its drift margin.
+__device__ __forceinline__ void block_min_part(const int* sizes, int K, unsigned long long* scr, int* minpart,
+                                               int* minsize, int* second) {
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  unsigned long long mk = ~0ull;
+  for (int p = threadIdx.x; p < K; p += blockDim.x) {
+    const unsigned long long key = ((unsigned long long)((unsigned)sizes[p] ^ 0x80000000u) << 32) | (unsigned)p;
+    mk = key < mk ? key : mk;
+  }
+  for (int off = 16; off; off >>= 1) {
+    const unsigned long long o = __shfl_xor_sync(kAll, mk, off);
+    mk = o < mk ? o : mk;
+  }
+  __syncthreads();
+  if (lane == 0) scr[wib] = mk;
+  __syncthreads();
+  mk = scr[0];
+  for (int x = 1; x < (int)(blockDim.x >> 5); x++) mk = scr[x] < mk ? scr[x] : mk;
+  const int mp = (int)(mk & 0xffffffffu);
+  int s2 = 0x7fffffff;
+  for (int p = threadIdx.x; p < K; p += blockDim.x)
+    if (p != mp) s2 = min(s2, sizes[p]);
+  s2 = warp_min(s2);
+  __syncthreads();
+  if (lane == 0) scr[wib] = (unsigned long long)(unsigned)s2;
+  __syncthreads();
+  int m2 = 0x7fffffff;
+  for (int x = 0; x < (int)(blockDim.x >> 5); x++) m2 = min(m2, (int)(unsigned)scr[x]);
+  __syncthreads();
+  *minpart = mp;
+  *minsize = sizes[mp];
+  *second = m2;
+}
+
+}  // namespace spec
+}  // namespace fp

@@ -116,6 +116,13 @@ int fp_reset_state(fp_instance* inst);
  * after the work is enqueued and its status has been read back. */
 int fp_refine(fp_instance* inst, int32_t passes);
 
+/* Refinement engine used by fp_refine: FP_ENGINE_AUTO (the speculative
+ * grid-wide engine where the metric has one, else the single-CTA walk) or
+ * FP_ENGINE_SEQUENTIAL (the single-CTA walk).  Both give identical results. */
+#define FP_ENGINE_AUTO       0
+#define FP_ENGINE_SEQUENTIAL 1
+int fp_set_engine(fp_instance* inst, int32_t engine);
+
 /* All six metrics of the current device state, in FP_OUT_* order
  * (shared/metric.cpp: TV_Refined, CN, TM_scratch, MGM_scratch, MGV_Scratch,
  * MGAV_Scratch). */
@@ -128,6 +135,13 @@ int fp_get_lists(fp_instance* inst, int32_t* ep_len /* noe */, int32_t* ep_part 
 int fp_get_part_sizes(fp_instance* inst, int32_t* sizes /* K */);
 /* Accepted moves of each of the last refine call's passes (up to n values). */
 int fp_get_moves(fp_instance* inst, int64_t* moves, int32_t n);
+/* Statistics of the last fp_refine on the grid-wide engine (up to 32 values):
+ * [0] windows, [1] single-vertex rounds of high-degree vertices, [2] moves
+ * committed from windows, [3..8] windows ended by: nothing (fully valid), a
+ * possibly stale TV marker, part-size drift, volume drift, a max-volume part
+ * changing, a shared net; [9] vertices walked in windows; [16..19] nanoseconds
+ * in evaluate, validate, commit phases and single-vertex rounds. */
+int fp_get_stats(fp_instance* inst, int64_t* out, int32_t n);
 /* Number of kernel launches the last fp_refine / fp_metrics call enqueued. */
 int fp_last_launches(fp_instance* inst, int64_t* launches);
 

@@ -146,3 +146,34 @@ def test_gpu_state_invariants_large(fp, orc, gpu_engine):
         want = {"TV": tv, "CN": cn, "TM": int(pairs.size), "MSM": int(msgs.max()), "MSV": int(send.max()),
                 "MSRV": int((send + recv).max())}
         assert g["metrics_final"] == want, metric
+
+
+ENGINE_CASES = [
+    ("colnet_8k_K8", lambda fp: fp.GenSpec.column_net(8192, 8192, 2, 16, seed=41), 8, 5),
+    ("zipf_20k_K256", lambda fp: fp.GenSpec.zipf(20000, 20000, 2.1, 2, 5000, beta=1.5, weight_rule=1, seed=42), 256, 3),
+    ("colnet_2k_K2", lambda fp: fp.GenSpec.column_net(2048, 2048, 2, 6, seed=43), 2, 6),
+]
+
+
+@pytest.mark.parametrize("name,mk,K,passes", ENGINE_CASES, ids=[c[0] for c in ENGINE_CASES])
+@pytest.mark.parametrize("metric", METRICS)
+def test_engines_agree(fp, orc, gpu_engine, name, mk, K, passes, metric):
+    """The speculative grid-wide engine and the single-CTA walk give the same
+    state, and both equal the oracle."""
+    hg = fp.generate(mk(fp))
+    res = {}
+    for engine in ("auto", "sequential"):
+        with gpu_engine.instance(hg, K, metric) as inst:
+            inst.set_engine(engine)
+            inst.initial_partition()
+            inst.refine(passes)
+            res[engine] = (inst.partition(), inst.lists(), inst.metrics(), inst.moves(passes))
+    a, b = res["auto"], res["sequential"]
+    np.testing.assert_array_equal(a[0], b[0])
+    for x, y in zip(a[1], b[1]):
+        np.testing.assert_array_equal(x, y)
+    assert a[2] == b[2]
+    np.testing.assert_array_equal(a[3], b[3])
+    o = orc.run_oracle(hg, K, metric, passes)
+    np.testing.assert_array_equal(a[0], o["part_vec"])
+    assert a[2] == o["metrics_final"]
