@@ -135,8 +135,8 @@ def algorithmic_bytes(metric, hg, ep_len, moved_mask, K):
     if moved_mask is not None and moved_mask.any():
         vv = np.nonzero(moved_mask)[0]
         net_lam = lam[hg.vnets.astype(np.int64)]
-        per_v = np.add.reduceat(net_lam, hg.vptr[:-1].astype(np.int64)) if P else np.zeros(hg.nov, np.int64)
-        per_v[deg == 0] = 0
+        cs = np.concatenate([np.zeros(1, np.int64), np.cumsum(net_lam)])
+        per_v = cs[hg.vptr[1:].astype(np.int64)] - cs[hg.vptr[:-1].astype(np.int64)]
         b += 16 * int(per_v[vv].sum())
     if metric != "TV":
         b += 8 * P + 4 * scanned + 4 * K

@@ -19,11 +19,16 @@ cudaError_t launch_refine(const DevInstance& I, int passes, cudaStream_t st);
 size_t metrics_scratch_bytes(int K);
 cudaError_t launch_spec_ldg(const DevInstance& I, const SpecBuf& B, int passes, int num_sms, cudaStream_t st,
                             int* grid_out);
+cudaError_t launch_spec_msg(const DevInstance& I, const SpecBuf& B, int passes, int num_sms, cudaStream_t st,
+                            int* grid_out);
+cudaError_t launch_spec_cn(const DevInstance& I, const SpecBuf& B, int passes, int num_sms, cudaStream_t st,
+                           int* grid_out);
 // Metrics the speculative grid-wide engine covers.
 static bool spec_supported(int metric) {
-  return metric == FP_METRIC_TV || metric == FP_METRIC_MSV || metric == FP_METRIC_MSRV;
+  return metric >= FP_METRIC_CN && metric <= FP_METRIC_MSRV;
 }
-constexpr int kHeavyDegHost = 256;   // must equal spec::kHeavyDeg (fp_spec_common.cuh)
+constexpr int kHeavyDegHost = 256;     // must equal spec::kHeavyDeg (fp_spec_common.cuh)
+constexpr int kSuperDegHost = 16384;   // must equal spec::kSuperDeg
 constexpr int kMaxSpecWarps = 16384;
 cudaError_t launch_metrics(const DevInstance& I, void* scratch, long long* out, int num_sms, cudaStream_t st,
                            int* launches);
@@ -56,8 +61,12 @@ struct fp_instance {
   int engine = FP_ENGINE_AUTO;
   SpecBuf sb{};
   int last_grid = 0;
-  std::vector<int> heavy_pos;     // host copy
+  std::vector<int> heavy_pos;     // whole-grid-round vertices, by position in visiting order
   int* heavy_pos_d = nullptr;
+  std::vector<int> mid_pos;       // CTA-evaluated vertices, by position
+  int* mid_pos_d = nullptr;
+  std::vector<int> heavy_ids;     // heavy vertices by id (TM / MSM walk ids)
+  int* heavy_ids_d = nullptr;
 };
 
 namespace {
@@ -232,6 +241,23 @@ int fp_ctx_set_stream(fp_ctx* ctx, void* stream) {
   return FP_OK;
 }
 
+// Claims (no claim: a value above every position) and both heavy-round
+// buffers start clear for every speculative launch: a launch leaves the buffer
+// of its last heavy round, and an aborted launch its claims, behind.
+static cudaError_t clear_spec_scratch(const SpecBuf& b, int noe, int K, cudaStream_t s) {
+  const size_t ne = (size_t)std::max(noe, 1);
+  cudaError_t e = cudaMemsetAsync(b.claim_m, 0x7f, sizeof(int) * ne, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(b.claim_c, 0x7f, sizeof(int) * ne, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(b.mask_c, 0, sizeof(uint32_t) * ne, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(b.hcnt, 0, sizeof(int) * 2 * K, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(b.hfirst, 0xff, sizeof(unsigned long long) * 2 * K, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(b.hgain, 0, sizeof(int) * 2 * K, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(b.hloss, 0, sizeof(int) * 2 * K, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(b.hadelta, 0, sizeof(int) * 2 * K, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(b.hmisc, 0, sizeof(int) * 16, s);
+  return e;
+}
+
 int fp_instance_create(fp_ctx* ctx, const fp_hypergraph* h, int32_t K, int32_t metric, double eps_factor,
                        fp_instance** out) {
   if (!ctx || !out || metric < 0 || metric > 5 || K < 2 || K > kMaxK || !(eps_factor > 0)) return FP_ERR_INVALID;
@@ -277,11 +303,18 @@ int fp_instance_create(fp_ctx* ctx, const fp_hypergraph* h, int32_t K, int32_t m
   d.min_pw = (int)(pb.xw - (pb.xw * 0.1));
   // Heavy vertices (more than kHeavyDegHost nets), by position in visiting order.
   in->heavy_pos.clear();
+  in->mid_pos.clear();
   for (int z = 0; z < g.nov; z++) {
     const int v = pb.order[z];
-    if ((int)(g.vptr[v + 1] - g.vptr[v]) > kHeavyDegHost) in->heavy_pos.push_back(z);
+    const int dv = (int)(g.vptr[v + 1] - g.vptr[v]);
+    if (dv > kSuperDegHost) in->heavy_pos.push_back(z);
+    else if (dv > kHeavyDegHost) in->mid_pos.push_back(z);
   }
   const int nheavy = (int)in->heavy_pos.size();
+  const int nmid = (int)in->mid_pos.size();
+  in->heavy_ids.clear();
+  for (int v = 0; v < g.nov; v++)
+    if ((int)(g.vptr[v + 1] - g.vptr[v]) > kHeavyDegHost) in->heavy_ids.push_back(v);
   const size_t KK = (size_t)K * K, words = (size_t)(K + 31) / 32;
   const bool msg = metric == FP_METRIC_TM || metric == FP_METRIC_MSM;
   uint32_t *vptr, *vnets, *nptr, *npins;
@@ -302,11 +335,13 @@ int fp_instance_create(fp_ctx* ctx, const fp_hypergraph* h, int32_t K, int32_t m
       (rc = dalloc(in, &in->sb.cand, (size_t)kSpecWindow * K)) || (rc = dalloc(in, &in->sb.ncand, kSpecWindow)) ||
       (rc = dalloc(in, &in->sb.pref, (size_t)kSpecWindow * K)) ||
       (rc = dalloc(in, &in->sb.wsum, kMaxSpecWarps)) || (rc = dalloc(in, &in->sb.vsum, kMaxSpecWarps)) ||
-      (rc = dalloc(in, &in->sb.claim_m, g.noe)) || (rc = dalloc(in, &in->sb.claim_c, g.noe)) ||
+      (rc = dalloc(in, &in->sb.claim_m, g.noe)) || (rc = dalloc(in, &in->sb.claim64, g.noe)) || (rc = dalloc(in, &in->sb.claim_c, g.noe)) ||
       (rc = dalloc(in, &in->sb.mask_c, g.noe)) || (rc = dalloc(in, &in->sb.hcnt, 2 * K)) ||
       (rc = dalloc(in, &in->sb.hfirst, 2 * K)) || (rc = dalloc(in, &in->sb.hgain, 2 * K)) ||
       (rc = dalloc(in, &in->sb.hloss, 2 * K)) || (rc = dalloc(in, &in->sb.hadelta, 2 * K)) ||
       (rc = dalloc(in, &in->sb.hmisc, 16)) || (rc = dalloc(in, &in->heavy_pos_d, std::max(nheavy, 1))) ||
+      (rc = dalloc(in, &in->heavy_ids_d, std::max(nheavy + nmid, 1))) ||
+      (rc = dalloc(in, &in->mid_pos_d, std::max(nmid, 1))) ||
       (rc = dalloc(in, &in->metric_out, 8))) {
     fp_instance_destroy(in);
     return rc;
@@ -320,19 +355,18 @@ int fp_instance_create(fp_ctx* ctx, const fp_hypergraph* h, int32_t K, int32_t m
   in->sb.max_warps = kMaxSpecWarps;
   in->sb.heavy_pos = in->heavy_pos_d;
   in->sb.nheavy = nheavy;
+  in->sb.mid_pos = in->mid_pos_d;
+  in->sb.nmid = nmid;
   {
     cudaStream_t s0 = ctx->stream;
-    e = cudaMemsetAsync(in->sb.claim_m, 0x7f, sizeof(int) * std::max(g.noe, 1), s0);
-    if (e == cudaSuccess) e = cudaMemsetAsync(in->sb.claim_c, 0x7f, sizeof(int) * std::max(g.noe, 1), s0);
-    if (e == cudaSuccess) e = cudaMemsetAsync(in->sb.mask_c, 0, sizeof(uint32_t) * std::max(g.noe, 1), s0);
-    if (e == cudaSuccess) e = cudaMemsetAsync(in->sb.hcnt, 0, sizeof(int) * 2 * K, s0);
-    if (e == cudaSuccess) e = cudaMemsetAsync(in->sb.hfirst, 0xff, sizeof(unsigned long long) * 2 * K, s0);
-    if (e == cudaSuccess) e = cudaMemsetAsync(in->sb.hgain, 0, sizeof(int) * 2 * K, s0);
-    if (e == cudaSuccess) e = cudaMemsetAsync(in->sb.hloss, 0, sizeof(int) * 2 * K, s0);
-    if (e == cudaSuccess) e = cudaMemsetAsync(in->sb.hadelta, 0, sizeof(int) * 2 * K, s0);
-    if (e == cudaSuccess) e = cudaMemsetAsync(in->sb.hmisc, 0, sizeof(int) * 16, s0);
+    e = clear_spec_scratch(in->sb, g.noe, K, s0);
     if (e == cudaSuccess && nheavy)
       e = cudaMemcpyAsync(in->heavy_pos_d, in->heavy_pos.data(), sizeof(int) * nheavy, cudaMemcpyHostToDevice, s0);
+    if (e == cudaSuccess && !in->heavy_ids.empty())
+      e = cudaMemcpyAsync(in->heavy_ids_d, in->heavy_ids.data(), sizeof(int) * in->heavy_ids.size(),
+                          cudaMemcpyHostToDevice, s0);
+    if (e == cudaSuccess && nmid)
+      e = cudaMemcpyAsync(in->mid_pos_d, in->mid_pos.data(), sizeof(int) * nmid, cudaMemcpyHostToDevice, s0);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s0);
     if (e != cudaSuccess) { fp_instance_destroy(in); return cuda_status(e); }
   }
@@ -402,7 +436,21 @@ int fp_refine(fp_instance* in, int32_t passes) {
     if (e == cudaSuccess) e = cudaMemcpyAsync(in->sb.ctl, none, sizeof(none), cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(in->sb.bar, 0, sizeof(unsigned) * 4, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(in->sb.stats, 0, sizeof(unsigned long long) * 32, s);
-    if (e == cudaSuccess) e = launch_spec_ldg(in->d, in->sb, passes, in->ctx->num_sms, s, &in->last_grid);
+    if (e == cudaSuccess) e = clear_spec_scratch(in->sb, in->g.noe, in->pb.K, s);
+    if (e == cudaSuccess) {
+      if (in->pb.metric == FP_METRIC_CN) {
+        e = cudaMemsetAsync(in->sb.claim64, 0, sizeof(unsigned long long) * std::max(in->g.noe, 1), s);
+        if (e == cudaSuccess) e = launch_spec_cn(in->d, in->sb, passes, in->ctx->num_sms, s, &in->last_grid);
+      } else if (in->pb.metric == FP_METRIC_TM || in->pb.metric == FP_METRIC_MSM) {
+        SpecBuf b = in->sb;
+        b.heavy_pos = in->heavy_ids_d;
+        b.nheavy = (int)in->heavy_ids.size();
+        b.nmid = 0;
+        e = launch_spec_msg(in->d, b, passes, in->ctx->num_sms, s, &in->last_grid);
+      } else {
+        e = launch_spec_ldg(in->d, in->sb, passes, in->ctx->num_sms, s, &in->last_grid);
+      }
+    }
   } else if (e == cudaSuccess) {
     e = launch_refine(in->d, passes, s);
   }

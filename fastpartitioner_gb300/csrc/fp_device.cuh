@@ -64,11 +64,14 @@ struct SpecBuf {
   int* pref;             // [K * wmax] per-part prefix of the window's size changes
   int* wsum;             // [max_warps] per-warp sums of wt
   int* vsum;             // [max_warps] per-warp sums of vd
+  unsigned long long* claim64;  // [noe] (round << 32) | ~position of the first claim (CN)
   int* claim_m;          // [noe] first mover position changing the net's part set
   int* claim_c;          // [noe] first mover position changing only counts
   uint32_t* mask_c;      // [noe] parts (mod 32) whose counts those movers change
-  const int* heavy_pos;  // positions (in visiting order) of heavy vertices, ascending
-  int nheavy;
+  const int* heavy_pos;  // positions (visiting order, ascending) of vertices that get a
+  int nheavy;            //     whole-grid round of their own
+  const int* mid_pos;    // positions (ascending) of medium vertices, evaluated by one CTA
+  int nmid;
   int* hcnt;             // [2*K] heavy-vertex tally (double-buffered)
   unsigned long long* hfirst;  // [2*K]
   int* hgain;            // [2*K]
@@ -120,6 +123,7 @@ __device__ __forceinline__ LdgKey shfl_key(const LdgKey& k, int off) {
 }
 
 // Block-wide LDG argmax; every thread gets the winner (part = -1 if none).
+// scratch holds one entry per warp of the launched block.
 __device__ __forceinline__ LdgKey block_ldg_argmax(LdgKey k, LdgKey* scratch) {
   for (int off = 16; off; off >>= 1) {
     LdgKey o = shfl_key(k, off);
@@ -130,7 +134,7 @@ __device__ __forceinline__ LdgKey block_ldg_argmax(LdgKey k, LdgKey* scratch) {
   if (lane == 0) scratch[warp] = k;
   __syncthreads();
   if (warp == 0) {
-    k = lane < kWarps ? scratch[lane] : LdgKey{-1.0, 0, -1, ~0ull};
+    k = lane < (int)(blockDim.x >> 5) ? scratch[lane] : LdgKey{-1.0, 0, -1, ~0ull};
     for (int off = 16; off; off >>= 1) {
       LdgKey o = shfl_key(k, off);
       if (ldg_better(o, k)) k = o;
@@ -143,7 +147,7 @@ __device__ __forceinline__ LdgKey block_ldg_argmax(LdgKey k, LdgKey* scratch) {
   return k;
 }
 
-// Block-wide minimum of a 64-bit key.
+// Block-wide minimum of a 64-bit key (scratch: one entry per warp of the block).
 __device__ __forceinline__ unsigned long long block_min_u64(unsigned long long x, unsigned long long* scratch) {
   for (int off = 16; off; off >>= 1) {
     unsigned long long o = __shfl_xor_sync(0xffffffffu, x, off);
@@ -154,7 +158,7 @@ __device__ __forceinline__ unsigned long long block_min_u64(unsigned long long x
   if (lane == 0) scratch[warp] = x;
   __syncthreads();
   if (warp == 0) {
-    x = lane < kWarps ? scratch[lane] : ~0ull;
+    x = lane < (int)(blockDim.x >> 5) ? scratch[lane] : ~0ull;
     for (int off = 16; off; off >>= 1) {
       unsigned long long o = __shfl_xor_sync(0xffffffffu, x, off);
       x = o < x ? o : x;

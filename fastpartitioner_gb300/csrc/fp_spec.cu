@@ -266,12 +266,234 @@ __device__ __forceinline__ void accept_final(bool failM, bool failN, int fsl, in
   *vslack = *good ? msl : (failM ? kBig : fsl);
 }
 
+// First index of the ascending list `pos_list` (n entries) with value >= x.
+__device__ __forceinline__ int lower_bound_pos(const int* pos_list, int n, int x) {
+  int lo = 0, hi = n;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (__ldg(&pos_list[mid]) < x) lo = mid + 1; else hi = mid;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ int block_reduce_max(int x, int* scr) {
+  x = warp_max(x);
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) scr[threadIdx.x >> 5] = x;
+  __syncthreads();
+  int r = scr[0];
+  for (int i = 1; i < (int)(blockDim.x >> 5); i++) r = max(r, scr[i]);
+  __syncthreads();
+  return r;
+}
+__device__ __forceinline__ int block_reduce_min(int x, int* scr) {
+  return -block_reduce_max(-x, scr);
+}
+
+// Evaluation of a medium vertex (more than kHeavyDeg nets) at position z by the
+// whole CTA: the warps split the tally, warp 0 decides, the threads split the
+// per-net pass.  Writes the same per-position record as a warp evaluation
+// (flag bit 2 marks it); a medium mover claims all its nets as part-set changes.
+__device__ void cta_eval_ldg(const DevInstance& I, const SpecBuf& B, const RoundCtx& R, int metric, int z, int pos,
+                             int par, int q, int* cnt_b, unsigned long long* first_b, int* gains_b, int* losses_b,
+                             int* adelta_b, int* iscr, int* s_mw, int* s_mv) {
+  __shared__ int sh[4];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const int K = I.K;
+  const int words = (K + 31) >> 5;
+  const bool rv = metric == kMSRV;
+  const int o = z - pos;
+  const int v = __ldg(&I.order[z]);
+  const int own = lds(&I.part_vec[v]);
+  const uint32_t base = __ldg(&I.vptr[v]);
+  const int deg = (int)(__ldg(&I.vptr[v + 1]) - base);
+  int* cnt = cnt_b + (size_t)wib * K;
+  unsigned long long* first = first_b + (size_t)wib * K;
+  for (int p = lane; p < K; p += 32) { cnt[p] = 0; first[p] = ~0ull; }
+  __syncwarp();
+  int c1 = 0;
+  for (int nb = wib * 32; nb < deg; nb += kSWarps * 32) c1 += tally_batch(I, own, base, nb, deg, cnt, first);
+  c1 = warp_sum(c1);
+  __syncthreads();
+  if (lane == 0) iscr[wib] = c1;
+  for (int p = threadIdx.x; p < K; p += blockDim.x) {
+    int c = 0;
+    unsigned long long f = ~0ull;
+    for (int x = 0; x < kSWarps; x++) {
+      c += cnt_b[(size_t)x * K + p];
+      const unsigned long long fx = first_b[(size_t)x * K + p];
+      f = fx < f ? fx : f;
+    }
+    cnt_b[p] = c;
+    first_b[p] = f;
+  }
+  __syncthreads();
+  int c1t = 0;
+  for (int x = 0; x < kSWarps; x++) c1t += iscr[x];
+  if (wib == 0) {
+    bool special;
+    int slack;
+    const int d = ldg_decide(I, R, cnt_b, first_b, metric, v, own, z == pos, &special, &slack);
+    unsigned long long* cl = B.cand + (size_t)o * K;
+    int nc = 0;
+    for (int p0 = 0; p0 < K; p0 += 32) {
+      const int p = p0 + lane;
+      bool ok = false;
+      unsigned long long ent = 0;
+      if (p < K) {
+        const int c = cnt_b[p];
+        if (c > 0 && !(metric == kTV && R.marker[p] == v)) {
+          ok = true;
+          const unsigned long long f = first_b[p];
+          ent = ((unsigned long long)p << 52) | ((unsigned long long)(c - (p == own ? 1 : 0)) << 36) |
+                (((f >> 32) & 0xffffull) << 20) | (f & 0xfffffull);
+        }
+      }
+      const unsigned m = __ballot_sync(kAll, ok);
+      if (ok) cl[nc + __popc(m & ((1u << lane) - 1u))] = ent;
+      nc += __popc(m);
+    }
+    if (metric == kTV) {
+      for (int wd = 0; wd < words; wd++) {
+        const int p = wd * 32 + lane;
+        const unsigned m = __ballot_sync(kAll, p < K && cnt_b[p] > 0);
+        if (lane == 0) B.scan[(size_t)o * words + wd] = m;
+      }
+    }
+    if (lane == 0) {
+      B.ncand[o] = nc;
+      sh[0] = d;
+      sh[1] = special ? 1 : 0;
+      sh[2] = slack;
+    }
+  }
+  __syncthreads();
+  const int d = sh[0];
+  const bool special = sh[1] != 0;
+  const int slack = sh[2];
+  bool mover = false, mt = false;
+  int vs = kBig, vdd = 0;
+  if (d != own) {
+    if (metric == kTV) {
+      mover = c1t >= deg - cnt_b[d];
+    } else {
+      int* gains = gains_b + (size_t)wib * K;
+      int* losses = losses_b + (size_t)wib * K;
+      int* adelta = adelta_b + (size_t)wib * K;
+      for (int p = lane; p < K; p += 32) { gains[p] = 0; losses[p] = 0; adelta[p] = 0; }
+      __syncwarp();
+      net_pass(I, metric, v, own, d, base, deg, threadIdx.x, blockDim.x, nullptr, gains, losses, adelta);
+      __syncthreads();
+      for (int p = threadIdx.x; p < K; p += blockDim.x) {
+        int g = 0, l = 0, a = 0;
+        for (int x = 0; x < kSWarps; x++) {
+          g += gains_b[(size_t)x * K + p];
+          l += losses_b[(size_t)x * K + p];
+          a += adelta_b[(size_t)x * K + p];
+        }
+        gains_b[p] = g;
+        losses_b[p] = l;
+        adelta_b[p] = a;
+      }
+      __syncthreads();
+      const AcceptPart a = accept_partial(R, gains_b, losses_b, adelta_b, K, rv, threadIdx.x, blockDim.x);
+      const bool fM = __syncthreads_or(a.failM);
+      const bool fN = __syncthreads_or(a.failN);
+      const bool amt = __syncthreads_or(a.mt);
+      const int fsl = block_reduce_max(a.fsl, iscr);
+      const int msl = block_reduce_min(a.msl, iscr);
+      vdd = block_reduce_max(a.vd, iscr);
+      bool good;
+      accept_final(fM, fN, fsl, msl, &good, &vs);
+      mover = good;
+      mt = mover && amt;
+    }
+  }
+  if (mover) {
+    for (int k = threadIdx.x; k < deg; k += blockDim.x) atomicMin(&B.claim_m[__ldg(&I.vnets[base + k])], z);
+    if (threadIdx.x == 0 && mt) atomicMin(&B.ctl[2 + par], z);
+  }
+  if (threadIdx.x == 0) {
+    const int wv = mover ? __ldg(&I.w[v]) : 0;
+    B.dec[o] = (own << 16) | d;
+    B.flag[o] = (unsigned char)((mover ? 1 : 0) | (special ? 2 : 0) | 4);
+    B.slack[o] = slack;
+    B.vslack[o] = vs;
+    B.wt[o] = wv;
+    B.vd[o] = mover ? vdd : 0;
+    const int owner = o / q - (int)blockIdx.x * kSWarps;   // warp of this CTA owning position z
+    s_mw[owner] += wv;
+    s_mv[owner] += mover ? vdd : 0;
+  }
+  __syncthreads();
+}
+
+// Validation of a medium vertex by the whole CTA (same rules as the warp
+// validation; a medium mover treats all its nets as part-set changes).
+__device__ void cta_validate_ldg(const DevInstance& I, const SpecBuf& B, const RoundCtx& R, int metric, int z, int pos,
+                                 int par, int q, int mtpos, long long pre_w, long long pre_v, int* iscr) {
+  __shared__ long long shd[2];
+  __shared__ int shw;
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const int o = z - pos;
+  const int fl = lds(&B.flag[o]);
+  const int pk = lds(&B.dec[o]);
+  const int own = pk >> 16, d = pk & 0xffff;
+  const int v = __ldg(&I.order[z]);
+  if (threadIdx.x == 0) {
+    const int owner = o / q;
+    long long D = pre_w, V = pre_v;
+    for (int x = (int)blockIdx.x * kSWarps; x < owner; x++) {
+      D += lds(&B.wsum[x]);
+      V += lds(&B.vsum[x]);
+    }
+    for (int o2 = owner * q; o2 < o; o2++) {
+      D += lds(&B.wt[o2]);
+      V += lds(&B.vd[o2]);
+    }
+    shd[0] = D;
+    shd[1] = V;
+    shw = ((fl & 2) && z != pos) ? 1 : 0;
+  }
+  __syncthreads();
+  const long long D = shd[0], V = shd[1];
+  const bool recheck = shw == 0 && D > max(lds(&B.slack[o]), 0);
+  __syncthreads();   // every thread has read shw before warp 0 may change it
+  if (recheck) {
+    if (wib == 0) {
+      const int d2 = ldg_recheck(I, R, B, o, v, own, metric);
+      if (lane == 0 && d2 != d) shw = 2;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0 && shw == 0) shw = V > max(lds(&B.vslack[o]), 0) ? 3 : mtpos < z ? 4 : 0;
+  __syncthreads();
+  int why = shw;
+  if (why == 0) {
+    const uint32_t base = __ldg(&I.vptr[v]);
+    const int deg = (int)(__ldg(&I.vptr[v + 1]) - base);
+    const unsigned ob = 1u << (own & 31);
+    const bool mover = fl & 1;
+    bool conf = false;
+    for (int k = threadIdx.x; k < deg; k += blockDim.x) {
+      const int e = (int)__ldg(&I.vnets[base + k]);
+      if (lds(&B.claim_m[e]) < z) conf = true;
+      if (lds(&B.claim_c[e]) < z && (mover || (lds(&B.mask_c[e]) & ob))) conf = true;
+    }
+    if (__syncthreads_or(conf)) why = 5;
+  }
+  if (why && threadIdx.x == 0) atomicMin(&B.ctl[par], (z << 3) | why);
+  __syncthreads();
+  (void)iscr;
+}
+
 __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, SpecBuf B, int passes) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ unsigned long long uscr[kSWarps];
   __shared__ int iscr[kSWarps];
   __shared__ int s_minpart, s_minsize, s_second, s_maxv, s_cc, s_count, s_d;
   __shared__ long long s_pre_w, s_pre_v;
+  __shared__ int s_mw[kSWarps], s_mv[kSWarps];
   const int metric = I.metric;
   const bool vol = metric != kTV;
   const bool rv = metric == kMSRV;
@@ -520,9 +742,10 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
       for (int z = z0; z < z1; z++) {
         const int o = z - pos;
         const int v = __ldg(&I.order[z]);
-        const int own = lds(&I.part_vec[v]);
         const uint32_t base = __ldg(&I.vptr[v]);
         const int deg = (int)(__ldg(&I.vptr[v + 1]) - base);
+        if (deg > kHeavyDeg) continue;   // medium vertex: evaluated by the whole CTA below
+        const int own = lds(&I.part_vec[v]);
         for (int p = lane; p < K; p += 32) { cnt[p] = 0; first[p] = ~0ull; }
         __syncwarp();
         int c1 = 0;
@@ -613,9 +836,20 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
         vsum += mover ? vdd : 0;
         __syncwarp();
       }
+      // medium vertices of this CTA's positions: the CTA evaluates them together
+      if (threadIdx.x < kSWarps) { s_mw[threadIdx.x] = 0; s_mv[threadIdx.x] = 0; }
+      __syncthreads();
+      const int cz0 = min(pos + blockIdx.x * kSWarps * q, end_w);
+      const int cz1 = min(cz0 + kSWarps * q, end_w);
+      for (int mi = lower_bound_pos(B.mid_pos, B.nmid, cz0); mi < B.nmid; mi++) {
+        const int z = __ldg(&B.mid_pos[mi]);
+        if (z >= cz1) break;
+        cta_eval_ldg(I, B, R, metric, z, pos, par, q, cnt_b, first_b, gains_b, losses_b, adelta_b, iscr, s_mw, s_mv);
+      }
+      __syncthreads();
       if (lane == 0) {
-        B.wsum[gw] = wsum;
-        B.vsum[gw] = vsum;
+        B.wsum[gw] = wsum + s_mw[wib];
+        B.vsum[gw] = vsum + s_mv[wib];
       }
       if (!grid_barrier(B.bar, I.status)) return;
       if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -684,6 +918,11 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
       for (int z = z0; z < z1; z++) {
         const int o = z - pos;
         const int fl = lds(&B.flag[o]);
+        if (fl & 4) {                    // medium vertex: validated by the CTA below
+          Dw += lds(&B.wt[o]);
+          Vw += lds(&B.vd[o]);
+          continue;
+        }
         int why = ((fl & 2) && z != pos) ? 1 : 0;
         if (!why && Dw > max(lds(&B.slack[o]), 0)) {
           // beyond the slack: decide again with the exact sizes at this position
@@ -721,6 +960,12 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
         Dw += lds(&B.wt[o]);
         Vw += lds(&B.vd[o]);
       }
+      __syncthreads();
+      for (int mi = lower_bound_pos(B.mid_pos, B.nmid, cz0); mi < B.nmid; mi++) {
+        const int z = __ldg(&B.mid_pos[mi]);
+        if (z >= cz1) break;
+        cta_validate_ldg(I, B, R, metric, z, pos, par, q, mtpos, s_pre_w, s_pre_v, iscr);
+      }
       if (!grid_barrier(B.bar, I.status)) return;
       // ---- C: commit every mover before the cut.
       const int cutw = lds(&B.ctl[par]);
@@ -741,7 +986,7 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
       for (int z = z0; z < z1; z++) {
         const int o = z - pos;
         const int fl = lds(&B.flag[o]);
-        if (!(fl & 1)) continue;
+        if (!(fl & 1) || (fl & 4)) continue;
         const int v = __ldg(&I.order[z]);
         const int pk = lds(&B.dec[o]);
         const int own = pk >> 16, d = pk & 0xffff;
@@ -759,6 +1004,36 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
           }
         }
         for (int k = lane; k < deg; k += 32) {
+          const int e = (int)__ldg(&I.vnets[base + k]);
+          B.claim_m[e] = kNone;
+          B.claim_c[e] = kNone;
+          B.mask_c[e] = 0;
+        }
+      }
+      for (int mi = lower_bound_pos(B.mid_pos, B.nmid, cz0); mi < B.nmid; mi++) {
+        const int z = __ldg(&B.mid_pos[mi]);
+        if (z >= cz1) break;
+        const int o = z - pos;
+        const int fl = lds(&B.flag[o]);
+        if (!(fl & 1)) continue;
+        const int v = __ldg(&I.order[z]);
+        const int pk = lds(&B.dec[o]);
+        const int own = pk >> 16, d = pk & 0xffff;
+        const uint32_t base = __ldg(&I.vptr[v]);
+        const int deg = (int)(__ldg(&I.vptr[v + 1]) - base);
+        if (z < cut) {
+          for (int k = threadIdx.x; k < deg; k += blockDim.x)
+            commit_net(I, v, own, d, (int)__ldg(&I.vnets[base + k]), vol ? &V : nullptr);
+          if (threadIdx.x == 0) {
+            atomicAdd(&B.stats[2], 1ull);
+            I.part_vec[v] = d;
+            const int wv = __ldg(&I.w[v]);
+            atomicAdd(&I.part_sizes[own], -wv);
+            atomicAdd(&I.part_sizes[d], wv);
+            atomicAdd((unsigned long long*)&I.moves[it], 1ull);
+          }
+        }
+        for (int k = threadIdx.x; k < deg; k += blockDim.x) {
           const int e = (int)__ldg(&I.vnets[base + k]);
           B.claim_m[e] = kNone;
           B.claim_c[e] = kNone;

@@ -17,6 +17,9 @@ constexpr unsigned kAll = 0xffffffffu;
 // Vertices with more nets than this are "heavy": they get a round of their own
 // in which every warp of the grid tallies a slice of their nets.
 constexpr int kHeavyDeg = 256;
+// Vertices with more nets than this get a whole-grid round (the LDG metrics;
+// those in between are evaluated inside a window by one CTA).
+constexpr int kSuperDeg = 16384;
 
 // Global nanosecond timer (per-phase time statistics).
 __device__ __forceinline__ unsigned long long gtimer() {

@@ -177,3 +177,49 @@ def test_engines_agree(fp, orc, gpu_engine, name, mk, K, passes, metric):
     o = orc.run_oracle(hg, K, metric, passes)
     np.testing.assert_array_equal(a[0], o["part_vec"])
     assert a[2] == o["metrics_final"]
+
+
+def heavy_hypergraph(fp):
+    """Vertex 0 in 20000 nets (a whole-grid round for every metric), vertices
+    1..6 in 300..4000 nets (CTA-evaluated for the LDG metrics, grid rounds for
+    TM / MSM), one net of 3000 pins, the rest light."""
+    rng = np.random.default_rng(77)
+    nov = 30000
+    nets = []
+    for i in range(20000):
+        nets.append([0] + rng.choice(np.arange(7, nov), size=int(rng.integers(1, 4)), replace=False).tolist())
+    for v, d in zip(range(1, 7), (300, 600, 1200, 2500, 4000, 257)):
+        for i in range(d):
+            nets.append([v] + rng.choice(np.arange(7, nov), size=int(rng.integers(1, 5)), replace=False).tolist())
+    nets.append(rng.choice(np.arange(7, nov), size=3000, replace=False).tolist())
+    for i in range(8000):
+        nets.append(rng.choice(np.arange(7, nov), size=int(rng.integers(2, 7)), replace=False).tolist())
+    order = rng.permutation(len(nets))
+    nets = [sorted(nets[i]) for i in order]
+    nptr = np.cumsum([0] + [len(n) for n in nets]).astype(np.uint32)
+    npins = np.concatenate([np.array(n, np.uint32) for n in nets])
+    return fp.Hypergraph.from_nets(nov, nptr, npins)
+
+
+@pytest.mark.parametrize("metric", METRICS)
+@pytest.mark.parametrize("K", [16, 64])
+def test_gpu_heavy_vertices_and_repeated_refine(fp, orc, gpu_engine, metric, K):
+    """High-degree vertices, passes split over two refine calls, and the same
+    instance refined again after reset_state: every result equals the oracle."""
+    hg = heavy_hypergraph(fp)
+    passes = 3
+    o = orc.run_oracle(hg, K, metric, passes)
+    assert o["status"] == 0
+    with gpu_engine.instance(hg, K, metric) as inst:
+        inst.initial_partition()
+        for attempt in range(2):
+            inst.refine(1)
+            inst.refine(passes - 1)
+            tag = f"{metric} K={K} attempt {attempt}"
+            np.testing.assert_array_equal(inst.partition(), o["part_vec"], err_msg=tag)
+            ln, pt, ct = inst.lists()
+            np.testing.assert_array_equal(ln, o["ep_len"], err_msg=tag)
+            np.testing.assert_array_equal(orc.flat_lists(hg, ln, pt), orc.flat_lists(hg, o["ep_len"], o["ep_part"]),
+                                          err_msg=tag)
+            assert inst.metrics() == o["metrics_final"], tag
+            inst.reset_state()
