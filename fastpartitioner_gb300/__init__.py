@@ -88,6 +88,12 @@ def library_path() -> Path:
     return _LIB_PATH
 
 
+class FpState(C.Structure):
+    """fp_state of include/fastpart.h: the reference's refinement arrays."""
+    _fields_ = [(n, C.c_void_p) for n in ("part_vec", "ep_starts", "ep_ends", "ep_parts", "ep_cnt", "part_sizes",
+                                          "marker", "send", "recv", "conn", "msgs")]
+
+
 def lib():
     """The loaded engine library (raises FastPartError-free OSError if absent)."""
     global _lib_handle
@@ -111,6 +117,8 @@ def lib():
             "fp_metrics": ([vp, vp], C.c_int),
             "fp_get_partition": ([vp, vp], C.c_int),
             "fp_get_lists": ([vp, vp, vp, vp], C.c_int),
+            "fp_set_state": ([vp, C.POINTER(FpState)], C.c_int),
+            "fp_get_state": ([vp, C.POINTER(FpState)], C.c_int),
             "fp_get_part_sizes": ([vp, vp], C.c_int),
             "fp_get_moves": ([vp, vp, i32], C.c_int),
             "fp_last_launches": ([vp, vp], C.c_int),
@@ -118,6 +126,7 @@ def lib():
             "fp_strerror": ([C.c_int], C.c_char_p),
             "fp_generate": ([C.POINTER(_GenParams), pp], C.c_int),
             "fp_graph_from_nets": ([i32, i32, vp, vp, vp, pp], C.c_int),
+            "fp_graph_from_vertices": ([i32, i32, vp, vp, vp, pp], C.c_int),
             "fp_read_patohlike": ([C.c_char_p, i32, i32, pp], C.c_int),
             "fp_write_patohlike": ([vp, C.c_char_p], C.c_int),
             "fp_graph_view": ([vp, C.POINTER(_Hypergraph)], C.c_int),
@@ -198,6 +207,18 @@ class Hypergraph:
         g = C.c_void_p()
         _check(lib().fp_graph_from_nets(nov, noe, _ptr(nptr), _ptr(npins), _ptr(s), C.byref(g)),
                "fp_graph_from_nets")
+        return _take_graph(g)
+
+    @staticmethod
+    def from_vertices(nov: int, noe: int, vptr, vnets, src=None) -> "Hypergraph":
+        """Builds net -> pins from vertex -> nets (the reference's createInverse,
+        shared/utils.cpp:32-56): the row_ptr / col_ind that partition() gets."""
+        vptr = np.ascontiguousarray(vptr, dtype=np.uint32)
+        vnets = np.ascontiguousarray(vnets, dtype=np.uint32)
+        s = None if src is None else np.ascontiguousarray(src, dtype=np.int32)
+        g = C.c_void_p()
+        _check(lib().fp_graph_from_vertices(nov, noe, _ptr(vptr), _ptr(vnets), _ptr(s), C.byref(g)),
+               "fp_graph_from_vertices")
         return _take_graph(g)
 
     def save_fphg(self, path) -> None:
@@ -387,6 +408,32 @@ class Instance:
         ct = np.empty(self.hg.pins, np.int32)
         _check(lib().fp_get_lists(self._h, _ptr(ln), _ptr(pt), _ptr(ct)), "fp_get_lists")
         return ln, pt, ct
+
+    STATE_FIELDS = ("part_vec", "ep_starts", "ep_ends", "ep_parts", "ep_cnt", "part_sizes", "marker", "send",
+                    "recv", "conn", "msgs")
+
+    def set_state(self, part_vec, ep_starts, ep_ends, ep_parts, ep_cnt, **optional) -> None:
+        """Uploads a refinement state in the reference's layout (fp_set_state);
+        optional: part_sizes, marker, send, recv, conn (K*K), msgs."""
+        arrs = dict(part_vec=part_vec, ep_starts=ep_starts, ep_ends=ep_ends, ep_parts=ep_parts, ep_cnt=ep_cnt)
+        for k, v in optional.items():
+            if k not in self.STATE_FIELDS:
+                raise TypeError(f"unknown state array {k}")
+            if v is not None:
+                arrs[k] = v
+        keep = {k: np.ascontiguousarray(v, dtype=np.int32) for k, v in arrs.items()}
+        st = FpState(**{k: v.ctypes.data for k, v in keep.items()})
+        _check(lib().fp_set_state(self._h, C.byref(st)), "fp_set_state")
+
+    def get_state(self) -> dict:
+        """Every array of fp_state, copied from the device (conn is K*K)."""
+        nov, noe, P, K = self.hg.nov, self.hg.noe, self.hg.pins, self.K
+        sizes = dict(part_vec=nov, ep_starts=noe, ep_ends=noe, ep_parts=P, ep_cnt=P, part_sizes=K, marker=K,
+                     send=K, recv=K, conn=K * K, msgs=K)
+        out = {k: np.empty(n, np.int32) for k, n in sizes.items()}
+        st = FpState(**{k: v.ctypes.data for k, v in out.items()})
+        _check(lib().fp_get_state(self._h, C.byref(st)), "fp_get_state")
+        return out
 
     def part_sizes(self) -> np.ndarray:
         s = np.empty(self.K, np.int32)

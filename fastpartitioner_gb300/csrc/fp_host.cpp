@@ -161,6 +161,29 @@ int fp_graph_from_nets(int32_t nov, int32_t noe, const uint32_t* nptr, const uin
   return FP_OK;
 }
 
+int fp_graph_from_vertices(int32_t nov, int32_t noe, const uint32_t* vptr, const uint32_t* vnets, const int32_t* src,
+                           fp_graph** out) {
+  if (!out || nov <= 0 || noe < 0 || !vptr || (!vnets && vptr[nov] > 0)) return FP_ERR_INVALID;
+  *out = nullptr;
+  for (int v = 0; v < nov; v++)
+    if (vptr[v + 1] < vptr[v]) return FP_ERR_INVALID;
+  fp_graph* gg = new (std::nothrow) fp_graph;
+  if (!gg) return FP_ERR_NOMEM;
+  HostGraph& g = gg->g;
+  g.nov = nov;
+  g.noe = noe;
+  g.pins = vptr[nov];
+  g.vptr.assign(vptr, vptr + nov + 1);
+  g.vnets.assign(vnets, vnets + g.pins);
+  for (uint32_t x : g.vnets)
+    if (x >= (uint32_t)noe) { delete gg; return FP_ERR_INVALID; }
+  build_net_csr(g);
+  if (src) g.src.assign(src, src + noe);
+  else choose_sources(g, 0);
+  *out = gg;
+  return FP_OK;
+}
+
 int fp_read_patohlike(const char* path, int32_t transpose, int32_t write_cache, fp_graph** out) {
   if (!path || !out) return FP_ERR_INVALID;
   *out = nullptr;

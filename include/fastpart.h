@@ -164,6 +164,12 @@ int fp_generate(const fp_gen_params* p, fp_graph** out);
  * CN drivers): vertex -> nets is its transpose, nets ascending per vertex. */
 int fp_graph_from_nets(int32_t nov, int32_t noe, const uint32_t* nptr, const uint32_t* npins,
                        const int32_t* src, fp_graph** out);
+/* Builds a host graph from a vertex -> nets CSR (the reference's row_ptr /
+ * col_ind as partition() receives them): net -> pins is built as the
+ * reference's createInverse does (shared/utils.cpp:32-56), pins ascending per
+ * net.  src NULL: lowest-id pin of each net. */
+int fp_graph_from_vertices(int32_t nov, int32_t noe, const uint32_t* vptr, const uint32_t* vnets,
+                           const int32_t* src, fp_graph** out);
 /* Reads a PaToH-like .hg file (shared/hypergraph_rw.cpp:97-242), honouring an
  * existing `<path>.plbin` cache exactly as the reference does.  `transpose` = 1
  * makes file lines nets (TV, CN drivers); 0 makes file lines vertices (TM, MSM,
@@ -173,6 +179,35 @@ int fp_read_patohlike(const char* path, int32_t transpose, int32_t write_cache, 
 int fp_write_patohlike(const fp_graph* g, const char* path);
 int fp_graph_view(const fp_graph* g, fp_hypergraph* view);
 int fp_graph_destroy(fp_graph* g);
+
+/* ---- refinement state in the reference's layout ----------------------- */
+/* The arrays the reference's partition() hands to its GPU wrapper after the
+ * initial stream (partition_gpu_wrapper, TV/partition.cpp:6-26,
+ * MGV/partition.cpp:4-27, MSRV/partition.cpp:4-25, TM/partition.cpp:3-7).
+ * Sizes: part_vec nov; ep_starts / ep_ends noe; ep_parts / ep_cnt pins (empty
+ * slots -1 / 0); part_sizes, marker, send, recv, msgs K; conn K*K row-major. */
+typedef struct fp_state {
+  int32_t* part_vec;
+  int32_t* ep_starts;   /* must equal the net offsets (prefix of net sizes)        */
+  int32_t* ep_ends;
+  int32_t* ep_parts;
+  int32_t* ep_cnt;
+  int32_t* part_sizes;  /* NULL on set: recounted from part_vec and the weights    */
+  int32_t* marker;      /* TV's last scanner per part; NULL on set: all -1         */
+  int32_t* send;        /* MSV / MSRV send volumes; NULL on set: recounted         */
+  int32_t* recv;        /* MSRV received volumes; NULL on set: recounted           */
+  int32_t* conn;        /* TM / MSM part_connections; NULL on set: recounted       */
+  int32_t* msgs;        /* TM / MSM part_messages; NULL on set: recounted          */
+} fp_state;
+
+/* Replaces the instance's state with a caller-built one (checked against the
+ * hypergraph: every list must equal the recount from part_vec); it becomes the
+ * state fp_reset_state() restores.  Replaces the wrapper's upload of these
+ * arrays before its refinement kernels. */
+int fp_set_state(fp_instance* inst, const fp_state* st);
+/* Copies the current device state out; NULL members are skipped.  ep_starts
+ * is filled with the net offsets. */
+int fp_get_state(fp_instance* inst, fp_state* st);
 
 /* ---- drop-in for partition_gpu() --------------------------------------- */
 /* Same arguments and the same stdout lines as the reference's partition_gpu()

@@ -223,3 +223,38 @@ def test_gpu_heavy_vertices_and_repeated_refine(fp, orc, gpu_engine, metric, K):
                                           err_msg=tag)
             assert inst.metrics() == o["metrics_final"], tag
             inst.reset_state()
+
+
+@pytest.mark.parametrize("metric", METRICS)
+def test_gpu_set_state_round_trip(fp, orc, gpu_engine, metric):
+    """A state taken out in the reference's layout (fp_get_state) and loaded
+    into a fresh instance (fp_set_state) refines to the oracle's result; the
+    optional arrays the LDG metrics leave out are recounted from the lists."""
+    hg = fp.generate(fp.GenSpec.zipf(6000, 6000, 2.1, 2, 800, beta=1.5, seed=51))
+    K, passes = 32, 3
+    o = orc.run_oracle(hg, K, metric, passes)
+    with gpu_engine.instance(hg, K, metric) as a:
+        a.initial_partition()
+        st = a.get_state()
+    np.testing.assert_array_equal(st["part_vec"], o["part_vec_init"])
+    np.testing.assert_array_equal(st["ep_starts"], hg.nptr[:-1].astype(np.int32))
+    variants = [dict(st)]
+    if metric not in ("TM", "MSM"):
+        variants.append({k: st[k] for k in ("part_vec", "ep_starts", "ep_ends", "ep_parts", "ep_cnt", "marker")})
+    for i, arrs in enumerate(variants):
+        with gpu_engine.instance(hg, K, metric) as b:
+            base = {k: arrs[k] for k in ("part_vec", "ep_starts", "ep_ends", "ep_parts", "ep_cnt")}
+            b.set_state(**base, **{k: v for k, v in arrs.items() if k not in base})
+            back = b.get_state()
+            for k in st:
+                np.testing.assert_array_equal(back[k], st[k], err_msg=f"{metric} variant {i} {k}")
+            b.refine(passes)
+            np.testing.assert_array_equal(b.partition(), o["part_vec"], err_msg=f"{metric} variant {i}")
+            assert b.metrics() == o["metrics_final"], f"{metric} variant {i}"
+    # a list that disagrees with the part vector is rejected
+    bad = dict(st)
+    bad["ep_cnt"] = st["ep_cnt"].copy()
+    bad["ep_cnt"][0] += 1
+    with gpu_engine.instance(hg, K, metric) as c:
+        with pytest.raises(fp.FastPartError):
+            c.set_state(bad["part_vec"], bad["ep_starts"], bad["ep_ends"], bad["ep_parts"], bad["ep_cnt"])

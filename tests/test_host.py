@@ -1,5 +1,6 @@
 """Host-side hypergraph handling: the generator and the PaToH-like file format."""
 import numpy as np
+import pytest
 
 from conftest import ROOT  # noqa: F401
 
@@ -79,3 +80,22 @@ def test_patohlike_lines_as_vertices(fp, tmp_path):
     # net -> pins is the inverse with ascending vertices
     np.testing.assert_array_equal(g.nptr, [0, 2, 4, 5])
     np.testing.assert_array_equal(g.npins, [0, 2, 0, 1, 1])
+
+
+def test_graph_from_vertices_is_the_inverse(fp):
+    """Net -> pins built from vertex -> nets equals the original net CSR (pins
+    ascending per net), and sources default to the lowest-id pin."""
+    hg = fp.generate(fp.GenSpec.zipf(3000, 2500, 2.1, 2, 300, beta=1.5, seed=9))
+    g2 = fp.Hypergraph.from_vertices(hg.nov, hg.noe, hg.vptr, hg.vnets, hg.src)
+    np.testing.assert_array_equal(g2.nptr, hg.nptr)
+    for e in range(0, hg.noe, 97):
+        a = np.sort(hg.npins[hg.nptr[e]:hg.nptr[e + 1]])
+        np.testing.assert_array_equal(g2.npins[g2.nptr[e]:g2.nptr[e + 1]], a)
+    np.testing.assert_array_equal(g2.src, hg.src)
+    g3 = fp.Hypergraph.from_vertices(hg.nov, hg.noe, hg.vptr, hg.vnets)
+    lo = np.minimum.reduceat(g3.npins, g3.nptr[:-1].astype(np.int64))
+    np.testing.assert_array_equal(g3.src, lo)
+    with pytest.raises(fp.FastPartError):
+        bad = hg.vnets.copy()
+        bad[0] = hg.noe
+        fp.Hypergraph.from_vertices(hg.nov, hg.noe, hg.vptr, bad)
