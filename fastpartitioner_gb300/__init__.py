@@ -114,6 +114,7 @@ def lib():
             "fp_refine": ([vp, i32], C.c_int),
             "fp_reset_state": ([vp], C.c_int),
             "fp_set_engine": ([vp, i32], C.c_int),
+            "fp_set_classes": ([vp, i64, i64], C.c_int),
             "fp_metrics": ([vp, vp], C.c_int),
             "fp_get_partition": ([vp, vp], C.c_int),
             "fp_get_lists": ([vp, vp, vp, vp], C.c_int),
@@ -391,6 +392,11 @@ class Instance:
             b += 4 * K * K + 2 * 4 * K * words
         return b
 
+    def set_classes(self, light_work: int, super_work: int) -> None:
+        """Work bounds of the warp / CTA / whole-grid vertex classes (TV, MSV,
+        MSRV); a tuning knob, results are unchanged."""
+        _check(lib().fp_set_classes(self._h, light_work, super_work), "fp_set_classes")
+
     def metrics(self) -> dict:
         out = np.zeros(6, np.int64)
         _check(lib().fp_metrics(self._h, _ptr(out)), "fp_metrics")
@@ -452,7 +458,9 @@ class Instance:
         names = ["windows", "heavy_rounds", "window_moves", "cut_none", "cut_stale", "cut_size", "cut_volume",
                  "cut_maxpart", "cut_conflict", "walked"]
         d = {n: int(x[i]) for i, n in enumerate(names)}
-        d.update(eval_ms=x[16] / 1e6, validate_ms=x[17] / 1e6, commit_ms=x[18] / 1e6, heavy_ms=x[19] / 1e6)
+        d.update(eval_ms=x[16] / 1e6, validate_ms=x[17] / 1e6, commit_ms=x[18] / 1e6, heavy_ms=x[19] / 1e6,
+                 round_state_ms=x[20] / 1e6, warp_max_cycles=int(x[21]), cta_max_cycles=int(x[23]),
+                 light_cycles=int(x[25]), light_evals=int(x[26]))
         return d
 
     def last_launches(self) -> int:

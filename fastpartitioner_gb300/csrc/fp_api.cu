@@ -27,8 +27,15 @@ cudaError_t launch_spec_cn(const DevInstance& I, const SpecBuf& B, int passes, i
 static bool spec_supported(int metric) {
   return metric >= FP_METRIC_CN && metric <= FP_METRIC_MSRV;
 }
-constexpr int kHeavyDegHost = 256;     // must equal spec::kHeavyDeg (fp_spec_common.cuh)
-constexpr int kSuperDegHost = 16384;   // must equal spec::kSuperDeg
+constexpr int kHeavyDegHost = 256;     // TM / MSM: vertices with more nets get a whole-grid round
+// LDG metrics: vertex classes by work = sum over its nets of min(net size, K),
+// the list slots an evaluation reads at most.  Light: one warp; medium: one CTA
+// inside the window; above the super bound (or with 65536 nets or more, the
+// limit of the candidate encoding): a whole-grid round.  MSV's windows are
+// short (nearly every vertex moves), so its medium vertices bound the round
+// time and the super bound is lower (bounds from a sweep on the c2 workload).
+constexpr int kLightWork = 2048;
+int default_super_work(int metric) { return metric == FP_METRIC_MSV ? 65536 : 262144; }
 constexpr int kMaxSpecWarps = 16384;
 cudaError_t launch_metrics(const DevInstance& I, void* scratch, long long* out, int num_sms, cudaStream_t st,
                            int* launches);
@@ -65,6 +72,7 @@ struct fp_instance {
   int* heavy_pos_d = nullptr;
   std::vector<int> mid_pos;       // CTA-evaluated vertices, by position
   int* mid_pos_d = nullptr;
+  unsigned char* vclass_d = nullptr;
   std::vector<int> heavy_ids;     // heavy vertices by id (TM / MSM walk ids)
   int* heavy_ids_d = nullptr;
 };
@@ -258,6 +266,42 @@ static cudaError_t clear_spec_scratch(const SpecBuf& b, int noe, int K, cudaStre
   return e;
 }
 
+// Vertex classes of the LDG engine (see kLightWork) and the position lists of
+// the medium and whole-grid vertices, uploaded to the device.
+static int classify(fp_instance* in, long long light_work, long long super_work) {
+  const HostGraph& g = in->g;
+  const Problem& pb = in->pb;
+  std::vector<unsigned char> cls(g.nov, 0);
+  in->heavy_pos.clear();
+  in->mid_pos.clear();
+  for (int z = 0; z < g.nov; z++) {
+    const int v = pb.order[z];
+    long long work = 0;
+    for (uint32_t k = g.vptr[v]; k < g.vptr[v + 1]; k++) {
+      const uint32_t e = g.vnets[k];
+      work += std::min<long long>(g.nptr[e + 1] - g.nptr[e], pb.K);
+    }
+    const long long deg = g.vptr[v + 1] - g.vptr[v];
+    if (work > super_work || deg >= 65536) {
+      cls[v] = 2;
+      in->heavy_pos.push_back(z);
+    } else if (work > light_work) {
+      cls[v] = 1;
+      in->mid_pos.push_back(z);
+    }
+  }
+  in->sb.nheavy = (int)in->heavy_pos.size();
+  in->sb.nmid = (int)in->mid_pos.size();
+  cudaStream_t s = in->ctx->stream;
+  cudaError_t e = cudaMemcpyAsync(in->vclass_d, cls.data(), g.nov, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess && in->sb.nheavy)
+    e = cudaMemcpyAsync(in->heavy_pos_d, in->heavy_pos.data(), sizeof(int) * in->sb.nheavy, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess && in->sb.nmid)
+    e = cudaMemcpyAsync(in->mid_pos_d, in->mid_pos.data(), sizeof(int) * in->sb.nmid, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);   // host vectors are pageable and local
+  return cuda_status(e);
+}
+
 int fp_instance_create(fp_ctx* ctx, const fp_hypergraph* h, int32_t K, int32_t metric, double eps_factor,
                        fp_instance** out) {
   if (!ctx || !out || metric < 0 || metric > 5 || K < 2 || K > kMaxK || !(eps_factor > 0)) return FP_ERR_INVALID;
@@ -301,17 +345,6 @@ int fp_instance_create(fp_ctx* ctx, const fp_hypergraph* h, int32_t K, int32_t m
   d.C = pb.C;
   d.max_pw = (int)(pb.xw + (pb.xw * 0.1));
   d.min_pw = (int)(pb.xw - (pb.xw * 0.1));
-  // Heavy vertices (more than kHeavyDegHost nets), by position in visiting order.
-  in->heavy_pos.clear();
-  in->mid_pos.clear();
-  for (int z = 0; z < g.nov; z++) {
-    const int v = pb.order[z];
-    const int dv = (int)(g.vptr[v + 1] - g.vptr[v]);
-    if (dv > kSuperDegHost) in->heavy_pos.push_back(z);
-    else if (dv > kHeavyDegHost) in->mid_pos.push_back(z);
-  }
-  const int nheavy = (int)in->heavy_pos.size();
-  const int nmid = (int)in->mid_pos.size();
   in->heavy_ids.clear();
   for (int v = 0; v < g.nov; v++)
     if ((int)(g.vptr[v + 1] - g.vptr[v]) > kHeavyDegHost) in->heavy_ids.push_back(v);
@@ -331,7 +364,7 @@ int fp_instance_create(fp_ctx* ctx, const fp_hypergraph* h, int32_t K, int32_t m
       (rc = dalloc(in, &in->sb.flag, kSpecWindow)) || (rc = dalloc(in, &in->sb.slack, kSpecWindow)) ||
       (rc = dalloc(in, &in->sb.vslack, kSpecWindow)) || (rc = dalloc(in, &in->sb.wt, kSpecWindow)) ||
       (rc = dalloc(in, &in->sb.vd, kSpecWindow)) || (rc = dalloc(in, &in->sb.scan, (size_t)kSpecWindow * words)) ||
-      (rc = dalloc(in, &in->sb.nflag, (size_t)kSpecWindow * kHeavyDegHost)) ||
+      (rc = dalloc(in, &in->sb.rec, g.pins)) || (rc = dalloc(in, &in->vclass_d, g.nov)) ||
       (rc = dalloc(in, &in->sb.cand, (size_t)kSpecWindow * K)) || (rc = dalloc(in, &in->sb.ncand, kSpecWindow)) ||
       (rc = dalloc(in, &in->sb.pref, (size_t)kSpecWindow * K)) ||
       (rc = dalloc(in, &in->sb.wsum, kMaxSpecWarps)) || (rc = dalloc(in, &in->sb.vsum, kMaxSpecWarps)) ||
@@ -339,9 +372,9 @@ int fp_instance_create(fp_ctx* ctx, const fp_hypergraph* h, int32_t K, int32_t m
       (rc = dalloc(in, &in->sb.mask_c, g.noe)) || (rc = dalloc(in, &in->sb.hcnt, 2 * K)) ||
       (rc = dalloc(in, &in->sb.hfirst, 2 * K)) || (rc = dalloc(in, &in->sb.hgain, 2 * K)) ||
       (rc = dalloc(in, &in->sb.hloss, 2 * K)) || (rc = dalloc(in, &in->sb.hadelta, 2 * K)) ||
-      (rc = dalloc(in, &in->sb.hmisc, 16)) || (rc = dalloc(in, &in->heavy_pos_d, std::max(nheavy, 1))) ||
-      (rc = dalloc(in, &in->heavy_ids_d, std::max(nheavy + nmid, 1))) ||
-      (rc = dalloc(in, &in->mid_pos_d, std::max(nmid, 1))) ||
+      (rc = dalloc(in, &in->sb.hmisc, 16)) || (rc = dalloc(in, &in->heavy_pos_d, g.nov)) ||
+      (rc = dalloc(in, &in->heavy_ids_d, std::max<size_t>(in->heavy_ids.size(), 1))) ||
+      (rc = dalloc(in, &in->mid_pos_d, g.nov)) ||
       (rc = dalloc(in, &in->metric_out, 8))) {
     fp_instance_destroy(in);
     return rc;
@@ -354,21 +387,18 @@ int fp_instance_create(fp_ctx* ctx, const fp_hypergraph* h, int32_t K, int32_t m
   in->sb.wmax = kSpecWindow;
   in->sb.max_warps = kMaxSpecWarps;
   in->sb.heavy_pos = in->heavy_pos_d;
-  in->sb.nheavy = nheavy;
   in->sb.mid_pos = in->mid_pos_d;
-  in->sb.nmid = nmid;
+  in->sb.vclass = in->vclass_d;
   {
     cudaStream_t s0 = ctx->stream;
     e = clear_spec_scratch(in->sb, g.noe, K, s0);
-    if (e == cudaSuccess && nheavy)
-      e = cudaMemcpyAsync(in->heavy_pos_d, in->heavy_pos.data(), sizeof(int) * nheavy, cudaMemcpyHostToDevice, s0);
     if (e == cudaSuccess && !in->heavy_ids.empty())
       e = cudaMemcpyAsync(in->heavy_ids_d, in->heavy_ids.data(), sizeof(int) * in->heavy_ids.size(),
                           cudaMemcpyHostToDevice, s0);
-    if (e == cudaSuccess && nmid)
-      e = cudaMemcpyAsync(in->mid_pos_d, in->mid_pos.data(), sizeof(int) * nmid, cudaMemcpyHostToDevice, s0);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s0);
     if (e != cudaSuccess) { fp_instance_destroy(in); return cuda_status(e); }
+    rc = classify(in, kLightWork, default_super_work(metric));
+    if (rc) { fp_instance_destroy(in); return rc; }
   }
   if (cudaMallocHost(&in->h_moves, sizeof(long long) * kMaxPasses) != cudaSuccess ||
       cudaMallocHost(&in->h_status, sizeof(int)) != cudaSuccess ||
@@ -462,6 +492,12 @@ int fp_refine(fp_instance* in, int32_t passes) {
   in->last_passes = passes;
   in->last_launches = 1;
   return *in->h_status;
+}
+
+int fp_set_classes(fp_instance* in, int64_t light_work, int64_t super_work) {
+  if (!in || light_work < 0 || super_work < light_work) return FP_ERR_INVALID;
+  cudaSetDevice(in->ctx->device);
+  return classify(in, light_work, super_work);
 }
 
 int fp_set_engine(fp_instance* in, int32_t engine) {
@@ -562,7 +598,10 @@ int fp_set_state(fp_instance* in, const fp_state* s) {
       if (s->marker[p] < -1 || s->marker[p] >= nov) return FP_ERR_INVALID;
       st.marker[p] = s->marker[p];
     }
-  // Volumes and messages: as given, else the count over the lists.
+  // Volumes and messages: as given, else the count over the lists; the arrays
+  // a metric does not keep stay zero (send: MSV, MSRV; recv: MSRV).
+  const bool keep_send = metric == FP_METRIC_MSV || metric == FP_METRIC_MSRV;
+  const bool keep_recv = metric == FP_METRIC_MSRV;
   st.send.assign(K, 0);
   st.recv.assign(K, 0);
   st.msgs.assign(K, 0);
@@ -573,8 +612,8 @@ int fp_set_state(fp_instance* in, const fp_state* s) {
     for (int j = 0; j < st.ep_len[e]; j++) {
       const int p = st.ep_part[b + j];
       if (p == sp) continue;
-      st.send[sp]++;
-      st.recv[p]++;
+      if (keep_send) st.send[sp]++;
+      if (keep_recv) st.recv[p]++;
       if (msg) st.conn[(size_t)sp * K + p]++;
     }
   }
@@ -587,8 +626,8 @@ int fp_set_state(fp_instance* in, const fp_state* s) {
         if (a != b && st.conn[(size_t)a * K + b] > 0) st.msgs[a]++;
     if (s->msgs) st.msgs.assign(s->msgs, s->msgs + K);
   }
-  if (s->send) st.send.assign(s->send, s->send + K);
-  if (s->recv) st.recv.assign(s->recv, s->recv + K);
+  if (s->send && keep_send) st.send.assign(s->send, s->send + K);
+  if (s->recv && keep_recv) st.recv.assign(s->recv, s->recv + K);
   cudaSetDevice(in->ctx->device);
   in->st = std::move(st);
   in->has_state = true;

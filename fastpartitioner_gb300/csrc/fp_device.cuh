@@ -57,8 +57,10 @@ struct SpecBuf {
   int* wt;               // [wmax] weight moved by a mover (0 otherwise)
   int* vd;               // [wmax] largest volume change of one part by a mover
   uint32_t* scan;        // [wmax * words] parts scanned per window offset (TV)
-  unsigned char* nflag;  // [wmax * 256] per mover net: bit0 loses own part, bit1 gains
-                         //     the new part, bit2 the mover is the net's source
+  uint32_t* rec;         // [pins] per (vertex, net) record of a move (spec::rec_pack),
+                         //     at the pair's vnets index
+  const unsigned char* vclass;  // [nov] 0: warp-evaluated, 1: CTA-evaluated (medium),
+                                //     2: whole-grid round (LDG metrics)
   unsigned long long* cand;  // [wmax * K] LDG candidates per window offset (part, count, first)
   int* ncand;            // [wmax]
   int* pref;             // [K * wmax] per-part prefix of the window's size changes

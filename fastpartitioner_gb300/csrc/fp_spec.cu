@@ -23,8 +23,14 @@
 //                 and the next window starts at the cut.
 //
 // Every committed outcome therefore equals the reference's sequential outcome.
-// Vertices with more than kHeavyDeg nets get a round of their own in which all
-// warps of the grid split the tally, the gain / loss sums and the move.
+//
+// A mover's slots (own part, destination) in each of its nets' lists are found
+// once, by a flattened pass over the slots (locate_batch), and recorded per
+// (vertex, net); the gain / loss terms and the commit then take O(1) per net.
+// Vertices are classed by work (list slots over their nets, host-side): light
+// ones are evaluated by one warp, medium ones by one CTA inside the window, and
+// the heaviest get a round of their own in which all warps of the grid split
+// the tally, the gain / loss sums and the move.
 
 #include "fp_spec_common.cuh"
 
@@ -165,71 +171,106 @@ __device__ int ldg_recheck(const DevInstance& I, const RoundCtx& R, const SpecBu
   return d;
 }
 
-// Per-net pass of a vertex with d != own, one net per thread (nets k0, k0 +
-// kstep, ...): which nets lose `own` / gain `d` (nflag bit0 / bit1; bit2 = v is
-// the net's source), and for MSV / MSRV the reference's gains / losses
+// The reference's gains / losses of the move own -> d on net e
 // (MGV/partition.cpp:294-337, MSRV/partition.cpp:303-350) and the exact change
-// of every part's volume that commit_net will make (adelta).
-__device__ void net_pass(const DevInstance& I, int metric, int v, int own, int d, uint32_t base, int deg, int k0,
-                         int kstep, unsigned char* nflag, int* gains, int* losses, int* adelta) {
-  const bool vol = metric != kTV;
-  const bool rv = metric == kMSRV;
-  for (int k = k0; k < deg; k += kstep) {
-    const int e = (int)__ldg(&I.vnets[base + k]);
-    const int s = (int)__ldg(&I.nptr[e]);
-    const int n = lds(&I.ep_len[e]);
-    int co = 0;
-    bool fd = false;
-    for (int j = 0; j < n; j++) {
-      const int p = lds(&I.ep_part[s + j]);
-      if (p == own) co = lds(&I.ep_cnt[s + j]);
-      if (p == d) fd = true;
-    }
-    const bool rem = co == 1, add = !fd;
-    const int sv = __ldg(&I.src[e]);
-    if (nflag) nflag[k] = (unsigned char)((rem ? 1 : 0) | (add ? 2 : 0) | (sv == v ? 4 : 0));
-    if (!vol) continue;
-    const int sp = sv == v ? own : lds(&I.part_vec[sv]);
-    if (sv == v) {
-      atomicAdd(&gains[own], n - 1);
-      atomicAdd(&losses[d], n - 1);
-    }
-    if (rem) {
-      if (sv != v) {
-        atomicAdd(&gains[sp], 1);
-        if (rv) atomicAdd(&gains[own], 1);
-      } else {
-        atomicAdd(&losses[d], -1);
-      }
-    }
-    if (add) {
-      if (sv != v) {
-        atomicAdd(&losses[sp], 1);
-        if (rv) atomicAdd(&losses[d], 1);
-      } else {
-        atomicAdd(&losses[d], 1);
-      }
-    }
-    const int n1 = rem ? n - 1 : n;
-    if (sv == v) {
-      atomicAdd(&adelta[own], -(n - 1));
-      atomicAdd(&adelta[d], n1 - 1);
-    }
-    if (rem) {
-      if (sv != v) {
-        atomicAdd(&adelta[sp], -1);
-        if (rv) atomicAdd(&adelta[own], -1);
-      }
-    } else if (rv && sv == v) {
-      atomicAdd(&adelta[own], 1);
-    }
-    if (!add) {
-      if (rv && sv == v) atomicAdd(&adelta[d], -1);
+// of every part's volume that commit_rec will make (adelta), from the net's
+// record r.
+__device__ __forceinline__ void net_terms(const DevInstance& I, bool rv, int v, int own, int d, int e, uint32_t r,
+                                          int* gains, int* losses, int* adelta) {
+  const int n = lds(&I.ep_len[e]);
+  const bool rem = rec_rem(r), add = rec_add(r);
+  const int sv = __ldg(&I.src[e]);
+  const int sp = sv == v ? own : lds(&I.part_vec[sv]);
+  if (sv == v) {
+    atomicAdd(&gains[own], n - 1);
+    atomicAdd(&losses[d], n - 1);
+  }
+  if (rem) {
+    if (sv != v) {
+      atomicAdd(&gains[sp], 1);
+      if (rv) atomicAdd(&gains[own], 1);
     } else {
-      atomicAdd(&adelta[sv == v ? d : sp], 1);
-      if (rv && sv != v) atomicAdd(&adelta[d], 1);
+      atomicAdd(&losses[d], -1);
     }
   }
+  if (add) {
+    if (sv != v) {
+      atomicAdd(&losses[sp], 1);
+      if (rv) atomicAdd(&losses[d], 1);
+    } else {
+      atomicAdd(&losses[d], 1);
+    }
+  }
+  const int n1 = rem ? n - 1 : n;
+  if (sv == v) {
+    atomicAdd(&adelta[own], -(n - 1));
+    atomicAdd(&adelta[d], n1 - 1);
+  }
+  if (rem) {
+    if (sv != v) {
+      atomicAdd(&adelta[sp], -1);
+      if (rv) atomicAdd(&adelta[own], -1);
+    }
+  } else if (rv && sv == v) {
+    atomicAdd(&adelta[own], 1);
+  }
+  if (!add) {
+    if (rv && sv == v) atomicAdd(&adelta[d], -1);
+  } else {
+    atomicAdd(&adelta[sv == v ? d : sp], 1);
+    if (rv && sv != v) atomicAdd(&adelta[d], 1);
+  }
+}
+
+// Records of v's nets for the move own -> d; warp wi of a group of nw warps
+// takes the batches of 32 nets wi, wi + nw, ...  With volumes (MSV / MSRV) the
+// gain / loss / volume terms are added to the warp's arrays.  loc: the warp's
+// 96 ints of scratch.
+__device__ void locate_all(const DevInstance& I, const SpecBuf& B, int metric, int v, int own, int d,
+                           uint32_t base, int deg, int wi, int nw, int* loc, int* gains, int* losses, int* adelta) {
+  const bool vol = metric != kTV, rv = metric == kMSRV;
+  for (int nb = wi * 32; nb < deg; nb += nw * 32) {
+    int e;
+    const uint32_t r = locate_batch(I, B.rec, v, own, d, base, nb, deg, loc, loc + 32, loc + 64, &e);
+    if (vol && e >= 0) net_terms(I, rv, v, own, d, e, r, gains, losses, adelta);
+  }
+}
+
+// Claims of the mover at position z on its nets k0, k0 + kstep, ...: a change
+// of the part set (or, with volumes, of the source's side) takes claim_m, a
+// count-only change claim_c and the bits of the two parts.
+__device__ __forceinline__ void claim_nets(const DevInstance& I, const SpecBuf& B, bool vol, int z, int own, int d,
+                                           uint32_t base, int deg, int k0, int kstep) {
+  const uint32_t bits = (1u << (own & 31)) | (1u << (d & 31));
+  for (int k = k0; k < deg; k += kstep) {
+    const int e = (int)__ldg(&I.vnets[base + k]);
+    if (rec_setchange(lds(&B.rec[base + k]), vol)) {
+      atomicMin(&B.claim_m[e], z);
+    } else {
+      atomicMin(&B.claim_c[e], z);
+      atomicOr(&B.mask_c[e], bits);
+    }
+  }
+}
+
+// Did an earlier mover of the window change something the vertex at z read on
+// its nets k0, k0 + kstep, ...: a part set, or the count of z's own part; or
+// does z (a mover) change the part set of a net whose counts an earlier mover
+// changes?
+__device__ __forceinline__ bool conflicts(const DevInstance& I, const SpecBuf& B, bool vol, int z, int own,
+                                          bool mover, uint32_t base, int deg, int k0, int kstep) {
+  const unsigned ob = 1u << (own & 31);
+  bool conf = false;
+  for (int k = k0; k < deg && !conf; k += kstep) {
+    const int e = (int)__ldg(&I.vnets[base + k]);
+    if (lds(&B.claim_m[e]) < z) {
+      conf = true;
+    } else if (lds(&B.claim_c[e]) < z) {
+      if (lds(&B.mask_c[e]) & ob) conf = true;
+      else if (mover && rec_setchange(lds(&B.rec[base + k]), vol)) conf = true;
+    }
+  }
+  return conf;
 }
 
 // Per-thread partial of the MSV / MSRV accept test (MGV/partition.cpp:339-362,
@@ -290,18 +331,18 @@ __device__ __forceinline__ int block_reduce_min(int x, int* scr) {
   return -block_reduce_max(-x, scr);
 }
 
-// Evaluation of a medium vertex (more than kHeavyDeg nets) at position z by the
-// whole CTA: the warps split the tally, warp 0 decides, the threads split the
-// per-net pass.  Writes the same per-position record as a warp evaluation
-// (flag bit 2 marks it); a medium mover claims all its nets as part-set changes.
+// Evaluation of a medium vertex at position z by the whole CTA: the warps split
+// the tally, warp 0 decides, the warps split the locate pass and the gain /
+// loss terms.  Writes the same per-position record as a warp evaluation (flag
+// bit 2 marks it).
 __device__ void cta_eval_ldg(const DevInstance& I, const SpecBuf& B, const RoundCtx& R, int metric, int z, int pos,
                              int par, int q, int* cnt_b, unsigned long long* first_b, int* gains_b, int* losses_b,
-                             int* adelta_b, int* iscr, int* s_mw, int* s_mv) {
+                             int* adelta_b, int* iscr, int* s_mw, int* s_mv, int* loc_b) {
   __shared__ int sh[4];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int K = I.K;
   const int words = (K + 31) >> 5;
-  const bool rv = metric == kMSRV;
+  const bool vol = metric != kTV, rv = metric == kMSRV;
   const int o = z - pos;
   const int v = __ldg(&I.order[z]);
   const int own = lds(&I.part_vec[v]);
@@ -374,43 +415,49 @@ __device__ void cta_eval_ldg(const DevInstance& I, const SpecBuf& B, const Round
   bool mover = false, mt = false;
   int vs = kBig, vdd = 0;
   if (d != own) {
-    if (metric == kTV) {
-      mover = c1t >= deg - cnt_b[d];
-    } else {
+    // TV moves iff the leave gain covers the arrival loss; MSV / MSRV need the
+    // accept test on the gain / loss sums.
+    const bool need = metric == kTV ? c1t >= deg - cnt_b[d] : true;
+    mover = metric == kTV && need;
+    if (need) {
       int* gains = gains_b + (size_t)wib * K;
       int* losses = losses_b + (size_t)wib * K;
       int* adelta = adelta_b + (size_t)wib * K;
-      for (int p = lane; p < K; p += 32) { gains[p] = 0; losses[p] = 0; adelta[p] = 0; }
-      __syncwarp();
-      net_pass(I, metric, v, own, d, base, deg, threadIdx.x, blockDim.x, nullptr, gains, losses, adelta);
-      __syncthreads();
-      for (int p = threadIdx.x; p < K; p += blockDim.x) {
-        int g = 0, l = 0, a = 0;
-        for (int x = 0; x < kSWarps; x++) {
-          g += gains_b[(size_t)x * K + p];
-          l += losses_b[(size_t)x * K + p];
-          a += adelta_b[(size_t)x * K + p];
-        }
-        gains_b[p] = g;
-        losses_b[p] = l;
-        adelta_b[p] = a;
+      if (vol) {
+        for (int p = lane; p < K; p += 32) { gains[p] = 0; losses[p] = 0; adelta[p] = 0; }
+        __syncwarp();
       }
+      locate_all(I, B, metric, v, own, d, base, deg, wib, kSWarps, loc_b + wib * 96, gains, losses, adelta);
       __syncthreads();
-      const AcceptPart a = accept_partial(R, gains_b, losses_b, adelta_b, K, rv, threadIdx.x, blockDim.x);
-      const bool fM = __syncthreads_or(a.failM);
-      const bool fN = __syncthreads_or(a.failN);
-      const bool amt = __syncthreads_or(a.mt);
-      const int fsl = block_reduce_max(a.fsl, iscr);
-      const int msl = block_reduce_min(a.msl, iscr);
-      vdd = block_reduce_max(a.vd, iscr);
-      bool good;
-      accept_final(fM, fN, fsl, msl, &good, &vs);
-      mover = good;
-      mt = mover && amt;
+      if (vol) {
+        for (int p = threadIdx.x; p < K; p += blockDim.x) {
+          int g = 0, l = 0, a = 0;
+          for (int x = 0; x < kSWarps; x++) {
+            g += gains_b[(size_t)x * K + p];
+            l += losses_b[(size_t)x * K + p];
+            a += adelta_b[(size_t)x * K + p];
+          }
+          gains_b[p] = g;
+          losses_b[p] = l;
+          adelta_b[p] = a;
+        }
+        __syncthreads();
+        const AcceptPart a = accept_partial(R, gains_b, losses_b, adelta_b, K, rv, threadIdx.x, blockDim.x);
+        const bool fM = __syncthreads_or(a.failM);
+        const bool fN = __syncthreads_or(a.failN);
+        const bool amt = __syncthreads_or(a.mt);
+        const int fsl = block_reduce_max(a.fsl, iscr);
+        const int msl = block_reduce_min(a.msl, iscr);
+        vdd = block_reduce_max(a.vd, iscr);
+        bool good;
+        accept_final(fM, fN, fsl, msl, &good, &vs);
+        mover = good;
+        mt = mover && amt;
+      }
     }
   }
   if (mover) {
-    for (int k = threadIdx.x; k < deg; k += blockDim.x) atomicMin(&B.claim_m[__ldg(&I.vnets[base + k])], z);
+    claim_nets(I, B, vol, z, own, d, base, deg, threadIdx.x, blockDim.x);
     if (threadIdx.x == 0 && mt) atomicMin(&B.ctl[2 + par], z);
   }
   if (threadIdx.x == 0) {
@@ -428,10 +475,9 @@ __device__ void cta_eval_ldg(const DevInstance& I, const SpecBuf& B, const Round
   __syncthreads();
 }
 
-// Validation of a medium vertex by the whole CTA (same rules as the warp
-// validation; a medium mover treats all its nets as part-set changes).
+// Validation of a medium vertex by the whole CTA (the warp validation's rules).
 __device__ void cta_validate_ldg(const DevInstance& I, const SpecBuf& B, const RoundCtx& R, int metric, int z, int pos,
-                                 int par, int q, int mtpos, long long pre_w, long long pre_v, int* iscr) {
+                                 int q, int par, int mtpos, long long pre_w, long long pre_v) {
   __shared__ long long shd[2];
   __shared__ int shw;
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -472,19 +518,11 @@ __device__ void cta_validate_ldg(const DevInstance& I, const SpecBuf& B, const R
   if (why == 0) {
     const uint32_t base = __ldg(&I.vptr[v]);
     const int deg = (int)(__ldg(&I.vptr[v + 1]) - base);
-    const unsigned ob = 1u << (own & 31);
-    const bool mover = fl & 1;
-    bool conf = false;
-    for (int k = threadIdx.x; k < deg; k += blockDim.x) {
-      const int e = (int)__ldg(&I.vnets[base + k]);
-      if (lds(&B.claim_m[e]) < z) conf = true;
-      if (lds(&B.claim_c[e]) < z && (mover || (lds(&B.mask_c[e]) & ob))) conf = true;
-    }
+    const bool conf = conflicts(I, B, metric != kTV, z, own, fl & 1, base, deg, threadIdx.x, blockDim.x);
     if (__syncthreads_or(conf)) why = 5;
   }
   if (why && threadIdx.x == 0) atomicMin(&B.ctl[par], (z << 3) | why);
   __syncthreads();
-  (void)iscr;
 }
 
 __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, SpecBuf B, int passes) {
@@ -494,6 +532,7 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
   __shared__ int s_minpart, s_minsize, s_second, s_maxv, s_cc, s_count, s_d;
   __shared__ long long s_pre_w, s_pre_v;
   __shared__ int s_mw[kSWarps], s_mv[kSWarps];
+  __shared__ int loc_b[kSWarps * 96];   // per-warp locate scratch
   const int metric = I.metric;
   const bool vol = metric != kTV;
   const bool rv = metric == kMSRV;
@@ -518,6 +557,7 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
   int* gains = gains_b + (size_t)wib * K;
   int* losses = losses_b + (size_t)wib * K;
   int* adelta = adelta_b + (size_t)wib * K;
+  int* loc = loc_b + wib * 96;
   Vol V{I.send, rv ? I.recv : nullptr};
 
   int round = 0;
@@ -598,6 +638,7 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
       }
       __syncthreads();
       const RoundCtx R{sizes_s, pen_s, marker_s, vol_s, mark_s, s_minpart, s_minsize, s_second, s_maxv, s_cc};
+      if (blockIdx.x == 0 && threadIdx.x == 0) B.stats[20] += gtimer() - tA;
       pass_start = false;
       prev_maxtouch = false;
       while (hidx < B.nheavy && __ldg(&B.heavy_pos[hidx]) < pos) hidx++;
@@ -654,23 +695,30 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
         const int d = s_d;
         const int hc1 = lds(&hmisc[0]);
         bool mover = false;
-        if (metric == kTV) {
-          mover = d != own && hc1 >= deg - cnt_b[d];
-        } else if (d != own) {
-          for (int p = lane; p < K; p += 32) { gains[p] = 0; losses[p] = 0; adelta[p] = 0; }
-          __syncwarp();
-          net_pass(I, metric, v, own, d, base, deg, gw * 32 + lane, nwarps * 32, nullptr, gains, losses, adelta);
-          __syncthreads();
-          for (int p = threadIdx.x; p < K; p += blockDim.x) {
-            int g = 0, l = 0, a = 0;
-            for (int x = 0; x < kSWarps; x++) {
-              g += gains_b[(size_t)x * K + p];
-              l += losses_b[(size_t)x * K + p];
-              a += adelta_b[(size_t)x * K + p];
+        if (d != own) {
+          const bool need = metric == kTV ? hc1 >= deg - cnt_b[d] : true;
+          mover = metric == kTV && need;
+          if (need) {
+            // records of all nets (every warp of the grid takes batches of 32)
+            if (vol) {
+              for (int p = lane; p < K; p += 32) { gains[p] = 0; losses[p] = 0; adelta[p] = 0; }
+              __syncwarp();
             }
-            if (g) atomicAdd(&hgain[p], g);
-            if (l) atomicAdd(&hloss[p], l);
-            if (a) atomicAdd(&hadelta[p], a);
+            locate_all(I, B, metric, v, own, d, base, deg, gw, nwarps, loc, gains, losses, adelta);
+            if (vol) {
+              __syncthreads();
+              for (int p = threadIdx.x; p < K; p += blockDim.x) {
+                int g = 0, l = 0, a = 0;
+                for (int x = 0; x < kSWarps; x++) {
+                  g += gains_b[(size_t)x * K + p];
+                  l += losses_b[(size_t)x * K + p];
+                  a += adelta_b[(size_t)x * K + p];
+                }
+                if (g) atomicAdd(&hgain[p], g);
+                if (l) atomicAdd(&hloss[p], l);
+                if (a) atomicAdd(&hadelta[p], a);
+              }
+            }
           }
         }
         if (!grid_barrier(B.bar, I.status)) return;
@@ -691,7 +739,7 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
         }
         if (mover) {
           for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < deg; i += gridDim.x * blockDim.x)
-            commit_net(I, v, own, d, (int)__ldg(&I.vnets[base + i]), vol ? &V : nullptr);
+            commit_rec(I, v, own, d, (int)__ldg(&I.vnets[base + i]), lds(&B.rec[base + i]), vol ? &V : nullptr);
           if (blockIdx.x == 0 && threadIdx.x == 0) {
             I.part_vec[v] = d;
             const int wv = __ldg(&I.w[v]);
@@ -739,12 +787,16 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
       const int z1 = min(z0 + q, end_w);
       // ---- A: evaluate
       int wsum = 0, vsum = 0;
+      const long long cA = clock64();
+      long long cV = 0;
+      int nV = 0;
       for (int z = z0; z < z1; z++) {
         const int o = z - pos;
         const int v = __ldg(&I.order[z]);
         const uint32_t base = __ldg(&I.vptr[v]);
         const int deg = (int)(__ldg(&I.vptr[v + 1]) - base);
-        if (deg > kHeavyDeg) continue;   // medium vertex: evaluated by the whole CTA below
+        if (__ldg(&B.vclass[v]) != 0) continue;   // medium vertex: evaluated by the whole CTA below
+        const long long cz = clock64();
         const int own = lds(&I.part_vec[v]);
         for (int p = lane; p < K; p += 32) { cnt[p] = 0; first[p] = ~0ull; }
         __syncwarp();
@@ -779,41 +831,34 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
           }
           if (lane == 0) B.ncand[o] = nc;
         }
-        unsigned char* nflag = B.nflag + (size_t)o * kHeavyDeg;
-        bool mover = false, mt = false;
+        // An isolated vertex (no nets, weight 0) changes nothing a later position
+        // reads; if its decision flips under the window's size drift, validation
+        // corrects it in place instead of cutting.  Its accept outcome does not
+        // depend on the destination (all gains and losses are zero).
+        const bool iso = deg == 0 && __ldg(&I.w[v]) == 0;
+        bool mover = false, mt = false, good = metric == kTV;
         int vs = kBig, vdd = 0;
-        if (d != own) {
-          if (metric == kTV) {
+        if (metric == kTV) {
+          if (d != own) {
             mover = c1 >= deg - cnt[d];
-            if (mover) net_pass(I, metric, v, own, d, base, deg, lane, 32, nflag, nullptr, nullptr, nullptr);
-          } else {
-            for (int p = lane; p < K; p += 32) { gains[p] = 0; losses[p] = 0; adelta[p] = 0; }
-            __syncwarp();
-            net_pass(I, metric, v, own, d, base, deg, lane, 32, nflag, gains, losses, adelta);
-            __syncwarp();
-            AcceptPart a = accept_partial(R, gains, losses, adelta, K, rv, lane, 32);
-            const bool fM = __any_sync(kAll, a.failM);
-            const bool fN = __any_sync(kAll, a.failN);
-            bool good;
-            accept_final(fM, fN, warp_max(a.fsl), warp_min(a.msl), &good, &vs);
-            mover = good;
-            mt = mover && __any_sync(kAll, a.mt);
-            vdd = warp_max(a.vd);
+            if (mover) locate_all(I, B, metric, v, own, d, base, deg, 0, 1, loc, nullptr, nullptr, nullptr);
           }
+        } else if (d != own || iso) {
+          for (int p = lane; p < K; p += 32) { gains[p] = 0; losses[p] = 0; adelta[p] = 0; }
+          __syncwarp();
+          if (d != own) locate_all(I, B, metric, v, own, d, base, deg, 0, 1, loc, gains, losses, adelta);
+          __syncwarp();
+          AcceptPart a = accept_partial(R, gains, losses, adelta, K, rv, lane, 32);
+          const bool fM = __any_sync(kAll, a.failM);
+          const bool fN = __any_sync(kAll, a.failN);
+          accept_final(fM, fN, warp_max(a.fsl), warp_min(a.msl), &good, &vs);
+          mover = good && d != own;
+          mt = mover && __any_sync(kAll, a.mt);
+          vdd = warp_max(a.vd);
         }
         __syncwarp();
         if (mover) {
-          // claims: part-set / source changes, or count-only changes
-          for (int k = lane; k < deg; k += 32) {
-            const int e = (int)__ldg(&I.vnets[base + k]);
-            const int fl = nflag[k];
-            if ((fl & 3) || (vol && (fl & 4))) {
-              atomicMin(&B.claim_m[e], z);
-            } else {
-              atomicMin(&B.claim_c[e], z);
-              atomicOr(&B.mask_c[e], (1u << (own & 31)) | (1u << (d & 31)));
-            }
-          }
+          claim_nets(I, B, vol, z, own, d, base, deg, lane, 32);
           if (lane == 0 && mt) atomicMin(&B.ctl[2 + par], z);
         }
         if (metric == kTV) {
@@ -826,7 +871,7 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
         const int wv = mover ? __ldg(&I.w[v]) : 0;
         if (lane == 0) {
           B.dec[o] = (own << 16) | d;   // own read now: part_vec changes in the commit phase
-          B.flag[o] = (unsigned char)((mover ? 1 : 0) | (special ? 2 : 0));
+          B.flag[o] = (unsigned char)((mover ? 1 : 0) | (special ? 2 : 0) | (iso ? 8 : 0) | (good ? 16 : 0));
           B.slack[o] = slack;
           B.vslack[o] = vs;
           B.wt[o] = wv;
@@ -834,19 +879,33 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
         }
         wsum += wv;
         vsum += mover ? vdd : 0;
+        cV += clock64() - cz;
+        nV++;
         __syncwarp();
+      }
+      if (lane == 0 && nV) {
+        // per-window statistics (cycles): slowest warp, and all light evaluations
+        atomicMax(&B.stats[22], (unsigned long long)(clock64() - cA));
+        atomicAdd(&B.stats[25], (unsigned long long)cV);
+        atomicAdd(&B.stats[26], (unsigned long long)nV);
       }
       // medium vertices of this CTA's positions: the CTA evaluates them together
       if (threadIdx.x < kSWarps) { s_mw[threadIdx.x] = 0; s_mv[threadIdx.x] = 0; }
       __syncthreads();
+      const long long cM = clock64();
       const int cz0 = min(pos + blockIdx.x * kSWarps * q, end_w);
       const int cz1 = min(cz0 + kSWarps * q, end_w);
       for (int mi = lower_bound_pos(B.mid_pos, B.nmid, cz0); mi < B.nmid; mi++) {
         const int z = __ldg(&B.mid_pos[mi]);
         if (z >= cz1) break;
-        cta_eval_ldg(I, B, R, metric, z, pos, par, q, cnt_b, first_b, gains_b, losses_b, adelta_b, iscr, s_mw, s_mv);
+        cta_eval_ldg(I, B, R, metric, z, pos, par, q, cnt_b, first_b, gains_b, losses_b, adelta_b, iscr, s_mw, s_mv,
+                     loc_b);
       }
       __syncthreads();
+      if (threadIdx.x == 0) {
+        const long long dm = clock64() - cM;
+        if (dm > 2000) atomicMax(&B.stats[24], (unsigned long long)dm);
+      }
       if (lane == 0) {
         B.wsum[gw] = wsum + s_mw[wib];
         B.vsum[gw] = vsum + s_mv[wib];
@@ -856,6 +915,10 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
         const unsigned long long tE = gtimer();
         B.stats[16] += tE - tA;
         tA = tE;
+        B.stats[21] += B.stats[22];   // no CTA writes these again before the next phase A
+        B.stats[22] = 0;
+        B.stats[23] += B.stats[24];
+        B.stats[24] = 0;
       }
       // ---- P: per-part prefix sums of the size changes of the window's movers
       // (exact part sizes at every window position).
@@ -927,7 +990,20 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
         if (!why && Dw > max(lds(&B.slack[o]), 0)) {
           // beyond the slack: decide again with the exact sizes at this position
           const int pk = lds(&B.dec[o]);
-          if (ldg_recheck(I, R, B, o, __ldg(&I.order[z]), pk >> 16, metric) != (pk & 0xffff)) why = 2;
+          const int own = pk >> 16;
+          const int d2 = ldg_recheck(I, R, B, o, __ldg(&I.order[z]), own, metric);
+          if (d2 != (pk & 0xffff)) {
+            if (fl & 8) {
+              // isolated vertex: take the exact decision (no weight, no nets, so
+              // no later position sees the difference)
+              if (lane == 0) {
+                B.dec[o] = (own << 16) | d2;
+                B.flag[o] = (unsigned char)((fl & ~1) | ((fl & 16) && d2 != own ? 1 : 0));
+              }
+            } else {
+              why = 2;
+            }
+          }
         }
         if (!why) why = Vw > max(lds(&B.vslack[o]), 0) ? 3 : mtpos < z ? 4 : 0;
         bool bad = why != 0;
@@ -937,20 +1013,7 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
           const bool mover = fl & 1;
           const uint32_t base = __ldg(&I.vptr[v]);
           const int deg = (int)(__ldg(&I.vptr[v + 1]) - base);
-          const unsigned ob = 1u << (own & 31);
-          const unsigned char* nflag = B.nflag + (size_t)o * kHeavyDeg;
-          bool conf = false;
-          for (int k = lane; k < deg; k += 32) {
-            const int e = (int)__ldg(&I.vnets[base + k]);
-            if (lds(&B.claim_m[e]) < z) conf = true;
-            if (lds(&B.claim_c[e]) < z) {
-              if (lds(&B.mask_c[e]) & ob) conf = true;
-              // a mover that changes this net's part set must not run next to
-              // earlier count updates on it
-              if (mover && ((nflag[k] & 3) || (vol && (nflag[k] & 4)))) conf = true;
-            }
-          }
-          bad = __any_sync(kAll, conf);
+          bad = __any_sync(kAll, conflicts(I, B, vol, z, own, mover, base, deg, lane, 32));
           why = 5;
         }
         if (bad) {
@@ -964,7 +1027,7 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
       for (int mi = lower_bound_pos(B.mid_pos, B.nmid, cz0); mi < B.nmid; mi++) {
         const int z = __ldg(&B.mid_pos[mi]);
         if (z >= cz1) break;
-        cta_validate_ldg(I, B, R, metric, z, pos, par, q, mtpos, s_pre_w, s_pre_v, iscr);
+        cta_validate_ldg(I, B, R, metric, z, pos, q, par, mtpos, s_pre_w, s_pre_v);
       }
       if (!grid_barrier(B.bar, I.status)) return;
       // ---- C: commit every mover before the cut.
@@ -993,7 +1056,8 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
         const uint32_t base = __ldg(&I.vptr[v]);
         const int deg = (int)(__ldg(&I.vptr[v + 1]) - base);
         if (z < cut) {
-          for (int k = lane; k < deg; k += 32) commit_net(I, v, own, d, (int)__ldg(&I.vnets[base + k]), vol ? &V : nullptr);
+          for (int k = lane; k < deg; k += 32)
+            commit_rec(I, v, own, d, (int)__ldg(&I.vnets[base + k]), lds(&B.rec[base + k]), vol ? &V : nullptr);
           if (lane == 0) {
             atomicAdd(&B.stats[2], 1ull);
             I.part_vec[v] = d;
@@ -1023,7 +1087,7 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
         const int deg = (int)(__ldg(&I.vptr[v + 1]) - base);
         if (z < cut) {
           for (int k = threadIdx.x; k < deg; k += blockDim.x)
-            commit_net(I, v, own, d, (int)__ldg(&I.vnets[base + k]), vol ? &V : nullptr);
+            commit_rec(I, v, own, d, (int)__ldg(&I.vnets[base + k]), lds(&B.rec[base + k]), vol ? &V : nullptr);
           if (threadIdx.x == 0) {
             atomicAdd(&B.stats[2], 1ull);
             I.part_vec[v] = d;

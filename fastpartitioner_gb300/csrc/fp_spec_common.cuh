@@ -14,12 +14,6 @@ constexpr int kSThreads = 256;
 constexpr int kSWarps = kSThreads / 32;
 constexpr int kNone = 0x7fffffff;
 constexpr unsigned kAll = 0xffffffffu;
-// Vertices with more nets than this are "heavy": they get a round of their own
-// in which every warp of the grid tallies a slice of their nets.
-constexpr int kHeavyDeg = 256;
-// Vertices with more nets than this get a whole-grid round (the LDG metrics;
-// those in between are evaluated inside a window by one CTA).
-constexpr int kSuperDeg = 16384;
 
 // Global nanosecond timer (per-phase time statistics).
 __device__ __forceinline__ unsigned long long gtimer() {
@@ -162,8 +156,13 @@ __device__ __forceinline__ int tally_batch(const DevInstance& I, int own, uint32
       key_slot[u] = j;
       aa[u] = f < total ? sl + j : -1;          // slot address, -1 past the end
     }
+    int cc[kU];
+    // parts and counts are loaded together: no second round trip for own's count
 #pragma unroll
-    for (int u = 0; u < kU; u++) pp[u] = aa[u] >= 0 ? lds(&I.ep_part[aa[u]]) : -1;
+    for (int u = 0; u < kU; u++) {
+      pp[u] = aa[u] >= 0 ? lds(&I.ep_part[aa[u]]) : -1;
+      cc[u] = aa[u] >= 0 ? lds(&I.ep_cnt[aa[u]]) : 0;
+    }
 #pragma unroll
     for (int u = 0; u < kU; u++) {
       if (aa[u] < 0) continue;
@@ -174,10 +173,114 @@ __device__ __forceinline__ int tally_batch(const DevInstance& I, int own, uint32
       }
       atomicAdd(&cnt[p], 1);
       atomicMin(&first[p], ((unsigned long long)key_net[u] << 32) | (unsigned)key_slot[u]);
-      if (p == own && lds(&I.ep_cnt[aa[u]]) == 1) c1++;
+      if (p == own && cc[u] == 1) c1++;
     }
   }
   return c1;
+}
+
+// Record of one (vertex, net) pair of a vertex about to move own -> d, one
+// 32-bit word at the pair's vnets index: the slot of `own` in the net's list,
+// the slot of `d` (kNoSlot: not listed), own's count there is 1 (the move takes
+// own off the list), v is the net's source.  The slots stay valid until the
+// move is committed: a net whose part set changes has no other mover in the
+// round, and count-only moves never move slots.
+constexpr uint32_t kNoSlot = 0x1fffu;   // slots < K <= 4096
+__device__ __forceinline__ uint32_t rec_pack(int jo, int jd, bool rem, bool src) {
+  return (uint32_t)jo | ((uint32_t)(jd < 0 ? kNoSlot : (uint32_t)jd) << 13) | (rem ? 1u << 26 : 0u) |
+         (src ? 1u << 27 : 0u);
+}
+__device__ __forceinline__ int rec_jo(uint32_t r) { return (int)(r & 0x1fffu); }
+__device__ __forceinline__ int rec_jd(uint32_t r) {
+  const uint32_t j = (r >> 13) & 0x1fffu;
+  return j == kNoSlot ? -1 : (int)j;
+}
+__device__ __forceinline__ bool rec_rem(uint32_t r) { return (r >> 26) & 1u; }
+__device__ __forceinline__ bool rec_add(uint32_t r) { return ((r >> 13) & 0x1fffu) == kNoSlot; }
+__device__ __forceinline__ bool rec_src(uint32_t r) { return (r >> 27) & 1u; }
+// The move changes the net's part set (or, with volumes, the net's send side).
+__device__ __forceinline__ bool rec_setchange(uint32_t r, bool vol) {
+  return rec_rem(r) || rec_add(r) || (vol && rec_src(r));
+}
+
+// Writes the records of nets [nb, nb + 32) of v for the move own -> d into
+// rec[base + k].  Slots of the 32 lists are flattened across the warp as in
+// tally_batch.  sj / sd / sc: 32 ints each of per-warp scratch.  Returns the
+// record of this lane's net nb + lane and its net id in *e_out (-1 past deg).
+__device__ __forceinline__ uint32_t locate_batch(const DevInstance& I, uint32_t* rec, int v, int own, int d,
+                                                 uint32_t base, int nb, int deg, int* sj, int* sd, int* sc,
+                                                 int* e_out) {
+  const int lane = threadIdx.x & 31;
+  const int k = nb + lane;
+  int s = 0, n = 0, e = -1;
+  if (k < deg) {
+    e = (int)__ldg(&I.vnets[base + k]);
+    s = (int)__ldg(&I.nptr[e]);
+    const int cap = (int)__ldg(&I.nptr[e + 1]) - s;
+    n = lds(&I.ep_len[e]);
+    if (n < 0 || n > cap) { dev_fail(I.status, kDevErrInvalid); n = 0; }
+  }
+  sj[lane] = -1;
+  sd[lane] = -1;
+  sc[lane] = 0;
+  int incl = n;
+  for (int off = 1; off < 32; off <<= 1) {
+    const int t = __shfl_up_sync(kAll, incl, off);
+    if (lane >= off) incl += t;
+  }
+  const int total = __shfl_sync(kAll, incl, 31);
+  __syncwarp();
+  constexpr int kU = 4;
+  for (int f0 = 0; f0 < total; f0 += 32 * kU) {
+    int aa[kU], kn[kU], kj[kU], pp[kU];
+#pragma unroll
+    for (int u = 0; u < kU; u++) {
+      const int f = f0 + u * 32 + lane;
+      int lo = 0, hi = 31;
+#pragma unroll
+      for (int it = 0; it < 5; it++) {
+        const int mid = (lo + hi) >> 1;
+        const int val = __shfl_sync(kAll, incl, mid);
+        if (f < val) hi = mid; else lo = mid + 1;
+      }
+      const int sl = __shfl_sync(kAll, s, lo);
+      const int nl = __shfl_sync(kAll, n, lo);
+      const int il = __shfl_sync(kAll, incl, lo);
+      kn[u] = lo;
+      kj[u] = f - (il - nl);
+      aa[u] = f < total ? sl + kj[u] : -1;
+    }
+    int cc[kU];
+#pragma unroll
+    for (int u = 0; u < kU; u++) {
+      pp[u] = aa[u] >= 0 ? lds(&I.ep_part[aa[u]]) : -1;
+      cc[u] = aa[u] >= 0 ? lds(&I.ep_cnt[aa[u]]) : 0;
+    }
+#pragma unroll
+    for (int u = 0; u < kU; u++) {
+      if (aa[u] < 0) continue;
+      // own and d are listed at most once per net: one writer per entry
+      if (pp[u] == own) {
+        sj[kn[u]] = kj[u];
+        sc[kn[u]] = cc[u] == 1;
+      }
+      if (pp[u] == d) sd[kn[u]] = kj[u];
+    }
+  }
+  __syncwarp();
+  uint32_t r = 0;
+  if (k < deg) {
+    const int jo = sj[lane];
+    if (jo < 0) {
+      dev_fail(I.status, kDevErrInvalid);   // v's own part must be listed on v's nets
+    } else {
+      r = rec_pack(jo, sd[lane], sc[lane] != 0, __ldg(&I.src[e]) == v);
+      rec[base + k] = r;
+    }
+  }
+  __syncwarp();
+  *e_out = e;
+  return r;
 }
 
 // Volume arrays updated while a vertex moves (MSV: send only; MSRV: both).
@@ -185,6 +288,53 @@ struct Vol {
   int* send;
   int* recv;
 };
+
+// commit_net with the slots taken from the move's record (no list search).
+__device__ __forceinline__ void commit_rec(const DevInstance& I, int v, int own, int d, int e, uint32_t r,
+                                           const Vol* vol) {
+  const int s = (int)__ldg(&I.nptr[e]);
+  const int cap = (int)__ldg(&I.nptr[e + 1]) - s;
+  int n = lds(&I.ep_len[e]);
+  const int jo = rec_jo(r);
+  int jd = rec_jd(r);
+  if (jo >= n || jd >= n || n > cap || (jd < 0 && n == cap && !rec_rem(r))) {
+    dev_fail(I.status, kDevErrInvalid);
+    return;
+  }
+  const int sv = vol ? __ldg(&I.src[e]) : -1;
+  const int sp = (vol && sv != v) ? lds(&I.part_vec[sv]) : d;
+  if (vol && sv == v) atomicAdd(&vol->send[own], -(n - 1));
+  const int co = atomicAdd(&I.ep_cnt[s + jo], -1) - 1;
+  if (co == 0) {
+    const int last = n - 1;
+    I.ep_part[s + jo] = lds(&I.ep_part[s + last]);
+    I.ep_cnt[s + jo] = lds(&I.ep_cnt[s + last]);
+    I.ep_part[s + last] = -1;
+    I.ep_cnt[s + last] = 0;
+    if (jd == last) jd = jo;
+    n = last;
+    if (vol && sv != v) {
+      atomicAdd(&vol->send[sp], -1);
+      if (vol->recv) atomicAdd(&vol->recv[own], -1);
+    }
+  } else {
+    if (vol && vol->recv && sv == v) atomicAdd(&vol->recv[own], 1);
+  }
+  if (vol && sv == v) atomicAdd(&vol->send[d], n - 1);
+  if (jd >= 0) {
+    atomicAdd(&I.ep_cnt[s + jd], 1);
+    if (vol && vol->recv && sv == v) atomicAdd(&vol->recv[d], -1);
+  } else {
+    I.ep_part[s + n] = d;
+    I.ep_cnt[s + n] = 1;
+    n++;
+    if (vol) {
+      atomicAdd(&vol->send[sp], 1);
+      if (vol->recv && sv != v) atomicAdd(&vol->recv[d], 1);
+    }
+  }
+  if (co == 0 || jd < 0) I.ep_len[e] = n;
+}
 
 // One thread applies vertex v's move own -> d to net e: the reference's
 // REMOVAL (decrement, swap-with-last when the count reaches zero) then ADDING

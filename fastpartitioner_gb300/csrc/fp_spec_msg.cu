@@ -8,7 +8,7 @@
 // matrix); the first mover ends the window, all vertices before it are
 // non-movers decided on exactly the sequential state, and the mover's move --
 // lists, connection counts, message counts, zero masks -- is applied by warps
-// of the whole grid.  Vertices with more than kHeavyDeg nets get a round of
+// of the whole grid.  Vertices with more than 256 nets get a round of
 // their own in which the whole grid computes their gain sets.
 
 #include "fp_spec_common.cuh"

@@ -126,6 +126,11 @@ int fp_set_engine(fp_instance* inst, int32_t engine);
 /* All six metrics of the current device state, in FP_OUT_* order
  * (shared/metric.cpp: TV_Refined, CN, TM_scratch, MGM_scratch, MGV_Scratch,
  * MGAV_Scratch). */
+/* Tuning of the speculative engine for TV / MSV / MSRV (no effect on results):
+ * a vertex whose work -- the sum over its nets of min(net size, K) -- is at
+ * most light_work is evaluated by one warp, at most super_work by one CTA,
+ * above it in a whole-grid round.  Defaults: 2048 and 262144 (MSV: 65536). */
+int fp_set_classes(fp_instance* inst, int64_t light_work, int64_t super_work);
 int fp_metrics(fp_instance* inst, int64_t out[6]);
 
 /* Copies of the current device state (caller-allocated host buffers). */
@@ -140,7 +145,10 @@ int fp_get_moves(fp_instance* inst, int64_t* moves, int32_t n);
  * committed from windows, [3..8] windows ended by: nothing (fully valid), a
  * possibly stale TV marker, part-size drift, volume drift, a max-volume part
  * changing, a shared net; [9] vertices walked in windows; [16..19] nanoseconds
- * in evaluate, validate, commit phases and single-vertex rounds. */
+ * in evaluate, validate, commit phases and single-vertex rounds; TV / MSV /
+ * MSRV also: [20] nanoseconds computing the round state, [21] / [23] SM cycles
+ * summed over windows of the slowest warp / CTA evaluation, [25] / [26] SM
+ * cycles and count of warp evaluations. */
 int fp_get_stats(fp_instance* inst, int64_t* out, int32_t n);
 /* Number of kernel launches the last fp_refine / fp_metrics call enqueued. */
 int fp_last_launches(fp_instance* inst, int64_t* launches);
@@ -194,8 +202,9 @@ typedef struct fp_state {
   int32_t* ep_cnt;
   int32_t* part_sizes;  /* NULL on set: recounted from part_vec and the weights    */
   int32_t* marker;      /* TV's last scanner per part; NULL on set: all -1         */
-  int32_t* send;        /* MSV / MSRV send volumes; NULL on set: recounted         */
-  int32_t* recv;        /* MSRV received volumes; NULL on set: recounted           */
+  int32_t* send;        /* MSV / MSRV send volumes; NULL on set: recounted (other
+                           metrics keep none: ignored on set, zero on get)         */
+  int32_t* recv;        /* MSRV received volumes; NULL on set: recounted (ditto)   */
   int32_t* conn;        /* TM / MSM part_connections; NULL on set: recounted       */
   int32_t* msgs;        /* TM / MSM part_messages; NULL on set: recounted          */
 } fp_state;
