@@ -389,7 +389,7 @@ class Instance:
         b = 4 * (self.hg.nov + self.hg.noe + 2 * self.hg.pins) + 4 * 5 * K
         if m in (2, 3):
             words = (K + 31) // 32
-            b += 4 * K * K + 2 * 4 * K * words
+            b += 4 * K * K + 4 * 4 * K * words   # conn, zero masks, conn == 1 masks
         return b
 
     def set_classes(self, light_work: int, super_work: int) -> None:

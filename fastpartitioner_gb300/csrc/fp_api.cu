@@ -23,11 +23,19 @@ cudaError_t launch_spec_msg(const DevInstance& I, const SpecBuf& B, int passes, 
                             int* grid_out);
 cudaError_t launch_spec_cn(const DevInstance& I, const SpecBuf& B, int passes, int num_sms, cudaStream_t st,
                            int* grid_out);
-// Metrics the speculative grid-wide engine covers.
-static bool spec_supported(int metric) {
-  return metric >= FP_METRIC_CN && metric <= FP_METRIC_MSRV;
+size_t spec_ldg_smem_bytes(int K);
+size_t spec_msg_smem_bytes(int K);
+// The speculative grid-wide engine covers every metric as long as its shared
+// memory fits a CTA (per-warp K-sized arrays); above that K the single-CTA walk
+// refines (same results).
+static bool spec_supported(int metric, int K, int max_smem) {
+  if (metric < FP_METRIC_CN || metric > FP_METRIC_MSRV) return false;
+  const size_t static_smem = 8192;   // the kernels' static shared arrays, with room to spare
+  if (metric == FP_METRIC_TM || metric == FP_METRIC_MSM)
+    return spec_msg_smem_bytes(K) + static_smem <= (size_t)max_smem;
+  if (metric == FP_METRIC_CN) return true;
+  return spec_ldg_smem_bytes(K) + static_smem <= (size_t)max_smem;
 }
-constexpr int kHeavyDegHost = 256;     // TM / MSM: vertices with more nets get a whole-grid round
 // LDG metrics: vertex classes by work = sum over its nets of min(net size, K),
 // the list slots an evaluation reads at most.  Light: one warp; medium: one CTA
 // inside the window; above the super bound (or with 65536 nets or more, the
@@ -46,6 +54,7 @@ using namespace fp;
 struct fp_ctx {
   int device = 0;
   int num_sms = 0;
+  int max_smem = 0;   // opt-in shared memory per CTA
   cudaStream_t own = nullptr;
   cudaStream_t stream = nullptr;
 };
@@ -73,8 +82,6 @@ struct fp_instance {
   std::vector<int> mid_pos;       // CTA-evaluated vertices, by position
   int* mid_pos_d = nullptr;
   unsigned char* vclass_d = nullptr;
-  std::vector<int> heavy_ids;     // heavy vertices by id (TM / MSM walk ids)
-  int* heavy_ids_d = nullptr;
 };
 
 namespace {
@@ -82,6 +89,7 @@ namespace {
 const int kMaxPasses = 4096;
 const int kMaxK = 4096;
 const int kSpecWindow = 16384;   // longest speculative window (vertices)
+const int kMsgWindow = 65536;    // longest TM / MSM window
 
 int cuda_status(cudaError_t e) {
   if (e == cudaSuccess) return FP_OK;
@@ -177,20 +185,29 @@ int upload_state(fp_instance* in) {
   cp(d.send, st.send.data(), sizeof(int) * K);
   cp(d.recv, st.recv.data(), sizeof(int) * K);
   cp(d.msgs, st.msgs.data(), sizeof(int) * K);
-  std::vector<uint32_t> zr, zc;
+  std::vector<uint32_t> zr, zc, c1r, c1c;
   if (in->pb.metric == FP_METRIC_TM || in->pb.metric == FP_METRIC_MSM) {
     const int words = (K + 31) / 32;
     zr.assign((size_t)K * words, 0);
     zc.assign((size_t)K * words, 0);
+    c1r.assign((size_t)K * words, 0);
+    c1c.assign((size_t)K * words, 0);
     for (int a = 0; a < K; a++)
-      for (int b = 0; b < K; b++)
-        if (st.conn[(size_t)a * K + b] == 0) {
+      for (int b = 0; b < K; b++) {
+        const int c = st.conn[(size_t)a * K + b];
+        if (c == 0) {
           zr[(size_t)a * words + (b >> 5)] |= 1u << (b & 31);
           zc[(size_t)b * words + (a >> 5)] |= 1u << (a & 31);
+        } else if (c == 1) {
+          c1r[(size_t)a * words + (b >> 5)] |= 1u << (b & 31);
+          c1c[(size_t)b * words + (a >> 5)] |= 1u << (a & 31);
         }
+      }
     cp(d.conn, st.conn.data(), sizeof(int) * st.conn.size());
     cp(d.zrow, zr.data(), sizeof(uint32_t) * zr.size());
     cp(d.zcol, zc.data(), sizeof(uint32_t) * zc.size());
+    cp(d.c1row, c1r.data(), sizeof(uint32_t) * c1r.size());
+    cp(d.c1col, c1c.data(), sizeof(uint32_t) * c1c.size());
   }
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);  // host vectors are pageable
   return cuda_status(e);
@@ -228,6 +245,7 @@ int fp_ctx_create(int32_t device, fp_ctx** out) {
   if (!c) return FP_ERR_NOMEM;
   c->device = device;
   cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
+  cudaDeviceGetAttribute(&c->max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
   e = cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking);
   if (e != cudaSuccess) { delete c; return cuda_status(e); }
   c->stream = c->own;
@@ -274,8 +292,11 @@ static int classify(fp_instance* in, long long light_work, long long super_work)
   std::vector<unsigned char> cls(g.nov, 0);
   in->heavy_pos.clear();
   in->mid_pos.clear();
+  // TM and MSM walk the vertices in id order (TM/partition.cpp:300), the others
+  // in the visiting order.
+  const bool by_id = pb.metric == FP_METRIC_TM || pb.metric == FP_METRIC_MSM;
   for (int z = 0; z < g.nov; z++) {
-    const int v = pb.order[z];
+    const int v = by_id ? z : pb.order[z];
     long long work = 0;
     for (uint32_t k = g.vptr[v]; k < g.vptr[v + 1]; k++) {
       const uint32_t e = g.vnets[k];
@@ -345,9 +366,6 @@ int fp_instance_create(fp_ctx* ctx, const fp_hypergraph* h, int32_t K, int32_t m
   d.C = pb.C;
   d.max_pw = (int)(pb.xw + (pb.xw * 0.1));
   d.min_pw = (int)(pb.xw - (pb.xw * 0.1));
-  in->heavy_ids.clear();
-  for (int v = 0; v < g.nov; v++)
-    if ((int)(g.vptr[v + 1] - g.vptr[v]) > kHeavyDegHost) in->heavy_ids.push_back(v);
   const size_t KK = (size_t)K * K, words = (size_t)(K + 31) / 32;
   const bool msg = metric == FP_METRIC_TM || metric == FP_METRIC_MSM;
   uint32_t *vptr, *vnets, *nptr, *npins;
@@ -359,8 +377,9 @@ int fp_instance_create(fp_ctx* ctx, const fp_hypergraph* h, int32_t K, int32_t m
       (rc = dalloc(in, &d.part_sizes, K)) || (rc = dalloc(in, &d.marker, K)) || (rc = dalloc(in, &d.send, K)) ||
       (rc = dalloc(in, &d.recv, K)) || (rc = dalloc(in, &d.msgs, K)) || (rc = dalloc(in, &d.conn, msg ? KK : 1)) ||
       (rc = dalloc(in, &d.zrow, msg ? K * words : 1)) || (rc = dalloc(in, &d.zcol, msg ? K * words : 1)) ||
+      (rc = dalloc(in, &d.c1row, msg ? K * words : 1)) || (rc = dalloc(in, &d.c1col, msg ? K * words : 1)) ||
       (rc = dalloc(in, &d.moves, kMaxPasses)) || (rc = dalloc(in, &d.status, 1)) ||
-      (rc = dalloc(in, &in->sb.ctl, 8)) || (rc = dalloc(in, &in->sb.bar, 4)) || (rc = dalloc(in, &in->sb.stats, 32)) || (rc = dalloc(in, &in->sb.dec, kSpecWindow)) ||
+      (rc = dalloc(in, &in->sb.ctl, 8)) || (rc = dalloc(in, &in->sb.bar, 4)) || (rc = dalloc(in, &in->sb.stats, 32)) || (rc = dalloc(in, &in->sb.dec, std::max(kSpecWindow, kMsgWindow))) ||
       (rc = dalloc(in, &in->sb.flag, kSpecWindow)) || (rc = dalloc(in, &in->sb.slack, kSpecWindow)) ||
       (rc = dalloc(in, &in->sb.vslack, kSpecWindow)) || (rc = dalloc(in, &in->sb.wt, kSpecWindow)) ||
       (rc = dalloc(in, &in->sb.vd, kSpecWindow)) || (rc = dalloc(in, &in->sb.scan, (size_t)kSpecWindow * words)) ||
@@ -373,7 +392,6 @@ int fp_instance_create(fp_ctx* ctx, const fp_hypergraph* h, int32_t K, int32_t m
       (rc = dalloc(in, &in->sb.hfirst, 2 * K)) || (rc = dalloc(in, &in->sb.hgain, 2 * K)) ||
       (rc = dalloc(in, &in->sb.hloss, 2 * K)) || (rc = dalloc(in, &in->sb.hadelta, 2 * K)) ||
       (rc = dalloc(in, &in->sb.hmisc, 16)) || (rc = dalloc(in, &in->heavy_pos_d, g.nov)) ||
-      (rc = dalloc(in, &in->heavy_ids_d, std::max<size_t>(in->heavy_ids.size(), 1))) ||
       (rc = dalloc(in, &in->mid_pos_d, g.nov)) ||
       (rc = dalloc(in, &in->metric_out, 8))) {
     fp_instance_destroy(in);
@@ -385,6 +403,7 @@ int fp_instance_create(fp_ctx* ctx, const fp_hypergraph* h, int32_t K, int32_t m
   in->allocs.push_back(ms);
   in->metric_scratch = ms;
   in->sb.wmax = kSpecWindow;
+  in->sb.wmax_msg = kMsgWindow;
   in->sb.max_warps = kMaxSpecWarps;
   in->sb.heavy_pos = in->heavy_pos_d;
   in->sb.mid_pos = in->mid_pos_d;
@@ -392,9 +411,6 @@ int fp_instance_create(fp_ctx* ctx, const fp_hypergraph* h, int32_t K, int32_t m
   {
     cudaStream_t s0 = ctx->stream;
     e = clear_spec_scratch(in->sb, g.noe, K, s0);
-    if (e == cudaSuccess && !in->heavy_ids.empty())
-      e = cudaMemcpyAsync(in->heavy_ids_d, in->heavy_ids.data(), sizeof(int) * in->heavy_ids.size(),
-                          cudaMemcpyHostToDevice, s0);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s0);
     if (e != cudaSuccess) { fp_instance_destroy(in); return cuda_status(e); }
     rc = classify(in, kLightWork, default_super_work(metric));
@@ -459,7 +475,8 @@ int fp_refine(fp_instance* in, int32_t passes) {
   cudaStream_t s = in->ctx->stream;
   cudaError_t e = cudaMemsetAsync(in->d.moves, 0, sizeof(long long) * passes, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(in->d.status, 0, sizeof(int), s);
-  const bool spec = in->engine == FP_ENGINE_AUTO && spec_supported(in->pb.metric);
+  const bool spec =
+      in->engine == FP_ENGINE_AUTO && spec_supported(in->pb.metric, in->pb.K, in->ctx->max_smem);
   if (spec) {
     static const int none[8] = {0x7fffffff, 0x7fffffff, 0x7fffffff, 0x7fffffff,
                                 0x7fffffff, 0x7fffffff, 0x7fffffff, 0x7fffffff};
@@ -472,11 +489,7 @@ int fp_refine(fp_instance* in, int32_t passes) {
         e = cudaMemsetAsync(in->sb.claim64, 0, sizeof(unsigned long long) * std::max(in->g.noe, 1), s);
         if (e == cudaSuccess) e = launch_spec_cn(in->d, in->sb, passes, in->ctx->num_sms, s, &in->last_grid);
       } else if (in->pb.metric == FP_METRIC_TM || in->pb.metric == FP_METRIC_MSM) {
-        SpecBuf b = in->sb;
-        b.heavy_pos = in->heavy_ids_d;
-        b.nheavy = (int)in->heavy_ids.size();
-        b.nmid = 0;
-        e = launch_spec_msg(in->d, b, passes, in->ctx->num_sms, s, &in->last_grid);
+        e = launch_spec_msg(in->d, in->sb, passes, in->ctx->num_sms, s, &in->last_grid);
       } else {
         e = launch_spec_ldg(in->d, in->sb, passes, in->ctx->num_sms, s, &in->last_grid);
       }

@@ -39,6 +39,8 @@ struct DevInstance {
   int* msgs;         // K (TM, MSM)
   uint32_t* zrow;    // K*K/32 bits: conn[k][r] == 0 (TM, MSM)
   uint32_t* zcol;    // K*K/32 bits: conn[s][k] == 0, column-major (TM, MSM)
+  uint32_t* c1row;   // K*K/32 bits: conn[a][b] == 1 (TM, MSM)
+  uint32_t* c1col;   // K*K/32 bits: conn[a][b] == 1, column-major (TM, MSM)
   // bookkeeping
   long long* moves;  // per pass
   int* status;       // device status word, 0 = ok
@@ -81,7 +83,8 @@ struct SpecBuf {
   int* hadelta;          // [2*K]
   int* hmisc;            // [16]
   unsigned long long* stats;  // [32] round statistics (see fp_get_stats)
-  int wmax;
+  int wmax;              // longest window of the LDG and CN engines
+  int wmax_msg;          // longest window of the TM / MSM engine (dec only)
   int max_warps;
 };
 

@@ -417,6 +417,10 @@ __device__ __forceinline__ void conn_add(const DevInstance& I, int* msgs, int a,
     atomicXor(&I.zrow[(size_t)a * words + (b >> 5)], 1u << (b & 31));
     atomicXor(&I.zcol[(size_t)b * words + (a >> 5)], 1u << (a & 31));
   }
+  if ((old == 1) != (now == 1)) {   // same parity argument for [value == 1]
+    atomicXor(&I.c1row[(size_t)a * words + (b >> 5)], 1u << (b & 31));
+    atomicXor(&I.c1col[(size_t)b * words + (a >> 5)], 1u << (a & 31));
+  }
 }
 
 __global__ void __launch_bounds__(kThreads, 1) refine_msg_kernel(DevInstance I, int passes, int msm) {

@@ -223,15 +223,17 @@ __device__ __forceinline__ void net_terms(const DevInstance& I, bool rv, int v, 
 }
 
 // Records of v's nets for the move own -> d; warp wi of a group of nw warps
-// takes the batches of 32 nets wi, wi + nw, ...  With volumes (MSV / MSRV) the
+// takes a contiguous share of the nets (net_range).  With volumes (MSV / MSRV) the
 // gain / loss / volume terms are added to the warp's arrays.  loc: the warp's
 // 96 ints of scratch.
 __device__ void locate_all(const DevInstance& I, const SpecBuf& B, int metric, int v, int own, int d,
                            uint32_t base, int deg, int wi, int nw, int* loc, int* gains, int* losses, int* adelta) {
   const bool vol = metric != kTV, rv = metric == kMSRV;
-  for (int nb = wi * 32; nb < deg; nb += nw * 32) {
+  int n0, n1;
+  net_range(deg, wi, nw, &n0, &n1);
+  for (int nb = n0; nb < n1; nb += 32) {
     int e;
-    const uint32_t r = locate_batch(I, B.rec, v, own, d, base, nb, deg, loc, loc + 32, loc + 64, &e);
+    const uint32_t r = locate_batch(I, B.rec, v, own, d, base, nb, n1, loc, loc + 32, loc + 64, &e);
     if (vol && e >= 0) net_terms(I, rv, v, own, d, e, r, gains, losses, adelta);
   }
 }
@@ -307,16 +309,6 @@ __device__ __forceinline__ void accept_final(bool failM, bool failN, int fsl, in
   *vslack = *good ? msl : (failM ? kBig : fsl);
 }
 
-// First index of the ascending list `pos_list` (n entries) with value >= x.
-__device__ __forceinline__ int lower_bound_pos(const int* pos_list, int n, int x) {
-  int lo = 0, hi = n;
-  while (lo < hi) {
-    const int mid = (lo + hi) >> 1;
-    if (__ldg(&pos_list[mid]) < x) lo = mid + 1; else hi = mid;
-  }
-  return lo;
-}
-
 __device__ __forceinline__ int block_reduce_max(int x, int* scr) {
   x = warp_max(x);
   __syncthreads();
@@ -353,7 +345,11 @@ __device__ void cta_eval_ldg(const DevInstance& I, const SpecBuf& B, const Round
   for (int p = lane; p < K; p += 32) { cnt[p] = 0; first[p] = ~0ull; }
   __syncwarp();
   int c1 = 0;
-  for (int nb = wib * 32; nb < deg; nb += kSWarps * 32) c1 += tally_batch(I, own, base, nb, deg, cnt, first);
+  {
+    int n0, n1;
+    net_range(deg, wib, kSWarps, &n0, &n1);
+    for (int nb = n0; nb < n1; nb += 32) c1 += tally_batch(I, own, base, nb, n1, cnt, first);
+  }
   c1 = warp_sum(c1);
   __syncthreads();
   if (lane == 0) iscr[wib] = c1;
@@ -661,7 +657,11 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
         for (int p = lane; p < K; p += 32) { cnt[p] = 0; first[p] = ~0ull; }
         __syncwarp();
         int c1 = 0;
-        for (int nb = gw * 32; nb < deg; nb += nwarps * 32) c1 += tally_batch(I, own, base, nb, deg, cnt, first);
+        {
+          int n0, n1;
+          net_range(deg, gw, nwarps, &n0, &n1);
+          for (int nb = n0; nb < n1; nb += 32) c1 += tally_batch(I, own, base, nb, n1, cnt, first);
+        }
         c1 = warp_sum(c1);
         __syncthreads();
         for (int p = threadIdx.x; p < K; p += blockDim.x) {

@@ -108,8 +108,26 @@ struct Carve {
   }
 };
 
-// Adds to the warp's part tally the nets [nb, nb + 32) of a vertex (base: its
-// offset in vnets, deg: its net count): for every listed part, the number of
+// First index of the ascending list `pos_list` (n entries) with value >= x.
+__device__ __forceinline__ int lower_bound_pos(const int* pos_list, int n, int x) {
+  int lo = 0, hi = n;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (__ldg(&pos_list[mid]) < x) lo = mid + 1; else hi = mid;
+  }
+  return lo;
+}
+
+// Contiguous share [*b, *e) of a vertex's deg nets for warp wi of nw warps
+// (balances vertices with few large nets across the warps of a group).
+__device__ __forceinline__ void net_range(int deg, int wi, int nw, int* b, int* e) {
+  const int g = (deg + nw - 1) / nw;
+  *b = min(wi * g, deg);
+  *e = min(*b + g, deg);
+}
+
+// Adds to the warp's part tally the nets [nb, min(nb + 32, deg)) of a vertex
+// (base: its offset in vnets; deg: the end of the warp's nets): for every listed part, the number of
 // nets listing it (cnt) and the (net index, slot) of its first sighting (first);
 // returns this lane's count of nets where `own` has exactly one pin.  Slots of
 // the 32 nets are flattened across the warp (inclusive scan of list lengths).
@@ -389,6 +407,55 @@ __device__ __forceinline__ void commit_net(const DevInstance& I, int v, int own,
     }
   }
   I.ep_len[e] = n;
+}
+
+// One warp applies v's move own -> d to the list of net e (REMOVAL then ADDING,
+// as commit_net, without volumes); the lanes search the slots of own and d
+// together.  The net must have no other mover at the same time.  Returns the
+// list length after the move (every lane).
+__device__ __forceinline__ int commit_net_warp(const DevInstance& I, int own, int d, int e) {
+  const int lane = threadIdx.x & 31;
+  const int s = (int)__ldg(&I.nptr[e]);
+  const int cap = (int)__ldg(&I.nptr[e + 1]) - s;
+  int n = lds(&I.ep_len[e]);
+  int jo = -1, jd = -1;
+  for (int j0 = 0; j0 < n; j0 += 32) {
+    const int j = j0 + lane;
+    const int p = j < n ? lds(&I.ep_part[s + j]) : -1;
+    const unsigned mo = __ballot_sync(kAll, p == own);
+    const unsigned md = __ballot_sync(kAll, p == d);
+    if (mo && jo < 0) jo = j0 + __ffs(mo) - 1;
+    if (md && jd < 0) jd = j0 + __ffs(md) - 1;
+  }
+  const int co = jo >= 0 ? lds(&I.ep_cnt[s + jo]) : 0;
+  if (jo < 0 || n > cap || (jd < 0 && n == cap && co > 1)) {
+    if (lane == 0) dev_fail(I.status, kDevErrInvalid);
+    return n;
+  }
+  if (lane == 0) {
+    if (co == 1) {
+      const int last = n - 1;
+      I.ep_part[s + jo] = lds(&I.ep_part[s + last]);
+      I.ep_cnt[s + jo] = lds(&I.ep_cnt[s + last]);
+      I.ep_part[s + last] = -1;
+      I.ep_cnt[s + last] = 0;
+      if (jd == last) jd = jo;
+      n = last;
+    } else {
+      I.ep_cnt[s + jo] = co - 1;
+    }
+    if (jd >= 0) {
+      I.ep_cnt[s + jd] = lds(&I.ep_cnt[s + jd]) + 1;
+    } else {
+      I.ep_part[s + n] = d;
+      I.ep_cnt[s + n] = 1;
+      n++;
+    }
+    I.ep_len[e] = n;
+  }
+  n = __shfl_sync(kAll, n, 0);
+  __syncwarp();
+  return n;
 }
 
 // Least-loaded part (lowest index on ties) and the second smallest size, for

@@ -2,14 +2,19 @@
 // (TM/partition.cpp:300-593) and MSM (MSM/partition.cpp:347-656).  Both walk the
 // vertices in id order.
 //
-// Moves are rare for these metrics, so a round is simple: every warp of the
-// grid evaluates a window of vertices against the current state (gain from the
-// K x K connection counts, loss per candidate part from the zero masks of that
-// matrix); the first mover ends the window, all vertices before it are
-// non-movers decided on exactly the sequential state, and the mover's move --
-// lists, connection counts, message counts, zero masks -- is applied by warps
-// of the whole grid.  Vertices with more than 256 nets get a round of
-// their own in which the whole grid computes their gain sets.
+// Moves are rare for these metrics, so a round is simple: the warps of the
+// grid evaluate a window of vertices against the current state and the first
+// mover ends the window.  Every vertex before it is a non-mover decided on
+// exactly the sequential state, and the mover's move (lists, connection counts,
+// message counts, masks) is applied by warps of the whole grid.
+//
+// Evaluation reads the K x K connection counts only through bit masks:
+// conn == 1 (gains, TM/partition.cpp:347-391) by the row and column of the
+// vertex's own part, and conn == 0 (losses per candidate part,
+// TM/partition.cpp:408-450) staged in shared memory when K <= 256.  Vertices
+// are classed by work like the LDG engine: light ones are evaluated by one
+// warp, medium ones by one CTA inside the window, the heaviest in a round of
+// their own split across the grid.
 
 #include "fp_spec_common.cuh"
 
@@ -19,11 +24,12 @@ namespace {
 
 using namespace spec;
 
-constexpr int kBig = 1000000000;
+constexpr int kStageK = 256;   // zero masks staged in shared memory up to this K
 
-// conn[a][b] += delta with the message count and the zero masks kept exact
-// (0->1 minus 1->0 crossings of a +-1 walk give the change of [value >= 1], and
-// the parity of zero crossings the change of [value == 0], whatever the order).
+// conn[a][b] += delta with the message count, the zero masks and the conn == 1
+// masks kept exact: the 0->1 minus 1->0 crossings of a +-1 walk give the change
+// of [value >= 1], and the parity of crossings into or out of a value gives the
+// change of [value == x], whatever the order of concurrent updates.
 __device__ __forceinline__ void conn_add_g(const DevInstance& I, int a, int b, int delta) {
   const int K = I.K;
   const int words = (K + 31) >> 5;
@@ -35,7 +41,20 @@ __device__ __forceinline__ void conn_add_g(const DevInstance& I, int a, int b, i
     atomicXor(&I.zrow[(size_t)a * words + (b >> 5)], 1u << (b & 31));
     atomicXor(&I.zcol[(size_t)b * words + (a >> 5)], 1u << (a & 31));
   }
+  if ((old == 1) != (now == 1)) {
+    atomicXor(&I.c1row[(size_t)a * words + (b >> 5)], 1u << (b & 31));
+    atomicXor(&I.c1col[(size_t)b * words + (a >> 5)], 1u << (a & 31));
+  }
 }
+
+// A word of a zero mask, staged in shared memory or read from L2.
+__device__ __forceinline__ uint32_t zword(const uint32_t* p, bool staged) { return staged ? *p : lds(p); }
+
+struct Masks {
+  const uint32_t* zr;   // conn == 0 by row (K x words)
+  const uint32_t* zc;   // conn == 0 by column
+  bool staged;
+};
 
 // Per-warp scratch of one evaluation.
 struct MsgWarp {
@@ -43,68 +62,110 @@ struct MsgWarp {
   uint32_t* S;               // sender parts (bitmask)
   unsigned long long* fsnd;  // first non-source net per sender part: (net index << 1) | own-alone
   int* gains;                // MSM: gains per part
-  int* maxl;                 // MSM: scratch lists
-  int* sndl;
+  int* sndl;                 // MSM: sender parts that are not max parts
+  uint32_t* c1r;             // conn[own][*] == 1
+  uint32_t* c1c;             // conn[*][own] == 1
 };
 
-// Receivers, senders and the source-side gain over nets [nb, nb + 32) of v
-// (TM/partition.cpp:320-393).  Returns this lane's source-side gain count.
-__device__ int msg_batch(const DevInstance& I, int v, int own, uint32_t base, int nb, int deg, const MsgWarp& Wk,
+__device__ __forceinline__ bool bit(const uint32_t* m, int i) { return (m[i >> 5] >> (i & 31)) & 1u; }
+
+// Clears the warp's scratch and loads the conn == 1 row and column of own.
+__device__ __forceinline__ void msg_begin(const DevInstance& I, const MsgWarp& Wk, int own, bool msm) {
+  const int lane = threadIdx.x & 31;
+  const int K = I.K;
+  const int words = (K + 31) >> 5;
+  for (int x = lane; x < words; x += 32) {
+    Wk.R[x] = 0;
+    Wk.S[x] = 0;
+    Wk.c1r[x] = lds(&I.c1row[(size_t)own * words + x]);
+    Wk.c1c[x] = lds(&I.c1col[(size_t)own * words + x]);
+  }
+  for (int p = lane; p < K; p += 32) {
+    Wk.fsnd[p] = ~0ull;
+    if (msm) Wk.gains[p] = 0;
+  }
+  __syncwarp();
+}
+
+// Receivers, senders and the source-side gain over nets [nb, min(nb + 32, nend))
+// of v (TM/partition.cpp:320-393).  Slots are flattened across the warp and
+// loaded 4 per lane per step with their counts.  Returns this lane's
+// source-side gain count.
+__device__ int msg_batch(const DevInstance& I, int v, int own, uint32_t base, int nb, int nend, const MsgWarp& Wk,
                          unsigned* oc1mask) {
   const int lane = threadIdx.x & 31;
   const int K = I.K;
   const int k = nb + lane;
-  int s = 0, n = 0, sv = -1;
-  if (k < deg) {
+  int s = 0, n = 0, sv = -1, ps = -1;
+  if (k < nend) {
     const int e = (int)__ldg(&I.vnets[base + k]);
     s = (int)__ldg(&I.nptr[e]);
+    const int cap = (int)__ldg(&I.nptr[e + 1]) - s;
     n = lds(&I.ep_len[e]);
     sv = __ldg(&I.src[e]);
+    if (sv != v) ps = lds(&I.part_vec[sv]);
+    if (n < 0 || n > cap || (sv != v && (unsigned)ps >= (unsigned)K)) {
+      dev_fail(I.status, kDevErrInvalid);
+      n = 0;
+      ps = 0;
+    }
   }
   if (lane == 0) *oc1mask = 0u;
-  __syncwarp();
   int incl = n;
   for (int off = 1; off < 32; off <<= 1) {
     const int t = __shfl_up_sync(kAll, incl, off);
     if (lane >= off) incl += t;
   }
   const int total = __shfl_sync(kAll, incl, 31);
+  __syncwarp();
   int g = 0;
-  for (int f0 = 0; f0 < total; f0 += 32) {
-    const int f = f0 + lane;
-    int lo = 0, hi = 31;
+  constexpr int kU = 4;
+  for (int f0 = 0; f0 < total; f0 += 32 * kU) {
+    int aa[kU], lo_[kU], src_[kU], pp[kU], cc[kU];
 #pragma unroll
-    for (int it = 0; it < 5; it++) {
-      const int mid = (lo + hi) >> 1;
-      const int val = __shfl_sync(kAll, incl, mid);
-      if (f < val) hi = mid; else lo = mid + 1;
+    for (int u = 0; u < kU; u++) {
+      const int f = f0 + u * 32 + lane;
+      int lo = 0, hi = 31;
+#pragma unroll
+      for (int it = 0; it < 5; it++) {
+        const int mid = (lo + hi) >> 1;
+        const int val = __shfl_sync(kAll, incl, mid);
+        if (f < val) hi = mid; else lo = mid + 1;
+      }
+      const int sl = __shfl_sync(kAll, s, lo);
+      const int nl = __shfl_sync(kAll, n, lo);
+      const int il = __shfl_sync(kAll, incl, lo);
+      src_[u] = __shfl_sync(kAll, sv, lo) == v;
+      lo_[u] = lo;
+      aa[u] = f < total ? sl + f - (il - nl) : -1;
     }
-    const int sl = __shfl_sync(kAll, s, lo);
-    const int nl = __shfl_sync(kAll, n, lo);
-    const int il = __shfl_sync(kAll, incl, lo);
-    const int svl = __shfl_sync(kAll, sv, lo);
-    if (f < total) {
-      const int a = sl + f - (il - nl);
-      const int t = lds(&I.ep_part[a]);
+#pragma unroll
+    for (int u = 0; u < kU; u++) {
+      pp[u] = aa[u] >= 0 ? lds(&I.ep_part[aa[u]]) : -1;
+      cc[u] = aa[u] >= 0 ? lds(&I.ep_cnt[aa[u]]) : 0;
+    }
+#pragma unroll
+    for (int u = 0; u < kU; u++) {
+      if (aa[u] < 0) continue;
+      const int t = pp[u];
       if ((unsigned)t >= (unsigned)K) {
         dev_fail(I.status, kDevErrInvalid);
-      } else if (svl == v) {
+      } else if (src_[u]) {
         if (t == own) {
-          if (lds(&I.ep_cnt[a]) > 1) atomicOr(&Wk.R[own >> 5], 1u << (own & 31));
+          if (cc[u] > 1) atomicOr(&Wk.R[own >> 5], 1u << (own & 31));
         } else {
           atomicOr(&Wk.R[t >> 5], 1u << (t & 31));
           // gain_loss_2d[own][t] is 1 here (raised once per listed part, lowered
           // after each net, TM/partition.cpp:347-369): the test is conn == 1.
-          if (lds(&I.conn[(size_t)own * K + t]) == 1) g++;
+          if (bit(Wk.c1r, t)) g++;
         }
-      } else if (t == own && lds(&I.ep_cnt[a]) == 1) {
-        atomicOr(oc1mask, 1u << lo);
+      } else if (t == own && cc[u] == 1) {
+        atomicOr(oc1mask, 1u << lo_[u]);
       }
     }
   }
   __syncwarp();
-  if (k < deg && sv != v) {
-    const int ps = lds(&I.part_vec[sv]);
+  if (k < nend && sv != v) {
     atomicOr(&Wk.S[ps >> 5], 1u << (ps & 31));
     atomicMin(&Wk.fsnd[ps], ((unsigned long long)k << 1) | ((*oc1mask >> lane) & 1u));
   }
@@ -112,22 +173,23 @@ __device__ int msg_batch(const DevInstance& I, int v, int own, uint32_t base, in
   return g;
 }
 
-// TM decision: first k below capacity with the largest gain - loss > 0
-// (TM/partition.cpp:408-450).  One warp (lanes over k) or, with pstep =
-// blockDim.x, one CTA (each thread returns its partial key).
-__device__ unsigned long long tm_best_partial(const DevInstance& I, const int* sizes, const uint32_t* R,
-                                              const uint32_t* S, int own, int gain, int k0, int kstep) {
+// TM: the part k below capacity with the largest gain - loss > 0, lowest k on
+// ties (TM/partition.cpp:408-450); threads k0, k0 + kstep, ... each return a
+// partial key (~0: none).
+__device__ unsigned long long tm_best_partial(const DevInstance& I, const Masks& M, const int* sizes,
+                                              const uint32_t* R, const uint32_t* S, int own, int gain, int k0,
+                                              int kstep) {
   const int K = I.K;
   const int words = (K + 31) >> 5;
   unsigned long long key = ~0ull;
   for (int k = k0; k < K; k += kstep) {
     if (k == own || !((double)sizes[k] < I.C)) continue;
-    const uint32_t* zr = I.zrow + (size_t)k * words;
-    const uint32_t* zc = I.zcol + (size_t)k * words;
+    const uint32_t* zr = M.zr + (size_t)k * words;
+    const uint32_t* zc = M.zc + (size_t)k * words;
     int loss = 0;
     for (int x = 0; x < words; x++) {
       const uint32_t self = (x == (k >> 5)) ? ~(1u << (k & 31)) : ~0u;
-      loss += __popc(R[x] & lds(&zr[x]) & self) + __popc(S[x] & lds(&zc[x]) & self);
+      loss += __popc(R[x] & zword(&zr[x], M.staged) & self) + __popc(S[x] & zword(&zc[x], M.staged) & self);
     }
     const int imp = gain - loss;
     if (imp > 0) {
@@ -141,27 +203,27 @@ __device__ unsigned long long tm_best_partial(const DevInstance& I, const int* s
 // MSM decision for candidate k (MSM/partition.cpp:460-520): every max-message
 // part must gain more than it loses, no other part may reach the maximum; the
 // total improvement over the max parts is returned (-1: not good).
-__device__ int msm_eval_k(const DevInstance& I, const int* msgs, const int* gains, const uint32_t* R, const uint32_t* S,
-                          const int* maxl, int nmax, const int* sndl, int nsnd, int mx, int k) {
+__device__ int msm_eval_k(const DevInstance& I, const Masks& M, const int* msgs, const int* gains, const uint32_t* R,
+                          const uint32_t* S, const int* maxl, int nmax, const int* sndl, int nsnd, int mx, int k) {
   const int K = I.K;
   const int words = (K + 31) >> 5;
-  const uint32_t* zr = I.zrow + (size_t)k * words;
+  const uint32_t* zr = M.zr + (size_t)k * words;
   int Lk = 0;
-  for (int x = 0; x < words; x++) Lk += __popc(R[x] & lds(&zr[x]));
+  for (int x = 0; x < words; x++) Lk += __popc(R[x] & zword(&zr[x], M.staged));
   int imp = 0;
   bool k_max = false;
   for (int q = 0; q < nmax; q++) {
     const int m = maxl[q];
     int l = m == k ? Lk : 0;
     if (m == k) k_max = true;
-    if ((S[m >> 5] >> (m & 31)) & 1u) l += (lds(&I.zrow[(size_t)m * words + (k >> 5)]) >> (k & 31)) & 1u;
+    if (bit(S, m)) l += (zword(&M.zr[(size_t)m * words + (k >> 5)], M.staged) >> (k & 31)) & 1u;
     if (gains[m] <= l) return -1;
     imp += gains[m] - l;
   }
   bool k_snd = false;
   for (int q = 0; q < nsnd; q++) {
     const int sp = sndl[q];
-    int l = (int)((lds(&I.zrow[(size_t)sp * words + (k >> 5)]) >> (k & 31)) & 1u);
+    int l = (int)((zword(&M.zr[(size_t)sp * words + (k >> 5)], M.staged) >> (k & 31)) & 1u);
     if (sp == k) { l += Lk; k_snd = true; }
     if (msgs[sp] + (l - gains[sp]) >= mx) return -1;
   }
@@ -169,30 +231,180 @@ __device__ int msm_eval_k(const DevInstance& I, const int* msgs, const int* gain
   return imp;
 }
 
-// Move of one net by one thread: lists (commit_net), then the connection
-// updates on the net's final list (TM/partition.cpp:519-587).
-__device__ void msg_commit_net(const DevInstance& I, int v, int own, int d, int e) {
-  commit_net(I, v, own, d, e, nullptr);
+__device__ __forceinline__ unsigned long long msm_key(int imp, int k) {
+  return ((unsigned long long)(0x7fffffff - imp) << 32) | (unsigned)k;
+}
+
+// Round state shared by the evaluations of a CTA.
+struct MsgRound {
+  const int* sizes;
+  const int* msgs;
+  const int* maxl;   // max-message parts (MSM)
+  int nmax, mx;
+};
+
+// Decision of one warp for v from its scratch (g: source-side gain count).
+__device__ int msg_decide_warp(const DevInstance& I, const Masks& M, const MsgRound& Rd, const MsgWarp& Wk, int own,
+                               int g, bool msm) {
+  const int lane = threadIdx.x & 31;
+  const int K = I.K;
+  int gs = 0;
+  for (int p = lane; p < K; p += 32) {
+    const unsigned long long f = Wk.fsnd[p];
+    if (f != ~0ull && (f & 1ull) && bit(Wk.c1c, p)) {
+      if (msm) Wk.gains[p] += 1;
+      else gs++;
+    }
+  }
+  gs = warp_sum(gs);
+  __syncwarp();
+  unsigned long long key = ~0ull;
+  if (!msm) {
+    const int gain = g + gs;
+    if (gain > 0) key = tm_best_partial(I, M, Rd.sizes, Wk.R, Wk.S, own, gain, lane, 32);
+  } else {
+    if (lane == 0) Wk.gains[own] += g;
+    __syncwarp();
+    bool has_gain = false, zero_gain_max = false;
+    for (int p = lane; p < K; p += 32) has_gain |= Wk.gains[p] > 0;
+    for (int q = lane; q < Rd.nmax; q += 32) zero_gain_max |= Wk.gains[Rd.maxl[q]] <= 0;
+    has_gain = __any_sync(kAll, has_gain);
+    zero_gain_max = __any_sync(kAll, zero_gain_max);
+    if (has_gain && !zero_gain_max) {
+      int nsnd = 0;
+      for (int p0 = 0; p0 < K; p0 += 32) {
+        const int p = p0 + lane;
+        const bool ok = p < K && bit(Wk.S, p) && Rd.msgs[p] != Rd.mx;
+        const unsigned m = __ballot_sync(kAll, ok);
+        if (ok) Wk.sndl[nsnd + __popc(m & ((1u << lane) - 1u))] = p;
+        nsnd += __popc(m);
+      }
+      __syncwarp();
+      for (int k = lane; k < K; k += 32) {
+        if (k == own) continue;
+        const int imp = msm_eval_k(I, M, Rd.msgs, Wk.gains, Wk.R, Wk.S, Rd.maxl, Rd.nmax, Wk.sndl, nsnd, Rd.mx, k);
+        if (imp >= 0) key = min(key, msm_key(imp, k));
+      }
+    }
+  }
+  for (int off = 16; off; off >>= 1) {
+    const unsigned long long o2 = __shfl_xor_sync(kAll, key, off);
+    key = o2 < key ? o2 : key;
+  }
+  return key != ~0ull ? (int)(key & 0xffffffffu) : -1;
+}
+
+// Decision of the whole CTA from the combined scratch of warp 0 (R, S, fsnd;
+// g: the CTA's source-side gain count).  uscr / iscr: per-warp scratch.
+__device__ int msg_decide_cta(const DevInstance& I, const Masks& M, const MsgRound& Rd, const MsgWarp& W0, int own,
+                              int g, bool msm, unsigned long long* uscr, int* iscr) {
+  __shared__ int s_nsnd;
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const int K = I.K;
+  int gs = 0;
+  for (int p = threadIdx.x; p < K; p += blockDim.x) {
+    const unsigned long long f = W0.fsnd[p];
+    const bool gp = f != ~0ull && (f & 1ull) && bit(W0.c1c, p);
+    if (msm) W0.gains[p] = (gp ? 1 : 0) + (p == own ? g : 0);
+    else gs += gp;
+  }
+  gs = warp_sum(gs);
+  __syncthreads();
+  if (lane == 0) iscr[wib] = gs;
+  __syncthreads();
+  int gs_t = 0;
+  for (int x = 0; x < (int)(blockDim.x >> 5); x++) gs_t += iscr[x];
+  unsigned long long key = ~0ull;
+  if (!msm) {
+    const int gain = g + gs_t;
+    if (gain > 0) key = tm_best_partial(I, M, Rd.sizes, W0.R, W0.S, own, gain, threadIdx.x, blockDim.x);
+  } else {
+    bool has_gain = false, zgm = false;
+    for (int p = threadIdx.x; p < K; p += blockDim.x) has_gain |= W0.gains[p] > 0;
+    for (int q = threadIdx.x; q < Rd.nmax; q += blockDim.x) zgm |= W0.gains[Rd.maxl[q]] <= 0;
+    has_gain = __syncthreads_or(has_gain);
+    zgm = __syncthreads_or(zgm);
+    if (has_gain && !zgm) {
+      if (threadIdx.x == 0) {
+        int c = 0;
+        for (int p = 0; p < K; p++)
+          if (bit(W0.S, p) && Rd.msgs[p] != Rd.mx) W0.sndl[c++] = p;
+        s_nsnd = c;
+      }
+      __syncthreads();
+      for (int k = threadIdx.x; k < K; k += blockDim.x) {
+        if (k == own) continue;
+        const int imp = msm_eval_k(I, M, Rd.msgs, W0.gains, W0.R, W0.S, Rd.maxl, Rd.nmax, W0.sndl, s_nsnd, Rd.mx, k);
+        if (imp >= 0) key = min(key, msm_key(imp, k));
+      }
+    }
+  }
+  key = block_min_u64(key, uscr);
+  return key != ~0ull ? (int)(key & 0xffffffffu) : -1;
+}
+
+// Combines the scratch of all warps of the CTA into warp 0's (R, S by OR,
+// fsnd by minimum); the caller synchronises before and after.
+__device__ __forceinline__ void msg_combine(const DevInstance& I, uint32_t* R_b, uint32_t* S_b,
+                                            unsigned long long* fs_b) {
+  const int K = I.K;
+  const int words = (K + 31) >> 5;
+  for (int x = threadIdx.x; x < words; x += blockDim.x) {
+    uint32_t r = 0, s = 0;
+    for (int y = 0; y < kSWarps; y++) { r |= R_b[(size_t)y * words + x]; s |= S_b[(size_t)y * words + x]; }
+    R_b[x] = r;
+    S_b[x] = s;
+  }
+  for (int p = threadIdx.x; p < K; p += blockDim.x) {
+    unsigned long long f = ~0ull;
+    for (int y = 0; y < kSWarps; y++) f = min(f, fs_b[(size_t)y * K + p]);
+    fs_b[p] = f;
+  }
+}
+
+// Move of v own -> d on net e by one warp: the list (commit_net_warp), then the
+// connection updates on the net's final list (TM/partition.cpp:519-587).
+__device__ void msg_commit_net_warp(const DevInstance& I, int v, int own, int d, int e) {
+  const int lane = threadIdx.x & 31;
+  const int n = commit_net_warp(I, own, d, e);
   const int s = (int)__ldg(&I.nptr[e]);
-  const int n = lds(&I.ep_len[e]);
   const int sv = __ldg(&I.src[e]);
   if (sv == v) {
-    for (int j = 0; j < n; j++) {
+    for (int j = lane; j < n; j += 32) {
       const int t = lds(&I.ep_part[s + j]);
       if (t != d) conn_add_g(I, d, t, 1);
       if (t != own && t != d) conn_add_g(I, own, t, -1);
       if (t == d && lds(&I.ep_cnt[s + j]) > 1) conn_add_g(I, own, t, -1);
     }
   } else {
-    const int sn = lds(&I.part_vec[sv]);
     bool dc1 = false, fo = false;
-    for (int j = 0; j < n; j++) {
+    for (int j = lane; j < n; j += 32) {
       const int t = lds(&I.ep_part[s + j]);
       if (t == d && lds(&I.ep_cnt[s + j]) == 1) dc1 = true;
       if (t == own) fo = true;
     }
-    if (dc1) conn_add_g(I, sn, d, 1);
-    if (!fo) conn_add_g(I, sn, own, -1);
+    dc1 = __any_sync(kAll, dc1);
+    fo = __any_sync(kAll, fo);
+    if (lane == 0) {
+      const int sn = lds(&I.part_vec[sv]);
+      if (dc1) conn_add_g(I, sn, d, 1);
+      if (!fo) conn_add_g(I, sn, own, -1);
+    }
+  }
+  __syncwarp();
+}
+
+// The move of v by the whole grid: one warp per net, then v's part and sizes.
+__device__ void msg_commit_grid(const DevInstance& I, int v, int own, int d, int gw, int nwarps, int it) {
+  const uint32_t base = __ldg(&I.vptr[v]);
+  const int deg = (int)(__ldg(&I.vptr[v + 1]) - base);
+  for (int i = gw; i < deg; i += nwarps) msg_commit_net_warp(I, v, own, d, (int)__ldg(&I.vnets[base + i]));
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    I.part_vec[v] = d;
+    const int wv = __ldg(&I.w[v]);
+    atomicAdd(&I.part_sizes[own], -wv);
+    atomicAdd(&I.part_sizes[d], wv);
+    atomicAdd((unsigned long long*)&I.moves[it], 1ull);
   }
 }
 
@@ -201,30 +413,39 @@ __global__ void __launch_bounds__(kSThreads) spec_msg_kernel(DevInstance I, Spec
   __shared__ unsigned long long uscr[kSWarps];
   __shared__ int iscr[kSWarps];
   __shared__ unsigned oc1m[kSWarps];
-  __shared__ int s_mx, s_nmax, s_best;
+  __shared__ int s_mx, s_nmax, s_stop;
   const bool msm = I.metric == 3;
   const int K = I.K;
   const int words = (K + 31) >> 5;
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int gw = blockIdx.x * kSWarps + wib;
   const int nwarps = gridDim.x * kSWarps;
+  const bool staged = K <= kStageK;
   Carve cv{smem_raw};
   int* sizes_s = cv.take<int>(K);
   int* msgs_s = cv.take<int>(K);
   int* maxl_s = cv.take<int>(K);                        // max-message parts (MSM)
   uint32_t* R_b = cv.take<uint32_t>((size_t)words * kSWarps);
   uint32_t* S_b = cv.take<uint32_t>((size_t)words * kSWarps);
+  uint32_t* c1r_b = cv.take<uint32_t>((size_t)words * kSWarps);
+  uint32_t* c1c_b = cv.take<uint32_t>((size_t)words * kSWarps);
   unsigned long long* fs_b = cv.take<unsigned long long>((size_t)K * kSWarps);
   int* gains_b = cv.take<int>((size_t)K * kSWarps);
   int* sndl_b = cv.take<int>((size_t)K * kSWarps);
-  MsgWarp Wk{R_b + (size_t)wib * words, S_b + (size_t)wib * words, fs_b + (size_t)wib * K,
-             gains_b + (size_t)wib * K, maxl_s, sndl_b + (size_t)wib * K};
+  uint32_t* zr_s = staged ? cv.take<uint32_t>((size_t)K * words) : nullptr;
+  uint32_t* zc_s = staged ? cv.take<uint32_t>((size_t)K * words) : nullptr;
+  const Masks M{staged ? zr_s : I.zrow, staged ? zc_s : I.zcol, staged};
+  const MsgWarp Wk{R_b + (size_t)wib * words, S_b + (size_t)wib * words, fs_b + (size_t)wib * K,
+                   gains_b + (size_t)wib * K, sndl_b + (size_t)wib * K, c1r_b + (size_t)wib * words,
+                   c1c_b + (size_t)wib * words};
+  const MsgWarp W0{R_b, S_b, fs_b, gains_b, sndl_b, c1r_b, c1c_b};
   unsigned long long tA = gtimer();
   int heavy_round = 0;
   int round = 0;
+  bool dirty = true;   // staged masks out of date (a move was committed)
   for (int it = 0; it < passes; it++) {
     int pos = 0;
-    int W = min(nwarps, B.wmax);
+    const int W = B.wmax_msg;
     int hidx = 0;
     while (pos < I.nov) {
       // ------------------------------------------------------------ round state
@@ -232,6 +453,13 @@ __global__ void __launch_bounds__(kSThreads) spec_msg_kernel(DevInstance I, Spec
         sizes_s[p] = lds(&I.part_sizes[p]);
         msgs_s[p] = lds(&I.msgs[p]);
       }
+      if (staged && dirty) {
+        for (int x = threadIdx.x; x < K * words; x += blockDim.x) {
+          zr_s[x] = lds(&I.zrow[x]);
+          zc_s[x] = lds(&I.zcol[x]);
+        }
+      }
+      dirty = false;
       __syncthreads();
       if (msm) {
         // max-message parts, recomputed for every vertex by the reference
@@ -252,13 +480,13 @@ __global__ void __launch_bounds__(kSThreads) spec_msg_kernel(DevInstance I, Spec
         }
         __syncthreads();
       }
+      const MsgRound Rd{sizes_s, msgs_s, maxl_s, msm ? s_nmax : 0, msm ? s_mx : 0};
       while (hidx < B.nheavy && __ldg(&B.heavy_pos[hidx]) < pos) hidx++;
       const int next_heavy = hidx < B.nheavy ? __ldg(&B.heavy_pos[hidx]) : I.nov;
 
       if (next_heavy == pos) {
         // ========================================================== heavy round
         const int hp = heavy_round & 1;
-        int* hg = B.hgain + hp * K;            // MSM gains / TM: [0] gain
         uint32_t* hR = reinterpret_cast<uint32_t*>(B.hloss + hp * K);      // words <= K
         uint32_t* hS = reinterpret_cast<uint32_t*>(B.hadelta + hp * K);
         unsigned long long* hf = B.hfirst + hp * K;
@@ -267,99 +495,36 @@ __global__ void __launch_bounds__(kSThreads) spec_msg_kernel(DevInstance I, Spec
         const int own = lds(&I.part_vec[v]);
         const uint32_t base = __ldg(&I.vptr[v]);
         const int deg = (int)(__ldg(&I.vptr[v + 1]) - base);
-        for (int x = lane; x < words; x += 32) { Wk.R[x] = 0; Wk.S[x] = 0; }
-        for (int p = lane; p < K; p += 32) Wk.fsnd[p] = ~0ull;
-        __syncwarp();
+        msg_begin(I, Wk, own, msm);
         int g = 0;
-        for (int nb = gw * 32; nb < deg; nb += nwarps * 32) g += msg_batch(I, v, own, base, nb, deg, Wk, &oc1m[wib]);
+        {
+          int n0, n1;
+          net_range(deg, gw, nwarps, &n0, &n1);
+          for (int nb = n0; nb < n1; nb += 32) g += msg_batch(I, v, own, base, nb, n1, Wk, &oc1m[wib]);
+        }
         g = warp_sum(g);
         __syncthreads();
+        msg_combine(I, R_b, S_b, fs_b);
+        __syncthreads();
         for (int x = threadIdx.x; x < words; x += blockDim.x) {
-          uint32_t r = 0, s = 0;
-          for (int y = 0; y < kSWarps; y++) { r |= R_b[(size_t)y * words + x]; s |= S_b[(size_t)y * words + x]; }
-          if (r) atomicOr(&hR[x], r);
-          if (s) atomicOr(&hS[x], s);
+          if (R_b[x]) atomicOr(&hR[x], R_b[x]);
+          if (S_b[x]) atomicOr(&hS[x], S_b[x]);
         }
-        for (int p = threadIdx.x; p < K; p += blockDim.x) {
-          unsigned long long f = ~0ull;
-          for (int y = 0; y < kSWarps; y++) f = min(f, fs_b[(size_t)y * K + p]);
-          if (f != ~0ull) atomicMin(&hf[p], f);
-        }
+        for (int p = threadIdx.x; p < K; p += blockDim.x)
+          if (fs_b[p] != ~0ull) atomicMin(&hf[p], fs_b[p]);
         if (lane == 0 && g) atomicAdd(&hmisc[0], g);
         if (!grid_barrier(B.bar, I.status)) return;
-        // every CTA: full sets, sender gains, decision
-        uint32_t* R = R_b;   // warp 0's arrays hold the global sets
-        uint32_t* S = S_b;
-        for (int x = threadIdx.x; x < words; x += blockDim.x) { R[x] = lds(&hR[x]); S[x] = lds(&hS[x]); }
-        int* gains = gains_b;
-        for (int p = threadIdx.x; p < K; p += blockDim.x) gains[p] = 0;
+        // every CTA takes the same decision from the global sets
+        for (int x = threadIdx.x; x < words; x += blockDim.x) { R_b[x] = lds(&hR[x]); S_b[x] = lds(&hS[x]); }
+        for (int p = threadIdx.x; p < K; p += blockDim.x) fs_b[p] = lds(&hf[p]);
         __syncthreads();
-        int gsum = 0;
-        for (int p = threadIdx.x; p < K; p += blockDim.x) {
-          const unsigned long long f = lds(&hf[p]);
-          if (f != ~0ull && (f & 1ull) && lds(&I.conn[(size_t)p * K + own]) == 1) {
-            if (msm) gains[p] += 1;
-            else gsum++;
-          }
-        }
-        gsum = warp_sum(gsum);
-        if (lane == 0) iscr[wib] = gsum;
-        __syncthreads();
-        int gain_total = lds(&hmisc[0]);
-        for (int x = 0; x < kSWarps; x++) gain_total += iscr[x];
-        __syncthreads();
-        int best = -1;
-        if (!msm) {
-          if (gain_total > 0) {
-            unsigned long long key = tm_best_partial(I, sizes_s, R, S, own, gain_total, threadIdx.x, blockDim.x);
-            key = block_min_u64(key, uscr);
-            if (key != ~0ull) best = (int)(key & 0xffffffffu);
-          }
-        } else {
-          if (threadIdx.x == 0) gains[own] += lds(&hmisc[0]);
-          __syncthreads();
-          bool has_gain = false;
-          for (int p = threadIdx.x; p < K; p += blockDim.x) has_gain |= gains[p] > 0;
-          has_gain = __syncthreads_or(has_gain);
-          if (has_gain) {
-            // sender parts that are not max parts
-            __shared__ int s_nsnd;
-            if (threadIdx.x == 0) {
-              int c = 0;
-              for (int p = 0; p < K; p++)
-                if (((S[p >> 5] >> (p & 31)) & 1u) && msgs_s[p] != s_mx) sndl_b[c++] = p;
-              s_nsnd = c;
-            }
-            __syncthreads();
-            unsigned long long key = ~0ull;
-            for (int k = threadIdx.x; k < K; k += blockDim.x) {
-              if (k == own) continue;
-              const int imp = msm_eval_k(I, msgs_s, gains, R, S, maxl_s, s_nmax, sndl_b, s_nsnd, s_mx, k);
-              if (imp >= 0) {
-                const unsigned long long kk = ((unsigned long long)(0x7fffffff - imp) << 32) | (unsigned)k;
-                key = kk < key ? kk : key;
-              }
-            }
-            key = block_min_u64(key, uscr);
-            if (key != ~0ull) best = (int)(key & 0xffffffffu);
-          }
-        }
+        const int best = msg_decide_cta(I, M, Rd, W0, own, lds(&hmisc[0]), msm, uscr, iscr);
         if (!grid_barrier(B.bar, I.status)) return;
-        if (best >= 0) {
-          for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < deg; i += gridDim.x * blockDim.x)
-            msg_commit_net(I, v, own, best, (int)__ldg(&I.vnets[base + i]));
-          if (blockIdx.x == 0 && threadIdx.x == 0) {
-            I.part_vec[v] = best;
-            const int wv = __ldg(&I.w[v]);
-            atomicAdd(&I.part_sizes[own], -wv);
-            atomicAdd(&I.part_sizes[best], wv);
-            atomicAdd((unsigned long long*)&I.moves[it], 1ull);
-          }
-        }
+        if (best >= 0) msg_commit_grid(I, v, own, best, gw, nwarps, it);
+        dirty = best >= 0;
         {
-          const int op = hp ^ 1;
+          const int op = hp ^ 1;   // clear the other heavy buffers for the next heavy round
           for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < K; p += gridDim.x * blockDim.x) {
-            B.hgain[op * K + p] = 0;
             B.hloss[op * K + p] = 0;
             B.hadelta[op * K + p] = 0;
             B.hfirst[op * K + p] = ~0ull;
@@ -383,77 +548,64 @@ __global__ void __launch_bounds__(kSThreads) spec_msg_kernel(DevInstance I, Spec
       // ============================================================ light round
       const int end_w = min(min(pos + W, I.nov), next_heavy);
       const int par = round & 1;
-      for (int v = pos + gw; v < end_w; v += nwarps) {
+      const int span = end_w - pos;
+      const int q = (span + nwarps - 1) / nwarps;
+      const int z0 = min(pos + gw * q, end_w);
+      const int z1 = min(z0 + q, end_w);
+      for (int v = z0; v < z1; v++) {
+        if (__ldg(&B.vclass[v]) != 0) continue;   // medium vertex: evaluated by the whole CTA below
+        if (lds(&B.ctl[par]) < v) break;           // an earlier mover ends the window
         const int own = lds(&I.part_vec[v]);
         const uint32_t base = __ldg(&I.vptr[v]);
         const int deg = (int)(__ldg(&I.vptr[v + 1]) - base);
-        for (int x = lane; x < words; x += 32) { Wk.R[x] = 0; Wk.S[x] = 0; }
-        for (int p = lane; p < K; p += 32) { Wk.fsnd[p] = ~0ull; Wk.gains[p] = 0; }
-        __syncwarp();
+        msg_begin(I, Wk, own, msm);
         int g = 0;
         for (int nb = 0; nb < deg; nb += 32) g += msg_batch(I, v, own, base, nb, deg, Wk, &oc1m[wib]);
         g = warp_sum(g);
-        int gs = 0;
-        for (int p = lane; p < K; p += 32) {
-          const unsigned long long f = Wk.fsnd[p];
-          if (f != ~0ull && (f & 1ull) && lds(&I.conn[(size_t)p * K + own]) == 1) {
-            if (msm) Wk.gains[p] += 1;
-            else gs++;
+        const int best = msg_decide_warp(I, M, Rd, Wk, own, g, msm);
+        if (best >= 0) {
+          if (lane == 0) {
+            B.dec[v - pos] = (own << 16) | best;
+            atomicMin(&B.ctl[par], v);
           }
+          break;
         }
-        gs = warp_sum(gs);
-        __syncwarp();
-        int best = -1;
-        if (!msm) {
-          const int gain = g + gs;
-          if (gain > 0) {
-            unsigned long long key = tm_best_partial(I, sizes_s, Wk.R, Wk.S, own, gain, lane, 32);
-            for (int off = 16; off; off >>= 1) {
-              const unsigned long long o2 = __shfl_xor_sync(kAll, key, off);
-              key = o2 < key ? o2 : key;
-            }
-            if (key != ~0ull) best = (int)(key & 0xffffffffu);
+      }
+      // medium vertices of this CTA's positions
+      const int cz0 = min(pos + blockIdx.x * kSWarps * q, end_w);
+      const int cz1 = min(cz0 + kSWarps * q, end_w);
+      for (int mi = lower_bound_pos(B.mid_pos, B.nmid, cz0); mi < B.nmid; mi++) {
+        const int v = __ldg(&B.mid_pos[mi]);
+        if (v >= cz1) break;
+        __syncthreads();
+        if (threadIdx.x == 0) s_stop = lds(&B.ctl[par]) < v;
+        __syncthreads();
+        if (s_stop) break;
+        const int own = lds(&I.part_vec[v]);
+        const uint32_t base = __ldg(&I.vptr[v]);
+        const int deg = (int)(__ldg(&I.vptr[v + 1]) - base);
+        msg_begin(I, Wk, own, msm);
+        int g = 0;
+        {
+          int n0, n1;
+          net_range(deg, wib, kSWarps, &n0, &n1);
+          for (int nb = n0; nb < n1; nb += 32) g += msg_batch(I, v, own, base, nb, n1, Wk, &oc1m[wib]);
+        }
+        g = warp_sum(g);
+        __syncthreads();
+        if (lane == 0) iscr[wib] = g;
+        msg_combine(I, R_b, S_b, fs_b);
+        __syncthreads();
+        int gt = 0;
+        for (int x = 0; x < kSWarps; x++) gt += iscr[x];
+        const int best = msg_decide_cta(I, M, Rd, W0, own, gt, msm, uscr, iscr);
+        if (best >= 0) {
+          if (threadIdx.x == 0) {
+            B.dec[v - pos] = (own << 16) | best;
+            atomicMin(&B.ctl[par], v);
           }
-        } else {
-          if (lane == 0) Wk.gains[own] += g;
-          __syncwarp();
-          bool has_gain = false;
-          bool zero_gain_max = false;
-          for (int p = lane; p < K; p += 32) has_gain |= Wk.gains[p] > 0;
-          for (int q = lane; q < s_nmax; q += 32) zero_gain_max |= Wk.gains[maxl_s[q]] <= 0;
-          has_gain = __any_sync(kAll, has_gain);
-          zero_gain_max = __any_sync(kAll, zero_gain_max);
-          if (has_gain && !zero_gain_max) {
-            int nsnd = 0;
-            for (int p0 = 0; p0 < K; p0 += 32) {
-              const int p = p0 + lane;
-              const bool ok = p < K && ((Wk.S[p >> 5] >> (p & 31)) & 1u) && msgs_s[p] != s_mx;
-              const unsigned m = __ballot_sync(kAll, ok);
-              if (ok) Wk.sndl[nsnd + __popc(m & ((1u << lane) - 1u))] = p;
-              nsnd += __popc(m);
-            }
-            __syncwarp();
-            unsigned long long key = ~0ull;
-            for (int k = lane; k < K; k += 32) {
-              if (k == own) continue;
-              const int imp = msm_eval_k(I, msgs_s, Wk.gains, Wk.R, Wk.S, maxl_s, s_nmax, Wk.sndl, nsnd, s_mx, k);
-              if (imp >= 0) {
-                const unsigned long long kk = ((unsigned long long)(0x7fffffff - imp) << 32) | (unsigned)k;
-                key = kk < key ? kk : key;
-              }
-            }
-            for (int off = 16; off; off >>= 1) {
-              const unsigned long long o2 = __shfl_xor_sync(kAll, key, off);
-              key = o2 < key ? o2 : key;
-            }
-            if (key != ~0ull) best = (int)(key & 0xffffffffu);
-          }
+          break;
         }
-        if (best >= 0 && lane == 0) {
-          B.dec[v - pos] = (own << 16) | best;
-          atomicMin(&B.ctl[par], v);
-        }
-        __syncwarp();
       }
       if (!grid_barrier(B.bar, I.status)) return;
       if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -467,30 +619,15 @@ __global__ void __launch_bounds__(kSThreads) spec_msg_kernel(DevInstance I, Spec
       if (f != kNone) {
         end = f + 1;
         const int pk = lds(&B.dec[f - pos]);
-        const int own = pk >> 16, d = pk & 0xffff;
-        const uint32_t base = __ldg(&I.vptr[f]);
-        const int deg = (int)(__ldg(&I.vptr[f + 1]) - base);
-        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < deg; i += gridDim.x * blockDim.x)
-          msg_commit_net(I, f, own, d, (int)__ldg(&I.vnets[base + i]));
-        if (blockIdx.x == 0 && threadIdx.x == 0) {
-          I.part_vec[f] = d;
-          const int wv = __ldg(&I.w[f]);
-          atomicAdd(&I.part_sizes[own], -wv);
-          atomicAdd(&I.part_sizes[d], wv);
-          atomicAdd((unsigned long long*)&I.moves[it], 1ull);
-          B.stats[2]++;
-        }
+        msg_commit_grid(I, f, pk >> 16, pk & 0xffff, gw, nwarps, it);
+        if (blockIdx.x == 0 && threadIdx.x == 0) B.stats[2]++;
+        dirty = true;
       }
       if (blockIdx.x == 0 && threadIdx.x == 0) {
         B.ctl[par ^ 1] = kNone;
         B.stats[0]++;
         B.stats[9] += end - pos;
         B.stats[f == kNone ? 3 : 8]++;
-      }
-      if (f == kNone) {
-        if (end_w == pos + W) W = min(2 * W, B.wmax);
-      } else {
-        W = max(256, min(B.wmax, 2 * (f - pos + 1)));
       }
       pos = end;
       round++;
@@ -509,8 +646,10 @@ __global__ void __launch_bounds__(kSThreads) spec_msg_kernel(DevInstance I, Spec
 size_t spec_msg_smem_bytes(int K) {
   auto a = [](size_t n) { return (n + 15) & ~size_t(15); };
   const size_t words = (size_t)(K + 31) / 32;
-  return 3 * a(sizeof(int) * K) + 2 * a(sizeof(uint32_t) * words * kSWarps) +
-         a(sizeof(unsigned long long) * (size_t)K * kSWarps) + 2 * a(sizeof(int) * (size_t)K * kSWarps);
+  size_t b = 3 * a(sizeof(int) * K) + 4 * a(sizeof(uint32_t) * words * kSWarps) +
+             a(sizeof(unsigned long long) * (size_t)K * kSWarps) + 2 * a(sizeof(int) * (size_t)K * kSWarps);
+  if (K <= kStageK) b += 2 * a(sizeof(uint32_t) * (size_t)K * words);
+  return b;
 }
 
 cudaError_t launch_spec_msg(const DevInstance& I, const SpecBuf& B, int passes, int num_sms, cudaStream_t st,
