@@ -39,11 +39,19 @@ static bool spec_supported(int metric, int K, int max_smem) {
 // LDG metrics: vertex classes by work = sum over its nets of min(net size, K),
 // the list slots an evaluation reads at most.  Light: one warp; medium: one CTA
 // inside the window; above the super bound (or with 65536 nets or more, the
-// limit of the candidate encoding): a whole-grid round.  MSV's windows are
-// short (nearly every vertex moves), so its medium vertices bound the round
-// time and the super bound is lower (bounds from a sweep on the c2 workload).
+// limit of the candidate encoding): a whole-grid round.  Windows that end
+// often (MSV moves nearly every vertex) favour a lower super bound, long ones
+// (TV, MSM) a higher one; bounds from a sweep on the c2 workload.  TM and MSM
+// use the same classes in id order.
 constexpr int kLightWork = 2048;
-int default_super_work(int metric) { return metric == FP_METRIC_MSV ? 65536 : 262144; }
+int default_super_work(int metric) {
+  switch (metric) {
+    case FP_METRIC_MSV: return 16384;
+    case FP_METRIC_MSRV:
+    case FP_METRIC_TM: return 65536;
+    default: return 262144;
+  }
+}
 constexpr int kMaxSpecWarps = 16384;
 cudaError_t launch_metrics(const DevInstance& I, void* scratch, long long* out, int num_sms, cudaStream_t st,
                            int* launches);
@@ -281,6 +289,7 @@ static cudaError_t clear_spec_scratch(const SpecBuf& b, int noe, int K, cudaStre
   if (e == cudaSuccess) e = cudaMemsetAsync(b.hloss, 0, sizeof(int) * 2 * K, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(b.hadelta, 0, sizeof(int) * 2 * K, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(b.hmisc, 0, sizeof(int) * 16, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(b.mcnt, 0, sizeof(int) * 2, s);
   return e;
 }
 
@@ -385,7 +394,7 @@ int fp_instance_create(fp_ctx* ctx, const fp_hypergraph* h, int32_t K, int32_t m
       (rc = dalloc(in, &in->sb.vd, kSpecWindow)) || (rc = dalloc(in, &in->sb.scan, (size_t)kSpecWindow * words)) ||
       (rc = dalloc(in, &in->sb.rec, g.pins)) || (rc = dalloc(in, &in->vclass_d, g.nov)) ||
       (rc = dalloc(in, &in->sb.cand, (size_t)kSpecWindow * K)) || (rc = dalloc(in, &in->sb.ncand, kSpecWindow)) ||
-      (rc = dalloc(in, &in->sb.pref, (size_t)kSpecWindow * K)) ||
+      (rc = dalloc(in, &in->sb.mlist, kSpecWindow)) || (rc = dalloc(in, &in->sb.mcnt, 2)) ||
       (rc = dalloc(in, &in->sb.wsum, kMaxSpecWarps)) || (rc = dalloc(in, &in->sb.vsum, kMaxSpecWarps)) ||
       (rc = dalloc(in, &in->sb.claim_m, g.noe)) || (rc = dalloc(in, &in->sb.claim64, g.noe)) || (rc = dalloc(in, &in->sb.claim_c, g.noe)) ||
       (rc = dalloc(in, &in->sb.mask_c, g.noe)) || (rc = dalloc(in, &in->sb.hcnt, 2 * K)) ||

@@ -65,7 +65,8 @@ struct SpecBuf {
                                 //     2: whole-grid round (LDG metrics)
   unsigned long long* cand;  // [wmax * K] LDG candidates per window offset (part, count, first)
   int* ncand;            // [wmax]
-  int* pref;             // [K * wmax] per-part prefix of the window's size changes
+  int* mlist;            // [wmax] window offsets of the round's movers (any order)
+  int* mcnt;             // [2] their count, double-buffered by round parity
   int* wsum;             // [max_warps] per-warp sums of wt
   int* vsum;             // [max_warps] per-warp sums of vd
   unsigned long long* claim64;  // [noe] (round << 32) | ~position of the first claim (CN)

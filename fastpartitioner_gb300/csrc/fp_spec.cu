@@ -128,12 +128,25 @@ __device__ int ldg_decide(const DevInstance& I, const RoundCtx& R, const int* cn
 }
 
 // The LDG decision of the vertex at window offset o again, from its stored
-// candidates and the exact part sizes at that position (round-start sizes plus
-// the prefix of the window's moves); one warp.
-__device__ int ldg_recheck(const DevInstance& I, const RoundCtx& R, const SpecBuf& B, int o, int v, int own,
-                           int metric) {
+// candidates and the exact part sizes at that position: round-start sizes plus
+// the moves of the window's movers before o (the mover list, nm entries),
+// summed into the warp's K-int scratch dsz.  One warp.
+__device__ int ldg_recheck(const DevInstance& I, const RoundCtx& R, const SpecBuf& B, int o, int own, int metric,
+                           int* dsz, int nm) {
   const int lane = threadIdx.x & 31;
   const int K = I.K;
+  for (int p = lane; p < K; p += 32) dsz[p] = 0;
+  __syncwarp();
+  for (int i = lane; i < nm; i += 32) {
+    const int o2 = lds(&B.mlist[i]);
+    if (o2 >= o) continue;
+    const int w = lds(&B.wt[o2]);
+    if (w == 0) continue;
+    const int pk = lds(&B.dec[o2]);
+    atomicAdd(&dsz[pk & 0xffff], w);
+    atomicAdd(&dsz[pk >> 16], -w);
+  }
+  __syncwarp();
   const unsigned long long* cl = B.cand + (size_t)o * K;
   const int nc = lds(&B.ncand[o]);
   LdgKey best{-1.0, 0, -1, ~0ull};
@@ -142,7 +155,7 @@ __device__ int ldg_recheck(const DevInstance& I, const RoundCtx& R, const SpecBu
     const int p = (int)(ent >> 52);
     const int c = (int)((ent >> 36) & 0xffffull);
     const unsigned long long f = (((ent >> 20) & 0xffffull) << 32) | (ent & 0xfffffull);
-    const int sz = R.sizes[p] + lds(&B.pref[(size_t)p * B.wmax + o]);
+    const int sz = R.sizes[p] + dsz[p];
     const double pen = __dsub_rn(1.0, __ddiv_rn((double)sz, I.C));
     LdgKey k{__dmul_rn((double)c, pen), sz, p, f};
     if (ldg_better(k, best)) best = k;
@@ -152,7 +165,7 @@ __device__ int ldg_recheck(const DevInstance& I, const RoundCtx& R, const SpecBu
   if (d0 < 0) {
     unsigned long long mk = ~0ull;
     for (int p = lane; p < K; p += 32) {
-      const int sz = R.sizes[p] + lds(&B.pref[(size_t)p * B.wmax + o]);
+      const int sz = R.sizes[p] + dsz[p];
       const unsigned long long key = ((unsigned long long)((unsigned)sz ^ 0x80000000u) << 32) | (unsigned)p;
       mk = key < mk ? key : mk;
     }
@@ -164,10 +177,10 @@ __device__ int ldg_recheck(const DevInstance& I, const RoundCtx& R, const SpecBu
   }
   int d = d0;
   if (metric == kTV) {
-    if (R.sizes[d] + lds(&B.pref[(size_t)d * B.wmax + o]) > I.max_pw) d = own;
-    if (R.sizes[d] + lds(&B.pref[(size_t)d * B.wmax + o]) < I.min_pw) d = own;
+    if (R.sizes[d] + dsz[d] > I.max_pw) d = own;
+    if (R.sizes[d] + dsz[d] < I.min_pw) d = own;
   }
-  (void)v;
+  __syncwarp();
   return d;
 }
 
@@ -454,7 +467,10 @@ __device__ void cta_eval_ldg(const DevInstance& I, const SpecBuf& B, const Round
   }
   if (mover) {
     claim_nets(I, B, vol, z, own, d, base, deg, threadIdx.x, blockDim.x);
-    if (threadIdx.x == 0 && mt) atomicMin(&B.ctl[2 + par], z);
+    if (threadIdx.x == 0) {
+      if (mt) atomicMin(&B.ctl[2 + par], z);
+      B.mlist[atomicAdd(&B.mcnt[par], 1)] = o;
+    }
   }
   if (threadIdx.x == 0) {
     const int wv = mover ? __ldg(&I.w[v]) : 0;
@@ -473,7 +489,7 @@ __device__ void cta_eval_ldg(const DevInstance& I, const SpecBuf& B, const Round
 
 // Validation of a medium vertex by the whole CTA (the warp validation's rules).
 __device__ void cta_validate_ldg(const DevInstance& I, const SpecBuf& B, const RoundCtx& R, int metric, int z, int pos,
-                                 int q, int par, int mtpos, long long pre_w, long long pre_v) {
+                                 int q, int par, int mtpos, long long pre_w, long long pre_v, int* dsz, int nm) {
   __shared__ long long shd[2];
   __shared__ int shw;
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -503,7 +519,7 @@ __device__ void cta_validate_ldg(const DevInstance& I, const SpecBuf& B, const R
   __syncthreads();   // every thread has read shw before warp 0 may change it
   if (recheck) {
     if (wib == 0) {
-      const int d2 = ldg_recheck(I, R, B, o, v, own, metric);
+      const int d2 = ldg_recheck(I, R, B, o, own, metric, dsz, nm);
       if (lane == 0 && d2 != d) shw = 2;
     }
     __syncthreads();
@@ -765,6 +781,7 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
         if (blockIdx.x == 0 && threadIdx.x == 0) {
           B.ctl[par ^ 1] = kNone;
           B.ctl[2 + (par ^ 1)] = kNone;
+          B.mcnt[par ^ 1] = 0;
         }
         pos += 1;
         heavy_round++;
@@ -859,7 +876,10 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
         __syncwarp();
         if (mover) {
           claim_nets(I, B, vol, z, own, d, base, deg, lane, 32);
-          if (lane == 0 && mt) atomicMin(&B.ctl[2 + par], z);
+          if (lane == 0) {
+            if (mt) atomicMin(&B.ctl[2 + par], z);
+            B.mlist[atomicAdd(&B.mcnt[par], 1)] = o;
+          }
         }
         if (metric == kTV) {
           for (int wd = 0; wd < words; wd++) {
@@ -920,30 +940,6 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
         B.stats[23] += B.stats[24];
         B.stats[24] = 0;
       }
-      // ---- P: per-part prefix sums of the size changes of the window's movers
-      // (exact part sizes at every window position).
-      for (int p = gw; p < K; p += nwarps) {
-        int carry = 0;
-        int* pr = B.pref + (size_t)p * B.wmax;
-        for (int o0 = 0; o0 < span; o0 += 32) {
-          const int o = o0 + lane;
-          int dl = 0;
-          if (o < span && (lds(&B.flag[o]) & 1)) {
-            const int pk = lds(&B.dec[o]);
-            const int wv = lds(&B.wt[o]);
-            if ((pk & 0xffff) == p) dl += wv;
-            if ((pk >> 16) == p) dl -= wv;
-          }
-          int incl = dl;
-          for (int off = 1; off < 32; off <<= 1) {
-            const int t = __shfl_up_sync(kAll, incl, off);
-            if (lane >= off) incl += t;
-          }
-          if (o < span) pr[o] = carry + incl - dl;
-          carry += __shfl_sync(kAll, incl, 31);
-        }
-      }
-      if (!grid_barrier(B.bar, I.status)) return;
       // ---- B: validate.  Prefix sums of moved weight and volume drift over the
       // warps before this one (warps own consecutive position ranges).
       {
@@ -978,6 +974,7 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
         Vw += lds(&B.vsum[blockIdx.x * kSWarps + x]);
       }
       const int mtpos = lds(&B.ctl[2 + par]);
+      const int nm = lds(&B.mcnt[par]);
       for (int z = z0; z < z1; z++) {
         const int o = z - pos;
         const int fl = lds(&B.flag[o]);
@@ -991,7 +988,7 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
           // beyond the slack: decide again with the exact sizes at this position
           const int pk = lds(&B.dec[o]);
           const int own = pk >> 16;
-          const int d2 = ldg_recheck(I, R, B, o, __ldg(&I.order[z]), own, metric);
+          const int d2 = ldg_recheck(I, R, B, o, own, metric, cnt, nm);
           if (d2 != (pk & 0xffff)) {
             if (fl & 8) {
               // isolated vertex: take the exact decision (no weight, no nets, so
@@ -1027,7 +1024,7 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
       for (int mi = lower_bound_pos(B.mid_pos, B.nmid, cz0); mi < B.nmid; mi++) {
         const int z = __ldg(&B.mid_pos[mi]);
         if (z >= cz1) break;
-        cta_validate_ldg(I, B, R, metric, z, pos, q, par, mtpos, s_pre_w, s_pre_v);
+        cta_validate_ldg(I, B, R, metric, z, pos, q, par, mtpos, s_pre_w, s_pre_v, cnt_b, nm);
       }
       if (!grid_barrier(B.bar, I.status)) return;
       // ---- C: commit every mover before the cut.
@@ -1122,6 +1119,7 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
       if (gw == 0 && lane == 0) {
         B.ctl[par ^ 1] = kNone;
         B.ctl[2 + (par ^ 1)] = kNone;
+        B.mcnt[par ^ 1] = 0;
       }
       prev_maxtouch = mt_c < cut;
       if (cut == end_w) {
