@@ -132,6 +132,7 @@ def lib():
             "fp_write_patohlike": ([vp, C.c_char_p], C.c_int),
             "fp_graph_view": ([vp, C.POINTER(_Hypergraph)], C.c_int),
             "fp_graph_destroy": ([vp], C.c_int),
+            "fp_metrics_noalloc": ([i32, i32, i32, i64, vp, vp, vp, vp, vp, vp, vp], C.c_int),
             "fp_partition_gpu": ([i32, vp, vp, vp, i32, i32, i64, vp, vp, i32, vp, C.c_char_p,
                                   i32, i32, vp, vp, vp, vp], C.c_int),
         }
@@ -484,6 +485,19 @@ class Instance:
             self.close()
         except Exception:
             pass
+
+
+NOALLOC_MAX_K = 1024   # FP_NOALLOC_MAX_K
+
+
+def metrics_noalloc(K, nov, noe, pins, nptr, src, part_vec, ep_len, ep_part, out, stream=None) -> None:
+    """fp_metrics_noalloc: the six metrics of a refinement state held in the
+    caller's device memory, written to `out` (6 int64, device) on `stream`,
+    with nothing allocated by the library.  Array arguments are device
+    addresses (ints, e.g. tensor.data_ptr()); `stream` a raw CUDA stream handle
+    or None for the default stream.  The call returns before the GPU is done."""
+    _check(lib().fp_metrics_noalloc(K, nov, noe, pins, nptr, src, part_vec, ep_len, ep_part, out, stream),
+           "fp_metrics_noalloc")
 
 
 def partition_gpu(metric, row_ptr, col_ind, net_appearence, nov, noe, pins, edge_wgths, src_nodes, K,

@@ -141,6 +141,34 @@ int fp_get_lists(fp_instance* inst, int32_t* ep_len /* noe */, int32_t* ep_part 
 int fp_get_part_sizes(fp_instance* inst, int32_t* sizes /* K */);
 /* Accepted moves of each of the last refine call's passes (up to n values). */
 int fp_get_moves(fp_instance* inst, int64_t* moves, int32_t n);
+/* ---- metric evaluation that allocates nothing ----------------------------
+ * No counterpart in the reference.  For callers that must not allocate device
+ * memory through this library: a serving loop that has already reserved its
+ * whole device-memory budget (an extra cudaMalloc would overrun it or fail),
+ * or code whose device memory belongs to another allocator (a cudaMalloc /
+ * cudaFree pair beside it fragments that pool, and cudaFree waits for the
+ * whole device).  It computes the six values of fp_metrics (FP_OUT_* order)
+ * from a refinement state that the caller keeps in its own device memory:
+ * nptr (noe + 1 net offsets, pins in total), src (noe), part_vec (nov), ep_len
+ * (noe) and ep_part (pins, each net's part list at its offset), as
+ * fp_get_state lays them out.  out: 6 int64 in device memory.  The work is
+ * queued on `stream` (NULL: the default stream) and the call returns without
+ * waiting; out is valid once the stream reaches it.
+ *
+ * Its scratch is one fixed array of the library's device image (147,520
+ * bytes, held on every device that loads the library until the process
+ * exits), so K may be at most FP_NOALLOC_MAX_K; a larger K returns
+ * FP_ERR_UNSUPPORTED.  The first call on a device, with that device current,
+ * looks up the array's device address; make that first call before any stream
+ * capture.  Every call on a device uses the same array: calls that can overlap
+ * on the GPU (different streams, no ordering between them) race and give wrong
+ * values.  A state that is not consistent (a part id outside [0, K), a list
+ * longer than its net, a source outside [0, nov)) makes all six outputs -1. */
+#define FP_NOALLOC_MAX_K 1024
+int fp_metrics_noalloc(int32_t K, int32_t nov, int32_t noe, int64_t pins, const uint32_t* nptr,
+                       const int32_t* src, const int32_t* part_vec, const int32_t* ep_len,
+                       const int32_t* ep_part, int64_t* out, void* stream);
+
 /* Statistics of the last fp_refine on the grid-wide engine (up to 32 values):
  * [0] windows, [1] single-vertex rounds of high-degree vertices, [2] moves
  * committed from windows, [3..8] windows ended by: nothing (fully valid), a
