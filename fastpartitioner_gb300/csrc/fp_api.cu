@@ -377,6 +377,8 @@ int fp_instance_create(fp_ctx* ctx, const fp_hypergraph* h, int32_t K, int32_t m
   d.min_pw = (int)(pb.xw - (pb.xw * 0.1));
   const size_t KK = (size_t)K * K, words = (size_t)(K + 31) / 32;
   const bool msg = metric == FP_METRIC_TM || metric == FP_METRIC_MSM;
+  const bool cn = metric == FP_METRIC_CN;
+  const bool ldg = !msg && !cn;
   uint32_t *vptr, *vnets, *nptr, *npins;
   int *src, *w, *order;
   if ((rc = dalloc(in, &vptr, g.nov + 1)) || (rc = dalloc(in, &vnets, g.pins)) || (rc = dalloc(in, &nptr, g.noe + 1)) ||
@@ -392,7 +394,9 @@ int fp_instance_create(fp_ctx* ctx, const fp_hypergraph* h, int32_t K, int32_t m
       (rc = dalloc(in, &in->sb.flag, kSpecWindow)) || (rc = dalloc(in, &in->sb.slack, kSpecWindow)) ||
       (rc = dalloc(in, &in->sb.vslack, kSpecWindow)) || (rc = dalloc(in, &in->sb.wt, kSpecWindow)) ||
       (rc = dalloc(in, &in->sb.vd, kSpecWindow)) || (rc = dalloc(in, &in->sb.scan, (size_t)kSpecWindow * words)) ||
-      (rc = dalloc(in, &in->sb.rec, g.pins)) || (rc = dalloc(in, &in->vclass_d, g.nov)) ||
+      (rc = dalloc(in, &in->sb.rec, ldg ? g.pins : 1)) ||
+      (rc = dalloc(in, &in->sb.cn_moved, cn ? g.pins : 1)) || (rc = dalloc(in, &in->sb.cn_kcnt, cn ? g.noe : 1)) ||
+      (rc = dalloc(in, &in->sb.cn_nets, cn ? g.noe : 1)) || (rc = dalloc(in, &in->sb.cn_cnt, 4)) || (rc = dalloc(in, &in->vclass_d, g.nov)) ||
       (rc = dalloc(in, &in->sb.cand, (size_t)kSpecWindow * K)) || (rc = dalloc(in, &in->sb.ncand, kSpecWindow)) ||
       (rc = dalloc(in, &in->sb.mlist, kSpecWindow)) || (rc = dalloc(in, &in->sb.mcnt, 2)) ||
       (rc = dalloc(in, &in->sb.wsum, kMaxSpecWarps)) || (rc = dalloc(in, &in->sb.vsum, kMaxSpecWarps)) ||
@@ -496,6 +500,8 @@ int fp_refine(fp_instance* in, int32_t passes) {
     if (e == cudaSuccess) {
       if (in->pb.metric == FP_METRIC_CN) {
         e = cudaMemsetAsync(in->sb.claim64, 0, sizeof(unsigned long long) * std::max(in->g.noe, 1), s);
+        if (e == cudaSuccess) e = cudaMemsetAsync(in->sb.cn_kcnt, 0, sizeof(int) * std::max(in->g.noe, 1), s);
+        if (e == cudaSuccess) e = cudaMemsetAsync(in->sb.cn_cnt, 0, sizeof(int) * 4, s);
         if (e == cudaSuccess) e = launch_spec_cn(in->d, in->sb, passes, in->ctx->num_sms, s, &in->last_grid);
       } else if (in->pb.metric == FP_METRIC_TM || in->pb.metric == FP_METRIC_MSM) {
         e = launch_spec_msg(in->d, in->sb, passes, in->ctx->num_sms, s, &in->last_grid);

@@ -70,6 +70,10 @@ struct SpecBuf {
   int* wsum;             // [max_warps] per-warp sums of wt
   int* vsum;             // [max_warps] per-warp sums of vd
   unsigned long long* claim64;  // [noe] (round << 32) | ~position of the first claim (CN)
+  int2* cn_moved;        // [pins] CN: (pin, window offset of its acting net) of pins to move
+  int* cn_kcnt;          // [noe] CN: pins of the round's moves per net (zero between rounds)
+  int2* cn_nets;         // [noe] CN: (net, packed old/new part) of the nets those moves touch
+  int* cn_cnt;           // [4] CN: counts of cn_moved [0,1] and cn_nets [2,3] by round parity
   int* claim_m;          // [noe] first mover position changing the net's part set
   int* claim_c;          // [noe] first mover position changing only counts
   uint32_t* mask_c;      // [noe] parts (mod 32) whose counts those movers change

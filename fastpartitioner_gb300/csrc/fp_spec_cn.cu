@@ -10,7 +10,12 @@
 // its own part list, the uncut net that kept it from acting, or the nets of
 // its smaller side -- was claimed by an earlier acting net.  The first invalid
 // net cuts the window; acting nets before the cut are applied concurrently
-// (their write sets are disjoint), each moving its pins in net pin order.
+// (their write sets are disjoint).
+//
+// An acting net moves its pins one at a time in the reference, each move
+// updating every net of the pin.  All of them move old -> new, so the k moves
+// that land on one net have a result that depends on k only (cn_apply_net);
+// the commit counts the moves per net, then updates each touched net once.
 
 #include "fp_spec_common.cuh"
 
@@ -63,6 +68,84 @@ __device__ int cn_eval(const DevInstance& I, int e, int* oldp_o, int* newp_o, in
   return 1;
 }
 
+// k moves oldp -> newp of pins of net x, each the reference's REMOVAL then
+// ADDING on x's list (CN/partition.cpp:311-370), applied at once by one warp:
+// the lanes find the two slots, lane 0 replays the k steps.  Only the first
+// step can append newp and only the last can remove oldp, so the k-fold result
+// follows from the counts.
+__device__ void cn_apply_net(const DevInstance& I, int x, int oldp, int newp, int k) {
+  const int lane = threadIdx.x & 31;
+  const int s = (int)__ldg(&I.nptr[x]);
+  const int cap = (int)__ldg(&I.nptr[x + 1]) - s;
+  int n = lds(&I.ep_len[x]);
+  int jo = -1, jd = -1;
+  for (int j0 = 0; j0 < n; j0 += 32) {
+    const int j = j0 + lane;
+    const int p = j < n ? lds(&I.ep_part[s + j]) : -1;
+    const unsigned mo = __ballot_sync(kAll, p == oldp);
+    const unsigned md = __ballot_sync(kAll, p == newp);
+    if (mo && jo < 0) jo = j0 + __ffs(mo) - 1;
+    if (md && jd < 0) jd = j0 + __ffs(md) - 1;
+  }
+  if (lane == 0) {
+    int co = jo >= 0 ? lds(&I.ep_cnt[s + jo]) : 0;
+    int cd = jd >= 0 ? lds(&I.ep_cnt[s + jd]) : 0;
+    if (jo < 0 || n > cap || co < k || k < 1) {
+      dev_fail(I.status, kDevErrInvalid);
+    } else {
+      bool ok = true;
+      // oldp's count reached zero: the last entry fills its slot
+      auto remove_old = [&]() {
+        const int last = n - 1;
+        if (last != jo) {
+          if (last == jd) {
+            I.ep_part[s + jo] = newp;
+            jd = jo;
+          } else {
+            I.ep_part[s + jo] = lds(&I.ep_part[s + last]);
+            I.ep_cnt[s + jo] = lds(&I.ep_cnt[s + last]);
+          }
+        }
+        I.ep_part[s + last] = -1;
+        I.ep_cnt[s + last] = 0;
+        n = last;
+        jo = -1;
+      };
+      auto append_new = [&]() {
+        if (n >= cap) { ok = false; return; }
+        jd = n;
+        cd = 1;
+        I.ep_part[s + jd] = newp;
+        n++;
+      };
+      if (jd >= 0) {
+        co -= k;
+        cd += k;
+        if (co == 0) remove_old();
+      } else {
+        co -= 1;   // first move
+        if (co == 0) {
+          remove_old();
+          append_new();   // k == 1
+        } else {
+          append_new();
+          co -= k - 1;    // the other k - 1 moves
+          cd += k - 1;
+          if (co == 0) remove_old();
+        }
+      }
+      if (!ok) {
+        dev_fail(I.status, kDevErrInvalid);
+      } else {
+        if (jo >= 0) I.ep_cnt[s + jo] = co;
+        I.ep_cnt[s + jd] = cd;
+        I.ep_len[x] = n;
+      }
+    }
+  }
+  __syncwarp();
+}
+
 __global__ void __launch_bounds__(kSThreads) spec_cn_kernel(DevInstance I, SpecBuf B, int passes) {
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int gw = blockIdx.x * kSWarps + wib;
@@ -91,6 +174,7 @@ __global__ void __launch_bounds__(kSThreads) spec_cn_kernel(DevInstance I, SpecB
             if (lds(&I.part_vec[u]) != oldp) continue;
             const uint32_t ub = __ldg(&I.vptr[u]), ue = __ldg(&I.vptr[u + 1]);
             for (uint32_t j = ub + lane; j < ue; j += 32) atomicMax(&B.claim64[__ldg(&I.vnets[j])], ckey(round, e));
+            if (lane == 0) B.cn_moved[atomicAdd(&B.cn_cnt[par], 1)] = make_int2(u, o);
           }
         }
         if (lane == 0) {
@@ -150,35 +234,42 @@ __global__ void __launch_bounds__(kSThreads) spec_cn_kernel(DevInstance I, SpecB
         if (threadIdx.x == 0) dev_fail(I.status, kDevErrInvalid);
         return;
       }
-      // ---- C: apply acting nets before the cut; clear every acting net's claims
-      for (int e = z0; e < z1; e++) {
-        const int o = e - pos;
-        if (!lds(&B.flag[o])) continue;
-        const int pk = lds(&B.dec[o]);
-        const int oldp = pk >> 16, newp = pk & 0xffff;
-        const int pb = (int)__ldg(&I.nptr[e]), pe = (int)__ldg(&I.nptr[e + 1]);
-        if (e < cut) {
-          // pins on the smaller side, in net pin order (CN/partition.cpp:311-370);
-          // the side was fixed before any of them moved
-          for (int k = pb; k < pe; k++) {
-            const int u = (int)__ldg(&I.npins[k]);
-            if (lds(&B.flag[o]) && lds(&I.part_vec[u]) != oldp) continue;
-            const uint32_t ub = __ldg(&I.vptr[u]), ue = __ldg(&I.vptr[u + 1]);
-            for (uint32_t j = ub + lane; j < ue; j += 32) commit_net(I, u, oldp, newp, (int)__ldg(&I.vnets[j]), nullptr);
-            __syncwarp();
-            if (lane == 0) {
-              I.part_vec[u] = newp;
-              const int wv = __ldg(&I.w[u]);
-              atomicAdd(&I.part_sizes[oldp], -wv);
-              atomicAdd(&I.part_sizes[newp], wv);
-              atomicAdd((unsigned long long*)&I.moves[it], 1ull);
-              atomicAdd(&B.stats[2], 1ull);
-            }
-            __syncwarp();
-          }
+      // ---- C1: pins of acting nets before the cut: part, sizes, moves per net
+      const int nmv = lds(&B.cn_cnt[par]);
+      for (int i = gw; i < nmv; i += nwarps) {
+        const int2 mv = lds(&B.cn_moved[i]);
+        if (pos + mv.y >= cut) continue;
+        const int u = mv.x;
+        const int pk = lds(&B.dec[mv.y]);
+        const uint32_t ub = __ldg(&I.vptr[u]), ue = __ldg(&I.vptr[u + 1]);
+        for (uint32_t j = ub + lane; j < ue; j += 32) {
+          const int x = (int)__ldg(&I.vnets[j]);
+          if (atomicAdd(&B.cn_kcnt[x], 1) == 0) B.cn_nets[atomicAdd(&B.cn_cnt[2 + par], 1)] = make_int2(x, pk);
+        }
+        if (lane == 0) {
+          const int oldp = pk >> 16, newp = pk & 0xffff;
+          I.part_vec[u] = newp;
+          const int wv = __ldg(&I.w[u]);
+          atomicAdd(&I.part_sizes[oldp], -wv);
+          atomicAdd(&I.part_sizes[newp], wv);
+          atomicAdd((unsigned long long*)&I.moves[it], 1ull);
+          atomicAdd(&B.stats[2], 1ull);
         }
       }
-      if (gw == 0 && lane == 0) B.ctl[par ^ 1] = kNone;
+      if (!grid_barrier(B.bar, I.status)) return;
+      // ---- C2: every touched net once, with all of its moves
+      const int nnet = lds(&B.cn_cnt[2 + par]);
+      for (int i = gw; i < nnet; i += nwarps) {
+        const int2 xe = lds(&B.cn_nets[i]);
+        const int k = lds(&B.cn_kcnt[xe.x]);
+        cn_apply_net(I, xe.x, xe.y >> 16, xe.y & 0xffff, k);
+        if (lane == 0) B.cn_kcnt[xe.x] = 0;
+      }
+      if (gw == 0 && lane == 0) {
+        B.ctl[par ^ 1] = kNone;
+        B.cn_cnt[par ^ 1] = 0;
+        B.cn_cnt[2 + (par ^ 1)] = 0;
+      }
       if (cut == end_w) {
         if (end_w == pos + W) W = min(2 * W, B.wmax);
       } else {
