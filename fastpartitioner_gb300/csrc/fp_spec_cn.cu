@@ -35,10 +35,80 @@ __device__ __forceinline__ bool claim_before(const SpecBuf& B, int round, int x,
   return (int)(c >> 32) == round && (int)(0xffffffffu - (unsigned)(c & 0xffffffffu)) < pos;
 }
 
+// Walk of the (pin, net) pairs of net e's pins on part oldp, 32 pins at a
+// time, the pairs flattened across the warp with 4 loads in flight per lane.
+//   kMode 0: returns a net of those pins that is not cut (-1: none);
+//   kMode 1: claims every such net for position e and records the pins to move
+//            (window offset o, round parity par); returns -1;
+//   kMode 2: returns 1 if an acting net before e claimed one of them, else -1.
+template <int kMode>
+__device__ int cn_walk(const DevInstance& I, const SpecBuf& B, int e, int oldp, int round, int o, int par) {
+  const int lane = threadIdx.x & 31;
+  const int pb = (int)__ldg(&I.nptr[e]), pe = (int)__ldg(&I.nptr[e + 1]);
+  for (int b0 = pb; b0 < pe; b0 += 32) {
+    const int k = b0 + lane;
+    int u = -1, d = 0;
+    uint32_t ub = 0;
+    if (k < pe) {
+      u = (int)__ldg(&I.npins[k]);
+      if (lds(&I.part_vec[u]) == oldp) {
+        ub = __ldg(&I.vptr[u]);
+        d = (int)(__ldg(&I.vptr[u + 1]) - ub);
+      } else {
+        u = -1;
+      }
+    }
+    if (kMode == 1 && u >= 0) B.cn_moved[atomicAdd(&B.cn_cnt[par], 1)] = make_int2(u, o);
+    int incl = d;
+    for (int off = 1; off < 32; off <<= 1) {
+      const int t = __shfl_up_sync(kAll, incl, off);
+      if (lane >= off) incl += t;
+    }
+    const int total = __shfl_sync(kAll, incl, 31);
+    constexpr int kU = 4;
+    for (int f0 = 0; f0 < total; f0 += 32 * kU) {
+      int xs[kU];
+#pragma unroll
+      for (int q = 0; q < kU; q++) {
+        const int f = f0 + q * 32 + lane;
+        int lo = 0, hi = 31;
+#pragma unroll
+        for (int it = 0; it < 5; it++) {
+          const int mid = (lo + hi) >> 1;
+          const int val = __shfl_sync(kAll, incl, mid);
+          if (f < val) hi = mid; else lo = mid + 1;
+        }
+        const uint32_t bl = __shfl_sync(kAll, ub, lo);
+        const int dl = __shfl_sync(kAll, d, lo);
+        const int il = __shfl_sync(kAll, incl, lo);
+        xs[q] = f < total ? (int)__ldg(&I.vnets[bl + (uint32_t)(f - (il - dl))]) : -1;
+      }
+      if (kMode == 0) {
+        int hit = -1;
+#pragma unroll
+        for (int q = 0; q < kU; q++)
+          if (xs[q] >= 0 && hit < 0 && lds(&I.ep_len[xs[q]]) == 1) hit = xs[q];
+        const unsigned m = __ballot_sync(kAll, hit >= 0);
+        if (m) return __shfl_sync(kAll, hit, __ffs(m) - 1);
+      } else if (kMode == 1) {
+#pragma unroll
+        for (int q = 0; q < kU; q++)
+          if (xs[q] >= 0) atomicMax(&B.claim64[xs[q]], ckey(round, e));
+      } else {
+        bool c = false;
+#pragma unroll
+        for (int q = 0; q < kU; q++)
+          if (xs[q] >= 0 && claim_before(B, round, xs[q], e)) c = true;
+        if (__any_sync(kAll, c)) return 1;
+      }
+    }
+  }
+  return -1;
+}
+
 // Evaluation of net e (one warp).  Returns 0 (no move), 1 (acting), and the
 // old / new parts; *uncut = a net proving "no move" (-1 if e is not two-part).
-__device__ int cn_eval(const DevInstance& I, int e, int* oldp_o, int* newp_o, int* uncut) {
-  const int lane = threadIdx.x & 31;
+__device__ int cn_eval(const DevInstance& I, const SpecBuf& B, int e, int* oldp_o, int* newp_o, int* uncut) {
   *uncut = -1;
   if (lds(&I.ep_len[e]) != 2) return 0;
   const int s = (int)__ldg(&I.nptr[e]);
@@ -48,24 +118,9 @@ __device__ int cn_eval(const DevInstance& I, int e, int* oldp_o, int* newp_o, in
   const int newp = c1 < c2 ? p2 : p1;
   *oldp_o = oldp;
   *newp_o = newp;
-  const int pb = (int)__ldg(&I.nptr[e]), pe = (int)__ldg(&I.nptr[e + 1]);
   // any pin on the smaller side with a net that is not cut?
-  for (int k = pb; k < pe; k++) {
-    const int u = (int)__ldg(&I.npins[k]);
-    if (lds(&I.part_vec[u]) != oldp) continue;
-    const uint32_t ub = __ldg(&I.vptr[u]), ue = __ldg(&I.vptr[u + 1]);
-    for (uint32_t j0 = ub; j0 < ue; j0 += 32) {
-      const uint32_t j = j0 + lane;
-      const int x = j < ue ? (int)__ldg(&I.vnets[j]) : -1;
-      const bool unc = x >= 0 && lds(&I.ep_len[x]) == 1;
-      const unsigned m = __ballot_sync(kAll, unc);
-      if (m) {
-        *uncut = __shfl_sync(kAll, x, __ffs(m) - 1);
-        return 0;
-      }
-    }
-  }
-  return 1;
+  *uncut = cn_walk<0>(I, B, e, oldp, 0, 0, 0);
+  return *uncut < 0 ? 1 : 0;
 }
 
 // k moves oldp -> newp of pins of net x, each the reference's REMOVAL then
@@ -166,17 +221,8 @@ __global__ void __launch_bounds__(kSThreads) spec_cn_kernel(DevInstance I, SpecB
       for (int e = z0; e < z1; e++) {
         const int o = e - pos;
         int oldp = 0, newp = 0, unc = -1;
-        const int act = cn_eval(I, e, &oldp, &newp, &unc);
-        if (act) {
-          const int pb = (int)__ldg(&I.nptr[e]), pe = (int)__ldg(&I.nptr[e + 1]);
-          for (int k = pb; k < pe; k++) {
-            const int u = (int)__ldg(&I.npins[k]);
-            if (lds(&I.part_vec[u]) != oldp) continue;
-            const uint32_t ub = __ldg(&I.vptr[u]), ue = __ldg(&I.vptr[u + 1]);
-            for (uint32_t j = ub + lane; j < ue; j += 32) atomicMax(&B.claim64[__ldg(&I.vnets[j])], ckey(round, e));
-            if (lane == 0) B.cn_moved[atomicAdd(&B.cn_cnt[par], 1)] = make_int2(u, o);
-          }
-        }
+        const int act = cn_eval(I, B, e, &oldp, &newp, &unc);
+        if (act) cn_walk<1>(I, B, e, oldp, round, o, par);
         if (lane == 0) {
           B.dec[o] = (oldp << 16) | newp;
           B.flag[o] = (unsigned char)act;
@@ -201,18 +247,7 @@ __global__ void __launch_bounds__(kSThreads) spec_cn_kernel(DevInstance I, SpecB
           if (unc >= 0 && claim_before(B, round, unc, e)) conf = true;
         }
         conf = __any_sync(kAll, conf);   // warp-uniform before the pin loop's votes
-        if (act && !conf) {
-          const int oldp = lds(&B.dec[o]) >> 16;
-          const int pb = (int)__ldg(&I.nptr[e]), pe = (int)__ldg(&I.nptr[e + 1]);
-          for (int k = pb; k < pe && !conf; k++) {
-            const int u = (int)__ldg(&I.npins[k]);
-            if (lds(&I.part_vec[u]) != oldp) continue;
-            const uint32_t ub = __ldg(&I.vptr[u]), ue = __ldg(&I.vptr[u + 1]);
-            for (uint32_t j = ub + lane; j < ue; j += 32)
-              if (claim_before(B, round, (int)__ldg(&I.vnets[j]), e)) conf = true;
-            conf = __any_sync(kAll, conf);
-          }
-        }
+        if (act && !conf) conf = cn_walk<2>(I, B, e, lds(&B.dec[o]) >> 16, round, 0, 0) > 0;
         conf = __any_sync(kAll, conf);
         if (conf) {
           if (lane == 0) atomicMin(&B.ctl[par], (e << 3) | 5);
