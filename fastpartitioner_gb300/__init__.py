@@ -461,7 +461,8 @@ class Instance:
         d = {n: int(x[i]) for i, n in enumerate(names)}
         d.update(eval_ms=x[16] / 1e6, validate_ms=x[17] / 1e6, commit_ms=x[18] / 1e6, heavy_ms=x[19] / 1e6,
                  round_state_ms=x[20] / 1e6, warp_max_cycles=int(x[21]), cta_max_cycles=int(x[23]),
-                 light_cycles=int(x[25]), light_evals=int(x[26]))
+                 light_cycles=int(x[25]), light_evals=int(x[26]), cut_owncount=int(x[27]),
+                 cut_setafter=int(x[28]))
         return d
 
     def last_launches(self) -> int:

@@ -290,6 +290,12 @@ static cudaError_t clear_spec_scratch(const SpecBuf& b, int noe, int K, cudaStre
   if (e == cudaSuccess) e = cudaMemsetAsync(b.hadelta, 0, sizeof(int) * 2 * K, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(b.hmisc, 0, sizeof(int) * 16, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(b.mcnt, 0, sizeof(int) * 2, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(b.ctab_over, 0, sizeof(int) * 2, s);
+  if (e == cudaSuccess && b.ctab_mask) {
+    const size_t n = (size_t)b.ctab_mask + 1;
+    e = cudaMemsetAsync(b.ctab_key, 0xff, sizeof(unsigned long long) * n, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b.ctab_pos, 0x7f, sizeof(int) * n, s);
+  }
   return e;
 }
 
@@ -379,6 +385,10 @@ int fp_instance_create(fp_ctx* ctx, const fp_hypergraph* h, int32_t K, int32_t m
   const bool msg = metric == FP_METRIC_TM || metric == FP_METRIC_MSM;
   const bool cn = metric == FP_METRIC_CN;
   const bool ldg = !msg && !cn;
+  // exact count claims of the LDG engine: a table well above the entries of a
+  // round (two per count-only net of a window's movers)
+  size_t ctab = 4096;
+  while (ctab < (size_t)2 * g.noe && ctab < ((size_t)1 << 21)) ctab <<= 1;
   uint32_t *vptr, *vnets, *nptr, *npins;
   int *src, *w, *order;
   if ((rc = dalloc(in, &vptr, g.nov + 1)) || (rc = dalloc(in, &vnets, g.pins)) || (rc = dalloc(in, &nptr, g.noe + 1)) ||
@@ -394,7 +404,9 @@ int fp_instance_create(fp_ctx* ctx, const fp_hypergraph* h, int32_t K, int32_t m
       (rc = dalloc(in, &in->sb.flag, kSpecWindow)) || (rc = dalloc(in, &in->sb.slack, kSpecWindow)) ||
       (rc = dalloc(in, &in->sb.vslack, kSpecWindow)) || (rc = dalloc(in, &in->sb.wt, kSpecWindow)) ||
       (rc = dalloc(in, &in->sb.vd, kSpecWindow)) || (rc = dalloc(in, &in->sb.scan, (size_t)kSpecWindow * words)) ||
-      (rc = dalloc(in, &in->sb.rec, ldg ? g.pins : 1)) ||
+      (rc = dalloc(in, &in->sb.rec, ldg ? g.pins : 1)) || (rc = dalloc(in, &in->sb.rec_slot, ldg ? g.pins : 1)) ||
+      (rc = dalloc(in, &in->sb.ctab_key, ldg ? ctab : 1)) || (rc = dalloc(in, &in->sb.ctab_pos, ldg ? ctab : 1)) ||
+      (rc = dalloc(in, &in->sb.ctab_over, 2)) ||
       (rc = dalloc(in, &in->sb.cn_moved, cn ? g.pins : 1)) || (rc = dalloc(in, &in->sb.cn_kcnt, cn ? g.noe : 1)) ||
       (rc = dalloc(in, &in->sb.cn_nets, cn ? g.noe : 1)) || (rc = dalloc(in, &in->sb.cn_cnt, 4)) || (rc = dalloc(in, &in->vclass_d, g.nov)) ||
       (rc = dalloc(in, &in->sb.cand, (size_t)kSpecWindow * K)) || (rc = dalloc(in, &in->sb.ncand, kSpecWindow)) ||
@@ -416,6 +428,7 @@ int fp_instance_create(fp_ctx* ctx, const fp_hypergraph* h, int32_t K, int32_t m
   in->allocs.push_back(ms);
   in->metric_scratch = ms;
   in->sb.wmax = kSpecWindow;
+  in->sb.ctab_mask = ldg ? (unsigned)(ctab - 1) : 0u;
   in->sb.wmax_msg = kMsgWindow;
   in->sb.max_warps = kMaxSpecWarps;
   in->sb.heavy_pos = in->heavy_pos_d;

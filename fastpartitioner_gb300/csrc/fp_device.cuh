@@ -77,6 +77,11 @@ struct SpecBuf {
   int* claim_m;          // [noe] first mover position changing the net's part set
   int* claim_c;          // [noe] first mover position changing only counts
   uint32_t* mask_c;      // [noe] parts (mod 32) whose counts those movers change
+  unsigned long long* ctab_key;  // [ctab_mask + 1] open-addressed (net << 12 | part), ~0: empty
+  int* ctab_pos;         // [ctab_mask + 1] first position of a count-only mover with that (net, part)
+  uint2* rec_slot;       // [pins] table slots of a count-only move's (net, own) and (net, new part)
+  int* ctab_over;        // [2] a probe ran past its bound this round (by round parity)
+  unsigned ctab_mask;
   const int* heavy_pos;  // positions (visiting order, ascending) of vertices that get a
   int nheavy;            //     whole-grid round of their own
   const int* mid_pos;    // positions (ascending) of medium vertices, evaluated by one CTA

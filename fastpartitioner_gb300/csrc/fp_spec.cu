@@ -251,11 +251,51 @@ __device__ void locate_all(const DevInstance& I, const SpecBuf& B, int metric, i
   }
 }
 
+// Count claims, exactly: an open-addressed table from (net, part) to the first
+// window position of a count-only mover that changes that part's count on that
+// net.  Movers insert in evaluation and clear the slots they recorded at
+// commit, so the table is empty between rounds.  A probe longer than kProbe
+// marks the round (ctab_over), whose checks then fall back to the part mask.
+constexpr int kProbe = 32;
+__device__ __forceinline__ uint32_t ctab_hash(int e, int p) {
+  uint32_t h = (uint32_t)e * 0x9E3779B1u ^ ((uint32_t)p * 0x85EBCA77u);
+  return h ^ (h >> 15);
+}
+__device__ __forceinline__ unsigned long long ctab_keyof(int e, int p) {
+  return ((unsigned long long)(unsigned)e << 12) | (unsigned)p;
+}
+__device__ uint32_t ctab_insert(const SpecBuf& B, int e, int p, int z, int par) {
+  const unsigned long long key = ctab_keyof(e, p);
+  uint32_t s = ctab_hash(e, p) & B.ctab_mask;
+  for (int i = 0; i < kProbe; i++) {
+    const unsigned long long prev = atomicCAS(&B.ctab_key[s], ~0ull, key);
+    if (prev == ~0ull || prev == key) {
+      atomicMin(&B.ctab_pos[s], z);
+      return s;
+    }
+    s = (s + 1) & B.ctab_mask;
+  }
+  atomicExch(&B.ctab_over[par], 1);
+  return ~0u;
+}
+// First position of a count-only mover on (e, p); kNone if none, -1 if unknown.
+__device__ int ctab_find(const SpecBuf& B, int e, int p) {
+  const unsigned long long key = ctab_keyof(e, p);
+  uint32_t s = ctab_hash(e, p) & B.ctab_mask;
+  for (int i = 0; i < kProbe; i++) {
+    const unsigned long long k = lds(&B.ctab_key[s]);
+    if (k == key) return lds(&B.ctab_pos[s]);
+    if (k == ~0ull) return kNone;
+    s = (s + 1) & B.ctab_mask;
+  }
+  return -1;
+}
+
 // Claims of the mover at position z on its nets k0, k0 + kstep, ...: a change
 // of the part set (or, with volumes, of the source's side) takes claim_m, a
-// count-only change claim_c and the bits of the two parts.
+// count-only change claim_c, the bits of the two parts and their table entries.
 __device__ __forceinline__ void claim_nets(const DevInstance& I, const SpecBuf& B, bool vol, int z, int own, int d,
-                                           uint32_t base, int deg, int k0, int kstep) {
+                                           uint32_t base, int deg, int k0, int kstep, int par) {
   const uint32_t bits = (1u << (own & 31)) | (1u << (d & 31));
   for (int k = k0; k < deg; k += kstep) {
     const int e = (int)__ldg(&I.vnets[base + k]);
@@ -264,25 +304,45 @@ __device__ __forceinline__ void claim_nets(const DevInstance& I, const SpecBuf& 
     } else {
       atomicMin(&B.claim_c[e], z);
       atomicOr(&B.mask_c[e], bits);
+      const uint32_t s1 = ctab_insert(B, e, own, z, par);
+      const uint32_t s2 = ctab_insert(B, e, d, z, par);
+      B.rec_slot[base + k] = make_uint2(s1, s2);
+    }
+  }
+}
+
+// Clears the claims of a mover on its nets k0, k0 + kstep, ... (commit phase).
+__device__ __forceinline__ void unclaim_nets(const DevInstance& I, const SpecBuf& B, bool vol, uint32_t base, int deg,
+                                             int k0, int kstep) {
+  for (int k = k0; k < deg; k += kstep) {
+    const int e = (int)__ldg(&I.vnets[base + k]);
+    B.claim_m[e] = kNone;
+    B.claim_c[e] = kNone;
+    B.mask_c[e] = 0;
+    if (!rec_setchange(lds(&B.rec[base + k]), vol)) {
+      const uint2 sl = lds(&B.rec_slot[base + k]);
+      if (sl.x != ~0u) { B.ctab_key[sl.x] = ~0ull; B.ctab_pos[sl.x] = kNone; }
+      if (sl.y != ~0u) { B.ctab_key[sl.y] = ~0ull; B.ctab_pos[sl.y] = kNone; }
     }
   }
 }
 
 // Did an earlier mover of the window change something the vertex at z read on
-// its nets k0, k0 + kstep, ...: a part set, or the count of z's own part; or
-// does z (a mover) change the part set of a net whose counts an earlier mover
-// changes?
-__device__ __forceinline__ bool conflicts(const DevInstance& I, const SpecBuf& B, bool vol, int z, int own,
-                                          bool mover, uint32_t base, int deg, int k0, int kstep) {
+// its nets k0, k0 + kstep, ...: a part set (5), or the count of z's own part
+// (6); or does z (a mover) change the part set of a net whose counts an
+// earlier mover changes (7)?  0: none.
+__device__ __forceinline__ int conflicts(const DevInstance& I, const SpecBuf& B, bool vol, int z, int own,
+                                         bool mover, uint32_t base, int deg, int k0, int kstep, bool ov) {
   const unsigned ob = 1u << (own & 31);
-  bool conf = false;
+  int conf = 0;
   for (int k = k0; k < deg && !conf; k += kstep) {
     const int e = (int)__ldg(&I.vnets[base + k]);
     if (lds(&B.claim_m[e]) < z) {
-      conf = true;
+      conf = 5;
     } else if (lds(&B.claim_c[e]) < z) {
-      if (lds(&B.mask_c[e]) & ob) conf = true;
-      else if (mover && rec_setchange(lds(&B.rec[base + k]), vol)) conf = true;
+      const bool hit = ov ? (lds(&B.mask_c[e]) & ob) != 0 : ctab_find(B, e, own) < z;
+      if (hit) conf = 6;
+      else if (mover && rec_setchange(lds(&B.rec[base + k]), vol)) conf = 7;
     }
   }
   return conf;
@@ -466,7 +526,7 @@ __device__ void cta_eval_ldg(const DevInstance& I, const SpecBuf& B, const Round
     }
   }
   if (mover) {
-    claim_nets(I, B, vol, z, own, d, base, deg, threadIdx.x, blockDim.x);
+    claim_nets(I, B, vol, z, own, d, base, deg, threadIdx.x, blockDim.x, par);
     if (threadIdx.x == 0) {
       if (mt) atomicMin(&B.ctl[2 + par], z);
       B.mlist[atomicAdd(&B.mcnt[par], 1)] = o;
@@ -530,8 +590,10 @@ __device__ void cta_validate_ldg(const DevInstance& I, const SpecBuf& B, const R
   if (why == 0) {
     const uint32_t base = __ldg(&I.vptr[v]);
     const int deg = (int)(__ldg(&I.vptr[v + 1]) - base);
-    const bool conf = conflicts(I, B, metric != kTV, z, own, fl & 1, base, deg, threadIdx.x, blockDim.x);
-    if (__syncthreads_or(conf)) why = 5;
+    const int conf = conflicts(I, B, metric != kTV, z, own, fl & 1, base, deg, threadIdx.x, blockDim.x,
+                               lds(&B.ctab_over[par]) != 0);
+    const int c5 = __syncthreads_or(conf == 5), c6 = __syncthreads_or(conf == 6), c7 = __syncthreads_or(conf == 7);
+    why = c5 ? 5 : c6 ? 6 : c7 ? 7 : 0;
   }
   if (why && threadIdx.x == 0) atomicMin(&B.ctl[par], (z << 3) | why);
   __syncthreads();
@@ -781,6 +843,7 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
         if (blockIdx.x == 0 && threadIdx.x == 0) {
           B.ctl[par ^ 1] = kNone;
           B.ctl[2 + (par ^ 1)] = kNone;
+          B.ctab_over[par ^ 1] = 0;
           B.mcnt[par ^ 1] = 0;
         }
         pos += 1;
@@ -875,7 +938,7 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
         }
         __syncwarp();
         if (mover) {
-          claim_nets(I, B, vol, z, own, d, base, deg, lane, 32);
+          claim_nets(I, B, vol, z, own, d, base, deg, lane, 32, par);
           if (lane == 0) {
             if (mt) atomicMin(&B.ctl[2 + par], z);
             B.mlist[atomicAdd(&B.mcnt[par], 1)] = o;
@@ -1010,8 +1073,10 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
           const bool mover = fl & 1;
           const uint32_t base = __ldg(&I.vptr[v]);
           const int deg = (int)(__ldg(&I.vptr[v + 1]) - base);
-          bad = __any_sync(kAll, conflicts(I, B, vol, z, own, mover, base, deg, lane, 32));
-          why = 5;
+          const int c = conflicts(I, B, vol, z, own, mover, base, deg, lane, 32, lds(&B.ctab_over[par]) != 0);
+          const int c5 = __any_sync(kAll, c == 5), c6 = __any_sync(kAll, c == 6), c7 = __any_sync(kAll, c == 7);
+          why = c5 ? 5 : c6 ? 6 : c7 ? 7 : 0;
+          bad = why != 0;
         }
         if (bad) {
           if (lane == 0) atomicMin(&B.ctl[par], (z << 3) | why);   // position, then cut reason
@@ -1033,7 +1098,8 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
       if (blockIdx.x == 0 && threadIdx.x == 0) {
         const unsigned long long tB = gtimer();
         B.stats[0]++;
-        B.stats[3 + (cutw == kNone ? 0 : (cutw & 7))]++;
+        const int why = cutw == kNone ? 0 : (cutw & 7);
+        B.stats[why <= 5 ? 3 + why : 21 + why]++;   // 6, 7: slots 27, 28
         B.stats[9] += cut - pos;
         B.stats[17] += tB - tA;
         tA = tB;
@@ -1064,12 +1130,7 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
             atomicAdd((unsigned long long*)&I.moves[it], 1ull);
           }
         }
-        for (int k = lane; k < deg; k += 32) {
-          const int e = (int)__ldg(&I.vnets[base + k]);
-          B.claim_m[e] = kNone;
-          B.claim_c[e] = kNone;
-          B.mask_c[e] = 0;
-        }
+        unclaim_nets(I, B, vol, base, deg, lane, 32);
       }
       for (int mi = lower_bound_pos(B.mid_pos, B.nmid, cz0); mi < B.nmid; mi++) {
         const int z = __ldg(&B.mid_pos[mi]);
@@ -1094,12 +1155,7 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
             atomicAdd((unsigned long long*)&I.moves[it], 1ull);
           }
         }
-        for (int k = threadIdx.x; k < deg; k += blockDim.x) {
-          const int e = (int)__ldg(&I.vnets[base + k]);
-          B.claim_m[e] = kNone;
-          B.claim_c[e] = kNone;
-          B.mask_c[e] = 0;
-        }
+        unclaim_nets(I, B, vol, base, deg, threadIdx.x, blockDim.x);
       }
       if (metric == kTV) {
         // marker = last scanner of each part among the walked positions
@@ -1119,6 +1175,7 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
       if (gw == 0 && lane == 0) {
         B.ctl[par ^ 1] = kNone;
         B.ctl[2 + (par ^ 1)] = kNone;
+        B.ctab_over[par ^ 1] = 0;
         B.mcnt[par ^ 1] = 0;
       }
       prev_maxtouch = mt_c < cut;
