@@ -462,7 +462,8 @@ class Instance:
         d.update(eval_ms=x[16] / 1e6, validate_ms=x[17] / 1e6, commit_ms=x[18] / 1e6, heavy_ms=x[19] / 1e6,
                  round_state_ms=x[20] / 1e6, warp_max_cycles=int(x[21]), cta_max_cycles=int(x[23]),
                  light_cycles=int(x[25]), light_evals=int(x[26]), cut_owncount=int(x[27]),
-                 cut_setafter=int(x[28]))
+                 cut_setafter=int(x[28]), cta_tally_cycles=int(x[29]), cta_decide_cycles=int(x[30]),
+                 cta_rest_cycles=int(x[31]))
         return d
 
     def last_launches(self) -> int:

@@ -43,15 +43,10 @@ using namespace spec;
 constexpr int kTV = 1, kMSRV = 5;
 constexpr int kBig = 1000000000;
 
-__device__ __forceinline__ int clamp_slack(double x) {
-  if (!(x > -1.0)) return -1;
-  if (x > 1.0e9) return kBig;
-  return (int)floor(x);
-}
-
 struct RoundCtx {
   const int* sizes;
   const double* pen;
+  const float* penf;   // pen rounded to float (same sign, relative error <= 2^-24)
   const int* marker;
   const int* vol;
   const int* mark;
@@ -61,25 +56,50 @@ struct RoundCtx {
 // LDG argmax over the tallied parts (TV/partition.cpp:98-145 with TV's clamps,
 // MGV/partition.cpp:28-65 without), executed by one warp, plus the part-size
 // drift under which the outcome cannot change.
+//
+// Scores are first formed in float (count times the float-rounded penalty:
+// same sign as the exact score, relative error below 2.4e-7); the exact double
+// score and the tie-breaks are then evaluated only for parts within 1e-6 of
+// the float maximum, a set that holds the exact argmax and all its ties.  The
+// slack bounds use float lower bounds of the score gaps (a low bound only
+// costs an exact re-check).
+__device__ __forceinline__ int slack_divf(float a, float b) {
+  const float x = __fdiv_rn(a, b) * (1.0f - 1e-5f) - 1.0f;
+  if (!(x > -1.0f)) return -1;
+  if (x > 1.0e9f) return kBig;
+  return (int)floorf(x);
+}
+
 __device__ int ldg_decide(const DevInstance& I, const RoundCtx& R, const int* cnt, const unsigned long long* first,
                           int metric, int v, int own, bool first_of_window, bool* special, int* slack_out) {
   const int lane = threadIdx.x & 31;
   const int K = I.K;
-  LdgKey best{-1.0, 0, -1, ~0ull};
+  float fb = 0.0f;   // largest positive float score
   bool sp = false;
   for (int p = lane; p < K; p += 32) {
     const int c = cnt[p];
     if (c > 0) {
       const bool stale = metric == kTV && R.marker[p] == v;
       if (stale && !first_of_window) sp = true;
-      if (!stale) {
-        LdgKey k{__dmul_rn((double)(c - (p == own ? 1 : 0)), R.pen[p]), R.sizes[p], p, first[p]};
-        if (ldg_better(k, best)) best = k;
-      }
+      if (!stale) fb = fmaxf(fb, __fmul_rn((float)(c - (p == own ? 1 : 0)), R.penf[p]));
     }
   }
-  best = warp_ldg_argmax(best);
+  for (int off = 16; off; off >>= 1) fb = fmaxf(fb, __shfl_xor_sync(kAll, fb, off));
   *special = __any_sync(kAll, sp);
+  const float fcut = fb * (1.0f - 1e-6f);
+  LdgKey best{-1.0, 0, -1, ~0ull};
+  if (fb > 0.0f) {
+    for (int p = lane; p < K; p += 32) {
+      const int c = cnt[p];
+      if (c <= 0 || (metric == kTV && R.marker[p] == v)) continue;
+      const int cc = c - (p == own ? 1 : 0);
+      const float f = __fmul_rn((float)cc, R.penf[p]);
+      if (!(f > 0.0f) || f < fcut) continue;
+      LdgKey k{__dmul_rn((double)cc, R.pen[p]), R.sizes[p], p, first[p]};
+      if (ldg_better(k, best)) best = k;
+    }
+    best = warp_ldg_argmax(best);
+  }
   const int d0 = best.part >= 0 ? best.part : R.minpart;
   int d = d0;
   if (metric == kTV) {
@@ -87,23 +107,24 @@ __device__ int ldg_decide(const DevInstance& I, const RoundCtx& R, const int* cn
     if (R.sizes[d] < I.min_pw) d = own;
   }
   // Drift margins: every part's size may move by at most D.  All conditions are
-  // monotone in D; a 1e-12 relative and one-unit margin covers the rounding.
+  // monotone in D.
   int sl = kBig;
-  const double C = I.C;
+  const float Cf = (float)I.C;
   if (best.part >= 0) {
     const int w = best.part;
     const int cw = cnt[w] - (w == own ? 1 : 0);
-    const double Sw = best.score;
-    sl = min(sl, clamp_slack(Sw * C / cw * (1.0 - 1e-12)) - 1);   // stays positive
+    const float Swf = (float)best.score;
+    sl = min(sl, slack_divf(Swf * (1.0f - 1e-6f) * Cf, (float)cw) - 1);   // stays positive
     for (int q = lane; q < K; q += 32) {
       const int c = cnt[q];
       if (q == w || c <= 0) continue;
       if (metric == kTV && R.marker[q] == v) continue;
       const int cq = c - (q == own ? 1 : 0);
       if (cq <= 0) continue;
-      const double diff = Sw - __dmul_rn((double)cq, R.pen[q]);
-      if (!(diff > 0)) { sl = -1; continue; }                     // tie: size / order decide
-      sl = min(sl, clamp_slack(diff * C / (double)(cw + cq) * (1.0 - 1e-12)) - 1);
+      const float fq = __fmul_rn((float)cq, R.penf[q]);
+      const float diff = Swf - fq - 1e-6f * (fabsf(Swf) + fabsf(fq));   // below the exact gap
+      if (!(diff > 0.0f)) { sl = -1; continue; }                       // (near) tie: size / order decide
+      sl = min(sl, slack_divf(diff * Cf, (float)(cw + cq)) - 1);
     }
   } else {
     for (int q = lane; q < K; q += 32) {
@@ -111,7 +132,9 @@ __device__ int ldg_decide(const DevInstance& I, const RoundCtx& R, const int* cn
       if (c <= 0) continue;
       if (metric == kTV && R.marker[q] == v) continue;
       if (c - (q == own ? 1 : 0) <= 0) continue;
-      sl = min(sl, clamp_slack((double)R.sizes[q] - C) - 1);       // stays non-positive
+      // size - C, shrunk past float rounding of C
+      const float x = (float)R.sizes[q] - Cf - 1e-6f * Cf - 1.0f;
+      sl = min(sl, (!(x > -1.0f) ? -1 : x > 1.0e9f ? kBig : (int)floorf(x)) - 1);   // stays non-positive
     }
     sl = min(sl, (R.second - R.minsize - 1) / 2);                 // least-loaded part stays
   }
@@ -415,6 +438,7 @@ __device__ void cta_eval_ldg(const DevInstance& I, const SpecBuf& B, const Round
   const int deg = (int)(__ldg(&I.vptr[v + 1]) - base);
   int* cnt = cnt_b + (size_t)wib * K;
   unsigned long long* first = first_b + (size_t)wib * K;
+  const long long t0 = clock64();
   for (int p = lane; p < K; p += 32) { cnt[p] = 0; first[p] = ~0ull; }
   __syncwarp();
   int c1 = 0;
@@ -440,6 +464,7 @@ __device__ void cta_eval_ldg(const DevInstance& I, const SpecBuf& B, const Round
   __syncthreads();
   int c1t = 0;
   for (int x = 0; x < kSWarps; x++) c1t += iscr[x];
+  const long long t1 = clock64();
   if (wib == 0) {
     bool special;
     int slack;
@@ -478,6 +503,7 @@ __device__ void cta_eval_ldg(const DevInstance& I, const SpecBuf& B, const Round
     }
   }
   __syncthreads();
+  const long long t2 = clock64();
   const int d = sh[0];
   const bool special = sh[1] != 0;
   const int slack = sh[2];
@@ -540,6 +566,11 @@ __device__ void cta_eval_ldg(const DevInstance& I, const SpecBuf& B, const Round
     B.vslack[o] = vs;
     B.wt[o] = wv;
     B.vd[o] = mover ? vdd : 0;
+    // CTA evaluation statistics (cycles): tally and merge / decision / the rest
+    const long long t3 = clock64();
+    atomicAdd(&B.stats[29], (unsigned long long)(t1 - t0));
+    atomicAdd(&B.stats[30], (unsigned long long)(t2 - t1));
+    atomicAdd(&B.stats[31], (unsigned long long)(t3 - t2));
     const int owner = o / q - (int)blockIdx.x * kSWarps;   // warp of this CTA owning position z
     s_mw[owner] += wv;
     s_mv[owner] += mover ? vdd : 0;
@@ -618,6 +649,7 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
   Carve cv{smem_raw};
   int* sizes_s = cv.take<int>(K);
   double* pen_s = cv.take<double>(K);
+  float* penf_s = cv.take<float>(K);
   int* marker_s = cv.take<int>(K);
   int* vol_s = cv.take<int>(K);
   int* mark_s = cv.take<int>(K);
@@ -650,6 +682,7 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
         const int sz = lds(&I.part_sizes[p]);
         sizes_s[p] = sz;
         pen_s[p] = __dsub_rn(1.0, __ddiv_rn((double)sz, I.C));
+        penf_s[p] = (float)pen_s[p];
         if (metric == kTV) marker_s[p] = lds(&I.marker[p]);
         if (vol) vol_s[p] = lds(&I.send[p]) + (rv ? lds(&I.recv[p]) : 0);
       }
@@ -711,7 +744,7 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
         }
       }
       __syncthreads();
-      const RoundCtx R{sizes_s, pen_s, marker_s, vol_s, mark_s, s_minpart, s_minsize, s_second, s_maxv, s_cc};
+      const RoundCtx R{sizes_s, pen_s, penf_s, marker_s, vol_s, mark_s, s_minpart, s_minsize, s_second, s_maxv, s_cc};
       if (blockIdx.x == 0 && threadIdx.x == 0) B.stats[20] += gtimer() - tA;
       pass_start = false;
       prev_maxtouch = false;
@@ -1201,7 +1234,7 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
 size_t spec_ldg_smem_bytes(int K) {
   auto a = [](size_t n) { return (n + 15) & ~size_t(15); };
   const size_t k4 = a(sizeof(int) * K), k8 = a(sizeof(double) * K);
-  return 4 * k4 + k8 + 4 * a(sizeof(int) * (size_t)K * kSWarps) + a(sizeof(unsigned long long) * (size_t)K * kSWarps);
+  return 5 * k4 + k8 + 4 * a(sizeof(int) * (size_t)K * kSWarps) + a(sizeof(unsigned long long) * (size_t)K * kSWarps);
 }
 
 cudaError_t launch_spec_ldg(const DevInstance& I, const SpecBuf& B, int passes, int num_sms, cudaStream_t st,

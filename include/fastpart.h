@@ -180,7 +180,8 @@ int fp_metrics_noalloc(int32_t K, int32_t nov, int32_t noe, int64_t pins, const 
  * cycles and count of warp evaluations, [27] / [28] windows ended by an earlier
  * mover changing the count of the position's own part on a shared net / by a
  * part-set change after earlier count changes ([8] then counts part-set
- * changes only). */
+ * changes only), [29..31] SM cycles of CTA evaluations in tally, decision and
+ * the rest. */
 int fp_get_stats(fp_instance* inst, int64_t* out, int32_t n);
 /* Number of kernel launches the last fp_refine / fp_metrics call enqueued. */
 int fp_last_launches(fp_instance* inst, int64_t* launches);
