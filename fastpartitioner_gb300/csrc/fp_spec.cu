@@ -152,17 +152,17 @@ __device__ int ldg_decide(const DevInstance& I, const RoundCtx& R, const int* cn
 
 // The LDG decision of the vertex at window offset o again, from its stored
 // candidates and the exact part sizes at that position: round-start sizes plus
-// the moves of the window's movers before o (the mover list, nm entries),
-// summed into the warp's K-int scratch dsz.  One warp.
+// the moves of the window's movers before o -- those before offset o_from
+// already summed per part in dsz_cta (the CTA's share), the rest read from the
+// window records -- gathered in the warp's K-int scratch dsz.  One warp.
 __device__ int ldg_recheck(const DevInstance& I, const RoundCtx& R, const SpecBuf& B, int o, int own, int metric,
-                           int* dsz, int nm) {
+                           int* dsz, const int* dsz_cta, int o_from) {
   const int lane = threadIdx.x & 31;
   const int K = I.K;
-  for (int p = lane; p < K; p += 32) dsz[p] = 0;
+  for (int p = lane; p < K; p += 32) dsz[p] = dsz_cta[p];
   __syncwarp();
-  for (int i = lane; i < nm; i += 32) {
-    const int o2 = lds(&B.mlist[i]);
-    if (o2 >= o) continue;
+  for (int o2 = o_from + lane; o2 < o; o2 += 32) {
+    if (!(lds(&B.flag[o2]) & 1)) continue;
     const int w = lds(&B.wt[o2]);
     if (w == 0) continue;
     const int pk = lds(&B.dec[o2]);
@@ -172,13 +172,29 @@ __device__ int ldg_recheck(const DevInstance& I, const RoundCtx& R, const SpecBu
   __syncwarp();
   const unsigned long long* cl = B.cand + (size_t)o * K;
   const int nc = lds(&B.ncand[o]);
+  // Float scores first: the float penalty 1 - sz / C is off by less than
+  // 4e-7 * (1 + sz / C), so a score of count c by less than c times that; the
+  // bound used is 1e-6 * c * (1 + sz / C).  Exact double scores only for
+  // candidates whose upper bound reaches the largest lower bound.
+  const float Cf = (float)I.C;
+  float fb = 0.0f;
+  for (int i = lane; i < nc; i += 32) {
+    const unsigned long long ent = lds(&cl[i]);
+    const int p = (int)(ent >> 52);
+    const int c = (int)((ent >> 36) & 0xffffull);
+    const float xf = __fdiv_rn((float)(R.sizes[p] + dsz[p]), Cf);
+    fb = fmaxf(fb, __fmul_rn((float)c, 1.0f - xf) - (float)c * 1e-6f * (1.0f + fabsf(xf)));
+  }
+  for (int off = 16; off; off >>= 1) fb = fmaxf(fb, __shfl_xor_sync(kAll, fb, off));
   LdgKey best{-1.0, 0, -1, ~0ull};
   for (int i = lane; i < nc; i += 32) {
     const unsigned long long ent = lds(&cl[i]);
     const int p = (int)(ent >> 52);
     const int c = (int)((ent >> 36) & 0xffffull);
-    const unsigned long long f = (((ent >> 20) & 0xffffull) << 32) | (ent & 0xfffffull);
     const int sz = R.sizes[p] + dsz[p];
+    const float xf = __fdiv_rn((float)sz, Cf);
+    if (__fmul_rn((float)c, 1.0f - xf) + (float)c * 1e-6f * (1.0f + fabsf(xf)) < fb) continue;   // cannot be best
+    const unsigned long long f = (((ent >> 20) & 0xffffull) << 32) | (ent & 0xfffffull);
     const double pen = __dsub_rn(1.0, __ddiv_rn((double)sz, I.C));
     LdgKey k{__dmul_rn((double)c, pen), sz, p, f};
     if (ldg_better(k, best)) best = k;
@@ -580,7 +596,8 @@ __device__ void cta_eval_ldg(const DevInstance& I, const SpecBuf& B, const Round
 
 // Validation of a medium vertex by the whole CTA (the warp validation's rules).
 __device__ void cta_validate_ldg(const DevInstance& I, const SpecBuf& B, const RoundCtx& R, int metric, int z, int pos,
-                                 int q, int par, int mtpos, long long pre_w, long long pre_v, int* dsz, int nm) {
+                                 int q, int par, int mtpos, long long pre_w, long long pre_v, int* dsz,
+                                 const int* dsz_cta, int o_from) {
   __shared__ long long shd[2];
   __shared__ int shw;
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -610,7 +627,7 @@ __device__ void cta_validate_ldg(const DevInstance& I, const SpecBuf& B, const R
   __syncthreads();   // every thread has read shw before warp 0 may change it
   if (recheck) {
     if (wib == 0) {
-      const int d2 = ldg_recheck(I, R, B, o, own, metric, dsz, nm);
+      const int d2 = ldg_recheck(I, R, B, o, own, metric, dsz, dsz_cta, o_from);
       if (lane == 0 && d2 != d) shw = 2;
     }
     __syncthreads();
@@ -1071,6 +1088,22 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
       }
       const int mtpos = lds(&B.ctl[2 + par]);
       const int nm = lds(&B.mcnt[par]);
+      // part-size changes of the window's movers before this CTA's first position
+      // (phase-A scratch gains_b is free now)
+      int* dsz_cta = gains_b;
+      const int cta_o0 = cz0 - pos;
+      for (int p = threadIdx.x; p < K; p += blockDim.x) dsz_cta[p] = 0;
+      __syncthreads();
+      for (int i = threadIdx.x; i < nm; i += blockDim.x) {
+        const int o2 = lds(&B.mlist[i]);
+        if (o2 >= cta_o0) continue;
+        const int w = lds(&B.wt[o2]);
+        if (w == 0) continue;
+        const int pk = lds(&B.dec[o2]);
+        atomicAdd(&dsz_cta[pk & 0xffff], w);
+        atomicAdd(&dsz_cta[pk >> 16], -w);
+      }
+      __syncthreads();
       for (int z = z0; z < z1; z++) {
         const int o = z - pos;
         const int fl = lds(&B.flag[o]);
@@ -1084,7 +1117,7 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
           // beyond the slack: decide again with the exact sizes at this position
           const int pk = lds(&B.dec[o]);
           const int own = pk >> 16;
-          const int d2 = ldg_recheck(I, R, B, o, own, metric, cnt, nm);
+          const int d2 = ldg_recheck(I, R, B, o, own, metric, cnt, dsz_cta, cta_o0);
           if (d2 != (pk & 0xffff)) {
             if (fl & 8) {
               // isolated vertex: take the exact decision (no weight, no nets, so
@@ -1122,7 +1155,7 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
       for (int mi = lower_bound_pos(B.mid_pos, B.nmid, cz0); mi < B.nmid; mi++) {
         const int z = __ldg(&B.mid_pos[mi]);
         if (z >= cz1) break;
-        cta_validate_ldg(I, B, R, metric, z, pos, q, par, mtpos, s_pre_w, s_pre_v, cnt_b, nm);
+        cta_validate_ldg(I, B, R, metric, z, pos, q, par, mtpos, s_pre_w, s_pre_v, cnt_b, dsz_cta, cta_o0);
       }
       if (!grid_barrier(B.bar, I.status)) return;
       // ---- C: commit every mover before the cut.
