@@ -45,8 +45,7 @@ constexpr int kBig = 1000000000;
 
 struct RoundCtx {
   const int* sizes;
-  const double* pen;
-  const float* penf;   // pen rounded to float (same sign, relative error <= 2^-24)
+  const float* penf;   // 1 - size / C in float (off by < 4e-7 * (1 + size / C))
   const int* marker;
   const int* vol;
   const int* mark;
@@ -57,12 +56,14 @@ struct RoundCtx {
 // MGV/partition.cpp:28-65 without), executed by one warp, plus the part-size
 // drift under which the outcome cannot change.
 //
-// Scores are first formed in float (count times the float-rounded penalty:
-// same sign as the exact score, relative error below 2.4e-7); the exact double
-// score and the tie-breaks are then evaluated only for parts within 1e-6 of
-// the float maximum, a set that holds the exact argmax and all its ties.  The
-// slack bounds use float lower bounds of the score gaps (a low bound only
-// costs an exact re-check).
+// Scores are first formed in float from the float penalty 1 - size / C, which
+// is off by less than 4e-7 * (1 + size / C); a score of count c is bounded
+// within tol = 1e-6 * c * (1 + |size / C|).  The exact double score (the
+// reference's arithmetic) and the tie-breaks are then evaluated only for parts
+// whose upper bound reaches the largest lower bound: a set that holds the
+// exact argmax and all its ties.  The slack bounds use lower bounds of the
+// score gaps (a low bound only costs an exact re-check).
+__device__ __forceinline__ float score_tol(int c, float pf) { return (float)c * 1e-6f * (1.0f + fabsf(1.0f - pf)); }
 __device__ __forceinline__ int slack_divf(float a, float b) {
   const float x = __fdiv_rn(a, b) * (1.0f - 1e-5f) - 1.0f;
   if (!(x > -1.0f)) return -1;
@@ -74,28 +75,36 @@ __device__ int ldg_decide(const DevInstance& I, const RoundCtx& R, const int* cn
                           int metric, int v, int own, bool first_of_window, bool* special, int* slack_out) {
   const int lane = threadIdx.x & 31;
   const int K = I.K;
-  float fb = 0.0f;   // largest positive float score
-  bool sp = false;
+  float fb = 0.0f;   // largest lower bound of a score (0: none positive for sure)
+  bool sp = false, any = false;
   for (int p = lane; p < K; p += 32) {
     const int c = cnt[p];
     if (c > 0) {
       const bool stale = metric == kTV && R.marker[p] == v;
       if (stale && !first_of_window) sp = true;
-      if (!stale) fb = fmaxf(fb, __fmul_rn((float)(c - (p == own ? 1 : 0)), R.penf[p]));
+      const int cc = c - (p == own ? 1 : 0);
+      if (!stale && cc > 0) {
+        const float pf = R.penf[p];
+        const float f = __fmul_rn((float)cc, pf), t = score_tol(cc, pf);
+        fb = fmaxf(fb, f - t);
+        any |= f + t > 0.0f;
+      }
     }
   }
   for (int off = 16; off; off >>= 1) fb = fmaxf(fb, __shfl_xor_sync(kAll, fb, off));
   *special = __any_sync(kAll, sp);
-  const float fcut = fb * (1.0f - 1e-6f);
   LdgKey best{-1.0, 0, -1, ~0ull};
-  if (fb > 0.0f) {
+  if (__any_sync(kAll, any)) {
     for (int p = lane; p < K; p += 32) {
       const int c = cnt[p];
       if (c <= 0 || (metric == kTV && R.marker[p] == v)) continue;
       const int cc = c - (p == own ? 1 : 0);
-      const float f = __fmul_rn((float)cc, R.penf[p]);
-      if (!(f > 0.0f) || f < fcut) continue;
-      LdgKey k{__dmul_rn((double)cc, R.pen[p]), R.sizes[p], p, first[p]};
+      if (cc <= 0) continue;
+      const float pf = R.penf[p];
+      const float f = __fmul_rn((float)cc, pf), t = score_tol(cc, pf);
+      if (!(f + t > 0.0f) || f + t < fb) continue;   // cannot be a positive best
+      const double pen = __dsub_rn(1.0, __ddiv_rn((double)R.sizes[p], I.C));   // TV/partition.cpp:103-104
+      LdgKey k{__dmul_rn((double)cc, pen), R.sizes[p], p, first[p]};
       if (ldg_better(k, best)) best = k;
     }
     best = warp_ldg_argmax(best);
@@ -121,7 +130,8 @@ __device__ int ldg_decide(const DevInstance& I, const RoundCtx& R, const int* cn
       if (metric == kTV && R.marker[q] == v) continue;
       const int cq = c - (q == own ? 1 : 0);
       if (cq <= 0) continue;
-      const float fq = __fmul_rn((float)cq, R.penf[q]);
+      const float pq = R.penf[q];
+      const float fq = __fmul_rn((float)cq, pq) + score_tol(cq, pq);   // above the exact score
       const float diff = Swf - fq - 1e-6f * (fabsf(Swf) + fabsf(fq));   // below the exact gap
       if (!(diff > 0.0f)) { sl = -1; continue; }                       // (near) tie: size / order decide
       sl = min(sl, slack_divf(diff * Cf, (float)(cw + cq)) - 1);
@@ -665,7 +675,6 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
   const int nwarps = gridDim.x * kSWarps;
   Carve cv{smem_raw};
   int* sizes_s = cv.take<int>(K);
-  double* pen_s = cv.take<double>(K);
   float* penf_s = cv.take<float>(K);
   int* marker_s = cv.take<int>(K);
   int* vol_s = cv.take<int>(K);
@@ -698,8 +707,7 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
       for (int p = threadIdx.x; p < K; p += blockDim.x) {
         const int sz = lds(&I.part_sizes[p]);
         sizes_s[p] = sz;
-        pen_s[p] = __dsub_rn(1.0, __ddiv_rn((double)sz, I.C));
-        penf_s[p] = (float)pen_s[p];
+        penf_s[p] = 1.0f - __fdiv_rn((float)sz, (float)I.C);
         if (metric == kTV) marker_s[p] = lds(&I.marker[p]);
         if (vol) vol_s[p] = lds(&I.send[p]) + (rv ? lds(&I.recv[p]) : 0);
       }
@@ -761,7 +769,7 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
         }
       }
       __syncthreads();
-      const RoundCtx R{sizes_s, pen_s, penf_s, marker_s, vol_s, mark_s, s_minpart, s_minsize, s_second, s_maxv, s_cc};
+      const RoundCtx R{sizes_s, penf_s, marker_s, vol_s, mark_s, s_minpart, s_minsize, s_second, s_maxv, s_cc};
       if (blockIdx.x == 0 && threadIdx.x == 0) B.stats[20] += gtimer() - tA;
       pass_start = false;
       prev_maxtouch = false;
@@ -1266,8 +1274,8 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
 
 size_t spec_ldg_smem_bytes(int K) {
   auto a = [](size_t n) { return (n + 15) & ~size_t(15); };
-  const size_t k4 = a(sizeof(int) * K), k8 = a(sizeof(double) * K);
-  return 5 * k4 + k8 + 4 * a(sizeof(int) * (size_t)K * kSWarps) + a(sizeof(unsigned long long) * (size_t)K * kSWarps);
+  const size_t k4 = a(sizeof(int) * K);
+  return 5 * k4 + 4 * a(sizeof(int) * (size_t)K * kSWarps) + a(sizeof(unsigned long long) * (size_t)K * kSWarps);
 }
 
 cudaError_t launch_spec_ldg(const DevInstance& I, const SpecBuf& B, int passes, int num_sms, cudaStream_t st,
