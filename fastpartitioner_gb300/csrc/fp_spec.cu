@@ -607,7 +607,7 @@ __device__ void cta_eval_ldg(const DevInstance& I, const SpecBuf& B, const Round
 // Validation of a medium vertex by the whole CTA (the warp validation's rules).
 __device__ void cta_validate_ldg(const DevInstance& I, const SpecBuf& B, const RoundCtx& R, int metric, int z, int pos,
                                  int q, int par, int mtpos, long long pre_w, long long pre_v, int* dsz,
-                                 const int* dsz_cta, int o_from) {
+                                 const int* dsz_cta, int o_from, bool check_nets) {
   __shared__ long long shd[2];
   __shared__ int shw;
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -645,7 +645,7 @@ __device__ void cta_validate_ldg(const DevInstance& I, const SpecBuf& B, const R
   if (threadIdx.x == 0 && shw == 0) shw = V > max(lds(&B.vslack[o]), 0) ? 3 : mtpos < z ? 4 : 0;
   __syncthreads();
   int why = shw;
-  if (why == 0) {
+  if (why == 0 && check_nets) {
     const uint32_t base = __ldg(&I.vptr[v]);
     const int deg = (int)(__ldg(&I.vptr[v + 1]) - base);
     const int conf = conflicts(I, B, metric != kTV, z, own, fl & 1, base, deg, threadIdx.x, blockDim.x,
@@ -661,7 +661,7 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ unsigned long long uscr[kSWarps];
   __shared__ int iscr[kSWarps];
-  __shared__ int s_minpart, s_minsize, s_second, s_maxv, s_cc, s_count, s_d;
+  __shared__ int s_minpart, s_minsize, s_second, s_maxv, s_cc, s_count, s_d, s_spec, s_slk;
   __shared__ long long s_pre_w, s_pre_v;
   __shared__ int s_mw[kSWarps], s_mv[kSWarps];
   __shared__ int loc_b[kSWarps * 96];   // per-warp locate scratch
@@ -776,27 +776,38 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
       while (hidx < B.nheavy && __ldg(&B.heavy_pos[hidx]) < pos) hidx++;
       const int next_heavy = hidx < B.nheavy ? __ldg(&B.heavy_pos[hidx]) : I.nov;
 
-      if (next_heavy == pos) {
-        // ========================================================== heavy round
-        const int hp = heavy_round & 1;
-        int* hcnt = B.hcnt + hp * K;
-        unsigned long long* hfirst = B.hfirst + hp * K;
-        int* hgain = B.hgain + hp * K;
-        int* hloss = B.hloss + hp * K;
-        int* hadelta = B.hadelta + hp * K;
-        int* hmisc = B.hmisc + hp * 8;
-        const int v = __ldg(&I.order[pos]);
-        const int own = lds(&I.part_vec[v]);
-        const uint32_t base = __ldg(&I.vptr[v]);
-        const int deg = (int)(__ldg(&I.vptr[v + 1]) - base);
-        // A: every warp tallies a slice of the nets; CTAs pre-reduce.
+      // ================================================================= round
+      // A window holds at most one whole-grid vertex (at zs) and ends before
+      // the next one.
+      int end_w = min(pos + W, I.nov);
+      const bool sup = next_heavy < end_w;
+      const int zs = sup ? next_heavy : -1;
+      if (sup && hidx + 1 < B.nheavy) end_w = min(end_w, (int)__ldg(&B.heavy_pos[hidx + 1]));
+      const int span = end_w - pos;
+      const int q = (span + nwarps - 1) / nwarps;
+      const int z0 = min(pos + gw * q, end_w);
+      const int z1 = min(z0 + q, end_w);
+      const int gtid = blockIdx.x * blockDim.x + threadIdx.x, gthreads = gridDim.x * blockDim.x;
+      const int hp = heavy_round & 1;   // double-buffered whole-grid tallies
+      int* hcnt = B.hcnt + hp * K;
+      unsigned long long* hfirst = B.hfirst + hp * K;
+      int* hgain = B.hgain + hp * K;
+      int* hloss = B.hloss + hp * K;
+      int* hadelta = B.hadelta + hp * K;
+      int* hmisc = B.hmisc + hp * 8;
+      const int vsup = sup ? __ldg(&I.order[zs]) : 0;
+      const int own_s = sup ? lds(&I.part_vec[vsup]) : 0;
+      const uint32_t base_s = sup ? __ldg(&I.vptr[vsup]) : 0;
+      const int deg_s = sup ? (int)(__ldg(&I.vptr[vsup + 1]) - base_s) : 0;
+      // ---- A1: tally slices of the whole-grid vertex, pre-reduced per CTA
+      if (sup) {
         for (int p = lane; p < K; p += 32) { cnt[p] = 0; first[p] = ~0ull; }
         __syncwarp();
         int c1 = 0;
         {
           int n0, n1;
-          net_range(deg, gw, nwarps, &n0, &n1);
-          for (int nb = n0; nb < n1; nb += 32) c1 += tally_batch(I, own, base, nb, n1, cnt, first);
+          net_range(deg_s, gw, nwarps, &n0, &n1);
+          for (int nb = n0; nb < n1; nb += 32) c1 += tally_batch(I, own_s, base_s, nb, n1, cnt, first);
         }
         c1 = warp_sum(c1);
         __syncthreads();
@@ -814,115 +825,8 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
           }
         }
         if (lane == 0 && c1) atomicAdd(&hmisc[0], c1);
-        if (!grid_barrier(B.bar, I.status)) return;
-        // B: every CTA takes the same decision from the global tally.
-        for (int p = threadIdx.x; p < K; p += blockDim.x) {
-          cnt_b[p] = lds(&hcnt[p]);
-          first_b[p] = lds(&hfirst[p]);
-        }
-        __syncthreads();
-        if (wib == 0) {
-          bool special;
-          int slack;
-          const int d = ldg_decide(I, R, cnt_b, first_b, metric, v, own, true, &special, &slack);
-          if (lane == 0) s_d = d;
-        }
-        __syncthreads();
-        const int d = s_d;
-        const int hc1 = lds(&hmisc[0]);
-        bool mover = false;
-        if (d != own) {
-          const bool need = metric == kTV ? hc1 >= deg - cnt_b[d] : true;
-          mover = metric == kTV && need;
-          if (need) {
-            // records of all nets (every warp of the grid takes batches of 32)
-            if (vol) {
-              for (int p = lane; p < K; p += 32) { gains[p] = 0; losses[p] = 0; adelta[p] = 0; }
-              __syncwarp();
-            }
-            locate_all(I, B, metric, v, own, d, base, deg, gw, nwarps, loc, gains, losses, adelta);
-            if (vol) {
-              __syncthreads();
-              for (int p = threadIdx.x; p < K; p += blockDim.x) {
-                int g = 0, l = 0, a = 0;
-                for (int x = 0; x < kSWarps; x++) {
-                  g += gains_b[(size_t)x * K + p];
-                  l += losses_b[(size_t)x * K + p];
-                  a += adelta_b[(size_t)x * K + p];
-                }
-                if (g) atomicAdd(&hgain[p], g);
-                if (l) atomicAdd(&hloss[p], l);
-                if (a) atomicAdd(&hadelta[p], a);
-              }
-            }
-          }
-        }
-        if (!grid_barrier(B.bar, I.status)) return;
-        // C: accept test (MSV/MSRV), commit, markers, clean-up.
-        if (vol && d != own) {
-          for (int p = threadIdx.x; p < K; p += blockDim.x) {
-            gains_b[p] = lds(&hgain[p]);
-            losses_b[p] = lds(&hloss[p]);
-            adelta_b[p] = lds(&hadelta[p]);
-          }
-          __syncthreads();
-          const AcceptPart a = accept_partial(R, gains_b, losses_b, adelta_b, K, rv, threadIdx.x, blockDim.x);
-          const bool fM = __syncthreads_or(a.failM);
-          const bool fN = __syncthreads_or(a.failN);
-          const bool mt = __syncthreads_or(a.mt);
-          mover = !fM && !fN;
-          prev_maxtouch = mover && mt;
-        }
-        if (mover) {
-          for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < deg; i += gridDim.x * blockDim.x)
-            commit_rec(I, v, own, d, (int)__ldg(&I.vnets[base + i]), lds(&B.rec[base + i]), vol ? &V : nullptr);
-          if (blockIdx.x == 0 && threadIdx.x == 0) {
-            I.part_vec[v] = d;
-            const int wv = __ldg(&I.w[v]);
-            atomicAdd(&I.part_sizes[own], -wv);
-            atomicAdd(&I.part_sizes[d], wv);
-            atomicAdd((unsigned long long*)&I.moves[it], 1ull);
-          }
-        }
-        if (metric == kTV && blockIdx.x == 0)
-          for (int p = threadIdx.x; p < K; p += blockDim.x)
-            if (cnt_b[p] > 0) I.marker[p] = v;
-        {
-          const int op = hp ^ 1;   // clear the other heavy buffers for the next heavy round
-          for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < K; p += gridDim.x * blockDim.x) {
-            B.hcnt[op * K + p] = 0;
-            B.hfirst[op * K + p] = ~0ull;
-            B.hgain[op * K + p] = 0;
-            B.hloss[op * K + p] = 0;
-            B.hadelta[op * K + p] = 0;
-          }
-          if (blockIdx.x == 0 && threadIdx.x < 8) B.hmisc[op * 8 + threadIdx.x] = 0;
-        }
-        if (blockIdx.x == 0 && threadIdx.x == 0) {
-          B.ctl[par ^ 1] = kNone;
-          B.ctl[2 + (par ^ 1)] = kNone;
-          B.ctab_over[par ^ 1] = 0;
-          B.mcnt[par ^ 1] = 0;
-        }
-        pos += 1;
-        heavy_round++;
-        if (blockIdx.x == 0 && threadIdx.x == 0) {
-          B.stats[1]++;
-          const unsigned long long tH = gtimer();
-          B.stats[19] += tH - tA;
-          tA = tH;
-        }
-        round++;
-        if (!grid_barrier(B.bar, I.status)) return;
-        continue;
+        __syncthreads();   // the per-warp arrays serve the evaluations below
       }
-
-      // ============================================================ light round
-      const int end_w = min(min(pos + W, I.nov), next_heavy);
-      const int span = end_w - pos;
-      const int q = (span + nwarps - 1) / nwarps;
-      const int z0 = min(pos + gw * q, end_w);
-      const int z1 = min(z0 + q, end_w);
       // ---- A: evaluate
       int wsum = 0, vsum = 0;
       const long long cA = clock64();
@@ -1047,6 +951,122 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
         const long long dm = clock64() - cM;
         if (dm > 2000) atomicMax(&B.stats[24], (unsigned long long)dm);
       }
+      if (sup) {
+        if (!grid_barrier(B.bar, I.status)) return;
+        // ---- A2: the whole-grid vertex's decision, taken by every CTA from the
+        // global tally (first of the window or not, like any position), and its
+        // locate / gain-loss slices
+        const int os = zs - pos;
+        for (int p = threadIdx.x; p < K; p += blockDim.x) {
+          cnt_b[p] = lds(&hcnt[p]);
+          first_b[p] = lds(&hfirst[p]);
+        }
+        __syncthreads();
+        if (wib == 0) {
+          bool special;
+          int slack;
+          const int d = ldg_decide(I, R, cnt_b, first_b, metric, vsup, own_s, zs == pos, &special, &slack);
+          if (lane == 0) { s_d = d; s_spec = special ? 1 : 0; s_slk = slack; }
+          if (blockIdx.x == 0) {
+            // candidates for an exact re-check, TV's scanned parts for the markers
+            unsigned long long* cl = B.cand + (size_t)os * K;
+            int nc = 0;
+            for (int p0 = 0; p0 < K; p0 += 32) {
+              const int p = p0 + lane;
+              bool ok = false;
+              unsigned long long ent = 0;
+              if (p < K) {
+                const int c = cnt_b[p];
+                if (c > 0 && !(metric == kTV && R.marker[p] == vsup)) {
+                  ok = true;
+                  const unsigned long long f = first_b[p];
+                  ent = ((unsigned long long)p << 52) | ((unsigned long long)(c - (p == own_s ? 1 : 0)) << 36) |
+                        (((f >> 32) & 0xffffull) << 20) | (f & 0xfffffull);
+                }
+              }
+              const unsigned m = __ballot_sync(kAll, ok);
+              if (ok) cl[nc + __popc(m & ((1u << lane) - 1u))] = ent;
+              nc += __popc(m);
+            }
+            if (lane == 0) B.ncand[os] = nc;
+            if (metric == kTV) {
+              for (int wd = 0; wd < words; wd++) {
+                const int p = wd * 32 + lane;
+                const unsigned m = __ballot_sync(kAll, p < K && cnt_b[p] > 0);
+                if (lane == 0) B.scan[(size_t)os * words + wd] = m;
+              }
+            }
+          }
+        }
+        __syncthreads();
+        const int d = s_d;
+        const bool need = d != own_s && (metric == kTV ? lds(&hmisc[0]) >= deg_s - cnt_b[d] : true);
+        if (need) {
+          if (vol) {
+            for (int p = lane; p < K; p += 32) { gains[p] = 0; losses[p] = 0; adelta[p] = 0; }
+            __syncwarp();
+          }
+          locate_all(I, B, metric, vsup, own_s, d, base_s, deg_s, gw, nwarps, loc, gains, losses, adelta);
+          if (vol) {
+            __syncthreads();
+            for (int p = threadIdx.x; p < K; p += blockDim.x) {
+              int g = 0, l = 0, a = 0;
+              for (int x = 0; x < kSWarps; x++) {
+                g += gains_b[(size_t)x * K + p];
+                l += losses_b[(size_t)x * K + p];
+                a += adelta_b[(size_t)x * K + p];
+              }
+              if (g) atomicAdd(&hgain[p], g);
+              if (l) atomicAdd(&hloss[p], l);
+              if (a) atomicAdd(&hadelta[p], a);
+            }
+          }
+        }
+        if (!grid_barrier(B.bar, I.status)) return;
+        // ---- A3: accept test (MSV / MSRV) in every CTA, claims, the record
+        bool mover = metric == kTV && need, mt = false;
+        int vs = kBig, vdd = 0;
+        if (vol && need) {
+          for (int p = threadIdx.x; p < K; p += blockDim.x) {
+            gains_b[p] = lds(&hgain[p]);
+            losses_b[p] = lds(&hloss[p]);
+            adelta_b[p] = lds(&hadelta[p]);
+          }
+          __syncthreads();
+          const AcceptPart a = accept_partial(R, gains_b, losses_b, adelta_b, K, rv, threadIdx.x, blockDim.x);
+          const bool fM = __syncthreads_or(a.failM);
+          const bool fN = __syncthreads_or(a.failN);
+          const bool amt = __syncthreads_or(a.mt);
+          const int fsl = block_reduce_max(a.fsl, iscr);
+          const int msl = block_reduce_min(a.msl, iscr);
+          vdd = block_reduce_max(a.vd, iscr);
+          bool good;
+          accept_final(fM, fN, fsl, msl, &good, &vs);
+          mover = good;
+          mt = mover && amt;
+        }
+        if (mover) claim_nets(I, B, vol, zs, own_s, d, base_s, deg_s, gtid, gthreads, par);
+        const int wv = mover ? __ldg(&I.w[vsup]) : 0;
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+          B.dec[os] = (own_s << 16) | d;
+          B.flag[os] = (unsigned char)((mover ? 1 : 0) | (s_spec ? 2 : 0) | 4);
+          B.slack[os] = s_slk;
+          B.vslack[os] = vs;
+          B.wt[os] = wv;
+          B.vd[os] = mover ? vdd : 0;
+          if (mover) {
+            if (mt) atomicMin(&B.ctl[2 + par], zs);
+            B.mlist[atomicAdd(&B.mcnt[par], 1)] = os;
+          }
+        }
+        // the warp owning position zs carries its weight and volume change
+        const int owner = os / q;
+        if (threadIdx.x == 0 && owner / kSWarps == (int)blockIdx.x) {
+          s_mw[owner % kSWarps] += wv;
+          s_mv[owner % kSWarps] += mover ? vdd : 0;
+        }
+        __syncthreads();
+      }
       if (lane == 0) {
         B.wsum[gw] = wsum + s_mw[wib];
         B.vsum[gw] = vsum + s_mv[wib];
@@ -1163,7 +1183,18 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
       for (int mi = lower_bound_pos(B.mid_pos, B.nmid, cz0); mi < B.nmid; mi++) {
         const int z = __ldg(&B.mid_pos[mi]);
         if (z >= cz1) break;
-        cta_validate_ldg(I, B, R, metric, z, pos, q, par, mtpos, s_pre_w, s_pre_v, cnt_b, dsz_cta, cta_o0);
+        cta_validate_ldg(I, B, R, metric, z, pos, q, par, mtpos, s_pre_w, s_pre_v, cnt_b, dsz_cta, cta_o0, true);
+      }
+      if (sup) {
+        // the whole-grid vertex: its nets checked by every thread, the rest by the
+        // CTA owning its position
+        const int os = zs - pos;
+        const int fl = lds(&B.flag[os]);
+        const int c = conflicts(I, B, vol, zs, own_s, fl & 1, base_s, deg_s, gtid, gthreads,
+                                lds(&B.ctab_over[par]) != 0);
+        if (c) atomicMin(&B.ctl[par], (zs << 3) | c);
+        if (zs >= cz0 && zs < cz1)
+          cta_validate_ldg(I, B, R, metric, zs, pos, q, par, mtpos, s_pre_w, s_pre_v, cnt_b, dsz_cta, cta_o0, false);
       }
       if (!grid_barrier(B.bar, I.status)) return;
       // ---- C: commit every mover before the cut.
@@ -1230,6 +1261,40 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
           }
         }
         unclaim_nets(I, B, vol, base, deg, threadIdx.x, blockDim.x);
+      }
+      if (sup) {
+        // the whole-grid vertex, by every thread; then its tallies' other buffer
+        // is cleared for the next one
+        const int os = zs - pos;
+        if (lds(&B.flag[os]) & 1) {
+          const int pk = lds(&B.dec[os]);
+          const int d = pk & 0xffff;
+          if (zs < cut) {
+            for (int i = gtid; i < deg_s; i += gthreads)
+              commit_rec(I, vsup, own_s, d, (int)__ldg(&I.vnets[base_s + i]), lds(&B.rec[base_s + i]),
+                         vol ? &V : nullptr);
+            if (gtid == 0) {
+              atomicAdd(&B.stats[2], 1ull);
+              I.part_vec[vsup] = d;
+              const int wv = __ldg(&I.w[vsup]);
+              atomicAdd(&I.part_sizes[own_s], -wv);
+              atomicAdd(&I.part_sizes[d], wv);
+              atomicAdd((unsigned long long*)&I.moves[it], 1ull);
+            }
+          }
+          unclaim_nets(I, B, vol, base_s, deg_s, gtid, gthreads);
+        }
+        const int op = hp ^ 1;
+        for (int p = gtid; p < K; p += gthreads) {
+          B.hcnt[op * K + p] = 0;
+          B.hfirst[op * K + p] = ~0ull;
+          B.hgain[op * K + p] = 0;
+          B.hloss[op * K + p] = 0;
+          B.hadelta[op * K + p] = 0;
+        }
+        if (gtid < 8) B.hmisc[op * 8 + gtid] = 0;
+        if (gtid == 0) B.stats[1]++;
+        heavy_round++;
       }
       if (metric == kTV) {
         // marker = last scanner of each part among the walked positions

@@ -258,3 +258,23 @@ def test_gpu_set_state_round_trip(fp, orc, gpu_engine, metric):
     with gpu_engine.instance(hg, K, metric) as c:
         with pytest.raises(fp.FastPartError):
             c.set_state(bad["part_vec"], bad["ep_starts"], bad["ep_ends"], bad["ep_parts"], bad["ep_cnt"])
+
+
+@pytest.mark.parametrize("metric", ["TV", "MSV", "MSRV", "TM", "MSM"])
+@pytest.mark.parametrize("bounds", [(16, 64), (64, 1024)])
+def test_gpu_vertex_classes_do_not_change_results(fp, orc, gpu_engine, metric, bounds):
+    """Tiny class bounds put many vertices in CTA evaluation and in whole-grid
+    evaluation inside the windows; the results still equal the oracle."""
+    hg = fp.generate(fp.GenSpec.zipf(8000, 8000, 2.1, 2, 1500, beta=1.5, weight_rule=1, seed=71))
+    K, passes = 32, 3
+    o = orc.run_oracle(hg, K, metric, passes)
+    with gpu_engine.instance(hg, K, metric) as inst:
+        inst.set_classes(*bounds)
+        inst.initial_partition()
+        inst.refine(passes)
+        np.testing.assert_array_equal(inst.partition(), o["part_vec"], err_msg=f"{metric} {bounds}")
+        ln, pt, _ = inst.lists()
+        np.testing.assert_array_equal(orc.flat_lists(hg, ln, pt), orc.flat_lists(hg, o["ep_len"], o["ep_part"]))
+        assert inst.metrics() == o["metrics_final"], f"{metric} {bounds}"
+        st = inst.stats()
+        assert st["heavy_rounds"] > 0, f"{metric} {bounds}: no whole-grid vertex exercised"
