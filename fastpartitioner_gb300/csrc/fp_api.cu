@@ -295,6 +295,7 @@ static cudaError_t clear_spec_scratch(const SpecBuf& b, int noe, int K, cudaStre
     const size_t n = (size_t)b.ctab_mask + 1;
     e = cudaMemsetAsync(b.ctab_key, 0xff, sizeof(unsigned long long) * n, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(b.ctab_pos, 0x7f, sizeof(int) * n, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b.ctab_cnt, 0, sizeof(int) * n, s);
   }
   return e;
 }
@@ -406,6 +407,7 @@ int fp_instance_create(fp_ctx* ctx, const fp_hypergraph* h, int32_t K, int32_t m
       (rc = dalloc(in, &in->sb.vd, kSpecWindow)) || (rc = dalloc(in, &in->sb.scan, (size_t)kSpecWindow * words)) ||
       (rc = dalloc(in, &in->sb.rec, ldg ? g.pins : 1)) || (rc = dalloc(in, &in->sb.rec_slot, ldg ? g.pins : 1)) ||
       (rc = dalloc(in, &in->sb.ctab_key, ldg ? ctab : 1)) || (rc = dalloc(in, &in->sb.ctab_pos, ldg ? ctab : 1)) ||
+      (rc = dalloc(in, &in->sb.ctab_cnt, ldg ? ctab : 1)) ||
       (rc = dalloc(in, &in->sb.ctab_over, 2)) ||
       (rc = dalloc(in, &in->sb.cn_moved, cn ? g.pins : 1)) || (rc = dalloc(in, &in->sb.cn_kcnt, cn ? g.noe : 1)) ||
       (rc = dalloc(in, &in->sb.cn_nets, cn ? g.noe : 1)) || (rc = dalloc(in, &in->sb.cn_cnt, 4)) || (rc = dalloc(in, &in->vclass_d, g.nov)) ||

@@ -79,6 +79,7 @@ struct SpecBuf {
   uint32_t* mask_c;      // [noe] parts (mod 32) whose counts those movers change
   unsigned long long* ctab_key;  // [ctab_mask + 1] open-addressed (net << 12 | part), ~0: empty
   int* ctab_pos;         // [ctab_mask + 1] first position of a count-only mover with that (net, part)
+  int* ctab_cnt;         // [ctab_mask + 1] count-only movers of the round on that (net, part)
   uint2* rec_slot;       // [pins] table slots of a count-only move's (net, own) and (net, new part)
   int* ctab_over;        // [2] a probe ran past its bound this round (by round parity)
   unsigned ctab_mask;

@@ -320,6 +320,7 @@ __device__ uint32_t ctab_insert(const SpecBuf& B, int e, int p, int z, int par) 
     const unsigned long long prev = atomicCAS(&B.ctab_key[s], ~0ull, key);
     if (prev == ~0ull || prev == key) {
       atomicMin(&B.ctab_pos[s], z);
+      atomicAdd(&B.ctab_cnt[s], 1);
       return s;
     }
     s = (s + 1) & B.ctab_mask;
@@ -327,13 +328,17 @@ __device__ uint32_t ctab_insert(const SpecBuf& B, int e, int p, int z, int par) 
   atomicExch(&B.ctab_over[par], 1);
   return ~0u;
 }
-// First position of a count-only mover on (e, p); kNone if none, -1 if unknown.
-__device__ int ctab_find(const SpecBuf& B, int e, int p) {
+// First position of a count-only mover on (e, p) and the number of such movers
+// in the round (*n); kNone if none, -1 if unknown.
+__device__ int ctab_find(const SpecBuf& B, int e, int p, int* n) {
   const unsigned long long key = ctab_keyof(e, p);
   uint32_t s = ctab_hash(e, p) & B.ctab_mask;
   for (int i = 0; i < kProbe; i++) {
     const unsigned long long k = lds(&B.ctab_key[s]);
-    if (k == key) return lds(&B.ctab_pos[s]);
+    if (k == key) {
+      *n = lds(&B.ctab_cnt[s]);
+      return lds(&B.ctab_pos[s]);
+    }
     if (k == ~0ull) return kNone;
     s = (s + 1) & B.ctab_mask;
   }
@@ -370,26 +375,46 @@ __device__ __forceinline__ void unclaim_nets(const DevInstance& I, const SpecBuf
     B.mask_c[e] = 0;
     if (!rec_setchange(lds(&B.rec[base + k]), vol)) {
       const uint2 sl = lds(&B.rec_slot[base + k]);
-      if (sl.x != ~0u) { B.ctab_key[sl.x] = ~0ull; B.ctab_pos[sl.x] = kNone; }
-      if (sl.y != ~0u) { B.ctab_key[sl.y] = ~0ull; B.ctab_pos[sl.y] = kNone; }
+      if (sl.x != ~0u) { B.ctab_key[sl.x] = ~0ull; B.ctab_pos[sl.x] = kNone; B.ctab_cnt[sl.x] = 0; }
+      if (sl.y != ~0u) { B.ctab_key[sl.y] = ~0ull; B.ctab_pos[sl.y] = kNone; B.ctab_cnt[sl.y] = 0; }
     }
   }
 }
 
 // Did an earlier mover of the window change something the vertex at z read on
-// its nets k0, k0 + kstep, ...: a part set (5), or the count of z's own part
-// (6); or does z (a mover) change the part set of a net whose counts an
-// earlier mover changes (7)?  0: none.
+// its nets k0, k0 + kstep, ...?  0: nothing; 5: a part set; 6: the count of
+// z's own part where it matters; 7: z (a mover) changes the part set of a net
+// whose counts an earlier mover changes.
+//
+// Counts enter a decision only through "own has exactly one pin on the net",
+// and only when the vertex would move (cand: decision != own; its move records
+// hold own's slot).  Before the commit the count c it saw is still in place;
+// earlier count-only moves can make it 1 only if c == 1 or if at least c - 1
+// of the round's count-only movers touch (net, own).
 __device__ __forceinline__ int conflicts(const DevInstance& I, const SpecBuf& B, bool vol, int z, int own,
-                                         bool mover, uint32_t base, int deg, int k0, int kstep, bool ov) {
+                                         bool cand, bool mover, uint32_t base, int deg, int k0, int kstep, bool ov) {
   const unsigned ob = 1u << (own & 31);
   int conf = 0;
   for (int k = k0; k < deg && !conf; k += kstep) {
     const int e = (int)__ldg(&I.vnets[base + k]);
     if (lds(&B.claim_m[e]) < z) {
       conf = 5;
-    } else if (lds(&B.claim_c[e]) < z) {
-      const bool hit = ov ? (lds(&B.mask_c[e]) & ob) != 0 : ctab_find(B, e, own) < z;
+    } else if (cand && lds(&B.claim_c[e]) < z) {
+      bool hit;
+      if (ov) {
+        hit = (lds(&B.mask_c[e]) & ob) != 0;
+      } else {
+        int n = 0;
+        const int fp = ctab_find(B, e, own, &n);
+        if (fp < 0) {
+          hit = true;
+        } else if (fp >= z) {
+          hit = false;
+        } else {
+          const int c = lds(&I.ep_cnt[(int)__ldg(&I.nptr[e]) + rec_jo(lds(&B.rec[base + k]))]);
+          hit = c <= 1 || n >= c - 1;
+        }
+      }
       if (hit) conf = 6;
       else if (mover && rec_setchange(lds(&B.rec[base + k]), vol)) conf = 7;
     }
@@ -540,7 +565,7 @@ __device__ void cta_eval_ldg(const DevInstance& I, const SpecBuf& B, const Round
     // accept test on the gain / loss sums.
     const bool need = metric == kTV ? c1t >= deg - cnt_b[d] : true;
     mover = metric == kTV && need;
-    if (need) {
+    {   // records for every decision that moves: own's slot per net serves the validation
       int* gains = gains_b + (size_t)wib * K;
       int* losses = losses_b + (size_t)wib * K;
       int* adelta = adelta_b + (size_t)wib * K;
@@ -648,7 +673,7 @@ __device__ void cta_validate_ldg(const DevInstance& I, const SpecBuf& B, const R
   if (why == 0 && check_nets) {
     const uint32_t base = __ldg(&I.vptr[v]);
     const int deg = (int)(__ldg(&I.vptr[v + 1]) - base);
-    const int conf = conflicts(I, B, metric != kTV, z, own, fl & 1, base, deg, threadIdx.x, blockDim.x,
+    const int conf = conflicts(I, B, metric != kTV, z, own, d != own, fl & 1, base, deg, threadIdx.x, blockDim.x,
                                lds(&B.ctab_over[par]) != 0);
     const int c5 = __syncthreads_or(conf == 5), c6 = __syncthreads_or(conf == 6), c7 = __syncthreads_or(conf == 7);
     why = c5 ? 5 : c6 ? 6 : c7 ? 7 : 0;
@@ -883,7 +908,8 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
         if (metric == kTV) {
           if (d != own) {
             mover = c1 >= deg - cnt[d];
-            if (mover) locate_all(I, B, metric, v, own, d, base, deg, 0, 1, loc, nullptr, nullptr, nullptr);
+            // the records also serve the validation (own's slot per net)
+            locate_all(I, B, metric, v, own, d, base, deg, 0, 1, loc, nullptr, nullptr, nullptr);
           }
         } else if (d != own || iso) {
           for (int p = lane; p < K; p += 32) { gains[p] = 0; losses[p] = 0; adelta[p] = 0; }
@@ -1001,7 +1027,7 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
         __syncthreads();
         const int d = s_d;
         const bool need = d != own_s && (metric == kTV ? lds(&hmisc[0]) >= deg_s - cnt_b[d] : true);
-        if (need) {
+        if (d != own_s) {   // records for every decision that moves (the validation reads own's slots)
           if (vol) {
             for (int p = lane; p < K; p += 32) { gains[p] = 0; losses[p] = 0; adelta[p] = 0; }
             __syncwarp();
@@ -1167,7 +1193,8 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
           const bool mover = fl & 1;
           const uint32_t base = __ldg(&I.vptr[v]);
           const int deg = (int)(__ldg(&I.vptr[v + 1]) - base);
-          const int c = conflicts(I, B, vol, z, own, mover, base, deg, lane, 32, lds(&B.ctab_over[par]) != 0);
+          const int dz = lds(&B.dec[o]) & 0xffff;
+          const int c = conflicts(I, B, vol, z, own, dz != own, mover, base, deg, lane, 32, lds(&B.ctab_over[par]) != 0);
           const int c5 = __any_sync(kAll, c == 5), c6 = __any_sync(kAll, c == 6), c7 = __any_sync(kAll, c == 7);
           why = c5 ? 5 : c6 ? 6 : c7 ? 7 : 0;
           bad = why != 0;
@@ -1190,8 +1217,8 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
         // CTA owning its position
         const int os = zs - pos;
         const int fl = lds(&B.flag[os]);
-        const int c = conflicts(I, B, vol, zs, own_s, fl & 1, base_s, deg_s, gtid, gthreads,
-                                lds(&B.ctab_over[par]) != 0);
+        const int c = conflicts(I, B, vol, zs, own_s, (lds(&B.dec[os]) & 0xffff) != own_s, fl & 1, base_s, deg_s,
+                                gtid, gthreads, lds(&B.ctab_over[par]) != 0);
         if (c) atomicMin(&B.ctl[par], (zs << 3) | c);
         if (zs >= cz0 && zs < cz1)
           cta_validate_ldg(I, B, R, metric, zs, pos, q, par, mtpos, s_pre_w, s_pre_v, cnt_b, dsz_cta, cta_o0, false);
