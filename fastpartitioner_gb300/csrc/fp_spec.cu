@@ -1348,7 +1348,9 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
       if (cut == end_w) {
         if (end_w == pos + W) W = min(2 * W, B.wmax);
       } else {
-        W = max(256, min(B.wmax, 2 * (cut - pos)));
+        // regrow from the last valid length: twice it for MSV (cuts come every
+        // ~200 positions), four times for the metrics with rarer cuts
+        W = max(256, min(B.wmax, (metric == 4 ? 2 : 4) * (cut - pos)));
       }
       pos = cut;
       round++;
