@@ -454,8 +454,8 @@ class Instance:
 
     def stats(self) -> dict:
         """Round statistics of the last refine on the grid-wide engine."""
-        x = np.zeros(32, np.int64)
-        _check(lib().fp_get_stats(self._h, _ptr(x), 32), "fp_get_stats")
+        x = np.zeros(48, np.int64)
+        _check(lib().fp_get_stats(self._h, _ptr(x), 48), "fp_get_stats")
         names = ["windows", "heavy_rounds", "window_moves", "cut_none", "cut_stale", "cut_size", "cut_volume",
                  "cut_maxpart", "cut_conflict", "walked"]
         d = {n: int(x[i]) for i, n in enumerate(names)}
@@ -463,7 +463,9 @@ class Instance:
                  round_state_ms=x[20] / 1e6, warp_max_cycles=int(x[21]), cta_max_cycles=int(x[23]),
                  light_cycles=int(x[25]), light_evals=int(x[26]), cut_owncount=int(x[27]),
                  cut_setafter=int(x[28]), cta_tally_cycles=int(x[29]), cta_decide_cycles=int(x[30]),
-                 cta_rest_cycles=int(x[31]))
+                 cta_rest_cycles=int(x[31]), local_eval_ms=x[32] / 1e6, grid_vertex_ms=x[33] / 1e6,
+                 grid_tally_ms=x[34] / 1e6, local_validate_ms=x[35] / 1e6, cta_evals=int(x[40]),
+                 light_tally_cycles=int(x[41]), light_decide_cycles=int(x[42]), light_rest_cycles=int(x[43]))
         return d
 
     def last_launches(self) -> int:

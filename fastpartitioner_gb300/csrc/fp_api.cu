@@ -41,15 +41,25 @@ static bool spec_supported(int metric, int K, int max_smem) {
 // inside the window; above the super bound (or with 65536 nets or more, the
 // limit of the candidate encoding): a whole-grid round.  Windows that end
 // often (MSV moves nearly every vertex) favour a lower super bound, long ones
-// (TV, MSM) a higher one; bounds from a sweep on the c2 workload.  TM and MSM
-// use the same classes in id order.
+// (TV, MSM) a higher one; bounds from a sweep on the 4M-vertex Zipf workload.
+// TM and MSM use the same classes in id order.
 constexpr int kLightWork = 2048;
 int default_super_work(int metric) {
   switch (metric) {
     case FP_METRIC_MSV: return 16384;
-    case FP_METRIC_MSRV:
+    case FP_METRIC_MSRV: return 32768;
     case FP_METRIC_TM: return 65536;
     default: return 262144;
+  }
+}
+// Whole-grid vertices one LDG window may hold.  Each one past the window's
+// eventual cut is evaluated again in a later window, so metrics whose windows
+// end early hold fewer.
+int default_grid_verts(int metric) {
+  switch (metric) {
+    case FP_METRIC_TV: return kMaxGridVerts;
+    case FP_METRIC_MSRV: return 4;
+    default: return 2;
   }
 }
 constexpr int kMaxSpecWarps = 16384;
@@ -283,12 +293,13 @@ static cudaError_t clear_spec_scratch(const SpecBuf& b, int noe, int K, cudaStre
   cudaError_t e = cudaMemsetAsync(b.claim_m, 0x7f, sizeof(int) * ne, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(b.claim_c, 0x7f, sizeof(int) * ne, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(b.mask_c, 0, sizeof(uint32_t) * ne, s);
-  if (e == cudaSuccess) e = cudaMemsetAsync(b.hcnt, 0, sizeof(int) * 2 * K, s);
-  if (e == cudaSuccess) e = cudaMemsetAsync(b.hfirst, 0xff, sizeof(unsigned long long) * 2 * K, s);
-  if (e == cudaSuccess) e = cudaMemsetAsync(b.hgain, 0, sizeof(int) * 2 * K, s);
-  if (e == cudaSuccess) e = cudaMemsetAsync(b.hloss, 0, sizeof(int) * 2 * K, s);
-  if (e == cudaSuccess) e = cudaMemsetAsync(b.hadelta, 0, sizeof(int) * 2 * K, s);
-  if (e == cudaSuccess) e = cudaMemsetAsync(b.hmisc, 0, sizeof(int) * 16, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(b.hcnt, 0, sizeof(int) * 2 * kMaxGridVerts * K, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(b.hfirst, 0xff, sizeof(unsigned long long) * 2 * kMaxGridVerts * K, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(b.hgain, 0, sizeof(int) * 2 * kMaxGridVerts * K, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(b.hloss, 0, sizeof(int) * 2 * kMaxGridVerts * K, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(b.hadelta, 0, sizeof(int) * 2 * kMaxGridVerts * K, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(b.hmisc, 0, sizeof(int) * 16 * kMaxGridVerts, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(b.mlast, 0, sizeof(unsigned long long) * K, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(b.mcnt, 0, sizeof(int) * 2, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(b.ctab_over, 0, sizeof(int) * 2, s);
   if (e == cudaSuccess && b.ctab_mask) {
@@ -401,7 +412,7 @@ int fp_instance_create(fp_ctx* ctx, const fp_hypergraph* h, int32_t K, int32_t m
       (rc = dalloc(in, &d.zrow, msg ? K * words : 1)) || (rc = dalloc(in, &d.zcol, msg ? K * words : 1)) ||
       (rc = dalloc(in, &d.c1row, msg ? K * words : 1)) || (rc = dalloc(in, &d.c1col, msg ? K * words : 1)) ||
       (rc = dalloc(in, &d.moves, kMaxPasses)) || (rc = dalloc(in, &d.status, 1)) ||
-      (rc = dalloc(in, &in->sb.ctl, 8)) || (rc = dalloc(in, &in->sb.bar, 4)) || (rc = dalloc(in, &in->sb.stats, 32)) || (rc = dalloc(in, &in->sb.dec, std::max(kSpecWindow, kMsgWindow))) ||
+      (rc = dalloc(in, &in->sb.ctl, 8)) || (rc = dalloc(in, &in->sb.bar, 4)) || (rc = dalloc(in, &in->sb.stats, kNumStats)) || (rc = dalloc(in, &in->sb.dec, std::max(kSpecWindow, kMsgWindow))) ||
       (rc = dalloc(in, &in->sb.flag, kSpecWindow)) || (rc = dalloc(in, &in->sb.slack, kSpecWindow)) ||
       (rc = dalloc(in, &in->sb.vslack, kSpecWindow)) || (rc = dalloc(in, &in->sb.wt, kSpecWindow)) ||
       (rc = dalloc(in, &in->sb.vd, kSpecWindow)) || (rc = dalloc(in, &in->sb.scan, (size_t)kSpecWindow * words)) ||
@@ -415,10 +426,12 @@ int fp_instance_create(fp_ctx* ctx, const fp_hypergraph* h, int32_t K, int32_t m
       (rc = dalloc(in, &in->sb.mlist, kSpecWindow)) || (rc = dalloc(in, &in->sb.mcnt, 2)) ||
       (rc = dalloc(in, &in->sb.wsum, kMaxSpecWarps)) || (rc = dalloc(in, &in->sb.vsum, kMaxSpecWarps)) ||
       (rc = dalloc(in, &in->sb.claim_m, g.noe)) || (rc = dalloc(in, &in->sb.claim64, g.noe)) || (rc = dalloc(in, &in->sb.claim_c, g.noe)) ||
-      (rc = dalloc(in, &in->sb.mask_c, g.noe)) || (rc = dalloc(in, &in->sb.hcnt, 2 * K)) ||
-      (rc = dalloc(in, &in->sb.hfirst, 2 * K)) || (rc = dalloc(in, &in->sb.hgain, 2 * K)) ||
-      (rc = dalloc(in, &in->sb.hloss, 2 * K)) || (rc = dalloc(in, &in->sb.hadelta, 2 * K)) ||
-      (rc = dalloc(in, &in->sb.hmisc, 16)) || (rc = dalloc(in, &in->heavy_pos_d, g.nov)) ||
+      (rc = dalloc(in, &in->sb.mask_c, g.noe)) || (rc = dalloc(in, &in->sb.hcnt, 2 * kMaxGridVerts * K)) ||
+      (rc = dalloc(in, &in->sb.hfirst, 2 * kMaxGridVerts * K)) ||
+      (rc = dalloc(in, &in->sb.hgain, 2 * kMaxGridVerts * K)) ||
+      (rc = dalloc(in, &in->sb.hloss, 2 * kMaxGridVerts * K)) ||
+      (rc = dalloc(in, &in->sb.hadelta, 2 * kMaxGridVerts * K)) ||
+      (rc = dalloc(in, &in->sb.hmisc, 16 * kMaxGridVerts)) || (rc = dalloc(in, &in->sb.mlast, K)) || (rc = dalloc(in, &in->heavy_pos_d, g.nov)) ||
       (rc = dalloc(in, &in->mid_pos_d, g.nov)) ||
       (rc = dalloc(in, &in->metric_out, 8))) {
     fp_instance_destroy(in);
@@ -432,6 +445,7 @@ int fp_instance_create(fp_ctx* ctx, const fp_hypergraph* h, int32_t K, int32_t m
   in->sb.wmax = kSpecWindow;
   in->sb.ctab_mask = ldg ? (unsigned)(ctab - 1) : 0u;
   in->sb.wmax_msg = kMsgWindow;
+  in->sb.gmax = default_grid_verts(metric);
   in->sb.max_warps = kMaxSpecWarps;
   in->sb.heavy_pos = in->heavy_pos_d;
   in->sb.mid_pos = in->mid_pos_d;
@@ -510,7 +524,7 @@ int fp_refine(fp_instance* in, int32_t passes) {
                                 0x7fffffff, 0x7fffffff, 0x7fffffff, 0x7fffffff};
     if (e == cudaSuccess) e = cudaMemcpyAsync(in->sb.ctl, none, sizeof(none), cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(in->sb.bar, 0, sizeof(unsigned) * 4, s);
-    if (e == cudaSuccess) e = cudaMemsetAsync(in->sb.stats, 0, sizeof(unsigned long long) * 32, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(in->sb.stats, 0, sizeof(unsigned long long) * kNumStats, s);
     if (e == cudaSuccess) e = clear_spec_scratch(in->sb, in->g.noe, in->pb.K, s);
     if (e == cudaSuccess) {
       if (in->pb.metric == FP_METRIC_CN) {
@@ -721,7 +735,7 @@ int fp_get_moves(fp_instance* in, int64_t* moves, int32_t n) {
 }
 
 int fp_get_stats(fp_instance* in, int64_t* out, int32_t n) {
-  if (!in || !out || n < 0 || n > 32) return FP_ERR_INVALID;
+  if (!in || !out || n < 0 || n > kNumStats) return FP_ERR_INVALID;
   return d2h(in, out, in->sb.stats, sizeof(int64_t) * n);
 }
 

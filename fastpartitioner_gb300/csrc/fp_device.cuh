@@ -46,6 +46,12 @@ struct DevInstance {
   int* status;       // device status word, 0 = ok
 };
 
+// Round statistics kept per instance (fp_get_stats).
+constexpr int kNumStats = 48;
+
+// Whole-grid vertices one window of the LDG engine may hold.
+constexpr int kMaxGridVerts = 8;
+
 // Device buffers of the speculative engine (fp_spec.cu), allocated with the
 // instance.
 struct SpecBuf {
@@ -87,13 +93,15 @@ struct SpecBuf {
   int nheavy;            //     whole-grid round of their own
   const int* mid_pos;    // positions (ascending) of medium vertices, evaluated by one CTA
   int nmid;
-  int* hcnt;             // [2*K] heavy-vertex tally (double-buffered)
-  unsigned long long* hfirst;  // [2*K]
-  int* hgain;            // [2*K]
-  int* hloss;            // [2*K]
-  int* hadelta;          // [2*K]
-  int* hmisc;            // [16]
-  unsigned long long* stats;  // [32] round statistics (see fp_get_stats)
+  int* hcnt;             // [2 * kMaxGridVerts * K] whole-grid vertex tallies, by round parity
+  unsigned long long* hfirst;  //     and slot (the TM / MSM engine uses slot 0)
+  int* hgain;            // [2 * kMaxGridVerts * K]
+  int* hloss;            // [2 * kMaxGridVerts * K]
+  int* hadelta;          // [2 * kMaxGridVerts * K]
+  int* hmisc;            // [2 * kMaxGridVerts * 8]
+  unsigned long long* mlast;  // [K] TV: (window stamp << 32) | last position whose scan holds the part
+  int gmax;              // whole-grid vertices one LDG window may hold (1 .. kMaxGridVerts)
+  unsigned long long* stats;  // [kNumStats] round statistics (see fp_get_stats)
   int wmax;              // longest window of the LDG and CN engines
   int wmax_msg;          // longest window of the TM / MSM engine (dec only)
   int max_warps;

@@ -50,6 +50,7 @@ struct RoundCtx {
   const int* vol;
   const int* mark;
   int minpart, minsize, second, maxv, cc;
+  float Cf;            // C rounded to float
 };
 
 // LDG argmax over the tallied parts (TV/partition.cpp:98-145 with TV's clamps,
@@ -71,64 +72,124 @@ __device__ __forceinline__ int slack_divf(float a, float b) {
   return (int)floorf(x);
 }
 
+// Candidate entry of a part for the exact re-check: part, count without the
+// vertex itself, first sighting (net index, slot).
+__device__ __forceinline__ unsigned long long cand_entry(int p, int c, unsigned long long f) {
+  return ((unsigned long long)p << 52) | ((unsigned long long)c << 36) | (((f >> 32) & 0xffffull) << 20) |
+         (f & 0xfffffull);
+}
+
+// One warp.  The tallied parts (count > 0, no stale TV marker) are first
+// compacted, in ascending order, into list (K ints of warp scratch); cand /
+// *ncand (if cand is not null) receive their re-check entries and scan (if not
+// null) TV's scanned-part bits.  The bound, exact and slack passes then walk
+// only the compacted parts.
 __device__ int ldg_decide(const DevInstance& I, const RoundCtx& R, const int* cnt, const unsigned long long* first,
-                          int metric, int v, int own, bool first_of_window, bool* special, int* slack_out) {
+                          int metric, int v, int own, bool first_of_window, int* list, unsigned long long* cand,
+                          int* ncand, uint32_t* scan, bool* special, int* slack_out) {
   const int lane = threadIdx.x & 31;
+  const unsigned below = (1u << lane) - 1u;
   const int K = I.K;
+  const bool tv = metric == kTV;
+  int nc = 0;
+  bool sp = false;
+#pragma unroll 4
+  for (int p0 = 0; p0 < K; p0 += 32) {
+    const int p = p0 + lane;
+    const int c = p < K ? cnt[p] : 0;
+    const bool stale = tv && c > 0 && R.marker[p] == v;
+    sp |= stale;
+    const bool ok = c > 0 && !stale;
+    const unsigned m = __ballot_sync(kAll, ok);
+    if (ok) {
+      const int i = nc + __popc(m & below);
+      list[i] = p;
+      if (cand) cand[i] = cand_entry(p, c - (p == own ? 1 : 0), first[p]);
+    }
+    if (scan) {
+      const unsigned ms = __ballot_sync(kAll, c > 0);
+      if (lane == 0) scan[p0 >> 5] = ms;
+    }
+    nc += __popc(m);
+  }
+  if (cand && lane == 0) *ncand = nc;
+  *special = __any_sync(kAll, sp) && !first_of_window;
+  __syncwarp();
   float fb = 0.0f;   // largest lower bound of a score (0: none positive for sure)
-  bool sp = false, any = false;
-  for (int p = lane; p < K; p += 32) {
-    const int c = cnt[p];
-    if (c > 0) {
-      const bool stale = metric == kTV && R.marker[p] == v;
-      if (stale && !first_of_window) sp = true;
-      const int cc = c - (p == own ? 1 : 0);
-      if (!stale && cc > 0) {
-        const float pf = R.penf[p];
-        const float f = __fmul_rn((float)cc, pf), t = score_tol(cc, pf);
-        fb = fmaxf(fb, f - t);
-        any |= f + t > 0.0f;
-      }
+  bool any = false;
+  for (int i = lane; i < nc; i += 32) {
+    const int p = list[i];
+    const int cc = cnt[p] - (p == own ? 1 : 0);
+    if (cc > 0) {
+      const float pf = R.penf[p];
+      const float f = __fmul_rn((float)cc, pf), t = score_tol(cc, pf);
+      fb = fmaxf(fb, f - t);
+      any |= f + t > 0.0f;
     }
   }
   for (int off = 16; off; off >>= 1) fb = fmaxf(fb, __shfl_xor_sync(kAll, fb, off));
-  *special = __any_sync(kAll, sp);
   LdgKey best{-1.0, 0, -1, ~0ull};
+  float sbest = 0.0f;   // a lower bound of the winner's exact score, in float
   if (__any_sync(kAll, any)) {
-    for (int p = lane; p < K; p += 32) {
-      const int c = cnt[p];
-      if (c <= 0 || (metric == kTV && R.marker[p] == v)) continue;
-      const int cc = c - (p == own ? 1 : 0);
+    // Parts whose upper bound reaches the largest lower bound: the argmax and
+    // all its ties are among them.  A single one with a positive lower bound
+    // is the argmax outright (every other score lies below fb); otherwise the
+    // exact double scores (TV/partition.cpp:103-104) and tie-breaks decide.
+    int nnear = 0, np = -1;
+    float nlo = 0.0f;
+    for (int i = lane; i < nc; i += 32) {
+      const int p = list[i];
+      const int cc = cnt[p] - (p == own ? 1 : 0);
       if (cc <= 0) continue;
       const float pf = R.penf[p];
       const float f = __fmul_rn((float)cc, pf), t = score_tol(cc, pf);
-      if (!(f + t > 0.0f) || f + t < fb) continue;   // cannot be a positive best
-      const double pen = __dsub_rn(1.0, __ddiv_rn((double)R.sizes[p], I.C));   // TV/partition.cpp:103-104
-      LdgKey k{__dmul_rn((double)cc, pen), R.sizes[p], p, first[p]};
-      if (ldg_better(k, best)) best = k;
+      if (!(f + t > 0.0f) || f + t < fb) continue;
+      nnear++;
+      np = p;
+      nlo = f - t;
     }
-    best = warp_ldg_argmax(best);
+    const int tot = __reduce_add_sync(kAll, nnear);
+    const unsigned hn = __ballot_sync(kAll, nnear > 0);
+    const int src = __ffs(hn) - 1;
+    const float lo1 = __shfl_sync(kAll, nlo, src);
+    if (tot == 1 && lo1 > 0.0f) {
+      best.part = __shfl_sync(kAll, np, src);
+      sbest = lo1;
+    } else {
+      for (int i = lane; i < nc; i += 32) {
+        const int p = list[i];
+        const int cc = cnt[p] - (p == own ? 1 : 0);
+        if (cc <= 0) continue;
+        const float pf = R.penf[p];
+        const float f = __fmul_rn((float)cc, pf), t = score_tol(cc, pf);
+        if (!(f + t > 0.0f) || f + t < fb) continue;   // cannot be a positive best
+        const double pen = __dsub_rn(1.0, __ddiv_rn((double)R.sizes[p], I.C));   // TV/partition.cpp:103-104
+        LdgKey k{__dmul_rn((double)cc, pen), R.sizes[p], p, first[p]};
+        if (ldg_better(k, best)) best = k;
+      }
+      best = warp_ldg_argmax(best);
+      sbest = (float)best.score;
+    }
   }
   const int d0 = best.part >= 0 ? best.part : R.minpart;
   int d = d0;
-  if (metric == kTV) {
+  if (tv) {
     if (R.sizes[d] > I.max_pw) d = own;
     if (R.sizes[d] < I.min_pw) d = own;
   }
   // Drift margins: every part's size may move by at most D.  All conditions are
   // monotone in D.
   int sl = kBig;
-  const float Cf = (float)I.C;
+  const float Cf = R.Cf;
   if (best.part >= 0) {
     const int w = best.part;
     const int cw = cnt[w] - (w == own ? 1 : 0);
-    const float Swf = (float)best.score;
+    const float Swf = sbest;
     sl = min(sl, slack_divf(Swf * (1.0f - 1e-6f) * Cf, (float)cw) - 1);   // stays positive
-    for (int q = lane; q < K; q += 32) {
-      const int c = cnt[q];
-      if (q == w || c <= 0) continue;
-      if (metric == kTV && R.marker[q] == v) continue;
-      const int cq = c - (q == own ? 1 : 0);
+    for (int i = lane; i < nc; i += 32) {
+      const int q = list[i];
+      if (q == w) continue;
+      const int cq = cnt[q] - (q == own ? 1 : 0);
       if (cq <= 0) continue;
       const float pq = R.penf[q];
       const float fq = __fmul_rn((float)cq, pq) + score_tol(cq, pq);   // above the exact score
@@ -137,18 +198,16 @@ __device__ int ldg_decide(const DevInstance& I, const RoundCtx& R, const int* cn
       sl = min(sl, slack_divf(diff * Cf, (float)(cw + cq)) - 1);
     }
   } else {
-    for (int q = lane; q < K; q += 32) {
-      const int c = cnt[q];
-      if (c <= 0) continue;
-      if (metric == kTV && R.marker[q] == v) continue;
-      if (c - (q == own ? 1 : 0) <= 0) continue;
+    for (int i = lane; i < nc; i += 32) {
+      const int q = list[i];
+      if (cnt[q] - (q == own ? 1 : 0) <= 0) continue;
       // size - C, shrunk past float rounding of C
       const float x = (float)R.sizes[q] - Cf - 1e-6f * Cf - 1.0f;
       sl = min(sl, (!(x > -1.0f) ? -1 : x > 1.0e9f ? kBig : (int)floorf(x)) - 1);   // stays non-positive
     }
     sl = min(sl, (R.second - R.minsize - 1) / 2);                 // least-loaded part stays
   }
-  if (metric == kTV) {
+  if (tv) {
     const int s0 = R.sizes[d0];
     sl = min(sl, s0 > I.max_pw ? s0 - I.max_pw - 1 : I.max_pw - s0);
     const int d1 = s0 > I.max_pw ? own : d0;
@@ -186,7 +245,7 @@ __device__ int ldg_recheck(const DevInstance& I, const RoundCtx& R, const SpecBu
   // 4e-7 * (1 + sz / C), so a score of count c by less than c times that; the
   // bound used is 1e-6 * c * (1 + sz / C).  Exact double scores only for
   // candidates whose upper bound reaches the largest lower bound.
-  const float Cf = (float)I.C;
+  const float Cf = R.Cf;
   float fb = 0.0f;
   for (int i = lane; i < nc; i += 32) {
     const unsigned long long ent = lds(&cl[i]);
@@ -196,20 +255,35 @@ __device__ int ldg_recheck(const DevInstance& I, const RoundCtx& R, const SpecBu
     fb = fmaxf(fb, __fmul_rn((float)c, 1.0f - xf) - (float)c * 1e-6f * (1.0f + fabsf(xf)));
   }
   for (int off = 16; off; off >>= 1) fb = fmaxf(fb, __shfl_xor_sync(kAll, fb, off));
-  LdgKey best{-1.0, 0, -1, ~0ull};
+  // a single part reaching fb > 0 is the argmax outright (as in ldg_decide)
+  int nnear = 0, np = -1;
   for (int i = lane; i < nc; i += 32) {
     const unsigned long long ent = lds(&cl[i]);
     const int p = (int)(ent >> 52);
     const int c = (int)((ent >> 36) & 0xffffull);
-    const int sz = R.sizes[p] + dsz[p];
-    const float xf = __fdiv_rn((float)sz, Cf);
+    const float xf = __fdiv_rn((float)(R.sizes[p] + dsz[p]), Cf);
     if (__fmul_rn((float)c, 1.0f - xf) + (float)c * 1e-6f * (1.0f + fabsf(xf)) < fb) continue;   // cannot be best
-    const unsigned long long f = (((ent >> 20) & 0xffffull) << 32) | (ent & 0xfffffull);
-    const double pen = __dsub_rn(1.0, __ddiv_rn((double)sz, I.C));
-    LdgKey k{__dmul_rn((double)c, pen), sz, p, f};
-    if (ldg_better(k, best)) best = k;
+    nnear++;
+    np = p;
   }
-  best = warp_ldg_argmax(best);
+  LdgKey best{-1.0, 0, -1, ~0ull};
+  if (fb > 0.0f && __reduce_add_sync(kAll, nnear) == 1) {
+    best.part = __shfl_sync(kAll, np, __ffs(__ballot_sync(kAll, nnear > 0)) - 1);
+  } else {
+    for (int i = lane; i < nc; i += 32) {
+      const unsigned long long ent = lds(&cl[i]);
+      const int p = (int)(ent >> 52);
+      const int c = (int)((ent >> 36) & 0xffffull);
+      const int sz = R.sizes[p] + dsz[p];
+      const float xf = __fdiv_rn((float)sz, Cf);
+      if (__fmul_rn((float)c, 1.0f - xf) + (float)c * 1e-6f * (1.0f + fabsf(xf)) < fb) continue;   // cannot be best
+      const unsigned long long f = (((ent >> 20) & 0xffffull) << 32) | (ent & 0xfffffull);
+      const double pen = __dsub_rn(1.0, __ddiv_rn((double)sz, I.C));
+      LdgKey k{__dmul_rn((double)c, pen), sz, p, f};
+      if (ldg_better(k, best)) best = k;
+    }
+    best = warp_ldg_argmax(best);
+  }
   int d0 = best.part;
   if (d0 < 0) {
     unsigned long long mk = ~0ull;
@@ -519,35 +593,9 @@ __device__ void cta_eval_ldg(const DevInstance& I, const SpecBuf& B, const Round
   if (wib == 0) {
     bool special;
     int slack;
-    const int d = ldg_decide(I, R, cnt_b, first_b, metric, v, own, z == pos, &special, &slack);
-    unsigned long long* cl = B.cand + (size_t)o * K;
-    int nc = 0;
-    for (int p0 = 0; p0 < K; p0 += 32) {
-      const int p = p0 + lane;
-      bool ok = false;
-      unsigned long long ent = 0;
-      if (p < K) {
-        const int c = cnt_b[p];
-        if (c > 0 && !(metric == kTV && R.marker[p] == v)) {
-          ok = true;
-          const unsigned long long f = first_b[p];
-          ent = ((unsigned long long)p << 52) | ((unsigned long long)(c - (p == own ? 1 : 0)) << 36) |
-                (((f >> 32) & 0xffffull) << 20) | (f & 0xfffffull);
-        }
-      }
-      const unsigned m = __ballot_sync(kAll, ok);
-      if (ok) cl[nc + __popc(m & ((1u << lane) - 1u))] = ent;
-      nc += __popc(m);
-    }
-    if (metric == kTV) {
-      for (int wd = 0; wd < words; wd++) {
-        const int p = wd * 32 + lane;
-        const unsigned m = __ballot_sync(kAll, p < K && cnt_b[p] > 0);
-        if (lane == 0) B.scan[(size_t)o * words + wd] = m;
-      }
-    }
+    const int d = ldg_decide(I, R, cnt_b, first_b, metric, v, own, z == pos, gains_b, B.cand + (size_t)o * K,
+                             &B.ncand[o], metric == kTV ? B.scan + (size_t)o * words : nullptr, &special, &slack);
     if (lane == 0) {
-      B.ncand[o] = nc;
       sh[0] = d;
       sh[1] = special ? 1 : 0;
       sh[2] = slack;
@@ -622,6 +670,7 @@ __device__ void cta_eval_ldg(const DevInstance& I, const SpecBuf& B, const Round
     atomicAdd(&B.stats[29], (unsigned long long)(t1 - t0));
     atomicAdd(&B.stats[30], (unsigned long long)(t2 - t1));
     atomicAdd(&B.stats[31], (unsigned long long)(t3 - t2));
+    atomicAdd(&B.stats[40], 1ull);
     const int owner = o / q - (int)blockIdx.x * kSWarps;   // warp of this CTA owning position z
     s_mw[owner] += wv;
     s_mv[owner] += mover ? vdd : 0;
@@ -682,11 +731,18 @@ __device__ void cta_validate_ldg(const DevInstance& I, const SpecBuf& B, const R
   __syncthreads();
 }
 
+static_assert(kMaxGridVerts <= kSWarps, "one warp decides each whole-grid vertex of a window");
+
 __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, SpecBuf B, int passes) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ unsigned long long uscr[kSWarps];
   __shared__ int iscr[kSWarps];
-  __shared__ int s_minpart, s_minsize, s_second, s_maxv, s_cc, s_count, s_d, s_spec, s_slk;
+  __shared__ int s_minpart, s_minsize, s_second, s_maxv, s_cc, s_count;
+  // the window's whole-grid vertices: position, vertex, own part, first net
+  // index, degree, decision, stale-marker risk, size slack
+  __shared__ int s_gz[kMaxGridVerts], s_gv[kMaxGridVerts], s_go[kMaxGridVerts], s_gd[kMaxGridVerts];
+  __shared__ uint32_t s_gb[kMaxGridVerts];
+  __shared__ int s_gdec[kMaxGridVerts], s_gspec[kMaxGridVerts], s_gslk[kMaxGridVerts];
   __shared__ long long s_pre_w, s_pre_v;
   __shared__ int s_mw[kSWarps], s_mv[kSWarps];
   __shared__ int loc_b[kSWarps * 96];   // per-warp locate scratch
@@ -698,6 +754,7 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int gw = blockIdx.x * kSWarps + wib;
   const int nwarps = gridDim.x * kSWarps;
+  const float Cf = (float)I.C;
   Carve cv{smem_raw};
   int* sizes_s = cv.take<int>(K);
   float* penf_s = cv.take<float>(K);
@@ -732,8 +789,19 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
       for (int p = threadIdx.x; p < K; p += blockDim.x) {
         const int sz = lds(&I.part_sizes[p]);
         sizes_s[p] = sz;
-        penf_s[p] = 1.0f - __fdiv_rn((float)sz, (float)I.C);
-        if (metric == kTV) marker_s[p] = lds(&I.marker[p]);
+        penf_s[p] = 1.0f - __fdiv_rn((float)sz, Cf);
+        if (metric == kTV) {
+          // a part scanned in the last window takes its last scanner as marker
+          // (block 0 stores it; the others read only parts not scanned there)
+          const unsigned long long ml = lds(&B.mlast[p]);
+          if (round > 0 && (int)(ml >> 32) == round) {
+            const int mv = __ldg(&I.order[(int)(ml & 0xffffffffu)]);
+            marker_s[p] = mv;
+            if (blockIdx.x == 0) I.marker[p] = mv;
+          } else {
+            marker_s[p] = lds(&I.marker[p]);
+          }
+        }
         if (vol) vol_s[p] = lds(&I.send[p]) + (rv ? lds(&I.recv[p]) : 0);
       }
       __syncthreads();
@@ -794,38 +862,46 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
         }
       }
       __syncthreads();
-      const RoundCtx R{sizes_s, penf_s, marker_s, vol_s, mark_s, s_minpart, s_minsize, s_second, s_maxv, s_cc};
+      const RoundCtx R{sizes_s, penf_s, marker_s, vol_s, mark_s, s_minpart, s_minsize, s_second, s_maxv, s_cc, Cf};
       if (blockIdx.x == 0 && threadIdx.x == 0) B.stats[20] += gtimer() - tA;
       pass_start = false;
       prev_maxtouch = false;
       while (hidx < B.nheavy && __ldg(&B.heavy_pos[hidx]) < pos) hidx++;
-      const int next_heavy = hidx < B.nheavy ? __ldg(&B.heavy_pos[hidx]) : I.nov;
 
       // ================================================================= round
-      // A window holds at most one whole-grid vertex (at zs) and ends before
-      // the next one.
+      // A window holds up to gmax whole-grid vertices and ends before the next
+      // one.
       int end_w = min(pos + W, I.nov);
-      const bool sup = next_heavy < end_w;
-      const int zs = sup ? next_heavy : -1;
-      if (sup && hidx + 1 < B.nheavy) end_w = min(end_w, (int)__ldg(&B.heavy_pos[hidx + 1]));
+      if (hidx + B.gmax < B.nheavy) end_w = min(end_w, (int)__ldg(&B.heavy_pos[hidx + B.gmax]));
+      int ns = 0;
+      while (ns < B.gmax && hidx + ns < B.nheavy && __ldg(&B.heavy_pos[hidx + ns]) < end_w) ns++;
       const int span = end_w - pos;
       const int q = (span + nwarps - 1) / nwarps;
       const int z0 = min(pos + gw * q, end_w);
       const int z1 = min(z0 + q, end_w);
       const int gtid = blockIdx.x * blockDim.x + threadIdx.x, gthreads = gridDim.x * blockDim.x;
-      const int hp = heavy_round & 1;   // double-buffered whole-grid tallies
-      int* hcnt = B.hcnt + hp * K;
-      unsigned long long* hfirst = B.hfirst + hp * K;
-      int* hgain = B.hgain + hp * K;
-      int* hloss = B.hloss + hp * K;
-      int* hadelta = B.hadelta + hp * K;
-      int* hmisc = B.hmisc + hp * 8;
-      const int vsup = sup ? __ldg(&I.order[zs]) : 0;
-      const int own_s = sup ? lds(&I.part_vec[vsup]) : 0;
-      const uint32_t base_s = sup ? __ldg(&I.vptr[vsup]) : 0;
-      const int deg_s = sup ? (int)(__ldg(&I.vptr[vsup + 1]) - base_s) : 0;
-      // ---- A1: tally slices of the whole-grid vertex, pre-reduced per CTA
-      if (sup) {
+      const int hp = heavy_round & 1;   // whole-grid tallies, double-buffered by parity
+      // slot j of this parity: K entries at hslot(j), 8 words of hmisc at hmslot(j)
+      auto hslot = [&](int j) { return ((size_t)hp * kMaxGridVerts + j) * K; };
+      auto hmslot = [&](int j) { return (hp * kMaxGridVerts + j) * 8; };
+      const unsigned long long tR = gtimer();
+      if ((int)threadIdx.x < ns) {
+        const int z = __ldg(&B.heavy_pos[hidx + threadIdx.x]);
+        const int v = __ldg(&I.order[z]);
+        const uint32_t b = __ldg(&I.vptr[v]);
+        s_gz[threadIdx.x] = z;
+        s_gv[threadIdx.x] = v;
+        s_go[threadIdx.x] = lds(&I.part_vec[v]);
+        s_gb[threadIdx.x] = b;
+        s_gd[threadIdx.x] = (int)(__ldg(&I.vptr[v + 1]) - b);
+      }
+      __syncthreads();
+      // ---- A1: tally slices of the whole-grid vertices, pre-reduced per CTA
+      for (int j = 0; j < ns; j++) {
+        const int own_s = s_go[j], deg_s = s_gd[j];
+        const uint32_t base_s = s_gb[j];
+        int* hcnt = B.hcnt + hslot(j);
+        unsigned long long* hfirst = B.hfirst + hslot(j);
         for (int p = lane; p < K; p += 32) { cnt[p] = 0; first[p] = ~0ull; }
         __syncwarp();
         int c1 = 0;
@@ -849,9 +925,10 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
             atomicMin(&hfirst[p], f);
           }
         }
-        if (lane == 0 && c1) atomicAdd(&hmisc[0], c1);
-        __syncthreads();   // the per-warp arrays serve the evaluations below
+        if (lane == 0 && c1) atomicAdd(&B.hmisc[hmslot(j)], c1);
+        __syncthreads();   // the per-warp arrays serve the next vertex and the evaluations below
       }
+      if (ns && threadIdx.x == 0) atomicMax(&B.stats[38], gtimer() - tR);
       // ---- A: evaluate
       int wsum = 0, vsum = 0;
       const long long cA = clock64();
@@ -871,33 +948,14 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
         for (int nb = 0; nb < deg; nb += 32) c1 += tally_batch(I, own, base, nb, deg, cnt, first);
         __syncwarp();
         c1 = warp_sum(c1);
+        const long long cT = clock64();
         bool special;
         int slack;
-        const int d = ldg_decide(I, R, cnt, first, metric, v, own, z == pos, &special, &slack);
-        {
-          // Candidates (part, count, first sighting) for an exact re-check of the
-          // decision if the part sizes drift beyond its slack.
-          unsigned long long* cl = B.cand + (size_t)o * K;
-          int nc = 0;
-          for (int p0 = 0; p0 < K; p0 += 32) {
-            const int p = p0 + lane;
-            bool ok = false;
-            unsigned long long ent = 0;
-            if (p < K) {
-              const int c = cnt[p];
-              if (c > 0 && !(metric == kTV && R.marker[p] == v)) {
-                ok = true;
-                const unsigned long long f = first[p];
-                ent = ((unsigned long long)p << 52) | ((unsigned long long)(c - (p == own ? 1 : 0)) << 36) |
-                      (((f >> 32) & 0xffffull) << 20) | (f & 0xfffffull);
-              }
-            }
-            const unsigned m = __ballot_sync(kAll, ok);
-            if (ok) cl[nc + __popc(m & ((1u << lane) - 1u))] = ent;
-            nc += __popc(m);
-          }
-          if (lane == 0) B.ncand[o] = nc;
-        }
+        // candidates (part, count, first sighting) for an exact re-check of the
+        // decision if the part sizes drift beyond its slack; TV's scanned parts
+        const int d = ldg_decide(I, R, cnt, first, metric, v, own, z == pos, gains, B.cand + (size_t)o * K,
+                                 &B.ncand[o], metric == kTV ? B.scan + (size_t)o * words : nullptr, &special, &slack);
+        const long long cD = clock64();
         // An isolated vertex (no nets, weight 0) changes nothing a later position
         // reads; if its decision flips under the window's size drift, validation
         // corrects it in place instead of cutting.  Its accept outcome does not
@@ -932,13 +990,6 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
             B.mlist[atomicAdd(&B.mcnt[par], 1)] = o;
           }
         }
-        if (metric == kTV) {
-          for (int wd = 0; wd < words; wd++) {
-            const int p = wd * 32 + lane;
-            const unsigned m = __ballot_sync(kAll, p < K && cnt[p] > 0);
-            if (lane == 0) B.scan[(size_t)o * words + wd] = m;
-          }
-        }
         const int wv = mover ? __ldg(&I.w[v]) : 0;
         if (lane == 0) {
           B.dec[o] = (own << 16) | d;   // own read now: part_vec changes in the commit phase
@@ -950,6 +1001,11 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
         }
         wsum += wv;
         vsum += mover ? vdd : 0;
+        if (lane == 0) {
+          atomicAdd(&B.stats[41], (unsigned long long)(cT - cz));
+          atomicAdd(&B.stats[42], (unsigned long long)(cD - cT));
+          atomicAdd(&B.stats[43], (unsigned long long)(clock64() - cD));
+        }
         cV += clock64() - cz;
         nV++;
         __syncwarp();
@@ -976,63 +1032,47 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
       if (threadIdx.x == 0) {
         const long long dm = clock64() - cM;
         if (dm > 2000) atomicMax(&B.stats[24], (unsigned long long)dm);
+        atomicMax(&B.stats[36], gtimer() - tR);
       }
-      if (sup) {
+      if (ns) {
         if (!grid_barrier(B.bar, I.status)) return;
-        // ---- A2: the whole-grid vertex's decision, taken by every CTA from the
-        // global tally (first of the window or not, like any position), and its
-        // locate / gain-loss slices
-        const int os = zs - pos;
-        for (int p = threadIdx.x; p < K; p += blockDim.x) {
-          cnt_b[p] = lds(&hcnt[p]);
-          first_b[p] = lds(&hfirst[p]);
-        }
-        __syncthreads();
-        if (wib == 0) {
-          bool special;
-          int slack;
-          const int d = ldg_decide(I, R, cnt_b, first_b, metric, vsup, own_s, zs == pos, &special, &slack);
-          if (lane == 0) { s_d = d; s_spec = special ? 1 : 0; s_slk = slack; }
-          if (blockIdx.x == 0) {
-            // candidates for an exact re-check, TV's scanned parts for the markers
-            unsigned long long* cl = B.cand + (size_t)os * K;
-            int nc = 0;
-            for (int p0 = 0; p0 < K; p0 += 32) {
-              const int p = p0 + lane;
-              bool ok = false;
-              unsigned long long ent = 0;
-              if (p < K) {
-                const int c = cnt_b[p];
-                if (c > 0 && !(metric == kTV && R.marker[p] == vsup)) {
-                  ok = true;
-                  const unsigned long long f = first_b[p];
-                  ent = ((unsigned long long)p << 52) | ((unsigned long long)(c - (p == own_s ? 1 : 0)) << 36) |
-                        (((f >> 32) & 0xffffull) << 20) | (f & 0xfffffull);
-                }
-              }
-              const unsigned m = __ballot_sync(kAll, ok);
-              if (ok) cl[nc + __popc(m & ((1u << lane) - 1u))] = ent;
-              nc += __popc(m);
-            }
-            if (lane == 0) B.ncand[os] = nc;
-            if (metric == kTV) {
-              for (int wd = 0; wd < words; wd++) {
-                const int p = wd * 32 + lane;
-                const unsigned m = __ballot_sync(kAll, p < K && cnt_b[p] > 0);
-                if (lane == 0) B.scan[(size_t)os * words + wd] = m;
-              }
-            }
+        const unsigned long long tG = gtimer();
+        // ---- A2: decisions of the whole-grid vertices, taken in every CTA from
+        // the global tallies (warp j decides vertex j; each is first of the
+        // window or not, like any position), then their locate / gain-loss slices
+        for (int j = 0; j < ns; j++) {
+          const size_t hs = hslot(j);
+          for (int p = threadIdx.x; p < K; p += blockDim.x) {
+            cnt_b[(size_t)j * K + p] = lds(&B.hcnt[hs + p]);
+            first_b[(size_t)j * K + p] = lds(&B.hfirst[hs + p]);
           }
         }
         __syncthreads();
-        const int d = s_d;
-        const bool need = d != own_s && (metric == kTV ? lds(&hmisc[0]) >= deg_s - cnt_b[d] : true);
-        if (d != own_s) {   // records for every decision that moves (the validation reads own's slots)
+        if (wib < ns) {
+          const int j = wib;
+          const int zs = s_gz[j], vsup = s_gv[j], own_s = s_go[j];
+          const int* cj = cnt_b + (size_t)j * K;
+          const unsigned long long* fj = first_b + (size_t)j * K;
+          bool special;
+          int slack;
+          // block 0 keeps the candidates for an exact re-check, TV's scanned parts
+          const int os = zs - pos;
+          const bool b0 = blockIdx.x == 0;
+          const int d = ldg_decide(I, R, cj, fj, metric, vsup, own_s, zs == pos, gains_b + (size_t)j * K,
+                                   b0 ? B.cand + (size_t)os * K : nullptr, b0 ? &B.ncand[os] : nullptr,
+                                   b0 && metric == kTV ? B.scan + (size_t)os * words : nullptr, &special, &slack);
+          if (lane == 0) { s_gdec[j] = d; s_gspec[j] = special ? 1 : 0; s_gslk[j] = slack; }
+        }
+        __syncthreads();
+        for (int j = 0; j < ns; j++) {
+          const int d = s_gdec[j], own_s = s_go[j];
+          if (d == own_s) continue;   // records for every decision that moves (the validation reads own's slots)
+          const size_t hs = hslot(j);
           if (vol) {
             for (int p = lane; p < K; p += 32) { gains[p] = 0; losses[p] = 0; adelta[p] = 0; }
             __syncwarp();
           }
-          locate_all(I, B, metric, vsup, own_s, d, base_s, deg_s, gw, nwarps, loc, gains, losses, adelta);
+          locate_all(I, B, metric, s_gv[j], own_s, d, s_gb[j], s_gd[j], gw, nwarps, loc, gains, losses, adelta);
           if (vol) {
             __syncthreads();
             for (int p = threadIdx.x; p < K; p += blockDim.x) {
@@ -1042,56 +1082,66 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
                 l += losses_b[(size_t)x * K + p];
                 a += adelta_b[(size_t)x * K + p];
               }
-              if (g) atomicAdd(&hgain[p], g);
-              if (l) atomicAdd(&hloss[p], l);
-              if (a) atomicAdd(&hadelta[p], a);
+              if (g) atomicAdd(&B.hgain[hs + p], g);
+              if (l) atomicAdd(&B.hloss[hs + p], l);
+              if (a) atomicAdd(&B.hadelta[hs + p], a);
             }
+            __syncthreads();   // the per-warp arrays serve the next vertex
           }
         }
         if (!grid_barrier(B.bar, I.status)) return;
-        // ---- A3: accept test (MSV / MSRV) in every CTA, claims, the record
-        bool mover = metric == kTV && need, mt = false;
-        int vs = kBig, vdd = 0;
-        if (vol && need) {
-          for (int p = threadIdx.x; p < K; p += blockDim.x) {
-            gains_b[p] = lds(&hgain[p]);
-            losses_b[p] = lds(&hloss[p]);
-            adelta_b[p] = lds(&hadelta[p]);
+        // ---- A3: accept tests (MSV / MSRV) in every CTA, claims, the records
+        for (int j = 0; j < ns; j++) {
+          const size_t hs = hslot(j);
+          const int zs = s_gz[j], vsup = s_gv[j], own_s = s_go[j], deg_s = s_gd[j], d = s_gdec[j];
+          const uint32_t base_s = s_gb[j];
+          const int os = zs - pos;
+          const bool need = d != own_s &&
+                            (metric == kTV ? lds(&B.hmisc[hmslot(j)]) >= deg_s - cnt_b[(size_t)j * K + d] : true);
+          bool mover = metric == kTV && need, mt = false;
+          int vs = kBig, vdd = 0;
+          if (vol && need) {
+            for (int p = threadIdx.x; p < K; p += blockDim.x) {
+              gains_b[p] = lds(&B.hgain[hs + p]);
+              losses_b[p] = lds(&B.hloss[hs + p]);
+              adelta_b[p] = lds(&B.hadelta[hs + p]);
+            }
+            __syncthreads();
+            const AcceptPart a = accept_partial(R, gains_b, losses_b, adelta_b, K, rv, threadIdx.x, blockDim.x);
+            const bool fM = __syncthreads_or(a.failM);
+            const bool fN = __syncthreads_or(a.failN);
+            const bool amt = __syncthreads_or(a.mt);
+            const int fsl = block_reduce_max(a.fsl, iscr);
+            const int msl = block_reduce_min(a.msl, iscr);
+            vdd = block_reduce_max(a.vd, iscr);
+            bool good;
+            accept_final(fM, fN, fsl, msl, &good, &vs);
+            mover = good;
+            mt = mover && amt;
+          }
+          if (mover) claim_nets(I, B, vol, zs, own_s, d, base_s, deg_s, gtid, gthreads, par);
+          const int wv = mover ? __ldg(&I.w[vsup]) : 0;
+          if (blockIdx.x == 0 && threadIdx.x == 0) {
+            B.dec[os] = (own_s << 16) | d;
+            B.flag[os] = (unsigned char)((mover ? 1 : 0) | (s_gspec[j] ? 2 : 0) | 4);
+            B.slack[os] = s_gslk[j];
+            B.vslack[os] = vs;
+            B.wt[os] = wv;
+            B.vd[os] = mover ? vdd : 0;
+            if (mover) {
+              if (mt) atomicMin(&B.ctl[2 + par], zs);
+              B.mlist[atomicAdd(&B.mcnt[par], 1)] = os;
+            }
+          }
+          // the warp owning position zs carries its weight and volume change
+          const int owner = os / q;
+          if (threadIdx.x == 0 && owner / kSWarps == (int)blockIdx.x) {
+            s_mw[owner % kSWarps] += wv;
+            s_mv[owner % kSWarps] += mover ? vdd : 0;
           }
           __syncthreads();
-          const AcceptPart a = accept_partial(R, gains_b, losses_b, adelta_b, K, rv, threadIdx.x, blockDim.x);
-          const bool fM = __syncthreads_or(a.failM);
-          const bool fN = __syncthreads_or(a.failN);
-          const bool amt = __syncthreads_or(a.mt);
-          const int fsl = block_reduce_max(a.fsl, iscr);
-          const int msl = block_reduce_min(a.msl, iscr);
-          vdd = block_reduce_max(a.vd, iscr);
-          bool good;
-          accept_final(fM, fN, fsl, msl, &good, &vs);
-          mover = good;
-          mt = mover && amt;
         }
-        if (mover) claim_nets(I, B, vol, zs, own_s, d, base_s, deg_s, gtid, gthreads, par);
-        const int wv = mover ? __ldg(&I.w[vsup]) : 0;
-        if (blockIdx.x == 0 && threadIdx.x == 0) {
-          B.dec[os] = (own_s << 16) | d;
-          B.flag[os] = (unsigned char)((mover ? 1 : 0) | (s_spec ? 2 : 0) | 4);
-          B.slack[os] = s_slk;
-          B.vslack[os] = vs;
-          B.wt[os] = wv;
-          B.vd[os] = mover ? vdd : 0;
-          if (mover) {
-            if (mt) atomicMin(&B.ctl[2 + par], zs);
-            B.mlist[atomicAdd(&B.mcnt[par], 1)] = os;
-          }
-        }
-        // the warp owning position zs carries its weight and volume change
-        const int owner = os / q;
-        if (threadIdx.x == 0 && owner / kSWarps == (int)blockIdx.x) {
-          s_mw[owner % kSWarps] += wv;
-          s_mv[owner % kSWarps] += mover ? vdd : 0;
-        }
-        __syncthreads();
+        if (blockIdx.x == 0 && threadIdx.x == 0) B.stats[33] += gtimer() - tG;
       }
       if (lane == 0) {
         B.wsum[gw] = wsum + s_mw[wib];
@@ -1109,6 +1159,7 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
       }
       // ---- B: validate.  Prefix sums of moved weight and volume drift over the
       // warps before this one (warps own consecutive position ranges).
+      const unsigned long long tV = gtimer();
       {
         long long pw = 0, pv = 0;
         const int lim = blockIdx.x * kSWarps;
@@ -1212,17 +1263,20 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
         if (z >= cz1) break;
         cta_validate_ldg(I, B, R, metric, z, pos, q, par, mtpos, s_pre_w, s_pre_v, cnt_b, dsz_cta, cta_o0, true);
       }
-      if (sup) {
-        // the whole-grid vertex: its nets checked by every thread, the rest by the
+      for (int j = 0; j < ns; j++) {
+        // a whole-grid vertex: its nets checked by every thread, the rest by the
         // CTA owning its position
+        const int zs = s_gz[j], own_s = s_go[j];
         const int os = zs - pos;
         const int fl = lds(&B.flag[os]);
-        const int c = conflicts(I, B, vol, zs, own_s, (lds(&B.dec[os]) & 0xffff) != own_s, fl & 1, base_s, deg_s,
+        const int c = conflicts(I, B, vol, zs, own_s, (lds(&B.dec[os]) & 0xffff) != own_s, fl & 1, s_gb[j], s_gd[j],
                                 gtid, gthreads, lds(&B.ctab_over[par]) != 0);
         if (c) atomicMin(&B.ctl[par], (zs << 3) | c);
         if (zs >= cz0 && zs < cz1)
           cta_validate_ldg(I, B, R, metric, zs, pos, q, par, mtpos, s_pre_w, s_pre_v, cnt_b, dsz_cta, cta_o0, false);
       }
+      __syncthreads();
+      if (threadIdx.x == 0) atomicMax(&B.stats[39], gtimer() - tV);
       if (!grid_barrier(B.bar, I.status)) return;
       // ---- C: commit every mover before the cut.
       const int cutw = lds(&B.ctl[par]);
@@ -1233,6 +1287,13 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
         const int why = cutw == kNone ? 0 : (cutw & 7);
         B.stats[why <= 5 ? 3 + why : 21 + why]++;   // 6, 7: slots 27, 28
         B.stats[9] += cut - pos;
+        // per-window maxima over CTAs (no CTA writes these again before the next phase A)
+        B.stats[32] += B.stats[36];
+        B.stats[34] += B.stats[38];
+        B.stats[35] += B.stats[39];
+        B.stats[36] = 0;
+        B.stats[38] = 0;
+        B.stats[39] = 0;
         B.stats[17] += tB - tA;
         tA = tB;
       }
@@ -1289,9 +1350,10 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
         }
         unclaim_nets(I, B, vol, base, deg, threadIdx.x, blockDim.x);
       }
-      if (sup) {
-        // the whole-grid vertex, by every thread; then its tallies' other buffer
-        // is cleared for the next one
+      for (int j = 0; j < ns; j++) {
+        // a whole-grid vertex, by every thread
+        const int zs = s_gz[j], vsup = s_gv[j], own_s = s_go[j], deg_s = s_gd[j];
+        const uint32_t base_s = s_gb[j];
         const int os = zs - pos;
         if (lds(&B.flag[os]) & 1) {
           const int pk = lds(&B.dec[os]);
@@ -1311,29 +1373,37 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
           }
           unclaim_nets(I, B, vol, base_s, deg_s, gtid, gthreads);
         }
-        const int op = hp ^ 1;
-        for (int p = gtid; p < K; p += gthreads) {
-          B.hcnt[op * K + p] = 0;
-          B.hfirst[op * K + p] = ~0ull;
-          B.hgain[op * K + p] = 0;
-          B.hloss[op * K + p] = 0;
-          B.hadelta[op * K + p] = 0;
+      }
+      if (ns) {
+        // the other parity's tallies are cleared for the next window with
+        // whole-grid vertices
+        const size_t ob = (size_t)(hp ^ 1) * kMaxGridVerts * K;
+        for (int p = gtid; p < kMaxGridVerts * K; p += gthreads) {
+          B.hcnt[ob + p] = 0;
+          B.hfirst[ob + p] = ~0ull;
+          B.hgain[ob + p] = 0;
+          B.hloss[ob + p] = 0;
+          B.hadelta[ob + p] = 0;
         }
-        if (gtid < 8) B.hmisc[op * 8 + gtid] = 0;
-        if (gtid == 0) B.stats[1]++;
+        if (gtid < 8 * kMaxGridVerts) B.hmisc[(hp ^ 1) * 8 * kMaxGridVerts + gtid] = 0;
+        if (gtid == 0) B.stats[1] += ns;
         heavy_round++;
       }
       if (metric == kTV) {
-        // marker = last scanner of each part among the walked positions
-        const int len = cut - pos;
-        for (int p = gw; p < K; p += nwarps) {
-          for (int o0 = len - 1; o0 >= 0; o0 -= 32) {
-            const int o = o0 - lane;
-            const bool b = o >= 0 && ((lds(&B.scan[(size_t)o * words + (p >> 5)]) >> (p & 31)) & 1u);
-            const unsigned m = __ballot_sync(kAll, b);
-            if (m) {
-              if (lane == 0) I.marker[p] = __ldg(&I.order[pos + o0 - (__ffs(m) - 1)]);
-              break;
+        // marker = last scanner of each part among the committed positions: each
+        // warp offers the last of its own positions per part, stamped with the
+        // window (round + 1), and the next round state reads the maximum
+        const int zc = min(z1, cut);
+        const unsigned long long stamp = (unsigned long long)(round + 1) << 32;
+        for (int wd = lane; wd < words; wd += 32) {
+          uint32_t seen = 0;
+          for (int z = zc - 1; z >= z0 && seen != ~0u; z--) {
+            uint32_t m = lds(&B.scan[(size_t)(z - pos) * words + wd]) & ~seen;
+            seen |= m;
+            while (m) {
+              const int b = __ffs(m) - 1;
+              m &= m - 1;
+              atomicMax(&B.mlast[wd * 32 + b], stamp | (unsigned)z);
             }
           }
         }
@@ -1360,6 +1430,13 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
         B.stats[18] += tC - tA;
         tA = tC;
       }
+    }
+  }
+  if (metric == kTV && blockIdx.x == 0) {
+    // markers of the last window (the loop's final barrier made them visible)
+    for (int p = threadIdx.x; p < K; p += blockDim.x) {
+      const unsigned long long ml = lds(&B.mlast[p]);
+      if (round > 0 && (int)(ml >> 32) == round) I.marker[p] = __ldg(&I.order[(int)(ml & 0xffffffffu)]);
     }
   }
 }

@@ -169,7 +169,7 @@ int fp_metrics_noalloc(int32_t K, int32_t nov, int32_t noe, int64_t pins, const 
                        const int32_t* src, const int32_t* part_vec, const int32_t* ep_len,
                        const int32_t* ep_part, int64_t* out, void* stream);
 
-/* Statistics of the last fp_refine on the grid-wide engine (up to 32 values):
+/* Statistics of the last fp_refine on the grid-wide engine (up to 48 values):
  * [0] windows, [1] single-vertex rounds of high-degree vertices, [2] moves
  * committed from windows, [3..8] windows ended by: nothing (fully valid), a
  * possibly stale TV marker, part-size drift, volume drift, a max-volume part
@@ -181,6 +181,11 @@ int fp_metrics_noalloc(int32_t K, int32_t nov, int32_t noe, int64_t pins, const 
  * mover changing the count of the position's own part on a shared net / by a
  * part-set change after earlier count changes ([8] then counts part-set
  * changes only), [29..31] SM cycles of CTA evaluations in tally, decision and
+ * the rest; nanoseconds summed over windows of: [32] the slowest CTA's
+ * evaluation of its own positions (light and medium), [33] the whole-grid
+ * vertices' decision and accept phases, [34] the slowest CTA's tally of
+ * whole-grid vertex slices, [35] the slowest CTA's validation; [40] CTA
+ * evaluations; [41..43] SM cycles of warp evaluations in tally, decision and
  * the rest. */
 int fp_get_stats(fp_instance* inst, int64_t* out, int32_t n);
 /* Number of kernel launches the last fp_refine / fp_metrics call enqueued. */
