@@ -1,7 +1,7 @@
 #!/usr/bin/env python
 """Benchmark of the GB300 refinement engine: pins/s per refinement pass.
 
-Workload (default "c2"): all six metrics (CN, TV, TM, MSM, MSV, MSRV), each on
+Workload (default "zipf4m"): all six metrics (CN, TV, TM, MSM, MSV, MSRV), each on
 its own resident instance: K = 256, eps = 0.05 (C = (W/K) * 1.05),
 4,194,304 vertices and 4,194,304 nets, net sizes Zipf(2.1) clipped to
 [2, 10000], pins drawn by a Zipf(1.5) vertex popularity, source = first drawn
@@ -42,9 +42,9 @@ sys.path.insert(0, str(ROOT))
 
 METRICS = ["CN", "TV", "TM", "MSM", "MSV", "MSRV"]
 WORKLOADS = {
-    "c2": dict(nov=4_194_304, noe=4_194_304, alpha=2.1, lo=2, hi=10000, beta=1.5, weight_rule=1, K=256,
+    "zipf4m": dict(nov=4_194_304, noe=4_194_304, alpha=2.1, lo=2, hi=10000, beta=1.5, weight_rule=1, K=256,
                eps=1.05, passes=10, seed=0),
-    "c1": dict(nov=16_384, noe=16_384, alpha=0.0, lo=2, hi=16, beta=0.0, weight_rule=0, K=8, eps=1.03,
+    "uniform16k": dict(nov=16_384, noe=16_384, alpha=0.0, lo=2, hi=16, beta=0.0, weight_rule=0, K=8, eps=1.03,
                passes=5, seed=0),
 }
 
@@ -419,7 +419,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="c2", choices=sorted(WORKLOADS))
+    ap.add_argument("--config", default="zipf4m", choices=sorted(WORKLOADS))
     ap.add_argument("--scale", type=int, default=1, help="divide vertex/net counts (quick runs)")
     ap.add_argument("--passes", type=int, default=0)
     ap.add_argument("--metrics", default="")
