@@ -465,7 +465,8 @@ class Instance:
                  cut_setafter=int(x[28]), cta_tally_cycles=int(x[29]), cta_decide_cycles=int(x[30]),
                  cta_rest_cycles=int(x[31]), local_eval_ms=x[32] / 1e6, grid_vertex_ms=x[33] / 1e6,
                  grid_tally_ms=x[34] / 1e6, local_validate_ms=x[35] / 1e6, cta_evals=int(x[40]),
-                 light_tally_cycles=int(x[41]), light_decide_cycles=int(x[42]), light_rest_cycles=int(x[43]))
+                 light_tally_cycles=int(x[41]), light_decide_cycles=int(x[42]), light_rest_cycles=int(x[43]),
+                 window_fixes=int(x[44]))
         return d
 
     def last_launches(self) -> int:

@@ -397,6 +397,7 @@ int fp_instance_create(fp_ctx* ctx, const fp_hypergraph* h, int32_t K, int32_t m
   const bool msg = metric == FP_METRIC_TM || metric == FP_METRIC_MSM;
   const bool cn = metric == FP_METRIC_CN;
   const bool ldg = !msg && !cn;
+  const bool vfix = metric == FP_METRIC_MSV || metric == FP_METRIC_MSRV;   // in-window decision fixes
   // exact count claims of the LDG engine: a table well above the entries of a
   // round (two per count-only net of a window's movers)
   size_t ctab = 4096;
@@ -419,7 +420,8 @@ int fp_instance_create(fp_ctx* ctx, const fp_hypergraph* h, int32_t K, int32_t m
       (rc = dalloc(in, &in->sb.rec, ldg ? g.pins : 1)) || (rc = dalloc(in, &in->sb.rec_slot, ldg ? g.pins : 1)) ||
       (rc = dalloc(in, &in->sb.ctab_key, ldg ? ctab : 1)) || (rc = dalloc(in, &in->sb.ctab_pos, ldg ? ctab : 1)) ||
       (rc = dalloc(in, &in->sb.ctab_cnt, ldg ? ctab : 1)) ||
-      (rc = dalloc(in, &in->sb.ctab_over, 2)) ||
+      (rc = dalloc(in, &in->sb.ctab_over, 2)) || (rc = dalloc(in, &in->sb.dfix, kSpecWindow)) ||
+      (rc = dalloc(in, &in->sb.rec_slot2, vfix ? g.pins : 1)) ||
       (rc = dalloc(in, &in->sb.cn_moved, cn ? g.pins : 1)) || (rc = dalloc(in, &in->sb.cn_kcnt, cn ? g.noe : 1)) ||
       (rc = dalloc(in, &in->sb.cn_nets, cn ? g.noe : 1)) || (rc = dalloc(in, &in->sb.cn_cnt, 4)) || (rc = dalloc(in, &in->vclass_d, g.nov)) ||
       (rc = dalloc(in, &in->sb.cand, (size_t)kSpecWindow * K)) || (rc = dalloc(in, &in->sb.ncand, kSpecWindow)) ||
@@ -446,6 +448,10 @@ int fp_instance_create(fp_ctx* ctx, const fp_hypergraph* h, int32_t K, int32_t m
   in->sb.ctab_mask = ldg ? (unsigned)(ctab - 1) : 0u;
   in->sb.wmax_msg = kMsgWindow;
   in->sb.gmax = default_grid_verts(metric);
+  // window regrowth after a cut: twice the last valid length for MSV (cuts
+  // every few hundred positions), four times for the metrics with rarer cuts
+  in->sb.wgrow = metric == FP_METRIC_MSV ? 2 : 4;
+  in->sb.maxfix = 32;
   in->sb.max_warps = kMaxSpecWarps;
   in->sb.heavy_pos = in->heavy_pos_d;
   in->sb.mid_pos = in->mid_pos_d;

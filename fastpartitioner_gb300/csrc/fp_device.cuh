@@ -56,10 +56,13 @@ constexpr int kMaxGridVerts = 8;
 // instance.
 struct SpecBuf {
   unsigned* bar;         // [4] grid barrier: arrivals, generation, abort
-  int* ctl;              // [8] per-round words, double-buffered by round parity:
-                         //     [0,1] cut, [2,3] first max-touching mover
+  int* ctl;              // [8] per-round words: [2,3] first max-touching mover (by round
+                         //     parity), [4,5] cut (by validation pass parity)
   int* dec;              // [wmax] (own part << 16) | decision per window offset
-  unsigned char* flag;   // [wmax] bit0 mover, bit1 stale-marker risk
+  unsigned char* flag;   // [wmax] bit0 mover, bit1 stale-marker risk, bit2 CTA / grid evaluated,
+                         //     bit3 isolated, bit4 accepted, bit5 decision fixed exact in the
+                         //     window, bit6 claims of a replaced move held (rec_slot2)
+  int* dfix;             // [wmax] exact decision of a position whose size check failed
   int* slack;            // [wmax] part-size drift the decision tolerates (-1: none)
   int* vslack;           // [wmax] volume drift the accept/reject outcome tolerates
   int* wt;               // [wmax] weight moved by a mover (0 otherwise)
@@ -87,6 +90,7 @@ struct SpecBuf {
   int* ctab_pos;         // [ctab_mask + 1] first position of a count-only mover with that (net, part)
   int* ctab_cnt;         // [ctab_mask + 1] count-only movers of the round on that (net, part)
   uint2* rec_slot;       // [pins] table slots of a count-only move's (net, own) and (net, new part)
+  uint2* rec_slot2;      // [pins] (MSV / MSRV) those of a move replaced by an in-window fix
   int* ctab_over;        // [2] a probe ran past its bound this round (by round parity)
   unsigned ctab_mask;
   const int* heavy_pos;  // positions (visiting order, ascending) of vertices that get a
@@ -101,6 +105,8 @@ struct SpecBuf {
   int* hmisc;            // [2 * kMaxGridVerts * 8]
   unsigned long long* mlast;  // [K] TV: (window stamp << 32) | last position whose scan holds the part
   int gmax;              // whole-grid vertices one LDG window may hold (1 .. kMaxGridVerts)
+  int wgrow;             // LDG window after a cut: this many times the last valid length
+  int maxfix;            // in-window decision fixes per window (MSV / MSRV)
   unsigned long long* stats;  // [kNumStats] round statistics (see fp_get_stats)
   int wmax;              // longest window of the LDG and CN engines
   int wmax_msg;          // longest window of the TM / MSM engine (dec only)

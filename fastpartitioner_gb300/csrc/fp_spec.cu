@@ -40,7 +40,7 @@ namespace {
 
 using namespace spec;
 
-constexpr int kTV = 1, kMSRV = 5;
+constexpr int kTV = 1, kMSV = 4, kMSRV = 5;
 constexpr int kBig = 1000000000;
 
 struct RoundCtx {
@@ -439,19 +439,23 @@ __device__ __forceinline__ void claim_nets(const DevInstance& I, const SpecBuf& 
   }
 }
 
-// Clears the claims of a mover on its nets k0, k0 + kstep, ... (commit phase).
+__device__ __forceinline__ void ctab_clear(const SpecBuf& B, uint2 sl) {
+  if (sl.x != ~0u) { B.ctab_key[sl.x] = ~0ull; B.ctab_pos[sl.x] = kNone; B.ctab_cnt[sl.x] = 0; }
+  if (sl.y != ~0u) { B.ctab_key[sl.y] = ~0ull; B.ctab_pos[sl.y] = kNone; B.ctab_cnt[sl.y] = 0; }
+}
+
+// Clears the claims of a vertex on its nets k0, k0 + kstep, ... (commit phase):
+// cur, those of its current move (its records and rec_slot); old, those of a
+// move an in-window fix replaced (rec_slot2).
 __device__ __forceinline__ void unclaim_nets(const DevInstance& I, const SpecBuf& B, bool vol, uint32_t base, int deg,
-                                             int k0, int kstep) {
+                                             int k0, int kstep, bool cur = true, bool old = false) {
   for (int k = k0; k < deg; k += kstep) {
     const int e = (int)__ldg(&I.vnets[base + k]);
     B.claim_m[e] = kNone;
     B.claim_c[e] = kNone;
     B.mask_c[e] = 0;
-    if (!rec_setchange(lds(&B.rec[base + k]), vol)) {
-      const uint2 sl = lds(&B.rec_slot[base + k]);
-      if (sl.x != ~0u) { B.ctab_key[sl.x] = ~0ull; B.ctab_pos[sl.x] = kNone; B.ctab_cnt[sl.x] = 0; }
-      if (sl.y != ~0u) { B.ctab_key[sl.y] = ~0ull; B.ctab_pos[sl.y] = kNone; B.ctab_cnt[sl.y] = 0; }
-    }
+    if (cur && !rec_setchange(lds(&B.rec[base + k]), vol)) ctab_clear(B, lds(&B.rec_slot[base + k]));
+    if (old) ctab_clear(B, lds(&B.rec_slot2[base + k]));
   }
 }
 
@@ -681,7 +685,7 @@ __device__ void cta_eval_ldg(const DevInstance& I, const SpecBuf& B, const Round
 // Validation of a medium vertex by the whole CTA (the warp validation's rules).
 __device__ void cta_validate_ldg(const DevInstance& I, const SpecBuf& B, const RoundCtx& R, int metric, int z, int pos,
                                  int q, int par, int mtpos, long long pre_w, long long pre_v, int* dsz,
-                                 const int* dsz_cta, int o_from, bool check_nets) {
+                                 const int* dsz_cta, int o_from, bool check_nets, int* cut) {
   __shared__ long long shd[2];
   __shared__ int shw;
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -727,8 +731,69 @@ __device__ void cta_validate_ldg(const DevInstance& I, const SpecBuf& B, const R
     const int c5 = __syncthreads_or(conf == 5), c6 = __syncthreads_or(conf == 6), c7 = __syncthreads_or(conf == 7);
     why = c5 ? 5 : c6 ? 6 : c7 ? 7 : 0;
   }
-  if (why && threadIdx.x == 0) atomicMin(&B.ctl[par], (z << 3) | why);
+  if (why && threadIdx.x == 0) atomicMin(cut, (z << 3) | why);
   __syncthreads();
+}
+
+// In-window fix of the light vertex at position z (window offset o) whose size
+// check failed: its decision becomes the exact one (dfix, taken with the sizes
+// the committed prefix leaves), and the move records, the accept test and the
+// claims are redone for it.  The replaced move's claims stay (a superset keeps
+// every later check conservative); their table slots go to rec_slot2 for the
+// commit.  One warp, the warp gw owning position z.
+__device__ void fix_position(const DevInstance& I, const SpecBuf& B, const RoundCtx& R, int metric, int z, int o,
+                             int par, int gw, int* loc, int* gains, int* losses, int* adelta) {
+  const int lane = threadIdx.x & 31;
+  const bool vol = metric != kTV, rv = metric == kMSRV;
+  const int K = I.K;
+  const int v = __ldg(&I.order[z]);
+  const uint32_t base = __ldg(&I.vptr[v]);
+  const int deg = (int)(__ldg(&I.vptr[v + 1]) - base);
+  const int fl = lds(&B.flag[o]);
+  const int own = lds(&B.dec[o]) >> 16;
+  const int d = lds(&B.dfix[o]);
+  const bool had = (fl & 1) != 0;
+  if (had) {
+    for (int k = lane; k < deg; k += 32)
+      B.rec_slot2[base + k] =
+          rec_setchange(lds(&B.rec[base + k]), vol) ? make_uint2(~0u, ~0u) : lds(&B.rec_slot[base + k]);
+  }
+  bool mover = false, mt = false, good = false;
+  int vs = kBig, vdd = 0;
+  if (d != own) {
+    for (int p = lane; p < K; p += 32) { gains[p] = 0; losses[p] = 0; adelta[p] = 0; }
+    __syncwarp();
+    locate_all(I, B, metric, v, own, d, base, deg, 0, 1, loc, gains, losses, adelta);
+    __syncwarp();
+    const AcceptPart a = accept_partial(R, gains, losses, adelta, K, rv, lane, 32);
+    const bool fM = __any_sync(kAll, a.failM);
+    const bool fN = __any_sync(kAll, a.failN);
+    accept_final(fM, fN, warp_max(a.fsl), warp_min(a.msl), &good, &vs);
+    mover = good;
+    mt = mover && __any_sync(kAll, a.mt);
+    vdd = warp_max(a.vd);
+  }
+  __syncwarp();
+  if (mover) {
+    claim_nets(I, B, vol, z, own, d, base, deg, lane, 32, par);
+    if (lane == 0) {
+      if (mt) atomicMin(&B.ctl[2 + par], z);
+      if (!had) B.mlist[atomicAdd(&B.mcnt[par], 1)] = o;   // a replaced mover is listed already
+    }
+  }
+  if (lane == 0) {
+    const int wv = mover ? __ldg(&I.w[v]) : 0;
+    const int vn = mover ? vdd : 0;
+    B.wsum[gw] += wv - lds(&B.wt[o]);
+    B.vsum[gw] += vn - lds(&B.vd[o]);
+    B.dec[o] = (own << 16) | d;
+    B.flag[o] = (unsigned char)((fl & 10) | (mover ? 1 : 0) | (good ? 16 : 0) | 32 | (had ? 64 : 0));
+    B.slack[o] = kBig;   // exact: no size check again
+    B.vslack[o] = vs;
+    B.wt[o] = wv;
+    B.vd[o] = vn;
+  }
+  __syncwarp();
 }
 
 static_assert(kMaxGridVerts <= kSWarps, "one warp decides each whole-grid vertex of a window");
@@ -774,8 +839,10 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
   int* loc = loc_b + wib * 96;
   Vol V{I.send, rv ? I.recv : nullptr};
 
+  const bool vfix = metric == kMSV || metric == kMSRV;
   int round = 0;
   int heavy_round = 0;
+  int vr = 0;   // validation passes (parity selects the cut word)
   unsigned long long tA = gtimer();
   for (int it = 0; it < passes; it++) {
     int pos = 0;
@@ -1157,129 +1224,158 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
         B.stats[23] += B.stats[24];
         B.stats[24] = 0;
       }
-      // ---- B: validate.  Prefix sums of moved weight and volume drift over the
-      // warps before this one (warps own consecutive position ranges).
-      const unsigned long long tV = gtimer();
-      {
-        long long pw = 0, pv = 0;
-        const int lim = blockIdx.x * kSWarps;
-        for (int g = threadIdx.x; g < lim; g += blockDim.x) {
-          pw += lds(&B.wsum[g]);
-          pv += lds(&B.vsum[g]);
+      int cutw;
+      for (int zfix = pos, nfix = 0;; nfix++) {
+        int* const cut_w = &B.ctl[4 + (vr & 1)];
+        // ---- B: validate.  Prefix sums of moved weight and volume drift over the
+        // warps before this one (warps own consecutive position ranges).
+        // Positions before zfix are known valid (an earlier pass of the window).
+        const unsigned long long tV = gtimer();
+        {
+          long long pw = 0, pv = 0;
+          const int lim = blockIdx.x * kSWarps;
+          for (int g = threadIdx.x; g < lim; g += blockDim.x) {
+            pw += lds(&B.wsum[g]);
+            pv += lds(&B.vsum[g]);
+          }
+          pw = warp_sum64(pw);
+          pv = warp_sum64(pv);
+          if (lane == 0) uscr[wib] = (unsigned long long)pw;
+          __syncthreads();
+          if (threadIdx.x == 0) {
+            long long a = 0;
+            for (int x = 0; x < kSWarps; x++) a += (long long)uscr[x];
+            s_pre_w = a;
+          }
+          __syncthreads();
+          if (lane == 0) uscr[wib] = (unsigned long long)pv;
+          __syncthreads();
+          if (threadIdx.x == 0) {
+            long long a = 0;
+            for (int x = 0; x < kSWarps; x++) a += (long long)uscr[x];
+            s_pre_v = a;
+          }
+          __syncthreads();
         }
-        pw = warp_sum64(pw);
-        pv = warp_sum64(pv);
-        if (lane == 0) uscr[wib] = (unsigned long long)pw;
+        long long Dw = s_pre_w, Vw = s_pre_v;
+        for (int x = 0; x < wib; x++) {
+          Dw += lds(&B.wsum[blockIdx.x * kSWarps + x]);
+          Vw += lds(&B.vsum[blockIdx.x * kSWarps + x]);
+        }
+        const int mtpos = lds(&B.ctl[2 + par]);
+        const int nm = lds(&B.mcnt[par]);
+        // part-size changes of the window's movers before this CTA's first position
+        // (phase-A scratch gains_b is free now)
+        int* dsz_cta = gains_b;
+        const int cta_o0 = cz0 - pos;
+        for (int p = threadIdx.x; p < K; p += blockDim.x) dsz_cta[p] = 0;
         __syncthreads();
-        if (threadIdx.x == 0) {
-          long long a = 0;
-          for (int x = 0; x < kSWarps; x++) a += (long long)uscr[x];
-          s_pre_w = a;
+        for (int i = threadIdx.x; i < nm; i += blockDim.x) {
+          const int o2 = lds(&B.mlist[i]);
+          if (o2 >= cta_o0) continue;
+          const int w = lds(&B.wt[o2]);
+          if (w == 0) continue;
+          const int pk = lds(&B.dec[o2]);
+          atomicAdd(&dsz_cta[pk & 0xffff], w);
+          atomicAdd(&dsz_cta[pk >> 16], -w);
         }
         __syncthreads();
-        if (lane == 0) uscr[wib] = (unsigned long long)pv;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-          long long a = 0;
-          for (int x = 0; x < kSWarps; x++) a += (long long)uscr[x];
-          s_pre_v = a;
-        }
-        __syncthreads();
-      }
-      long long Dw = s_pre_w, Vw = s_pre_v;
-      for (int x = 0; x < wib; x++) {
-        Dw += lds(&B.wsum[blockIdx.x * kSWarps + x]);
-        Vw += lds(&B.vsum[blockIdx.x * kSWarps + x]);
-      }
-      const int mtpos = lds(&B.ctl[2 + par]);
-      const int nm = lds(&B.mcnt[par]);
-      // part-size changes of the window's movers before this CTA's first position
-      // (phase-A scratch gains_b is free now)
-      int* dsz_cta = gains_b;
-      const int cta_o0 = cz0 - pos;
-      for (int p = threadIdx.x; p < K; p += blockDim.x) dsz_cta[p] = 0;
-      __syncthreads();
-      for (int i = threadIdx.x; i < nm; i += blockDim.x) {
-        const int o2 = lds(&B.mlist[i]);
-        if (o2 >= cta_o0) continue;
-        const int w = lds(&B.wt[o2]);
-        if (w == 0) continue;
-        const int pk = lds(&B.dec[o2]);
-        atomicAdd(&dsz_cta[pk & 0xffff], w);
-        atomicAdd(&dsz_cta[pk >> 16], -w);
-      }
-      __syncthreads();
-      for (int z = z0; z < z1; z++) {
-        const int o = z - pos;
-        const int fl = lds(&B.flag[o]);
-        if (fl & 4) {                    // medium vertex: validated by the CTA below
-          Dw += lds(&B.wt[o]);
-          Vw += lds(&B.vd[o]);
-          continue;
-        }
-        int why = ((fl & 2) && z != pos) ? 1 : 0;
-        if (!why && Dw > max(lds(&B.slack[o]), 0)) {
-          // beyond the slack: decide again with the exact sizes at this position
-          const int pk = lds(&B.dec[o]);
-          const int own = pk >> 16;
-          const int d2 = ldg_recheck(I, R, B, o, own, metric, cnt, dsz_cta, cta_o0);
-          if (d2 != (pk & 0xffff)) {
-            if (fl & 8) {
-              // isolated vertex: take the exact decision (no weight, no nets, so
-              // no later position sees the difference)
-              if (lane == 0) {
-                B.dec[o] = (own << 16) | d2;
-                B.flag[o] = (unsigned char)((fl & ~1) | ((fl & 16) && d2 != own ? 1 : 0));
+        for (int z = z0; z < z1; z++) {
+          const int o = z - pos;
+          if (z < zfix) {
+            Dw += lds(&B.wt[o]);
+            Vw += lds(&B.vd[o]);
+            continue;
+          }
+          const int fl = lds(&B.flag[o]);
+          if (fl & 4) {                    // medium vertex: validated by the CTA below
+            Dw += lds(&B.wt[o]);
+            Vw += lds(&B.vd[o]);
+            continue;
+          }
+          int why = ((fl & 2) && z != pos) ? 1 : 0;
+          if (!why && Dw > max(lds(&B.slack[o]), 0)) {
+            // beyond the slack: decide again with the exact sizes at this position
+            const int pk = lds(&B.dec[o]);
+            const int own = pk >> 16;
+            const int d2 = ldg_recheck(I, R, B, o, own, metric, cnt, dsz_cta, cta_o0);
+            if (d2 != (pk & 0xffff)) {
+              if (fl & 8) {
+                // isolated vertex: take the exact decision (no weight, no nets, so
+                // no later position sees the difference)
+                if (lane == 0) {
+                  B.dec[o] = (own << 16) | d2;
+                  B.flag[o] = (unsigned char)((fl & ~1) | ((fl & 16) && d2 != own ? 1 : 0));
+                }
+              } else {
+                why = 2;
+                if (lane == 0) B.dfix[o] = d2;
               }
-            } else {
-              why = 2;
             }
           }
+          if (!why) why = Vw > max(lds(&B.vslack[o]), 0) ? 3 : mtpos < z ? 4 : 0;
+          bool bad = why != 0;
+          if (!bad) {
+            const int v = __ldg(&I.order[z]);
+            const int own = lds(&B.dec[o]) >> 16;
+            const bool mover = fl & 1;
+            const uint32_t base = __ldg(&I.vptr[v]);
+            const int deg = (int)(__ldg(&I.vptr[v + 1]) - base);
+            const int dz = lds(&B.dec[o]) & 0xffff;
+            const int c = conflicts(I, B, vol, z, own, dz != own, mover, base, deg, lane, 32, lds(&B.ctab_over[par]) != 0);
+            const int c5 = __any_sync(kAll, c == 5), c6 = __any_sync(kAll, c == 6), c7 = __any_sync(kAll, c == 7);
+            why = c5 ? 5 : c6 ? 6 : c7 ? 7 : 0;
+            bad = why != 0;
+          }
+          if (bad) {
+            if (lane == 0) atomicMin(cut_w, (z << 3) | why);   // position, then cut reason
+            break;
+          }
+          Dw += lds(&B.wt[o]);
+          Vw += lds(&B.vd[o]);
         }
-        if (!why) why = Vw > max(lds(&B.vslack[o]), 0) ? 3 : mtpos < z ? 4 : 0;
-        bool bad = why != 0;
-        if (!bad) {
-          const int v = __ldg(&I.order[z]);
-          const int own = lds(&B.dec[o]) >> 16;
-          const bool mover = fl & 1;
-          const uint32_t base = __ldg(&I.vptr[v]);
-          const int deg = (int)(__ldg(&I.vptr[v + 1]) - base);
-          const int dz = lds(&B.dec[o]) & 0xffff;
-          const int c = conflicts(I, B, vol, z, own, dz != own, mover, base, deg, lane, 32, lds(&B.ctab_over[par]) != 0);
-          const int c5 = __any_sync(kAll, c == 5), c6 = __any_sync(kAll, c == 6), c7 = __any_sync(kAll, c == 7);
-          why = c5 ? 5 : c6 ? 6 : c7 ? 7 : 0;
-          bad = why != 0;
+        __syncthreads();
+        for (int mi = lower_bound_pos(B.mid_pos, B.nmid, cz0); mi < B.nmid; mi++) {
+          const int z = __ldg(&B.mid_pos[mi]);
+          if (z >= cz1) break;
+          if (z < zfix) continue;
+          cta_validate_ldg(I, B, R, metric, z, pos, q, par, mtpos, s_pre_w, s_pre_v, cnt_b, dsz_cta, cta_o0, true, cut_w);
         }
-        if (bad) {
-          if (lane == 0) atomicMin(&B.ctl[par], (z << 3) | why);   // position, then cut reason
-          break;
+        for (int j = 0; j < ns; j++) {
+          // a whole-grid vertex: its nets checked by every thread, the rest by the
+          // CTA owning its position
+          const int zs = s_gz[j], own_s = s_go[j];
+          if (zs < zfix) continue;
+          const int os = zs - pos;
+          const int fl = lds(&B.flag[os]);
+          const int c = conflicts(I, B, vol, zs, own_s, (lds(&B.dec[os]) & 0xffff) != own_s, fl & 1, s_gb[j], s_gd[j],
+                                  gtid, gthreads, lds(&B.ctab_over[par]) != 0);
+          if (c) atomicMin(cut_w, (zs << 3) | c);
+          if (zs >= cz0 && zs < cz1)
+            cta_validate_ldg(I, B, R, metric, zs, pos, q, par, mtpos, s_pre_w, s_pre_v, cnt_b, dsz_cta, cta_o0, false,
+                             cut_w);
         }
-        Dw += lds(&B.wt[o]);
-        Vw += lds(&B.vd[o]);
+        __syncthreads();
+        if (threadIdx.x == 0) atomicMax(&B.stats[39], gtimer() - tV);
+        if (!grid_barrier(B.bar, I.status)) return;
+        cutw = lds(cut_w);
+        if (blockIdx.x == 0 && threadIdx.x == 0) B.ctl[4 + ((vr + 1) & 1)] = kNone;   // the next pass's word
+        vr++;
+        // a size flip of a light position (MSV / MSRV): fix it and validate again
+        bool fix = vfix && nfix < B.maxfix && cutw != kNone && (cutw & 7) == 2;
+        const int zc = cutw >> 3;
+        if (fix) fix = zc < end_w && __ldg(&B.vclass[__ldg(&I.order[zc])]) == 0;
+        if (!fix) break;
+        if (gw == (zc - pos) / q) fix_position(I, B, R, metric, zc, zc - pos, par, gw, loc, gains, losses, adelta);
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+          B.stats[44]++;
+          B.stats[35] += B.stats[39];
+          B.stats[39] = 0;
+        }
+        if (!grid_barrier(B.bar, I.status)) return;
+        zfix = zc;
       }
-      __syncthreads();
-      for (int mi = lower_bound_pos(B.mid_pos, B.nmid, cz0); mi < B.nmid; mi++) {
-        const int z = __ldg(&B.mid_pos[mi]);
-        if (z >= cz1) break;
-        cta_validate_ldg(I, B, R, metric, z, pos, q, par, mtpos, s_pre_w, s_pre_v, cnt_b, dsz_cta, cta_o0, true);
-      }
-      for (int j = 0; j < ns; j++) {
-        // a whole-grid vertex: its nets checked by every thread, the rest by the
-        // CTA owning its position
-        const int zs = s_gz[j], own_s = s_go[j];
-        const int os = zs - pos;
-        const int fl = lds(&B.flag[os]);
-        const int c = conflicts(I, B, vol, zs, own_s, (lds(&B.dec[os]) & 0xffff) != own_s, fl & 1, s_gb[j], s_gd[j],
-                                gtid, gthreads, lds(&B.ctab_over[par]) != 0);
-        if (c) atomicMin(&B.ctl[par], (zs << 3) | c);
-        if (zs >= cz0 && zs < cz1)
-          cta_validate_ldg(I, B, R, metric, zs, pos, q, par, mtpos, s_pre_w, s_pre_v, cnt_b, dsz_cta, cta_o0, false);
-      }
-      __syncthreads();
-      if (threadIdx.x == 0) atomicMax(&B.stats[39], gtimer() - tV);
-      if (!grid_barrier(B.bar, I.status)) return;
       // ---- C: commit every mover before the cut.
-      const int cutw = lds(&B.ctl[par]);
       const int cut = cutw == kNone ? end_w : min(cutw >> 3, end_w);
       if (blockIdx.x == 0 && threadIdx.x == 0) {
         const unsigned long long tB = gtimer();
@@ -1305,13 +1401,13 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
       for (int z = z0; z < z1; z++) {
         const int o = z - pos;
         const int fl = lds(&B.flag[o]);
-        if (!(fl & 1) || (fl & 4)) continue;
+        if (!(fl & (1 | 64)) || (fl & 4)) continue;   // claims held: a mover or a replaced mover
         const int v = __ldg(&I.order[z]);
         const int pk = lds(&B.dec[o]);
         const int own = pk >> 16, d = pk & 0xffff;
         const uint32_t base = __ldg(&I.vptr[v]);
         const int deg = (int)(__ldg(&I.vptr[v + 1]) - base);
-        if (z < cut) {
+        if ((fl & 1) && z < cut) {
           for (int k = lane; k < deg; k += 32)
             commit_rec(I, v, own, d, (int)__ldg(&I.vnets[base + k]), lds(&B.rec[base + k]), vol ? &V : nullptr);
           if (lane == 0) {
@@ -1323,7 +1419,7 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
             atomicAdd((unsigned long long*)&I.moves[it], 1ull);
           }
         }
-        unclaim_nets(I, B, vol, base, deg, lane, 32);
+        unclaim_nets(I, B, vol, base, deg, lane, 32, fl & 1, fl & 64);
       }
       for (int mi = lower_bound_pos(B.mid_pos, B.nmid, cz0); mi < B.nmid; mi++) {
         const int z = __ldg(&B.mid_pos[mi]);
@@ -1409,7 +1505,6 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
         }
       }
       if (gw == 0 && lane == 0) {
-        B.ctl[par ^ 1] = kNone;
         B.ctl[2 + (par ^ 1)] = kNone;
         B.ctab_over[par ^ 1] = 0;
         B.mcnt[par ^ 1] = 0;
@@ -1418,9 +1513,8 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
       if (cut == end_w) {
         if (end_w == pos + W) W = min(2 * W, B.wmax);
       } else {
-        // regrow from the last valid length: twice it for MSV (cuts come every
-        // ~200 positions), four times for the metrics with rarer cuts
-        W = max(256, min(B.wmax, (metric == 4 ? 2 : 4) * (cut - pos)));
+        // regrow from the last valid length
+        W = max(256, min(B.wmax, B.wgrow * (cut - pos)));
       }
       pos = cut;
       round++;
