@@ -52,12 +52,14 @@ int default_super_work(int metric) {
     default: return 262144;
   }
 }
-// Whole-grid vertices one LDG window may hold.  Each one past the window's
-// eventual cut is evaluated again in a later window, so metrics whose windows
-// end early hold fewer.
+// Whole-grid vertices one window may hold.  Each one past the window's
+// eventual cut (first mover for TM / MSM) is evaluated again in a later window,
+// so metrics whose windows end early hold fewer.
 int default_grid_verts(int metric) {
   switch (metric) {
-    case FP_METRIC_TV: return kMaxGridVerts;
+    case FP_METRIC_TV:
+    case FP_METRIC_MSM: return kMaxGridVerts;
+    case FP_METRIC_TM:
     case FP_METRIC_MSRV: return 4;
     default: return 2;
   }

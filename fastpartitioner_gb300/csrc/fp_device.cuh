@@ -49,7 +49,7 @@ struct DevInstance {
 // Round statistics kept per instance (fp_get_stats).
 constexpr int kNumStats = 48;
 
-// Whole-grid vertices one window of the LDG engine may hold.
+// Whole-grid vertices one window may hold (slots of the whole-grid tallies).
 constexpr int kMaxGridVerts = 8;
 
 // Device buffers of the speculative engine (fp_spec.cu), allocated with the
@@ -104,7 +104,7 @@ struct SpecBuf {
   int* hadelta;          // [2 * kMaxGridVerts * K]
   int* hmisc;            // [2 * kMaxGridVerts * 8]
   unsigned long long* mlast;  // [K] TV: (window stamp << 32) | last position whose scan holds the part
-  int gmax;              // whole-grid vertices one LDG window may hold (1 .. kMaxGridVerts)
+  int gmax;              // whole-grid vertices one window may hold (1 .. kMaxGridVerts)
   int wgrow;             // LDG window after a cut: this many times the last valid length
   int maxfix;            // in-window decision fixes per window (MSV / MSRV)
   unsigned long long* stats;  // [kNumStats] round statistics (see fp_get_stats)

@@ -13,8 +13,9 @@
 // vertex's own part, and conn == 0 (losses per candidate part,
 // TM/partition.cpp:408-450) staged in shared memory when K <= 256.  Vertices
 // are classed by work like the LDG engine: light ones are evaluated by one
-// warp, medium ones by one CTA inside the window, the heaviest in a round of
-// their own split across the grid.
+// warp, medium ones by one CTA, the heaviest (up to gmax per window) by all
+// warps of the grid, whose slices meet in global sets that one CTA per vertex
+// decides from after a grid barrier.
 
 #include "fp_spec_common.cuh"
 
@@ -414,6 +415,8 @@ __global__ void __launch_bounds__(kSThreads) spec_msg_kernel(DevInstance I, Spec
   __shared__ int iscr[kSWarps];
   __shared__ unsigned oc1m[kSWarps];
   __shared__ int s_mx, s_nmax, s_stop;
+  __shared__ int s_gz[kMaxGridVerts], s_go[kMaxGridVerts], s_gd[kMaxGridVerts];
+  __shared__ uint32_t s_gb[kMaxGridVerts];
   const bool msm = I.metric == 3;
   const int K = I.K;
   const int words = (K + 31) >> 5;
@@ -482,19 +485,35 @@ __global__ void __launch_bounds__(kSThreads) spec_msg_kernel(DevInstance I, Spec
       }
       const MsgRound Rd{sizes_s, msgs_s, maxl_s, msm ? s_nmax : 0, msm ? s_mx : 0};
       while (hidx < B.nheavy && __ldg(&B.heavy_pos[hidx]) < pos) hidx++;
-      const int next_heavy = hidx < B.nheavy ? __ldg(&B.heavy_pos[hidx]) : I.nov;
 
-      if (next_heavy == pos) {
-        // ========================================================== heavy round
-        const int hp = heavy_round & 1;
-        uint32_t* hR = reinterpret_cast<uint32_t*>(B.hloss + hp * K);      // words <= K
-        uint32_t* hS = reinterpret_cast<uint32_t*>(B.hadelta + hp * K);
-        unsigned long long* hf = B.hfirst + hp * K;
-        int* hmisc = B.hmisc + hp * 8;
-        const int v = pos;
-        const int own = lds(&I.part_vec[v]);
-        const uint32_t base = __ldg(&I.vptr[v]);
-        const int deg = (int)(__ldg(&I.vptr[v + 1]) - base);
+      // ================================================================= round
+      // A window holds up to gmax whole-grid vertices and ends before the next
+      // one, or at its first mover.
+      int end_w = min(pos + W, I.nov);
+      if (hidx + B.gmax < B.nheavy) end_w = min(end_w, (int)__ldg(&B.heavy_pos[hidx + B.gmax]));
+      int ns = 0;
+      while (ns < B.gmax && hidx + ns < B.nheavy && __ldg(&B.heavy_pos[hidx + ns]) < end_w) ns++;
+      const int hp = heavy_round & 1;   // whole-grid sets, double-buffered by parity
+      // slot j of this parity: K words at hslot(j) (receivers in hloss, senders in
+      // hadelta, first non-source nets in hfirst), 8 words of hmisc at hmslot(j)
+      auto hslot = [&](int j) { return ((size_t)hp * kMaxGridVerts + j) * K; };
+      auto hmslot = [&](int j) { return (hp * kMaxGridVerts + j) * 8; };
+      if ((int)threadIdx.x < ns) {
+        const int v = __ldg(&B.heavy_pos[hidx + threadIdx.x]);
+        const uint32_t b = __ldg(&I.vptr[v]);
+        s_gz[threadIdx.x] = v;
+        s_go[threadIdx.x] = lds(&I.part_vec[v]);
+        s_gb[threadIdx.x] = b;
+        s_gd[threadIdx.x] = (int)(__ldg(&I.vptr[v + 1]) - b);
+      }
+      __syncthreads();
+      // ---- tally slices of the whole-grid vertices, combined per CTA
+      for (int j = 0; j < ns; j++) {
+        const int v = s_gz[j], own = s_go[j], deg = s_gd[j];
+        const uint32_t base = s_gb[j];
+        uint32_t* hR = reinterpret_cast<uint32_t*>(B.hloss + hslot(j));      // words <= K
+        uint32_t* hS = reinterpret_cast<uint32_t*>(B.hadelta + hslot(j));
+        unsigned long long* hf = B.hfirst + hslot(j);
         msg_begin(I, Wk, own, msm);
         int g = 0;
         {
@@ -512,41 +531,10 @@ __global__ void __launch_bounds__(kSThreads) spec_msg_kernel(DevInstance I, Spec
         }
         for (int p = threadIdx.x; p < K; p += blockDim.x)
           if (fs_b[p] != ~0ull) atomicMin(&hf[p], fs_b[p]);
-        if (lane == 0 && g) atomicAdd(&hmisc[0], g);
-        if (!grid_barrier(B.bar, I.status)) return;
-        // every CTA takes the same decision from the global sets
-        for (int x = threadIdx.x; x < words; x += blockDim.x) { R_b[x] = lds(&hR[x]); S_b[x] = lds(&hS[x]); }
-        for (int p = threadIdx.x; p < K; p += blockDim.x) fs_b[p] = lds(&hf[p]);
-        __syncthreads();
-        const int best = msg_decide_cta(I, M, Rd, W0, own, lds(&hmisc[0]), msm, uscr, iscr);
-        if (!grid_barrier(B.bar, I.status)) return;
-        if (best >= 0) msg_commit_grid(I, v, own, best, gw, nwarps, it);
-        dirty = best >= 0;
-        {
-          const int op = hp ^ 1;   // clear the other heavy buffers for the next heavy round
-          for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < K; p += gridDim.x * blockDim.x) {
-            B.hloss[op * K + p] = 0;
-            B.hadelta[op * K + p] = 0;
-            B.hfirst[op * K + p] = ~0ull;
-          }
-          if (blockIdx.x == 0 && threadIdx.x < 8) B.hmisc[op * 8 + threadIdx.x] = 0;
-        }
-        if (blockIdx.x == 0 && threadIdx.x == 0) B.ctl[(round & 1) ^ 1] = kNone;
-        pos += 1;
-        heavy_round++;
-        round++;
-        if (!grid_barrier(B.bar, I.status)) return;
-        if (blockIdx.x == 0 && threadIdx.x == 0) {
-          B.stats[1]++;
-          const unsigned long long tH = gtimer();
-          B.stats[19] += tH - tA;
-          tA = tH;
-        }
-        continue;
+        if (lane == 0 && g) atomicAdd(&B.hmisc[hmslot(j)], g);
+        __syncthreads();   // the per-warp scratch serves the next vertex and the evaluations below
       }
 
-      // ============================================================ light round
-      const int end_w = min(min(pos + W, I.nov), next_heavy);
       const int par = round & 1;
       const int span = end_w - pos;
       const int q = (span + nwarps - 1) / nwarps;
@@ -613,6 +601,38 @@ __global__ void __launch_bounds__(kSThreads) spec_msg_kernel(DevInstance I, Spec
         B.stats[16] += tE - tA;
         tA = tE;
       }
+      if (ns) {
+        // ---- the whole-grid vertices before the first mover: CTA j decides
+        // vertex j from the global sets (one read of the first mover per CTA:
+        // other CTAs may lower it meanwhile)
+        if (threadIdx.x == 0) s_stop = lds(&B.ctl[par]);
+        __syncthreads();
+        const int f0 = s_stop;
+        for (int j = blockIdx.x; j < ns; j += gridDim.x) {
+          const int v = s_gz[j], own = s_go[j];
+          if (v > f0) break;
+          const size_t hs = hslot(j);
+          for (int x = threadIdx.x; x < words; x += blockDim.x) {
+            R_b[x] = lds(reinterpret_cast<const uint32_t*>(B.hloss + hs) + x);
+            S_b[x] = lds(reinterpret_cast<const uint32_t*>(B.hadelta + hs) + x);
+            c1c_b[x] = lds(&I.c1col[(size_t)own * words + x]);
+          }
+          for (int p = threadIdx.x; p < K; p += blockDim.x) fs_b[p] = lds(&B.hfirst[hs + p]);
+          __syncthreads();
+          const int best = msg_decide_cta(I, M, Rd, W0, own, lds(&B.hmisc[hmslot(j)]), msm, uscr, iscr);
+          if (best >= 0 && threadIdx.x == 0) {
+            B.dec[v - pos] = (own << 16) | best;
+            atomicMin(&B.ctl[par], v);
+          }
+          __syncthreads();
+        }
+        if (!grid_barrier(B.bar, I.status)) return;
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+          const unsigned long long tH = gtimer();
+          B.stats[19] += tH - tA;
+          tA = tH;
+        }
+      }
       // ---- commit the first mover (if any); the window ends after it
       const int f = lds(&B.ctl[par]);
       int end = end_w;
@@ -623,9 +643,22 @@ __global__ void __launch_bounds__(kSThreads) spec_msg_kernel(DevInstance I, Spec
         if (blockIdx.x == 0 && threadIdx.x == 0) B.stats[2]++;
         dirty = true;
       }
+      if (ns) {
+        // the other parity's sets are cleared for the next window with
+        // whole-grid vertices
+        const size_t ob = (size_t)(hp ^ 1) * kMaxGridVerts * K;
+        for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < kMaxGridVerts * K; p += gridDim.x * blockDim.x) {
+          B.hloss[ob + p] = 0;
+          B.hadelta[ob + p] = 0;
+          B.hfirst[ob + p] = ~0ull;
+        }
+        if (blockIdx.x == 0 && threadIdx.x < 8 * kMaxGridVerts) B.hmisc[(hp ^ 1) * 8 * kMaxGridVerts + threadIdx.x] = 0;
+        heavy_round++;
+      }
       if (blockIdx.x == 0 && threadIdx.x == 0) {
         B.ctl[par ^ 1] = kNone;
         B.stats[0]++;
+        B.stats[1] += ns;
         B.stats[9] += end - pos;
         B.stats[f == kNone ? 3 : 8]++;
       }

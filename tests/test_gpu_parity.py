@@ -278,3 +278,23 @@ def test_gpu_vertex_classes_do_not_change_results(fp, orc, gpu_engine, metric, b
         assert inst.metrics() == o["metrics_final"], f"{metric} {bounds}"
         st = inst.stats()
         assert st["heavy_rounds"] > 0, f"{metric} {bounds}: no whole-grid vertex exercised"
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("seed", [5, 83])
+def test_gpu_msv_in_window_fixes(fp, orc, gpu_engine, seed):
+    """MSV moves nearly every vertex, so part-size drift flips decisions inside
+    most windows; the first flipped light position is fixed in place (new
+    records, accept test and claims) and the window validated again.  The
+    result still equals the oracle's, lists and metrics included."""
+    hg = fp.generate(fp.GenSpec.zipf(20000, 20000, 2.1, 2, 2000, beta=1.5, weight_rule=1, seed=seed))
+    K, passes = 64, 3
+    o = orc.run_oracle(hg, K, "MSV", passes)
+    with gpu_engine.instance(hg, K, "MSV") as inst:
+        inst.initial_partition()
+        inst.refine(passes)
+        np.testing.assert_array_equal(inst.partition(), o["part_vec"])
+        ln, pt, _ = inst.lists()
+        np.testing.assert_array_equal(orc.flat_lists(hg, ln, pt), orc.flat_lists(hg, o["ep_len"], o["ep_part"]))
+        assert inst.metrics() == o["metrics_final"]
+        assert inst.stats()["window_fixes"] > 0, "no in-window fix exercised"
