@@ -448,7 +448,9 @@ __global__ void __launch_bounds__(kSThreads) spec_msg_kernel(DevInstance I, Spec
   bool dirty = true;   // staged masks out of date (a move was committed)
   for (int it = 0; it < passes; it++) {
     int pos = 0;
-    const int W = B.wmax_msg;
+    // window length: one position per warp to start, doubled after a window
+    // without a mover, twice the distance to the mover after one
+    int W = min(nwarps, B.wmax_msg);
     int hidx = 0;
     while (pos < I.nov) {
       // ------------------------------------------------------------ round state
@@ -498,6 +500,7 @@ __global__ void __launch_bounds__(kSThreads) spec_msg_kernel(DevInstance I, Spec
       // hadelta, first non-source nets in hfirst), 8 words of hmisc at hmslot(j)
       auto hslot = [&](int j) { return ((size_t)hp * kMaxGridVerts + j) * K; };
       auto hmslot = [&](int j) { return (hp * kMaxGridVerts + j) * 8; };
+      const unsigned long long tR = gtimer();
       if ((int)threadIdx.x < ns) {
         const int v = __ldg(&B.heavy_pos[hidx + threadIdx.x]);
         const uint32_t b = __ldg(&I.vptr[v]);
@@ -534,6 +537,7 @@ __global__ void __launch_bounds__(kSThreads) spec_msg_kernel(DevInstance I, Spec
         if (lane == 0 && g) atomicAdd(&B.hmisc[hmslot(j)], g);
         __syncthreads();   // the per-warp scratch serves the next vertex and the evaluations below
       }
+      if (ns && threadIdx.x == 0) atomicMax(&B.stats[38], gtimer() - tR);
 
       const int par = round & 1;
       const int span = end_w - pos;
@@ -595,11 +599,18 @@ __global__ void __launch_bounds__(kSThreads) spec_msg_kernel(DevInstance I, Spec
           break;
         }
       }
+      __syncthreads();
+      if (threadIdx.x == 0) atomicMax(&B.stats[36], gtimer() - tR);
       if (!grid_barrier(B.bar, I.status)) return;
       if (blockIdx.x == 0 && threadIdx.x == 0) {
         const unsigned long long tE = gtimer();
         B.stats[16] += tE - tA;
         tA = tE;
+        // per-window maxima over CTAs (no CTA writes these again before the next window)
+        B.stats[32] += B.stats[36];
+        B.stats[34] += B.stats[38];
+        B.stats[36] = 0;
+        B.stats[38] = 0;
       }
       if (ns) {
         // ---- the whole-grid vertices before the first mover: CTA j decides
@@ -662,6 +673,7 @@ __global__ void __launch_bounds__(kSThreads) spec_msg_kernel(DevInstance I, Spec
         B.stats[9] += end - pos;
         B.stats[f == kNone ? 3 : 8]++;
       }
+      W = f == kNone ? min(2 * W, B.wmax_msg) : max(min(nwarps, B.wmax_msg), min(B.wmax_msg, 2 * (end - pos)));
       pos = end;
       round++;
       if (!grid_barrier(B.bar, I.status)) return;
