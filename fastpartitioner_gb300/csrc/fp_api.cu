@@ -47,8 +47,8 @@ constexpr int kLightWork = 2048;
 int default_super_work(int metric) {
   switch (metric) {
     case FP_METRIC_MSV: return 16384;
-    case FP_METRIC_MSRV: return 32768;
-    case FP_METRIC_TM: return 65536;
+    case FP_METRIC_MSRV:
+    case FP_METRIC_TM: return 32768;
     default: return 262144;
   }
 }
