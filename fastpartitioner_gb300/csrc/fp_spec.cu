@@ -15,9 +15,11 @@
 //                 of one of its nets, or the count of its own part there; the
 //                 weight moved before it stays within its size slack (the LDG
 //                 argmax, its tie-breaks and TV's clamps cannot flip); the
-//                 volumes stay within its volume slack; no earlier mover touched
-//                 a max-volume part; for TV, no stale marker can apply.  The
-//                 first invalid position cuts the window.
+//                 volumes stay within its volume slack; if it would leave its
+//                 part, no earlier mover touched a max-volume part; for TV, no
+//                 stale marker can apply.  The first invalid position cuts the
+//                 window (MSV / MSRV fix a position whose decision the size
+//                 drift flipped in place and validate again from it).
 //   C  commit     all movers before the cut are applied at once -- on any net
 //                 they either are alone or only shift counts, which commute --
 //                 and the next window starts at the cut.
@@ -28,9 +30,9 @@
 // once, by a flattened pass over the slots (locate_batch), and recorded per
 // (vertex, net); the gain / loss terms and the commit then take O(1) per net.
 // Vertices are classed by work (list slots over their nets, host-side): light
-// ones are evaluated by one warp, medium ones by one CTA inside the window, and
-// the heaviest get a round of their own in which all warps of the grid split
-// the tally, the gain / loss sums and the move.
+// ones are evaluated by one warp, medium ones by one CTA, and the heaviest (up
+// to gmax per window) by all warps of the grid, which split the tally, the gain
+// / loss sums and the move in two extra grid phases of the window.
 
 #include "fp_spec_common.cuh"
 
@@ -720,7 +722,7 @@ __device__ void cta_validate_ldg(const DevInstance& I, const SpecBuf& B, const R
     }
     __syncthreads();
   }
-  if (threadIdx.x == 0 && shw == 0) shw = V > max(lds(&B.vslack[o]), 0) ? 3 : mtpos < z ? 4 : 0;
+  if (threadIdx.x == 0 && shw == 0) shw = V > max(lds(&B.vslack[o]), 0) ? 3 : (mtpos < z && d != own) ? 4 : 0;
   __syncthreads();
   int why = shw;
   if (why == 0 && check_nets) {
@@ -1313,7 +1315,13 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
               }
             }
           }
-          if (!why) why = Vw > max(lds(&B.vslack[o]), 0) ? 3 : mtpos < z ? 4 : 0;
+          if (!why) {
+            // the max-volume parts enter only the accept test of a vertex whose
+            // decision leaves its part (MSRV/partition.cpp:308-400,
+            // MGV/partition.cpp:292-362), and they change only with a move
+            const int pk = lds(&B.dec[o]);
+            why = Vw > max(lds(&B.vslack[o]), 0) ? 3 : (mtpos < z && (pk & 0xffff) != (pk >> 16)) ? 4 : 0;
+          }
           bool bad = why != 0;
           if (!bad) {
             const int v = __ldg(&I.order[z]);
