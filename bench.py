@@ -49,6 +49,24 @@ WORKLOADS = {
 }
 
 
+def measured_traffic(kernel, config, scale):
+    """DRAM bytes per launch of `kernel` on the full-size workload, from an ncu
+    summary under profiles/: a line `traffic: <kernel> <config> <bytes>` (the
+    capture's dram__bytes_read.sum + dram__bytes_write.sum per launch, scaled to
+    full size as that summary states).  None when absent or not full size."""
+    if scale != 1:
+        return None
+    for md in sorted((ROOT / "profiles").glob("*.md")):
+        for line in md.read_text().splitlines():
+            f = line.strip().strip("`").split()
+            if len(f) == 4 and f[0] == "traffic:" and f[1] == kernel and f[2] == config:
+                try:
+                    return int(float(f[3]))
+                except ValueError:
+                    return None
+    return None
+
+
 def spec_for(fp, w, scale=1, unit_weights=False):
     nov, noe = max(w["nov"] // scale, 1024), max(w["noe"] // scale, 1024)
     if w["alpha"] > 0:
@@ -280,13 +298,7 @@ def run_ours(args):
                             "algorithmic_bytes_per_launch": int(k["bytes"] / k["launches"]),
                             "achieved_gbs": ach, "frac": ach / peak}
     dom = max(per_kernel, key=lambda n: per_kernel[n]["share"])
-    traffic = None
-    prof = ROOT / "profiles" / "traffic.json"
-    if prof.exists():
-        try:
-            traffic = json.loads(prof.read_text()).get(args.config, {}).get(dom)
-        except Exception:
-            traffic = None
+    traffic = measured_traffic(dom, args.config, args.scale)
 
     cpu = None
     if not args.no_cpu_baseline and rank == 0:
