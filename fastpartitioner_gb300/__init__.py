@@ -466,7 +466,8 @@ class Instance:
                  cta_rest_cycles=int(x[31]), local_eval_ms=x[32] / 1e6, grid_vertex_ms=x[33] / 1e6,
                  grid_tally_ms=x[34] / 1e6, local_validate_ms=x[35] / 1e6, cta_evals=int(x[40]),
                  light_tally_cycles=int(x[41]), light_decide_cycles=int(x[42]), light_rest_cycles=int(x[43]),
-                 window_fixes=int(x[44]))
+                 window_fixes=int(x[44]), val_prefix_cta_ns=int(x[45]), val_light_cta_ns=int(x[46]),
+                 val_rest_cta_ns=int(x[47]))
         return d
 
     def last_launches(self) -> int:

@@ -1266,6 +1266,7 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
         }
         const int mtpos = lds(&B.ctl[2 + par]);
         const int nm = lds(&B.mcnt[par]);
+        const unsigned long long tV1 = gtimer();
         // part-size changes of the window's movers before this CTA's first position
         // (phase-A scratch gains_b is free now)
         int* dsz_cta = gains_b;
@@ -1343,6 +1344,7 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
           Vw += lds(&B.vd[o]);
         }
         __syncthreads();
+        const unsigned long long tV2 = gtimer();
         for (int mi = lower_bound_pos(B.mid_pos, B.nmid, cz0); mi < B.nmid; mi++) {
           const int z = __ldg(&B.mid_pos[mi]);
           if (z >= cz1) break;
@@ -1364,7 +1366,14 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
                              cut_w);
         }
         __syncthreads();
-        if (threadIdx.x == 0) atomicMax(&B.stats[39], gtimer() - tV);
+        if (threadIdx.x == 0) {
+          const unsigned long long tV3 = gtimer();
+          atomicMax(&B.stats[39], tV3 - tV);
+          // per-pass phase times of this CTA: prefix sums, light positions, the rest
+          atomicAdd(&B.stats[45], tV1 - tV);
+          atomicAdd(&B.stats[46], tV2 - tV1);
+          atomicAdd(&B.stats[47], tV3 - tV2);
+        }
         if (!grid_barrier(B.bar, I.status)) return;
         cutw = lds(cut_w);
         if (blockIdx.x == 0 && threadIdx.x == 0) B.ctl[4 + ((vr + 1) & 1)] = kNone;   // the next pass's word

@@ -186,7 +186,9 @@ int fp_metrics_noalloc(int32_t K, int32_t nov, int32_t noe, int64_t pins, const 
  * vertices' decision and accept phases, [34] the slowest CTA's tally of
  * whole-grid vertex slices, [35] the slowest CTA's validation; [40] CTA
  * evaluations; [41..43] SM cycles of warp evaluations in tally, decision and
- * the rest; [44] decisions fixed inside a window (MSV / MSRV). */
+ * the rest; [44] decisions fixed inside a window (MSV / MSRV); [45..47]
+ * nanoseconds summed over CTAs and validation passes in prefix sums, light
+ * positions and the rest (medium and whole-grid vertices). */
 int fp_get_stats(fp_instance* inst, int64_t* out, int32_t n);
 /* Number of kernel launches the last fp_refine / fp_metrics call enqueued. */
 int fp_last_launches(fp_instance* inst, int64_t* launches);
