@@ -27,11 +27,14 @@ template <class T>
 __device__ __forceinline__ T lds(const T* p) { return __ldcg(p); }
 
 // Grid-wide barrier of a co-resident (cooperatively launched) grid with a
-// bounded wait.  bar[0] = arrivals, bar[1] = generation, bar[2] = abort flag.
-// Returns false in every thread of the CTA if the wait gave up (another CTA
-// stopped arriving) or another CTA aborted; the kernel then reports
-// FP_ERR_DEVICE_TIMEOUT through `status` and returns.
-constexpr unsigned kBarrierSpins = 1u << 24;   // with 64 ns naps: about a second or more
+// bounded wait.  bar[0] = arrivals, bar[2] = abort flag (bar[1], bar[3]
+// unused).  Every CTA adds to bar[0] once per barrier: CTA 0 adds
+// 2^31 - (gridDim.x - 1), the others 1, so bit 31 flips exactly when the last
+// CTA arrives and the low bits return to their value -- no reset, one atomic
+// per CTA.  Returns false in every thread of the CTA if the wait gave up
+// (another CTA stopped arriving) or another CTA aborted; the kernel then
+// reports FP_ERR_DEVICE_TIMEOUT through `status` and returns.
+constexpr unsigned kBarrierSpins = 1u << 21;   // polls of an L2 line with 32 ns naps: about a second or more
 
 __device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
   unsigned v;
@@ -44,24 +47,17 @@ __device__ __forceinline__ bool grid_barrier(unsigned* bar, int* status) {
   __syncthreads();
   if (threadIdx.x == 0) {
     int ok = 1;
+    const unsigned inc = blockIdx.x == 0 ? 0x80000000u - (gridDim.x - 1) : 1u;
     __threadfence();
-    const unsigned gen = ld_acquire(&bar[1]);
-    const unsigned arrived = atomicAdd(&bar[0], 1u);
-    if (arrived == gridDim.x - 1) {
-      atomicExch(&bar[0], 0u);
-      __threadfence();
-      atomicAdd(&bar[1], 1u);
-    } else {
-      unsigned spins = 0;
-      while (ld_acquire(&bar[1]) == gen) {
-        if (ld_acquire(&bar[2]) != 0u || ++spins > kBarrierSpins) {
-          ok = 0;
-          break;
-        }
-        __nanosleep(64);
+    const unsigned old = atomicAdd(&bar[0], inc);
+    unsigned spins = 0;
+    while (((old ^ ld_acquire(&bar[0])) & 0x80000000u) == 0u) {
+      if ((++spins & 255u) == 0u && (ld_acquire(&bar[2]) != 0u || spins > kBarrierSpins)) {
+        ok = 0;
+        break;
       }
+      __nanosleep(32);
     }
-    if (ld_acquire(&bar[2]) != 0u) ok = 0;
     if (!ok) {
       atomicExch(&bar[2], 1u);
       atomicCAS(status, 0, -4);   // FP_ERR_DEVICE_TIMEOUT
