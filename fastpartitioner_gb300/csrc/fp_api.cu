@@ -427,7 +427,8 @@ int fp_instance_create(fp_ctx* ctx, const fp_hypergraph* h, int32_t K, int32_t m
       (rc = dalloc(in, &in->sb.cn_moved, cn ? g.pins : 1)) || (rc = dalloc(in, &in->sb.cn_kcnt, cn ? g.noe : 1)) ||
       (rc = dalloc(in, &in->sb.cn_nets, cn ? g.noe : 1)) || (rc = dalloc(in, &in->sb.cn_cnt, 4)) || (rc = dalloc(in, &in->vclass_d, g.nov)) ||
       (rc = dalloc(in, &in->sb.cand, (size_t)kSpecWindow * K)) || (rc = dalloc(in, &in->sb.ncand, kSpecWindow)) ||
-      (rc = dalloc(in, &in->sb.mlist, kSpecWindow)) || (rc = dalloc(in, &in->sb.mcnt, 2)) ||
+      (rc = dalloc(in, &in->sb.mlist, kSpecWindow)) || (rc = dalloc(in, &in->sb.midx, kSpecWindow)) ||
+      (rc = dalloc(in, &in->sb.mcnt, 2)) ||
       (rc = dalloc(in, &in->sb.wsum, kMaxSpecWarps)) || (rc = dalloc(in, &in->sb.vsum, kMaxSpecWarps)) ||
       (rc = dalloc(in, &in->sb.claim_m, g.noe)) || (rc = dalloc(in, &in->sb.claim64, g.noe)) || (rc = dalloc(in, &in->sb.claim_c, g.noe)) ||
       (rc = dalloc(in, &in->sb.mask_c, g.noe)) || (rc = dalloc(in, &in->sb.hcnt, 2 * kMaxGridVerts * K)) ||

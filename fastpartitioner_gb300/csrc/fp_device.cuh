@@ -74,7 +74,9 @@ struct SpecBuf {
                                 //     2: whole-grid round (LDG metrics)
   unsigned long long* cand;  // [wmax * K] LDG candidates per window offset (part, count, first)
   int* ncand;            // [wmax]
-  int* mlist;            // [wmax] window offsets of the round's movers (any order)
+  int4* mlist;           // [wmax] the round's movers (any order): window offset, weight,
+                         //     (own part << 16) | destination
+  int* midx;             // [wmax] index of a mover's mlist entry, by window offset
   int* mcnt;             // [2] their count, double-buffered by round parity
   int* wsum;             // [max_warps] per-warp sums of wt
   int* vsum;             // [max_warps] per-warp sums of vd

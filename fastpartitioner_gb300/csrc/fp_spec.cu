@@ -233,10 +233,9 @@ __device__ int ldg_recheck(const DevInstance& I, const RoundCtx& R, const SpecBu
   for (int p = lane; p < K; p += 32) dsz[p] = dsz_cta[p];
   __syncwarp();
   for (int o2 = o_from + lane; o2 < o; o2 += 32) {
-    if (!(lds(&B.flag[o2]) & 1)) continue;
-    const int w = lds(&B.wt[o2]);
-    if (w == 0) continue;
+    const int w = lds(&B.wt[o2]);   // 0 unless a mover
     const int pk = lds(&B.dec[o2]);
+    if (w == 0) continue;
     atomicAdd(&dsz[pk & 0xffff], w);
     atomicAdd(&dsz[pk >> 16], -w);
   }
@@ -439,6 +438,13 @@ __device__ __forceinline__ void claim_nets(const DevInstance& I, const SpecBuf& 
       B.rec_slot[base + k] = make_uint2(s1, s2);
     }
   }
+}
+
+// Appends a mover of window offset o to the round's list.
+__device__ __forceinline__ void list_mover(const SpecBuf& B, int par, int o, int wv, int pk) {
+  const int i = atomicAdd(&B.mcnt[par], 1);
+  B.mlist[i] = make_int4(o, wv, pk, 0);
+  B.midx[o] = i;
 }
 
 __device__ __forceinline__ void ctab_clear(const SpecBuf& B, uint2 sl) {
@@ -660,7 +666,7 @@ __device__ void cta_eval_ldg(const DevInstance& I, const SpecBuf& B, const Round
     claim_nets(I, B, vol, z, own, d, base, deg, threadIdx.x, blockDim.x, par);
     if (threadIdx.x == 0) {
       if (mt) atomicMin(&B.ctl[2 + par], z);
-      B.mlist[atomicAdd(&B.mcnt[par], 1)] = o;
+      list_mover(B, par, o, __ldg(&I.w[v]), (own << 16) | d);
     }
   }
   if (threadIdx.x == 0) {
@@ -686,8 +692,9 @@ __device__ void cta_eval_ldg(const DevInstance& I, const SpecBuf& B, const Round
 
 // Validation of a medium vertex by the whole CTA (the warp validation's rules).
 __device__ void cta_validate_ldg(const DevInstance& I, const SpecBuf& B, const RoundCtx& R, int metric, int z, int pos,
-                                 int q, int par, int mtpos, long long pre_w, long long pre_v, int* dsz,
-                                 const int* dsz_cta, int o_from, bool check_nets, int* cut) {
+                                 int q, int par, int mtpos, long long pre_w, long long pre_v, const int* cw,
+                                 const int* cv, int* dsz, const int* dsz_cta, int o_from, bool check_nets,
+                                 int* cut) {
   __shared__ long long shd[2];
   __shared__ int shw;
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -696,20 +703,26 @@ __device__ void cta_validate_ldg(const DevInstance& I, const SpecBuf& B, const R
   const int pk = lds(&B.dec[o]);
   const int own = pk >> 16, d = pk & 0xffff;
   const int v = __ldg(&I.order[z]);
-  if (threadIdx.x == 0) {
+  if (wib == 0) {
+    // drift before z: earlier CTAs, this CTA's warps before the owner (cw / cv),
+    // the owner's positions before z
     const int owner = o / q;
-    long long D = pre_w, V = pre_v;
-    for (int x = (int)blockIdx.x * kSWarps; x < owner; x++) {
-      D += lds(&B.wsum[x]);
-      V += lds(&B.vsum[x]);
+    long long D = 0, V = 0;
+    for (int x = lane; x < owner - (int)blockIdx.x * kSWarps; x += 32) {
+      D += cw[x];
+      V += cv[x];
     }
-    for (int o2 = owner * q; o2 < o; o2++) {
+    for (int o2 = owner * q + lane; o2 < o; o2 += 32) {
       D += lds(&B.wt[o2]);
       V += lds(&B.vd[o2]);
     }
-    shd[0] = D;
-    shd[1] = V;
-    shw = ((fl & 2) && z != pos) ? 1 : 0;
+    D = warp_sum64(D);
+    V = warp_sum64(V);
+    if (lane == 0) {
+      shd[0] = pre_w + D;
+      shd[1] = pre_v + V;
+      shw = ((fl & 2) && z != pos) ? 1 : 0;
+    }
   }
   __syncthreads();
   const long long D = shd[0], V = shd[1];
@@ -778,14 +791,13 @@ __device__ void fix_position(const DevInstance& I, const SpecBuf& B, const Round
   __syncwarp();
   if (mover) {
     claim_nets(I, B, vol, z, own, d, base, deg, lane, 32, par);
-    if (lane == 0) {
-      if (mt) atomicMin(&B.ctl[2 + par], z);
-      if (!had) B.mlist[atomicAdd(&B.mcnt[par], 1)] = o;   // a replaced mover is listed already
-    }
+    if (lane == 0 && mt) atomicMin(&B.ctl[2 + par], z);
   }
   if (lane == 0) {
     const int wv = mover ? __ldg(&I.w[v]) : 0;
     const int vn = mover ? vdd : 0;
+    if (had) B.mlist[lds(&B.midx[o])] = make_int4(o, wv, (own << 16) | d, 0);   // the replaced mover's entry
+    else if (mover) list_mover(B, par, o, wv, (own << 16) | d);
     B.wsum[gw] += wv - lds(&B.wt[o]);
     B.vsum[gw] += vn - lds(&B.vd[o]);
     B.dec[o] = (own << 16) | d;
@@ -800,7 +812,9 @@ __device__ void fix_position(const DevInstance& I, const SpecBuf& B, const Round
 
 static_assert(kMaxGridVerts <= kSWarps, "one warp decides each whole-grid vertex of a window");
 
-__global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, SpecBuf B, int passes) {
+// Two CTAs per SM: without the hint the compiler trades registers for a third
+// CTA and spills, which measured slower.
+__global__ void __launch_bounds__(kSThreads, 2) spec_ldg_kernel(DevInstance I, SpecBuf B, int passes) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ unsigned long long uscr[kSWarps];
   __shared__ int iscr[kSWarps];
@@ -811,6 +825,8 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
   __shared__ uint32_t s_gb[kMaxGridVerts];
   __shared__ int s_gdec[kMaxGridVerts], s_gspec[kMaxGridVerts], s_gslk[kMaxGridVerts];
   __shared__ long long s_pre_w, s_pre_v;
+  __shared__ unsigned long long uscr2[kSWarps];
+  __shared__ int s_cw[kSWarps], s_cv[kSWarps], s_mt, s_nm;   // this CTA's warps' sums, round words
   __shared__ int s_mw[kSWarps], s_mv[kSWarps];
   __shared__ int loc_b[kSWarps * 96];   // per-warp locate scratch
   const int metric = I.metric;
@@ -1052,14 +1068,14 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
           vdd = warp_max(a.vd);
         }
         __syncwarp();
+        const int wv = mover ? __ldg(&I.w[v]) : 0;
         if (mover) {
           claim_nets(I, B, vol, z, own, d, base, deg, lane, 32, par);
           if (lane == 0) {
             if (mt) atomicMin(&B.ctl[2 + par], z);
-            B.mlist[atomicAdd(&B.mcnt[par], 1)] = o;
+            list_mover(B, par, o, wv, (own << 16) | d);
           }
         }
-        const int wv = mover ? __ldg(&I.w[v]) : 0;
         if (lane == 0) {
           B.dec[o] = (own << 16) | d;   // own read now: part_vec changes in the commit phase
           B.flag[o] = (unsigned char)((mover ? 1 : 0) | (special ? 2 : 0) | (iso ? 8 : 0) | (good ? 16 : 0));
@@ -1199,7 +1215,7 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
             B.vd[os] = mover ? vdd : 0;
             if (mover) {
               if (mt) atomicMin(&B.ctl[2 + par], zs);
-              B.mlist[atomicAdd(&B.mcnt[par], 1)] = os;
+              list_mover(B, par, os, wv, (own_s << 16) | d);
             }
           }
           // the warp owning position zs carries its weight and volume change
@@ -1233,39 +1249,49 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
         // warps before this one (warps own consecutive position ranges).
         // Positions before zfix are known valid (an earlier pass of the window).
         const unsigned long long tV = gtimer();
+        long long Dw, Vw;
         {
+          // one round of independent loads: the earlier warps' sums, this CTA's
+          // warps' sums, the round words
           long long pw = 0, pv = 0;
           const int lim = blockIdx.x * kSWarps;
           for (int g = threadIdx.x; g < lim; g += blockDim.x) {
             pw += lds(&B.wsum[g]);
             pv += lds(&B.vsum[g]);
           }
+          if (threadIdx.x < kSWarps) {
+            s_cw[threadIdx.x] = lds(&B.wsum[lim + threadIdx.x]);
+            s_cv[threadIdx.x] = lds(&B.vsum[lim + threadIdx.x]);
+          }
+          if (threadIdx.x == 0) {
+            s_mt = lds(&B.ctl[2 + par]);
+            s_nm = lds(&B.mcnt[par]);
+          }
           pw = warp_sum64(pw);
           pv = warp_sum64(pv);
-          if (lane == 0) uscr[wib] = (unsigned long long)pw;
+          if (lane == 0) {
+            uscr[wib] = (unsigned long long)pw;
+            uscr2[wib] = (unsigned long long)pv;
+          }
           __syncthreads();
+          long long a = 0, b = 0;
+          for (int x = 0; x < kSWarps; x++) {
+            a += (long long)uscr[x];
+            b += (long long)uscr2[x];
+          }
           if (threadIdx.x == 0) {
-            long long a = 0;
-            for (int x = 0; x < kSWarps; x++) a += (long long)uscr[x];
             s_pre_w = a;
+            s_pre_v = b;
           }
-          __syncthreads();
-          if (lane == 0) uscr[wib] = (unsigned long long)pv;
-          __syncthreads();
-          if (threadIdx.x == 0) {
-            long long a = 0;
-            for (int x = 0; x < kSWarps; x++) a += (long long)uscr[x];
-            s_pre_v = a;
+          Dw = a;
+          Vw = b;
+          for (int x = 0; x < wib; x++) {
+            Dw += s_cw[x];
+            Vw += s_cv[x];
           }
-          __syncthreads();
         }
-        long long Dw = s_pre_w, Vw = s_pre_v;
-        for (int x = 0; x < wib; x++) {
-          Dw += lds(&B.wsum[blockIdx.x * kSWarps + x]);
-          Vw += lds(&B.vsum[blockIdx.x * kSWarps + x]);
-        }
-        const int mtpos = lds(&B.ctl[2 + par]);
-        const int nm = lds(&B.mcnt[par]);
+        const int mtpos = s_mt;
+        const int nm = s_nm;
         const unsigned long long tV1 = gtimer();
         // part-size changes of the window's movers before this CTA's first position
         // (phase-A scratch gains_b is free now)
@@ -1274,40 +1300,40 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
         for (int p = threadIdx.x; p < K; p += blockDim.x) dsz_cta[p] = 0;
         __syncthreads();
         for (int i = threadIdx.x; i < nm; i += blockDim.x) {
-          const int o2 = lds(&B.mlist[i]);
-          if (o2 >= cta_o0) continue;
-          const int w = lds(&B.wt[o2]);
-          if (w == 0) continue;
-          const int pk = lds(&B.dec[o2]);
-          atomicAdd(&dsz_cta[pk & 0xffff], w);
-          atomicAdd(&dsz_cta[pk >> 16], -w);
+          const int4 m = lds(&B.mlist[i]);
+          if (m.x >= cta_o0 || m.y == 0) continue;
+          atomicAdd(&dsz_cta[m.z & 0xffff], m.y);
+          atomicAdd(&dsz_cta[m.z >> 16], -m.y);
         }
         __syncthreads();
+        const bool ov = lds(&B.ctab_over[par]) != 0;
         for (int z = z0; z < z1; z++) {
           const int o = z - pos;
-          if (z < zfix) {
-            Dw += lds(&B.wt[o]);
-            Vw += lds(&B.vd[o]);
-            continue;
-          }
+          // the position's words in one round of independent loads
+          const int wz = lds(&B.wt[o]), vz = lds(&B.vd[o]);
           const int fl = lds(&B.flag[o]);
-          if (fl & 4) {                    // medium vertex: validated by the CTA below
-            Dw += lds(&B.wt[o]);
-            Vw += lds(&B.vd[o]);
+          const int slk = lds(&B.slack[o]), vslk = lds(&B.vslack[o]);
+          int pk = lds(&B.dec[o]);
+          const int v = __ldg(&I.order[z]);
+          if (z < zfix || (fl & 4)) {      // valid already / medium vertex, validated by the CTA below
+            Dw += wz;
+            Vw += vz;
             continue;
           }
+          const uint32_t base = __ldg(&I.vptr[v]);
+          const int deg = (int)(__ldg(&I.vptr[v + 1]) - base);
+          const int own = pk >> 16;
           int why = ((fl & 2) && z != pos) ? 1 : 0;
-          if (!why && Dw > max(lds(&B.slack[o]), 0)) {
+          if (!why && Dw > max(slk, 0)) {
             // beyond the slack: decide again with the exact sizes at this position
-            const int pk = lds(&B.dec[o]);
-            const int own = pk >> 16;
             const int d2 = ldg_recheck(I, R, B, o, own, metric, cnt, dsz_cta, cta_o0);
             if (d2 != (pk & 0xffff)) {
               if (fl & 8) {
                 // isolated vertex: take the exact decision (no weight, no nets, so
                 // no later position sees the difference)
+                pk = (own << 16) | d2;
                 if (lane == 0) {
-                  B.dec[o] = (own << 16) | d2;
+                  B.dec[o] = pk;
                   B.flag[o] = (unsigned char)((fl & ~1) | ((fl & 16) && d2 != own ? 1 : 0));
                 }
               } else {
@@ -1316,32 +1342,21 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
               }
             }
           }
+          // the max-volume parts enter only the accept test of a vertex whose
+          // decision leaves its part (MSRV/partition.cpp:308-400,
+          // MGV/partition.cpp:292-362), and they change only with a move
+          if (!why) why = Vw > max(vslk, 0) ? 3 : (mtpos < z && (pk & 0xffff) != own) ? 4 : 0;
           if (!why) {
-            // the max-volume parts enter only the accept test of a vertex whose
-            // decision leaves its part (MSRV/partition.cpp:308-400,
-            // MGV/partition.cpp:292-362), and they change only with a move
-            const int pk = lds(&B.dec[o]);
-            why = Vw > max(lds(&B.vslack[o]), 0) ? 3 : (mtpos < z && (pk & 0xffff) != (pk >> 16)) ? 4 : 0;
-          }
-          bool bad = why != 0;
-          if (!bad) {
-            const int v = __ldg(&I.order[z]);
-            const int own = lds(&B.dec[o]) >> 16;
-            const bool mover = fl & 1;
-            const uint32_t base = __ldg(&I.vptr[v]);
-            const int deg = (int)(__ldg(&I.vptr[v + 1]) - base);
-            const int dz = lds(&B.dec[o]) & 0xffff;
-            const int c = conflicts(I, B, vol, z, own, dz != own, mover, base, deg, lane, 32, lds(&B.ctab_over[par]) != 0);
+            const int c = conflicts(I, B, vol, z, own, (pk & 0xffff) != own, fl & 1, base, deg, lane, 32, ov);
             const int c5 = __any_sync(kAll, c == 5), c6 = __any_sync(kAll, c == 6), c7 = __any_sync(kAll, c == 7);
             why = c5 ? 5 : c6 ? 6 : c7 ? 7 : 0;
-            bad = why != 0;
           }
-          if (bad) {
+          if (why) {
             if (lane == 0) atomicMin(cut_w, (z << 3) | why);   // position, then cut reason
             break;
           }
-          Dw += lds(&B.wt[o]);
-          Vw += lds(&B.vd[o]);
+          Dw += wz;
+          Vw += vz;
         }
         __syncthreads();
         const unsigned long long tV2 = gtimer();
@@ -1349,7 +1364,8 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
           const int z = __ldg(&B.mid_pos[mi]);
           if (z >= cz1) break;
           if (z < zfix) continue;
-          cta_validate_ldg(I, B, R, metric, z, pos, q, par, mtpos, s_pre_w, s_pre_v, cnt_b, dsz_cta, cta_o0, true, cut_w);
+          cta_validate_ldg(I, B, R, metric, z, pos, q, par, mtpos, s_pre_w, s_pre_v, s_cw, s_cv, cnt_b, dsz_cta,
+                           cta_o0, true, cut_w);
         }
         for (int j = 0; j < ns; j++) {
           // a whole-grid vertex: its nets checked by every thread, the rest by the
@@ -1362,8 +1378,8 @@ __global__ void __launch_bounds__(kSThreads) spec_ldg_kernel(DevInstance I, Spec
                                   gtid, gthreads, lds(&B.ctab_over[par]) != 0);
           if (c) atomicMin(cut_w, (zs << 3) | c);
           if (zs >= cz0 && zs < cz1)
-            cta_validate_ldg(I, B, R, metric, zs, pos, q, par, mtpos, s_pre_w, s_pre_v, cnt_b, dsz_cta, cta_o0, false,
-                             cut_w);
+            cta_validate_ldg(I, B, R, metric, zs, pos, q, par, mtpos, s_pre_w, s_pre_v, s_cw, s_cv, cnt_b, dsz_cta,
+                             cta_o0, false, cut_w);
         }
         __syncthreads();
         if (threadIdx.x == 0) {
