@@ -44,6 +44,8 @@ static bool spec_supported(int metric, int K, int max_smem) {
 // (TV, MSM) a higher one; bounds from a sweep on the 4M-vertex Zipf workload.
 // TM and MSM use the same classes in id order.
 constexpr int kLightWork = 2048;
+constexpr int kCnLightPins = 128;   // CN: nets with more pins are evaluated by one CTA,
+constexpr int kCnGridPins = 1024;   //     with more than this by the whole grid
 int default_super_work(int metric) {
   switch (metric) {
     case FP_METRIC_MSV: return 16384;
@@ -58,6 +60,7 @@ int default_super_work(int metric) {
 int default_grid_verts(int metric) {
   switch (metric) {
     case FP_METRIC_TV:
+    case FP_METRIC_CN:
     case FP_METRIC_MSM: return kMaxGridVerts;
     case FP_METRIC_TM:
     case FP_METRIC_MSRV: return 4;
@@ -321,6 +324,30 @@ static int classify(fp_instance* in, long long light_work, long long super_work)
   std::vector<unsigned char> cls(g.nov, 0);
   in->heavy_pos.clear();
   in->mid_pos.clear();
+  if (pb.metric == FP_METRIC_CN) {
+    // CN walks the nets in id order (CN/partition.cpp:245); a net with more
+    // than light_work pins is evaluated by a whole CTA, with more than
+    // super_work by the whole grid
+    const long long grid_pins = std::max(light_work, super_work);
+    for (int e = 0; e < g.noe; e++) {
+      const long long n = g.nptr[e + 1] - g.nptr[e];
+      if (n > grid_pins) in->heavy_pos.push_back(e);
+      else if (n > light_work) in->mid_pos.push_back(e);
+    }
+    in->sb.cn_big = (int)std::min<long long>(light_work, 0x7fffffff);
+    in->sb.cn_grid = (int)std::min<long long>(grid_pins, 0x7fffffff);
+    in->sb.nheavy = (int)in->heavy_pos.size();
+    in->sb.nmid = (int)in->mid_pos.size();
+    cudaError_t e = cudaSuccess;
+    if (in->sb.nmid)
+      e = cudaMemcpyAsync(in->mid_pos_d, in->mid_pos.data(), sizeof(int) * in->sb.nmid, cudaMemcpyHostToDevice,
+                          in->ctx->stream);
+    if (e == cudaSuccess && in->sb.nheavy)
+      e = cudaMemcpyAsync(in->heavy_pos_d, in->heavy_pos.data(), sizeof(int) * in->sb.nheavy,
+                          cudaMemcpyHostToDevice, in->ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(in->ctx->stream);
+    return cuda_status(e);
+  }
   // TM and MSM walk the vertices in id order (TM/partition.cpp:300), the others
   // in the visiting order.
   const bool by_id = pb.metric == FP_METRIC_TM || pb.metric == FP_METRIC_MSM;
@@ -425,7 +452,8 @@ int fp_instance_create(fp_ctx* ctx, const fp_hypergraph* h, int32_t K, int32_t m
       (rc = dalloc(in, &in->sb.ctab_over, 2)) || (rc = dalloc(in, &in->sb.dfix, kSpecWindow)) ||
       (rc = dalloc(in, &in->sb.rec_slot2, vfix ? g.pins : 1)) ||
       (rc = dalloc(in, &in->sb.cn_moved, cn ? g.pins : 1)) || (rc = dalloc(in, &in->sb.cn_kcnt, cn ? g.noe : 1)) ||
-      (rc = dalloc(in, &in->sb.cn_nets, cn ? g.noe : 1)) || (rc = dalloc(in, &in->sb.cn_cnt, 4)) || (rc = dalloc(in, &in->vclass_d, g.nov)) ||
+      (rc = dalloc(in, &in->sb.cn_nets, cn ? g.noe : 1)) || (rc = dalloc(in, &in->sb.cn_cnt, 4)) ||
+      (rc = dalloc(in, &in->sb.cn_wit, cn ? g.nov : 1)) || (rc = dalloc(in, &in->vclass_d, g.nov)) ||
       (rc = dalloc(in, &in->sb.cand, (size_t)kSpecWindow * K)) || (rc = dalloc(in, &in->sb.ncand, kSpecWindow)) ||
       (rc = dalloc(in, &in->sb.mlist, kSpecWindow)) || (rc = dalloc(in, &in->sb.midx, kSpecWindow)) ||
       (rc = dalloc(in, &in->sb.mcnt, 2)) ||
@@ -436,8 +464,8 @@ int fp_instance_create(fp_ctx* ctx, const fp_hypergraph* h, int32_t K, int32_t m
       (rc = dalloc(in, &in->sb.hgain, 2 * kMaxGridVerts * K)) ||
       (rc = dalloc(in, &in->sb.hloss, 2 * kMaxGridVerts * K)) ||
       (rc = dalloc(in, &in->sb.hadelta, 2 * kMaxGridVerts * K)) ||
-      (rc = dalloc(in, &in->sb.hmisc, 16 * kMaxGridVerts)) || (rc = dalloc(in, &in->sb.mlast, K)) || (rc = dalloc(in, &in->heavy_pos_d, g.nov)) ||
-      (rc = dalloc(in, &in->mid_pos_d, g.nov)) ||
+      (rc = dalloc(in, &in->sb.hmisc, 16 * kMaxGridVerts)) || (rc = dalloc(in, &in->sb.mlast, K)) || (rc = dalloc(in, &in->heavy_pos_d, std::max(g.nov, g.noe))) ||
+      (rc = dalloc(in, &in->mid_pos_d, std::max(g.nov, g.noe))) ||
       (rc = dalloc(in, &in->metric_out, 8))) {
     fp_instance_destroy(in);
     return rc;
@@ -462,9 +490,11 @@ int fp_instance_create(fp_ctx* ctx, const fp_hypergraph* h, int32_t K, int32_t m
   {
     cudaStream_t s0 = ctx->stream;
     e = clear_spec_scratch(in->sb, g.noe, K, s0);
+    if (e == cudaSuccess && cn) e = cudaMemsetAsync(in->sb.cn_wit, 0xff, sizeof(int) * g.nov, s0);   // no witnesses
     if (e == cudaSuccess) e = cudaStreamSynchronize(s0);
     if (e != cudaSuccess) { fp_instance_destroy(in); return cuda_status(e); }
-    rc = classify(in, kLightWork, default_super_work(metric));
+    rc = classify(in, metric == FP_METRIC_CN ? kCnLightPins : kLightWork,
+                  metric == FP_METRIC_CN ? kCnGridPins : default_super_work(metric));
     if (rc) { fp_instance_destroy(in); return rc; }
   }
   if (cudaMallocHost(&in->h_moves, sizeof(long long) * kMaxPasses) != cudaSuccess ||

@@ -85,6 +85,7 @@ struct SpecBuf {
   int* cn_kcnt;          // [noe] CN: pins of the round's moves per net (zero between rounds)
   int2* cn_nets;         // [noe] CN: (net, packed old/new part) of the nets those moves touch
   int* cn_cnt;           // [4] CN: counts of cn_moved [0,1] and cn_nets [2,3] by round parity
+  int* cn_wit;           // [nov] CN: a net of the vertex found uncut before (-1: none)
   int* claim_m;          // [noe] first mover position changing the net's part set
   int* claim_c;          // [noe] first mover position changing only counts
   uint32_t* mask_c;      // [noe] parts (mod 32) whose counts those movers change
@@ -98,7 +99,9 @@ struct SpecBuf {
   const int* heavy_pos;  // positions (visiting order, ascending) of vertices that get a
   int nheavy;            //     whole-grid round of their own
   const int* mid_pos;    // positions (ascending) of medium vertices, evaluated by one CTA
-  int nmid;
+  int nmid;              //     (CN: nets with more than cn_big pins, up to cn_grid)
+  int cn_big, cn_grid;   // CN: nets with more than cn_grid pins are evaluated by the grid
+                         //     (heavy_pos)
   int* hcnt;             // [2 * kMaxGridVerts * K] whole-grid vertex tallies, by round parity
   unsigned long long* hfirst;  //     and slot (the TM / MSM engine uses slot 0)
   int* hgain;            // [2 * kMaxGridVerts * K]

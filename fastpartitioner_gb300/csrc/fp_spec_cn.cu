@@ -35,17 +35,23 @@ __device__ __forceinline__ bool claim_before(const SpecBuf& B, int round, int x,
   return (int)(c >> 32) == round && (int)(0xffffffffu - (unsigned)(c & 0xffffffffu)) < pos;
 }
 
-// Walk of the (pin, net) pairs of net e's pins on part oldp, 32 pins at a
-// time, the pairs flattened across the warp with 4 loads in flight per lane.
+// Walk of the (pin, net) pairs of net e's pins [pb, pe) on part oldp, 32 pins
+// at a time, the pairs flattened across the warp with 4 loads in flight per
+// lane.
 //   kMode 0: returns a net of those pins that is not cut (-1: none);
 //   kMode 1: claims every such net for position e and records the pins to move
 //            (window offset o, round parity par); returns -1;
 //   kMode 2: returns 1 if an acting net before e claimed one of them, else -1.
+// Modes 0 and 2 stop early when *stop (shared by the warps splitting a net's
+// pins) is set.
+// gstop: the same in global memory (the grid's warps splitting a net).
 template <int kMode>
-__device__ int cn_walk(const DevInstance& I, const SpecBuf& B, int e, int oldp, int round, int o, int par) {
+__device__ int cn_walk_range(const DevInstance& I, const SpecBuf& B, int e, int pb, int pe, int oldp, int round,
+                             int o, int par, const volatile int* stop, const int* gstop = nullptr) {
   const int lane = threadIdx.x & 31;
-  const int pb = (int)__ldg(&I.nptr[e]), pe = (int)__ldg(&I.nptr[e + 1]);
   for (int b0 = pb; b0 < pe; b0 += 32) {
+    if (kMode != 1 && stop && __shfl_sync(kAll, *stop, 0)) return -1;   // warp-uniform: lane 0's read
+    if (kMode != 1 && gstop && __shfl_sync(kAll, lds(gstop), 0)) return -1;
     const int k = b0 + lane;
     int u = -1, d = 0;
     uint32_t ub = 0;
@@ -57,6 +63,15 @@ __device__ int cn_walk(const DevInstance& I, const SpecBuf& B, int e, int oldp, 
       } else {
         u = -1;
       }
+    }
+    if (kMode == 0) {
+      // a pin's cached witness: a net of the pin found uncut before; still
+      // uncut, it ends the search without walking the pin's nets (hub pins
+      // lie on millions of nets)
+      const int w = u >= 0 ? lds(&B.cn_wit[u]) : -1;
+      const int hit = (w >= 0 && lds(&I.ep_len[w]) == 1) ? w : -1;
+      const unsigned m = __ballot_sync(kAll, hit >= 0);
+      if (m) return __shfl_sync(kAll, hit, __ffs(m) - 1);
     }
     if (kMode == 1 && u >= 0) B.cn_moved[atomicAdd(&B.cn_cnt[par], 1)] = make_int2(u, o);
     int incl = d;
@@ -84,12 +99,27 @@ __device__ int cn_walk(const DevInstance& I, const SpecBuf& B, int e, int oldp, 
         xs[q] = f < total ? (int)__ldg(&I.vnets[bl + (uint32_t)(f - (il - dl))]) : -1;
       }
       if (kMode == 0) {
-        int hit = -1;
+        int hit = -1, hq = 0;
 #pragma unroll
         for (int q = 0; q < kU; q++)
-          if (xs[q] >= 0 && hit < 0 && lds(&I.ep_len[xs[q]]) == 1) hit = xs[q];
+          if (xs[q] >= 0 && hit < 0 && lds(&I.ep_len[xs[q]]) == 1) { hit = xs[q]; hq = q; }
         const unsigned m = __ballot_sync(kAll, hit >= 0);
-        if (m) return __shfl_sync(kAll, hit, __ffs(m) - 1);
+        if (m) {
+          const int src = __ffs(m) - 1;
+          const int x = __shfl_sync(kAll, hit, src);
+          // the pin of that pair keeps it as its witness
+          const int f = f0 + __shfl_sync(kAll, hq, src) * 32 + src;
+          int lo = 0, hi = 31;
+#pragma unroll
+          for (int it = 0; it < 5; it++) {
+            const int mid = (lo + hi) >> 1;
+            const int val = __shfl_sync(kAll, incl, mid);
+            if (f < val) hi = mid; else lo = mid + 1;
+          }
+          const int uw = __shfl_sync(kAll, u, lo);
+          if (lane == 0 && uw >= 0) B.cn_wit[uw] = x;
+          return x;
+        }
       } else if (kMode == 1) {
 #pragma unroll
         for (int q = 0; q < kU; q++)
@@ -104,6 +134,106 @@ __device__ int cn_walk(const DevInstance& I, const SpecBuf& B, int e, int oldp, 
     }
   }
   return -1;
+}
+
+template <int kMode>
+__device__ __forceinline__ int cn_walk(const DevInstance& I, const SpecBuf& B, int e, int oldp, int round, int o,
+                                       int par) {
+  return cn_walk_range<kMode>(I, B, e, (int)__ldg(&I.nptr[e]), (int)__ldg(&I.nptr[e + 1]), oldp, round, o, par,
+                              nullptr);
+}
+
+// Warp gw's contiguous share (of nw warps) of net e's pins.
+__device__ __forceinline__ void cn_grid_share(const DevInstance& I, int e, int gw, int nw, int* pb, int* pe) {
+  const int b = (int)__ldg(&I.nptr[e]), n = (int)__ldg(&I.nptr[e + 1]) - b;
+  const int g = (n + nw - 1) / nw;
+  *pb = b + min(gw * g, n);
+  *pe = b + min(gw * g + g, n);
+}
+
+// Two-part test of net e (CN/partition.cpp:262-270): old (smaller side) and
+// new parts, false if the net does not span exactly two parts.
+__device__ __forceinline__ bool cn_two(const DevInstance& I, int e, int* oldp, int* newp) {
+  if (lds(&I.ep_len[e]) != 2) return false;
+  const int s = (int)__ldg(&I.nptr[e]);
+  const int p1 = lds(&I.ep_part[s]), c1 = lds(&I.ep_cnt[s]);
+  const int p2 = lds(&I.ep_part[s + 1]), c2 = lds(&I.ep_cnt[s + 1]);
+  *oldp = c1 < c2 ? p1 : p2;
+  *newp = c1 < c2 ? p2 : p1;
+  return true;
+}
+
+// Warp wib's contiguous share of net e's pins.
+__device__ __forceinline__ void cn_pin_share(const DevInstance& I, int e, int* pb, int* pe) {
+  const int b = (int)__ldg(&I.nptr[e]), n = (int)__ldg(&I.nptr[e + 1]) - b;
+  const int g = (n + kSWarps - 1) / kSWarps, w = (int)(threadIdx.x >> 5);
+  *pb = b + min(w * g, n);
+  *pe = b + min(w * g + g, n);
+}
+
+// Evaluation of a net with many pins by the whole CTA: the warps split its
+// pins (cn_eval's rules), then the claims of an acting net.
+__device__ void cn_eval_cta(const DevInstance& I, const SpecBuf& B, int e, int o, int round, int par) {
+  __shared__ int sh_two, sh_old, sh_new, sh_unc;
+  __shared__ volatile int sh_stop;
+  const int lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    sh_two = 0;
+    sh_unc = -1;
+    sh_stop = 0;
+    if (lds(&I.ep_len[e]) == 2) {
+      const int s = (int)__ldg(&I.nptr[e]);
+      const int p1 = lds(&I.ep_part[s]), c1 = lds(&I.ep_cnt[s]);
+      const int p2 = lds(&I.ep_part[s + 1]), c2 = lds(&I.ep_cnt[s + 1]);
+      sh_two = 1;
+      sh_old = c1 < c2 ? p1 : p2;
+      sh_new = c1 < c2 ? p2 : p1;
+    }
+  }
+  __syncthreads();
+  int act = 0;
+  const int oldp = sh_two ? sh_old : 0, newp = sh_two ? sh_new : 0;
+  if (sh_two) {
+    int pb, pe;
+    cn_pin_share(I, e, &pb, &pe);
+    const int hit = cn_walk_range<0>(I, B, e, pb, pe, oldp, 0, 0, 0, &sh_stop);
+    if (hit >= 0 && lane == 0) {
+      atomicCAS(&sh_unc, -1, hit);   // any uncut net is a witness
+      sh_stop = 1;
+    }
+    __syncthreads();
+    act = sh_unc < 0;
+    if (act) cn_walk_range<1>(I, B, e, pb, pe, oldp, round, o, par, nullptr);
+  }
+  if (threadIdx.x == 0) {
+    B.dec[o] = (oldp << 16) | newp;
+    B.flag[o] = (unsigned char)act;
+    B.slack[o] = sh_unc;   // the uncut net that blocks the move (-1: none)
+  }
+  __syncthreads();
+}
+
+// Validation of a net with many pins by the whole CTA (the warp loop's rules);
+// a conflict lowers the cut word.
+__device__ void cn_validate_cta(const DevInstance& I, const SpecBuf& B, int e, int o, int round, int* cut) {
+  __shared__ volatile int sh_conf;
+  const int lane = threadIdx.x & 31;
+  const int act = lds(&B.flag[o]);
+  if (threadIdx.x == 0) {
+    int c = claim_before(B, round, e, e) ? 1 : 0;
+    const int unc = lds(&B.slack[o]);
+    if (unc >= 0 && claim_before(B, round, unc, e)) c = 1;
+    sh_conf = c;
+  }
+  __syncthreads();
+  if (act && !sh_conf) {
+    int pb, pe;
+    cn_pin_share(I, e, &pb, &pe);
+    if (cn_walk_range<2>(I, B, e, pb, pe, lds(&B.dec[o]) >> 16, round, 0, 0, &sh_conf) > 0 && lane == 0) sh_conf = 1;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && sh_conf) atomicMin(cut, (e << 3) | 5);
+  __syncthreads();
 }
 
 // Evaluation of net e (one warp).  Returns 0 (no move), 1 (acting), and the
@@ -201,18 +331,48 @@ __device__ void cn_apply_net(const DevInstance& I, int x, int oldp, int newp, in
   __syncwarp();
 }
 
-__global__ void __launch_bounds__(kSThreads) spec_cn_kernel(DevInstance I, SpecBuf B, int passes) {
+// Three CTAs per SM: without the hint the compiler spills to fit more.
+__global__ void __launch_bounds__(kSThreads, 3) spec_cn_kernel(DevInstance I, SpecBuf B, int passes) {
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int gw = blockIdx.x * kSWarps + wib;
   const int nwarps = gridDim.x * kSWarps;
+  // the window's grid-evaluated nets: id, two-part, old and new part
+  __shared__ int s_ge[kMaxGridVerts], s_gt[kMaxGridVerts], s_go[kMaxGridVerts], s_gn[kMaxGridVerts];
   unsigned long long tA = gtimer();
   int round = 1;   // claims of round 0 (the cleared array) never match
+  int heavy_round = 0;
   for (int it = 0; it < passes; it++) {
     int pos = 0;
     int W = min(nwarps * 4, B.wmax);
+    int hidx = 0;
     while (pos < I.noe) {
       const int par = round & 1;
-      const int end_w = min(pos + W, I.noe);
+      // a window holds up to gmax nets evaluated by the grid and ends before the next
+      while (hidx < B.nheavy && __ldg(&B.heavy_pos[hidx]) < pos) hidx++;
+      int end_w = min(pos + W, I.noe);
+      if (hidx + B.gmax < B.nheavy) end_w = min(end_w, (int)__ldg(&B.heavy_pos[hidx + B.gmax]));
+      int ns = 0;
+      while (ns < B.gmax && hidx + ns < B.nheavy && __ldg(&B.heavy_pos[hidx + ns]) < end_w) ns++;
+      const int hp = heavy_round & 1;
+      // slot j of this parity in hmisc: [0] uncut witness + 1 (0: none), [1] conflict
+      auto hm = [&](int j) { return B.hmisc + (hp * kMaxGridVerts + j) * 8; };
+      if ((int)threadIdx.x < ns) {
+        const int e = __ldg(&B.heavy_pos[hidx + threadIdx.x]);
+        int op = 0, np = 0;
+        s_ge[threadIdx.x] = e;
+        s_gt[threadIdx.x] = cn_two(I, e, &op, &np) ? 1 : 0;
+        s_go[threadIdx.x] = op;
+        s_gn[threadIdx.x] = np;
+      }
+      __syncthreads();
+      // ---- A0: the grid's warps split the pins of each grid net (uncut search)
+      for (int j = 0; j < ns; j++) {
+        if (!s_gt[j]) continue;
+        int pb, pe;
+        cn_grid_share(I, s_ge[j], gw, nwarps, &pb, &pe);
+        const int hit = cn_walk_range<0>(I, B, s_ge[j], pb, pe, s_go[j], 0, 0, 0, nullptr, hm(j));
+        if (hit >= 0 && lane == 0) atomicCAS(hm(j), 0, hit + 1);
+      }
       const int span = end_w - pos;
       const int q = (span + nwarps - 1) / nwarps;
       const int z0 = min(pos + gw * q, end_w);
@@ -220,6 +380,7 @@ __global__ void __launch_bounds__(kSThreads) spec_cn_kernel(DevInstance I, SpecB
       // ---- A: evaluate; acting nets claim the nets of the pins they move
       for (int e = z0; e < z1; e++) {
         const int o = e - pos;
+        if ((int)(__ldg(&I.nptr[e + 1]) - __ldg(&I.nptr[e])) > B.cn_big) continue;   // the CTA evaluates it below
         int oldp = 0, newp = 0, unc = -1;
         const int act = cn_eval(I, B, e, &oldp, &newp, &unc);
         if (act) cn_walk<1>(I, B, e, oldp, round, o, par);
@@ -230,7 +391,34 @@ __global__ void __launch_bounds__(kSThreads) spec_cn_kernel(DevInstance I, SpecB
         }
         __syncwarp();
       }
+      // nets with many pins of this CTA's positions: the whole CTA each
+      const int cz0 = min(pos + blockIdx.x * kSWarps * q, end_w);
+      const int cz1 = min(cz0 + kSWarps * q, end_w);
+      for (int mi = lower_bound_pos(B.mid_pos, B.nmid, cz0); mi < B.nmid; mi++) {
+        const int e = __ldg(&B.mid_pos[mi]);
+        if (e >= cz1) break;
+        cn_eval_cta(I, B, e, e - pos, round, par);
+      }
       if (!grid_barrier(B.bar, I.status)) return;
+      if (ns) {
+        // ---- A1: an acting grid net's claims and pins, split across the grid
+        for (int j = 0; j < ns; j++) {
+          const int e = s_ge[j], o = e - pos;
+          const int unc = lds(hm(j)) - 1;
+          const int act = s_gt[j] && unc < 0;
+          if (act) {
+            int pb, pe;
+            cn_grid_share(I, e, gw, nwarps, &pb, &pe);
+            cn_walk_range<1>(I, B, e, pb, pe, s_go[j], round, o, par, nullptr);
+          }
+          if (blockIdx.x == 0 && threadIdx.x == 0) {
+            B.dec[o] = s_gt[j] ? (s_go[j] << 16) | s_gn[j] : 0;
+            B.flag[o] = (unsigned char)act;
+            B.slack[o] = s_gt[j] ? unc : -1;
+          }
+        }
+        if (!grid_barrier(B.bar, I.status)) return;
+      }
       if (blockIdx.x == 0 && threadIdx.x == 0) {
         const unsigned long long tE = gtimer();
         B.stats[16] += tE - tA;
@@ -239,6 +427,7 @@ __global__ void __launch_bounds__(kSThreads) spec_cn_kernel(DevInstance I, SpecB
       // ---- B: validate against earlier acting nets' claims
       for (int e = z0; e < z1; e++) {
         const int o = e - pos;
+        if ((int)(__ldg(&I.nptr[e + 1]) - __ldg(&I.nptr[e])) > B.cn_big) continue;   // validated by the CTA below
         const int act = lds(&B.flag[o]);
         bool conf = false;
         if (lane == 0) {
@@ -253,6 +442,26 @@ __global__ void __launch_bounds__(kSThreads) spec_cn_kernel(DevInstance I, SpecB
           if (lane == 0) atomicMin(&B.ctl[par], (e << 3) | 5);
           break;
         }
+      }
+      __syncthreads();
+      for (int mi = lower_bound_pos(B.mid_pos, B.nmid, cz0); mi < B.nmid; mi++) {
+        const int e = __ldg(&B.mid_pos[mi]);
+        if (e >= cz1) break;
+        cn_validate_cta(I, B, e, e - pos, round, &B.ctl[par]);
+      }
+      for (int j = 0; j < ns; j++) {
+        // a grid net: its own list and witness by every warp (cheap), its
+        // moving pins' nets split across the grid
+        const int e = s_ge[j], o = e - pos;
+        const int unc = lds(&B.slack[o]);
+        bool conf = claim_before(B, round, e, e) || (unc >= 0 && claim_before(B, round, unc, e));
+        if (!conf && lds(&B.flag[o])) {
+          int pb, pe;
+          cn_grid_share(I, e, gw, nwarps, &pb, &pe);
+          conf = cn_walk_range<2>(I, B, e, pb, pe, s_go[j], round, 0, 0, nullptr, hm(j) + 1) > 0;
+          if (conf && lane == 0) atomicExch(hm(j) + 1, 1);
+        }
+        if (conf && lane == 0) atomicMin(&B.ctl[par], (e << 3) | 5);
       }
       if (!grid_barrier(B.bar, I.status)) return;
       const int cutw = lds(&B.ctl[par]);
@@ -304,6 +513,12 @@ __global__ void __launch_bounds__(kSThreads) spec_cn_kernel(DevInstance I, SpecB
         B.ctl[par ^ 1] = kNone;
         B.cn_cnt[par ^ 1] = 0;
         B.cn_cnt[2 + (par ^ 1)] = 0;
+      }
+      if (ns) {
+        // the other parity's grid-net words, for the next window with grid nets
+        if (blockIdx.x == 0 && threadIdx.x < 8 * kMaxGridVerts) B.hmisc[(hp ^ 1) * 8 * kMaxGridVerts + threadIdx.x] = 0;
+        if (blockIdx.x == 0 && threadIdx.x == 0) B.stats[1] += ns;
+        heavy_round++;
       }
       if (cut == end_w) {
         if (end_w == pos + W) W = min(2 * W, B.wmax);

@@ -126,11 +126,13 @@ int fp_set_engine(fp_instance* inst, int32_t engine);
 /* All six metrics of the current device state, in FP_OUT_* order
  * (shared/metric.cpp: TV_Refined, CN, TM_scratch, MGM_scratch, MGV_Scratch,
  * MGAV_Scratch). */
-/* Tuning of the speculative engine for TV / MSV / MSRV / TM / MSM (no effect on
- * results): a vertex whose work -- the sum over its nets of min(net size, K) --
+/* Tuning of the speculative engine (no effect on results).  TV / MSV / MSRV /
+ * TM / MSM: a vertex whose work -- the sum over its nets of min(net size, K) --
  * is at most light_work is evaluated by one warp, at most super_work by one
- * CTA, above it in a whole-grid round.  Defaults: 2048 and 262144 (MSV 16384,
- * MSRV and TM 65536). */
+ * CTA, above it by the whole grid.  Defaults: 2048 and 262144 (MSV 16384,
+ * MSRV and TM 32768).  CN: a net with more than light_work pins is evaluated
+ * by one CTA, with more than super_work pins by the whole grid (defaults 128
+ * and 1024). */
 int fp_set_classes(fp_instance* inst, int64_t light_work, int64_t super_work);
 int fp_metrics(fp_instance* inst, int64_t out[6]);
 

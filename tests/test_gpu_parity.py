@@ -260,11 +260,12 @@ def test_gpu_set_state_round_trip(fp, orc, gpu_engine, metric):
             c.set_state(bad["part_vec"], bad["ep_starts"], bad["ep_ends"], bad["ep_parts"], bad["ep_cnt"])
 
 
-@pytest.mark.parametrize("metric", ["TV", "MSV", "MSRV", "TM", "MSM"])
+@pytest.mark.parametrize("metric", ["TV", "MSV", "MSRV", "TM", "MSM", "CN"])
 @pytest.mark.parametrize("bounds", [(16, 64), (64, 1024)])
 def test_gpu_vertex_classes_do_not_change_results(fp, orc, gpu_engine, metric, bounds):
-    """Tiny class bounds put many vertices in CTA evaluation and in whole-grid
-    evaluation inside the windows; the results still equal the oracle."""
+    """Tiny class bounds put many vertices (CN: nets, by pins) in CTA evaluation
+    and in whole-grid evaluation inside the windows; the results still equal
+    the oracle."""
     hg = fp.generate(fp.GenSpec.zipf(8000, 8000, 2.1, 2, 1500, beta=1.5, weight_rule=1, seed=71))
     K, passes = 32, 3
     o = orc.run_oracle(hg, K, metric, passes)
