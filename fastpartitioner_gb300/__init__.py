@@ -394,8 +394,9 @@ class Instance:
         return b
 
     def set_classes(self, light_work: int, super_work: int) -> None:
-        """Work bounds of the warp / CTA / whole-grid vertex classes (TV, MSV,
-        MSRV); a tuning knob, results are unchanged."""
+        """Bounds of the warp / CTA / whole-grid evaluation classes; a tuning
+        knob, results are unchanged.  TV, MSV, MSRV, TM, MSM: vertex work (the
+        sum over its nets of min(net size, K)); CN: net pins."""
         _check(lib().fp_set_classes(self._h, light_work, super_work), "fp_set_classes")
 
     def metrics(self) -> dict:
