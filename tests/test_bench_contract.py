@@ -1,0 +1,66 @@
+"""Host-side pieces of bench.py that need no GPU: the workload table, the
+roofline traffic read from the committed ncu summary, and the algorithmic-byte
+model the roofline divides by."""
+import sys
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+ROOT = Path(__file__).resolve().parents[1]
+sys.path.insert(0, str(ROOT))
+bench = pytest.importorskip("bench")
+
+
+def test_workloads_are_named_by_shape_and_complete():
+    need = {"nov", "noe", "alpha", "lo", "hi", "beta", "weight_rule", "K", "eps", "passes", "seed"}
+    assert "zipf4m" in bench.WORKLOADS
+    for name, w in bench.WORKLOADS.items():
+        assert need <= set(w), name
+        assert w["K"] >= 2 and w["passes"] >= 1 and w["eps"] > 1.0, name
+    z = bench.WORKLOADS["zipf4m"]
+    assert (z["nov"], z["noe"], z["K"], z["passes"]) == (4_194_304, 4_194_304, 256, 10)
+
+
+def test_traffic_comes_from_the_committed_summary():
+    """The dominant kernel's DRAM traffic per full-size launch is a line of the
+    ncu summary under profiles/; it is not claimed for reduced-scale runs or
+    for kernels the summaries do not cover."""
+    t = bench.measured_traffic("spec_ldg_kernel", "zipf4m", 1)
+    assert isinstance(t, int) and t > 0
+    text = (ROOT / "profiles" / "spec_ldg_kernel_traffic_zipf4m.md").read_text()
+    assert f"traffic: spec_ldg_kernel zipf4m {t}" in text
+    assert bench.measured_traffic("spec_ldg_kernel", "zipf4m", 2) is None
+    assert bench.measured_traffic("spec_cn_kernel", "zipf4m", 1) is None
+    assert bench.measured_traffic("spec_ldg_kernel", "uniform16k", 1) is None
+
+
+def test_every_metric_maps_to_a_kernel():
+    assert set(bench.KERNEL_OF) == set(bench.METRICS)
+    assert set(bench.KERNEL_OF.values()) == {"spec_ldg_kernel", "spec_cn_kernel", "spec_msg_kernel"}
+
+
+@pytest.fixture(scope="module")
+def small_hg():
+    import fastpartitioner_gb300 as fp
+    return fp.generate(fp.GenSpec.zipf(2000, 2000, 2.1, 2, 200, beta=1.5, weight_rule=1, seed=3))
+
+
+def test_algorithmic_bytes_model(small_hg):
+    """Positive, grows with the moved vertices, and orders the metrics by what
+    they read: CN reads only the two-part nets' pins, the volume and message
+    metrics read more than TV."""
+    hg = small_hg
+    K = 16
+    rng = np.random.default_rng(0)
+    ln = rng.integers(1, 4, size=hg.noe).astype(np.int32)
+    none = np.zeros(hg.nov, bool)
+    some = rng.random(hg.nov) < 0.3
+    tv0 = bench.algorithmic_bytes("TV", hg, ln, none, K)
+    tv1 = bench.algorithmic_bytes("TV", hg, ln, some, K)
+    assert 0 < tv0 < tv1
+    assert bench.algorithmic_bytes("MSV", hg, ln, none, K) > tv0
+    assert bench.algorithmic_bytes("TM", hg, ln, none, K) > bench.algorithmic_bytes("MSV", hg, ln, none, K)
+    cn = bench.algorithmic_bytes("CN", hg, ln, none, K)
+    sizes = np.diff(hg.nptr).astype(np.int64)
+    assert cn == 4 * (hg.noe + 1) + 8 * hg.noe + int(np.sum(8 * sizes[ln == 2]))
