@@ -679,10 +679,12 @@ __device__ void cta_eval_ldg(const DevInstance& I, const SpecBuf& B, const Round
     B.vd[o] = mover ? vdd : 0;
     // CTA evaluation statistics (cycles): tally and merge / decision / the rest
     const long long t3 = clock64();
-    atomicAdd(&B.stats[29], (unsigned long long)(t1 - t0));
-    atomicAdd(&B.stats[30], (unsigned long long)(t2 - t1));
-    atomicAdd(&B.stats[31], (unsigned long long)(t3 - t2));
-    atomicAdd(&B.stats[40], 1ull);
+    if (kTimingStats) {
+      atomicAdd(&B.stats[29], (unsigned long long)(t1 - t0));
+      atomicAdd(&B.stats[30], (unsigned long long)(t2 - t1));
+      atomicAdd(&B.stats[31], (unsigned long long)(t3 - t2));
+      atomicAdd(&B.stats[40], 1ull);
+    }
     const int owner = o / q - (int)blockIdx.x * kSWarps;   // warp of this CTA owning position z
     s_mw[owner] += wv;
     s_mv[owner] += mover ? vdd : 0;
@@ -1013,7 +1015,7 @@ __global__ void __launch_bounds__(kSThreads, 2) spec_ldg_kernel(DevInstance I, S
         if (lane == 0 && c1) atomicAdd(&B.hmisc[hmslot(j)], c1);
         __syncthreads();   // the per-warp arrays serve the next vertex and the evaluations below
       }
-      if (ns && threadIdx.x == 0) atomicMax(&B.stats[38], gtimer() - tR);
+      if (kTimingStats && ns && threadIdx.x == 0) atomicMax(&B.stats[38], gtimer() - tR);
       // ---- A: evaluate
       int wsum = 0, vsum = 0;
       const long long cA = clock64();
@@ -1086,7 +1088,7 @@ __global__ void __launch_bounds__(kSThreads, 2) spec_ldg_kernel(DevInstance I, S
         }
         wsum += wv;
         vsum += mover ? vdd : 0;
-        if (lane == 0) {
+        if (kTimingStats && lane == 0) {
           atomicAdd(&B.stats[41], (unsigned long long)(cT - cz));
           atomicAdd(&B.stats[42], (unsigned long long)(cD - cT));
           atomicAdd(&B.stats[43], (unsigned long long)(clock64() - cD));
@@ -1095,7 +1097,7 @@ __global__ void __launch_bounds__(kSThreads, 2) spec_ldg_kernel(DevInstance I, S
         nV++;
         __syncwarp();
       }
-      if (lane == 0 && nV) {
+      if (kTimingStats && lane == 0 && nV) {
         // per-window statistics (cycles): slowest warp, and all light evaluations
         atomicMax(&B.stats[22], (unsigned long long)(clock64() - cA));
         atomicAdd(&B.stats[25], (unsigned long long)cV);
@@ -1114,7 +1116,7 @@ __global__ void __launch_bounds__(kSThreads, 2) spec_ldg_kernel(DevInstance I, S
                      loc_b);
       }
       __syncthreads();
-      if (threadIdx.x == 0) {
+      if (kTimingStats && threadIdx.x == 0) {
         const long long dm = clock64() - cM;
         if (dm > 2000) atomicMax(&B.stats[24], (unsigned long long)dm);
         atomicMax(&B.stats[36], gtimer() - tR);
@@ -1382,7 +1384,7 @@ __global__ void __launch_bounds__(kSThreads, 2) spec_ldg_kernel(DevInstance I, S
                              cta_o0, false, cut_w);
         }
         __syncthreads();
-        if (threadIdx.x == 0) {
+        if (kTimingStats && threadIdx.x == 0) {
           const unsigned long long tV3 = gtimer();
           atomicMax(&B.stats[39], tV3 - tV);
           // per-pass phase times of this CTA: prefix sums, light positions, the rest

@@ -34,6 +34,14 @@ __device__ __forceinline__ T lds(const T* p) { return __ldcg(p); }
 // per CTA.  Returns false in every thread of the CTA if the wait gave up
 // (another CTA stopped arriving) or another CTA aborted; the kernel then
 // reports FP_ERR_DEVICE_TIMEOUT through `status` and returns.
+// Per-warp / per-CTA timing statistics (atomics in the hot loops): collected
+// only by builds with FP_TIMING_STATS defined.
+#ifdef FP_TIMING_STATS
+constexpr bool kTimingStats = true;
+#else
+constexpr bool kTimingStats = false;
+#endif
+
 constexpr unsigned kBarrierSpins = 1u << 21;   // polls of an L2 line with 32 ns naps: about a second or more
 
 __device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {

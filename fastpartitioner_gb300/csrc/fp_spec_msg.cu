@@ -409,7 +409,9 @@ __device__ void msg_commit_grid(const DevInstance& I, int v, int own, int d, int
   }
 }
 
-__global__ void __launch_bounds__(kSThreads) spec_msg_kernel(DevInstance I, SpecBuf B, int passes) {
+// Three CTAs per SM (the compiler's own choice otherwise varies with the code
+// and can spill).
+__global__ void __launch_bounds__(kSThreads, 3) spec_msg_kernel(DevInstance I, SpecBuf B, int passes) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ unsigned long long uscr[kSWarps];
   __shared__ int iscr[kSWarps];
@@ -537,7 +539,7 @@ __global__ void __launch_bounds__(kSThreads) spec_msg_kernel(DevInstance I, Spec
         if (lane == 0 && g) atomicAdd(&B.hmisc[hmslot(j)], g);
         __syncthreads();   // the per-warp scratch serves the next vertex and the evaluations below
       }
-      if (ns && threadIdx.x == 0) atomicMax(&B.stats[38], gtimer() - tR);
+      if (kTimingStats && ns && threadIdx.x == 0) atomicMax(&B.stats[38], gtimer() - tR);
 
       const int par = round & 1;
       const int span = end_w - pos;
@@ -600,7 +602,7 @@ __global__ void __launch_bounds__(kSThreads) spec_msg_kernel(DevInstance I, Spec
         }
       }
       __syncthreads();
-      if (threadIdx.x == 0) atomicMax(&B.stats[36], gtimer() - tR);
+      if (kTimingStats && threadIdx.x == 0) atomicMax(&B.stats[36], gtimer() - tR);
       if (!grid_barrier(B.bar, I.status)) return;
       if (blockIdx.x == 0 && threadIdx.x == 0) {
         const unsigned long long tE = gtimer();

@@ -190,7 +190,10 @@ int fp_metrics_noalloc(int32_t K, int32_t nov, int32_t noe, int64_t pins, const 
  * evaluations; [41..43] SM cycles of warp evaluations in tally, decision and
  * the rest; [44] decisions fixed inside a window (MSV / MSRV); [45..47]
  * nanoseconds summed over CTAs and validation passes in prefix sums, light
- * positions and the rest (medium and whole-grid vertices). */
+ * positions and the rest (medium and whole-grid vertices).  The per-warp and
+ * per-CTA timings ([21..26], [29..43] except the [33] phase time, [45..47]) are
+ * collected only by a library built with FP_TIMING_STATS defined, and are zero
+ * otherwise. */
 int fp_get_stats(fp_instance* inst, int64_t* out, int32_t n);
 /* Number of kernel launches the last fp_refine / fp_metrics call enqueued. */
 int fp_last_launches(fp_instance* inst, int64_t* launches);
