@@ -34,9 +34,15 @@ def _sources():
     return sorted(CSRC.glob("*.cu")) + sorted(CSRC.glob("*.cpp"))
 
 
+def _defines() -> list:
+    """FP_TIMING_STATS=1 in the environment builds the per-warp / per-CTA timing
+    statistics of the refinement kernels (diagnostics; atomics in hot loops)."""
+    return ["-DFP_TIMING_STATS"] if os.environ.get("FP_TIMING_STATS") == "1" else []
+
+
 def _compile(src: Path, nvcc: str) -> Path:
     obj = BUILD / (src.name + ".o")
-    common = ["-O3", "-std=c++17", "-I", str(INCLUDE), "-Xcompiler", "-fPIC,-ffp-contract=off"]
+    common = ["-O3", "-std=c++17", "-I", str(INCLUDE), *_defines(), "-Xcompiler", "-fPIC,-ffp-contract=off"]
     if src.suffix == ".cu":
         cmd = [nvcc, *ARCH, "-lineinfo", *common, "-c", str(src), "-o", str(obj)]
     else:
@@ -49,6 +55,9 @@ def _compile(src: Path, nvcc: str) -> Path:
 
 def _stale() -> bool:
     if not LIB.exists():
+        return True
+    stamp = BUILD / "defines.txt"
+    if (stamp.read_text() if stamp.exists() else "") != " ".join(_defines()):
         return True
     t = LIB.stat().st_mtime
     deps = _sources() + list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + list(INCLUDE.glob("*.h"))
@@ -70,6 +79,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     if res.returncode != 0:
         raise RuntimeError(f"link failed: {' '.join(cmd)}\n{res.stdout}\n{res.stderr}")
     os.replace(tmp, LIB)
+    (BUILD / "defines.txt").write_text(" ".join(_defines()))
     if verbose:
         print(f"built {LIB}", file=sys.stderr)
     return LIB
