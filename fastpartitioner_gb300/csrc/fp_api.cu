@@ -37,9 +37,9 @@ static bool spec_supported(int metric, int K, int max_smem) {
   return spec_ldg_smem_bytes(K) + static_smem <= (size_t)max_smem;
 }
 // LDG metrics: vertex classes by work = sum over its nets of min(net size, K),
-// the list slots an evaluation reads at most.  Light: one warp; medium: one CTA
-// inside the window; above the super bound (or with 65536 nets or more, the
-// limit of the candidate encoding): a whole-grid round.  Windows that end
+// the list slots an evaluation reads at most.  Light: one warp; medium: one CTA;
+// above the super bound (or with 65536 nets or more, the limit of the candidate
+// encoding): all warps of the grid, all inside the window.  Windows that end
 // often (MSV moves nearly every vertex) favour a lower super bound, long ones
 // (TV, MSM) a higher one; bounds from a sweep on the 4M-vertex Zipf workload.
 // TM and MSM use the same classes in id order.
@@ -290,9 +290,10 @@ int fp_ctx_set_stream(fp_ctx* ctx, void* stream) {
   return FP_OK;
 }
 
-// Claims (no claim: a value above every position) and both heavy-round
-// buffers start clear for every speculative launch: a launch leaves the buffer
-// of its last heavy round, and an aborted launch its claims, behind.
+// Claims (no claim: a value above every position) and both parities of the
+// whole-grid tallies start clear for every speculative launch: a launch leaves
+// the tallies of its last window with whole-grid vertices, and an aborted
+// launch its claims, behind.
 static cudaError_t clear_spec_scratch(const SpecBuf& b, int noe, int K, cudaStream_t s) {
   const size_t ne = (size_t)std::max(noe, 1);
   cudaError_t e = cudaMemsetAsync(b.claim_m, 0x7f, sizeof(int) * ne, s);

@@ -71,7 +71,7 @@ struct SpecBuf {
   uint32_t* rec;         // [pins] per (vertex, net) record of a move (spec::rec_pack),
                          //     at the pair's vnets index
   const unsigned char* vclass;  // [nov] 0: warp-evaluated, 1: CTA-evaluated (medium),
-                                //     2: whole-grid round (LDG metrics)
+                                //     2: evaluated by the whole grid
   unsigned long long* cand;  // [wmax * K] LDG candidates per window offset (part, count, first)
   int* ncand;            // [wmax]
   int4* mlist;           // [wmax] the round's movers (any order): window offset, weight,
@@ -96,8 +96,8 @@ struct SpecBuf {
   uint2* rec_slot2;      // [pins] (MSV / MSRV) those of a move replaced by an in-window fix
   int* ctab_over;        // [2] a probe ran past its bound this round (by round parity)
   unsigned ctab_mask;
-  const int* heavy_pos;  // positions (visiting order, ascending) of vertices that get a
-  int nheavy;            //     whole-grid round of their own
+  const int* heavy_pos;  // positions (visiting order, ascending) of vertices evaluated by
+  int nheavy;            //     the whole grid (CN: nets with more than cn_grid pins)
   const int* mid_pos;    // positions (ascending) of medium vertices, evaluated by one CTA
   int nmid;              //     (CN: nets with more than cn_big pins, up to cn_grid)
   int cn_big, cn_grid;   // CN: nets with more than cn_grid pins are evaluated by the grid

@@ -172,11 +172,11 @@ int fp_metrics_noalloc(int32_t K, int32_t nov, int32_t noe, int64_t pins, const 
                        const int32_t* ep_part, int64_t* out, void* stream);
 
 /* Statistics of the last fp_refine on the grid-wide engine (up to 48 values):
- * [0] windows, [1] single-vertex rounds of high-degree vertices, [2] moves
+ * [0] windows, [1] whole-grid evaluations of heavy vertices (CN: nets), [2] moves
  * committed from windows, [3..8] windows ended by: nothing (fully valid), a
  * possibly stale TV marker, part-size drift, volume drift, a max-volume part
  * changing, a shared net; [9] vertices walked in windows; [16..19] nanoseconds
- * in evaluate, validate, commit phases and single-vertex rounds; TV / MSV /
+ * in evaluate, validate, commit phases and (TM / MSM) whole-grid decisions; TV / MSV /
  * MSRV also: [20] nanoseconds computing the round state, [21] / [23] SM cycles
  * summed over windows of the slowest warp / CTA evaluation, [25] / [26] SM
  * cycles and count of warp evaluations, [27] / [28] windows ended by an earlier
