@@ -105,6 +105,7 @@ def lib():
         pp = C.POINTER(C.c_void_p)
         sig = {
             "fp_validate": ([C.POINTER(_Hypergraph)], C.c_int),
+            "fp_bfs_order": ([C.POINTER(_Hypergraph), C.c_int32, C.c_void_p, C.c_void_p], C.c_int),
             "fp_ctx_create": ([i32, pp], C.c_int),
             "fp_ctx_destroy": ([vp], C.c_int),
             "fp_ctx_set_stream": ([vp, vp], C.c_int),
@@ -192,6 +193,18 @@ class Hypergraph:
         """fp_validate status (0 when the engine accepts the hypergraph)."""
         v = self.view()
         return int(lib().fp_validate(C.byref(v)))
+
+    def bfs_order(self, start: int) -> np.ndarray:
+        """The reference's BFS visiting order (-o 1; fp_bfs_order): three BFS
+        runs, from `start`, from the farthest vertex, and from the farthest
+        again, listing vertices in discovery order.  The reference drivers
+        start from rand() % nov (TV/tv.cpp:120).  Raises FastPartError if a
+        vertex is not reached.  Host code, no GPU."""
+        out = np.empty(self.nov, np.int32)
+        far = np.empty(2, np.int32)
+        v = self.view()
+        _check(lib().fp_bfs_order(C.byref(v), int(start), _ptr(out), _ptr(far)), "fp_bfs_order")
+        return out
 
     def view(self) -> _Hypergraph:
         return _Hypergraph(self.nov, self.noe, self.pins, _ptr(self.vptr), _ptr(self.vnets),

@@ -184,6 +184,71 @@ int fp_graph_from_vertices(int32_t nov, int32_t noe, const uint32_t* vptr, const
   return FP_OK;
 }
 
+int fp_bfs_order(const fp_hypergraph* h, int32_t start, int32_t* ordering, int32_t* far_out) {
+  if (!h || !ordering) return FP_ERR_INVALID;
+  int rc = fp_validate(h);
+  if (rc) return rc;
+  const int nov = h->nov, noe = h->noe;
+  if (start < 0 || start >= nov) return FP_ERR_INVALID;
+  // net -> pins with the pins of a net in ascending vertex id: the order the
+  // reference's createInverse builds and its BFS walks (shared/utils.cpp:32-56)
+  std::vector<uint32_t> iptr(noe + 1, 0), ipins(h->pins);
+  for (long long k = 0; k < h->pins; k++) iptr[h->vnets[k] + 1]++;
+  for (int e = 0; e < noe; e++) iptr[e + 1] += iptr[e];
+  {
+    std::vector<uint32_t> fill(iptr.begin(), iptr.end() - 1);
+    for (int v = 0; v < nov; v++)
+      for (uint32_t k = h->vptr[v]; k < h->vptr[v + 1]; k++) ipins[fill[h->vnets[k]]++] = (uint32_t)v;
+  }
+  // One level at a time, frontier in discovery order: a vertex's nets in
+  // vertex -> nets order, a net's pins in ascending id (the one-thread walk of
+  // topDown, shared/utils.cpp:538-590).
+  std::vector<int> dist(nov), queue, next;
+  auto bfs = [&](int s, int32_t* order) {
+    std::fill(dist.begin(), dist.end(), -1);
+    queue.assign(1, s);
+    dist[s] = 0;
+    int n = 0, level = 0;
+    if (order) order[n++] = s;
+    while (!queue.empty()) {
+      next.clear();
+      for (int v : queue)
+        for (uint32_t k = h->vptr[v]; k < h->vptr[v + 1]; k++) {
+          const uint32_t e = h->vnets[k];
+          for (uint32_t j = iptr[e]; j < iptr[e + 1]; j++) {
+            const int u = (int)ipins[j];
+            if (dist[u] < 0) {
+              dist[u] = level + 1;
+              next.push_back(u);
+            }
+          }
+        }
+      if (next.empty()) break;
+      level++;
+      if (order)
+        for (int u : next) order[n++] = u;
+      queue.swap(next);
+    }
+    return n;
+  };
+  // the farthest vertex: the lowest id at the largest distance
+  // (bfsFarthest_queue_par, shared/utils.cpp:433-480)
+  auto farthest = [&]() {
+    int f = -1, fd = -1;
+    for (int i = 0; i < nov; i++)
+      if (dist[i] > fd) { f = i; fd = dist[i]; }
+    return f;
+  };
+  bfs(start, nullptr);
+  const int f1 = farthest();
+  bfs(f1, nullptr);
+  const int f2 = farthest();
+  for (int i = 0; i < nov; i++) ordering[i] = -1;
+  const int reached = bfs(f2, ordering);   // bfsOrdering_queue_par, shared/utils.cpp:482-536
+  if (far_out) { far_out[0] = f1; far_out[1] = f2; }
+  return reached == nov ? FP_OK : FP_ERR_UNSUPPORTED;
+}
+
 int fp_read_patohlike(const char* path, int32_t transpose, int32_t write_cache, fp_graph** out) {
   if (!path || !out) return FP_ERR_INVALID;
   *out = nullptr;

@@ -213,6 +213,18 @@ typedef struct {
 } fp_gen_params;
 
 int fp_generate(const fp_gen_params* p, fp_graph** out);
+/* BFS visiting order, the reference's -o 1 (TV/tv.cpp:110-128 with one thread;
+ * replaces bfsFarthest_queue_par x 2 + bfsOrdering_queue_par,
+ * shared/utils.cpp:433-536).  A BFS from `start` finds the farthest vertex
+ * (lowest id on ties), a BFS from it the farthest again, and a BFS from that
+ * one lists the vertices level by level in discovery order: a vertex's nets in
+ * vertex -> nets order, a net's pins in ascending id (createInverse's order).
+ * The reference driver starts from rand() % nov.  Writes nov entries to
+ * `ordering` (-1 past the reached vertices) and, if far_out is not null, the
+ * two farthest vertices.  FP_ERR_UNSUPPORTED if a vertex is not reached: the
+ * reference's partitioners would then read ordering entries of -1.  Host code
+ * (no GPU). */
+int fp_bfs_order(const fp_hypergraph* h, int32_t start, int32_t* ordering, int32_t* far_out);
 /* Builds a host graph from a net -> pins CSR (the .hg orientation of the TV and
  * CN drivers): vertex -> nets is its transpose, nets ascending per vertex. */
 int fp_graph_from_nets(int32_t nov, int32_t noe, const uint32_t* nptr, const uint32_t* npins,

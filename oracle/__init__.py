@@ -157,6 +157,26 @@ def run_reference(hg, K: int, metric: str, passes: int, threads: int = 1, captur
         return out
 
 
+def run_reference_bfs(hg, start: int, timeout: float = 600):
+    """The reference's BFS ordering (-o 1: createInverse, bfsFarthest_queue_par
+    twice, bfsOrdering_queue_par, one thread) from vertex `start`, through the
+    ref_bfs harness.  Returns (first farthest, second farthest, ordering with
+    -1 past the reached vertices)."""
+    exe = REF_DIR / "ref_bfs"
+    if not exe.exists():
+        raise FileNotFoundError(f"{exe} not built (reference sources unavailable)")
+    with tempfile.TemporaryDirectory(prefix="fpbfs") as td:
+        inst = Path(td) / "inst.fphg"
+        hg.save_fphg(inst)
+        env = dict(os.environ, OMP_NUM_THREADS="1")
+        res = subprocess.run([str(exe), str(inst), str(int(start))], capture_output=True, text=True,
+                             timeout=timeout, env=env, cwd=td)
+        if res.returncode != 0:
+            raise RuntimeError(f"reference bfs failed ({res.returncode}): {res.stderr[-2000:]}")
+        vals = np.array(res.stdout.split(), dtype=np.int64)
+        return int(vals[0]), int(vals[1]), vals[2:2 + hg.nov].astype(np.int32)
+
+
 def flat_lists(hg, ep_len, ep_part):
     """Concatenation of every net's listed parts, in list order (the form the
     reference capture stores)."""
