@@ -26,10 +26,13 @@ cudaError_t launch_spec_cn(const DevInstance& I, const SpecBuf& B, int passes, i
 size_t spec_ldg_smem_bytes(int K);
 size_t spec_msg_smem_bytes(int K);
 // The speculative grid-wide engine covers every metric as long as its shared
-// memory fits a CTA (per-warp K-sized arrays); above that K the single-CTA walk
-// refines (same results).
-static bool spec_supported(int metric, int K, int max_smem) {
+// memory fits a CTA (per-warp K-sized arrays) and the walked positions (vertices;
+// nets for CN) stay below 2^28, the range of its cut words (position << 3 |
+// reason); otherwise the single-CTA walk refines (same results).
+constexpr int kMaxSpecPositions = 1 << 28;
+static bool spec_supported(int metric, int K, int max_smem, int nov, int noe) {
   if (metric < FP_METRIC_CN || metric > FP_METRIC_MSRV) return false;
+  if ((metric == FP_METRIC_CN ? noe : nov) >= kMaxSpecPositions) return false;
   const size_t static_smem = 8192;   // the kernels' static shared arrays, with room to spare
   if (metric == FP_METRIC_TM || metric == FP_METRIC_MSM)
     return spec_msg_smem_bytes(K) + static_smem <= (size_t)max_smem;
@@ -558,7 +561,8 @@ int fp_refine(fp_instance* in, int32_t passes) {
   cudaError_t e = cudaMemsetAsync(in->d.moves, 0, sizeof(long long) * passes, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(in->d.status, 0, sizeof(int), s);
   const bool spec =
-      in->engine == FP_ENGINE_AUTO && spec_supported(in->pb.metric, in->pb.K, in->ctx->max_smem);
+      in->engine == FP_ENGINE_AUTO &&
+      spec_supported(in->pb.metric, in->pb.K, in->ctx->max_smem, in->g.nov, in->g.noe);
   if (spec) {
     static const int none[8] = {0x7fffffff, 0x7fffffff, 0x7fffffff, 0x7fffffff,
                                 0x7fffffff, 0x7fffffff, 0x7fffffff, 0x7fffffff};
