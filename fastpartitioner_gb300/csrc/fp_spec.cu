@@ -74,8 +74,10 @@ __device__ __forceinline__ int slack_divf(float a, float b) {
   return (int)floorf(x);
 }
 
-// Candidate entry of a part for the exact re-check: part, count without the
-// vertex itself, first sighting (net index, slot).
+// Candidate entry of a part for the exact re-check: part (12 bits), count
+// without the vertex itself (16 bits), first sighting (net index, 16 bits;
+// slot, 20 bits).  A vertex whose count or first net index does not fit (one
+// with 65536 nets or more) stores no list: ncand = -1.
 __device__ __forceinline__ unsigned long long cand_entry(int p, int c, unsigned long long f) {
   return ((unsigned long long)p << 52) | ((unsigned long long)c << 36) | (((f >> 32) & 0xffffull) << 20) |
          (f & 0xfffffull);
@@ -94,7 +96,7 @@ __device__ int ldg_decide(const DevInstance& I, const RoundCtx& R, const int* cn
   const int K = I.K;
   const bool tv = metric == kTV;
   int nc = 0;
-  bool sp = false;
+  bool sp = false, wide = false;
 #pragma unroll 4
   for (int p0 = 0; p0 < K; p0 += 32) {
     const int p = p0 + lane;
@@ -106,7 +108,11 @@ __device__ int ldg_decide(const DevInstance& I, const RoundCtx& R, const int* cn
     if (ok) {
       const int i = nc + __popc(m & below);
       list[i] = p;
-      if (cand) cand[i] = cand_entry(p, c - (p == own ? 1 : 0), first[p]);
+      if (cand) {
+        const unsigned long long f = first[p];
+        wide |= c > 0xffff || (f >> 32) > 0xffffull;
+        cand[i] = cand_entry(p, c - (p == own ? 1 : 0), f);
+      }
     }
     if (scan) {
       const unsigned ms = __ballot_sync(kAll, c > 0);
@@ -114,7 +120,8 @@ __device__ int ldg_decide(const DevInstance& I, const RoundCtx& R, const int* cn
     }
     nc += __popc(m);
   }
-  if (cand && lane == 0) *ncand = nc;
+  wide = __any_sync(kAll, wide);
+  if (cand && lane == 0) *ncand = wide ? -1 : nc;
   *special = __any_sync(kAll, sp) && !first_of_window;
   __syncwarp();
   float fb = 0.0f;   // largest lower bound of a score (0: none positive for sure)
@@ -226,6 +233,7 @@ __device__ int ldg_decide(const DevInstance& I, const RoundCtx& R, const int* cn
 // the moves of the window's movers before o -- those before offset o_from
 // already summed per part in dsz_cta (the CTA's share), the rest read from the
 // window records -- gathered in the warp's K-int scratch dsz.  One warp.
+// Returns -1 if the vertex has no candidate list (65536 nets or more).
 __device__ int ldg_recheck(const DevInstance& I, const RoundCtx& R, const SpecBuf& B, int o, int own, int metric,
                            int* dsz, const int* dsz_cta, int o_from) {
   const int lane = threadIdx.x & 31;
@@ -242,6 +250,7 @@ __device__ int ldg_recheck(const DevInstance& I, const RoundCtx& R, const SpecBu
   __syncwarp();
   const unsigned long long* cl = B.cand + (size_t)o * K;
   const int nc = lds(&B.ncand[o]);
+  if (nc < 0) return -1;   // no list (65536 nets or more): the caller cuts
   // Float scores first: the float penalty 1 - sz / C is off by less than
   // 4e-7 * (1 + sz / C), so a score of count c by less than c times that; the
   // bound used is 1e-6 * c * (1 + sz / C).  Exact double scores only for
