@@ -177,6 +177,29 @@ def run_reference_bfs(hg, start: int, timeout: float = 600):
         return int(vals[0]), int(vals[1]), vals[2:2 + hg.nov].astype(np.int32)
 
 
+def run_reference_read(path, timeout: float = 600) -> dict:
+    """The reference's read_patohlike on `path` (it reads <path>.plbin when
+    present and writes it otherwise), through the ref_read harness: ok, nov,
+    noe, pins and the line CSR (col_ptr, row_ind) with the per-id counts."""
+    exe = REF_DIR / "ref_read"
+    if not exe.exists():
+        raise FileNotFoundError(f"{exe} not built (reference sources unavailable)")
+    with tempfile.TemporaryDirectory(prefix="fpread") as td:
+        out = Path(td) / "out.bin"
+        res = subprocess.run([str(exe), str(path), str(out)], capture_output=True, text=True, timeout=timeout)
+        if res.returncode != 0:
+            raise RuntimeError(f"reference read failed ({res.returncode}): {res.stderr[-2000:]}")
+        raw = out.read_bytes()
+    ok, nov, noe = np.frombuffer(raw[:12], np.int32)
+    pins = int(np.frombuffer(raw[12:20], np.int64)[0])
+    r = {"ok": bool(ok), "nov": int(np.uint32(nov)), "noe": int(np.uint32(noe)), "pins": pins}
+    if ok:
+        arr = np.frombuffer(raw[20:], np.uint32)
+        n, m = r["noe"] + 1, pins
+        r["col_ptr"], r["row_ind"], r["appear"] = arr[:n], arr[n:n + m], arr[n + m:n + m + r["nov"]]
+    return r
+
+
 def flat_lists(hg, ep_len, ep_part):
     """Concatenation of every net's listed parts, in list order (the form the
     reference capture stores)."""
