@@ -106,6 +106,7 @@ def lib():
         sig = {
             "fp_validate": ([C.POINTER(_Hypergraph)], C.c_int),
             "fp_bfs_order": ([C.POINTER(_Hypergraph), C.c_int32, C.c_void_p, C.c_void_p], C.c_int),
+            "fp_stream_partition": ([C.POINTER(_Hypergraph), i32, i32, dbl, C.POINTER(FpState)], C.c_int),
             "fp_ctx_create": ([i32, pp], C.c_int),
             "fp_ctx_destroy": ([vp], C.c_int),
             "fp_ctx_set_stream": ([vp, vp], C.c_int),
@@ -508,6 +509,22 @@ class Instance:
 
 
 NOALLOC_MAX_K = 1024   # FP_NOALLOC_MAX_K
+
+
+def stream_partition(hg: Hypergraph, K: int, metric, eps: float = 1.05) -> dict:
+    """The metric's streaming initial partition on the host (fp_stream_partition),
+    in the fp_state layout: part_vec, ep_starts, ep_ends, ep_parts, ep_cnt,
+    part_sizes, marker, send, recv, conn (K*K), msgs.  No GPU needed; an
+    instance takes it with set_state."""
+    nov, noe, P = hg.nov, hg.noe, hg.pins
+    sizes = dict(part_vec=nov, ep_starts=noe, ep_ends=noe, ep_parts=P, ep_cnt=P, part_sizes=K, marker=K,
+                 send=K, recv=K, conn=K * K, msgs=K)
+    out = {k: np.empty(n, np.int32) for k, n in sizes.items()}
+    st = FpState(**{k: v.ctypes.data for k, v in out.items()})
+    v = hg.view()
+    _check(lib().fp_stream_partition(C.byref(v), int(K), metric_id(metric), float(eps), C.byref(st)),
+           "fp_stream_partition")
+    return out
 
 
 def metrics_noalloc(K, nov, noe, pins, nptr, src, part_vec, ep_len, ep_part, out, stream=None) -> None:

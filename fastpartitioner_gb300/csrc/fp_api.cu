@@ -113,7 +113,6 @@ struct fp_instance {
 namespace {
 
 const int kMaxPasses = 4096;
-const int kMaxK = 4096;
 const int kSpecWindow = 16384;   // longest speculative window (vertices)
 const int kMsgWindow = 65536;    // longest TM / MSM window
 
@@ -387,34 +386,13 @@ int fp_instance_create(fp_ctx* ctx, const fp_hypergraph* h, int32_t K, int32_t m
                        fp_instance** out) {
   if (!ctx || !out || metric < 0 || metric > 5 || K < 2 || K > kMaxK || !(eps_factor > 0)) return FP_ERR_INVALID;
   *out = nullptr;
-  int rc = validate(h);
-  if (rc) return rc;
   fp_instance* in = new (std::nothrow) fp_instance;
   if (!in) return FP_ERR_NOMEM;
   in->ctx = ctx;
-  HostGraph& g = in->g;
-  g.nov = h->nov;
-  g.noe = h->noe;
-  g.pins = h->pins;
-  g.vptr.assign(h->vptr, h->vptr + h->nov + 1);
-  g.vnets.assign(h->vnets, h->vnets + h->pins);
-  g.nptr.assign(h->nptr, h->nptr + h->noe + 1);
-  g.npins.assign(h->npins, h->npins + h->pins);
-  g.src.assign(h->src, h->src + h->noe);
-  Problem& pb = in->pb;
-  pb.g = &in->g;
-  pb.K = K;
-  pb.metric = metric;
-  pb.eps_factor = eps_factor;
-  pb.w.resize(g.nov);
-  long long W = 0;
-  for (int v = 0; v < g.nov; v++) { pb.w[v] = h->weights ? h->weights[v] : 1; W += pb.w[v]; }
-  if (h->weights) g.weights = pb.w;
-  pb.order.resize(g.nov);
-  for (int z = 0; z < g.nov; z++) pb.order[z] = h->ordering ? h->ordering[z] : z;
-  pb.xw = (int)(W / K);
-  if (pb.xw < 1) { delete in; return FP_ERR_INVALID; }
-  pb.C = pb.xw * eps_factor;
+  int rc = make_problem(h, K, metric, eps_factor, in->g, in->pb);   // validates h
+  if (rc) { delete in; return rc; }
+  const HostGraph& g = in->g;
+  const Problem& pb = in->pb;
 
   cudaSetDevice(ctx->device);
   DevInstance& d = in->d;

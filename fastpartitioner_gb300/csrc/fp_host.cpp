@@ -121,7 +121,69 @@ bool write_plbin(const std::string& path, int nov, int noe, long long pins, cons
 
 }  // namespace
 
+namespace fp {
+
+int make_problem(const fp_hypergraph* h, int K, int metric, double eps_factor, HostGraph& g, Problem& pb) {
+  if (metric < 0 || metric > 5 || K < 2 || K > kMaxK || !(eps_factor > 0)) return FP_ERR_INVALID;
+  const int rc = fp_validate(h);
+  if (rc) return rc;
+  g.nov = h->nov;
+  g.noe = h->noe;
+  g.pins = h->pins;
+  g.vptr.assign(h->vptr, h->vptr + h->nov + 1);
+  g.vnets.assign(h->vnets, h->vnets + h->pins);
+  g.nptr.assign(h->nptr, h->nptr + h->noe + 1);
+  g.npins.assign(h->npins, h->npins + h->pins);
+  g.src.assign(h->src, h->src + h->noe);
+  pb.g = &g;
+  pb.K = K;
+  pb.metric = metric;
+  pb.eps_factor = eps_factor;
+  pb.w.resize(g.nov);
+  long long W = 0;
+  for (int v = 0; v < g.nov; v++) { pb.w[v] = h->weights ? h->weights[v] : 1; W += pb.w[v]; }
+  if (h->weights) g.weights = pb.w;
+  pb.order.resize(g.nov);
+  for (int z = 0; z < g.nov; z++) pb.order[z] = h->ordering ? h->ordering[z] : z;
+  pb.xw = (int)(W / K);
+  if (pb.xw < 1) return FP_ERR_INVALID;
+  pb.C = pb.xw * eps_factor;
+  return FP_OK;
+}
+
+}  // namespace fp
+
 extern "C" {
+
+int fp_stream_partition(const fp_hypergraph* h, int32_t K, int32_t metric, double eps_factor, fp_state* out) {
+  if (!h || !out) return FP_ERR_INVALID;
+  fp::HostGraph g;
+  fp::Problem pb;
+  int rc = fp::make_problem(h, K, metric, eps_factor, g, pb);
+  if (rc) return rc;
+  fp::HostState st;
+  rc = fp::initial_partition(pb, st);
+  if (rc) return rc;
+  const size_t KK = (size_t)K * K;
+  if (out->part_vec) std::copy(st.part_vec.begin(), st.part_vec.end(), out->part_vec);
+  if (out->ep_starts)
+    for (int e = 0; e < g.noe; e++) out->ep_starts[e] = (int)g.nptr[e];
+  if (out->ep_ends)
+    for (int e = 0; e < g.noe; e++) out->ep_ends[e] = (int)g.nptr[e] + st.ep_len[e];
+  if (out->ep_parts) std::copy(st.ep_part.begin(), st.ep_part.end(), out->ep_parts);
+  if (out->ep_cnt) std::copy(st.ep_cnt.begin(), st.ep_cnt.end(), out->ep_cnt);
+  if (out->part_sizes) std::copy(st.part_sizes.begin(), st.part_sizes.end(), out->part_sizes);
+  if (out->marker) std::copy(st.marker.begin(), st.marker.end(), out->marker);
+  if (out->send) std::copy(st.send.begin(), st.send.end(), out->send);
+  if (out->recv) std::copy(st.recv.begin(), st.recv.end(), out->recv);
+  if (out->msgs) std::copy(st.msgs.begin(), st.msgs.end(), out->msgs);
+  if (out->conn) {
+    if (st.conn.size() == KK) std::copy(st.conn.begin(), st.conn.end(), out->conn);
+    else std::fill(out->conn, out->conn + KK, 0);
+  }
+  return FP_OK;
+}
+
 
 int fp_generate(const fp_gen_params* p, fp_graph** out) {
   if (!p || !out) return FP_ERR_INVALID;

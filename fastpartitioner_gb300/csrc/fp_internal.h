@@ -60,6 +60,13 @@ struct Problem {
 // Streaming initial partitioners (host).  Return FP_OK or an error code.
 int initial_partition(const Problem& pb, HostState& st);
 
+// Largest K the library supports (13-bit list slots in the device records).
+constexpr int kMaxK = 4096;
+
+// Copies a validated hypergraph into g and fills pb (weights, visiting order,
+// xw = W / K, C = xw * eps_factor) as the reference derives them.
+int make_problem(const fp_hypergraph* h, int K, int metric, double eps_factor, HostGraph& g, Problem& pb);
+
 }  // namespace fp
 
 // Opaque handle of the public header: a host-owned hypergraph.

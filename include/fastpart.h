@@ -274,6 +274,14 @@ int fp_set_state(fp_instance* inst, const fp_state* st);
 /* Copies the current device state out; NULL members are skipped.  ep_starts
  * is filled with the net offsets. */
 int fp_get_state(fp_instance* inst, fp_state* st);
+/* The metric's streaming initial partition on the host (the CPU half of the
+ * reference's partition_gpu(): TV/partition.cpp:207-264, CN/partition.cpp:
+ * 132-221, TM/partition.cpp:87-250, MSM/partition.cpp:146-309,
+ * MGV/partition.cpp:122-189, MSRV/partition.cpp:123-196), written to `out` in
+ * the fp_state layout (NULL members skipped; conn zero for the metrics that
+ * keep none).  The same stream fp_initial_partition runs; no GPU needed.
+ * fp_set_state then hands the state to an instance. */
+int fp_stream_partition(const fp_hypergraph* h, int32_t K, int32_t metric, double eps_factor, fp_state* out);
 
 /* ---- drop-in for partition_gpu() --------------------------------------- */
 /* Same arguments and the same stdout lines as the reference's partition_gpu()
