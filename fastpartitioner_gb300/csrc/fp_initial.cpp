@@ -166,8 +166,17 @@ int stream_msg(const Problem& pb, HostState& st) {
   st.conn.assign((size_t)K * K, 0);
   if (pb.metric == FP_METRIC_MSM)
     for (int i = 0; i < K; i++) st.conn[(size_t)i * K + i] = -1;
-  std::vector<int> smark(K, -1), src_part(g.noe, -1);
-  std::vector<int> act_parts, act_nets, own_nets;
+  // conn > 0 as bit sets by row and by column.  The stream only raises
+  // connection counts, so a bit is set once, when its count leaves 0.
+  const int W = (K + 63) / 64;
+  std::vector<uint64_t> prow((size_t)K * W, 0), pcol((size_t)K * W, 0);
+  auto set_pos = [&](int a, int b) {
+    prow[(size_t)a * W + (b >> 6)] |= 1ull << (b & 63);
+    pcol[(size_t)b * W + (a >> 6)] |= 1ull << (a & 63);
+  };
+  std::vector<int> smark(K, -1), src_part(g.noe, -1), mult(K, 0);
+  std::vector<int> act_parts, act_nets, own_nets, mparts, dcount;
+  std::vector<uint64_t> act(W), planes;
   for (int z = 0; z < g.nov; z++) {
     const int v = pb.order[z];
     act_parts.clear();
@@ -179,37 +188,70 @@ int stream_msg(const Problem& pb, HostState& st) {
       const int sp = src_part[e];
       if (sp != -1) {
         if (smark[sp] != v) { smark[sp] = v; act_parts.push_back(sp); }
-        act_nets.push_back(e);
+        act_nets.push_back((int)(i - g.vptr[v]));   // index among v's nets
       }
     }
     // Part saving the most messages among parts below capacity; ties to the
-    // smaller part, then the lower index.
+    // smaller part, then the lower index.  saved(k) counts the active source
+    // parts sp with conn[sp][k] > 0, and over the vertex's own nets every
+    // listed part p with conn[k][p] > 0 (TM/partition.cpp:113-150): the first
+    // sum is a popcount of column k under the active-part mask, the second one
+    // of row k under the bit planes of each part's multiplicity.
+    std::fill(act.begin(), act.end(), 0);
+    for (int sp : act_parts) act[sp >> 6] |= 1ull << (sp & 63);
+    mparts.clear();
+    int mmax = 0;
+    for (int e : own_nets) {
+      const int s = st.ep_start[e];
+      for (int j = 0; j < st.ep_len[e]; j++) {
+        const int p = st.ep_part[s + j];
+        if (mult[p]++ == 0) mparts.push_back(p);
+        mmax = std::max(mmax, mult[p]);
+      }
+    }
+    int nplanes = 0;
+    while ((mmax >> nplanes) != 0) nplanes++;
+    planes.assign((size_t)nplanes * W, 0);
+    for (int p : mparts)
+      for (int b = 0; b < nplanes; b++)
+        if ((mult[p] >> b) & 1) planes[(size_t)b * W + (p >> 6)] |= 1ull << (p & 63);
+    for (int p : mparts) mult[p] = 0;
     int best = -1, arg = -1;
     for (int k = 0; k < K; k++) {
       if (!(st.part_sizes[k] < pb.C)) continue;
+      const uint64_t* col = &pcol[(size_t)k * W];
+      const uint64_t* row = &prow[(size_t)k * W];
       int saved = 0;
-      for (int sp : act_parts) saved += st.conn[(size_t)sp * K + k] > 0;
-      for (int e : own_nets) {
-        const int s = st.ep_start[e];
-        for (int j = 0; j < st.ep_len[e]; j++) saved += st.conn[(size_t)k * K + st.ep_part[s + j]] > 0;
+      for (int x = 0; x < W; x++) saved += __builtin_popcountll(col[x] & act[x]);
+      for (int b = 0; b < nplanes; b++) {
+        int c = 0;
+        for (int x = 0; x < W; x++) c += __builtin_popcountll(row[x] & planes[(size_t)b * W + x]);
+        saved += c << b;
       }
       if (saved > best || (saved == best && st.part_sizes[k] < st.part_sizes[arg])) { best = saved; arg = k; }
     }
     const int d = arg >= 0 ? arg : argmin_size(st.part_sizes);
     st.part_vec[v] = d;
     st.part_sizes[d] += pb.w[v];
-    for (uint32_t i = g.vptr[v]; i < g.vptr[v + 1]; i++) list_add(st, (int)g.vnets[i], d);
-    for (int e : act_nets) {
+    // d's count in each of v's nets after adding v (the reference looks it up
+    // again, TM/partition.cpp:210-223)
+    dcount.resize(g.vptr[v + 1] - g.vptr[v]);
+    for (uint32_t i = g.vptr[v]; i < g.vptr[v + 1]; i++) {
+      const int e = (int)g.vnets[i];
+      const int j = list_add(st, e, d);
+      dcount[i - g.vptr[v]] = st.ep_cnt[st.ep_start[e] + j];
+    }
+    for (int k : act_nets) {
+      const int e = (int)g.vnets[g.vptr[v] + k];
       const int sp = src_part[e];
       if (sp == d) continue;
       int& c = st.conn[(size_t)sp * K + d];
       if (c == 0) {
         st.msgs[sp]++;
         c = 1;
-      } else {
-        const int s = st.ep_start[e];
-        const int j = list_find(&st.ep_part[s], st.ep_len[e], d);
-        if (j >= 0 && st.ep_cnt[s + j] == 1) c++;
+        set_pos(sp, d);
+      } else if (dcount[k] == 1) {
+        c++;
       }
     }
     for (int e : own_nets) {
@@ -219,7 +261,7 @@ int stream_msg(const Problem& pb, HostState& st) {
         const int p = st.ep_part[s + j];
         if (p == d) continue;
         int& c = st.conn[(size_t)d * K + p];
-        if (c == 0) { st.msgs[d]++; c = 1; }
+        if (c == 0) { st.msgs[d]++; c = 1; set_pos(d, p); }
         else c++;
       }
     }
