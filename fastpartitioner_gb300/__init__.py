@@ -131,6 +131,7 @@ def lib():
             "fp_graph_from_nets": ([i32, i32, vp, vp, vp, pp], C.c_int),
             "fp_graph_from_vertices": ([i32, i32, vp, vp, vp, pp], C.c_int),
             "fp_read_patohlike": ([C.c_char_p, i32, i32, pp], C.c_int),
+            "fp_thin_nets": ([C.POINTER(_Hypergraph), i32, i32, pp], C.c_int),
             "fp_write_patohlike": ([vp, C.c_char_p], C.c_int),
             "fp_graph_view": ([vp, C.POINTER(_Hypergraph)], C.c_int),
             "fp_graph_destroy": ([vp], C.c_int),
@@ -206,6 +207,15 @@ class Hypergraph:
         v = self.view()
         _check(lib().fp_bfs_order(C.byref(v), int(start), _ptr(out), _ptr(far)), "fp_bfs_order")
         return out
+
+    def thin(self, mean_factor: int, min_pins: int) -> "Hypergraph":
+        """CN thinning (fp_thin_nets, the CN driver's -m 1 -n min_pins -z
+        mean_factor): the hypergraph of the nets with fewer than mean_factor x
+        mean and fewer than min_pins pins.  Host code."""
+        g = C.c_void_p()
+        v = self.view()
+        _check(lib().fp_thin_nets(C.byref(v), int(mean_factor), int(min_pins), C.byref(g)), "fp_thin_nets")
+        return _take_graph(g)
 
     def view(self) -> _Hypergraph:
         return _Hypergraph(self.nov, self.noe, self.pins, _ptr(self.vptr), _ptr(self.vnets),

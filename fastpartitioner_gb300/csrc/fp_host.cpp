@@ -311,6 +311,44 @@ int fp_bfs_order(const fp_hypergraph* h, int32_t start, int32_t* ordering, int32
   return reached == nov ? FP_OK : FP_ERR_UNSUPPORTED;
 }
 
+int fp_thin_nets(const fp_hypergraph* h, int32_t thin_mean, int32_t thin_min, fp_graph** out) {
+  if (!h || !out) return FP_ERR_INVALID;
+  *out = nullptr;
+  const int rc = fp_validate(h);
+  if (rc) return rc;
+  const int nov = h->nov, noe = h->noe;
+  // mean net size in float, as the driver computes it: pins / (noe + .0f)
+  const double mean = noe > 0 ? (double)((float)h->pins / ((float)noe + 0.0f)) : 0.0;
+  fp_graph* gg = new (std::nothrow) fp_graph;
+  if (!gg) return FP_ERR_NOMEM;
+  HostGraph& g = gg->g;
+  g.nov = nov;
+  std::vector<int> renum(noe, -1);
+  g.nptr.assign(1, 0);
+  for (int e = 0; e < noe; e++) {
+    const int degree = (int)(h->nptr[e + 1] - h->nptr[e]);
+    if (degree < thin_mean * mean && degree < thin_min) {
+      renum[e] = (int)g.src.size();
+      g.npins.insert(g.npins.end(), h->npins + h->nptr[e], h->npins + h->nptr[e + 1]);
+      g.nptr.push_back((uint32_t)g.npins.size());
+      g.src.push_back(h->src[e]);
+    }
+  }
+  g.noe = (int)g.src.size();
+  g.pins = (long long)g.npins.size();
+  // each vertex keeps its kept nets in its own net order, renumbered
+  g.vptr.assign(nov + 1, 0);
+  g.vnets.reserve(g.pins);
+  for (int v = 0; v < nov; v++) {
+    for (uint32_t k = h->vptr[v]; k < h->vptr[v + 1]; k++)
+      if (renum[h->vnets[k]] >= 0) g.vnets.push_back((uint32_t)renum[h->vnets[k]]);
+    g.vptr[v + 1] = (uint32_t)g.vnets.size();
+  }
+  if (h->weights) g.weights.assign(h->weights, h->weights + nov);
+  *out = gg;
+  return FP_OK;
+}
+
 int fp_read_patohlike(const char* path, int32_t transpose, int32_t write_cache, fp_graph** out) {
   if (!path || !out) return FP_ERR_INVALID;
   *out = nullptr;

@@ -241,6 +241,14 @@ int fp_graph_from_vertices(int32_t nov, int32_t noe, const uint32_t* vptr, const
  * MGV, MSRV drivers, TM/tm.cpp:65).  Sources: src_rule as in fp_gen_params,
  * applied to each net's pins. */
 int fp_read_patohlike(const char* path, int32_t transpose, int32_t write_cache, fp_graph** out);
+/* CN thinning (-m 1 -n thin_min -z thin_mean; replaces the driver's filter,
+ * CN/cn.cpp:201-268): keeps the nets with fewer than thin_mean x (pins / noe,
+ * in float) and fewer than thin_min pins, renumbered in order, with their pins
+ * and sources; every vertex keeps its kept nets in its own order.  The driver
+ * then runs the ordinary CN partition on the thinned hypergraph
+ * (thin_partition, CN/partition.cpp:841-1196, is partition() writing into the
+ * caller's part vector) and evaluates the six metrics on the full one. */
+int fp_thin_nets(const fp_hypergraph* h, int32_t thin_mean, int32_t thin_min, fp_graph** out);
 int fp_write_patohlike(const fp_graph* g, const char* path);
 int fp_graph_view(const fp_graph* g, fp_hypergraph* view);
 int fp_graph_destroy(fp_graph* g);
