@@ -15,6 +15,7 @@ import ctypes as C
 import os
 import re
 import subprocess
+import sys
 import tempfile
 from pathlib import Path
 
@@ -49,13 +50,20 @@ class _Run(C.Structure):
 
 
 def build(quiet: bool = True) -> None:
-    """Builds libfporacle.so and, where the reference sources are reachable, the
-    reference harness binaries."""
-    res = subprocess.run(["make", "-C", str(HERE), "-j8", "all"], capture_output=True, text=True)
+    """Builds libfporacle.so (required) and, where the reference sources are
+    reachable, the reference harness binaries (optional: the tests that need
+    one skip when it is missing, so a harness that does not build only warns)."""
+    res = subprocess.run(["make", "-C", str(HERE), "-j8", "oracle"], capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError(f"oracle build failed:\n{res.stdout}\n{res.stderr}")
     if not quiet:
         print(res.stdout)
+    ref = subprocess.run(["make", "-C", str(HERE), "-j8", "-k", "ref"], capture_output=True, text=True)
+    if ref.returncode != 0:
+        print(f"warning: some reference harnesses did not build:\n{ref.stdout[-2000:]}\n{ref.stderr[-2000:]}",
+              file=sys.stderr)
+    elif not quiet:
+        print(ref.stdout)
 
 
 _lib = None
