@@ -168,6 +168,23 @@ KERNEL_OF = {"TV": "spec_ldg_kernel", "MSV": "spec_ldg_kernel", "MSRV": "spec_ld
              "CN": "spec_cn_kernel", "TM": "spec_msg_kernel", "MSM": "spec_msg_kernel"}
 
 
+def whole_job(units_per_rank, seconds, device="cpu"):
+    """Whole-job throughput of independent replicas: every rank processes the
+    same `units_per_rank`, the job takes as long as its slowest rank (an
+    all-reduce MAX of `seconds` over the process group when one is up; the
+    tensor lives on `device`, "cpu" for gloo, "cuda:N" for nccl), and the value
+    is all ranks' units over that time.  Returns (value, max seconds, ranks)."""
+    import torch
+    import torch.distributed as tdist
+    nranks = 1
+    if tdist.is_available() and tdist.is_initialized():
+        t = torch.tensor([seconds], dtype=torch.float64, device=device)
+        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+        seconds = float(t.item())
+        nranks = tdist.get_world_size()
+    return units_per_rank * nranks / seconds, seconds, nranks
+
+
 def run_ours(args):
     import torch
     import fastpartitioner_gb300 as fp
@@ -253,14 +270,8 @@ def run_ours(args):
     torch.cuda.synchronize()
     if dist:
         tdist.barrier()
-    total_t = sum(sum(v) for v in per_metric.values())
-    if dist:
-        tt = torch.tensor([total_t], device=f"cuda:{device}", dtype=torch.float64)
-        tdist.all_reduce(tt, op=tdist.ReduceOp.MAX)
-        total_t = float(tt.item())
-    nranks = int(os.environ.get("WORLD_SIZE", "1")) if dist else 1
-    work = hg.pins * len(metrics) * args.steps
-    value = work * nranks / total_t
+    value, total_t, nranks = whole_job(hg.pins * len(metrics) * args.steps,
+                                       sum(sum(v) for v in per_metric.values()), f"cuda:{device}")
 
     # e2e: the call a user makes per metric -- host state -> device, all passes,
     # part vector -> host -- timed on the wall clock, one schedule.
@@ -277,7 +288,7 @@ def run_ours(args):
         e2e_t += t1 - t0
         h2d += inst.state_bytes()
         d2h += pv.nbytes
-    e2e_value = hg.pins * passes * len(metrics) * nranks / e2e_t
+    e2e_value, e2e_t, _ = whole_job(hg.pins * passes * len(metrics), e2e_t, f"cuda:{device}")
 
     # Roofline per kernel: algorithmic bytes of one launch (one pass of one
     # metric) / its CUDA-event duration; the dominant kernel is the one with the
