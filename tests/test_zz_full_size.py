@@ -1,0 +1,64 @@
+"""Bit-exact parity at the benchmark's full size: the zipf4m workload (4,194,304
+vertices and nets, 21.35 M pins, degree weights, K = 256, eps factor 1.05),
+two refinement passes of every metric on the GPU, called through the C ABI,
+against the CPU oracle on the same instance.
+
+Checked per metric: the part vector after the stream and after refinement,
+every net's λ and its ordered (part, count) list, the moves per pass, the part
+sizes and all six metric values before and after.  The six oracle runs go on
+threads (the oracle's ctypes calls release the GIL) while the GPU instances
+run, so the whole test takes about a minute."""
+import sys
+from concurrent.futures import ThreadPoolExecutor
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from conftest import METRICS
+from test_gpu_parity import run_gpu
+
+ROOT = Path(__file__).resolve().parents[1]
+sys.path.insert(0, str(ROOT))
+
+pytestmark = pytest.mark.gpu
+PASSES = 2
+
+
+def listed(hg, ln):
+    """Mask of the listed slots: slot i of net e (in [nptr[e], nptr[e+1])) is
+    listed when i - nptr[e] < λ(e)."""
+    sizes = np.diff(hg.nptr).astype(np.int64)
+    first = np.repeat(hg.nptr[:-1].astype(np.int64), sizes)
+    return np.arange(hg.pins, dtype=np.int64) - first < np.repeat(np.asarray(ln, np.int64), sizes)
+
+
+def compare(hg, g, o, tag):
+    """Every observable of one GPU run `g` (run_gpu's dict) against the oracle's `o`."""
+    np.testing.assert_array_equal(g["part_vec_init"], o["part_vec_init"], err_msg=tag)
+    np.testing.assert_array_equal(g["part_vec"], o["part_vec"], err_msg=tag)
+    np.testing.assert_array_equal(g["ep_len"], o["ep_len"], err_msg=tag)
+    keep = listed(hg, o["ep_len"])
+    np.testing.assert_array_equal(g["ep_part"][keep], o["ep_part"][keep], err_msg=tag)
+    np.testing.assert_array_equal(g["ep_cnt"][keep], o["ep_cnt"][keep], err_msg=tag)
+    np.testing.assert_array_equal(g["moves"], o["moves"], err_msg=tag)
+    assert g["metrics_init"] == o["metrics_init"], tag
+    assert g["metrics_final"] == o["metrics_final"], tag
+    w = np.ones(hg.nov, np.int64) if hg.weights is None else hg.weights.astype(np.int64)
+    np.testing.assert_array_equal(g["sizes"], np.bincount(o["part_vec"], weights=w, minlength=len(g["sizes"])),
+                                  err_msg=tag)
+
+
+def test_full_size_workload_matches_oracle(fp, orc, gpu_engine):
+    import bench
+    w = bench.WORKLOADS["zipf4m"]
+    hg = fp.generate(bench.spec_for(fp, w))
+    assert (hg.nov, hg.noe, w["K"]) == (4_194_304, 4_194_304, 256)
+    with ThreadPoolExecutor(len(METRICS)) as ex:
+        futs = {m: ex.submit(orc.run_oracle, hg, w["K"], m, PASSES, w["eps"]) for m in METRICS}
+        for m in METRICS:
+            g = run_gpu(gpu_engine, hg, w["K"], m, PASSES, eps=w["eps"])
+            o = futs.pop(m).result()
+            assert o["status"] == 0, m
+            compare(hg, g, o, f"zipf4m {m}")
+            del g, o
