@@ -46,7 +46,18 @@ WORKLOADS = {
                eps=1.05, passes=10, seed=0),
     "uniform16k": dict(nov=16_384, noe=16_384, alpha=0.0, lo=2, hi=16, beta=0.0, weight_rule=0, K=8, eps=1.03,
                passes=5, seed=0),
+    # high-K heavy-tail stress of the message and send+receive volume metrics:
+    # ~119 M pins, nets up to 100,000 pins, uniform vertex popularity
+    "zipf16m_k1024": dict(nov=16_777_216, noe=8_388_608, alpha=1.9, lo=2, hi=100_000, beta=0.0, weight_rule=0,
+               K=1024, eps=1.05, passes=10, seed=0, metrics="TM,MSRV"),
 }
+
+
+def metrics_for(w, arg):
+    """The metrics a run covers: --metrics, else the workload's own list, else all six."""
+    if arg:
+        return arg.split(",")
+    return w["metrics"].split(",") if "metrics" in w else list(METRICS)
 
 
 def measured_traffic(kernel, config, scale):
@@ -202,7 +213,7 @@ def run_ours(args):
         torch.cuda.set_device(0)
     w = WORKLOADS[args.config]
     passes = args.passes or w["passes"]
-    metrics = args.metrics.split(",") if args.metrics else METRICS
+    metrics = metrics_for(w, args.metrics)
     t_gen = time.time()
     hg = fp.generate(spec_for(fp, w, args.scale))
     t_gen = time.time() - t_gen
@@ -389,7 +400,7 @@ def cpu_baseline(fp, w, args):
     threads = os.cpu_count() or 1
     scale = args.cpu_scale
     passes = args.cpu_passes
-    metrics = args.metrics.split(",") if args.metrics else METRICS
+    metrics = metrics_for(w, args.metrics)
     work, t, kind, hg = reference_timing(w, args, scale, passes, metrics, threads)
     return {"value": work / t, "unit": "pins/s", "cores": threads if kind == "reference" else 1, "kind": kind,
             "sample": f"{hg.nov} vertices / {hg.pins} pins ({args.config} distribution at 1/{scale} scale, unit "
@@ -407,7 +418,7 @@ def run_reference_arm(args):
     except Exception:
         pass
     w = WORKLOADS[args.config]
-    metrics = args.metrics.split(",") if args.metrics else METRICS
+    metrics = metrics_for(w, args.metrics)
     threads = os.cpu_count() or 1
     passes = args.cpu_passes
     vals = []

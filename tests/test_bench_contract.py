@@ -20,6 +20,10 @@ def test_workloads_are_named_by_shape_and_complete():
         assert w["K"] >= 2 and w["passes"] >= 1 and w["eps"] > 1.0, name
     z = bench.WORKLOADS["zipf4m"]
     assert (z["nov"], z["noe"], z["K"], z["passes"]) == (4_194_304, 4_194_304, 256, 10)
+    s = bench.WORKLOADS["zipf16m_k1024"]
+    assert (s["nov"], s["noe"], s["K"], s["hi"], s["alpha"]) == (16_777_216, 8_388_608, 1024, 100_000, 1.9)
+    assert bench.metrics_for(s, "") == ["TM", "MSRV"]
+    assert bench.metrics_for(z, "") == bench.METRICS and bench.metrics_for(z, "TV,CN") == ["TV", "CN"]
 
 
 def test_traffic_comes_from_the_committed_summary():

@@ -30,3 +30,33 @@ def test_oracle_equals_reference(fp, orc, name, mk, seed):
             np.testing.assert_array_equal(orc.flat_lists(hg, o["ep_len"], o["ep_part"]), r["lists"],
                                           err_msg=f"{m} {K}")
             assert o["metrics_final"] == r["metrics_final"], (m, K)
+
+
+# The benchmark's workload shapes at sizes the reference finishes in seconds:
+# uniform16k at full size (eps factor 1.05, which the reference fixes,
+# TV/partition.cpp:159) and zipf16m_k1024 at 1/64 scale (K = 1024, nets up to
+# 100,000 pins).  The six metrics run on threads (each is a subprocess).
+SHAPES = [("uniform16k", 1, 5), ("zipf16m_k1024", 64, 2)]
+
+
+@pytest.mark.parametrize("name,scale,passes", SHAPES, ids=[s[0] for s in SHAPES])
+def test_oracle_equals_reference_on_workload_shapes(fp, orc, name, scale, passes):
+    if not orc.reference_available():
+        pytest.skip("reference harness not built (reference sources unavailable)")
+    from concurrent.futures import ThreadPoolExecutor
+    import bench
+    w = bench.WORKLOADS[name]
+    hg = fp.generate(bench.spec_for(fp, w, scale, unit_weights=True))
+    K = w["K"]
+
+    def both(m):
+        return orc.run_oracle(hg, K, m, passes), orc.run_reference(hg, K, m, passes)
+
+    with ThreadPoolExecutor(len(METRICS)) as ex:
+        for m, (o, r) in zip(METRICS, ex.map(both, METRICS)):
+            assert o["status"] == 0, m
+            np.testing.assert_array_equal(o["part_vec_init"], r["part_vec_init"], err_msg=m)
+            np.testing.assert_array_equal(o["part_vec"], r["part_vec"], err_msg=m)
+            np.testing.assert_array_equal(orc.flat_lists(hg, o["ep_len"], o["ep_part"]), r["lists"], err_msg=m)
+            assert o["metrics_init"] == r["metrics_init"], m
+            assert o["metrics_final"] == r["metrics_final"], m

@@ -1,13 +1,18 @@
-"""Bit-exact parity at the benchmark's full size: the zipf4m workload (4,194,304
-vertices and nets, 21.35 M pins, degree weights, K = 256, eps factor 1.05),
-two refinement passes of every metric on the GPU, called through the C ABI,
-against the CPU oracle on the same instance.
+"""Bit-exact parity on the benchmark's workloads, GPU (through the C ABI)
+against the CPU oracle on the same instance:
+
+* zipf4m at full size: 4,194,304 vertices and nets, 21.35 M pins, degree
+  weights, K = 256, eps factor 1.05, two passes of every metric;
+* uniform16k as specified: 16,384 vertices and nets, column-net pattern with
+  2-16 pins per net, unit weights, K = 8, eps factor 1.03, five passes;
+* zipf16m_k1024 at 1/64 scale: 262,144 vertices, 131,072 nets, 1.86 M pins,
+  net sizes Zipf(1.9) up to 100,000 pins, K = 1024, two passes.  At full size
+  (~119 M pins) the oracle's K = 1024 streams alone take many minutes.
 
 Checked per metric: the part vector after the stream and after refinement,
 every net's λ and its ordered (part, count) list, the moves per pass, the part
-sizes and all six metric values before and after.  The six oracle runs go on
-threads (the oracle's ctypes calls release the GIL) while the GPU instances
-run, so the whole test takes about a minute."""
+sizes and all six metric values before and after.  The oracle runs go on
+threads (its ctypes calls release the GIL) while the GPU instances run."""
 import sys
 from concurrent.futures import ThreadPoolExecutor
 from pathlib import Path
@@ -22,7 +27,13 @@ ROOT = Path(__file__).resolve().parents[1]
 sys.path.insert(0, str(ROOT))
 
 pytestmark = pytest.mark.gpu
-PASSES = 2
+
+# workload name, scale divisor, passes, expected (nov, noe)
+WORKLOADS = [
+    ("uniform16k", 1, 5, (16_384, 16_384)),
+    ("zipf16m_k1024", 64, 2, (262_144, 131_072)),
+    ("zipf4m", 1, 2, (4_194_304, 4_194_304)),
+]
 
 
 def listed(hg, ln):
@@ -49,16 +60,17 @@ def compare(hg, g, o, tag):
                                   err_msg=tag)
 
 
-def test_full_size_workload_matches_oracle(fp, orc, gpu_engine):
+@pytest.mark.parametrize("name,scale,passes,dims", WORKLOADS, ids=[w[0] for w in WORKLOADS])
+def test_workload_matches_oracle(fp, orc, gpu_engine, name, scale, passes, dims):
     import bench
-    w = bench.WORKLOADS["zipf4m"]
-    hg = fp.generate(bench.spec_for(fp, w))
-    assert (hg.nov, hg.noe, w["K"]) == (4_194_304, 4_194_304, 256)
+    w = bench.WORKLOADS[name]
+    hg = fp.generate(bench.spec_for(fp, w, scale))
+    assert (hg.nov, hg.noe) == dims
     with ThreadPoolExecutor(len(METRICS)) as ex:
-        futs = {m: ex.submit(orc.run_oracle, hg, w["K"], m, PASSES, w["eps"]) for m in METRICS}
+        futs = {m: ex.submit(orc.run_oracle, hg, w["K"], m, passes, w["eps"]) for m in METRICS}
         for m in METRICS:
-            g = run_gpu(gpu_engine, hg, w["K"], m, PASSES, eps=w["eps"])
+            g = run_gpu(gpu_engine, hg, w["K"], m, passes, eps=w["eps"])
             o = futs.pop(m).result()
             assert o["status"] == 0, m
-            compare(hg, g, o, f"zipf4m {m}")
+            compare(hg, g, o, f"{name} {m}")
             del g, o
