@@ -12,7 +12,6 @@
 
 #include "fp_internal.h"
 
-#include <climits>
 #include <algorithm>
 
 namespace fp {
@@ -39,22 +38,121 @@ inline int list_add(HostState& st, int e, int p) {
   return j;
 }
 
-int argmin_size(const std::vector<int>& sizes) {
-  int best = INT_MAX, idx = -1;
-  for (size_t i = 0; i < sizes.size(); i++)
-    if (sizes[i] < best) { best = sizes[i]; idx = (int)i; }
-  return idx;
+// list_add when `left` more of the current vertex's nets are known to list p
+// (a vertex lists no net twice): once they are found, p is appended to the
+// remaining nets without a search.
+inline int list_add_known(HostState& st, int e, int p, int& left) {
+  const int s = st.ep_start[e];
+  if (left > 0) {
+    const int j = list_find(&st.ep_part[s], st.ep_len[e], p);
+    if (j >= 0) {
+      st.ep_cnt[s + j]++;
+      left--;
+      return j;
+    }
+  }
+  const int j = st.ep_len[e]++;
+  st.ep_part[s + j] = p;
+  st.ep_cnt[s + j] = 1;
+  return j;
 }
+
+// The streams read, per (vertex, net) pair in visiting order, the net's list
+// header and then its list: two dependent misses on a random net.  A cursor
+// walks the same pair sequence ahead of the stream and requests both early:
+// headers kHdrAhead pairs ahead, lists (their header now cached) kListAhead
+// pairs ahead.
+struct PairAhead {
+  const Problem& pb;
+  const HostState& st;
+  int z = 0;
+  uint32_t i = 0, end = 0;
+  PairAhead(const Problem& p, const HostState& s) : pb(p), st(s) { seek(0); }
+  void seek(int zz) {
+    const HostGraph& g = *pb.g;
+    for (z = zz; z < g.nov; z++) {
+      const int v = pb.order[z];
+      i = g.vptr[v];
+      end = g.vptr[v + 1];
+      if (i < end) return;
+    }
+  }
+  // Net of the cursor's pair, or -1 past the last pair; then one pair on.
+  int next() {
+    if (z >= pb.g->nov) return -1;
+    const int e = (int)pb.g->vnets[i];
+    if (++i == end) seek(z + 1);
+    return e;
+  }
+};
+
+constexpr int kHdrAhead = 64;
+constexpr int kListAhead = 16;
+
+struct Prefetcher {
+  PairAhead hdr, list;
+  Prefetcher(const Problem& pb, const HostState& st) : hdr(pb, st), list(pb, st) {
+    for (int k = 0; k < kHdrAhead; k++) header(hdr.next());
+    for (int k = 0; k < kListAhead; k++) body(list.next());
+  }
+  void header(int e) {
+    if (e < 0) return;
+    __builtin_prefetch(&hdr.st.ep_len[e]);
+    __builtin_prefetch(&hdr.st.ep_start[e]);
+  }
+  void body(int e) {
+    if (e < 0) return;
+    const int s = list.st.ep_start[e];
+    __builtin_prefetch(&list.st.ep_part[s]);
+    __builtin_prefetch(&list.st.ep_cnt[s]);
+  }
+  // Called once per pair the stream reads.
+  void step() {
+    header(hdr.next());
+    body(list.next());
+  }
+};
+
+// The least-loaded part (the lowest index among the smallest sizes), the
+// streams' fallback: a tournament tree over the K part sizes, updated after each
+// assignment in O(log K).  Most vertices of a heavy-tailed instance have no
+// nets and take this fallback, so a scan of all K sizes per vertex would
+// dominate the stream.
+struct LeastLoaded {
+  const std::vector<int>& sizes;
+  int n = 1;
+  std::vector<int> win;   // win[x]: winning part of node x's subtree, -1 = padding
+  explicit LeastLoaded(const std::vector<int>& s) : sizes(s) {
+    const int K = (int)s.size();
+    while (n < K) n <<= 1;
+    win.assign(2 * (size_t)n, -1);
+    for (int k = 0; k < K; k++) win[n + k] = k;
+    for (int x = n - 1; x >= 1; x--) win[x] = pick(win[2 * x], win[2 * x + 1]);
+  }
+  // a from the left subtree (lower indices), b from the right one
+  int pick(int a, int b) const {
+    if (a < 0) return b;
+    if (b < 0) return a;
+    return sizes[b] < sizes[a] ? b : a;
+  }
+  void changed(int k) {
+    for (int x = (n + k) >> 1; x >= 1; x >>= 1) win[x] = pick(win[2 * x], win[2 * x + 1]);
+  }
+  int argmin() const { return win[1]; }
+};
 
 // LDG decision over the parts seen by the current vertex, in first-seen order:
 // highest score * (1 - size / C) above zero, ties to the smaller part, then to
 // the earlier part; if no part scores, the least loaded part (lowest index).
 int ldg_decide(const Problem& pb, const HostState& st, const std::vector<int>& seen, int nseen,
-               const std::vector<int>& count) {
+               const std::vector<int>& count, const LeastLoaded& least) {
   double best = 0;
   int arg = -1;
   for (int i = 0; i < nseen; i++) {
     int p = seen[i];
+    // Sizes are never negative, so a score is at most its count: a part whose
+    // count is below the best score can neither beat nor tie it.
+    if (arg >= 0 && count[p] < best) continue;
     double pen = 1 - (1.0 * st.part_sizes[p] / pb.C);
     double sc = (double)count[p] * pen;
     if (sc > 0 && (arg == -1 || sc > best || (sc == best && st.part_sizes[p] < st.part_sizes[arg]))) {
@@ -62,7 +160,7 @@ int ldg_decide(const Problem& pb, const HostState& st, const std::vector<int>& s
       arg = p;
     }
   }
-  return arg >= 0 ? arg : argmin_size(st.part_sizes);
+  return arg >= 0 ? arg : least.argmin();
 }
 
 void state_alloc(const Problem& pb, HostState& st) {
@@ -86,34 +184,42 @@ int stream_ldg(const Problem& pb, HostState& st) {
   const bool vol = pb.metric == FP_METRIC_MSV || pb.metric == FP_METRIC_MSRV;
   const bool rv = pb.metric == FP_METRIC_MSRV;
   const int max_pw = (int)(pb.xw + (pb.xw * 0.1));
-  std::vector<int> seen(K), count(K, 0);
+  // count[p]: listed entries of part p over v's nets (zero between vertices);
+  // seen: the parts in first-seen order (one spare slot for the branch-free
+  // append).  marker[p] = v for every part v saw, as the reference leaves it.
+  std::vector<int> seen(K + 1), count(K, 0);
+  LeastLoaded least(st.part_sizes);
+  Prefetcher pf(pb, st);
   for (int z = 0; z < g.nov; z++) {
     const int v = pb.order[z];
     int nseen = 0;
     for (uint32_t i = g.vptr[v]; i < g.vptr[v + 1]; i++) {
+      pf.step();
       const int e = (int)g.vnets[i];
-      const int s = st.ep_start[e];
-      for (int j = 0; j < st.ep_len[e]; j++) {
-        const int p = st.ep_part[s + j];
-        if (st.marker[p] != v) {
-          st.marker[p] = v;
-          count[p] = 1;
-          seen[nseen++] = p;
-        } else {
-          count[p]++;
-        }
+      const int* lp = &st.ep_part[st.ep_start[e]];
+      const int len = st.ep_len[e];
+      for (int j = 0; j < len; j++) {
+        const int p = lp[j];
+        seen[nseen] = p;
+        nseen += count[p]++ == 0;
       }
     }
-    const int d = ldg_decide(pb, st, seen, nseen, count);
+    const int d = ldg_decide(pb, st, seen, nseen, count, least);
     // TV's LDG2 sends a part above max_pw back to the vertex's current part,
     // which is -1 during the stream (TV/partition.cpp:135-138).
     if (pb.metric == FP_METRIC_TV && st.part_sizes[d] > max_pw) return FP_ERR_UNSUPPORTED;
+    int left = count[d];   // nets of v that list d
+    for (int i = 0; i < nseen; i++) {
+      st.marker[seen[i]] = v;
+      count[seen[i]] = 0;
+    }
     st.part_sizes[d] += pb.w[v];
+    if (pb.w[v]) least.changed(d);
     st.part_vec[v] = d;
     for (uint32_t i = g.vptr[v]; i < g.vptr[v + 1]; i++) {
       const int e = (int)g.vnets[i];
       if (!vol) {
-        list_add(st, e, d);
+        list_add_known(st, e, d, left);
         continue;
       }
       const int s = st.ep_start[e];
@@ -129,7 +235,7 @@ int stream_ldg(const Problem& pb, HostState& st) {
         }
       }
       const int before = st.ep_len[e];
-      list_add(st, e, d);
+      list_add_known(st, e, d, left);
       if (st.ep_len[e] != before && sv != v && sp != -1) {
         st.send[sp]++;
         if (rv) st.recv[d]++;
@@ -142,18 +248,22 @@ int stream_ldg(const Problem& pb, HostState& st) {
 int stream_cn(const Problem& pb, HostState& st) {
   const HostGraph& g = *pb.g;
   std::vector<int> seen(pb.K), count(pb.K, 0), mark(pb.K, -1);
+  LeastLoaded least(st.part_sizes);
+  Prefetcher pf(pb, st);
   for (int z = 0; z < g.nov; z++) {
     const int v = pb.order[z];
     int nseen = 0;
     for (uint32_t i = g.vptr[v]; i < g.vptr[v + 1]; i++) {
+      pf.step();
       const int e = (int)g.vnets[i];
       if (st.ep_len[e] != 1) continue;
       const int p = st.ep_part[st.ep_start[e]];
       if (mark[p] != v) { mark[p] = v; count[p] = 1; seen[nseen++] = p; }
       else count[p]++;
     }
-    const int d = ldg_decide(pb, st, seen, nseen, count);
+    const int d = ldg_decide(pb, st, seen, nseen, count, least);
     st.part_sizes[d] += pb.w[v];
+    if (pb.w[v]) least.changed(d);
     st.part_vec[v] = d;
     for (uint32_t i = g.vptr[v]; i < g.vptr[v + 1]; i++) list_add(st, (int)g.vnets[i], d);
   }
@@ -177,6 +287,7 @@ int stream_msg(const Problem& pb, HostState& st) {
   std::vector<int> smark(K, -1), src_part(g.noe, -1), mult(K, 0);
   std::vector<int> act_parts, act_nets, own_nets, mparts, dcount;
   std::vector<uint64_t> act(W), planes;
+  LeastLoaded least(st.part_sizes);
   for (int z = 0; z < g.nov; z++) {
     const int v = pb.order[z];
     act_parts.clear();
@@ -209,6 +320,12 @@ int stream_msg(const Problem& pb, HostState& st) {
         mmax = std::max(mmax, mult[p]);
       }
     }
+    int best = -1, arg = -1;
+    // With no active source part and no listed part on its own nets, a vertex
+    // saves nothing anywhere: the loop below would pick the smallest part below
+    // capacity (lowest index first), which is the least-loaded part, the same
+    // as the fallback when no part is below capacity.
+    const bool idle = act_parts.empty() && mmax == 0;
     int nplanes = 0;
     while ((mmax >> nplanes) != 0) nplanes++;
     planes.assign((size_t)nplanes * W, 0);
@@ -216,8 +333,7 @@ int stream_msg(const Problem& pb, HostState& st) {
       for (int b = 0; b < nplanes; b++)
         if ((mult[p] >> b) & 1) planes[(size_t)b * W + (p >> 6)] |= 1ull << (p & 63);
     for (int p : mparts) mult[p] = 0;
-    int best = -1, arg = -1;
-    for (int k = 0; k < K; k++) {
+    for (int k = idle ? K : 0; k < K; k++) {
       if (!(st.part_sizes[k] < pb.C)) continue;
       const uint64_t* col = &pcol[(size_t)k * W];
       const uint64_t* row = &prow[(size_t)k * W];
@@ -230,9 +346,10 @@ int stream_msg(const Problem& pb, HostState& st) {
       }
       if (saved > best || (saved == best && st.part_sizes[k] < st.part_sizes[arg])) { best = saved; arg = k; }
     }
-    const int d = arg >= 0 ? arg : argmin_size(st.part_sizes);
+    const int d = arg >= 0 ? arg : least.argmin();
     st.part_vec[v] = d;
     st.part_sizes[d] += pb.w[v];
+    if (pb.w[v]) least.changed(d);
     // d's count in each of v's nets after adding v (the reference looks it up
     // again, TM/partition.cpp:210-223)
     dcount.resize(g.vptr[v + 1] - g.vptr[v]);

@@ -50,3 +50,39 @@ def test_stream_rejects_bad_arguments():
     for K, metric, eps in ((1, "TV", 1.05), (5000, "TV", 1.05), (8, 7, 1.05), (8, "TV", 0.0)):
         with pytest.raises((fp.FastPartError, ValueError)):
             fp.stream_partition(hg, K, metric, eps)
+
+
+FP_ERR_UNSUPPORTED = -5   # include/fastpart.h
+
+MORE = [
+    ("colnet_2k_K3", lambda: fp.generate(fp.GenSpec.column_net(2048, 2048, 2, 12, seed=31)), 3, 1.05),
+    ("zipf_8k_K100_weighted", lambda: fp.generate(fp.GenSpec.zipf(8000, 6000, 2.1, 2, 900, beta=1.5, weight_rule=1,
+                                                                    seed=32)), 100, 1.05),
+    ("zipf_6k_K1000", lambda: fp.generate(fp.GenSpec.zipf(6000, 5000, 1.9, 2, 300, seed=33)), 1000, 1.05),
+    ("zipf_5k_K37_tight", lambda: fp.generate(fp.GenSpec.zipf(5000, 5000, 2.5, 2, 60, beta=1.2, seed=34)), 37, 1.01),
+    # eps factor above TV's 1.1 clamp: TV's stream is unsupported, the others run
+    ("zipf_3k_K16_loose", lambda: fp.generate(fp.GenSpec.zipf(3000, 3000, 2.1, 2, 200, beta=1.5, seed=35)), 16, 1.3),
+]
+
+
+@pytest.mark.parametrize("name,mk,K,eps", MORE, ids=[c[0] for c in MORE])
+@pytest.mark.parametrize("metric", METRICS)
+def test_stream_matches_oracle_odd_K_and_status(name, mk, K, eps, metric):
+    """K off powers of two (the least-loaded tree's padding), K = 1000, zero
+    vertex weights (isolated vertices under degree weights), a tight balance
+    factor; where the oracle reports an unsupported input (a TV stream part above
+    max_pw), the library reports the same status."""
+    hg = mk()
+    o = oracle.run_oracle(hg, K, metric, 0, eps_factor=eps)
+    assert (o["status"] != 0) == (name == "zipf_3k_K16_loose" and metric == "TV")
+    if o["status"] != 0:
+        assert o["status"] == -3                    # the oracle's "unsupported"
+        with pytest.raises(fp.FastPartError) as ei:
+            fp.stream_partition(hg, K, metric, eps)
+        assert ei.value.status == FP_ERR_UNSUPPORTED
+        return
+    s = fp.stream_partition(hg, K, metric, eps)
+    np.testing.assert_array_equal(s["part_vec"], o["part_vec_init"])
+    np.testing.assert_array_equal(s["ep_ends"] - s["ep_starts"], o["ep_len_init"])
+    np.testing.assert_array_equal(s["ep_parts"], o["ep_part_init"])
+    np.testing.assert_array_equal(s["ep_cnt"], o["ep_cnt_init"])
