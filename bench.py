@@ -447,6 +447,84 @@ def run_reference_arm(args):
     print(json.dumps(line), flush=True)
 
 
+def same_results(a, b):
+    """Whether two runs gave every request the same status, part vector and metrics."""
+    for x, y in zip(a, b):
+        if x.rid != y.rid or x.status != y.status:
+            return False
+        if x.status == 0 and (not np.array_equal(x.part_vec, y.part_vec) or x.metrics != y.metrics):
+            return False
+    return len(a) == len(b)
+
+
+def run_batch(args):
+    """Mixed batch: requests of uneven size, K and metric (vertices
+    log-uniform in [1e3, 1e6], nets = vertices x U[0.5, 2], Zipf(2.2) net sizes
+    up to 2000 pins, K from {2, 4, ..., 512}, metric uniform over the six,
+    --batch-passes passes), the pipelined runner against the plain
+    per-request loop on the same requests; partitions/s on the wall clock,
+    hypergraph construction and streaming initial partitions included."""
+    import torch
+    import fastpartitioner_gb300 as fp
+    from fastpartitioner_gb300 import serving as sv
+    torch.cuda.set_device(0)
+    eng = fp.Engine(0)
+    mk = lambda: sv.mixed_batch(args.batch_n, seed=args.batch_seed, passes=args.batch_passes)
+    for _ in range(args.warmup):
+        sv.run_pipelined(eng, mk()[:4], workers=args.workers)
+    plain = sv.run_plain(eng, mk())
+    pipe = sv.run_pipelined(eng, mk(), workers=args.workers)
+    sp, spp = sv.summary(plain), sv.summary(pipe)
+    eng.close()
+    line = {
+        "metric": "partitions/s (mixed batch, pipelined vs plain per-request loop)",
+        "value": spp["partitions_per_s"], "unit": "partitions/s", "n_gpus": 1, "steps": 1,
+        "warmup": args.warmup, "ms_per_step": 1e3 * spp["makespan_s"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded generator)",
+        "config": {"workload": f"mixed batch of {args.batch_n} hypergraphs (seed {args.batch_seed}), "
+                               f"{args.batch_passes} passes each", "workers": args.workers,
+                   "plain_loop": sp, "pipelined": spp,
+                   "speedup_vs_plain": spp["partitions_per_s"] / sp["partitions_per_s"],
+                   "same_alone_and_in_the_mix": same_results(plain, pipe)},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_serve(args):
+    """Continuous serving: Poisson arrivals at --rate per second for
+    --duration seconds, each request a hypergraph as in the mixed batch with
+    vertices log-uniform in [1e3, --serve-vmax], admission by device footprint
+    under --budget-gb; against a serial queue of plain per-request calls on the
+    same arrivals.  Latency is arrival to result."""
+    import torch
+    import fastpartitioner_gb300 as fp
+    from fastpartitioner_gb300 import serving as sv
+    torch.cuda.set_device(0)
+    eng = fp.Engine(0)
+    n = max(1, int(round(args.rate * args.duration)))
+    mk = lambda: sv.poisson_arrivals(sv.mixed_batch(n, seed=args.batch_seed, vmax=args.serve_vmax,
+                                                    passes=args.batch_passes), args.rate, seed=1)
+    for _ in range(args.warmup):
+        sv.run_pipelined(eng, sv.mixed_batch(4, seed=99, vmax=20_000), workers=args.workers)
+    srv = sv.Server(eng, budget_bytes=int(args.budget_gb * 2**30), workers=args.workers, slots=args.slots)
+    served = srv.run(mk())
+    serial = sv.run_plain(eng, mk())
+    ss, sq = sv.summary(served), sv.summary(serial)
+    eng.close()
+    line = {
+        "metric": "p99 latency (continuous serving vs a serial plain-GPU queue)",
+        "value": ss["p99_latency_s"], "unit": "s", "n_gpus": 1, "steps": 1, "warmup": args.warmup,
+        "ms_per_step": 1e3 * ss["makespan_s"], "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded generator, Poisson arrivals)",
+        "config": {"workload": f"{n} requests at {args.rate}/s, vertices log-uniform in [1e3, {args.serve_vmax}], "
+                               f"{args.batch_passes} passes", "budget_gb": args.budget_gb,
+                   "workers": args.workers, "slots": args.slots, "served": ss, "serial_queue": sq,
+                   "peak_reserved_gb": srv.peak_reserved / 2**30,
+                   "same_alone_and_in_the_mix": same_results(sorted(serial, key=lambda r: r.rid), served)},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -460,8 +538,23 @@ def main():
     ap.add_argument("--cpu-scale", type=int, default=8)
     ap.add_argument("--cpu-passes", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--mode", default="refine", choices=["refine", "batch", "serve"],
+                    help="refine: the pins/s line; batch / serve: the many-request runners")
+    ap.add_argument("--batch-n", type=int, default=64)
+    ap.add_argument("--batch-seed", type=int, default=0)
+    ap.add_argument("--batch-passes", type=int, default=8)
+    ap.add_argument("--workers", type=int, default=os.cpu_count() or 8)
+    ap.add_argument("--rate", type=float, default=20.0)
+    ap.add_argument("--duration", type=float, default=5.0)
+    ap.add_argument("--serve-vmax", type=int, default=1_000_000)
+    ap.add_argument("--budget-gb", type=float, default=150.0)
+    ap.add_argument("--slots", type=int, default=32)
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.mode == "batch":
+        run_batch(args)
+    elif args.mode == "serve":
+        run_serve(args)
+    elif args.impl == "reference":
         run_reference_arm(args)
     else:
         run_ours(args)

@@ -112,6 +112,8 @@ def lib():
             "fp_ctx_set_stream": ([vp, vp], C.c_int),
             "fp_instance_create": ([vp, C.POINTER(_Hypergraph), i32, i32, dbl, pp], C.c_int),
             "fp_instance_destroy": ([vp], C.c_int),
+            "fp_instance_device_bytes": ([vp, C.POINTER(i64)], C.c_int),
+            "fp_instance_footprint": ([i32, i32, i64, i32, i32, C.POINTER(i64)], C.c_int),
             "fp_initial_partition": ([vp], C.c_int),
             "fp_refine": ([vp, i32], C.c_int),
             "fp_reset_state": ([vp], C.c_int),
@@ -500,6 +502,12 @@ class Instance:
         _check(lib().fp_last_launches(self._h, _ptr(x)), "fp_last_launches")
         return int(x[0])
 
+    def device_bytes(self) -> int:
+        """Bytes of the instance's device allocations (fp_instance_device_bytes)."""
+        out = C.c_int64()
+        _check(lib().fp_instance_device_bytes(self._h, C.byref(out)), "fp_instance_device_bytes")
+        return int(out.value)
+
     def close(self):
         if self._h:
             lib().fp_instance_destroy(self._h)
@@ -519,6 +527,15 @@ class Instance:
 
 
 NOALLOC_MAX_K = 1024   # FP_NOALLOC_MAX_K
+
+
+def footprint(nov: int, noe: int, pins: int, K: int, metric) -> int:
+    """Device bytes an instance of these sizes allocates (fp_instance_footprint);
+    no device needed."""
+    out = C.c_int64()
+    _check(lib().fp_instance_footprint(int(nov), int(noe), int(pins), int(K), metric_id(metric), C.byref(out)),
+           "fp_instance_footprint")
+    return int(out.value)
 
 
 def stream_partition(hg: Hypergraph, K: int, metric, eps: float = 1.05) -> dict:

@@ -93,6 +93,7 @@ struct fp_instance {
   bool has_state = false;
   DevInstance d{};
   std::vector<void*> allocs;
+  long long dev_bytes = 0;        // bytes of the device allocations in `allocs`
   void* metric_scratch = nullptr;
   long long* metric_out = nullptr;
   long long* h_moves = nullptr;   // pinned
@@ -128,6 +129,7 @@ int dalloc(fp_instance* in, T** p, size_t n) {
   cudaError_t e = cudaMalloc(&q, std::max<size_t>(n, 1) * sizeof(T));
   if (e != cudaSuccess) return cuda_status(e);
   in->allocs.push_back(q);
+  in->dev_bytes += (long long)(std::max<size_t>(n, 1) * sizeof(T));
   *p = static_cast<T*>(q);
   return FP_OK;
 }
@@ -456,6 +458,7 @@ int fp_instance_create(fp_ctx* ctx, const fp_hypergraph* h, int32_t K, int32_t m
   cudaError_t e = cudaMalloc(&ms, metrics_scratch_bytes(K));
   if (e != cudaSuccess) { fp_instance_destroy(in); return cuda_status(e); }
   in->allocs.push_back(ms);
+  in->dev_bytes += (long long)metrics_scratch_bytes(K);
   in->metric_scratch = ms;
   in->sb.wmax = kSpecWindow;
   in->sb.ctab_mask = ldg ? (unsigned)(ctab - 1) : 0u;
@@ -498,6 +501,57 @@ int fp_instance_create(fp_ctx* ctx, const fp_hypergraph* h, int32_t K, int32_t m
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) { fp_instance_destroy(in); return cuda_status(e); }
   *out = in;
+  return FP_OK;
+}
+
+int fp_instance_device_bytes(fp_instance* in, int64_t* bytes) {
+  if (!in || !bytes) return FP_ERR_INVALID;
+  *bytes = in->dev_bytes;
+  return FP_OK;
+}
+
+// The bytes fp_instance_create allocates on the device, from the sizes alone:
+// the same buffers, element types and counts, in the same order.
+int fp_instance_footprint(int32_t nov, int32_t noe, int64_t pins, int32_t K, int32_t metric, int64_t* bytes) {
+  if (!bytes || nov <= 0 || noe < 0 || pins < 0 || pins >= (1ll << 31) || metric < 0 || metric > 5 || K < 2 ||
+      K > kMaxK)
+    return FP_ERR_INVALID;
+  const size_t KK = (size_t)K * K, words = (size_t)(K + 31) / 32;
+  const bool msg = metric == FP_METRIC_TM || metric == FP_METRIC_MSM;
+  const bool cn = metric == FP_METRIC_CN;
+  const bool ldg = !msg && !cn;
+  const bool vfix = metric == FP_METRIC_MSV || metric == FP_METRIC_MSRV;
+  size_t ctab = 4096;
+  while (ctab < (size_t)2 * noe && ctab < ((size_t)1 << 21)) ctab <<= 1;
+  const size_t P = (size_t)pins, V = (size_t)nov, E = (size_t)noe, G2K = 2 * (size_t)kMaxGridVerts * K;
+  const size_t W = kSpecWindow, VE = std::max(V, E);
+  long long b = 0;
+  auto add = [&b](size_t n, size_t elem) { b += (long long)(std::max<size_t>(n, 1) * elem); };
+  // hypergraph, state
+  add(V + 1, 4); add(P, 4); add(E + 1, 4); add(P, 4); add(E, 4); add(V, 4); add(V, 4);
+  add(V, 4); add(E, 4); add(P, 4); add(P, 4);
+  for (int k = 0; k < 5; k++) add(K, 4);                   // part_sizes, marker, send, recv, msgs
+  add(msg ? KK : 1, 4);                                    // conn
+  for (int k = 0; k < 4; k++) add(msg ? K * words : 1, 4);  // zero and conn == 1 masks
+  add(kMaxPasses, 8); add(1, 4);                           // moves, status
+  // speculation scratch
+  add(8, 4); add(4, 4); add(kNumStats, 8); add(std::max(kSpecWindow, kMsgWindow), 4);
+  add(W, 1); add(W, 4); add(W, 4); add(W, 4); add(W, 4);   // flag, slack, vslack, wt, vd
+  add(W * words, 4);                                       // scan
+  add(ldg ? P : 1, 4); add(ldg ? P : 1, 8);                // rec, rec_slot
+  add(ldg ? ctab : 1, 8); add(ldg ? ctab : 1, 4); add(ldg ? ctab : 1, 4);
+  add(2, 4); add(W, 4);                                    // ctab_over, dfix
+  add(vfix ? P : 1, 8);                                    // rec_slot2
+  add(cn ? P : 1, 8); add(cn ? E : 1, 4); add(cn ? E : 1, 8); add(4, 4); add(cn ? V : 1, 4);
+  add(V, 1);                                               // vertex classes
+  add(W * K, 8); add(W, 4); add(W, 16); add(W, 4); add(2, 4);   // cand, ncand, mlist, midx, mcnt
+  add(kMaxSpecWarps, 4); add(kMaxSpecWarps, 4);            // wsum, vsum
+  add(E, 4); add(E, 8); add(E, 4); add(E, 4);              // claim_m, claim64, claim_c, mask_c
+  add(G2K, 4); add(G2K, 8); add(G2K, 4); add(G2K, 4); add(G2K, 4);
+  add(16 * (size_t)kMaxGridVerts, 4); add(K, 8);           // hmisc, mlast
+  add(VE, 4); add(VE, 4); add(8, 8);                       // heavy / medium positions, metric_out
+  b += (long long)metrics_scratch_bytes(K);
+  *bytes = b;
   return FP_OK;
 }
 

@@ -99,6 +99,14 @@ int fp_instance_create(fp_ctx* ctx, const fp_hypergraph* hg, int32_t K, int32_t 
                        double eps_factor, fp_instance** out);
 int fp_instance_destroy(fp_instance* inst);
 
+/* Device bytes an instance holds (the sum of its device allocations), and the
+ * bytes fp_instance_create would allocate for a hypergraph of these sizes
+ * (no device needed), for admission against a memory budget.  The allocator
+ * rounds each allocation up, so the memory taken is a little larger.  No
+ * counterpart in the reference. */
+int fp_instance_device_bytes(fp_instance* inst, int64_t* bytes);
+int fp_instance_footprint(int32_t nov, int32_t noe, int64_t pins, int32_t K, int32_t metric, int64_t* bytes);
+
 /* Streaming initial partition of the metric (host, vertex order), uploaded as
  * the refinement state: part vector, per-net ordered part lists, part sizes and
  * the metric's auxiliary state (TV marker, MSV/MSRV volumes, TM/MSM K x K
