@@ -47,6 +47,16 @@ METRIC_NAMES = ["CN", "TV", "TM", "MSM", "MSV", "MSRV"]
 # Order of fp_metrics() values: the order the reference prints them.
 OUTPUT_ORDER = ["TV", "CN", "TM", "MSM", "MSV", "MSRV"]
 
+# status codes of include/fastpart.h
+OK = 0
+ERR_INVALID = -1
+ERR_CUDA = -2
+ERR_NOMEM = -3
+ERR_DEVICE_TIMEOUT = -4
+ERR_UNSUPPORTED = -5
+ERR_STATE = -6
+ERR_IO = -7
+
 
 class FastPartError(RuntimeError):
     def __init__(self, status: int, what: str = ""):

@@ -258,40 +258,48 @@ const char* fp_strerror(int status) {
   }
 }
 
-int fp_validate(const fp_hypergraph* hg) { return validate(hg); }
+int fp_validate(const fp_hypergraph* hg) {
+  return fp::guarded([&]() -> int { return validate(hg); });
+}
 
 int fp_ctx_create(int32_t device, fp_ctx** out) {
-  if (!out) return FP_ERR_INVALID;
-  *out = nullptr;
-  int n = 0;
-  if (cudaGetDeviceCount(&n) != cudaSuccess || n <= 0) return FP_ERR_CUDA;
-  if (device < 0 || device >= n) return FP_ERR_INVALID;
-  cudaError_t e = cudaSetDevice(device);
-  if (e != cudaSuccess) return cuda_status(e);
-  fp_ctx* c = new (std::nothrow) fp_ctx;
-  if (!c) return FP_ERR_NOMEM;
-  c->device = device;
-  cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
-  cudaDeviceGetAttribute(&c->max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
-  e = cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking);
-  if (e != cudaSuccess) { delete c; return cuda_status(e); }
-  c->stream = c->own;
-  *out = c;
-  return FP_OK;
+  return fp::guarded([&]() -> int {
+    if (!out) return FP_ERR_INVALID;
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n <= 0) return FP_ERR_CUDA;
+    if (device < 0 || device >= n) return FP_ERR_INVALID;
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) return cuda_status(e);
+    fp_ctx* c = new (std::nothrow) fp_ctx;
+    if (!c) return FP_ERR_NOMEM;
+    c->device = device;
+    cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
+    cudaDeviceGetAttribute(&c->max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
+    e = cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking);
+    if (e != cudaSuccess) { delete c; return cuda_status(e); }
+    c->stream = c->own;
+    *out = c;
+    return FP_OK;
+  });
 }
 
 int fp_ctx_destroy(fp_ctx* ctx) {
-  if (!ctx) return FP_ERR_INVALID;
-  cudaSetDevice(ctx->device);
-  if (ctx->own) cudaStreamDestroy(ctx->own);
-  delete ctx;
-  return FP_OK;
+  return fp::guarded([&]() -> int {
+    if (!ctx) return FP_ERR_INVALID;
+    cudaSetDevice(ctx->device);
+    if (ctx->own) cudaStreamDestroy(ctx->own);
+    delete ctx;
+    return FP_OK;
+  });
 }
 
 int fp_ctx_set_stream(fp_ctx* ctx, void* stream) {
-  if (!ctx) return FP_ERR_INVALID;
-  ctx->stream = stream ? static_cast<cudaStream_t>(stream) : ctx->own;
-  return FP_OK;
+  return fp::guarded([&]() -> int {
+    if (!ctx) return FP_ERR_INVALID;
+    ctx->stream = stream ? static_cast<cudaStream_t>(stream) : ctx->own;
+    return FP_OK;
+  });
 }
 
 // Claims (no claim: a value above every position) and both parities of the
@@ -386,273 +394,299 @@ static int classify(fp_instance* in, long long light_work, long long super_work)
 
 int fp_instance_create(fp_ctx* ctx, const fp_hypergraph* h, int32_t K, int32_t metric, double eps_factor,
                        fp_instance** out) {
-  if (!ctx || !out || metric < 0 || metric > 5 || K < 2 || K > kMaxK || !(eps_factor > 0)) return FP_ERR_INVALID;
-  *out = nullptr;
-  fp_instance* in = new (std::nothrow) fp_instance;
-  if (!in) return FP_ERR_NOMEM;
-  in->ctx = ctx;
-  int rc = make_problem(h, K, metric, eps_factor, in->g, in->pb);   // validates h
-  if (rc) { delete in; return rc; }
-  const HostGraph& g = in->g;
-  const Problem& pb = in->pb;
+  // an exception releases the half-built instance (its device buffers included)
+  fp_instance* made = nullptr;
+  return fp::guarded([&]() -> int {
+    if (!ctx || !out || metric < 0 || metric > 5 || K < 2 || K > kMaxK || !(eps_factor > 0)) return FP_ERR_INVALID;
+    *out = nullptr;
+    fp_instance* in = new (std::nothrow) fp_instance;
+    if (!in) return FP_ERR_NOMEM;
+    made = in;
+    in->ctx = ctx;
+    int rc = make_problem(h, K, metric, eps_factor, in->g, in->pb);   // validates h
+    if (rc) { delete in; return rc; }
+    const HostGraph& g = in->g;
+    const Problem& pb = in->pb;
 
-  cudaSetDevice(ctx->device);
-  DevInstance& d = in->d;
-  d.nov = g.nov;
-  d.noe = g.noe;
-  d.pins = g.pins;
-  d.K = K;
-  d.metric = metric;
-  d.C = pb.C;
-  d.max_pw = (int)(pb.xw + (pb.xw * 0.1));
-  d.min_pw = (int)(pb.xw - (pb.xw * 0.1));
-  const size_t KK = (size_t)K * K, words = (size_t)(K + 31) / 32;
-  const bool msg = metric == FP_METRIC_TM || metric == FP_METRIC_MSM;
-  const bool cn = metric == FP_METRIC_CN;
-  const bool ldg = !msg && !cn;
-  const bool vfix = metric == FP_METRIC_MSV || metric == FP_METRIC_MSRV;   // in-window decision fixes
-  // exact count claims of the LDG engine: a table well above the entries of a
-  // round (two per count-only net of a window's movers)
-  size_t ctab = 4096;
-  while (ctab < (size_t)2 * g.noe && ctab < ((size_t)1 << 21)) ctab <<= 1;
-  uint32_t *vptr, *vnets, *nptr, *npins;
-  int *src, *w, *order;
-  if ((rc = dalloc(in, &vptr, g.nov + 1)) || (rc = dalloc(in, &vnets, g.pins)) || (rc = dalloc(in, &nptr, g.noe + 1)) ||
-      (rc = dalloc(in, &npins, g.pins)) || (rc = dalloc(in, &src, g.noe)) || (rc = dalloc(in, &w, g.nov)) ||
-      (rc = dalloc(in, &order, g.nov)) || (rc = dalloc(in, &d.part_vec, g.nov)) || (rc = dalloc(in, &d.ep_len, g.noe)) ||
-      (rc = dalloc(in, &d.ep_part, g.pins)) || (rc = dalloc(in, &d.ep_cnt, g.pins)) ||
-      (rc = dalloc(in, &d.part_sizes, K)) || (rc = dalloc(in, &d.marker, K)) || (rc = dalloc(in, &d.send, K)) ||
-      (rc = dalloc(in, &d.recv, K)) || (rc = dalloc(in, &d.msgs, K)) || (rc = dalloc(in, &d.conn, msg ? KK : 1)) ||
-      (rc = dalloc(in, &d.zrow, msg ? K * words : 1)) || (rc = dalloc(in, &d.zcol, msg ? K * words : 1)) ||
-      (rc = dalloc(in, &d.c1row, msg ? K * words : 1)) || (rc = dalloc(in, &d.c1col, msg ? K * words : 1)) ||
-      (rc = dalloc(in, &d.moves, kMaxPasses)) || (rc = dalloc(in, &d.status, 1)) ||
-      (rc = dalloc(in, &in->sb.ctl, 8)) || (rc = dalloc(in, &in->sb.bar, 4)) || (rc = dalloc(in, &in->sb.stats, kNumStats)) || (rc = dalloc(in, &in->sb.dec, std::max(kSpecWindow, kMsgWindow))) ||
-      (rc = dalloc(in, &in->sb.flag, kSpecWindow)) || (rc = dalloc(in, &in->sb.slack, kSpecWindow)) ||
-      (rc = dalloc(in, &in->sb.vslack, kSpecWindow)) || (rc = dalloc(in, &in->sb.wt, kSpecWindow)) ||
-      (rc = dalloc(in, &in->sb.vd, kSpecWindow)) || (rc = dalloc(in, &in->sb.scan, (size_t)kSpecWindow * words)) ||
-      (rc = dalloc(in, &in->sb.rec, ldg ? g.pins : 1)) || (rc = dalloc(in, &in->sb.rec_slot, ldg ? g.pins : 1)) ||
-      (rc = dalloc(in, &in->sb.ctab_key, ldg ? ctab : 1)) || (rc = dalloc(in, &in->sb.ctab_pos, ldg ? ctab : 1)) ||
-      (rc = dalloc(in, &in->sb.ctab_cnt, ldg ? ctab : 1)) ||
-      (rc = dalloc(in, &in->sb.ctab_over, 2)) || (rc = dalloc(in, &in->sb.dfix, kSpecWindow)) ||
-      (rc = dalloc(in, &in->sb.rec_slot2, vfix ? g.pins : 1)) ||
-      (rc = dalloc(in, &in->sb.cn_moved, cn ? g.pins : 1)) || (rc = dalloc(in, &in->sb.cn_kcnt, cn ? g.noe : 1)) ||
-      (rc = dalloc(in, &in->sb.cn_nets, cn ? g.noe : 1)) || (rc = dalloc(in, &in->sb.cn_cnt, 4)) ||
-      (rc = dalloc(in, &in->sb.cn_wit, cn ? g.nov : 1)) || (rc = dalloc(in, &in->vclass_d, g.nov)) ||
-      (rc = dalloc(in, &in->sb.cand, (size_t)kSpecWindow * K)) || (rc = dalloc(in, &in->sb.ncand, kSpecWindow)) ||
-      (rc = dalloc(in, &in->sb.mlist, kSpecWindow)) || (rc = dalloc(in, &in->sb.midx, kSpecWindow)) ||
-      (rc = dalloc(in, &in->sb.mcnt, 2)) ||
-      (rc = dalloc(in, &in->sb.wsum, kMaxSpecWarps)) || (rc = dalloc(in, &in->sb.vsum, kMaxSpecWarps)) ||
-      (rc = dalloc(in, &in->sb.claim_m, g.noe)) || (rc = dalloc(in, &in->sb.claim64, g.noe)) || (rc = dalloc(in, &in->sb.claim_c, g.noe)) ||
-      (rc = dalloc(in, &in->sb.mask_c, g.noe)) || (rc = dalloc(in, &in->sb.hcnt, 2 * kMaxGridVerts * K)) ||
-      (rc = dalloc(in, &in->sb.hfirst, 2 * kMaxGridVerts * K)) ||
-      (rc = dalloc(in, &in->sb.hgain, 2 * kMaxGridVerts * K)) ||
-      (rc = dalloc(in, &in->sb.hloss, 2 * kMaxGridVerts * K)) ||
-      (rc = dalloc(in, &in->sb.hadelta, 2 * kMaxGridVerts * K)) ||
-      (rc = dalloc(in, &in->sb.hmisc, 16 * kMaxGridVerts)) || (rc = dalloc(in, &in->sb.mlast, K)) || (rc = dalloc(in, &in->heavy_pos_d, std::max(g.nov, g.noe))) ||
-      (rc = dalloc(in, &in->mid_pos_d, std::max(g.nov, g.noe))) ||
-      (rc = dalloc(in, &in->metric_out, 8))) {
-    fp_instance_destroy(in);
-    return rc;
-  }
-  void* ms = nullptr;
-  cudaError_t e = cudaMalloc(&ms, metrics_scratch_bytes(K));
-  if (e != cudaSuccess) { fp_instance_destroy(in); return cuda_status(e); }
-  in->allocs.push_back(ms);
-  in->dev_bytes += (long long)metrics_scratch_bytes(K);
-  in->metric_scratch = ms;
-  in->sb.wmax = kSpecWindow;
-  in->sb.ctab_mask = ldg ? (unsigned)(ctab - 1) : 0u;
-  in->sb.wmax_msg = kMsgWindow;
-  in->sb.gmax = default_grid_verts(metric);
-  // window regrowth after a cut: twice the last valid length for MSV (cuts
-  // every few hundred positions), four times for the metrics with rarer cuts
-  in->sb.wgrow = metric == FP_METRIC_MSV ? 2 : 4;
-  in->sb.maxfix = 32;
-  in->sb.max_warps = kMaxSpecWarps;
-  in->sb.heavy_pos = in->heavy_pos_d;
-  in->sb.mid_pos = in->mid_pos_d;
-  in->sb.vclass = in->vclass_d;
-  {
-    cudaStream_t s0 = ctx->stream;
-    e = clear_spec_scratch(in->sb, g.noe, K, s0);
-    if (e == cudaSuccess && cn) e = cudaMemsetAsync(in->sb.cn_wit, 0xff, sizeof(int) * g.nov, s0);   // no witnesses
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s0);
+    cudaSetDevice(ctx->device);
+    DevInstance& d = in->d;
+    d.nov = g.nov;
+    d.noe = g.noe;
+    d.pins = g.pins;
+    d.K = K;
+    d.metric = metric;
+    d.C = pb.C;
+    d.max_pw = (int)(pb.xw + (pb.xw * 0.1));
+    d.min_pw = (int)(pb.xw - (pb.xw * 0.1));
+    const size_t KK = (size_t)K * K, words = (size_t)(K + 31) / 32;
+    const bool msg = metric == FP_METRIC_TM || metric == FP_METRIC_MSM;
+    const bool cn = metric == FP_METRIC_CN;
+    const bool ldg = !msg && !cn;
+    const bool vfix = metric == FP_METRIC_MSV || metric == FP_METRIC_MSRV;   // in-window decision fixes
+    // exact count claims of the LDG engine: a table well above the entries of a
+    // round (two per count-only net of a window's movers)
+    size_t ctab = 4096;
+    while (ctab < (size_t)2 * g.noe && ctab < ((size_t)1 << 21)) ctab <<= 1;
+    uint32_t *vptr, *vnets, *nptr, *npins;
+    int *src, *w, *order;
+    if ((rc = dalloc(in, &vptr, g.nov + 1)) || (rc = dalloc(in, &vnets, g.pins)) || (rc = dalloc(in, &nptr, g.noe + 1)) ||
+        (rc = dalloc(in, &npins, g.pins)) || (rc = dalloc(in, &src, g.noe)) || (rc = dalloc(in, &w, g.nov)) ||
+        (rc = dalloc(in, &order, g.nov)) || (rc = dalloc(in, &d.part_vec, g.nov)) || (rc = dalloc(in, &d.ep_len, g.noe)) ||
+        (rc = dalloc(in, &d.ep_part, g.pins)) || (rc = dalloc(in, &d.ep_cnt, g.pins)) ||
+        (rc = dalloc(in, &d.part_sizes, K)) || (rc = dalloc(in, &d.marker, K)) || (rc = dalloc(in, &d.send, K)) ||
+        (rc = dalloc(in, &d.recv, K)) || (rc = dalloc(in, &d.msgs, K)) || (rc = dalloc(in, &d.conn, msg ? KK : 1)) ||
+        (rc = dalloc(in, &d.zrow, msg ? K * words : 1)) || (rc = dalloc(in, &d.zcol, msg ? K * words : 1)) ||
+        (rc = dalloc(in, &d.c1row, msg ? K * words : 1)) || (rc = dalloc(in, &d.c1col, msg ? K * words : 1)) ||
+        (rc = dalloc(in, &d.moves, kMaxPasses)) || (rc = dalloc(in, &d.status, 1)) ||
+        (rc = dalloc(in, &in->sb.ctl, 8)) || (rc = dalloc(in, &in->sb.bar, 4)) || (rc = dalloc(in, &in->sb.stats, kNumStats)) || (rc = dalloc(in, &in->sb.dec, std::max(kSpecWindow, kMsgWindow))) ||
+        (rc = dalloc(in, &in->sb.flag, kSpecWindow)) || (rc = dalloc(in, &in->sb.slack, kSpecWindow)) ||
+        (rc = dalloc(in, &in->sb.vslack, kSpecWindow)) || (rc = dalloc(in, &in->sb.wt, kSpecWindow)) ||
+        (rc = dalloc(in, &in->sb.vd, kSpecWindow)) || (rc = dalloc(in, &in->sb.scan, (size_t)kSpecWindow * words)) ||
+        (rc = dalloc(in, &in->sb.rec, ldg ? g.pins : 1)) || (rc = dalloc(in, &in->sb.rec_slot, ldg ? g.pins : 1)) ||
+        (rc = dalloc(in, &in->sb.ctab_key, ldg ? ctab : 1)) || (rc = dalloc(in, &in->sb.ctab_pos, ldg ? ctab : 1)) ||
+        (rc = dalloc(in, &in->sb.ctab_cnt, ldg ? ctab : 1)) ||
+        (rc = dalloc(in, &in->sb.ctab_over, 2)) || (rc = dalloc(in, &in->sb.dfix, kSpecWindow)) ||
+        (rc = dalloc(in, &in->sb.rec_slot2, vfix ? g.pins : 1)) ||
+        (rc = dalloc(in, &in->sb.cn_moved, cn ? g.pins : 1)) || (rc = dalloc(in, &in->sb.cn_kcnt, cn ? g.noe : 1)) ||
+        (rc = dalloc(in, &in->sb.cn_nets, cn ? g.noe : 1)) || (rc = dalloc(in, &in->sb.cn_cnt, 4)) ||
+        (rc = dalloc(in, &in->sb.cn_wit, cn ? g.nov : 1)) || (rc = dalloc(in, &in->vclass_d, g.nov)) ||
+        (rc = dalloc(in, &in->sb.cand, (size_t)kSpecWindow * K)) || (rc = dalloc(in, &in->sb.ncand, kSpecWindow)) ||
+        (rc = dalloc(in, &in->sb.mlist, kSpecWindow)) || (rc = dalloc(in, &in->sb.midx, kSpecWindow)) ||
+        (rc = dalloc(in, &in->sb.mcnt, 2)) ||
+        (rc = dalloc(in, &in->sb.wsum, kMaxSpecWarps)) || (rc = dalloc(in, &in->sb.vsum, kMaxSpecWarps)) ||
+        (rc = dalloc(in, &in->sb.claim_m, g.noe)) || (rc = dalloc(in, &in->sb.claim64, g.noe)) || (rc = dalloc(in, &in->sb.claim_c, g.noe)) ||
+        (rc = dalloc(in, &in->sb.mask_c, g.noe)) || (rc = dalloc(in, &in->sb.hcnt, 2 * kMaxGridVerts * K)) ||
+        (rc = dalloc(in, &in->sb.hfirst, 2 * kMaxGridVerts * K)) ||
+        (rc = dalloc(in, &in->sb.hgain, 2 * kMaxGridVerts * K)) ||
+        (rc = dalloc(in, &in->sb.hloss, 2 * kMaxGridVerts * K)) ||
+        (rc = dalloc(in, &in->sb.hadelta, 2 * kMaxGridVerts * K)) ||
+        (rc = dalloc(in, &in->sb.hmisc, 16 * kMaxGridVerts)) || (rc = dalloc(in, &in->sb.mlast, K)) || (rc = dalloc(in, &in->heavy_pos_d, std::max(g.nov, g.noe))) ||
+        (rc = dalloc(in, &in->mid_pos_d, std::max(g.nov, g.noe))) ||
+        (rc = dalloc(in, &in->metric_out, 8))) {
+      fp_instance_destroy(in);
+      return rc;
+    }
+    void* ms = nullptr;
+    cudaError_t e = cudaMalloc(&ms, metrics_scratch_bytes(K));
     if (e != cudaSuccess) { fp_instance_destroy(in); return cuda_status(e); }
-    rc = classify(in, metric == FP_METRIC_CN ? kCnLightPins : kLightWork,
-                  metric == FP_METRIC_CN ? kCnGridPins : default_super_work(metric));
-    if (rc) { fp_instance_destroy(in); return rc; }
-  }
-  if (cudaMallocHost(&in->h_moves, sizeof(long long) * kMaxPasses) != cudaSuccess ||
-      cudaMallocHost(&in->h_status, sizeof(int)) != cudaSuccess ||
-      cudaMallocHost(&in->h_metrics, sizeof(long long) * 8) != cudaSuccess) {
-    fp_instance_destroy(in);
-    return FP_ERR_NOMEM;
-  }
-  d.vptr = vptr; d.vnets = vnets; d.nptr = nptr; d.npins = npins; d.src = src; d.w = w; d.order = order;
-  cudaStream_t s = ctx->stream;
-  e = cudaMemcpyAsync(vptr, g.vptr.data(), sizeof(uint32_t) * (g.nov + 1), cudaMemcpyHostToDevice, s);
-  if (e == cudaSuccess && g.pins) e = cudaMemcpyAsync(vnets, g.vnets.data(), sizeof(uint32_t) * g.pins, cudaMemcpyHostToDevice, s);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(nptr, g.nptr.data(), sizeof(uint32_t) * (g.noe + 1), cudaMemcpyHostToDevice, s);
-  if (e == cudaSuccess && g.pins) e = cudaMemcpyAsync(npins, g.npins.data(), sizeof(uint32_t) * g.pins, cudaMemcpyHostToDevice, s);
-  if (e == cudaSuccess && g.noe) e = cudaMemcpyAsync(src, g.src.data(), sizeof(int) * g.noe, cudaMemcpyHostToDevice, s);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(w, pb.w.data(), sizeof(int) * g.nov, cudaMemcpyHostToDevice, s);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(order, pb.order.data(), sizeof(int) * g.nov, cudaMemcpyHostToDevice, s);
-  if (e == cudaSuccess) e = cudaMemsetAsync(d.status, 0, sizeof(int), s);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-  if (e != cudaSuccess) { fp_instance_destroy(in); return cuda_status(e); }
-  *out = in;
-  return FP_OK;
+    in->allocs.push_back(ms);
+    in->dev_bytes += (long long)metrics_scratch_bytes(K);
+    in->metric_scratch = ms;
+    in->sb.wmax = kSpecWindow;
+    in->sb.ctab_mask = ldg ? (unsigned)(ctab - 1) : 0u;
+    in->sb.wmax_msg = kMsgWindow;
+    in->sb.gmax = default_grid_verts(metric);
+    // window regrowth after a cut: twice the last valid length for MSV (cuts
+    // every few hundred positions), four times for the metrics with rarer cuts
+    in->sb.wgrow = metric == FP_METRIC_MSV ? 2 : 4;
+    in->sb.maxfix = 32;
+    in->sb.max_warps = kMaxSpecWarps;
+    in->sb.heavy_pos = in->heavy_pos_d;
+    in->sb.mid_pos = in->mid_pos_d;
+    in->sb.vclass = in->vclass_d;
+    {
+      cudaStream_t s0 = ctx->stream;
+      e = clear_spec_scratch(in->sb, g.noe, K, s0);
+      if (e == cudaSuccess && cn) e = cudaMemsetAsync(in->sb.cn_wit, 0xff, sizeof(int) * g.nov, s0);   // no witnesses
+      if (e == cudaSuccess) e = cudaStreamSynchronize(s0);
+      if (e != cudaSuccess) { fp_instance_destroy(in); return cuda_status(e); }
+      rc = classify(in, metric == FP_METRIC_CN ? kCnLightPins : kLightWork,
+                    metric == FP_METRIC_CN ? kCnGridPins : default_super_work(metric));
+      if (rc) { fp_instance_destroy(in); return rc; }
+    }
+    if (cudaMallocHost(&in->h_moves, sizeof(long long) * kMaxPasses) != cudaSuccess ||
+        cudaMallocHost(&in->h_status, sizeof(int)) != cudaSuccess ||
+        cudaMallocHost(&in->h_metrics, sizeof(long long) * 8) != cudaSuccess) {
+      fp_instance_destroy(in);
+      return FP_ERR_NOMEM;
+    }
+    d.vptr = vptr; d.vnets = vnets; d.nptr = nptr; d.npins = npins; d.src = src; d.w = w; d.order = order;
+    cudaStream_t s = ctx->stream;
+    e = cudaMemcpyAsync(vptr, g.vptr.data(), sizeof(uint32_t) * (g.nov + 1), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess && g.pins) e = cudaMemcpyAsync(vnets, g.vnets.data(), sizeof(uint32_t) * g.pins, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(nptr, g.nptr.data(), sizeof(uint32_t) * (g.noe + 1), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess && g.pins) e = cudaMemcpyAsync(npins, g.npins.data(), sizeof(uint32_t) * g.pins, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess && g.noe) e = cudaMemcpyAsync(src, g.src.data(), sizeof(int) * g.noe, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(w, pb.w.data(), sizeof(int) * g.nov, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(order, pb.order.data(), sizeof(int) * g.nov, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d.status, 0, sizeof(int), s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) { fp_instance_destroy(in); return cuda_status(e); }
+    *out = in;
+    return FP_OK;
+  }, [&] {
+    if (made) fp_instance_destroy(made);
+    if (out) *out = nullptr;
+  });
 }
 
 int fp_instance_device_bytes(fp_instance* in, int64_t* bytes) {
-  if (!in || !bytes) return FP_ERR_INVALID;
-  *bytes = in->dev_bytes;
-  return FP_OK;
+  return fp::guarded([&]() -> int {
+    if (!in || !bytes) return FP_ERR_INVALID;
+    *bytes = in->dev_bytes;
+    return FP_OK;
+  });
 }
 
 // The bytes fp_instance_create allocates on the device, from the sizes alone:
 // the same buffers, element types and counts, in the same order.
 int fp_instance_footprint(int32_t nov, int32_t noe, int64_t pins, int32_t K, int32_t metric, int64_t* bytes) {
-  if (!bytes || nov <= 0 || noe < 0 || pins < 0 || pins >= (1ll << 31) || metric < 0 || metric > 5 || K < 2 ||
-      K > kMaxK)
-    return FP_ERR_INVALID;
-  const size_t KK = (size_t)K * K, words = (size_t)(K + 31) / 32;
-  const bool msg = metric == FP_METRIC_TM || metric == FP_METRIC_MSM;
-  const bool cn = metric == FP_METRIC_CN;
-  const bool ldg = !msg && !cn;
-  const bool vfix = metric == FP_METRIC_MSV || metric == FP_METRIC_MSRV;
-  size_t ctab = 4096;
-  while (ctab < (size_t)2 * noe && ctab < ((size_t)1 << 21)) ctab <<= 1;
-  const size_t P = (size_t)pins, V = (size_t)nov, E = (size_t)noe, G2K = 2 * (size_t)kMaxGridVerts * K;
-  const size_t W = kSpecWindow, VE = std::max(V, E);
-  long long b = 0;
-  auto add = [&b](size_t n, size_t elem) { b += (long long)(std::max<size_t>(n, 1) * elem); };
-  // hypergraph, state
-  add(V + 1, 4); add(P, 4); add(E + 1, 4); add(P, 4); add(E, 4); add(V, 4); add(V, 4);
-  add(V, 4); add(E, 4); add(P, 4); add(P, 4);
-  for (int k = 0; k < 5; k++) add(K, 4);                   // part_sizes, marker, send, recv, msgs
-  add(msg ? KK : 1, 4);                                    // conn
-  for (int k = 0; k < 4; k++) add(msg ? K * words : 1, 4);  // zero and conn == 1 masks
-  add(kMaxPasses, 8); add(1, 4);                           // moves, status
-  // speculation scratch
-  add(8, 4); add(4, 4); add(kNumStats, 8); add(std::max(kSpecWindow, kMsgWindow), 4);
-  add(W, 1); add(W, 4); add(W, 4); add(W, 4); add(W, 4);   // flag, slack, vslack, wt, vd
-  add(W * words, 4);                                       // scan
-  add(ldg ? P : 1, 4); add(ldg ? P : 1, 8);                // rec, rec_slot
-  add(ldg ? ctab : 1, 8); add(ldg ? ctab : 1, 4); add(ldg ? ctab : 1, 4);
-  add(2, 4); add(W, 4);                                    // ctab_over, dfix
-  add(vfix ? P : 1, 8);                                    // rec_slot2
-  add(cn ? P : 1, 8); add(cn ? E : 1, 4); add(cn ? E : 1, 8); add(4, 4); add(cn ? V : 1, 4);
-  add(V, 1);                                               // vertex classes
-  add(W * K, 8); add(W, 4); add(W, 16); add(W, 4); add(2, 4);   // cand, ncand, mlist, midx, mcnt
-  add(kMaxSpecWarps, 4); add(kMaxSpecWarps, 4);            // wsum, vsum
-  add(E, 4); add(E, 8); add(E, 4); add(E, 4);              // claim_m, claim64, claim_c, mask_c
-  add(G2K, 4); add(G2K, 8); add(G2K, 4); add(G2K, 4); add(G2K, 4);
-  add(16 * (size_t)kMaxGridVerts, 4); add(K, 8);           // hmisc, mlast
-  add(VE, 4); add(VE, 4); add(8, 8);                       // heavy / medium positions, metric_out
-  b += (long long)metrics_scratch_bytes(K);
-  *bytes = b;
-  return FP_OK;
+  return fp::guarded([&]() -> int {
+    if (!bytes || nov <= 0 || noe < 0 || pins < 0 || pins >= (1ll << 31) || metric < 0 || metric > 5 || K < 2 ||
+        K > kMaxK)
+      return FP_ERR_INVALID;
+    const size_t KK = (size_t)K * K, words = (size_t)(K + 31) / 32;
+    const bool msg = metric == FP_METRIC_TM || metric == FP_METRIC_MSM;
+    const bool cn = metric == FP_METRIC_CN;
+    const bool ldg = !msg && !cn;
+    const bool vfix = metric == FP_METRIC_MSV || metric == FP_METRIC_MSRV;
+    size_t ctab = 4096;
+    while (ctab < (size_t)2 * noe && ctab < ((size_t)1 << 21)) ctab <<= 1;
+    const size_t P = (size_t)pins, V = (size_t)nov, E = (size_t)noe, G2K = 2 * (size_t)kMaxGridVerts * K;
+    const size_t W = kSpecWindow, VE = std::max(V, E);
+    long long b = 0;
+    auto add = [&b](size_t n, size_t elem) { b += (long long)(std::max<size_t>(n, 1) * elem); };
+    // hypergraph, state
+    add(V + 1, 4); add(P, 4); add(E + 1, 4); add(P, 4); add(E, 4); add(V, 4); add(V, 4);
+    add(V, 4); add(E, 4); add(P, 4); add(P, 4);
+    for (int k = 0; k < 5; k++) add(K, 4);                   // part_sizes, marker, send, recv, msgs
+    add(msg ? KK : 1, 4);                                    // conn
+    for (int k = 0; k < 4; k++) add(msg ? K * words : 1, 4);  // zero and conn == 1 masks
+    add(kMaxPasses, 8); add(1, 4);                           // moves, status
+    // speculation scratch
+    add(8, 4); add(4, 4); add(kNumStats, 8); add(std::max(kSpecWindow, kMsgWindow), 4);
+    add(W, 1); add(W, 4); add(W, 4); add(W, 4); add(W, 4);   // flag, slack, vslack, wt, vd
+    add(W * words, 4);                                       // scan
+    add(ldg ? P : 1, 4); add(ldg ? P : 1, 8);                // rec, rec_slot
+    add(ldg ? ctab : 1, 8); add(ldg ? ctab : 1, 4); add(ldg ? ctab : 1, 4);
+    add(2, 4); add(W, 4);                                    // ctab_over, dfix
+    add(vfix ? P : 1, 8);                                    // rec_slot2
+    add(cn ? P : 1, 8); add(cn ? E : 1, 4); add(cn ? E : 1, 8); add(4, 4); add(cn ? V : 1, 4);
+    add(V, 1);                                               // vertex classes
+    add(W * K, 8); add(W, 4); add(W, 16); add(W, 4); add(2, 4);   // cand, ncand, mlist, midx, mcnt
+    add(kMaxSpecWarps, 4); add(kMaxSpecWarps, 4);            // wsum, vsum
+    add(E, 4); add(E, 8); add(E, 4); add(E, 4);              // claim_m, claim64, claim_c, mask_c
+    add(G2K, 4); add(G2K, 8); add(G2K, 4); add(G2K, 4); add(G2K, 4);
+    add(16 * (size_t)kMaxGridVerts, 4); add(K, 8);           // hmisc, mlast
+    add(VE, 4); add(VE, 4); add(8, 8);                       // heavy / medium positions, metric_out
+    b += (long long)metrics_scratch_bytes(K);
+    *bytes = b;
+    return FP_OK;
+  });
 }
 
 int fp_instance_destroy(fp_instance* in) {
-  if (!in) return FP_ERR_INVALID;
-  cudaSetDevice(in->ctx->device);
-  for (void* p : in->allocs) cudaFree(p);
-  if (in->h_moves) cudaFreeHost(in->h_moves);
-  if (in->h_status) cudaFreeHost(in->h_status);
-  if (in->h_metrics) cudaFreeHost(in->h_metrics);
-  delete in;
-  return FP_OK;
+  return fp::guarded([&]() -> int {
+    if (!in) return FP_ERR_INVALID;
+    cudaSetDevice(in->ctx->device);
+    for (void* p : in->allocs) cudaFree(p);
+    if (in->h_moves) cudaFreeHost(in->h_moves);
+    if (in->h_status) cudaFreeHost(in->h_status);
+    if (in->h_metrics) cudaFreeHost(in->h_metrics);
+    delete in;
+    return FP_OK;
+  });
 }
 
 int fp_initial_partition(fp_instance* in) {
-  if (!in) return FP_ERR_INVALID;
-  int rc = initial_partition(in->pb, in->st);
-  if (rc) return rc;
-  cudaSetDevice(in->ctx->device);
-  rc = upload_state(in);
-  if (rc) return rc;
-  in->has_state = true;
-  return FP_OK;
+  return fp::guarded([&]() -> int {
+    if (!in) return FP_ERR_INVALID;
+    int rc = initial_partition(in->pb, in->st);
+    if (rc) return rc;
+    cudaSetDevice(in->ctx->device);
+    rc = upload_state(in);
+    if (rc) return rc;
+    in->has_state = true;
+    return FP_OK;
+  });
 }
 
 int fp_reset_state(fp_instance* in) {
-  if (!in) return FP_ERR_INVALID;
-  if (!in->has_state) return FP_ERR_STATE;
-  cudaSetDevice(in->ctx->device);
-  return upload_state(in);
+  return fp::guarded([&]() -> int {
+    if (!in) return FP_ERR_INVALID;
+    if (!in->has_state) return FP_ERR_STATE;
+    cudaSetDevice(in->ctx->device);
+    return upload_state(in);
+  });
 }
 
 int fp_refine(fp_instance* in, int32_t passes) {
-  if (!in || passes < 0 || passes > kMaxPasses) return FP_ERR_INVALID;
-  if (!in->has_state) return FP_ERR_STATE;
-  if (passes == 0) { in->last_passes = 0; in->last_launches = 0; return FP_OK; }
-  cudaSetDevice(in->ctx->device);
-  cudaStream_t s = in->ctx->stream;
-  cudaError_t e = cudaMemsetAsync(in->d.moves, 0, sizeof(long long) * passes, s);
-  if (e == cudaSuccess) e = cudaMemsetAsync(in->d.status, 0, sizeof(int), s);
-  const bool spec =
-      in->engine == FP_ENGINE_AUTO &&
-      spec_supported(in->pb.metric, in->pb.K, in->ctx->max_smem, in->g.nov, in->g.noe);
-  if (spec) {
-    static const int none[8] = {0x7fffffff, 0x7fffffff, 0x7fffffff, 0x7fffffff,
-                                0x7fffffff, 0x7fffffff, 0x7fffffff, 0x7fffffff};
-    if (e == cudaSuccess) e = cudaMemcpyAsync(in->sb.ctl, none, sizeof(none), cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess) e = cudaMemsetAsync(in->sb.bar, 0, sizeof(unsigned) * 4, s);
-    if (e == cudaSuccess) e = cudaMemsetAsync(in->sb.stats, 0, sizeof(unsigned long long) * kNumStats, s);
-    if (e == cudaSuccess) e = clear_spec_scratch(in->sb, in->g.noe, in->pb.K, s);
-    if (e == cudaSuccess) {
-      if (in->pb.metric == FP_METRIC_CN) {
-        e = cudaMemsetAsync(in->sb.claim64, 0, sizeof(unsigned long long) * std::max(in->g.noe, 1), s);
-        if (e == cudaSuccess) e = cudaMemsetAsync(in->sb.cn_kcnt, 0, sizeof(int) * std::max(in->g.noe, 1), s);
-        if (e == cudaSuccess) e = cudaMemsetAsync(in->sb.cn_cnt, 0, sizeof(int) * 4, s);
-        if (e == cudaSuccess) e = launch_spec_cn(in->d, in->sb, passes, in->ctx->num_sms, s, &in->last_grid);
-      } else if (in->pb.metric == FP_METRIC_TM || in->pb.metric == FP_METRIC_MSM) {
-        e = launch_spec_msg(in->d, in->sb, passes, in->ctx->num_sms, s, &in->last_grid);
-      } else {
-        e = launch_spec_ldg(in->d, in->sb, passes, in->ctx->num_sms, s, &in->last_grid);
+  return fp::guarded([&]() -> int {
+    if (!in || passes < 0 || passes > kMaxPasses) return FP_ERR_INVALID;
+    if (!in->has_state) return FP_ERR_STATE;
+    if (passes == 0) { in->last_passes = 0; in->last_launches = 0; return FP_OK; }
+    cudaSetDevice(in->ctx->device);
+    cudaStream_t s = in->ctx->stream;
+    cudaError_t e = cudaMemsetAsync(in->d.moves, 0, sizeof(long long) * passes, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(in->d.status, 0, sizeof(int), s);
+    const bool spec =
+        in->engine == FP_ENGINE_AUTO &&
+        spec_supported(in->pb.metric, in->pb.K, in->ctx->max_smem, in->g.nov, in->g.noe);
+    if (spec) {
+      static const int none[8] = {0x7fffffff, 0x7fffffff, 0x7fffffff, 0x7fffffff,
+                                  0x7fffffff, 0x7fffffff, 0x7fffffff, 0x7fffffff};
+      if (e == cudaSuccess) e = cudaMemcpyAsync(in->sb.ctl, none, sizeof(none), cudaMemcpyHostToDevice, s);
+      if (e == cudaSuccess) e = cudaMemsetAsync(in->sb.bar, 0, sizeof(unsigned) * 4, s);
+      if (e == cudaSuccess) e = cudaMemsetAsync(in->sb.stats, 0, sizeof(unsigned long long) * kNumStats, s);
+      if (e == cudaSuccess) e = clear_spec_scratch(in->sb, in->g.noe, in->pb.K, s);
+      if (e == cudaSuccess) {
+        if (in->pb.metric == FP_METRIC_CN) {
+          e = cudaMemsetAsync(in->sb.claim64, 0, sizeof(unsigned long long) * std::max(in->g.noe, 1), s);
+          if (e == cudaSuccess) e = cudaMemsetAsync(in->sb.cn_kcnt, 0, sizeof(int) * std::max(in->g.noe, 1), s);
+          if (e == cudaSuccess) e = cudaMemsetAsync(in->sb.cn_cnt, 0, sizeof(int) * 4, s);
+          if (e == cudaSuccess) e = launch_spec_cn(in->d, in->sb, passes, in->ctx->num_sms, s, &in->last_grid);
+        } else if (in->pb.metric == FP_METRIC_TM || in->pb.metric == FP_METRIC_MSM) {
+          e = launch_spec_msg(in->d, in->sb, passes, in->ctx->num_sms, s, &in->last_grid);
+        } else {
+          e = launch_spec_ldg(in->d, in->sb, passes, in->ctx->num_sms, s, &in->last_grid);
+        }
       }
+    } else if (e == cudaSuccess) {
+      e = launch_refine(in->d, passes, s);
     }
-  } else if (e == cudaSuccess) {
-    e = launch_refine(in->d, passes, s);
-  }
-  if (e == cudaSuccess) e = cudaMemcpyAsync(in->h_status, in->d.status, sizeof(int), cudaMemcpyDeviceToHost, s);
-  if (e == cudaSuccess)
-    e = cudaMemcpyAsync(in->h_moves, in->d.moves, sizeof(long long) * passes, cudaMemcpyDeviceToHost, s);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-  if (e != cudaSuccess) return cuda_status(e);
-  in->last_passes = passes;
-  in->last_launches = 1;
-  return *in->h_status;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(in->h_status, in->d.status, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(in->h_moves, in->d.moves, sizeof(long long) * passes, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_status(e);
+    in->last_passes = passes;
+    in->last_launches = 1;
+    return *in->h_status;
+  });
 }
 
 int fp_set_classes(fp_instance* in, int64_t light_work, int64_t super_work) {
-  if (!in || light_work < 0 || super_work < light_work) return FP_ERR_INVALID;
-  cudaSetDevice(in->ctx->device);
-  return classify(in, light_work, super_work);
+  return fp::guarded([&]() -> int {
+    if (!in || light_work < 0 || super_work < light_work) return FP_ERR_INVALID;
+    cudaSetDevice(in->ctx->device);
+    return classify(in, light_work, super_work);
+  });
 }
 
 int fp_set_engine(fp_instance* in, int32_t engine) {
-  if (!in || (engine != FP_ENGINE_AUTO && engine != FP_ENGINE_SEQUENTIAL)) return FP_ERR_INVALID;
-  in->engine = engine;
-  return FP_OK;
+  return fp::guarded([&]() -> int {
+    if (!in || (engine != FP_ENGINE_AUTO && engine != FP_ENGINE_SEQUENTIAL)) return FP_ERR_INVALID;
+    in->engine = engine;
+    return FP_OK;
+  });
 }
 
 int fp_metrics(fp_instance* in, int64_t out[6]) {
-  if (!in || !out) return FP_ERR_INVALID;
-  if (!in->has_state) return FP_ERR_STATE;
-  cudaSetDevice(in->ctx->device);
-  cudaStream_t s = in->ctx->stream;
-  int launches = 0;
-  cudaError_t e = launch_metrics(in->d, in->metric_scratch, in->metric_out, in->ctx->num_sms, s, &launches);
-  if (e == cudaSuccess)
-    e = cudaMemcpyAsync(in->h_metrics, in->metric_out, sizeof(long long) * 6, cudaMemcpyDeviceToHost, s);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-  if (e != cudaSuccess) return cuda_status(e);
-  for (int i = 0; i < 6; i++) out[i] = in->h_metrics[i];
-  in->last_launches = launches;
-  return FP_OK;
+  return fp::guarded([&]() -> int {
+    if (!in || !out) return FP_ERR_INVALID;
+    if (!in->has_state) return FP_ERR_STATE;
+    cudaSetDevice(in->ctx->device);
+    cudaStream_t s = in->ctx->stream;
+    int launches = 0;
+    cudaError_t e = launch_metrics(in->d, in->metric_scratch, in->metric_out, in->ctx->num_sms, s, &launches);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(in->h_metrics, in->metric_out, sizeof(long long) * 6, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_status(e);
+    for (int i = 0; i < 6; i++) out[i] = in->h_metrics[i];
+    in->last_launches = launches;
+    return FP_OK;
+  });
 }
 
 static int d2h(fp_instance* in, void* dst, const void* src, size_t bytes) {
@@ -665,160 +699,176 @@ static int d2h(fp_instance* in, void* dst, const void* src, size_t bytes) {
 }
 
 int fp_get_partition(fp_instance* in, int32_t* part_vec) {
-  if (!in || !part_vec) return FP_ERR_INVALID;
-  if (!in->has_state) return FP_ERR_STATE;
-  return d2h(in, part_vec, in->d.part_vec, sizeof(int) * in->g.nov);
+  return fp::guarded([&]() -> int {
+    if (!in || !part_vec) return FP_ERR_INVALID;
+    if (!in->has_state) return FP_ERR_STATE;
+    return d2h(in, part_vec, in->d.part_vec, sizeof(int) * in->g.nov);
+  });
 }
 
 int fp_get_lists(fp_instance* in, int32_t* ep_len, int32_t* ep_part, int32_t* ep_cnt) {
-  if (!in) return FP_ERR_INVALID;
-  if (!in->has_state) return FP_ERR_STATE;
-  int rc = FP_OK;
-  if (ep_len && (rc = d2h(in, ep_len, in->d.ep_len, sizeof(int) * in->g.noe))) return rc;
-  if (ep_part && (rc = d2h(in, ep_part, in->d.ep_part, sizeof(int) * in->g.pins))) return rc;
-  if (ep_cnt && (rc = d2h(in, ep_cnt, in->d.ep_cnt, sizeof(int) * in->g.pins))) return rc;
-  return FP_OK;
+  return fp::guarded([&]() -> int {
+    if (!in) return FP_ERR_INVALID;
+    if (!in->has_state) return FP_ERR_STATE;
+    int rc = FP_OK;
+    if (ep_len && (rc = d2h(in, ep_len, in->d.ep_len, sizeof(int) * in->g.noe))) return rc;
+    if (ep_part && (rc = d2h(in, ep_part, in->d.ep_part, sizeof(int) * in->g.pins))) return rc;
+    if (ep_cnt && (rc = d2h(in, ep_cnt, in->d.ep_cnt, sizeof(int) * in->g.pins))) return rc;
+    return FP_OK;
+  });
 }
 
 int fp_set_state(fp_instance* in, const fp_state* s) {
-  if (!in || !s || !s->part_vec || !s->ep_starts || !s->ep_ends || !s->ep_parts || !s->ep_cnt)
-    return FP_ERR_INVALID;
-  const HostGraph& g = in->g;
-  const int K = in->pb.K, metric = in->pb.metric, nov = g.nov, noe = g.noe;
-  const bool msg = metric == FP_METRIC_TM || metric == FP_METRIC_MSM;
-  HostState st;
-  st.part_vec.assign(s->part_vec, s->part_vec + nov);
-  st.part_sizes.assign(K, 0);
-  for (int v = 0; v < nov; v++) {
-    const int p = st.part_vec[v];
-    if (p < 0 || p >= K) return FP_ERR_INVALID;
-    st.part_sizes[p] += in->pb.w[v];
-  }
-  if (s->part_sizes)
-    for (int p = 0; p < K; p++)
-      if (s->part_sizes[p] != st.part_sizes[p]) return FP_ERR_INVALID;
-  st.ep_start.assign(g.nptr.begin(), g.nptr.end());
-  st.ep_len.assign(noe, 0);
-  st.ep_part.assign(g.pins, -1);
-  st.ep_cnt.assign(g.pins, 0);
-  // Every list must hold exactly the parts of the net's pins with their counts
-  // (the reference's checkMe invariant, MSM/partition.cpp:2-68).
-  std::vector<int> mark(K, -1), count(K, 0), listed(K, -1);
-  for (int e = 0; e < noe; e++) {
-    const int b = (int)g.nptr[e], size = (int)(g.nptr[e + 1] - g.nptr[e]);
-    if (s->ep_starts[e] != b) return FP_ERR_INVALID;
-    const int len = s->ep_ends[e] - b;
-    if (len < 1 || len > size || len > K) return FP_ERR_INVALID;
-    int distinct = 0;
-    for (int k = b; k < b + size; k++) {
-      const int p = st.part_vec[g.npins[k]];
-      if (mark[p] != e) { mark[p] = e; count[p] = 0; distinct++; }
-      count[p]++;
+  return fp::guarded([&]() -> int {
+    if (!in || !s || !s->part_vec || !s->ep_starts || !s->ep_ends || !s->ep_parts || !s->ep_cnt)
+      return FP_ERR_INVALID;
+    const HostGraph& g = in->g;
+    const int K = in->pb.K, metric = in->pb.metric, nov = g.nov, noe = g.noe;
+    const bool msg = metric == FP_METRIC_TM || metric == FP_METRIC_MSM;
+    HostState st;
+    st.part_vec.assign(s->part_vec, s->part_vec + nov);
+    st.part_sizes.assign(K, 0);
+    for (int v = 0; v < nov; v++) {
+      const int p = st.part_vec[v];
+      if (p < 0 || p >= K) return FP_ERR_INVALID;
+      st.part_sizes[p] += in->pb.w[v];
     }
-    if (distinct != len) return FP_ERR_INVALID;
-    for (int j = 0; j < len; j++) {
-      const int p = s->ep_parts[b + j], c = s->ep_cnt[b + j];
-      if (p < 0 || p >= K || mark[p] != e || listed[p] == e || count[p] != c) return FP_ERR_INVALID;
-      listed[p] = e;
-      st.ep_part[b + j] = p;
-      st.ep_cnt[b + j] = c;
+    if (s->part_sizes)
+      for (int p = 0; p < K; p++)
+        if (s->part_sizes[p] != st.part_sizes[p]) return FP_ERR_INVALID;
+    st.ep_start.assign(g.nptr.begin(), g.nptr.end());
+    st.ep_len.assign(noe, 0);
+    st.ep_part.assign(g.pins, -1);
+    st.ep_cnt.assign(g.pins, 0);
+    // Every list must hold exactly the parts of the net's pins with their counts
+    // (the reference's checkMe invariant, MSM/partition.cpp:2-68).
+    std::vector<int> mark(K, -1), count(K, 0), listed(K, -1);
+    for (int e = 0; e < noe; e++) {
+      const int b = (int)g.nptr[e], size = (int)(g.nptr[e + 1] - g.nptr[e]);
+      if (s->ep_starts[e] != b) return FP_ERR_INVALID;
+      const int len = s->ep_ends[e] - b;
+      if (len < 1 || len > size || len > K) return FP_ERR_INVALID;
+      int distinct = 0;
+      for (int k = b; k < b + size; k++) {
+        const int p = st.part_vec[g.npins[k]];
+        if (mark[p] != e) { mark[p] = e; count[p] = 0; distinct++; }
+        count[p]++;
+      }
+      if (distinct != len) return FP_ERR_INVALID;
+      for (int j = 0; j < len; j++) {
+        const int p = s->ep_parts[b + j], c = s->ep_cnt[b + j];
+        if (p < 0 || p >= K || mark[p] != e || listed[p] == e || count[p] != c) return FP_ERR_INVALID;
+        listed[p] = e;
+        st.ep_part[b + j] = p;
+        st.ep_cnt[b + j] = c;
+      }
+      st.ep_len[e] = len;
     }
-    st.ep_len[e] = len;
-  }
-  st.marker.assign(K, -1);
-  if (s->marker)
-    for (int p = 0; p < K; p++) {
-      if (s->marker[p] < -1 || s->marker[p] >= nov) return FP_ERR_INVALID;
-      st.marker[p] = s->marker[p];
+    st.marker.assign(K, -1);
+    if (s->marker)
+      for (int p = 0; p < K; p++) {
+        if (s->marker[p] < -1 || s->marker[p] >= nov) return FP_ERR_INVALID;
+        st.marker[p] = s->marker[p];
+      }
+    // Volumes and messages: as given, else the count over the lists; the arrays
+    // a metric does not keep stay zero (send: MSV, MSRV; recv: MSRV).
+    const bool keep_send = metric == FP_METRIC_MSV || metric == FP_METRIC_MSRV;
+    const bool keep_recv = metric == FP_METRIC_MSRV;
+    st.send.assign(K, 0);
+    st.recv.assign(K, 0);
+    st.msgs.assign(K, 0);
+    if (msg) st.conn.assign((size_t)K * K, 0);
+    for (int e = 0; e < noe; e++) {
+      const int sp = st.part_vec[g.src[e]];
+      const int b = st.ep_start[e];
+      for (int j = 0; j < st.ep_len[e]; j++) {
+        const int p = st.ep_part[b + j];
+        if (p == sp) continue;
+        if (keep_send) st.send[sp]++;
+        if (keep_recv) st.recv[p]++;
+        if (msg) st.conn[(size_t)sp * K + p]++;
+      }
     }
-  // Volumes and messages: as given, else the count over the lists; the arrays
-  // a metric does not keep stay zero (send: MSV, MSRV; recv: MSRV).
-  const bool keep_send = metric == FP_METRIC_MSV || metric == FP_METRIC_MSRV;
-  const bool keep_recv = metric == FP_METRIC_MSRV;
-  st.send.assign(K, 0);
-  st.recv.assign(K, 0);
-  st.msgs.assign(K, 0);
-  if (msg) st.conn.assign((size_t)K * K, 0);
-  for (int e = 0; e < noe; e++) {
-    const int sp = st.part_vec[g.src[e]];
-    const int b = st.ep_start[e];
-    for (int j = 0; j < st.ep_len[e]; j++) {
-      const int p = st.ep_part[b + j];
-      if (p == sp) continue;
-      if (keep_send) st.send[sp]++;
-      if (keep_recv) st.recv[p]++;
-      if (msg) st.conn[(size_t)sp * K + p]++;
+    if (msg) {
+      if (metric == FP_METRIC_MSM)
+        for (int p = 0; p < K; p++) st.conn[(size_t)p * K + p] = -1;   // MSM/partition.cpp:101
+      if (s->conn) st.conn.assign(s->conn, s->conn + (size_t)K * K);
+      for (int a = 0; a < K; a++)
+        for (int b = 0; b < K; b++)
+          if (a != b && st.conn[(size_t)a * K + b] > 0) st.msgs[a]++;
+      if (s->msgs) st.msgs.assign(s->msgs, s->msgs + K);
     }
-  }
-  if (msg) {
-    if (metric == FP_METRIC_MSM)
-      for (int p = 0; p < K; p++) st.conn[(size_t)p * K + p] = -1;   // MSM/partition.cpp:101
-    if (s->conn) st.conn.assign(s->conn, s->conn + (size_t)K * K);
-    for (int a = 0; a < K; a++)
-      for (int b = 0; b < K; b++)
-        if (a != b && st.conn[(size_t)a * K + b] > 0) st.msgs[a]++;
-    if (s->msgs) st.msgs.assign(s->msgs, s->msgs + K);
-  }
-  if (s->send && keep_send) st.send.assign(s->send, s->send + K);
-  if (s->recv && keep_recv) st.recv.assign(s->recv, s->recv + K);
-  cudaSetDevice(in->ctx->device);
-  in->st = std::move(st);
-  in->has_state = true;
-  return upload_state(in);
+    if (s->send && keep_send) st.send.assign(s->send, s->send + K);
+    if (s->recv && keep_recv) st.recv.assign(s->recv, s->recv + K);
+    cudaSetDevice(in->ctx->device);
+    in->st = std::move(st);
+    in->has_state = true;
+    return upload_state(in);
+  });
 }
 
 int fp_get_state(fp_instance* in, fp_state* s) {
-  if (!in || !s) return FP_ERR_INVALID;
-  if (!in->has_state) return FP_ERR_STATE;
-  const HostGraph& g = in->g;
-  const int K = in->pb.K;
-  const bool msg = in->pb.metric == FP_METRIC_TM || in->pb.metric == FP_METRIC_MSM;
-  int rc = FP_OK;
-  if (s->part_vec && (rc = d2h(in, s->part_vec, in->d.part_vec, sizeof(int) * g.nov))) return rc;
-  if (s->ep_starts)
-    for (int e = 0; e < g.noe; e++) s->ep_starts[e] = (int)g.nptr[e];
-  if (s->ep_ends) {
-    if ((rc = d2h(in, s->ep_ends, in->d.ep_len, sizeof(int) * g.noe))) return rc;
-    for (int e = 0; e < g.noe; e++) s->ep_ends[e] += (int)g.nptr[e];
-  }
-  if (s->ep_parts && (rc = d2h(in, s->ep_parts, in->d.ep_part, sizeof(int) * g.pins))) return rc;
-  if (s->ep_cnt && (rc = d2h(in, s->ep_cnt, in->d.ep_cnt, sizeof(int) * g.pins))) return rc;
-  if (s->part_sizes && (rc = d2h(in, s->part_sizes, in->d.part_sizes, sizeof(int) * K))) return rc;
-  if (s->marker && (rc = d2h(in, s->marker, in->d.marker, sizeof(int) * K))) return rc;
-  if (s->send && (rc = d2h(in, s->send, in->d.send, sizeof(int) * K))) return rc;
-  if (s->recv && (rc = d2h(in, s->recv, in->d.recv, sizeof(int) * K))) return rc;
-  if (s->msgs && (rc = d2h(in, s->msgs, in->d.msgs, sizeof(int) * K))) return rc;
-  if (s->conn) {
-    if (msg) {
-      if ((rc = d2h(in, s->conn, in->d.conn, sizeof(int) * (size_t)K * K))) return rc;
-    } else {
-      std::fill(s->conn, s->conn + (size_t)K * K, 0);
+  return fp::guarded([&]() -> int {
+    if (!in || !s) return FP_ERR_INVALID;
+    if (!in->has_state) return FP_ERR_STATE;
+    const HostGraph& g = in->g;
+    const int K = in->pb.K;
+    const bool msg = in->pb.metric == FP_METRIC_TM || in->pb.metric == FP_METRIC_MSM;
+    int rc = FP_OK;
+    if (s->part_vec && (rc = d2h(in, s->part_vec, in->d.part_vec, sizeof(int) * g.nov))) return rc;
+    if (s->ep_starts)
+      for (int e = 0; e < g.noe; e++) s->ep_starts[e] = (int)g.nptr[e];
+    if (s->ep_ends) {
+      if ((rc = d2h(in, s->ep_ends, in->d.ep_len, sizeof(int) * g.noe))) return rc;
+      for (int e = 0; e < g.noe; e++) s->ep_ends[e] += (int)g.nptr[e];
     }
-  }
-  return FP_OK;
+    if (s->ep_parts && (rc = d2h(in, s->ep_parts, in->d.ep_part, sizeof(int) * g.pins))) return rc;
+    if (s->ep_cnt && (rc = d2h(in, s->ep_cnt, in->d.ep_cnt, sizeof(int) * g.pins))) return rc;
+    if (s->part_sizes && (rc = d2h(in, s->part_sizes, in->d.part_sizes, sizeof(int) * K))) return rc;
+    if (s->marker && (rc = d2h(in, s->marker, in->d.marker, sizeof(int) * K))) return rc;
+    if (s->send && (rc = d2h(in, s->send, in->d.send, sizeof(int) * K))) return rc;
+    if (s->recv && (rc = d2h(in, s->recv, in->d.recv, sizeof(int) * K))) return rc;
+    if (s->msgs && (rc = d2h(in, s->msgs, in->d.msgs, sizeof(int) * K))) return rc;
+    if (s->conn) {
+      if (msg) {
+        if ((rc = d2h(in, s->conn, in->d.conn, sizeof(int) * (size_t)K * K))) return rc;
+      } else {
+        std::fill(s->conn, s->conn + (size_t)K * K, 0);
+      }
+    }
+    return FP_OK;
+  });
 }
 
 int fp_get_part_sizes(fp_instance* in, int32_t* sizes) {
-  if (!in || !sizes) return FP_ERR_INVALID;
-  if (!in->has_state) return FP_ERR_STATE;
-  return d2h(in, sizes, in->d.part_sizes, sizeof(int) * in->pb.K);
+  return fp::guarded([&]() -> int {
+    if (!in || !sizes) return FP_ERR_INVALID;
+    if (!in->has_state) return FP_ERR_STATE;
+    return d2h(in, sizes, in->d.part_sizes, sizeof(int) * in->pb.K);
+  });
 }
 
 int fp_get_moves(fp_instance* in, int64_t* moves, int32_t n) {
-  if (!in || !moves || n < 0) return FP_ERR_INVALID;
-  for (int i = 0; i < n; i++) moves[i] = i < in->last_passes ? in->h_moves[i] : 0;
-  return FP_OK;
+  return fp::guarded([&]() -> int {
+    if (!in || !moves || n < 0) return FP_ERR_INVALID;
+    for (int i = 0; i < n; i++) moves[i] = i < in->last_passes ? in->h_moves[i] : 0;
+    return FP_OK;
+  });
 }
 
 int fp_get_stats(fp_instance* in, int64_t* out, int32_t n) {
-  if (!in || !out || n < 0 || n > kNumStats) return FP_ERR_INVALID;
-  return d2h(in, out, in->sb.stats, sizeof(int64_t) * n);
+  return fp::guarded([&]() -> int {
+    if (!in || !out || n < 0 || n > kNumStats) return FP_ERR_INVALID;
+    return d2h(in, out, in->sb.stats, sizeof(int64_t) * n);
+  });
 }
 
 int fp_last_launches(fp_instance* in, int64_t* launches) {
-  if (!in || !launches) return FP_ERR_INVALID;
-  *launches = in->last_launches;
-  return FP_OK;
+  return fp::guarded([&]() -> int {
+    if (!in || !launches) return FP_ERR_INVALID;
+    *launches = in->last_launches;
+    return FP_OK;
+  });
 }
 
 }  // extern "C"

@@ -2,8 +2,10 @@
 #pragma once
 
 #include <cstdint>
-#include <vector>
+#include <new>
 #include <string>
+#include <utility>
+#include <vector>
 
 #include "../../include/fastpart.h"
 
@@ -66,6 +68,27 @@ constexpr int kMaxK = 4096;
 // Copies a validated hypergraph into g and fills pb (weights, visiting order,
 // xw = W / K, C = xw * eps_factor) as the reference derives them.
 int make_problem(const fp_hypergraph* h, int K, int metric, double eps_factor, HostGraph& g, Problem& pb);
+
+// Runs an entry point's body and turns a C++ exception into a status code, so
+// that nothing thrown crosses the C ABI: a failed allocation is FP_ERR_NOMEM,
+// anything else FP_ERR_INVALID.  `on_throw` releases what the body had built.
+template <class Body, class Cleanup>
+int guarded(Body&& body, Cleanup&& on_throw) noexcept {
+  try {
+    return body();
+  } catch (const std::bad_alloc&) {
+    on_throw();
+    return FP_ERR_NOMEM;
+  } catch (...) {
+    on_throw();
+    return FP_ERR_INVALID;
+  }
+}
+
+template <class Body>
+int guarded(Body&& body) noexcept {
+  return guarded(std::forward<Body>(body), [] {});
+}
 
 }  // namespace fp
 

@@ -36,7 +36,7 @@ from typing import Callable, Optional
 
 import numpy as np
 
-from . import FastPartError, GenSpec, Hypergraph, footprint, generate, stream_partition
+from . import ERR_NOMEM, FastPartError, GenSpec, Hypergraph, footprint, generate, stream_partition
 
 METRIC_NAMES = ("TV", "CN", "TM", "MSM", "MSV", "MSRV")
 
@@ -223,7 +223,7 @@ class Server:
     reservations it waits for belong to earlier requests, which the GPU
     finishes in that same order."""
 
-    ERR_NOMEM = -2
+    ERR_NOMEM = ERR_NOMEM
 
     def __init__(self, engine, budget_bytes: int, workers: int = 8, slots: int = 32,
                  clock: Callable[[], float] = time.perf_counter, footprint_fn=footprint):

@@ -3,6 +3,7 @@ declares, and its host-only parts behave (no compute call needs a GPU here)."""
 import ctypes as C
 import re
 import subprocess
+import sys
 
 import numpy as np
 import pytest
@@ -84,3 +85,73 @@ def test_no_gpu_is_an_error_not_a_fallback(fp):
     with pytest.raises(fp.FastPartError) as ei:
         fp.Engine(0)
     assert ei.value.status == -2
+
+
+def test_python_status_codes_match_the_header(fp):
+    text = (ROOT / "include" / "fastpart.h").read_text()
+    codes = re.findall(r"#define FP_(OK|ERR_\w+)\s+(-?\d+)", text)
+    assert len(codes) == 8
+    for name, val in codes:
+        assert getattr(fp, name) == int(val), name
+
+
+def _plbin(path, noe, nov, pins, body=b""):
+    import struct
+    path.write_bytes(struct.pack("<IIq", noe, nov, pins) + body)
+
+
+def test_corrupt_inputs_are_rejected_not_fatal(fp, tmp_path):
+    """Headers with counts beyond int32 or the pin limit, caches shorter than
+    their header says, and CSR offsets that go backwards give a status code;
+    none makes the library allocate from the header or read past a buffer."""
+    import struct
+    cases = {
+        "huge_noe": (0x7FFFFFFF, 10, 4, b""),
+        "noe_above_int32": (0x80000001, 10, 4, b""),
+        "pins_above_limit": (2, 10, 1 << 40, b""),
+        "no_vertices": (1, 0, 2, struct.pack("<III", 2, 0, 1)),
+        "truncated": (2, 10, 4, struct.pack("<III", 2, 0, 1)),
+        "id_out_of_range": (1, 10, 2, struct.pack("<III", 2, 0, 11)),
+    }
+    for name, (noe, nov, pins, body) in cases.items():
+        txt = tmp_path / f"{name}.hg"
+        txt.write_text("garbage\n")                     # the cache is read first
+        _plbin(tmp_path / f"{name}.hg.plbin", noe, nov, pins, body)
+        with pytest.raises(fp.FastPartError) as ei:
+            fp.read_patohlike(txt, transpose=True)
+        assert ei.value.status == fp.ERR_IO, name
+    for name, header in {"pins_huge": "0 5 2 1099511627776", "nov_huge": "0 5000000000 2 4",
+                         "negative_nov": "0 -5 2 4"}.items():
+        p = tmp_path / f"{name}.hg"
+        p.write_text(header + "\n0 1\n2 3\n")
+        with pytest.raises(fp.FastPartError) as ei:
+            fp.read_patohlike(p, transpose=True)
+        assert ei.value.status == fp.ERR_IO, name
+    lib = fp.lib()
+    g = C.c_void_p()
+    back = np.array([0, 3, 2, 4], np.uint32)             # net 1 ends before it starts
+    pins = np.array([0, 1, 2, 3], np.uint32)
+    assert lib.fp_graph_from_nets(5, 3, back.ctypes.data, pins.ctypes.data, None, C.byref(g)) == fp.ERR_INVALID
+    off = np.array([1, 2, 4], np.uint32)                 # offsets not starting at 0
+    assert lib.fp_graph_from_nets(5, 2, off.ctypes.data, pins.ctypes.data, None, C.byref(g)) == fp.ERR_INVALID
+    assert lib.fp_graph_from_vertices(2, 3, off.ctypes.data, pins.ctypes.data, None, C.byref(g)) == fp.ERR_INVALID
+
+
+def test_failed_host_allocation_is_a_status_not_an_abort(fp):
+    """Under an address-space limit, a hypergraph too large to build gives
+    FP_ERR_NOMEM from the C ABI (a C++ exception never crosses it)."""
+    code = (
+        "import resource, sys\n"
+        f"sys.path.insert(0, {str(ROOT)!r})\n"
+        "import fastpartitioner_gb300 as fp\n"
+        "fp.lib()\n"
+        "resource.setrlimit(resource.RLIMIT_AS, (3 << 30, 3 << 30))\n"
+        "try:\n"
+        "    fp.generate(fp.GenSpec.column_net(400_000_000, 400_000_000, 2, 16, seed=1))\n"
+        "    print('built')\n"
+        "except fp.FastPartError as e:\n"
+        "    print('status', e.status)\n"
+    )
+    res = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=300)
+    assert res.returncode == 0, res.stderr[-2000:]
+    assert res.stdout.strip() == f"status {fp.ERR_NOMEM}"

@@ -52,8 +52,6 @@ def test_stream_rejects_bad_arguments():
             fp.stream_partition(hg, K, metric, eps)
 
 
-FP_ERR_UNSUPPORTED = -5   # include/fastpart.h
-
 MORE = [
     ("colnet_2k_K3", lambda: fp.generate(fp.GenSpec.column_net(2048, 2048, 2, 12, seed=31)), 3, 1.05),
     ("zipf_8k_K100_weighted", lambda: fp.generate(fp.GenSpec.zipf(8000, 6000, 2.1, 2, 900, beta=1.5, weight_rule=1,
@@ -79,7 +77,7 @@ def test_stream_matches_oracle_odd_K_and_status(name, mk, K, eps, metric):
         assert o["status"] == -3                    # the oracle's "unsupported"
         with pytest.raises(fp.FastPartError) as ei:
             fp.stream_partition(hg, K, metric, eps)
-        assert ei.value.status == FP_ERR_UNSUPPORTED
+        assert ei.value.status == fp.ERR_UNSUPPORTED
         return
     s = fp.stream_partition(hg, K, metric, eps)
     np.testing.assert_array_equal(s["part_vec"], o["part_vec_init"])
