@@ -68,3 +68,36 @@ def test_algorithmic_bytes_model(small_hg):
     cn = bench.algorithmic_bytes("CN", hg, ln, none, K)
     sizes = np.diff(hg.nptr).astype(np.int64)
     assert cn == 4 * (hg.noe + 1) + 8 * hg.noe + int(np.sum(8 * sizes[ln == 2]))
+
+
+def _reference_line(monkeypatch, capsys, available):
+    import json
+    import oracle
+    if available and not oracle.reference_available():
+        pytest.skip("reference harness not built (reference sources unavailable)")
+    monkeypatch.setenv("RANK", "0")
+    monkeypatch.setenv("WORLD_SIZE", "1")
+    if not available:
+        monkeypatch.setattr(oracle, "reference_available", lambda *a: False)
+    args = bench.argparse.Namespace(config="zipf4m", metrics="TV,CN", cpu_scale=256, cpu_passes=1, warmup=1, steps=2)
+    bench.run_reference_arm(args)
+    lines = capsys.readouterr().out.strip().splitlines()
+    assert len(lines) == 1
+    return json.loads(lines[0])
+
+
+@pytest.mark.parametrize("available", [True, False], ids=["reference", "port"])
+def test_reference_arm_line(monkeypatch, capsys, available):
+    """bench.py --impl reference on a tiny sample: one JSON line with the
+    contract's keys, the same metric and unit as the GPU arm, an e2e with no
+    host-device bytes and a cpu_baseline describing the run."""
+    line = _reference_line(monkeypatch, capsys, available)
+    need = {"metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better", "scaling",
+            "vs_baseline", "dtype", "data", "config", "impl", "cpu_baseline", "e2e"}
+    assert need <= set(line)
+    assert line["impl"] == "reference" and line["unit"] == "pins/s" and line["higher_is_better"] is True
+    assert line["metric"] == bench.METRIC and line["value"] > 0 and line["steps"] == 2
+    cb = line["cpu_baseline"]
+    assert cb["kind"] == ("reference" if available else "port") and cb["value"] == line["value"]
+    assert cb["cores"] >= 1 and "vertices" in cb["sample"] and "passes of each of TV,CN" in cb["sample"]
+    assert line["e2e"] == {"value": line["value"], "unit": "pins/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
