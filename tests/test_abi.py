@@ -155,3 +155,18 @@ def test_failed_host_allocation_is_a_status_not_an_abort(fp):
     res = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=300)
     assert res.returncode == 0, res.stderr[-2000:]
     assert res.stdout.strip() == f"status {fp.ERR_NOMEM}"
+
+
+def test_footprint_lists_every_instance_allocation():
+    """fp_instance_footprint mirrors fp_instance_create's device allocations:
+    one size term per dalloc call (a loop of n terms counts n), so an
+    allocation added to one and not the other fails here.  The GPU tests check
+    the byte totals against fp_instance_device_bytes."""
+    src = (ROOT / "fastpartitioner_gb300" / "csrc" / "fp_api.cu").read_text()
+    create = src[src.index("int fp_instance_create("):src.index("int fp_instance_device_bytes(")]
+    foot = src[src.index("int fp_instance_footprint("):src.index("int fp_instance_destroy(")]
+    n_alloc = len(re.findall(r"\bdalloc\(in,", create))
+    n_terms = sum(int(m.group(2)) if m.group(2) else 1
+                  for m in re.finditer(r"(for \(int k = 0; k < (\d+); k\+\+\) )?\badd\(", foot))
+    assert n_alloc > 40 and n_terms == n_alloc
+    assert "metrics_scratch_bytes(K)" in create and "metrics_scratch_bytes(K)" in foot
