@@ -280,9 +280,22 @@ int stream_msg(const Problem& pb, HostState& st) {
   // connection counts, so a bit is set once, when its count leaves 0.
   const int W = (K + 63) / 64;
   std::vector<uint64_t> prow((size_t)K * W, 0), pcol((size_t)K * W, 0);
+  std::vector<int> rowcnt(K, 0), colcnt(K, 0);      // set bits per row / column
   auto set_pos = [&](int a, int b) {
     prow[(size_t)a * W + (b >> 6)] |= 1ull << (b & 63);
     pcol[(size_t)b * W + (a >> 6)] |= 1ull << (a & 63);
+    rowcnt[a]++;
+    colcnt[b]++;
+  };
+  std::vector<int> saved(K);
+  const uint64_t last_mask = (K & 63) ? (1ull << (K & 63)) - 1 : ~0ull;
+  // saved[k] -= amount for every k < K whose bit in `bits` is clear
+  auto sub_zeros = [&](const uint64_t* bits, int amount) {
+    for (int x = 0; x < W; x++) {
+      uint64_t zb = ~bits[x];
+      if (x == W - 1) zb &= last_mask;
+      for (; zb; zb &= zb - 1) saved[x * 64 + __builtin_ctzll(zb)] -= amount;
+    }
   };
   std::vector<int> smark(K, -1), src_part(g.noe, -1), mult(K, 0);
   std::vector<int> act_parts, act_nets, own_nets, mparts, dcount;
@@ -328,23 +341,44 @@ int stream_msg(const Problem& pb, HostState& st) {
     const bool idle = act_parts.empty() && mmax == 0;
     int nplanes = 0;
     while ((mmax >> nplanes) != 0) nplanes++;
-    planes.assign((size_t)nplanes * W, 0);
-    for (int p : mparts)
-      for (int b = 0; b < nplanes; b++)
-        if ((mult[p] >> b) & 1) planes[(size_t)b * W + (p >> 6)] |= 1ull << (p & 63);
-    for (int p : mparts) mult[p] = 0;
-    for (int k = idle ? K : 0; k < K; k++) {
-      if (!(st.part_sizes[k] < pb.C)) continue;
-      const uint64_t* col = &pcol[(size_t)k * W];
-      const uint64_t* row = &prow[(size_t)k * W];
-      int saved = 0;
-      for (int x = 0; x < W; x++) saved += __builtin_popcountll(col[x] & act[x]);
-      for (int b = 0; b < nplanes; b++) {
-        int c = 0;
-        for (int x = 0; x < W; x++) c += __builtin_popcountll(row[x] & planes[(size_t)b * W + x]);
-        saved += c << b;
+    // The same saved(k) two ways, the cheaper per vertex: popcounts over every
+    // part (K * W * (1 + planes) words), or -- once most counts are positive --
+    // the largest possible saving less the clear bits of the active parts'
+    // rows (conn[sp][k] == 0) and of the listed parts' columns
+    // (conn[k][p] == 0, weighted by the part's multiplicity).
+    long long zcost = K;
+    for (int sp : act_parts) zcost += W + (K - rowcnt[sp]);
+    for (int p : mparts) zcost += W + (K - colcnt[p]);
+    if (!idle && zcost < (long long)K * W * (1 + nplanes)) {
+      int msum = 0;
+      for (int p : mparts) msum += mult[p];
+      std::fill(saved.begin(), saved.end(), (int)act_parts.size() + msum);
+      for (int sp : act_parts) sub_zeros(&prow[(size_t)sp * W], 1);
+      for (int p : mparts) sub_zeros(&pcol[(size_t)p * W], mult[p]);
+      for (int p : mparts) mult[p] = 0;
+      for (int k = 0; k < K; k++) {
+        if (!(st.part_sizes[k] < pb.C)) continue;
+        if (saved[k] > best || (saved[k] == best && st.part_sizes[k] < st.part_sizes[arg])) { best = saved[k]; arg = k; }
       }
-      if (saved > best || (saved == best && st.part_sizes[k] < st.part_sizes[arg])) { best = saved; arg = k; }
+    } else {
+      planes.assign((size_t)nplanes * W, 0);
+      for (int p : mparts)
+        for (int b = 0; b < nplanes; b++)
+          if ((mult[p] >> b) & 1) planes[(size_t)b * W + (p >> 6)] |= 1ull << (p & 63);
+      for (int p : mparts) mult[p] = 0;
+      for (int k = idle ? K : 0; k < K; k++) {
+        if (!(st.part_sizes[k] < pb.C)) continue;
+        const uint64_t* col = &pcol[(size_t)k * W];
+        const uint64_t* row = &prow[(size_t)k * W];
+        int sv = 0;
+        for (int x = 0; x < W; x++) sv += __builtin_popcountll(col[x] & act[x]);
+        for (int b = 0; b < nplanes; b++) {
+          int c = 0;
+          for (int x = 0; x < W; x++) c += __builtin_popcountll(row[x] & planes[(size_t)b * W + x]);
+          sv += c << b;
+        }
+        if (sv > best || (sv == best && st.part_sizes[k] < st.part_sizes[arg])) { best = sv; arg = k; }
+      }
     }
     const int d = arg >= 0 ? arg : least.argmin();
     st.part_vec[v] = d;
