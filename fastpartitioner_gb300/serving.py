@@ -36,7 +36,7 @@ from typing import Callable, Optional
 
 import numpy as np
 
-from . import ERR_NOMEM, FastPartError, GenSpec, Hypergraph, footprint, generate, stream_partition
+from . import ERR_INVALID, ERR_NOMEM, FastPartError, GenSpec, Hypergraph, footprint, generate, stream_partition
 
 METRIC_NAMES = ("TV", "CN", "TM", "MSM", "MSV", "MSRV")
 
@@ -71,6 +71,7 @@ class Result:
     t_ready: float = 0.0                 # host preparation done
     t_start: float = 0.0                 # first GPU call
     t_done: float = 0.0                  # result read back
+    error: str = ""                      # a failure that was not the library's
 
     @property
     def latency(self) -> float:
@@ -84,6 +85,18 @@ class Prepared:
     state: Optional[dict] = None
     status: int = 0
     t_ready: float = 0.0
+    error: str = ""
+
+
+def _failed(p: Prepared, e: BaseException) -> None:
+    """Marks a preparation failed: the library's status, FP_ERR_NOMEM for a
+    host allocation failure, FP_ERR_INVALID for anything else (kept as text)."""
+    if isinstance(e, FastPartError):
+        p.status = e.status
+    else:
+        p.status = ERR_NOMEM if isinstance(e, MemoryError) else ERR_INVALID
+        p.error = repr(e)
+    p.hg = p.state = None
 
 
 # ---- workloads -------------------------------------------------------------
@@ -125,8 +138,8 @@ def _prepare(r: Request, clock: Callable[[], float], t0: float) -> Prepared:
     try:
         p.hg = r.hypergraph()
         p.state = stream_partition(p.hg, r.K, r.metric, r.eps)
-    except FastPartError as e:
-        p.status = e.status
+    except Exception as e:      # a failed request is a result, not an abort
+        _failed(p, e)
     p.t_ready = clock() - t0
     return p
 
@@ -134,7 +147,7 @@ def _prepare(r: Request, clock: Callable[[], float], t0: float) -> Prepared:
 def _refine_on_gpu(engine, p: Prepared, clock, t0) -> Result:
     """The GPU part of one request, from a host-prepared stream state."""
     r = p.request
-    res = Result(rid=r.rid, status=p.status, t_arrival=r.arrival, t_ready=p.t_ready)
+    res = Result(rid=r.rid, status=p.status, t_arrival=r.arrival, t_ready=p.t_ready, error=p.error)
     res.t_start = clock() - t0
     if p.status == 0:
         res.pins = p.hg.pins
@@ -174,8 +187,10 @@ def run_plain(engine, requests: list, clock: Callable[[], float] = time.perf_cou
                 inst.refine(r.passes)
                 res.metrics = inst.metrics()
                 res.part_vec = inst.partition()
-        except FastPartError as e:
-            res.status = e.status
+        except Exception as e:
+            p = Prepared(request=r)
+            _failed(p, e)
+            res.status, res.error = p.status, p.error
         res.t_done = clock() - t0
         out.append(res)
     return out
@@ -248,8 +263,8 @@ class Server:
             try:
                 p.hg = r.hypergraph()
                 need = self.footprint_fn(p.hg.nov, p.hg.noe, p.hg.pins, r.K, r.metric)
-            except FastPartError as e:
-                p.status = e.status
+            except Exception as e:  # the turn below is taken whatever happened
+                _failed(p, e)
             with cv:
                 while book["turn"] != idx or (p.status == 0 and need <= self.budget and
                                               book["reserved"] + need > self.budget):
@@ -266,10 +281,8 @@ class Server:
             if p.status == 0:
                 try:
                     p.state = stream_partition(p.hg, r.K, r.metric, r.eps)
-                except FastPartError as e:
-                    p.status = e.status
-            if p.status != 0:
-                p.hg = None
+                except Exception as e:
+                    _failed(p, e)
             p.t_ready = self.clock() - t0
             return p, need
 

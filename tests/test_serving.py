@@ -188,3 +188,29 @@ def test_bench_batch_and_serve_lines(monkeypatch, capsys):
     assert b["config"]["plain_loop"]["completed"] == 10
     assert v["unit"] == "s" and v["higher_is_better"] is False and v["config"]["same_alone_and_in_the_mix"] is True
     assert v["config"]["served"]["requests"] == 10 and v["config"]["peak_reserved_gb"] <= 1.0
+
+
+class BrokenRequest(sv.Request):
+    def hypergraph(self):
+        raise ValueError("no payload")
+
+
+@pytest.mark.parametrize("runner", ["plain", "pipelined", "server"])
+def test_a_failing_request_is_a_result(runner):
+    """A request whose hypergraph cannot be built fails alone: its result
+    carries FP_ERR_INVALID and the error text, the others complete, and the
+    serving loop's turn order does not stall on it."""
+    reqs = sv.poisson_arrivals(small_batch(9, seed=8), rate=500.0, seed=5)
+    bad = reqs[3]
+    reqs[3] = BrokenRequest(**bad.__dict__)
+    eng = FakeEngine()
+    if runner == "plain":
+        out = sv.run_plain(eng, reqs)
+    elif runner == "pipelined":
+        out = sv.run_pipelined(eng, reqs, workers=3)
+    else:
+        out = sv.Server(eng, budget_bytes=1 << 40, workers=3, slots=4).run(reqs)
+    by = {r.rid: r for r in out}
+    assert len(by) == 9
+    assert by[bad.rid].status == fp.ERR_INVALID and "no payload" in by[bad.rid].error
+    assert all(r.status == 0 for rid, r in by.items() if rid != bad.rid)
