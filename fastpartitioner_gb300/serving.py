@@ -160,8 +160,11 @@ def _refine_on_gpu(engine, p: Prepared, clock, t0) -> Result:
                 inst.refine(r.passes)
                 res.metrics = inst.metrics()
                 res.part_vec = inst.partition()
-        except FastPartError as e:
-            res.status = e.status
+        except Exception as e:      # the serving loop must go on to release what it holds
+            q = Prepared(request=r)
+            _failed(q, e)
+            res.status, res.error = q.status, q.error
+            res.part_vec = res.metrics = None
     res.t_done = clock() - t0
     return res
 

@@ -214,3 +214,27 @@ def test_a_failing_request_is_a_result(runner):
     assert len(by) == 9
     assert by[bad.rid].status == fp.ERR_INVALID and "no payload" in by[bad.rid].error
     assert all(r.status == 0 for rid, r in by.items() if rid != bad.rid)
+
+
+class FailingRefineEngine(FakeEngine):
+    """refine() fails for one K: a GPU-side failure of one request."""
+
+    def instance(self, hg, K, metric, eps=1.05):
+        inst = super().instance(hg, K, metric, eps)
+        if K == 16:
+            def boom(passes):
+                raise RuntimeError("device lost")
+            inst.refine = boom
+        return inst
+
+
+def test_gpu_side_failure_releases_the_request():
+    reqs = sv.poisson_arrivals(small_batch(10, seed=9), rate=800.0, seed=6)
+    foot = max(fp.footprint(*(lambda h: (h.nov, h.noe, h.pins))(r.hypergraph()), r.K, r.metric) for r in reqs)
+    out = sv.Server(FailingRefineEngine(), budget_bytes=foot, workers=3, slots=4).run(reqs)
+    assert len(out) == 10
+    for r, q in zip(out, sorted(reqs, key=lambda x: x.rid)):
+        if q.K == 16:
+            assert r.status == fp.ERR_INVALID and "device lost" in r.error and r.part_vec is None
+        else:
+            assert r.status == 0
