@@ -99,3 +99,40 @@ def test_graph_from_vertices_is_the_inverse(fp):
         bad = hg.vnets.copy()
         bad[0] = hg.noe
         fp.Hypergraph.from_vertices(hg.nov, hg.noe, hg.vptr, bad)
+
+
+# The hypergraph and partition of the reference's README (its Figures 1 and 2):
+# N1 = {v1, v2, v3}, N2 = {v1, v6, v7, v8}, N3 = {v3, v4, v5}, N4 = {v6, v7};
+# P1 = {v1, v2}, P2 = {v3, v4, v5}, P3 = {v6, v7, v8}, K = 4 (one part empty).
+# N1 and N2 are cut, N3 and N4 are not: TV = 2, CN = 2.
+README_NETS = [[0, 1, 2], [0, 5, 6, 7], [2, 3, 4], [5, 6]]
+README_PARTS = [0, 0, 1, 1, 1, 2, 2, 2]
+
+
+def recount_metrics(hg, part_vec, K):
+    """The six metrics of a part vector, from the net -> pins CSR and the sources
+    (shared/metric.cpp:3-391, CN/cn.cpp:17-94)."""
+    sizes = np.diff(hg.nptr).astype(np.int64)
+    net_of_pin = np.repeat(np.arange(hg.noe), sizes)
+    key = np.unique(net_of_pin * K + part_vec[hg.npins])
+    net, part = key // K, key % K
+    lam = np.bincount(net, minlength=hg.noe)
+    spart = part_vec[hg.src][net]
+    other = part != spart
+    send = np.bincount(spart[other], minlength=K)
+    recv = np.bincount(part[other], minlength=K)
+    pairs = np.unique(spart[other] * K + part[other])
+    msgs = np.bincount(pairs // K, minlength=K)
+    return {"TV": int(np.sum(lam - 1)), "CN": int(np.sum(lam > 1)), "TM": int(pairs.size),
+            "MSM": int(msgs.max()), "MSV": int(send.max()), "MSRV": int((send + recv).max())}
+
+
+def test_readme_example_metrics():
+    import fastpartitioner_gb300 as fp
+    nptr = np.cumsum([0] + [len(n) for n in README_NETS]).astype(np.uint32)
+    hg = fp.Hypergraph.from_nets(8, nptr, np.concatenate([np.array(n, np.uint32) for n in README_NETS]))
+    m = recount_metrics(hg, np.array(README_PARTS), 4)
+    assert m["TV"] == 2 and m["CN"] == 2
+    # sources are each net's lowest pin: v1, v1, v3, v6; P1 sends to P2 (N1) and P3 (N2)
+    assert list(hg.src) == [0, 0, 2, 5]
+    assert m == {"TV": 2, "CN": 2, "TM": 2, "MSM": 2, "MSV": 2, "MSRV": 2}

@@ -113,3 +113,34 @@ def test_results_same_alone_and_in_the_mix(fp, gpu_engine):
         assert (a.part_vec == b.part_vec).all() and (a.part_vec == c.part_vec).all(), a.rid
         assert a.metrics == b.metrics == c.metrics, a.rid
         assert a.device_bytes == b.device_bytes == c.device_bytes
+
+
+@pytest.mark.parametrize("metric", METRICS)
+def test_readme_example_on_the_device(fp, gpu_engine, metric):
+    """The reference README's example partition, loaded with fp_set_state: the
+    device metric kernels give TV = 2 and CN = 2 (the README's cut nets N1 and
+    N2), and the four source-based metrics of the same partition."""
+    from test_host import README_NETS, README_PARTS, recount_metrics
+    nptr = np.cumsum([0] + [len(n) for n in README_NETS]).astype(np.uint32)
+    npins = np.concatenate([np.array(n, np.uint32) for n in README_NETS])
+    hg = fp.Hypergraph.from_nets(8, nptr, npins)
+    pv = np.array(README_PARTS, np.int32)
+    K = 4
+    ep_parts = np.full(hg.pins, -1, np.int32)
+    ep_cnt = np.zeros(hg.pins, np.int32)
+    ends = np.zeros(hg.noe, np.int32)
+    for e in range(hg.noe):
+        b = int(hg.nptr[e])
+        order = []
+        for u in hg.npins[hg.nptr[e]:hg.nptr[e + 1]]:
+            if pv[u] not in order:
+                order.append(int(pv[u]))
+        for j, p in enumerate(order):
+            ep_parts[b + j] = p
+            ep_cnt[b + j] = int(np.sum(pv[hg.npins[hg.nptr[e]:hg.nptr[e + 1]]] == p))
+        ends[e] = b + len(order)
+    with gpu_engine.instance(hg, K, metric) as inst:
+        inst.set_state(pv, hg.nptr[:-1].astype(np.int32), ends, ep_parts, ep_cnt)
+        m = inst.metrics()
+    assert m["TV"] == 2 and m["CN"] == 2
+    assert m == recount_metrics(hg, pv.astype(np.int64), K)
