@@ -121,6 +121,15 @@ def _read_capture(path: Path, nov: int, noe: int):
     return part_vec, ep_len, flat
 
 
+class ReferenceRunError(RuntimeError):
+    """The reference harness exited non-zero; `returncode` < 0 is the signal
+    that ended it."""
+
+    def __init__(self, returncode: int, message: str):
+        super().__init__(message)
+        self.returncode = returncode
+
+
 def run_reference(hg, K: int, metric: str, passes: int, threads: int = 1, capture: bool = True,
                   timeout: float = 3600):
     """Runs the reference's own partition() (threads == 1) or partition_par()
@@ -140,7 +149,8 @@ def run_reference(hg, K: int, metric: str, passes: int, threads: int = 1, captur
         res = subprocess.run([str(exe), str(inst), str(K), str(passes), str(threads), prefix],
                              capture_output=True, text=True, timeout=timeout, env=env, cwd=td)
         if res.returncode != 0:
-            raise RuntimeError(f"reference run failed ({res.returncode}):\n{res.stdout[-2000:]}\n{res.stderr[-2000:]}")
+            raise ReferenceRunError(res.returncode, f"reference run failed ({res.returncode}):\n"
+                                                    f"{res.stdout[-2000:]}\n{res.stderr[-2000:]}")
         text = res.stdout
         out = {"stdout": text}
         before, after = {}, {}

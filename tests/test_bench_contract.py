@@ -101,3 +101,30 @@ def test_reference_arm_line(monkeypatch, capsys, available):
     assert cb["kind"] == ("reference" if available else "port") and cb["value"] == line["value"]
     assert cb["cores"] >= 1 and "vertices" in cb["sample"] and "passes of each of TV,CN" in cb["sample"]
     assert line["e2e"] == {"value": line["value"], "unit": "pins/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+
+
+def test_reference_run_ended_by_a_signal_is_retried(monkeypatch, capsys):
+    """A reference run that a signal ends is run again and counted; a run that
+    fails with an exit status is not retried."""
+    import oracle
+    if not oracle.reference_available():
+        pytest.skip("reference harness not built (reference sources unavailable)")
+    real = oracle.run_reference
+    calls = {"n": 0}
+
+    def flaky(*a, **k):
+        calls["n"] += 1
+        if calls["n"] == 2:
+            raise oracle.ReferenceRunError(-11, "reference run failed (-11)")
+        return real(*a, **k)
+
+    monkeypatch.setattr(oracle, "run_reference", flaky)
+    line = _reference_line(monkeypatch, capsys, True)
+    assert line["cpu_baseline"]["crashed_runs_retried"] == 1 and line["value"] > 0
+
+    def failing(*a, **k):
+        raise oracle.ReferenceRunError(3, "reference run failed (3)")
+
+    monkeypatch.setattr(oracle, "run_reference", failing)
+    with pytest.raises(oracle.ReferenceRunError):
+        bench.run_reference_retrying(oracle, None, 8, "TV", 1, 1)
