@@ -144,3 +144,28 @@ def test_readme_example_on_the_device(fp, gpu_engine, metric):
         m = inst.metrics()
     assert m["TV"] == 2 and m["CN"] == 2
     assert m == recount_metrics(hg, pv.astype(np.int64), K)
+
+
+from test_dropin_cn_driver import after_lines, cn_driver, run_driver  # noqa: E402,F401  (cn_driver is a fixture)
+
+
+def test_reference_cn_driver_on_the_device(fp, gpu_engine, cn_driver, tmp_path):
+    """The reference's own CN driver with -g 1 -- its partition_gpu(), the shim
+    of INTEGRATION.md, libfastpart.so on the GPU -- refines exactly as its CPU
+    path (-g 0): the same After Refinement lines and the same part vector
+    file.  The files keep their nets' pins unsorted, as drawn, so the GPU moves
+    pins in the file's order as the reference does."""
+    for seed, K, passes in ((71, 8, 3), (72, 32, 2)):
+        hg = fp.generate(fp.GenSpec.zipf(3000 + seed, 2500, 2.1, 2, 120, beta=1.2, seed=seed))
+        outs = []
+        for gpu in (0, 1):
+            d = tmp_path / f"s{seed}_g{gpu}"
+            d.mkdir()
+            fp.write_patohlike(hg, d / "g.hg")
+            res = run_driver(cn_driver, d / "g.hg", K, passes, gpu)
+            assert res.returncode == 0, res.stderr[-2000:]
+            assert "fastpart:" not in res.stderr, res.stderr[-2000:]
+            outs.append((after_lines(res.stdout), (d / f"g.hg.fastpart.{K}").read_text()))
+        assert len(outs[0][0]) == 6
+        assert outs[1][0] == outs[0][0], (seed, K)
+        assert outs[1][1] == outs[0][1], (seed, K)
