@@ -1,0 +1,123 @@
+"""The drop-in, end to end: each of the reference's own drivers (TV/tv.cpp,
+CN/cn.cpp, TM/tm.cpp, MGV/mgv.cpp, MSRV/mgav.cpp, MSM/msm.cpp, with their
+partition.cpp and shared/, from the staging copy oracle/Makefile keeps) is
+built with its shim from INTEGRATION.md in place of gpu_partition.cu and
+linked against libfastpart.so.  Here (no GPU) every driver must link; those
+whose command line reaches the CPU refinement run it, and with -g the GPU branch
+reports the library's error instead of crashing.  The GPU comparison (-g 1
+against the CPU refinement) runs with the GPU tests."""
+import re
+import shutil
+import subprocess
+from concurrent.futures import ThreadPoolExecutor
+
+import pytest
+
+from conftest import ROOT
+
+SRC = ROOT / "oracle" / "_ref" / "src"
+CFLAGS = ["-O2", "-std=c++11", "-fopenmp", "-ffp-contract=off", "-w"]
+
+# metric -> (reference directory, driver, marker of its shim block in INTEGRATION.md)
+DRIVERS = {
+    "TV": ("TV", "tv.cpp", "FP_METRIC_TV, row_ptr"),
+    "CN": ("CN", "cn.cpp", "FP_METRIC_CN, row_ptr"),
+    "TM": ("TM", "tm.cpp", "FP_METRIC_TM, row_ptr"),
+    "MSV": ("MGV", "mgv.cpp", "FP_METRIC_MSV, row_ptr"),
+    "MSRV": ("MSRV", "mgav.cpp", "FP_METRIC_TV, row_ptr"),   # TV's shim with FP_METRIC_MSRV, as documented
+    "MSM": ("MSM", "msm.cpp", "FP_METRIC_MSM, row_ptr"),
+}
+# MSM/msm.cpp calls a partition_gpu that MSM/partition.h does not declare
+MSM_DECL = ("#include <string>\nvoid partition_gpu(unsigned int*, unsigned int*, unsigned int*, int, int, long long,"
+            " int*, int*, int, int*, std::string, int, int);\n")
+
+
+def shim_source(tmp, metric):
+    blocks = re.findall(r"```(?:cpp|c\+\+)\n(.*?)```", (ROOT / "INTEGRATION.md").read_text(), re.S)
+    common = [b for b in blocks if "fp_wrapper_refine(int metric" in b]
+    mine = [b for b in blocks if DRIVERS[metric][2] in b]
+    assert len(common) == 1 and len(mine) == 1, metric
+    (tmp / "fp_wrapper_common.h").write_text("#pragma once\n" + common[0])
+    code = mine[0].replace("FP_METRIC_TV", "FP_METRIC_MSRV") if metric == "MSRV" else mine[0]
+    path = tmp / f"{metric.lower()}_fp_wrapper.cpp"
+    path.write_text(code)
+    return path
+
+
+def build_driver(fp, tmp, metric):
+    d, driver, _ = DRIVERS[metric]
+    work = tmp / metric
+    work.mkdir()
+    shim = shim_source(work, metric)
+    lib = fp.library_path()
+    extra = []
+    if metric == "MSM":
+        (work / "msm_decl.h").write_text(MSM_DECL)
+        extra = ["-include", str(work / "msm_decl.h")]
+    exe = work / f"{metric.lower()}_gb300"
+    cmd = ["g++", *CFLAGS, *extra, "-I", str(SRC / d), "-I", str(SRC / "shared"), "-I", str(ROOT / "include"),
+           "-I", str(work), str(SRC / d / driver), str(SRC / d / "partition.cpp"), str(SRC / "shared" / "metric.cpp"),
+           str(SRC / "shared" / "utils.cpp"), str(SRC / "shared" / "hypergraph_rw.cpp"), str(shim),
+           "-L", str(lib.parent), "-lfastpart", f"-Wl,-rpath,{lib.parent}", "-o", str(exe)]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    return exe if res.returncode == 0 else res.stderr[-3000:]
+
+
+@pytest.fixture(scope="session")
+def drivers(fp, tmp_path_factory):
+    """metric -> path of the reference driver linked against libfastpart.so."""
+    if not all((SRC / d / drv).exists() for d, drv, _ in DRIVERS.values()) or shutil.which("g++") is None:
+        pytest.skip("reference drivers not staged (oracle/_ref/src)")
+    tmp = tmp_path_factory.mktemp("drivers")
+    with ThreadPoolExecutor(len(DRIVERS)) as ex:
+        built = dict(zip(DRIVERS, ex.map(lambda m: build_driver(fp, tmp, m), DRIVERS)))
+    bad = {m: err for m, err in built.items() if isinstance(err, str)}
+    assert not bad, bad
+    return built
+
+
+def run_driver(exe, hg_path, K, passes, gpu):
+    return subprocess.run([str(exe), "-f", str(hg_path), "-k", str(K), "-r", "1", "-i", str(passes), "-g", str(gpu)],
+                          capture_output=True, text=True, timeout=600, cwd=hg_path.parent)
+
+
+def after_lines(text):
+    return re.findall(r"^After Refinement (TV|CN|TM|MGM|MGV|MGAV) : (-?\d+)$", text, re.M)
+
+
+def square_case(fp, seed):
+    """A square instance (the TM / MGV / MSRV / MSM drivers read file lines as
+    vertices, so only a square file is defined for them)."""
+    return fp.generate(fp.GenSpec.zipf(3000, 3000, 2.1, 2, 120, beta=1.2, seed=seed))
+
+
+# Two drivers' command lines are broken in the reference itself:
+# * MSRV/mgav.cpp registers "-t" twice and binds nothing to a GPU switch
+#   (mgav.cpp:27-28): CLI11 stops it at start-up;
+# * MSM/msm.cpp binds "-g" to the thread count and sets GPE = NT (msm.cpp:28,37):
+#   "-g 1" takes the GPU branch, "-g 0" asks for zero threads, so its CPU
+#   refinement cannot be reached from the command line.
+CPU_PATH = ["TV", "CN", "TM", "MSV"]       # drivers whose -g 0 runs the CPU refinement
+
+
+@pytest.mark.parametrize("metric", list(DRIVERS))
+def test_reference_driver_links_and_runs(fp, drivers, tmp_path, metric):
+    """Every driver links against libfastpart.so.  Those with a reachable CPU
+    refinement run it as the reference does; with -g and no usable device, the
+    GPU branch reports the library's status and the driver completes."""
+    import torch
+    hg = square_case(fp, 71)
+    path = tmp_path / "g.hg"
+    fp.write_patohlike(hg, path)
+    if metric == "MSRV":
+        res = run_driver(drivers[metric], path, 8, 3, 0)
+        assert res.returncode != 0 and "already added" in (res.stdout + res.stderr).lower(), res.stderr[-500:]
+        return
+    if metric in CPU_PATH:
+        cpu = run_driver(drivers[metric], path, 8, 3, 0)
+        assert cpu.returncode == 0, cpu.stderr[-2000:]
+        assert len(after_lines(cpu.stdout)) == 6, cpu.stdout[-1500:]
+    if not torch.cuda.is_available():
+        gpu = run_driver(drivers[metric], path, 8, 3, 1)
+        assert gpu.returncode == 0, gpu.stderr[-2000:]
+        assert "fastpart:" in gpu.stderr, gpu.stderr[-500:]

@@ -146,26 +146,30 @@ def test_readme_example_on_the_device(fp, gpu_engine, metric):
     assert m == recount_metrics(hg, pv.astype(np.int64), K)
 
 
-from test_dropin_cn_driver import after_lines, cn_driver, run_driver  # noqa: E402,F401  (cn_driver is a fixture)
+from test_dropin_drivers import CPU_PATH, after_lines, drivers, run_driver, square_case  # noqa: E402,F401
 
 
-def test_reference_cn_driver_on_the_device(fp, gpu_engine, cn_driver, tmp_path):
-    """The reference's own CN driver with -g 1 -- its partition_gpu(), the shim
-    of INTEGRATION.md, libfastpart.so on the GPU -- refines exactly as its CPU
-    path (-g 0): the same After Refinement lines and the same part vector
-    file.  The files keep their nets' pins unsorted, as drawn, so the GPU moves
-    pins in the file's order as the reference does."""
+@pytest.mark.parametrize("metric", CPU_PATH)
+def test_reference_driver_on_the_device(fp, gpu_engine, drivers, tmp_path, metric):
+    """The reference's own driver with -g 1 -- its partition_gpu(), the shim of
+    INTEGRATION.md, libfastpart.so on the GPU -- refines exactly as its CPU path
+    (-g 0): the same After Refinement lines and, for CN, the same part vector
+    file.  The TV and CN drivers hand their metric code wrong or uninitialised
+    net sizes (TV/tv.cpp:51, CN/cn.cpp:280-284), so MGV and MGAV, which use them,
+    are left out there.  The files keep their nets' pins unsorted, as drawn."""
+    skip = {"MGV", "MGAV"} if metric in ("TV", "CN") else set()
     for seed, K, passes in ((71, 8, 3), (72, 32, 2)):
-        hg = fp.generate(fp.GenSpec.zipf(3000 + seed, 2500, 2.1, 2, 120, beta=1.2, seed=seed))
+        hg = square_case(fp, seed)
         outs = []
         for gpu in (0, 1):
             d = tmp_path / f"s{seed}_g{gpu}"
             d.mkdir()
             fp.write_patohlike(hg, d / "g.hg")
-            res = run_driver(cn_driver, d / "g.hg", K, passes, gpu)
+            res = run_driver(drivers[metric], d / "g.hg", K, passes, gpu)
             assert res.returncode == 0, res.stderr[-2000:]
             assert "fastpart:" not in res.stderr, res.stderr[-2000:]
-            outs.append((after_lines(res.stdout), (d / f"g.hg.fastpart.{K}").read_text()))
-        assert len(outs[0][0]) == 6
-        assert outs[1][0] == outs[0][0], (seed, K)
-        assert outs[1][1] == outs[0][1], (seed, K)
+            lines = [x for x in after_lines(res.stdout) if x[0] not in skip]
+            part = d / f"g.hg.fastpart.{K}"
+            outs.append((lines, part.read_text() if part.exists() else None))
+        assert len(outs[0][0]) == 6 - len(skip)
+        assert outs[1] == outs[0], (metric, seed, K)
