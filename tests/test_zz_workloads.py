@@ -157,6 +157,8 @@ def test_reference_driver_on_the_device(fp, gpu_engine, drivers, tmp_path, metri
     file.  The TV and CN drivers hand their metric code wrong or uninitialised
     net sizes (TV/tv.cpp:51, CN/cn.cpp:280-284), so MGV and MGAV, which use them,
     are left out there.  The files keep their nets' pins unsorted, as drawn."""
+    if isinstance(drivers[metric], str):
+        pytest.skip(f"the reference driver did not build on this machine: {drivers[metric][-300:]}")
     skip = {"MGV", "MGAV"} if metric in ("TV", "CN") else set()
     for seed, K, passes in ((71, 8, 3), (72, 32, 2)):
         hg = square_case(fp, seed)
