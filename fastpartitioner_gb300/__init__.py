@@ -117,6 +117,7 @@ def lib():
             "fp_validate": ([C.POINTER(_Hypergraph)], C.c_int),
             "fp_bfs_order": ([C.POINTER(_Hypergraph), C.c_int32, C.c_void_p, C.c_void_p], C.c_int),
             "fp_stream_partition": ([C.POINTER(_Hypergraph), i32, i32, dbl, C.POINTER(FpState)], C.c_int),
+            "fp_check_state": ([C.POINTER(_Hypergraph), i32, i32, dbl, C.POINTER(FpState)], C.c_int),
             "fp_ctx_create": ([i32, pp], C.c_int),
             "fp_ctx_destroy": ([vp], C.c_int),
             "fp_ctx_set_stream": ([vp, vp], C.c_int),
@@ -457,16 +458,11 @@ class Instance:
                     "recv", "conn", "msgs")
 
     def set_state(self, part_vec, ep_starts, ep_ends, ep_parts, ep_cnt, **optional) -> None:
-        """Uploads a refinement state in the reference's layout (fp_set_state);
-        optional: part_sizes, marker, send, recv, conn (K*K), msgs."""
-        arrs = dict(part_vec=part_vec, ep_starts=ep_starts, ep_ends=ep_ends, ep_parts=ep_parts, ep_cnt=ep_cnt)
-        for k, v in optional.items():
-            if k not in self.STATE_FIELDS:
-                raise TypeError(f"unknown state array {k}")
-            if v is not None:
-                arrs[k] = v
-        keep = {k: np.ascontiguousarray(v, dtype=np.int32) for k, v in arrs.items()}
-        st = FpState(**{k: v.ctypes.data for k, v in keep.items()})
+        """Uploads a refinement state in the reference's layout (fp_set_state):
+        ep_ends[e] is the number of parts listed for net e (lambda(e)), as the
+        reference keeps it; optional: part_sizes, marker, send, recv, conn
+        (K*K), msgs."""
+        st, keep = _state_struct(part_vec, ep_starts, ep_ends, ep_parts, ep_cnt, **optional)
         _check(lib().fp_set_state(self._h, C.byref(st)), "fp_set_state")
 
     def get_state(self) -> dict:
@@ -548,9 +544,33 @@ def footprint(nov: int, noe: int, pins: int, K: int, metric) -> int:
     return int(out.value)
 
 
+def _state_struct(part_vec, ep_starts, ep_ends, ep_parts, ep_cnt, **optional):
+    """An FpState over int32 copies of the arrays (returned with it: they must
+    stay alive while the struct is used)."""
+    arrs = dict(part_vec=part_vec, ep_starts=ep_starts, ep_ends=ep_ends, ep_parts=ep_parts, ep_cnt=ep_cnt)
+    for k, v in optional.items():
+        if k not in Instance.STATE_FIELDS:
+            raise TypeError(f"unknown state array {k}")
+        if v is not None:
+            arrs[k] = v
+    keep = {k: np.ascontiguousarray(v, dtype=np.int32) for k, v in arrs.items()}
+    return FpState(**{k: v.ctypes.data for k, v in keep.items()}), keep
+
+
+def check_state(hg: Hypergraph, K: int, metric, part_vec, ep_starts, ep_ends, ep_parts, ep_cnt,
+                eps: float = 1.05, **optional) -> None:
+    """fp_check_state: raises FastPartError unless the arrays are a valid
+    refinement state of hg in the reference's layout (ep_ends = lambda(e)) --
+    the check set_state applies, on the host alone."""
+    st, keep = _state_struct(part_vec, ep_starts, ep_ends, ep_parts, ep_cnt, **optional)
+    v = hg.view()
+    _check(lib().fp_check_state(C.byref(v), int(K), metric_id(metric), float(eps), C.byref(st)), "fp_check_state")
+
+
 def stream_partition(hg: Hypergraph, K: int, metric, eps: float = 1.05) -> dict:
     """The metric's streaming initial partition on the host (fp_stream_partition),
-    in the fp_state layout: part_vec, ep_starts, ep_ends, ep_parts, ep_cnt,
+    in the fp_state layout (ep_ends[e] = lambda(e), the reference's count of
+    listed parts): part_vec, ep_starts, ep_ends, ep_parts, ep_cnt,
     part_sizes, marker, send, recv, conn (K*K), msgs.  No GPU needed; an
     instance takes it with set_state."""
     nov, noe, P = hg.nov, hg.noe, hg.pins

@@ -720,86 +720,10 @@ int fp_get_lists(fp_instance* in, int32_t* ep_len, int32_t* ep_part, int32_t* ep
 
 int fp_set_state(fp_instance* in, const fp_state* s) {
   return fp::guarded([&]() -> int {
-    if (!in || !s || !s->part_vec || !s->ep_starts || !s->ep_ends || !s->ep_parts || !s->ep_cnt)
-      return FP_ERR_INVALID;
-    const HostGraph& g = in->g;
-    const int K = in->pb.K, metric = in->pb.metric, nov = g.nov, noe = g.noe;
-    const bool msg = metric == FP_METRIC_TM || metric == FP_METRIC_MSM;
+    if (!in) return FP_ERR_INVALID;
     HostState st;
-    st.part_vec.assign(s->part_vec, s->part_vec + nov);
-    st.part_sizes.assign(K, 0);
-    for (int v = 0; v < nov; v++) {
-      const int p = st.part_vec[v];
-      if (p < 0 || p >= K) return FP_ERR_INVALID;
-      st.part_sizes[p] += in->pb.w[v];
-    }
-    if (s->part_sizes)
-      for (int p = 0; p < K; p++)
-        if (s->part_sizes[p] != st.part_sizes[p]) return FP_ERR_INVALID;
-    st.ep_start.assign(g.nptr.begin(), g.nptr.end());
-    st.ep_len.assign(noe, 0);
-    st.ep_part.assign(g.pins, -1);
-    st.ep_cnt.assign(g.pins, 0);
-    // Every list must hold exactly the parts of the net's pins with their counts
-    // (the reference's checkMe invariant, MSM/partition.cpp:2-68).
-    std::vector<int> mark(K, -1), count(K, 0), listed(K, -1);
-    for (int e = 0; e < noe; e++) {
-      const int b = (int)g.nptr[e], size = (int)(g.nptr[e + 1] - g.nptr[e]);
-      if (s->ep_starts[e] != b) return FP_ERR_INVALID;
-      const int len = s->ep_ends[e] - b;
-      if (len < 1 || len > size || len > K) return FP_ERR_INVALID;
-      int distinct = 0;
-      for (int k = b; k < b + size; k++) {
-        const int p = st.part_vec[g.npins[k]];
-        if (mark[p] != e) { mark[p] = e; count[p] = 0; distinct++; }
-        count[p]++;
-      }
-      if (distinct != len) return FP_ERR_INVALID;
-      for (int j = 0; j < len; j++) {
-        const int p = s->ep_parts[b + j], c = s->ep_cnt[b + j];
-        if (p < 0 || p >= K || mark[p] != e || listed[p] == e || count[p] != c) return FP_ERR_INVALID;
-        listed[p] = e;
-        st.ep_part[b + j] = p;
-        st.ep_cnt[b + j] = c;
-      }
-      st.ep_len[e] = len;
-    }
-    st.marker.assign(K, -1);
-    if (s->marker)
-      for (int p = 0; p < K; p++) {
-        if (s->marker[p] < -1 || s->marker[p] >= nov) return FP_ERR_INVALID;
-        st.marker[p] = s->marker[p];
-      }
-    // Volumes and messages: as given, else the count over the lists; the arrays
-    // a metric does not keep stay zero (send: MSV, MSRV; recv: MSRV).
-    const bool keep_send = metric == FP_METRIC_MSV || metric == FP_METRIC_MSRV;
-    const bool keep_recv = metric == FP_METRIC_MSRV;
-    st.send.assign(K, 0);
-    st.recv.assign(K, 0);
-    st.msgs.assign(K, 0);
-    if (msg) st.conn.assign((size_t)K * K, 0);
-    for (int e = 0; e < noe; e++) {
-      const int sp = st.part_vec[g.src[e]];
-      const int b = st.ep_start[e];
-      for (int j = 0; j < st.ep_len[e]; j++) {
-        const int p = st.ep_part[b + j];
-        if (p == sp) continue;
-        if (keep_send) st.send[sp]++;
-        if (keep_recv) st.recv[p]++;
-        if (msg) st.conn[(size_t)sp * K + p]++;
-      }
-    }
-    if (msg) {
-      if (metric == FP_METRIC_MSM)
-        for (int p = 0; p < K; p++) st.conn[(size_t)p * K + p] = -1;   // MSM/partition.cpp:101
-      if (s->conn) st.conn.assign(s->conn, s->conn + (size_t)K * K);
-      for (int a = 0; a < K; a++)
-        for (int b = 0; b < K; b++)
-          if (a != b && st.conn[(size_t)a * K + b] > 0) st.msgs[a]++;
-      if (s->msgs) st.msgs.assign(s->msgs, s->msgs + K);
-    }
-    if (s->send && keep_send) st.send.assign(s->send, s->send + K);
-    if (s->recv && keep_recv) st.recv.assign(s->recv, s->recv + K);
+    const int rc = state_from_caller(in->g, in->pb, s, st);
+    if (rc) return rc;
     cudaSetDevice(in->ctx->device);
     in->st = std::move(st);
     in->has_state = true;
@@ -818,10 +742,7 @@ int fp_get_state(fp_instance* in, fp_state* s) {
     if (s->part_vec && (rc = d2h(in, s->part_vec, in->d.part_vec, sizeof(int) * g.nov))) return rc;
     if (s->ep_starts)
       for (int e = 0; e < g.noe; e++) s->ep_starts[e] = (int)g.nptr[e];
-    if (s->ep_ends) {
-      if ((rc = d2h(in, s->ep_ends, in->d.ep_len, sizeof(int) * g.noe))) return rc;
-      for (int e = 0; e < g.noe; e++) s->ep_ends[e] += (int)g.nptr[e];
-    }
+    if (s->ep_ends && (rc = d2h(in, s->ep_ends, in->d.ep_len, sizeof(int) * g.noe))) return rc;
     if (s->ep_parts && (rc = d2h(in, s->ep_parts, in->d.ep_part, sizeof(int) * g.pins))) return rc;
     if (s->ep_cnt && (rc = d2h(in, s->ep_cnt, in->d.ep_cnt, sizeof(int) * g.pins))) return rc;
     if (s->part_sizes && (rc = d2h(in, s->part_sizes, in->d.part_sizes, sizeof(int) * K))) return rc;

@@ -165,6 +165,92 @@ int make_problem(const fp_hypergraph* h, int K, int metric, double eps_factor, H
   return FP_OK;
 }
 
+// Checks a caller-built refinement state in the reference's layout against the
+// hypergraph and converts it into the engine's host state.  ep_ends[e] is
+// lambda(e), the number of parts listed for net e: the stream increments it
+// from 0 (TV/partition.cpp:1066-1075) and the metric code reads it as that count
+// (shared/metric.cpp:3-14,57-68).  ep_starts must equal the net offsets.
+int state_from_caller(const HostGraph& g, const Problem& pb, const fp_state* s, HostState& st) {
+  if (!s || !s->part_vec || !s->ep_starts || !s->ep_ends || !s->ep_parts || !s->ep_cnt) return FP_ERR_INVALID;
+  const int K = pb.K, metric = pb.metric, nov = g.nov, noe = g.noe;
+  const bool msg = metric == FP_METRIC_TM || metric == FP_METRIC_MSM;
+  st.part_vec.assign(s->part_vec, s->part_vec + nov);
+  st.part_sizes.assign(K, 0);
+  for (int v = 0; v < nov; v++) {
+    const int p = st.part_vec[v];
+    if (p < 0 || p >= K) return FP_ERR_INVALID;
+    st.part_sizes[p] += pb.w[v];
+  }
+  if (s->part_sizes)
+    for (int p = 0; p < K; p++)
+      if (s->part_sizes[p] != st.part_sizes[p]) return FP_ERR_INVALID;
+  st.ep_start.assign(g.nptr.begin(), g.nptr.end());
+  st.ep_len.assign(noe, 0);
+  st.ep_part.assign(g.pins, -1);
+  st.ep_cnt.assign(g.pins, 0);
+  // Every list must hold exactly the parts of the net's pins with their counts
+  // (the reference's checkMe invariant, MSM/partition.cpp:2-68).
+  std::vector<int> mark(K, -1), count(K, 0), listed(K, -1);
+  for (int e = 0; e < noe; e++) {
+    const int b = (int)g.nptr[e], size = (int)(g.nptr[e + 1] - g.nptr[e]);
+    if (s->ep_starts[e] != b) return FP_ERR_INVALID;
+    const int len = s->ep_ends[e];   // lambda(e): the list length, as the reference keeps it
+    if (len < 1 || len > size || len > K) return FP_ERR_INVALID;
+    int distinct = 0;
+    for (int k = b; k < b + size; k++) {
+      const int p = st.part_vec[g.npins[k]];
+      if (mark[p] != e) { mark[p] = e; count[p] = 0; distinct++; }
+      count[p]++;
+    }
+    if (distinct != len) return FP_ERR_INVALID;
+    for (int j = 0; j < len; j++) {
+      const int p = s->ep_parts[b + j], c = s->ep_cnt[b + j];
+      if (p < 0 || p >= K || mark[p] != e || listed[p] == e || count[p] != c) return FP_ERR_INVALID;
+      listed[p] = e;
+      st.ep_part[b + j] = p;
+      st.ep_cnt[b + j] = c;
+    }
+    st.ep_len[e] = len;
+  }
+  st.marker.assign(K, -1);
+  if (s->marker)
+    for (int p = 0; p < K; p++) {
+      if (s->marker[p] < -1 || s->marker[p] >= nov) return FP_ERR_INVALID;
+      st.marker[p] = s->marker[p];
+    }
+  // Volumes and messages: as given, else the count over the lists; the arrays
+  // a metric does not keep stay zero (send: MSV, MSRV; recv: MSRV).
+  const bool keep_send = metric == FP_METRIC_MSV || metric == FP_METRIC_MSRV;
+  const bool keep_recv = metric == FP_METRIC_MSRV;
+  st.send.assign(K, 0);
+  st.recv.assign(K, 0);
+  st.msgs.assign(K, 0);
+  if (msg) st.conn.assign((size_t)K * K, 0);
+  for (int e = 0; e < noe; e++) {
+    const int sp = st.part_vec[g.src[e]];
+    const int b = st.ep_start[e];
+    for (int j = 0; j < st.ep_len[e]; j++) {
+      const int p = st.ep_part[b + j];
+      if (p == sp) continue;
+      if (keep_send) st.send[sp]++;
+      if (keep_recv) st.recv[p]++;
+      if (msg) st.conn[(size_t)sp * K + p]++;
+    }
+  }
+  if (msg) {
+    if (metric == FP_METRIC_MSM)
+      for (int p = 0; p < K; p++) st.conn[(size_t)p * K + p] = -1;   // MSM/partition.cpp:101
+    if (s->conn) st.conn.assign(s->conn, s->conn + (size_t)K * K);
+    for (int a = 0; a < K; a++)
+      for (int b = 0; b < K; b++)
+        if (a != b && st.conn[(size_t)a * K + b] > 0) st.msgs[a]++;
+    if (s->msgs) st.msgs.assign(s->msgs, s->msgs + K);
+  }
+  if (s->send && keep_send) st.send.assign(s->send, s->send + K);
+  if (s->recv && keep_recv) st.recv.assign(s->recv, s->recv + K);
+  return FP_OK;
+}
+
 }  // namespace fp
 
 extern "C" {
@@ -184,7 +270,7 @@ int fp_stream_partition(const fp_hypergraph* h, int32_t K, int32_t metric, doubl
     if (out->ep_starts)
       for (int e = 0; e < g.noe; e++) out->ep_starts[e] = (int)g.nptr[e];
     if (out->ep_ends)
-      for (int e = 0; e < g.noe; e++) out->ep_ends[e] = (int)g.nptr[e] + st.ep_len[e];
+      std::copy(st.ep_len.begin(), st.ep_len.end(), out->ep_ends);
     if (out->ep_parts) std::copy(st.ep_part.begin(), st.ep_part.end(), out->ep_parts);
     if (out->ep_cnt) std::copy(st.ep_cnt.begin(), st.ep_cnt.end(), out->ep_cnt);
     if (out->part_sizes) std::copy(st.part_sizes.begin(), st.part_sizes.end(), out->part_sizes);
@@ -200,6 +286,18 @@ int fp_stream_partition(const fp_hypergraph* h, int32_t K, int32_t metric, doubl
   });
 }
 
+
+int fp_check_state(const fp_hypergraph* h, int32_t K, int32_t metric, double eps_factor, const fp_state* st) {
+  return fp::guarded([&]() -> int {
+    if (!h || !st) return FP_ERR_INVALID;
+    fp::HostGraph g;
+    fp::Problem pb;
+    int rc = fp::make_problem(h, K, metric, eps_factor, g, pb);
+    if (rc) return rc;
+    fp::HostState hs;
+    return fp::state_from_caller(g, pb, st, hs);
+  });
+}
 
 int fp_generate(const fp_gen_params* p, fp_graph** out) {
   return fp::guarded([&]() -> int {

@@ -69,6 +69,11 @@ constexpr int kMaxK = 4096;
 // xw = W / K, C = xw * eps_factor) as the reference derives them.
 int make_problem(const fp_hypergraph* h, int K, int metric, double eps_factor, HostGraph& g, Problem& pb);
 
+// Checks a caller's state in the reference's layout (fp_state: ep_ends[e] is
+// the number of parts listed for net e) against g and pb and converts it into
+// the engine's host state; FP_ERR_INVALID if it is not the recount of part_vec.
+int state_from_caller(const HostGraph& g, const Problem& pb, const fp_state* s, HostState& st);
+
 // Runs an entry point's body and turns a C++ exception into a status code, so
 // that nothing thrown crosses the C ABI: a failed allocation is FP_ERR_NOMEM,
 // anything else FP_ERR_INVALID.  `on_throw` releases what the body had built.

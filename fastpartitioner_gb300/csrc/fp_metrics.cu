@@ -329,7 +329,18 @@ extern "C" int fp_metrics_noalloc(int32_t K, int32_t nov, int32_t noe, int64_t p
   long long want = ((long long)noe + (threads / 32) - 1) / (threads / 32);
   long long grid = (long long)nd.num_sms * 4;
   if (grid > want) grid = want > 0 ? want : 1;
-  metrics_nets_checked_kernel<<<(int)grid, threads, smem, st>>>(I, M);
-  metrics_final_checked_kernel<<<1, 1024, 0, st>>>(I, M, reinterpret_cast<long long*>(out));
-  return cudaGetLastError() == cudaSuccess ? FP_OK : FP_ERR_CUDA;
+  // cudaLaunchKernelEx returns each launch's own status, so an error the
+  // caller left pending is neither reported as this call's nor cleared.
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3(threads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  err = cudaLaunchKernelEx(&cfg, metrics_nets_checked_kernel, I, M);
+  if (err != cudaSuccess) return FP_ERR_CUDA;
+  cfg.gridDim = dim3(1);
+  cfg.blockDim = dim3(1024);
+  cfg.dynamicSmemBytes = 0;
+  err = cudaLaunchKernelEx(&cfg, metrics_final_checked_kernel, I, M, reinterpret_cast<long long*>(out));
+  return err == cudaSuccess ? FP_OK : FP_ERR_CUDA;
 }

@@ -266,11 +266,15 @@ int fp_graph_destroy(fp_graph* g);
  * initial stream (partition_gpu_wrapper, TV/partition.cpp:6-26,
  * MGV/partition.cpp:4-27, MSRV/partition.cpp:4-25, TM/partition.cpp:3-7).
  * Sizes: part_vec nov; ep_starts / ep_ends noe; ep_parts / ep_cnt pins (empty
- * slots -1 / 0); part_sizes, marker, send, recv, msgs K; conn K*K row-major. */
+ * slots -1 / 0); part_sizes, marker, send, recv, msgs K; conn K*K row-major.
+ * Net e's list is ep_parts / ep_cnt [ep_starts[e], ep_starts[e] + ep_ends[e]):
+ * ep_ends[e] is lambda(e), the NUMBER of parts listed, not an end offset -- the
+ * stream counts it up from 0 (TV/partition.cpp:1066-1075) and the reference's
+ * metric code reads it as that count (TV(), CN(), shared/metric.cpp:3-14,57-68). */
 typedef struct fp_state {
   int32_t* part_vec;
   int32_t* ep_starts;   /* must equal the net offsets (prefix of net sizes)        */
-  int32_t* ep_ends;
+  int32_t* ep_ends;     /* lambda(e): parts listed for net e                       */
   int32_t* ep_parts;
   int32_t* ep_cnt;
   int32_t* part_sizes;  /* NULL on set: recounted from part_vec and the weights    */
@@ -288,8 +292,15 @@ typedef struct fp_state {
  * arrays before its refinement kernels. */
 int fp_set_state(fp_instance* inst, const fp_state* st);
 /* Copies the current device state out; NULL members are skipped.  ep_starts
- * is filled with the net offsets. */
+ * is filled with the net offsets, ep_ends with lambda(e). */
 int fp_get_state(fp_instance* inst, fp_state* st);
+/* The check fp_set_state applies, on the host alone (no device): FP_OK if `st`
+ * is a valid state of hypergraph h for this K and metric -- part ids in [0, K),
+ * ep_starts the net offsets, every net's list (ep_ends[e] = lambda(e) entries)
+ * exactly the parts of its pins with their counts, part_sizes (if given) the
+ * weighted recount -- else FP_ERR_INVALID.  The reference keeps this invariant
+ * and checks it in checkMe (MSM/partition.cpp:2-68). */
+int fp_check_state(const fp_hypergraph* h, int32_t K, int32_t metric, double eps_factor, const fp_state* st);
 /* The metric's streaming initial partition on the host (the CPU half of the
  * reference's partition_gpu(): TV/partition.cpp:207-264, CN/partition.cpp:
  * 132-221, TM/partition.cpp:87-250, MSM/partition.cpp:146-309,

@@ -224,3 +224,61 @@ def flat_lists(hg, ep_len, ep_part):
     starts = hg.nptr[:-1].astype(np.int64)
     idx = np.concatenate([np.arange(s, s + n) for s, n in zip(starts, ep_len)]) if len(ep_len) else np.zeros(0, np.int64)
     return ep_part[idx.astype(np.int64)] if idx.size else np.zeros(0, np.int32)
+
+
+def run_reference_wrapper_state(hg, K: int, metric: str, timeout: float = 600) -> dict:
+    """Runs the reference's own partition_gpu() (TV, CN, TM, MSV, MSRV) through
+    the harness, whose stand-in partition_gpu_wrapper records the state arrays
+    partition_gpu() hands to its GPU wrapper after the initial stream: the
+    exact input a drop-in shim receives.  Returns them by name (part_vec,
+    psizes, ep_start, ep_ends, ep_parts, ep_cnt, and marker / send / conn /
+    msgs where the metric's wrapper takes them)."""
+    metric = metric.upper()
+    exe = REF_DIR / REF_BIN[metric]
+    if metric == "MSM" or not exe.exists():
+        raise FileNotFoundError(f"no partition_gpu harness for {metric}")
+    with tempfile.TemporaryDirectory(prefix="fpwrap") as td:
+        inst = Path(td) / "inst.fphg"
+        hg.save_fphg(inst)
+        prefix = str(Path(td) / "cap")
+        res = subprocess.run([str(exe), str(inst), str(K), "1", "0", prefix], capture_output=True, text=True,
+                             timeout=timeout, cwd=td)
+        if res.returncode != 0:
+            raise ReferenceRunError(res.returncode, f"reference partition_gpu failed ({res.returncode}):\n"
+                                                    f"{res.stdout[-2000:]}\n{res.stderr[-2000:]}")
+        raw = Path(prefix + ".wrap").read_bytes()
+    out, pos = {}, 0
+    while pos < len(raw):
+        name = raw[pos:pos + 8].rstrip(b"\0").decode()
+        n = int(np.frombuffer(raw, np.int64, 1, pos + 8)[0])
+        out[name] = np.frombuffer(raw, np.int32, n, pos + 16).copy()
+        pos += 16 + 4 * n
+    return out
+
+
+_ref_metrics_lib = None
+
+
+def reference_metrics(hg, K: int, part_vec, ep_starts, ep_ends, ep_parts, ep_cnt) -> dict:
+    """The reference's own metric evaluators (shared/metric.cpp, built into
+    oracle/_ref/libref_metrics.so) on a state in the reference's layout:
+    TV, CN, TM, MSM, MSV, MSRV as partition_gpu() computes them after
+    refinement, plus TV_lambda = TV(ep_ends), its pre-refinement form."""
+    global _ref_metrics_lib
+    if _ref_metrics_lib is None:
+        path = REF_DIR / "libref_metrics.so"
+        if not path.exists():
+            raise FileNotFoundError(f"{path} not built (reference sources unavailable)")
+        L = C.CDLL(str(path))
+        L.ref_metrics.argtypes = [C.c_int, C.c_int, C.c_int, C.c_longlong] + [C.c_void_p] * 10
+        L.ref_metrics.restype = C.c_int
+        _ref_metrics_lib = L
+    a = lambda x, dt: np.ascontiguousarray(x, dtype=dt)
+    sizes = np.diff(hg.nptr).astype(np.uint32)
+    arrs = [a(hg.vptr, np.uint32), a(hg.vnets, np.uint32), sizes, a(hg.src, np.int32), a(part_vec, np.int32),
+            a(ep_starts, np.int32), a(ep_ends, np.int32), a(ep_parts, np.int32), a(ep_cnt, np.int32)]
+    out = np.zeros(7, np.int64)
+    _ref_metrics_lib.ref_metrics(K, hg.nov, hg.noe, hg.pins, *[x.ctypes.data for x in arrs], out.ctypes.data)
+    d = dict(zip(OUTPUT_ORDER, map(int, out[:6])))
+    d["TV_lambda"] = int(out[6])
+    return d

@@ -18,7 +18,9 @@
 // ordered per-net part lists and then forwards to the reference evaluator.
 //
 // usage: ref_<metric> <instance.fphg> <K> <passes> <threads> <capture-prefix|->
-//        threads == 1 runs partition(), otherwise partition_par(..., threads).
+//        threads == 1 runs partition(), threads > 1 partition_par(..., threads),
+//        threads == 0 partition_gpu() (TV, CN, TM, MGV, MSRV) with the
+//        recording wrappers below in place of the reference's gpu_partition.cu.
 
 #include <cstdio>
 #include <cstdlib>
@@ -60,21 +62,74 @@ int MGAV_Scratch(int* part_vec, unsigned int* row_ptr, unsigned int* col_ind, in
                           net_appearence, K, nov, noe, pins);
 }
 
-// The GPU wrappers the reference partition.cpp files declare; never called here.
+// The GPU wrappers the reference partition.cpp files declare.  partition()
+// and partition_par() never call them; partition_gpu() (threads == 0 below)
+// does, after its initial stream, with the state arrays it would hand to the
+// GPU.  These stand-ins record exactly those arrays in <capture-prefix>.wrap
+// and return without refining, so that a test sees the state a drop-in shim
+// receives at the boundary.
+//
+// .wrap layout: a sequence of records {char name[8]; int64 count; int32 data[count]}.
+static void wrap_put(FILE* f, const char* name, const int* data, long long n) {
+  char tag[8] = {0};
+  for (int i = 0; i < 8 && name[i]; i++) tag[i] = name[i];
+  std::fwrite(tag, 1, 8, f);
+  std::fwrite(&n, 8, 1, f);
+  if (n > 0) std::fwrite(data, 4, (size_t)n, f);
+}
+static FILE* wrap_open() {
+  if (g_capture_prefix.empty() || g_capture_prefix == "-") return nullptr;
+  return std::fopen((g_capture_prefix + ".wrap").c_str(), "wb");
+}
+static void wrap_common(FILE* f, int nov, int noe, long long pins, int K, int* part_vec, int* part_sizes,
+                        int* ep_starts, int* ep_ends, int* ep_parts, int* ep_cnt) {
+  const int dims[4] = {nov, noe, (int)pins, K};
+  wrap_put(f, "dims", dims, 4);
+  wrap_put(f, "part_vec", part_vec, nov);
+  wrap_put(f, "psizes", part_sizes, K);
+  wrap_put(f, "ep_start", ep_starts, noe);
+  wrap_put(f, "ep_ends", ep_ends, noe);
+  wrap_put(f, "ep_parts", ep_parts, pins);
+  wrap_put(f, "ep_cnt", ep_cnt, pins);
+}
+
 #if defined(FP_REF_TV) || defined(FP_REF_MSRV)
-void partition_gpu_wrapper(unsigned int*, unsigned int*, unsigned int*, int, int, long long, int*, int*, int,
-                           int*, int*, int*, int*, int*, int*, int*, int*, int*, double*, int, double) {
-  std::abort();
+void partition_gpu_wrapper(unsigned int*, unsigned int*, unsigned int*, int nov, int noe, long long pins, int*,
+                           int*, int K, int*, int* marker, int*, int* part_sizes, int* ep_starts, int* ep_ends,
+                           int* ep_parts, int* part_vec, int* ep_cnt, double*, int, double) {
+  if (FILE* f = wrap_open()) {
+    wrap_common(f, nov, noe, pins, K, part_vec, part_sizes, ep_starts, ep_ends, ep_parts, ep_cnt);
+    wrap_put(f, "marker", marker, K);
+    std::fclose(f);
+  }
 }
 #elif defined(FP_REF_CN)
-void partition_gpu_wrapper(unsigned int*, unsigned int*, unsigned int*, int, int, long long, int*, int*, int,
-                           int*, int, int, unsigned int*, unsigned int*, int*, int*, int*, int*, int*, int*) {
-  std::abort();
+void partition_gpu_wrapper(unsigned int*, unsigned int*, unsigned int*, int nov, int noe, long long pins, int*,
+                           int*, int K, int*, int, int, unsigned int*, unsigned int*, int* part_sizes,
+                           int* ep_starts, int* ep_parts, int* ep_ends, int* ep_cnt, int* part_vec) {
+  if (FILE* f = wrap_open()) {
+    wrap_common(f, nov, noe, pins, K, part_vec, part_sizes, ep_starts, ep_ends, ep_parts, ep_cnt);
+    std::fclose(f);
+  }
 }
 #elif defined(FP_REF_TM)
-void partition_gpu_wrapper(unsigned int*, unsigned int*, unsigned int*, int, int, long long, int*, int*, int,
-                           int*, int, int, int*, int*, int*, int*, int*, int**, int*, int*) {
-  std::abort();
+static void tm_capture(int nov, int noe, long long pins, int K, int* part_vec, int* ep_starts, int* ep_parts,
+                       int* ep_ends, int* ep_cnt, int** part_connections, int* part_sizes, int* part_messages) {
+  if (FILE* f = wrap_open()) {
+    wrap_common(f, nov, noe, pins, K, part_vec, part_sizes, ep_starts, ep_ends, ep_parts, ep_cnt);
+    std::vector<int> conn((size_t)K * K);
+    for (int a = 0; a < K; a++)
+      for (int b = 0; b < K; b++) conn[(size_t)a * K + b] = part_connections[a][b];
+    wrap_put(f, "conn", conn.data(), (long long)K * K);
+    wrap_put(f, "msgs", part_messages, K);
+    std::fclose(f);
+  }
+}
+void partition_gpu_wrapper(unsigned int*, unsigned int*, unsigned int*, int nov, int noe, long long pins, int*,
+                           int*, int K, int*, int, int, int* part_vec, int* ep_starts, int* ep_parts, int* ep_ends,
+                           int* ep_cnt, int** part_connections, int* part_sizes, int* part_messages) {
+  tm_capture(nov, noe, pins, K, part_vec, ep_starts, ep_parts, ep_ends, ep_cnt, part_connections, part_sizes,
+             part_messages);
 }
 void partition_gpu_optimized_wrapper(unsigned int*, unsigned int*, unsigned int*, int, int, long long, int*, int*,
                                      int, int*, int, int, int*, int*, int*, int*, int*, int**, int*, int*) {
@@ -85,9 +140,14 @@ void partition_gpu_threads_wrapper(unsigned int*, unsigned int*, unsigned int*, 
   std::abort();
 }
 #elif defined(FP_REF_MGV)
-void partition_gpu_wrapper(unsigned int*, unsigned int*, unsigned int*, int, int, long long, int*, int*, int,
-                           int*, int, int, int*, double*, int*, int*, int*, int*, int*, int*, int*, int*) {
-  std::abort();
+void partition_gpu_wrapper(unsigned int*, unsigned int*, unsigned int*, int nov, int noe, long long pins, int*,
+                           int*, int K, int*, int, int, int* send_volumes, double*, int*, int*, int* ep_starts,
+                           int* ep_parts, int* ep_ends, int* ep_cnt, int* part_sizes, int* part_vec) {
+  if (FILE* f = wrap_open()) {
+    wrap_common(f, nov, noe, pins, K, part_vec, part_sizes, ep_starts, ep_ends, ep_parts, ep_cnt);
+    wrap_put(f, "send", send_volumes, K);
+    std::fclose(f);
+  }
 }
 #endif
 
@@ -153,6 +213,18 @@ int main(int argc, char** argv) {
                                                                           : g_capture_prefix;
   int refi_opt = passes > 0 ? 1 : 0;
   int refi_iter = passes > 0 ? passes : 1;
+#if !defined(FP_REF_MSM)
+  if (threads == 0) {
+#if defined(FP_REF_CN)
+    partition_gpu(row_ptr, col_ind, net_app, nov, noe, pins, ew, srcs, K, order, fname, refi_opt, refi_iter,
+                  col_ptr, row_ind);
+#else
+    partition_gpu(row_ptr, col_ind, net_app, nov, noe, pins, ew, srcs, K, order, fname, refi_opt, refi_iter);
+#endif
+    std::fflush(stdout);
+    return 0;
+  }
+#endif
 #if defined(FP_REF_CN)
   if (threads <= 1)
     partition(row_ptr, col_ind, net_app, nov, noe, pins, ew, srcs, K, order, fname, refi_opt, refi_iter, col_ptr,

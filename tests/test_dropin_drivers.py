@@ -2,10 +2,11 @@
 CN/cn.cpp, TM/tm.cpp, MGV/mgv.cpp, MSRV/mgav.cpp, MSM/msm.cpp, with their
 partition.cpp and shared/, from the staging copy oracle/Makefile keeps) is
 built with its shim from INTEGRATION.md in place of gpu_partition.cu and
-linked against libfastpart.so.  Here (no GPU) every driver must link; those
-whose command line reaches the CPU refinement run it, and with -g the GPU branch
-reports the library's error instead of crashing.  The GPU comparison (-g 1
-against the CPU refinement) runs with the GPU tests."""
+linked against libfastpart.so, with the driver fixes INTEGRATION.md lists
+applied to a copy of the driver source.  Here (no GPU) every driver must link;
+those whose command line reaches the CPU refinement run it, and with -g the GPU
+branch reports the library's error instead of crashing.  The GPU comparison
+(-g 1 against the CPU refinement) runs with the GPU tests."""
 import re
 import shutil
 import subprocess
@@ -44,11 +45,40 @@ def shim_source(tmp, metric):
     return path
 
 
+def driver_fixes():
+    """{driver path: [(kind, anchor, code)]} from INTEGRATION.md's "driver fix"
+    blocks: kind "insert after" puts code after the anchor line, "replace"
+    puts it in place of the anchor text (first occurrence)."""
+    blocks = re.findall(r"```(?:cpp|c\+\+)\n(.*?)```", (ROOT / "INTEGRATION.md").read_text(), re.S)
+    fixes = {}
+    for b in blocks:
+        head, _, code = b.partition("\n")
+        m = re.match(r'// driver fix (\S+): (insert after|replace) "(.*)"', head)
+        if m:
+            fixes.setdefault(m.group(1), []).append((m.group(2), m.group(3), code))
+    return fixes
+
+
+def fixed_driver_source(d, driver):
+    """The driver's source with INTEGRATION.md's fixes for it applied."""
+    text = (SRC / d / driver).read_text()
+    for kind, anchor, code in driver_fixes().get(f"{d}/{driver}", []):
+        if kind == "insert after":
+            line = anchor + "\n"
+            assert line in text, (driver, anchor)
+            text = text.replace(line, line + code, 1)
+        else:
+            assert anchor in text, (driver, anchor)
+            text = text.replace(anchor, code.rstrip("\n"), 1)
+    return text
+
+
 def build_driver(fp, tmp, metric):
     d, driver, _ = DRIVERS[metric]
     work = tmp / metric
     work.mkdir()
     shim = shim_source(work, metric)
+    (work / driver).write_text(fixed_driver_source(d, driver))
     lib = fp.library_path()
     extra = []
     if metric == "MSM":
@@ -56,7 +86,7 @@ def build_driver(fp, tmp, metric):
         extra = ["-include", str(work / "msm_decl.h")]
     exe = work / f"{metric.lower()}_gb300"
     cmd = ["g++", *CFLAGS, *extra, "-I", str(SRC / d), "-I", str(SRC / "shared"), "-I", str(ROOT / "include"),
-           "-I", str(work), str(SRC / d / driver), str(SRC / d / "partition.cpp"), str(SRC / "shared" / "metric.cpp"),
+           "-I", str(work), str(work / driver), str(SRC / d / "partition.cpp"), str(SRC / "shared" / "metric.cpp"),
            str(SRC / "shared" / "utils.cpp"), str(SRC / "shared" / "hypergraph_rw.cpp"), str(shim),
            "-L", str(lib.parent), "-lfastpart", f"-Wl,-rpath,{lib.parent}", "-o", str(exe)]
     res = subprocess.run(cmd, capture_output=True, text=True)
@@ -85,8 +115,24 @@ def after_lines(text):
 
 def square_case(fp, seed):
     """A square instance (the TM / MGV / MSRV / MSM drivers read file lines as
-    vertices, so only a square file is defined for them)."""
-    return fp.generate(fp.GenSpec.zipf(3000, 3000, 2.1, 2, 120, beta=1.2, seed=seed))
+    vertices, so only a square file is defined for them) in which every vertex
+    lies on a net: those drivers read each vertex id as a net, and the
+    reference has no defined source for an empty net.  3,000 nets keep the
+    reference's one-int overflow past ep_starts (TM/partition.cpp:71-74,
+    CN/partition.cpp:116) inside the allocator's rounding."""
+    import numpy as np
+    hg = fp.generate(fp.GenSpec.zipf(3000, 3000, 2.1, 2, 120, beta=1.2, seed=seed))
+    deg = np.diff(hg.vptr)
+    lonely = np.flatnonzero(deg == 0)
+    if lonely.size == 0:
+        return hg
+    rng = np.random.default_rng(seed)
+    nets = [list(hg.npins[hg.nptr[e]:hg.nptr[e + 1]]) for e in range(hg.noe)]
+    for v in lonely:
+        nets[int(rng.integers(hg.noe))].append(int(v))       # appended: pins stay unsorted
+    nptr = np.cumsum([0] + [len(n) for n in nets]).astype(np.uint32)
+    npins = np.concatenate([np.array(n, np.uint32) for n in nets])
+    return fp.Hypergraph.from_nets(hg.nov, nptr, npins)
 
 
 # Two drivers' command lines are broken in the reference itself:

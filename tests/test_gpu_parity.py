@@ -238,6 +238,7 @@ def test_gpu_set_state_round_trip(fp, orc, gpu_engine, metric):
         st = a.get_state()
     np.testing.assert_array_equal(st["part_vec"], o["part_vec_init"])
     np.testing.assert_array_equal(st["ep_starts"], hg.nptr[:-1].astype(np.int32))
+    np.testing.assert_array_equal(st["ep_ends"], o["ep_len_init"])      # lambda(e), the reference's layout
     variants = [dict(st)]
     if metric not in ("TM", "MSM"):
         variants.append({k: st[k] for k in ("part_vec", "ep_starts", "ep_ends", "ep_parts", "ep_cnt", "marker")})
@@ -251,6 +252,13 @@ def test_gpu_set_state_round_trip(fp, orc, gpu_engine, metric):
             b.refine(passes)
             np.testing.assert_array_equal(b.partition(), o["part_vec"], err_msg=f"{metric} variant {i}")
             assert b.metrics() == o["metrics_final"], f"{metric} variant {i}"
+            # the refined state, read out as a shim hands it back, is what the
+            # reference's own metric code (shared/metric.cpp) evaluates
+            if (orc.REF_DIR / "libref_metrics.so").exists():
+                r = b.get_state()
+                ref = orc.reference_metrics(hg, K, r["part_vec"], r["ep_starts"], r["ep_ends"], r["ep_parts"],
+                                            r["ep_cnt"])
+                assert {k: ref[k] for k in o["metrics_final"]} == o["metrics_final"], f"{metric} variant {i}"
     # a list that disagrees with the part vector is rejected
     bad = dict(st)
     bad["ep_cnt"] = st["ep_cnt"].copy()

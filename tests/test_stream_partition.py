@@ -38,7 +38,7 @@ def test_stream_matches_oracle(name, mk, K, eps, shuffle, metric):
     assert o["status"] == 0
     np.testing.assert_array_equal(s["part_vec"], o["part_vec_init"])
     np.testing.assert_array_equal(s["ep_starts"], hg.nptr[:-1].astype(np.int32))
-    np.testing.assert_array_equal(s["ep_ends"] - s["ep_starts"], o["ep_len_init"])
+    np.testing.assert_array_equal(s["ep_ends"], o["ep_len_init"])   # lambda(e), the reference's layout
     np.testing.assert_array_equal(s["ep_parts"], o["ep_part_init"])
     np.testing.assert_array_equal(s["ep_cnt"], o["ep_cnt_init"])
     w = np.ones(hg.nov, np.int64) if hg.weights is None else hg.weights.astype(np.int64)
@@ -81,6 +81,6 @@ def test_stream_matches_oracle_odd_K_and_status(name, mk, K, eps, metric):
         return
     s = fp.stream_partition(hg, K, metric, eps)
     np.testing.assert_array_equal(s["part_vec"], o["part_vec_init"])
-    np.testing.assert_array_equal(s["ep_ends"] - s["ep_starts"], o["ep_len_init"])
+    np.testing.assert_array_equal(s["ep_ends"], o["ep_len_init"])   # lambda(e), the reference's layout
     np.testing.assert_array_equal(s["ep_parts"], o["ep_part_init"])
     np.testing.assert_array_equal(s["ep_cnt"], o["ep_cnt_init"])

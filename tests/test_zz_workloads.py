@@ -138,7 +138,7 @@ def test_readme_example_on_the_device(fp, gpu_engine, metric):
         for j, p in enumerate(order):
             ep_parts[b + j] = p
             ep_cnt[b + j] = int(np.sum(pv[hg.npins[hg.nptr[e]:hg.nptr[e + 1]]] == p))
-        ends[e] = b + len(order)
+        ends[e] = len(order)                 # lambda(e), as the reference keeps it
     with gpu_engine.instance(hg, K, metric) as inst:
         inst.set_state(pv, hg.nptr[:-1].astype(np.int32), ends, ep_parts, ep_cnt)
         m = inst.metrics()
@@ -153,13 +153,13 @@ from test_dropin_drivers import CPU_PATH, after_lines, drivers, run_driver, squa
 def test_reference_driver_on_the_device(fp, gpu_engine, drivers, tmp_path, metric):
     """The reference's own driver with -g 1 -- its partition_gpu(), the shim of
     INTEGRATION.md, libfastpart.so on the GPU -- refines exactly as its CPU path
-    (-g 0): the same After Refinement lines and, for CN, the same part vector
-    file.  The TV and CN drivers hand their metric code wrong or uninitialised
-    net sizes (TV/tv.cpp:51, CN/cn.cpp:280-284), so MGV and MGAV, which use them,
-    are left out there.  The files keep their nets' pins unsorted, as drawn."""
+    (-g 0): the same six After Refinement lines and, for CN, the same part
+    vector file.  The drivers carry INTEGRATION.md's fixes of the net sizes the
+    TV and CN drivers hand their metric code (TV/tv.cpp:51, CN/cn.cpp:280-284).
+    The files keep their nets' pins unsorted, as drawn."""
     if isinstance(drivers[metric], str):
         pytest.skip(f"the reference driver did not build on this machine: {drivers[metric][-300:]}")
-    skip = {"MGV", "MGAV"} if metric in ("TV", "CN") else set()
+    skip = set()
     for seed, K, passes in ((71, 8, 3), (72, 32, 2)):
         hg = square_case(fp, seed)
         outs = []

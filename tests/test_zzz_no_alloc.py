@@ -27,7 +27,7 @@ def device_state(torch, hg, st, dev):
     """The state arrays fp_metrics_noalloc reads, as int32 device tensors
     (allocated here by the test, not by the library)."""
     t = lambda a: torch.from_numpy(np.ascontiguousarray(a).astype(np.int32)).to(dev)
-    ep_len = st["ep_ends"] - st["ep_starts"]
+    ep_len = st["ep_ends"]                     # lambda(e) per net
     return dict(nptr=t(hg.nptr.astype(np.int64)), src=t(hg.src), part_vec=t(st["part_vec"]), ep_len=t(ep_len),
                 ep_part=t(st["ep_parts"]))
 
