@@ -5,7 +5,10 @@ Workload (default "zipf4m"): all six metrics (CN, TV, TM, MSM, MSV, MSRV), each 
 its own resident instance: K = 256, eps = 0.05 (C = (W/K) * 1.05),
 4,194,304 vertices and 4,194,304 nets, net sizes Zipf(2.1) clipped to
 [2, 10000], pins drawn by a Zipf(1.5) vertex popularity, source = first drawn
-pin, vertex weight = degree; 10 refinement passes.  Synthetic and seeded.
+pin; 10 refinement passes.  Synthetic and seeded.  The headline line uses unit
+vertex weights, the reference's own semantics (it counts vertices), so that the
+reference arm runs the same instance; the workload's degree weights are timed
+in the same run as a second figure ("degree_weights").
 
 A step is one refinement pass of each of the six resident instances; the
 instances carry their state between steps and restart from the streaming
@@ -17,8 +20,11 @@ six metrics (the reference's "Refinement took" span).
           refinement launch
   e2e     through the C ABI with host buffers: host -> device upload of the
           state, the passes, device -> host copy of the part vector
-  cpu_baseline / --impl reference: the reference's own OpenMP partition_par()
-          (compiled from its sources into oracle/_ref) on the host cores
+  --impl reference: the reference's own OpenMP partition_par() (compiled from
+          its sources into oracle/_ref) on every host core, on the same instance
+          (drawn by the oracle's generator, no product library loaded) and the
+          same pass schedule; cpu_baseline is the same on the first passes of
+          the schedule (a bounded sample)
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 """
@@ -198,6 +204,64 @@ def whole_job(units_per_rank, seconds, device="cpu"):
     return units_per_rank * nranks / seconds, seconds, nranks
 
 
+def time_schedule(eng, stream, hg, w, metrics, passes, steps, warmup, account=True):
+    """Resident instances of every metric on hg; W untimed warm-up steps, then
+    `steps` timed steps (one pass of each instance per step, restarting from
+    the initial partition every `passes` steps).  Returns (instances,
+    per-metric seconds per step, per-metric algorithmic bytes per step,
+    seconds of host initial partitions)."""
+    import torch
+    insts = {}
+    t_init = time.time()
+    for m in metrics:
+        inst = eng.instance(hg, w["K"], m, w["eps"])
+        inst.initial_partition()
+        insts[m] = inst
+    t_init = time.time() - t_init
+    done = {"n": 0}
+
+    def reset_all():
+        for inst in insts.values():
+            inst.reset_state()
+        done["n"] = 0
+
+    def one_step(timed, acc=None):
+        if done["n"] == passes:
+            reset_all()
+        out = {}
+        for m in metrics:
+            inst = insts[m]
+            if acc is not None:
+                ln, _, _ = inst.lists()
+                before = inst.partition()
+            torch.cuda.synchronize()
+            if timed:
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+            inst.refine(1)
+            if timed:
+                e1.record(stream)
+                e1.synchronize()
+                out[m] = e0.elapsed_time(e1) / 1e3
+            if acc is not None:
+                after = inst.partition()
+                acc[m].append(algorithmic_bytes(m, hg, ln, before != after, w["K"]))
+        done["n"] += 1
+        return out
+
+    for _ in range(warmup):
+        one_step(False)
+    reset_all()
+    torch.cuda.synchronize()
+    per_metric = {m: [] for m in metrics}
+    bytes_acc = {m: [] for m in metrics} if account else None
+    for _ in range(steps):
+        for m, t in one_step(True, bytes_acc).items():
+            per_metric[m].append(t)
+    torch.cuda.synchronize()
+    return insts, per_metric, bytes_acc, t_init
+
+
 def run_ours(args):
     import torch
     import fastpartitioner_gb300 as fp
@@ -217,74 +281,23 @@ def run_ours(args):
     passes = args.passes or w["passes"]
     metrics = metrics_for(w, args.metrics)
     t_gen = time.time()
-    hg = fp.generate(spec_for(fp, w, args.scale))
+    hg = fp.generate(spec_for(fp, w, args.scale, unit_weights=True))
     t_gen = time.time() - t_gen
     stream = torch.cuda.Stream(device=device)
     eng = fp.Engine(device)
     eng.set_stream(stream.cuda_stream)
-    insts = {}
-    t_init = time.time()
-    for m in metrics:
-        inst = eng.instance(hg, w["K"], m, w["eps"])
-        inst.initial_partition()
-        insts[m] = inst
-    t_init = time.time() - t_init
 
-    # A step is one refinement pass of every metric's instance; the instances
-    # carry their state from step to step and restart from the initial
-    # partition (untimed) after every `passes` steps, so the default
-    # --steps 10 times one complete 10-pass schedule.
-    done = {"n": 0}
-
-    def reset_all():
-        for inst in insts.values():
-            inst.reset_state()
-        done["n"] = 0
-
-    def one_step(timed, account=None):
-        if done["n"] == passes:
-            reset_all()
-        out = {}
-        for m in metrics:
-            inst = insts[m]
-            if account is not None:
-                ln, _, _ = inst.lists()
-                before = inst.partition()
-            torch.cuda.synchronize()
-            if timed:
-                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                e0.record(stream)
-            inst.refine(1)
-            if timed:
-                e1.record(stream)
-                e1.synchronize()
-                out[m] = e0.elapsed_time(e1) / 1e3
-            if account is not None:
-                after = inst.partition()
-                account[m].append(algorithmic_bytes(m, hg, ln, before != after, w["K"]))
-        done["n"] += 1
-        return out
-
-    for _ in range(args.warmup):
-        one_step(False)
-    reset_all()
+    # Headline: unit weights, the reference's semantics.
     if dist:
         tdist.barrier()
-    torch.cuda.synchronize()
-    per_metric = {m: [] for m in metrics}
-    bytes_acc = {m: [] for m in metrics}
-    launches = 0
     with Clocks(device) as clk:
-        for _ in range(args.steps):
-            r = one_step(True, bytes_acc)
-            for m, t in r.items():
-                per_metric[m].append(t)
-            launches += len(metrics)
-    torch.cuda.synchronize()
+        insts, per_metric, bytes_acc, t_init = time_schedule(eng, stream, hg, w, metrics, passes, args.steps,
+                                                             args.warmup)
     if dist:
         tdist.barrier()
-    value, total_t, nranks = whole_job(hg.pins * len(metrics) * args.steps,
-                                       sum(sum(v) for v in per_metric.values()), f"cuda:{device}")
+    launches = len(metrics) * args.steps
+    total_t = sum(sum(v) for v in per_metric.values())
+    value, total_t, nranks = whole_job(hg.pins * len(metrics) * args.steps, total_t, f"cuda:{device}")
 
     # e2e: the call a user makes per metric -- host state -> device, all passes,
     # part vector -> host -- timed on the wall clock, one schedule.
@@ -302,6 +315,8 @@ def run_ours(args):
         h2d += inst.state_bytes()
         d2h += pv.nbytes
     e2e_value, e2e_t, _ = whole_job(hg.pins * passes * len(metrics), e2e_t, f"cuda:{device}")
+    for inst in insts.values():
+        inst.close()
 
     # Roofline per kernel: algorithmic bytes of one launch (one pass of one
     # metric) / its CUDA-event duration; the dominant kernel is the one with the
@@ -323,10 +338,30 @@ def run_ours(args):
                             "achieved_gbs": ach, "frac": ach / peak}
     dom = max(per_kernel, key=lambda n: per_kernel[n]["share"])
     traffic = measured_traffic(dom, args.config, args.scale)
+    unique = unique_bytes(hg, w["K"])
+    dom_metrics = per_kernel[dom]["metrics"]
+    uniq_per_launch = sum(unique[m] * len(per_metric[m]) for m in dom_metrics) / per_kernel[dom]["launches"]
+    uniq_gbs = uniq_per_launch / (per_kernel[dom]["avg_launch_ms"] / 1e3) / 1e9
+
+    # Second figure: the workload's degree weights (the reference has no vertex
+    # weights, so the headline and the reference arm use unit weights).
+    degree = None
+    if w["weight_rule"] and not args.no_degree:
+        hgd = fp.generate(spec_for(fp, w, args.scale))
+        di, dpm, _, dinit = time_schedule(eng, stream, hgd, w, metrics, passes, args.steps, args.warmup,
+                                          account=False)
+        for inst in di.values():
+            inst.close()
+        dt = sum(sum(v) for v in dpm.values())
+        dval, dt, _ = whole_job(hgd.pins * len(metrics) * args.steps, dt, f"cuda:{device}")
+        degree = {"value": dval, "unit": "pins/s", "ms_per_step": dt / args.steps * 1e3,
+                  "per_metric_pins_per_s": {m: hgd.pins * len(v) / sum(v) for m, v in dpm.items()},
+                  "per_metric_ms_per_pass": {m: 1e3 * statistics.mean(v) for m, v in dpm.items()},
+                  "host_initial_partition_s": round(dinit, 2)}
 
     cpu = None
     if not args.no_cpu_baseline and rank == 0:
-        cpu = cpu_baseline(fp, w, args)
+        cpu = cpu_baseline(w, args, per_metric)
     clocks = clk.summary()
     line = {
         "metric": METRIC,
@@ -342,11 +377,9 @@ def run_ours(args):
         "dtype": "int32",
         "data": "synthetic (seeded generator, fastpartitioner_gb300/csrc/fp_gen.cpp)",
         "config": {
-            "workload": f"{args.config}: {hg.nov} vertices, {hg.noe} nets, {hg.pins} pins, K={w['K']}, "
-                        f"eps factor {w['eps']}, {passes}-pass schedule, metrics {','.join(metrics)}",
-            "step": "one refinement pass of each metric's resident instance (state carried between steps; "
-                    f"restart from the initial partition every {passes} steps, untimed)",
-            "weights": "degree" if w["weight_rule"] else "unit",
+            "workload": workload_text(args.config, w, hg.nov, hg.noe, hg.pins, passes, metrics),
+            "step": STEP_TEXT.format(passes=passes),
+            "weights": "unit (the reference counts vertices); degree weights in degree_weights",
             "l2": "inputs larger than L2 (per-instance CSRs and lists exceed 129 MB)" if hg.pins > 8_000_000
                   else "inputs smaller than L2",
             "per_metric_pins_per_s": {m: hg.pins * len(v) / sum(v) for m, v in per_metric.items()},
@@ -357,18 +390,19 @@ def run_ours(args):
             "parallelism": "one instance per metric on one GPU (replicas only across GPUs)",
             "e2e_step": f"per metric: reset_state (host -> device) + refine({passes}) + partition (device -> host)",
         },
+        "degree_weights": degree,
         "e2e": {"value": e2e_value, "unit": "pins/s", "h2d_bytes_per_step": h2d // len(metrics),
                 "d2h_bytes_per_step": d2h // len(metrics)},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": per_kernel[dom]["achieved_gbs"], "peak": peak,
                      "unit": "GB/s", "frac": per_kernel[dom]["achieved_gbs"] / peak,
                      "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
-                     else peak_kind, "traffic": traffic, "per_kernel": per_kernel},
+                     else peak_kind, "traffic": traffic,
+                     "unique_bytes_per_launch": int(uniq_per_launch), "unique_achieved": uniq_gbs,
+                     "unique_frac": uniq_gbs / peak, "per_kernel": per_kernel},
         "cpu_baseline": cpu,
         "clocks": clocks,
     }
-    for inst in insts.values():
-        inst.close()
     eng.close()
     if dist:
         tdist.destroy_process_group()
@@ -376,61 +410,121 @@ def run_ours(args):
         print(json.dumps(line), flush=True)
 
 
-# A run of the reference harness has ended with SIGSEGV (once in about 500
-# CN runs on 8 threads; not reproduced at 1 thread, nor in 400 later runs).  A
-# run that a signal ended is run again, up to this many times, and the number
-# of such runs is reported with the baseline.
-REFERENCE_TRIES = 5
+STEP_TEXT = ("one refinement pass of each metric's resident instance (state carried between steps; "
+             "restart from the initial partition every {passes} steps, untimed)")
 
 
-def run_reference_retrying(oracle, hg, K, metric, passes, threads):
-    """oracle.run_reference, again after a run that a signal ended; returns
-    (result, crashed runs)."""
+def workload_text(name, w, nov, noe, pins, passes, metrics):
+    """The workload string, the same on both arms."""
+    return (f"{name}: {nov} vertices, {noe} nets, {pins} pins, unit weights, K={w['K']}, eps factor {w['eps']}, "
+            f"{passes}-pass schedule, metrics {','.join(metrics)}")
+
+
+def unique_bytes(hg, K):
+    """Bytes a pass touches at least once (each array read once, the refined
+    arrays written once): vertex CSR, net offsets, part vector, the per-net
+    (part, count) lists; the LDG and message metrics also read the sources and
+    the net -> pins CSR is not needed; TM / MSM also a K x K count table.  A
+    per-pass lower bound against which re-reads of the lists show up."""
+    P, nov, noe = hg.pins, hg.nov, hg.noe
+    base = 4 * (nov + 1) + 4 * P + 4 * (noe + 1) + 2 * 4 * nov + 2 * 4 * (noe + 2 * P)
+    out = {m: base + 4 * noe for m in METRICS}
+    out["CN"] = 4 * (noe + 1) + 4 * P + 2 * 4 * nov + 2 * 4 * (noe + 2 * P)
+    for m in ("TM", "MSM"):
+        out[m] += 4 * K * K
+    return out
+
+
+# The reference's partition_par() is racy: on small instances at K = 256 with 8
+# threads, 8 of 20 TV runs and up to 10 of 20 CN runs ended with SIGSEGV (the
+# full-size instance ran cleanly).  A run that a signal ended is run again, up
+# to this many times, and the number of such runs is reported with the baseline.
+REFERENCE_TRIES = 12
+
+
+def run_reference_retrying(oracle, path, K, metric, passes, threads):
+    """oracle.run_reference_file, again after a run that a signal ended;
+    returns (result, crashed runs)."""
     crashes = 0
     while True:
         try:
-            return oracle.run_reference(hg, K, metric, passes, threads=threads, capture=False), crashes
+            return oracle.run_reference_file(path, K, metric, passes, threads=threads), crashes
         except oracle.ReferenceRunError as e:
             crashes += 1
             if e.returncode >= 0 or crashes >= REFERENCE_TRIES:
                 raise
 
 
-def reference_timing(w, args, scale, passes, metrics, threads):
-    """Runs the reference's partition_par (threads > 1) on a bounded sample and
-    returns (pins * passes, refinement seconds, kind, hypergraph, crashed runs
-    retried)."""
-    import fastpartitioner_gb300 as fp
+def instance_file(w, scale, tmpdir):
+    """The workload's unit-weight instance drawn by the oracle's generator
+    (the product generator's draws, no product library loaded) as an .fphg
+    file; returns (path, (nov, noe, pins))."""
     import oracle
-    hg = fp.generate(spec_for(fp, w, scale, unit_weights=True))
-    if oracle.reference_available():
-        tot_t, tot_w, crashes = 0.0, 0, 0
-        for m in metrics:
-            r, c = run_reference_retrying(oracle, hg, w["K"], m, passes, threads)
-            crashes += c
-            tot_t += r["refine_seconds"]
-            tot_w += hg.pins * passes
-        return tot_w, tot_t, "reference", hg, crashes
-    tot_t, tot_w = 0.0, 0
+    nov, noe = max(w["nov"] // scale, 1024), max(w["noe"] // scale, 1024)
+    path = Path(tmpdir) / f"inst_{scale}.fphg"
+    if w["alpha"] > 0:
+        oracle.generate_fphg(path, nov, noe, w["lo"], min(w["hi"], nov), w["alpha"], w["beta"], 1, 0, w["seed"])
+    else:
+        oracle.generate_fphg(path, nov, noe, w["lo"], w["hi"], 0.0, 0.0, 0, 1, w["seed"])
+    return path, oracle.fphg_header(path)
+
+
+def reference_schedule(path, K, metrics, steps, passes, threads, kind="reference"):
+    """The reference's partition_par() (threads > 1; partition() otherwise) on
+    the instance file for `steps` steps of the pass schedule: per metric, runs
+    of `passes` passes (the schedule restarts from the stream, as the GPU arm's
+    instances do) and a shorter last run for the remainder.  kind "port": the
+    oracle's restatement (one thread) where the reference was not built.
+    Returns {metric: (passes timed, refinement seconds)} and the crashed runs
+    retried."""
+    import oracle
+    out, crashes = {}, 0
+    inst = oracle.FphgInstance(path) if kind == "port" else None
     for m in metrics:
-        o = oracle.run_oracle(hg, w["K"], m, passes, eps_factor=1.05)
-        tot_t += o["refine_seconds"]
-        tot_w += hg.pins * passes
-    return tot_w, tot_t, "port", hg, 0
+        left, t, n = steps, 0.0, 0
+        while left > 0:
+            run = min(left, passes)
+            if inst is not None:
+                t += oracle.run_oracle(inst, K, m, run, eps_factor=1.05)["refine_seconds"]
+            else:
+                r, c = run_reference_retrying(oracle, path, K, m, run, threads)
+                crashes += c
+                t += r["refine_seconds"]
+            n += run
+            left -= run
+        out[m] = (n, t)
+    return out, crashes
 
 
-def cpu_baseline(fp, w, args):
-    import oracle  # noqa: F401
-    threads = os.cpu_count() or 1
-    scale = args.cpu_scale
-    passes = args.cpu_passes
-    metrics = metrics_for(w, args.metrics)
-    work, t, kind, hg, crashes = reference_timing(w, args, scale, passes, metrics, threads)
+def reference_available():
+    try:
+        import oracle
+        return oracle.reference_available()
+    except Exception:
+        return False
+
+
+def cpu_baseline(w, args, per_metric_gpu):
+    """The reference's partition_par() with every host thread on the same
+    full-size instance, the first --cpu-passes passes of the schedule of each
+    metric: a bounded sample of the reference arm's run.  The GPU's time for
+    the same passes is reported beside it."""
+    kind = "reference" if reference_available() else "port"
+    threads = (os.cpu_count() or 1) if kind == "reference" else 1
+    metrics = list(per_metric_gpu)
+    n = min(args.cpu_passes, args.steps)
+    with tempfile.TemporaryDirectory(prefix="fpbench") as td:
+        path, (nov, noe, pins) = instance_file(w, args.scale, td)
+        res, crashes = reference_schedule(path, w["K"], metrics, n, w["passes"], threads, kind)
+    t = sum(v[1] for v in res.values())
+    gpu_t = sum(sum(per_metric_gpu[m][:n]) for m in metrics)
     engine = f"partition_par with {threads} threads" if kind == "reference" else "the oracle restatement, one thread"
-    return {"value": work / t, "unit": "pins/s", "cores": threads if kind == "reference" else 1, "kind": kind,
+    return {"value": pins * n * len(metrics) / t, "unit": "pins/s", "cores": threads, "kind": kind,
             "crashed_runs_retried": crashes,
-            "sample": f"{hg.nov} vertices / {hg.pins} pins ({args.config} distribution at 1/{scale} scale, unit "
-                      f"weights: the reference has none), {passes} passes of each of {','.join(metrics)}, {engine}"}
+            "per_metric_pins_per_s": {m: pins * k / s for m, (k, s) in res.items()},
+            "gpu_same_passes_pins_per_s": pins * n * len(metrics) / gpu_t if gpu_t > 0 else None,
+            "sample": f"the same instance ({nov} vertices / {pins} pins, unit weights), passes 1-{n} of the "
+                      f"{w['passes']}-pass schedule of each of {','.join(metrics)}, {engine}"}
 
 
 def run_reference_arm(args):
@@ -444,31 +538,36 @@ def run_reference_arm(args):
         pass
     w = WORKLOADS[args.config]
     metrics = metrics_for(w, args.metrics)
-    threads = os.cpu_count() or 1
-    passes = args.cpu_passes
-    vals = []
-    kind = None
-    hg = None
-    crashes = 0
-    for i in range(args.warmup + args.steps):
-        work, t, kind, hg, c = reference_timing(w, args, args.cpu_scale, passes, metrics, threads)
-        crashes += c
-        if i >= args.warmup:
-            vals.append((work, t))
-    tot_w = sum(a for a, _ in vals)
-    tot_t = sum(b for _, b in vals)
-    value = tot_w / tot_t
-    sample = (f"{hg.nov} vertices / {hg.pins} pins ({args.config} distribution at 1/{args.cpu_scale} scale, unit "
-              f"weights), {passes} passes of each of {','.join(metrics)}")
+    passes = args.passes or w["passes"]
+    # the reference compiled from its sources, else the oracle's restatement
+    kind = "reference" if reference_available() else "port"
+    threads = (os.cpu_count() or 1) if kind == "reference" else 1
+    with tempfile.TemporaryDirectory(prefix="fpbench") as td:
+        # untimed warm-up: the same schedule on a 1/64-scale draw, W passes
+        warm_crashes = 0
+        if args.warmup:
+            wpath, _ = instance_file(w, 64 * args.scale, td)
+            _, warm_crashes = reference_schedule(wpath, w["K"], metrics, args.warmup, passes, threads, kind)
+        path, (nov, noe, pins) = instance_file(w, args.scale, td)
+        res, crashes = reference_schedule(path, w["K"], metrics, args.steps, passes, threads, kind)
+        crashes += warm_crashes
+    tot_t = sum(t for _, t in res.values())
+    value = pins * args.steps * len(metrics) / tot_t
+    engine = f"partition_par with {threads} threads" if kind == "reference" else "the oracle restatement, one thread"
+    sample = (f"the whole workload ({nov} vertices / {pins} pins): {args.steps} steps = passes 1-{args.steps} of "
+              f"the {passes}-pass schedule of each of {','.join(metrics)}, {engine}")
     line = {
         "metric": METRIC,
         "value": value, "unit": "pins/s", "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": tot_t / len(vals) * 1e3,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": tot_t / args.steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
-        "data": "synthetic (seeded generator)", "impl": "reference",
-        "config": {"workload": f"{args.config} sample: {sample}", "threads": threads},
-        "cpu_baseline": {"value": value, "unit": "pins/s", "cores": threads if kind == "reference" else 1,
-                         "kind": kind, "sample": sample, "crashed_runs_retried": crashes},
+        "data": "synthetic (seeded generator; instance drawn by oracle/fp_oracle_gen.cpp)", "impl": "reference",
+        "config": {"workload": workload_text(args.config, w, nov, noe, pins, passes, metrics),
+                   "step": STEP_TEXT.format(passes=passes), "threads": threads,
+                   "per_metric_pins_per_s": {m: pins * k / t for m, (k, t) in res.items()},
+                   "per_metric_refine_s": {m: t for m, (_, t) in res.items()}},
+        "cpu_baseline": {"value": value, "unit": "pins/s", "cores": threads, "kind": kind, "sample": sample,
+                         "crashed_runs_retried": crashes},
         "e2e": {"value": value, "unit": "pins/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -562,9 +661,10 @@ def main():
     ap.add_argument("--scale", type=int, default=1, help="divide vertex/net counts (quick runs)")
     ap.add_argument("--passes", type=int, default=0)
     ap.add_argument("--metrics", default="")
-    ap.add_argument("--cpu-scale", type=int, default=8)
-    ap.add_argument("--cpu-passes", type=int, default=2)
+    ap.add_argument("--cpu-passes", type=int, default=2,
+                    help="cpu_baseline: passes of each metric's schedule (a bounded sample)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-degree", action="store_true", help="skip the degree-weight figure")
     ap.add_argument("--mode", default="refine", choices=["refine", "batch", "serve"],
                     help="refine: the pins/s line; batch / serve: the many-request runners")
     ap.add_argument("--batch-n", type=int, default=64)

@@ -282,3 +282,70 @@ def reference_metrics(hg, K: int, part_vec, ep_starts, ep_ends, ep_parts, ep_cnt
     d = dict(zip(OUTPUT_ORDER, map(int, out[:6])))
     d["TV_lambda"] = int(out[6])
     return d
+
+
+def generate_fphg(path, nov: int, noe: int, size_lo: int, size_hi: int, size_alpha: float = 0.0,
+                  pin_beta: float = 0.0, src_rule: int = 0, sort_pins: int = 1, seed: int = 0) -> None:
+    """Draws a seeded workload instance (fp_oracle_gen.cpp, the same draws as
+    the product generator) and writes it as the .fphg file the reference
+    harness reads -- without loading the product library."""
+    L = _oracle()
+    f = L.fpo_generate_fphg
+    f.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int, C.c_int, C.c_ulonglong,
+                  C.c_char_p]
+    f.restype = C.c_int
+    if f(nov, noe, size_lo, size_hi, size_alpha, pin_beta, src_rule, sort_pins, seed, str(path).encode()) != 0:
+        raise RuntimeError(f"oracle generator failed for {path}")
+
+
+def fphg_header(path) -> tuple:
+    """(nov, noe, pins) of an .fphg file."""
+    raw = Path(path).read_bytes()[:24]
+    nov, noe = np.frombuffer(raw, np.int32, 2, 8)
+    return int(nov), int(noe), int(np.frombuffer(raw, np.int64, 1, 16)[0])
+
+
+def run_reference_file(path, K: int, metric: str, passes: int, threads: int = 1, timeout: float = 3600) -> dict:
+    """The reference's partition() / partition_par() on an .fphg instance file,
+    no capture: its printed metrics and 'Refinement took' seconds."""
+    metric = metric.upper()
+    exe = REF_DIR / REF_BIN[metric]
+    if not exe.exists():
+        raise FileNotFoundError(f"{exe} not built (reference sources unavailable)")
+    env = dict(os.environ)
+    env.setdefault("OMP_NUM_THREADS", str(max(threads, 1)))
+    with tempfile.TemporaryDirectory(prefix="fpref") as td:
+        res = subprocess.run([str(exe), str(path), str(K), str(passes), str(threads), "-"], capture_output=True,
+                             text=True, timeout=timeout, env=env, cwd=td)
+    if res.returncode != 0:
+        raise ReferenceRunError(res.returncode, f"reference run failed ({res.returncode}):\n"
+                                                f"{res.stdout[-2000:]}\n{res.stderr[-2000:]}")
+    out = {"stdout": res.stdout}
+    after = {}
+    for key in OUTPUT_ORDER:
+        ma = re.search(rf"^After Refinement {_PRINT_NAMES[key]} : (-?\d+)$", res.stdout, re.M)
+        if ma:
+            after[key] = int(ma.group(1))
+    out["metrics_final"] = after
+    mt = re.search(r"^Refinement took : ([0-9.eE+-]+) seconds", res.stdout, re.M)
+    out["refine_seconds"] = float(mt.group(1)) if mt else None
+    return out
+
+
+class FphgInstance:
+    """An .fphg instance as numpy arrays (the attributes run_oracle reads),
+    loaded without the product library."""
+
+    def __init__(self, path):
+        raw = Path(path).read_bytes()
+        if raw[:5] != b"FPHG1":
+            raise ValueError("not an FPHG1 file")
+        self.nov, self.noe, self.pins = fphg_header(path)
+        off = 24
+        for name, n, dt in (("vptr", self.nov + 1, np.uint32), ("vnets", self.pins, np.uint32),
+                            ("nptr", self.noe + 1, np.uint32), ("npins", self.pins, np.uint32),
+                            ("src", self.noe, np.int32)):
+            setattr(self, name, np.frombuffer(raw, dt, n, off).copy())
+            off += 4 * n
+        self.weights = None
+        self.ordering = None

@@ -79,7 +79,11 @@ def _reference_line(monkeypatch, capsys, available):
     monkeypatch.setenv("WORLD_SIZE", "1")
     if not available:
         monkeypatch.setattr(oracle, "reference_available", lambda *a: False)
-    args = bench.argparse.Namespace(config="zipf4m", metrics="TV,CN", cpu_scale=256, cpu_passes=1, warmup=1, steps=2)
+    # one host thread: the reference's sequential partition(); its OpenMP path
+    # is racy on instances this small (runs end with SIGSEGV)
+    monkeypatch.setattr(bench.os, "cpu_count", lambda: 1)
+    args = bench.argparse.Namespace(config="zipf4m", metrics="TV,CN", scale=256, passes=0, cpu_passes=1, warmup=1,
+                                    steps=2)
     bench.run_reference_arm(args)
     lines = capsys.readouterr().out.strip().splitlines()
     assert len(lines) == 1
@@ -99,7 +103,11 @@ def test_reference_arm_line(monkeypatch, capsys, available):
     assert line["metric"] == bench.METRIC and line["value"] > 0 and line["steps"] == 2
     cb = line["cpu_baseline"]
     assert cb["kind"] == ("reference" if available else "port") and cb["value"] == line["value"]
-    assert cb["cores"] >= 1 and "vertices" in cb["sample"] and "passes of each of TV,CN" in cb["sample"]
+    assert cb["cores"] >= 1 and "vertices" in cb["sample"] and "schedule of each of TV,CN" in cb["sample"]
+    # the same workload string as the GPU arm, and no product library in the process's work
+    w = bench.WORKLOADS["zipf4m"]
+    assert line["config"]["workload"].startswith("zipf4m: 16384 vertices, 16384 nets")
+    assert set(line["config"]["per_metric_pins_per_s"]) == {"TV", "CN"}
     assert line["e2e"] == {"value": line["value"], "unit": "pins/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
 
 
@@ -109,7 +117,7 @@ def test_reference_run_ended_by_a_signal_is_retried(monkeypatch, capsys):
     import oracle
     if not oracle.reference_available():
         pytest.skip("reference harness not built (reference sources unavailable)")
-    real = oracle.run_reference
+    real = oracle.run_reference_file
     calls = {"n": 0}
 
     def flaky(*a, **k):
@@ -118,13 +126,29 @@ def test_reference_run_ended_by_a_signal_is_retried(monkeypatch, capsys):
             raise oracle.ReferenceRunError(-11, "reference run failed (-11)")
         return real(*a, **k)
 
-    monkeypatch.setattr(oracle, "run_reference", flaky)
+    monkeypatch.setattr(oracle, "run_reference_file", flaky)
     line = _reference_line(monkeypatch, capsys, True)
     assert line["cpu_baseline"]["crashed_runs_retried"] == 1 and line["value"] > 0
 
     def failing(*a, **k):
         raise oracle.ReferenceRunError(3, "reference run failed (3)")
 
-    monkeypatch.setattr(oracle, "run_reference", failing)
+    monkeypatch.setattr(oracle, "run_reference_file", failing)
     with pytest.raises(oracle.ReferenceRunError):
         bench.run_reference_retrying(oracle, None, 8, "TV", 1, 1)
+
+
+def test_reference_arm_loads_no_product_library(tmp_path):
+    """The reference arm draws its instance with the oracle's generator: the
+    process never imports the product package nor maps libfastpart.so."""
+    import subprocess
+    code = ("import sys, json; sys.argv = ['bench.py', '--impl', 'reference', '--scale', '256', '--metrics', 'TV', "
+            "'--steps', '1', '--warmup', '0']; import bench; bench.main(); "
+            "maps = open('/proc/self/maps').read(); "
+            "assert 'fastpartitioner_gb300' not in sys.modules, 'product package imported'; "
+            "assert 'libfastpart' not in maps, 'product library mapped'")
+    res = subprocess.run([sys.executable, "-c", code], cwd=ROOT, capture_output=True, text=True, timeout=600)
+    assert res.returncode == 0, res.stderr[-2000:]
+    import json
+    line = json.loads(res.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["value"] > 0
