@@ -129,6 +129,9 @@ def lib():
             "fp_refine": ([vp, i32], C.c_int),
             "fp_reset_state": ([vp], C.c_int),
             "fp_set_engine": ([vp, i32], C.c_int),
+            "fp_debug_barrier_fault": ([vp, i32, i32], C.c_int),
+            "fp_set_decision_log": ([vp, i32], C.c_int),
+            "fp_get_decisions": ([vp, vp, vp, vp, vp], C.c_int),
             "fp_set_classes": ([vp, i64, i64], C.c_int),
             "fp_metrics": ([vp, vp], C.c_int),
             "fp_get_partition": ([vp, vp], C.c_int),
@@ -484,6 +487,25 @@ class Instance:
         m = np.zeros(n, np.int64)
         _check(lib().fp_get_moves(self._h, _ptr(m), n), "fp_get_moves")
         return m
+
+    def set_decision_log(self, on: bool = True) -> None:
+        """fp_set_decision_log: record the decisions of each refine call's last pass."""
+        _check(lib().fp_set_decision_log(self._h, int(bool(on))), "fp_set_decision_log")
+
+    def decisions(self) -> dict:
+        """fp_get_decisions: the last refine's last-pass records as int32 arrays
+        dest, gain, loss, moved (one entry per vertex; per net for CN)."""
+        n = self.hg.noe if metric_id(self.metric) == 0 else self.hg.nov
+        out = {k: np.empty(n, np.int32) for k in ("dest", "gain", "loss", "moved")}
+        _check(lib().fp_get_decisions(self._h, *(_ptr(out[k]) for k in ("dest", "gain", "loss", "moved"))),
+               "fp_get_decisions")
+        return out
+
+    def debug_barrier_fault(self, leave_at: int, poll_limit: int = 0) -> None:
+        """fp_debug_barrier_fault: the next refine launches' last CTA leaves at
+        its leave_at-th grid barrier without arriving, and the others give up
+        after poll_limit polls (0: the default limit); (0, 0) turns it off."""
+        _check(lib().fp_debug_barrier_fault(self._h, int(leave_at), int(poll_limit)), "fp_debug_barrier_fault")
 
     def stats(self) -> dict:
         """Round statistics of the last refine on the grid-wide engine."""

@@ -102,6 +102,10 @@ struct fp_instance {
   int last_passes = 0;
   long long last_launches = 0;
   int engine = FP_ENGINE_AUTO;
+  unsigned fault_leave_at = 0;    // fp_debug_barrier_fault: test hooks of the grid barrier
+  unsigned fault_poll_limit = 0;
+  int4* recs = nullptr;           // fp_set_decision_log: one record per vertex (net for CN)
+  bool recs_valid = false;        // the last fp_refine wrote them
   SpecBuf sb{};
   int last_grid = 0;
   std::vector<int> heavy_pos;     // whole-grid-round vertices, by position in visiting order
@@ -442,6 +446,8 @@ int fp_instance_create(fp_ctx* ctx, const fp_hypergraph* h, int32_t K, int32_t m
         (rc = dalloc(in, &in->sb.flag, kSpecWindow)) || (rc = dalloc(in, &in->sb.slack, kSpecWindow)) ||
         (rc = dalloc(in, &in->sb.vslack, kSpecWindow)) || (rc = dalloc(in, &in->sb.wt, kSpecWindow)) ||
         (rc = dalloc(in, &in->sb.vd, kSpecWindow)) || (rc = dalloc(in, &in->sb.scan, (size_t)kSpecWindow * words)) ||
+        (rc = dalloc(in, &in->sb.rgain, std::max(kSpecWindow, kMsgWindow))) ||
+        (rc = dalloc(in, &in->sb.rloss, std::max(kSpecWindow, kMsgWindow))) ||
         (rc = dalloc(in, &in->sb.rec, ldg ? g.pins : 1)) || (rc = dalloc(in, &in->sb.rec_slot, ldg ? g.pins : 1)) ||
         (rc = dalloc(in, &in->sb.ctab_key, ldg ? ctab : 1)) || (rc = dalloc(in, &in->sb.ctab_pos, ldg ? ctab : 1)) ||
         (rc = dalloc(in, &in->sb.ctab_cnt, ldg ? ctab : 1)) ||
@@ -557,6 +563,7 @@ int fp_instance_footprint(int32_t nov, int32_t noe, int64_t pins, int32_t K, int
     add(8, 4); add(4, 4); add(kNumStats, 8); add(std::max(kSpecWindow, kMsgWindow), 4);
     add(W, 1); add(W, 4); add(W, 4); add(W, 4); add(W, 4);   // flag, slack, vslack, wt, vd
     add(W * words, 4);                                       // scan
+    add(std::max(kSpecWindow, kMsgWindow), 4); add(std::max(kSpecWindow, kMsgWindow), 4);   // rgain, rloss
     add(ldg ? P : 1, 4); add(ldg ? P : 1, 8);                // rec, rec_slot
     add(ldg ? ctab : 1, 8); add(ldg ? ctab : 1, 4); add(ldg ? ctab : 1, 4);
     add(2, 4); add(W, 4);                                    // ctab_over, dfix
@@ -580,6 +587,7 @@ int fp_instance_destroy(fp_instance* in) {
     if (!in) return FP_ERR_INVALID;
     cudaSetDevice(in->ctx->device);
     for (void* p : in->allocs) cudaFree(p);
+    if (in->recs) cudaFree(in->recs);
     if (in->h_moves) cudaFreeHost(in->h_moves);
     if (in->h_status) cudaFreeHost(in->h_status);
     if (in->h_metrics) cudaFreeHost(in->h_metrics);
@@ -622,11 +630,18 @@ int fp_refine(fp_instance* in, int32_t passes) {
     const bool spec =
         in->engine == FP_ENGINE_AUTO &&
         spec_supported(in->pb.metric, in->pb.K, in->ctx->max_smem, in->g.nov, in->g.noe);
+    in->d.recs = spec ? in->recs : nullptr;
+    in->recs_valid = false;
     if (spec) {
       static const int none[8] = {0x7fffffff, 0x7fffffff, 0x7fffffff, 0x7fffffff,
                                   0x7fffffff, 0x7fffffff, 0x7fffffff, 0x7fffffff};
       if (e == cudaSuccess) e = cudaMemcpyAsync(in->sb.ctl, none, sizeof(none), cudaMemcpyHostToDevice, s);
       if (e == cudaSuccess) e = cudaMemsetAsync(in->sb.bar, 0, sizeof(unsigned) * 4, s);
+      if (e == cudaSuccess && (in->fault_leave_at || in->fault_poll_limit)) {
+        const unsigned hooks[4] = {0u, in->fault_leave_at, 0u, in->fault_poll_limit};
+        e = cudaMemcpyAsync(in->sb.bar, hooks, sizeof(hooks), cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);   // `hooks` is on this stack frame
+      }
       if (e == cudaSuccess) e = cudaMemsetAsync(in->sb.stats, 0, sizeof(unsigned long long) * kNumStats, s);
       if (e == cudaSuccess) e = clear_spec_scratch(in->sb, in->g.noe, in->pb.K, s);
       if (e == cudaSuccess) {
@@ -651,6 +666,7 @@ int fp_refine(fp_instance* in, int32_t passes) {
     if (e != cudaSuccess) return cuda_status(e);
     in->last_passes = passes;
     in->last_launches = 1;
+    in->recs_valid = in->d.recs != nullptr && *in->h_status == FP_OK;
     return *in->h_status;
   });
 }
@@ -660,6 +676,62 @@ int fp_set_classes(fp_instance* in, int64_t light_work, int64_t super_work) {
     if (!in || light_work < 0 || super_work < light_work) return FP_ERR_INVALID;
     cudaSetDevice(in->ctx->device);
     return classify(in, light_work, super_work);
+  });
+}
+
+static int d2h(fp_instance* in, void* dst, const void* src, size_t bytes);
+
+int fp_set_decision_log(fp_instance* in, int32_t on) {
+  return fp::guarded([&]() -> int {
+    if (!in) return FP_ERR_INVALID;
+    cudaSetDevice(in->ctx->device);
+    const size_t n = (size_t)std::max(in->pb.metric == FP_METRIC_CN ? in->g.noe : in->g.nov, 1);
+    in->recs_valid = false;
+    if (!on) {
+      if (in->recs) {
+        cudaError_t e = cudaStreamSynchronize(in->ctx->stream);
+        if (e == cudaSuccess) e = cudaFree(in->recs);
+        in->recs = nullptr;
+        in->dev_bytes -= (long long)(n * sizeof(int4));
+        if (e != cudaSuccess) return cuda_status(e);
+      }
+      return FP_OK;
+    }
+    if (in->recs) return FP_OK;
+    void* p = nullptr;
+    cudaError_t e = cudaMalloc(&p, n * sizeof(int4));
+    if (e != cudaSuccess) return cuda_status(e);
+    in->recs = static_cast<int4*>(p);
+    in->dev_bytes += (long long)(n * sizeof(int4));
+    return FP_OK;
+  });
+}
+
+int fp_get_decisions(fp_instance* in, int32_t* dest, int32_t* gain, int32_t* loss, int32_t* moved) {
+  return fp::guarded([&]() -> int {
+    if (!in) return FP_ERR_INVALID;
+    if (!in->recs) return FP_ERR_STATE;
+    if (!in->recs_valid) return in->last_passes > 0 && !in->d.recs ? FP_ERR_UNSUPPORTED : FP_ERR_STATE;
+    const size_t n = (size_t)(in->pb.metric == FP_METRIC_CN ? in->g.noe : in->g.nov);
+    std::vector<int4> h(n);
+    int rc = d2h(in, h.data(), in->recs, n * sizeof(int4));
+    if (rc) return rc;
+    for (size_t i = 0; i < n; i++) {
+      if (dest) dest[i] = h[i].x;
+      if (gain) gain[i] = h[i].y;
+      if (loss) loss[i] = h[i].z;
+      if (moved) moved[i] = h[i].w;
+    }
+    return FP_OK;
+  });
+}
+
+int fp_debug_barrier_fault(fp_instance* in, int32_t leave_at, int32_t poll_limit) {
+  return fp::guarded([&]() -> int {
+    if (!in || leave_at < 0 || poll_limit < 0) return FP_ERR_INVALID;
+    in->fault_leave_at = (unsigned)leave_at;
+    in->fault_poll_limit = (unsigned)poll_limit;
+    return FP_OK;
   });
 }
 

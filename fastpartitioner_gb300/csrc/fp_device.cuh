@@ -44,6 +44,10 @@ struct DevInstance {
   // bookkeeping
   long long* moves;  // per pass
   int* status;       // device status word, 0 = ok
+  // decision records of the last pass of a refine call (fp_set_decision_log),
+  // one per vertex (per net for CN): (destination, gain, loss, moved); null
+  // when the log is off
+  int4* recs;
 };
 
 // Round statistics kept per instance (fp_get_stats).
@@ -67,6 +71,8 @@ struct SpecBuf {
   int* vslack;           // [wmax] volume drift the accept/reject outcome tolerates
   int* wt;               // [wmax] weight moved by a mover (0 otherwise)
   int* vd;               // [wmax] largest volume change of one part by a mover
+  int* rgain;            // [wmax] decision-record gain / loss of each window offset (with
+  int* rloss;            //     the decision log on)
   uint32_t* scan;        // [wmax * words] parts scanned per window offset (TV)
   uint32_t* rec;         // [pins] per (vertex, net) record of a move (spec::rec_pack),
                          //     at the pair's vnets index

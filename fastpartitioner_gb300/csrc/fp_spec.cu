@@ -561,6 +561,16 @@ __device__ __forceinline__ int block_reduce_max(int x, int* scr) {
   __syncthreads();
   return r;
 }
+__device__ __forceinline__ int block_reduce_sum(int x, int* scr) {
+  x = warp_sum(x);
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) scr[threadIdx.x >> 5] = x;
+  __syncthreads();
+  int s = 0;
+  for (int i = 0; i < (int)(blockDim.x >> 5); i++) s += scr[i];
+  __syncthreads();
+  return s;
+}
 __device__ __forceinline__ int block_reduce_min(int x, int* scr) {
   return -block_reduce_max(-x, scr);
 }
@@ -571,7 +581,7 @@ __device__ __forceinline__ int block_reduce_min(int x, int* scr) {
 // bit 2 marks it).
 __device__ void cta_eval_ldg(const DevInstance& I, const SpecBuf& B, const RoundCtx& R, int metric, int z, int pos,
                              int par, int q, int* cnt_b, unsigned long long* first_b, int* gains_b, int* losses_b,
-                             int* adelta_b, int* iscr, int* s_mw, int* s_mv, int* loc_b) {
+                             int* adelta_b, int* iscr, int* s_mw, int* s_mv, int* loc_b, bool logp) {
   __shared__ int sh[4];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int K = I.K;
@@ -629,9 +639,14 @@ __device__ void cta_eval_ldg(const DevInstance& I, const SpecBuf& B, const Round
   const int slack = sh[2];
   bool mover = false, mt = false;
   int vs = kBig, vdd = 0;
+  int rg = 0, rl = 0;   // decision record (with the log on)
   if (d != own) {
     // TV moves iff the leave gain covers the arrival loss; MSV / MSRV need the
     // accept test on the gain / loss sums.
+    if (metric == kTV) {
+      rg = c1t;
+      rl = deg - cnt_b[d];
+    }
     const bool need = metric == kTV ? c1t >= deg - cnt_b[d] : true;
     mover = metric == kTV && need;
     {   // records for every decision that moves: own's slot per net serves the validation
@@ -668,6 +683,12 @@ __device__ void cta_eval_ldg(const DevInstance& I, const SpecBuf& B, const Round
         accept_final(fM, fN, fsl, msl, &good, &vs);
         mover = good;
         mt = mover && amt;
+        if (logp) {
+          int g = 0, l = 0;
+          for (int p = threadIdx.x; p < K; p += blockDim.x) { g += gains_b[p]; l += losses_b[p]; }
+          rg = block_reduce_sum(g, iscr);
+          rl = block_reduce_sum(l, iscr);
+        }
       }
     }
   }
@@ -680,6 +701,7 @@ __device__ void cta_eval_ldg(const DevInstance& I, const SpecBuf& B, const Round
   }
   if (threadIdx.x == 0) {
     const int wv = mover ? __ldg(&I.w[v]) : 0;
+    if (logp) { B.rgain[o] = rg; B.rloss[o] = rl; }
     B.dec[o] = (own << 16) | d;
     B.flag[o] = (unsigned char)((mover ? 1 : 0) | (special ? 2 : 0) | 4);
     B.slack[o] = slack;
@@ -768,7 +790,7 @@ __device__ void cta_validate_ldg(const DevInstance& I, const SpecBuf& B, const R
 // every later check conservative); their table slots go to rec_slot2 for the
 // commit.  One warp, the warp gw owning position z.
 __device__ void fix_position(const DevInstance& I, const SpecBuf& B, const RoundCtx& R, int metric, int z, int o,
-                             int par, int gw, int* loc, int* gains, int* losses, int* adelta) {
+                             int par, int gw, int* loc, int* gains, int* losses, int* adelta, bool logp) {
   const int lane = threadIdx.x & 31;
   const bool vol = metric != kTV, rv = metric == kMSRV;
   const int K = I.K;
@@ -800,6 +822,15 @@ __device__ void fix_position(const DevInstance& I, const SpecBuf& B, const Round
     vdd = warp_max(a.vd);
   }
   __syncwarp();
+  if (logp) {
+    int rg = 0, rl = 0;
+    if (d != own) {
+      for (int p = lane; p < K; p += 32) { rg += gains[p]; rl += losses[p]; }
+      rg = warp_sum(rg);
+      rl = warp_sum(rl);
+    }
+    if (lane == 0) { B.rgain[o] = rg; B.rloss[o] = rl; }
+  }
   if (mover) {
     claim_nets(I, B, vol, z, own, d, base, deg, lane, 32, par);
     if (lane == 0 && mt) atomicMin(&B.ctl[2 + par], z);
@@ -826,6 +857,7 @@ static_assert(kMaxGridVerts <= kSWarps, "one warp decides each whole-grid vertex
 // Two CTAs per SM: without the hint the compiler trades registers for a third
 // CTA and spills, which measured slower.
 __global__ void __launch_bounds__(kSThreads, 2) spec_ldg_kernel(DevInstance I, SpecBuf B, int passes) {
+  barrier_start();
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ unsigned long long uscr[kSWarps];
   __shared__ int iscr[kSWarps];
@@ -874,6 +906,7 @@ __global__ void __launch_bounds__(kSThreads, 2) spec_ldg_kernel(DevInstance I, S
   int vr = 0;   // validation passes (parity selects the cut word)
   unsigned long long tA = gtimer();
   for (int it = 0; it < passes; it++) {
+    const bool logp = I.recs != nullptr && it == passes - 1;   // decision records of the last pass
     int pos = 0;
     int W = min(nwarps, B.wmax);
     int hidx = 0;
@@ -1079,6 +1112,22 @@ __global__ void __launch_bounds__(kSThreads, 2) spec_ldg_kernel(DevInstance I, S
           vdd = warp_max(a.vd);
         }
         __syncwarp();
+        if (logp) {
+          // decision record: TV's leave gain / arrival loss (TV/partition.cpp:355-378),
+          // MSV / MSRV's gain and loss vectors summed (MGV/partition.cpp:294-337)
+          int rg = 0, rl = 0;
+          if (d != own) {
+            if (metric == kTV) {
+              rg = c1;
+              rl = deg - cnt[d];
+            } else {
+              for (int p = lane; p < K; p += 32) { rg += gains[p]; rl += losses[p]; }
+              rg = warp_sum(rg);
+              rl = warp_sum(rl);
+            }
+          }
+          if (lane == 0) { B.rgain[o] = rg; B.rloss[o] = rl; }
+        }
         const int wv = mover ? __ldg(&I.w[v]) : 0;
         if (mover) {
           claim_nets(I, B, vol, z, own, d, base, deg, lane, 32, par);
@@ -1122,7 +1171,7 @@ __global__ void __launch_bounds__(kSThreads, 2) spec_ldg_kernel(DevInstance I, S
         const int z = __ldg(&B.mid_pos[mi]);
         if (z >= cz1) break;
         cta_eval_ldg(I, B, R, metric, z, pos, par, q, cnt_b, first_b, gains_b, losses_b, adelta_b, iscr, s_mw, s_mv,
-                     loc_b);
+                     loc_b, logp);
       }
       __syncthreads();
       if (kTimingStats && threadIdx.x == 0) {
@@ -1196,6 +1245,11 @@ __global__ void __launch_bounds__(kSThreads, 2) spec_ldg_kernel(DevInstance I, S
                             (metric == kTV ? lds(&B.hmisc[hmslot(j)]) >= deg_s - cnt_b[(size_t)j * K + d] : true);
           bool mover = metric == kTV && need, mt = false;
           int vs = kBig, vdd = 0;
+          int rg = 0, rl = 0;   // decision record (with the log on)
+          if (metric == kTV && d != own_s) {
+            rg = lds(&B.hmisc[hmslot(j)]);
+            rl = deg_s - cnt_b[(size_t)j * K + d];
+          }
           if (vol && need) {
             for (int p = threadIdx.x; p < K; p += blockDim.x) {
               gains_b[p] = lds(&B.hgain[hs + p]);
@@ -1214,10 +1268,17 @@ __global__ void __launch_bounds__(kSThreads, 2) spec_ldg_kernel(DevInstance I, S
             accept_final(fM, fN, fsl, msl, &good, &vs);
             mover = good;
             mt = mover && amt;
+            if (logp) {
+              int g = 0, l = 0;
+              for (int p = threadIdx.x; p < K; p += blockDim.x) { g += gains_b[p]; l += losses_b[p]; }
+              rg = block_reduce_sum(g, iscr);
+              rl = block_reduce_sum(l, iscr);
+            }
           }
           if (mover) claim_nets(I, B, vol, zs, own_s, d, base_s, deg_s, gtid, gthreads, par);
           const int wv = mover ? __ldg(&I.w[vsup]) : 0;
           if (blockIdx.x == 0 && threadIdx.x == 0) {
+            if (logp) { B.rgain[os] = rg; B.rloss[os] = rl; }
             B.dec[os] = (own_s << 16) | d;
             B.flag[os] = (unsigned char)((mover ? 1 : 0) | (s_gspec[j] ? 2 : 0) | 4);
             B.slack[os] = s_gslk[j];
@@ -1410,7 +1471,8 @@ __global__ void __launch_bounds__(kSThreads, 2) spec_ldg_kernel(DevInstance I, S
         const int zc = cutw >> 3;
         if (fix) fix = zc < end_w && __ldg(&B.vclass[__ldg(&I.order[zc])]) == 0;
         if (!fix) break;
-        if (gw == (zc - pos) / q) fix_position(I, B, R, metric, zc, zc - pos, par, gw, loc, gains, losses, adelta);
+        if (gw == (zc - pos) / q)
+          fix_position(I, B, R, metric, zc, zc - pos, par, gw, loc, gains, losses, adelta, logp);
         if (blockIdx.x == 0 && threadIdx.x == 0) {
           B.stats[44]++;
           B.stats[35] += B.stats[39];
@@ -1442,6 +1504,15 @@ __global__ void __launch_bounds__(kSThreads, 2) spec_ldg_kernel(DevInstance I, S
         return;
       }
       const int mt_c = lds(&B.ctl[2 + par]);
+      if (logp) {
+        // decision records of this warp's committed positions
+        for (int z = z0 + lane; z < min(z1, cut); z += 32) {
+          const int o = z - pos;
+          const int fl = lds(&B.flag[o]);
+          I.recs[__ldg(&I.order[z])] =
+              make_int4(lds(&B.dec[o]) & 0xffff, lds(&B.rgain[o]), lds(&B.rloss[o]), fl & 1);
+        }
+      }
       for (int z = z0; z < z1; z++) {
         const int o = z - pos;
         const int fl = lds(&B.flag[o]);

@@ -153,13 +153,14 @@ __device__ __forceinline__ void cn_grid_share(const DevInstance& I, int e, int g
 
 // Two-part test of net e (CN/partition.cpp:262-270): old (smaller side) and
 // new parts, false if the net does not span exactly two parts.
-__device__ __forceinline__ bool cn_two(const DevInstance& I, int e, int* oldp, int* newp) {
+__device__ __forceinline__ bool cn_two(const DevInstance& I, int e, int* oldp, int* newp, int* oldc = nullptr) {
   if (lds(&I.ep_len[e]) != 2) return false;
   const int s = (int)__ldg(&I.nptr[e]);
   const int p1 = lds(&I.ep_part[s]), c1 = lds(&I.ep_cnt[s]);
   const int p2 = lds(&I.ep_part[s + 1]), c2 = lds(&I.ep_cnt[s + 1]);
   *oldp = c1 < c2 ? p1 : p2;
   *newp = c1 < c2 ? p2 : p1;
+  if (oldc) *oldc = c1 < c2 ? c1 : c2;
   return true;
 }
 
@@ -173,8 +174,8 @@ __device__ __forceinline__ void cn_pin_share(const DevInstance& I, int e, int* p
 
 // Evaluation of a net with many pins by the whole CTA: the warps split its
 // pins (cn_eval's rules), then the claims of an acting net.
-__device__ void cn_eval_cta(const DevInstance& I, const SpecBuf& B, int e, int o, int round, int par) {
-  __shared__ int sh_two, sh_old, sh_new, sh_unc;
+__device__ void cn_eval_cta(const DevInstance& I, const SpecBuf& B, int e, int o, int round, int par, bool logp) {
+  __shared__ int sh_two, sh_old, sh_new, sh_unc, sh_cold;
   __shared__ volatile int sh_stop;
   const int lane = threadIdx.x & 31;
   if (threadIdx.x == 0) {
@@ -188,6 +189,7 @@ __device__ void cn_eval_cta(const DevInstance& I, const SpecBuf& B, int e, int o
       sh_two = 1;
       sh_old = c1 < c2 ? p1 : p2;
       sh_new = c1 < c2 ? p2 : p1;
+      sh_cold = c1 < c2 ? c1 : c2;
     }
   }
   __syncthreads();
@@ -209,6 +211,7 @@ __device__ void cn_eval_cta(const DevInstance& I, const SpecBuf& B, int e, int o
     B.dec[o] = (oldp << 16) | newp;
     B.flag[o] = (unsigned char)act;
     B.slack[o] = sh_unc;   // the uncut net that blocks the move (-1: none)
+    if (logp) B.rgain[o] = sh_two ? sh_cold : -1;
   }
   __syncthreads();
 }
@@ -238,8 +241,10 @@ __device__ void cn_validate_cta(const DevInstance& I, const SpecBuf& B, int e, i
 
 // Evaluation of net e (one warp).  Returns 0 (no move), 1 (acting), and the
 // old / new parts; *uncut = a net proving "no move" (-1 if e is not two-part).
-__device__ int cn_eval(const DevInstance& I, const SpecBuf& B, int e, int* oldp_o, int* newp_o, int* uncut) {
+__device__ int cn_eval(const DevInstance& I, const SpecBuf& B, int e, int* oldp_o, int* newp_o, int* uncut,
+                       int* oldc_o) {
   *uncut = -1;
+  *oldc_o = -1;
   if (lds(&I.ep_len[e]) != 2) return 0;
   const int s = (int)__ldg(&I.nptr[e]);
   const int p1 = lds(&I.ep_part[s]), c1 = lds(&I.ep_cnt[s]);
@@ -248,6 +253,7 @@ __device__ int cn_eval(const DevInstance& I, const SpecBuf& B, int e, int* oldp_
   const int newp = c1 < c2 ? p2 : p1;
   *oldp_o = oldp;
   *newp_o = newp;
+  *oldc_o = c1 < c2 ? c1 : c2;
   // any pin on the smaller side with a net that is not cut?
   *uncut = cn_walk<0>(I, B, e, oldp, 0, 0, 0);
   return *uncut < 0 ? 1 : 0;
@@ -333,6 +339,7 @@ __device__ void cn_apply_net(const DevInstance& I, int x, int oldp, int newp, in
 
 // Three CTAs per SM: without the hint the compiler spills to fit more.
 __global__ void __launch_bounds__(kSThreads, 3) spec_cn_kernel(DevInstance I, SpecBuf B, int passes) {
+  barrier_start();
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int gw = blockIdx.x * kSWarps + wib;
   const int nwarps = gridDim.x * kSWarps;
@@ -341,7 +348,11 @@ __global__ void __launch_bounds__(kSThreads, 3) spec_cn_kernel(DevInstance I, Sp
   unsigned long long tA = gtimer();
   int round = 1;   // claims of round 0 (the cleared array) never match
   int heavy_round = 0;
+  __shared__ int s_gc[kMaxGridVerts];
   for (int it = 0; it < passes; it++) {
+    // decision records of the last pass: (new part, pins moved, old part,
+    // acting) of a two-part net, (-1, 0, -1, 0) of any other net
+    const bool logp = I.recs != nullptr && it == passes - 1;
     int pos = 0;
     int W = min(nwarps * 4, B.wmax);
     int hidx = 0;
@@ -358,11 +369,12 @@ __global__ void __launch_bounds__(kSThreads, 3) spec_cn_kernel(DevInstance I, Sp
       auto hm = [&](int j) { return B.hmisc + (hp * kMaxGridVerts + j) * 8; };
       if ((int)threadIdx.x < ns) {
         const int e = __ldg(&B.heavy_pos[hidx + threadIdx.x]);
-        int op = 0, np = 0;
+        int op = 0, np = 0, oc = -1;
         s_ge[threadIdx.x] = e;
-        s_gt[threadIdx.x] = cn_two(I, e, &op, &np) ? 1 : 0;
+        s_gt[threadIdx.x] = cn_two(I, e, &op, &np, &oc) ? 1 : 0;
         s_go[threadIdx.x] = op;
         s_gn[threadIdx.x] = np;
+        s_gc[threadIdx.x] = oc;
       }
       __syncthreads();
       // ---- A0: the grid's warps split the pins of each grid net (uncut search)
@@ -381,13 +393,14 @@ __global__ void __launch_bounds__(kSThreads, 3) spec_cn_kernel(DevInstance I, Sp
       for (int e = z0; e < z1; e++) {
         const int o = e - pos;
         if ((int)(__ldg(&I.nptr[e + 1]) - __ldg(&I.nptr[e])) > B.cn_big) continue;   // the CTA evaluates it below
-        int oldp = 0, newp = 0, unc = -1;
-        const int act = cn_eval(I, B, e, &oldp, &newp, &unc);
+        int oldp = 0, newp = 0, unc = -1, oldc = -1;
+        const int act = cn_eval(I, B, e, &oldp, &newp, &unc, &oldc);
         if (act) cn_walk<1>(I, B, e, oldp, round, o, par);
         if (lane == 0) {
           B.dec[o] = (oldp << 16) | newp;
           B.flag[o] = (unsigned char)act;
           B.slack[o] = unc;   // the uncut net that blocks the move (-1: none)
+          if (logp) B.rgain[o] = oldc;
         }
         __syncwarp();
       }
@@ -397,7 +410,7 @@ __global__ void __launch_bounds__(kSThreads, 3) spec_cn_kernel(DevInstance I, Sp
       for (int mi = lower_bound_pos(B.mid_pos, B.nmid, cz0); mi < B.nmid; mi++) {
         const int e = __ldg(&B.mid_pos[mi]);
         if (e >= cz1) break;
-        cn_eval_cta(I, B, e, e - pos, round, par);
+        cn_eval_cta(I, B, e, e - pos, round, par, logp);
       }
       if (!grid_barrier(B.bar, I.status)) return;
       if (ns) {
@@ -415,6 +428,7 @@ __global__ void __launch_bounds__(kSThreads, 3) spec_cn_kernel(DevInstance I, Sp
             B.dec[o] = s_gt[j] ? (s_go[j] << 16) | s_gn[j] : 0;
             B.flag[o] = (unsigned char)act;
             B.slack[o] = s_gt[j] ? unc : -1;
+            if (logp) B.rgain[o] = s_gt[j] ? s_gc[j] : -1;
           }
         }
         if (!grid_barrier(B.bar, I.status)) return;
@@ -477,6 +491,15 @@ __global__ void __launch_bounds__(kSThreads, 3) spec_cn_kernel(DevInstance I, Sp
       if (cut <= pos) {
         if (threadIdx.x == 0) dev_fail(I.status, kDevErrInvalid);
         return;
+      }
+      if (logp) {
+        for (int e = z0 + lane; e < min(z1, cut); e += 32) {
+          const int o = e - pos;
+          const int oc = lds(&B.rgain[o]);
+          const int act = lds(&B.flag[o]) & 1;
+          const int pk = lds(&B.dec[o]);
+          I.recs[e] = oc >= 0 ? make_int4(pk & 0xffff, act ? oc : 0, pk >> 16, act) : make_int4(-1, 0, -1, 0);
+        }
       }
       // ---- C1: pins of acting nets before the cut: part, sizes, moves per net
       const int nmv = lds(&B.cn_cnt[par]);

@@ -27,13 +27,18 @@ template <class T>
 __device__ __forceinline__ T lds(const T* p) { return __ldcg(p); }
 
 // Grid-wide barrier of a co-resident (cooperatively launched) grid with a
-// bounded wait.  bar[0] = arrivals, bar[2] = abort flag (bar[1], bar[3]
-// unused).  Every CTA adds to bar[0] once per barrier: CTA 0 adds
-// 2^31 - (gridDim.x - 1), the others 1, so bit 31 flips exactly when the last
-// CTA arrives and the low bits return to their value -- no reset, one atomic
-// per CTA.  Returns false in every thread of the CTA if the wait gave up
-// (another CTA stopped arriving) or another CTA aborted; the kernel then
-// reports FP_ERR_DEVICE_TIMEOUT through `status` and returns.
+// bounded wait.  bar[0] = arrivals, bar[2] = abort flag.  Every CTA adds to
+// bar[0] once per barrier: CTA 0 adds 2^31 - (gridDim.x - 1), the others 1, so
+// bit 31 flips exactly when the last CTA arrives and the low bits return to
+// their value -- no reset, one atomic per CTA.  Returns false in every thread
+// of the CTA if the wait gave up (another CTA stopped arriving) or another CTA
+// aborted; the kernel then reports FP_ERR_DEVICE_TIMEOUT through `status` and
+// returns.
+//
+// Failure-detection test hooks (fp_debug_barrier_fault; both zero unless a
+// test sets them): bar[1] = n > 0 makes the grid's last CTA leave at its n-th
+// barrier without arriving, as a CTA that stopped would; bar[3] > 0 replaces
+// the poll limit, so that the other CTAs give up after that many polls.
 // Per-warp / per-CTA timing statistics (atomics in the hot loops): collected
 // only by builds with FP_TIMING_STATS defined.
 #ifdef FP_TIMING_STATS
@@ -50,25 +55,39 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
   return v;
 }
 
+// Barriers this CTA has entered in this launch (thread 0 only); a kernel
+// calls barrier_start() before its first grid_barrier.
+static __shared__ unsigned s_barriers;
+__device__ __forceinline__ void barrier_start() {
+  if (threadIdx.x == 0) s_barriers = 0;
+}
+
 __device__ __forceinline__ bool grid_barrier(unsigned* bar, int* status) {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
     int ok = 1;
-    const unsigned inc = blockIdx.x == 0 ? 0x80000000u - (gridDim.x - 1) : 1u;
-    __threadfence();
-    const unsigned old = atomicAdd(&bar[0], inc);
-    unsigned spins = 0;
-    while (((old ^ ld_acquire(&bar[0])) & 0x80000000u) == 0u) {
-      if ((++spins & 255u) == 0u && (ld_acquire(&bar[2]) != 0u || spins > kBarrierSpins)) {
-        ok = 0;
-        break;
+    const unsigned n = ++s_barriers;
+    const unsigned leave_at = __ldcg(&bar[1]);
+    if (leave_at != 0u && n == leave_at && blockIdx.x == gridDim.x - 1) {
+      ok = 0;   // test hook: this CTA stops arriving
+    } else {
+      const unsigned limit = __ldcg(&bar[3]) != 0u ? __ldcg(&bar[3]) : kBarrierSpins;
+      const unsigned inc = blockIdx.x == 0 ? 0x80000000u - (gridDim.x - 1) : 1u;
+      __threadfence();
+      const unsigned old = atomicAdd(&bar[0], inc);
+      unsigned spins = 0;
+      while (((old ^ ld_acquire(&bar[0])) & 0x80000000u) == 0u) {
+        if ((++spins & 255u) == 0u && (ld_acquire(&bar[2]) != 0u || spins > limit)) {
+          ok = 0;
+          break;
+        }
+        __nanosleep(32);
       }
-      __nanosleep(32);
-    }
-    if (!ok) {
-      atomicExch(&bar[2], 1u);
-      atomicCAS(status, 0, -4);   // FP_ERR_DEVICE_TIMEOUT
+      if (!ok) {
+        atomicExch(&bar[2], 1u);
+        atomicCAS(status, 0, -4);   // FP_ERR_DEVICE_TIMEOUT
+      }
     }
     __threadfence();
     s_ok = ok;

@@ -245,8 +245,11 @@ struct MsgRound {
 };
 
 // Decision of one warp for v from its scratch (g: source-side gain count).
+// rec (if not null) receives the decision record's gain and loss: TM's gain
+// and the loss at the chosen part (TM/partition.cpp:330-450), MSM's gain
+// vector summed and the chosen part's improvement (MSM/partition.cpp:388-518).
 __device__ int msg_decide_warp(const DevInstance& I, const Masks& M, const MsgRound& Rd, const MsgWarp& Wk, int own,
-                               int g, bool msm) {
+                               int g, bool msm, int2* rec = nullptr) {
   const int lane = threadIdx.x & 31;
   const int K = I.K;
   int gs = 0;
@@ -292,13 +295,24 @@ __device__ int msg_decide_warp(const DevInstance& I, const Masks& M, const MsgRo
     const unsigned long long o2 = __shfl_xor_sync(kAll, key, off);
     key = o2 < key ? o2 : key;
   }
+  if (rec) {
+    const int imp = key != ~0ull ? 0x7fffffff - (int)(key >> 32) : -1;
+    if (!msm) {
+      const int gain = g + gs;
+      *rec = make_int2(gain, key != ~0ull ? gain - imp : 0);
+    } else {
+      int gsum = 0;
+      for (int p = lane; p < K; p += 32) gsum += Wk.gains[p];
+      *rec = make_int2(warp_sum(gsum), imp);
+    }
+  }
   return key != ~0ull ? (int)(key & 0xffffffffu) : -1;
 }
 
 // Decision of the whole CTA from the combined scratch of warp 0 (R, S, fsnd;
 // g: the CTA's source-side gain count).  uscr / iscr: per-warp scratch.
 __device__ int msg_decide_cta(const DevInstance& I, const Masks& M, const MsgRound& Rd, const MsgWarp& W0, int own,
-                              int g, bool msm, unsigned long long* uscr, int* iscr) {
+                              int g, bool msm, unsigned long long* uscr, int* iscr, int2* rec = nullptr) {
   __shared__ int s_nsnd;
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int K = I.K;
@@ -341,6 +355,24 @@ __device__ int msg_decide_cta(const DevInstance& I, const Masks& M, const MsgRou
     }
   }
   key = block_min_u64(key, uscr);
+  if (rec) {
+    const int imp = key != ~0ull ? 0x7fffffff - (int)(key >> 32) : -1;
+    if (!msm) {
+      const int gain = g + gs_t;
+      *rec = make_int2(gain, key != ~0ull ? gain - imp : 0);
+    } else {
+      int gsum = 0;
+      for (int p = threadIdx.x; p < K; p += blockDim.x) gsum += W0.gains[p];
+      gsum = warp_sum(gsum);
+      __syncthreads();
+      if (lane == 0) iscr[wib] = gsum;
+      __syncthreads();
+      int t = 0;
+      for (int x = 0; x < (int)(blockDim.x >> 5); x++) t += iscr[x];
+      __syncthreads();
+      *rec = make_int2(t, imp);
+    }
+  }
   return key != ~0ull ? (int)(key & 0xffffffffu) : -1;
 }
 
@@ -412,6 +444,7 @@ __device__ void msg_commit_grid(const DevInstance& I, int v, int own, int d, int
 // Three CTAs per SM (the compiler's own choice otherwise varies with the code
 // and can spill).
 __global__ void __launch_bounds__(kSThreads, 3) spec_msg_kernel(DevInstance I, SpecBuf B, int passes) {
+  barrier_start();
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ unsigned long long uscr[kSWarps];
   __shared__ int iscr[kSWarps];
@@ -449,6 +482,9 @@ __global__ void __launch_bounds__(kSThreads, 3) spec_msg_kernel(DevInstance I, S
   int round = 0;
   bool dirty = true;   // staged masks out of date (a move was committed)
   for (int it = 0; it < passes; it++) {
+    // decision records of the last pass: a vertex evaluated before the window's
+    // first mover saw the final state; one after it is evaluated again later
+    const bool logp = I.recs != nullptr && it == passes - 1;
     int pos = 0;
     // window length: one position per warp to start, doubled after a window
     // without a mover, twice the distance to the mover after one
@@ -556,7 +592,9 @@ __global__ void __launch_bounds__(kSThreads, 3) spec_msg_kernel(DevInstance I, S
         int g = 0;
         for (int nb = 0; nb < deg; nb += 32) g += msg_batch(I, v, own, base, nb, deg, Wk, &oc1m[wib]);
         g = warp_sum(g);
-        const int best = msg_decide_warp(I, M, Rd, Wk, own, g, msm);
+        int2 rec;
+        const int best = msg_decide_warp(I, M, Rd, Wk, own, g, msm, logp ? &rec : nullptr);
+        if (logp && lane == 0) I.recs[v] = make_int4(best, rec.x, rec.y, best >= 0);
         if (best >= 0) {
           if (lane == 0) {
             B.dec[v - pos] = (own << 16) | best;
@@ -592,7 +630,9 @@ __global__ void __launch_bounds__(kSThreads, 3) spec_msg_kernel(DevInstance I, S
         __syncthreads();
         int gt = 0;
         for (int x = 0; x < kSWarps; x++) gt += iscr[x];
-        const int best = msg_decide_cta(I, M, Rd, W0, own, gt, msm, uscr, iscr);
+        int2 rec;
+        const int best = msg_decide_cta(I, M, Rd, W0, own, gt, msm, uscr, iscr, logp ? &rec : nullptr);
+        if (logp && threadIdx.x == 0) I.recs[v] = make_int4(best, rec.x, rec.y, best >= 0);
         if (best >= 0) {
           if (threadIdx.x == 0) {
             B.dec[v - pos] = (own << 16) | best;
@@ -632,7 +672,10 @@ __global__ void __launch_bounds__(kSThreads, 3) spec_msg_kernel(DevInstance I, S
           }
           for (int p = threadIdx.x; p < K; p += blockDim.x) fs_b[p] = lds(&B.hfirst[hs + p]);
           __syncthreads();
-          const int best = msg_decide_cta(I, M, Rd, W0, own, lds(&B.hmisc[hmslot(j)]), msm, uscr, iscr);
+          int2 rec;
+          const int best =
+              msg_decide_cta(I, M, Rd, W0, own, lds(&B.hmisc[hmslot(j)]), msm, uscr, iscr, logp ? &rec : nullptr);
+          if (logp && threadIdx.x == 0) I.recs[v] = make_int4(best, rec.x, rec.y, best >= 0);
           if (best >= 0 && threadIdx.x == 0) {
             B.dec[v - pos] = (own << 16) | best;
             atomicMin(&B.ctl[par], v);

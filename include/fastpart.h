@@ -179,6 +179,48 @@ int fp_metrics_noalloc(int32_t K, int32_t nov, int32_t noe, int64_t pins, const 
                        const int32_t* src, const int32_t* part_vec, const int32_t* ep_len,
                        const int32_t* ep_part, int64_t* out, void* stream);
 
+/* Decision records (no counterpart in the reference's interface: its
+ * refinement loops compute them and keep none).  With the log on, fp_refine
+ * records the decisions of its LAST pass: one record per vertex -- per net for
+ * CN -- of (dest, gain, loss, moved), each the value the reference computes
+ * for it at its turn in that pass:
+ *   TV    dest = the LDG decision after the max_pw / min_pw clamps; gain /
+ *         loss = leave_gain / arrival_loss when dest differs from the vertex's
+ *         part, else 0 / 0 (TV/partition.cpp:318-380)
+ *   MSV,  dest = the LDG decision; gain / loss = the sums over all parts of
+ *   MSRV  the gains[] / losses[] vectors when dest differs, else 0 / 0
+ *         (MGV/partition.cpp:294-362, MSRV/partition.cpp:308-400)
+ *   TM    dest = the part moved to, -1 if none; gain = the messages the move
+ *         removes; loss = the messages it adds at dest, 0 if none
+ *         (TM/partition.cpp:330-450)
+ *   MSM   dest = the part moved to, -1 if none; gain = the sum of the gains[]
+ *         vector; loss = the improvement over the max parts at dest, -1 if none
+ *         (MSM/partition.cpp:388-518)
+ *   CN    per net: dest = the new part of a two-part net, -1 otherwise; gain
+ *         = the pins moved (0 if an uncut net vetoed the move); loss = the old
+ *         part, -1 otherwise (CN/partition.cpp:262-377)
+ * moved = 1 if the move was made.  The log takes 16 bytes per record of
+ * device memory (counted by fp_instance_device_bytes, not by
+ * fp_instance_footprint).  fp_get_decisions copies the records of the last
+ * fp_refine out (NULL members skipped); FP_ERR_STATE if the log is off or no
+ * refine has run with it, FP_ERR_UNSUPPORTED if that refine ran on the
+ * single-CTA walk (FP_ENGINE_SEQUENTIAL, or an instance beyond the grid-wide
+ * engine's limits). */
+int fp_set_decision_log(fp_instance* inst, int32_t on);
+int fp_get_decisions(fp_instance* inst, int32_t* dest, int32_t* gain, int32_t* loss, int32_t* moved);
+
+/* Failure-detection test hook of the grid-wide engine (no counterpart in the
+ * reference, whose wrapper exits on any CUDA error, TV/gpu_partition.cu:10-16).
+ * Every grid-wide wait of the engine is bounded: a CTA that stops arriving at
+ * a barrier makes the others give up after a poll limit (about a second by
+ * default), and fp_refine returns FP_ERR_DEVICE_TIMEOUT with the device
+ * usable.  With leave_at = n > 0 the last CTA of the next fp_refine launches
+ * leaves at its n-th barrier without arriving, as a stopped CTA would;
+ * poll_limit > 0 replaces the default limit (polls of the barrier word).  Both
+ * zero (the default) turns the hook off.  The refined state after a timeout is
+ * partial: fp_reset_state restores the initial one. */
+int fp_debug_barrier_fault(fp_instance* inst, int32_t leave_at, int32_t poll_limit);
+
 /* Statistics of the last fp_refine on the grid-wide engine (up to 48 values):
  * [0] windows, [1] whole-grid evaluations of heavy vertices (CN: nets), [2] moves
  * committed from windows, [3..8] windows ended by: nothing (fully valid), a

@@ -46,7 +46,9 @@ class _Run(C.Structure):
                 ("part_vec", C.c_void_p), ("ep_len", C.c_void_p), ("ep_part", C.c_void_p),
                 ("ep_cnt", C.c_void_p), ("metrics_init", C.c_longlong * 6),
                 ("metrics_final", C.c_longlong * 6), ("moves", C.c_longlong * 64),
-                ("refine_seconds", C.c_double), ("status", C.c_int)]
+                ("refine_seconds", C.c_double), ("status", C.c_int),
+                ("rec_dest", C.c_void_p), ("rec_gain", C.c_void_p), ("rec_loss", C.c_void_p),
+                ("rec_moved", C.c_void_p)]
 
 
 def build(quiet: bool = True) -> None:
@@ -84,15 +86,20 @@ def _p(a):
     return None if a is None else a.ctypes.data
 
 
-def run_oracle(hg, K: int, metric: str, passes: int, eps_factor: float = 1.05, refine: bool = True):
+def run_oracle(hg, K: int, metric: str, passes: int, eps_factor: float = 1.05, refine: bool = True,
+               records: bool = False):
     """Runs the restated reference pipeline (stream + passes + metrics).
-    Returns a dict of numpy arrays and metric dicts."""
+    Returns a dict of numpy arrays and metric dicts; with records, also the
+    decision records of the last pass (rec_dest, rec_gain, rec_loss,
+    rec_moved: one entry per vertex, per net for CN)."""
     m = METRIC_IDS[metric.upper()]
     nov, noe, pins = hg.nov, hg.noe, hg.pins
-    out = {k: np.empty(n, np.int32) for k, n in (("part_vec_init", nov), ("ep_len_init", noe),
-                                                   ("ep_part_init", pins), ("ep_cnt_init", pins),
-                                                   ("part_vec", nov), ("ep_len", noe),
-                                                   ("ep_part", pins), ("ep_cnt", pins))}
+    nrec = noe if metric.upper() == "CN" else nov
+    shapes = [("part_vec_init", nov), ("ep_len_init", noe), ("ep_part_init", pins), ("ep_cnt_init", pins),
+              ("part_vec", nov), ("ep_len", noe), ("ep_part", pins), ("ep_cnt", pins)]
+    if records:
+        shapes += [("rec_dest", nrec), ("rec_gain", nrec), ("rec_loss", nrec), ("rec_moved", nrec)]
+    out = {k: np.full(n, -2, np.int32) if k.startswith("rec_") else np.empty(n, np.int32) for k, n in shapes}
     h = _Hg(nov, noe, pins, _p(hg.vptr), _p(hg.vnets), _p(hg.nptr), _p(hg.npins), _p(hg.src),
             _p(hg.weights), _p(hg.ordering))
     r = _Run()

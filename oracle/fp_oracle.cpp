@@ -71,6 +71,13 @@ typedef struct {
   long long moves[64];         // accepted moves per pass (first 64 passes)
   double refine_seconds;       // the reference's "Refinement took" span
   int status;                  // 0 ok, <0 error
+  // decision records of the last refinement pass (caller allocated, nov
+  // entries -- noe for CN -- or NULL); their meaning per metric is that of
+  // fp_get_decisions in include/fastpart.h
+  int* rec_dest;
+  int* rec_gain;
+  int* rec_loss;
+  int* rec_moved;
 } fpo_run;
 
 }  // extern "C"
@@ -78,6 +85,20 @@ typedef struct {
 namespace {
 
 enum { M_CN = 0, M_TV = 1, M_TM = 2, M_MSM = 3, M_MSV = 4, M_MSRV = 5 };
+
+// Decision records of the last pass: one entry per visited vertex (per net for
+// CN), written by the refinements below when `on` (the pass is the last one).
+struct Records {
+  int *dest = nullptr, *gain = nullptr, *loss = nullptr, *moved = nullptr;
+  bool on = false;
+  void put(int i, int d, int g, int l, bool mv) const {
+    if (!on) return;
+    if (dest) dest[i] = d;
+    if (gain) gain[i] = g;
+    if (loss) loss[i] = l;
+    if (moved) moved[i] = mv ? 1 : 0;
+  }
+};
 
 struct HG {
   int nov, noe;
@@ -407,7 +428,7 @@ void move_lists(Ctx& c, int v, int own, int d) {
 
 // TV refinement (TV/partition.cpp:307-440).  `marker` carries over from the
 // initial stream and across passes, as in the reference.
-void refine_tv(Ctx& c, int passes, std::vector<int>& marker, long long* moves) {
+void refine_tv(Ctx& c, int passes, std::vector<int>& marker, long long* moves, Records rec) {
   const HG& g = *c.g;
   std::vector<int> active(c.K);
   std::vector<double> scores(c.K, 0.0);
@@ -415,6 +436,7 @@ void refine_tv(Ctx& c, int passes, std::vector<int>& marker, long long* moves) {
   const int min_pw = (int)(c.xw - (c.xw * 0.1));
   for (int it = 0; it < passes; it++) {
     long long mv = 0;
+    rec.on = it == passes - 1;
     for (int z = 0; z < g.nov; z++) {
       int v = g.order[z];
       int own = c.part_vec[v];
@@ -423,7 +445,10 @@ void refine_tv(Ctx& c, int passes, std::vector<int>& marker, long long* moves) {
       int d = ldg_argmax(c, active, nact, scores);
       if (c.part_sizes[d] > max_pw) d = c.part_vec[v];
       if (c.part_sizes[d] < min_pw && c.part_vec[v] != -1) d = c.part_vec[v];
-      if (own == d) continue;
+      if (own == d) {
+        rec.put(v, d, 0, 0, false);
+        continue;
+      }
       int leave_gain = 0, arrival_loss = 0;
       for (unsigned i = g.vptr[v]; i < g.vptr[v + 1]; i++) {
         int e = g.vnets[i];
@@ -435,6 +460,7 @@ void refine_tv(Ctx& c, int passes, std::vector<int>& marker, long long* moves) {
         }
         if (!found) arrival_loss++;
       }
+      rec.put(v, d, leave_gain, arrival_loss, leave_gain >= arrival_loss);
       if (leave_gain >= arrival_loss) {
         mv++;
         c.part_vec[v] = d;
@@ -448,13 +474,17 @@ void refine_tv(Ctx& c, int passes, std::vector<int>& marker, long long* moves) {
 }
 
 // CN refinement (CN/partition.cpp:245-377), net-centric, nets in id order.
-void refine_cn(Ctx& c, int passes, long long* moves) {
+void refine_cn(Ctx& c, int passes, long long* moves, Records rec) {
   const HG& g = *c.g;
   std::vector<int> push(g.nov);
   for (int it = 0; it < passes; it++) {
     long long mv = 0;
+    rec.on = it == passes - 1;
     for (int e = 0; e < g.noe; e++) {
-      if (c.L.len[e] != 2) continue;
+      if (c.L.len[e] != 2) {
+        rec.put(e, -1, 0, -1, false);
+        continue;
+      }
       int s = c.L.start[e];
       int p1 = c.L.part[s], c1 = c.L.cnt[s];
       int p2 = c.L.part[s + 1], c2 = c.L.cnt[s + 1];
@@ -471,6 +501,7 @@ void refine_cn(Ctx& c, int passes, long long* moves) {
           }
         }
       }
+      rec.put(e, newp, not_in_cut ? 0 : np, oldp, !not_in_cut);
       if (!not_in_cut) {
         for (int q = 0; q < np; q++) {
           int u = push[q];
@@ -530,12 +561,14 @@ void commit_msg(Ctx& c, int v, int own, int d, std::vector<int>& conn, std::vect
 }
 
 // TM refinement (TM/partition.cpp:300-593); vertices in id order.
-void refine_tm(Ctx& c, int passes, std::vector<int>& conn, std::vector<int>& msgs, long long* moves) {
+void refine_tm(Ctx& c, int passes, std::vector<int>& conn, std::vector<int>& msgs, long long* moves,
+               Records rec) {
   const HG& g = *c.g;
   const int K = c.K;
   std::vector<int> receivers(K), senders(K);
   for (int it = 0; it < passes; it++) {
     long long mv = 0;
+    rec.on = it == passes - 1;
     std::vector<int> mrec(K, -1), msnd(K, -1);
     for (int v = 0; v < g.nov; v++) {
       int best = -1, best_imp = 0;
@@ -584,6 +617,7 @@ void refine_tm(Ctx& c, int passes, std::vector<int>& conn, std::vector<int>& msg
           if (gain > loss && gain - loss > best_imp) { best = k; best_imp = gain - loss; }
         }
       }
+      rec.put(v, best, gain, best != -1 ? gain - best_imp : 0, best != -1);
       if (best != -1) {
         mv++;
         commit_msg(c, v, own, best, conn, msgs);
@@ -594,12 +628,14 @@ void refine_tm(Ctx& c, int passes, std::vector<int>& conn, std::vector<int>& msg
 }
 
 // MSM refinement (MSM/partition.cpp:347-656); vertices in id order.
-void refine_msm(Ctx& c, int passes, std::vector<int>& conn, std::vector<int>& msgs, long long* moves) {
+void refine_msm(Ctx& c, int passes, std::vector<int>& conn, std::vector<int>& msgs, long long* moves,
+                Records rec) {
   const HG& g = *c.g;
   const int K = c.K;
   std::vector<int> gains(K), losses(K), max_parts(K), mmark(K), receivers(K), senders(K);
   for (int it = 0; it < passes; it++) {
     long long mv = 0;
+    rec.on = it == passes - 1;
     std::vector<int> mrec(K, -1), msnd(K, -1);
     for (int v = 0; v < g.nov; v++) {
       int best = -1, best_imp = -1;
@@ -660,6 +696,11 @@ void refine_msm(Ctx& c, int passes, std::vector<int>& conn, std::vector<int>& ms
           if (good && imp > best_imp) { best = k; best_imp = imp; }
         }
       }
+      if (rec.on) {
+        int gsum = 0;
+        for (int p = 0; p < K; p++) gsum += gains[p];
+        rec.put(v, best, gsum, best_imp, best != -1);
+      }
       if (best != -1) {
         mv++;
         commit_msg(c, v, own, best, conn, msgs);
@@ -679,7 +720,7 @@ struct MaxSet {
 // MSV (MGV) refinement (MGV/partition.cpp:222-477) and MSRV refinement
 // (MSRV/partition.cpp:240-517).  recv is ignored for MSV.
 void refine_vol(Ctx& c, int metric, int passes, std::vector<int>& send, std::vector<int>& recv,
-                long long* moves, int& status) {
+                long long* moves, int& status, Records rec) {
   const HG& g = *c.g;
   const int K = c.K;
   const bool rv = (metric == M_MSRV);
@@ -700,6 +741,7 @@ void refine_vol(Ctx& c, int metric, int passes, std::vector<int>& send, std::vec
   };
   for (int it = 0; it < passes; it++) {
     long long mv = 0;
+    rec.on = it == passes - 1;
     std::fill(marker.begin(), marker.end(), -1);
     full_scan();
     for (int z = 0; z < g.nov; z++) {
@@ -710,7 +752,10 @@ void refine_vol(Ctx& c, int metric, int passes, std::vector<int>& send, std::vec
       int nact = gather_scores(c, v, marker, scores, active);
       scores[own]--;
       int d = ldg_argmax(c, active, nact, scores);
-      if (own == d) continue;
+      if (own == d) {
+        rec.put(v, d, 0, 0, false);
+        continue;
+      }
       for (unsigned i = g.vptr[v]; i < g.vptr[v + 1]; i++) {
         int e = g.vnets[i];
         int s = c.L.start[e], n = c.L.len[e];
@@ -749,6 +794,11 @@ void refine_vol(Ctx& c, int metric, int passes, std::vector<int>& send, std::vec
       for (int i = 0; good && i < K; i++) {
         if (M.mark[i] == M.cc) continue;
         if (vol(i) + (losses[i] - gains[i]) >= M.val) good = false;
+      }
+      if (rec.on) {
+        int gsum = 0, lsum = 0;
+        for (int p = 0; p < K; p++) { gsum += gains[p]; lsum += losses[p]; }
+        rec.put(v, d, gsum, lsum, good);
       }
       if (!good) continue;
       mv++;
@@ -879,13 +929,18 @@ extern "C" int fpo_partition(const fpo_hg* in, fpo_run* r) {
 
   std::memset(r->moves, 0, sizeof(r->moves));
   auto t0 = std::chrono::steady_clock::now();
+  Records rec;
+  rec.dest = r->rec_dest;
+  rec.gain = r->rec_gain;
+  rec.loss = r->rec_loss;
+  rec.moved = r->rec_moved;
   if (r->refine && r->passes > 0) {
     switch (m) {
-      case M_TV: refine_tv(c, r->passes, marker, r->moves); break;
-      case M_CN: refine_cn(c, r->passes, r->moves); break;
-      case M_TM: refine_tm(c, r->passes, conn, msgs, r->moves); break;
-      case M_MSM: refine_msm(c, r->passes, conn, msgs, r->moves); break;
-      default: refine_vol(c, m, r->passes, send, recv, r->moves, status); break;
+      case M_TV: refine_tv(c, r->passes, marker, r->moves, rec); break;
+      case M_CN: refine_cn(c, r->passes, r->moves, rec); break;
+      case M_TM: refine_tm(c, r->passes, conn, msgs, r->moves, rec); break;
+      case M_MSM: refine_msm(c, r->passes, conn, msgs, r->moves, rec); break;
+      default: refine_vol(c, m, r->passes, send, recv, r->moves, status, rec); break;
     }
   }
   auto t1 = std::chrono::steady_clock::now();
