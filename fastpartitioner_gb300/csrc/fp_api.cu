@@ -486,9 +486,6 @@ int fp_instance_create(fp_ctx* ctx, const fp_hypergraph* h, int32_t K, int32_t m
     // every few hundred positions), four times for the metrics with rarer cuts
     in->sb.wgrow = metric == FP_METRIC_MSV ? 2 : 4;
     in->sb.maxfix = 32;
-    in->sb.has_iso = 0;
-    for (int v = 0; v < g.nov; v++)
-      if (g.vptr[v + 1] == g.vptr[v]) { in->sb.has_iso = 1; break; }
     in->sb.max_warps = kMaxSpecWarps;
     in->sb.heavy_pos = in->heavy_pos_d;
     in->sb.mid_pos = in->mid_pos_d;

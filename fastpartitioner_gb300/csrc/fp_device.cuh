@@ -118,7 +118,6 @@ struct SpecBuf {
   int gmax;              // whole-grid vertices one window may hold (1 .. kMaxGridVerts)
   int wgrow;             // LDG window after a cut: this many times the last valid length
   int maxfix;            // in-window decision fixes per window (MSV / MSRV)
-  int has_iso;           // some vertex has no nets (the LDG engine's size walker decides them)
   unsigned long long* stats;  // [kNumStats] round statistics (see fp_get_stats)
   int wmax;              // longest window of the LDG and CN engines
   int wmax_msg;          // longest window of the TM / MSM engine (dec only)

@@ -852,202 +852,6 @@ __device__ void fix_position(const DevInstance& I, const SpecBuf& B, const Round
   __syncwarp();
 }
 
-// ---------------------------------------------------------------- size walker
-//
-// A vertex without nets reads nothing but the part sizes: its decision is the
-// least-loaded part, lowest index on ties (TV/partition.cpp:119-131,
-// MGV/partition.cpp:49-61), TV's clamps keep it home when that part's size is
-// outside [min_pw, max_pw] (TV/partition.cpp:135-143), all its gains and
-// losses are zero, so TV and MSV always accept the move (leave_gain 0 >=
-// arrival_loss 0; no max-volume part loses, no other part gains), and MSRV
-// never does (gains <= losses, MSRV/partition.cpp:363).  With unit weights
-// such a vertex moves a unit of size on nearly every visit, so the sizes seen
-// by every later decision change at almost every position.
-//
-// These vertices are therefore not speculated.  After the window's other
-// positions have been evaluated, one warp walks the window in visiting order
-// with the exact part sizes: a mover among the evaluated positions shifts its
-// weight, a vertex without nets takes the least-loaded part of that moment.
-// The evaluated decisions are taken as speculated; validation then rechecks
-// them against the exact sizes, which now include these moves, and the window
-// is cut at the first one that no longer holds -- every walked decision before
-// the cut was made on the sizes the reference has there.
-//
-// The least-loaded part comes from two level bitmaps of the sizes: the parts
-// at the minimum size m and at m + 1, with a summary word of their non-empty
-// words (K <= 1024).  All lanes run the same scalar steps on shared memory.
-constexpr int kWalkMaxK = 1024;
-
-struct Levels {
-  uint32_t* L0;   // parts at size m
-  uint32_t* L1;   // parts at size m + 1
-  uint32_t s0, s1;   // bit x: word x of L0 / L1 is not zero
-  int m;
-};
-
-__device__ __forceinline__ void lv_clear(uint32_t* L, int words) {
-  const int lane = threadIdx.x & 31;
-  if (lane < words) L[lane] = 0u;
-  __syncwarp();
-}
-
-// L = the parts whose size is `level` (words of K bits), returns its summary.
-__device__ __forceinline__ uint32_t lv_scan(const int* sz, int K, uint32_t* L, int level) {
-  const int lane = threadIdx.x & 31;
-  uint32_t sum = 0;
-  for (int p0 = 0; p0 < K; p0 += 32) {
-    const int p = p0 + lane;
-    const unsigned b = __ballot_sync(kAll, p < K && sz[p] == level);
-    if (lane == 0) L[p0 >> 5] = b;
-    if (b) sum |= 1u << (p0 >> 5);
-  }
-  __syncwarp();
-  return sum;
-}
-
-__device__ __forceinline__ void lv_rebuild(const int* sz, int K, Levels& lv) {
-  const int lane = threadIdx.x & 31;
-  int m = 2147483647;
-  for (int p = lane; p < K; p += 32) m = min(m, sz[p]);
-  m = warp_min(m);
-  lv.m = m;
-  lv.s0 = lv_scan(sz, K, lv.L0, m);
-  lv.s1 = lv_scan(sz, K, lv.L1, m + 1);
-}
-
-__device__ __forceinline__ void lv_clr(uint32_t* L, uint32_t& sum, int p) {
-  const int x = p >> 5;
-  const uint32_t w = L[x] & ~(1u << (p & 31));
-  __syncwarp();
-  L[x] = w;
-  __syncwarp();
-  if (!w) sum &= ~(1u << x);
-}
-__device__ __forceinline__ void lv_set(uint32_t* L, uint32_t& sum, int p) {
-  const int x = p >> 5;
-  const uint32_t w = L[x] | (1u << (p & 31));
-  __syncwarp();
-  L[x] = w;
-  __syncwarp();
-  sum |= 1u << x;
-}
-
-// Part p's size from ov to nv, with the level bitmaps kept (sz[p] = nv).
-__device__ __forceinline__ void lv_move(int* sz, int words, Levels& lv, int p, int ov, int nv) {
-  if (ov == lv.m) lv_clr(lv.L0, lv.s0, p);
-  else if (ov == lv.m + 1) lv_clr(lv.L1, lv.s1, p);
-  __syncwarp();
-  sz[p] = nv;
-  __syncwarp();
-  if (nv < lv.m) {
-    if (nv == lv.m - 1) {            // the old minimum level becomes m + 1
-      uint32_t* t = lv.L1;
-      lv.L1 = lv.L0;
-      lv.L0 = t;
-      lv.s1 = lv.s0;
-    } else {                          // nothing is left at the new m + 1
-      lv_clear(lv.L1, words);
-      lv.s1 = 0u;
-    }
-    lv_clear(lv.L0, words);
-    lv.s0 = 0u;
-    lv.m = nv;
-    lv_set(lv.L0, lv.s0, p);
-  } else if (nv == lv.m) {
-    lv_set(lv.L0, lv.s0, p);
-  } else if (nv == lv.m + 1) {
-    lv_set(lv.L1, lv.s1, p);
-  }
-}
-
-// After moves: the minimum level is not empty.
-__device__ __forceinline__ void lv_settle(const int* sz, int K, Levels& lv) {
-  if (lv.s0) return;
-  if (lv.s1) {
-    uint32_t* t = lv.L0;
-    lv.L0 = lv.L1;
-    lv.L1 = t;
-    lv.s0 = lv.s1;
-    lv.m += 1;
-    lv.s1 = lv_scan(sz, K, lv.L1, lv.m + 1);
-  } else {
-    lv_rebuild(sz, K, lv);
-  }
-}
-
-__device__ __forceinline__ int lv_argmin(const Levels& lv) {
-  const int x = __ffs(lv.s0) - 1;
-  return x * 32 + __ffs(lv.L0[x]) - 1;
-}
-
-// One warp: decides the window's positions flagged 128 (vertices without nets)
-// at offsets [o_from, o_end) from the sizes `sizes0` at offset o_from.  sz: K
-// ints, lvbuf: 2 * 32 words of shared memory.  A walked mover gets its decision, weight and flags
-// like an evaluated one, an entry in the mover list, and its weight in its
-// warp's drift sum (q positions per warp).
-__device__ void size_walk(const DevInstance& I, const SpecBuf& B, int metric, const int* sizes0, int* sz,
-                          uint32_t* lvbuf, int o_from, int o_end, int par, int q) {
-  const int lane = threadIdx.x & 31;
-  const int K = I.K;
-  const int words = (K + 31) >> 5;
-  const bool tv = metric == kTV, rv = metric == kMSRV;
-  for (int p = lane; p < K; p += 32) sz[p] = sizes0[p];
-  __syncwarp();
-  Levels lv{lvbuf, lvbuf + 32, 0u, 0u, 0};
-  lv_rebuild(sz, K, lv);
-  for (int c0 = o_from; c0 < o_end; c0 += 32) {
-    // the chunk's words, one position per lane
-    const int oc = c0 + lane;
-    int pk = 0, fl = 0, wt = 0, wiso = 0;
-    if (oc < o_end) {
-      pk = lds(&B.dec[oc]);
-      fl = lds(&B.flag[oc]);
-      wt = lds(&B.wt[oc]);
-      wiso = lds(&B.slack[oc]);
-    }
-    const int n = min(32, o_end - c0);
-    for (int i = 0; i < n; i++) {
-      const int f = __shfl_sync(kAll, fl, i);
-      const int k = __shfl_sync(kAll, pk, i);
-      const int own = k >> 16;
-      if (!(f & 128)) {
-        // an evaluated position: its move (as speculated) shifts the sizes
-        const int w = __shfl_sync(kAll, wt, i);
-        if ((f & 1) && w != 0) {
-          const int d = k & 0xffff;
-          lv_move(sz, words, lv, own, sz[own], sz[own] - w);
-          lv_move(sz, words, lv, d, sz[d], sz[d] + w);
-          lv_settle(sz, K, lv);
-        }
-        continue;
-      }
-      const int w = __shfl_sync(kAll, wiso, i);
-      const int a = lv_argmin(lv);
-      int d = a;
-      if (tv && (lv.m > I.max_pw || lv.m < I.min_pw)) d = own;
-      const bool mover = d != own && !rv;
-      if (mover && w != 0) {
-        lv_move(sz, words, lv, own, sz[own], sz[own] - w);
-        lv_move(sz, words, lv, d, sz[d], sz[d] + w);
-        lv_settle(sz, K, lv);
-      }
-      if (lane == 0) {
-        const int o = c0 + i;
-        B.dec[o] = (own << 16) | d;
-        if (mover) {
-          B.flag[o] = (unsigned char)(128 | 16 | 1);
-          B.wt[o] = w;
-          if (w != 0) {
-            list_mover(B, par, o, w, (own << 16) | d);
-            atomicAdd(&B.wsum[o / q], w);
-          }
-        }
-      }
-    }
-  }
-  __syncwarp();
-}
-
 static_assert(kMaxGridVerts <= kSWarps, "one warp decides each whole-grid vertex of a window");
 
 // Two CTAs per SM: without the hint the compiler trades registers for a third
@@ -1097,8 +901,6 @@ __global__ void __launch_bounds__(kSThreads, 2) spec_ldg_kernel(DevInstance I, S
   Vol V{I.send, rv ? I.recv : nullptr};
 
   const bool vfix = metric == kMSV || metric == kMSRV;
-  // vertices without nets are decided by the size walker (K <= kWalkMaxK)
-  const bool walk = B.has_iso != 0 && K <= kWalkMaxK;
   int round = 0;
   int heavy_round = 0;
   int vr = 0;   // validation passes (parity selects the cut word)
@@ -1266,22 +1068,6 @@ __global__ void __launch_bounds__(kSThreads, 2) spec_ldg_kernel(DevInstance I, S
         const int v = __ldg(&I.order[z]);
         const uint32_t base = __ldg(&I.vptr[v]);
         const int deg = (int)(__ldg(&I.vptr[v + 1]) - base);
-        if (walk && deg == 0) {
-          // no nets: decided by the size walker after this phase
-          if (lane == 0) {
-            const int own = lds(&I.part_vec[v]);
-            B.dec[o] = (own << 16) | own;
-            B.flag[o] = 128;
-            B.slack[o] = __ldg(&I.w[v]);   // the walker's weight
-            B.vslack[o] = kBig;
-            B.wt[o] = 0;
-            B.vd[o] = 0;
-            if (logp) { B.rgain[o] = 0; B.rloss[o] = 0; }
-          }
-          if (metric == kTV)
-            for (int x = lane; x < words; x += 32) B.scan[(size_t)o * words + x] = 0u;
-          continue;
-        }
         if (__ldg(&B.vclass[v]) != 0) continue;   // medium vertex: evaluated by the whole CTA below
         const long long cz = clock64();
         const int own = lds(&I.part_vec[v]);
@@ -1519,14 +1305,6 @@ __global__ void __launch_bounds__(kSThreads, 2) spec_ldg_kernel(DevInstance I, S
         B.vsum[gw] = vsum + s_mv[wib];
       }
       if (!grid_barrier(B.bar, I.status)) return;
-      // the vertices without nets, in order, with the exact sizes (MSRV's never
-      // move: walked only for their decision records)
-      const bool walked = walk && (metric != kMSRV || logp);
-      if (walked) {
-        if (blockIdx.x == 0 && wib == 0)
-          size_walk(I, B, metric, sizes_s, cnt_b, reinterpret_cast<uint32_t*>(cnt_b + K), 0, end_w - pos, par, q);
-        if (!grid_barrier(B.bar, I.status)) return;
-      }
       if (blockIdx.x == 0 && threadIdx.x == 0) {
         const unsigned long long tE = gtimer();
         B.stats[16] += tE - tA;
@@ -1609,8 +1387,7 @@ __global__ void __launch_bounds__(kSThreads, 2) spec_ldg_kernel(DevInstance I, S
           const int slk = lds(&B.slack[o]), vslk = lds(&B.vslack[o]);
           int pk = lds(&B.dec[o]);
           const int v = __ldg(&I.order[z]);
-          if (z < zfix || (fl & (4 | 128))) {   // valid already / medium vertex, validated by the CTA below /
-                                                 // decided by the size walker on exact sizes
+          if (z < zfix || (fl & 4)) {      // valid already / medium vertex, validated by the CTA below
             Dw += wz;
             Vw += vz;
             continue;
@@ -1690,8 +1467,7 @@ __global__ void __launch_bounds__(kSThreads, 2) spec_ldg_kernel(DevInstance I, S
         if (blockIdx.x == 0 && threadIdx.x == 0) B.ctl[4 + ((vr + 1) & 1)] = kNone;   // the next pass's word
         vr++;
         // a size flip of a light position (MSV / MSRV): fix it and validate again
-        // (a fix would change the sizes the walker decided the later positions on)
-        bool fix = vfix && !walked && nfix < B.maxfix && cutw != kNone && (cutw & 7) == 2;
+        bool fix = vfix && nfix < B.maxfix && cutw != kNone && (cutw & 7) == 2;
         const int zc = cutw >> 3;
         if (fix) fix = zc < end_w && __ldg(&B.vclass[__ldg(&I.order[zc])]) == 0;
         if (!fix) break;
