@@ -5,10 +5,7 @@ Workload (default "zipf4m"): all six metrics (CN, TV, TM, MSM, MSV, MSRV), each 
 its own resident instance: K = 256, eps = 0.05 (C = (W/K) * 1.05),
 4,194,304 vertices and 4,194,304 nets, net sizes Zipf(2.1) clipped to
 [2, 10000], pins drawn by a Zipf(1.5) vertex popularity, source = first drawn
-pin; 10 refinement passes.  Synthetic and seeded.  The headline line uses unit
-vertex weights, the reference's own semantics (it counts vertices), so that the
-reference arm runs the same instance; the workload's degree weights are timed
-in the same run as a second figure ("degree_weights").
+pin, vertex weight = degree; 10 refinement passes.  Synthetic and seeded.
 
 A step is one refinement pass of each of the six resident instances; the
 instances carry their state between steps and restart from the streaming
@@ -21,10 +18,12 @@ six metrics (the reference's "Refinement took" span).
   e2e     through the C ABI with host buffers: host -> device upload of the
           state, the passes, device -> host copy of the part vector
   --impl reference: the reference's own OpenMP partition_par() (compiled from
-          its sources into oracle/_ref) on every host core, on the same instance
-          (drawn by the oracle's generator, no product library loaded) and the
-          same pass schedule; cpu_baseline is the same on the first passes of
-          the schedule (a bounded sample)
+          its sources into oracle/_ref) on every host core, on the same
+          hypergraph (drawn by the oracle's generator, no product library
+          loaded), K and pass schedule.  The reference has no vertex weights
+          (it counts vertices), so it runs the unit-weight form of the
+          instance; cpu_baseline is the same on the first passes of the
+          schedule (a bounded sample)
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 """
@@ -281,13 +280,12 @@ def run_ours(args):
     passes = args.passes or w["passes"]
     metrics = metrics_for(w, args.metrics)
     t_gen = time.time()
-    hg = fp.generate(spec_for(fp, w, args.scale, unit_weights=True))
+    hg = fp.generate(spec_for(fp, w, args.scale))
     t_gen = time.time() - t_gen
     stream = torch.cuda.Stream(device=device)
     eng = fp.Engine(device)
     eng.set_stream(stream.cuda_stream)
 
-    # Headline: unit weights, the reference's semantics.
     if dist:
         tdist.barrier()
     with Clocks(device) as clk:
@@ -343,22 +341,6 @@ def run_ours(args):
     uniq_per_launch = sum(unique[m] * len(per_metric[m]) for m in dom_metrics) / per_kernel[dom]["launches"]
     uniq_gbs = uniq_per_launch / (per_kernel[dom]["avg_launch_ms"] / 1e3) / 1e9
 
-    # Second figure: the workload's degree weights (the reference has no vertex
-    # weights, so the headline and the reference arm use unit weights).
-    degree = None
-    if w["weight_rule"] and not args.no_degree:
-        hgd = fp.generate(spec_for(fp, w, args.scale))
-        di, dpm, _, dinit = time_schedule(eng, stream, hgd, w, metrics, passes, args.steps, args.warmup,
-                                          account=False)
-        for inst in di.values():
-            inst.close()
-        dt = sum(sum(v) for v in dpm.values())
-        dval, dt, _ = whole_job(hgd.pins * len(metrics) * args.steps, dt, f"cuda:{device}")
-        degree = {"value": dval, "unit": "pins/s", "ms_per_step": dt / args.steps * 1e3,
-                  "per_metric_pins_per_s": {m: hgd.pins * len(v) / sum(v) for m, v in dpm.items()},
-                  "per_metric_ms_per_pass": {m: 1e3 * statistics.mean(v) for m, v in dpm.items()},
-                  "host_initial_partition_s": round(dinit, 2)}
-
     cpu = None
     if not args.no_cpu_baseline and rank == 0:
         cpu = cpu_baseline(w, args, per_metric)
@@ -377,9 +359,11 @@ def run_ours(args):
         "dtype": "int32",
         "data": "synthetic (seeded generator, fastpartitioner_gb300/csrc/fp_gen.cpp)",
         "config": {
-            "workload": workload_text(args.config, w, hg.nov, hg.noe, hg.pins, passes, metrics),
+            "workload": workload_text(args.config, w, hg.nov, hg.noe, hg.pins, passes, metrics,
+                                      "degree" if w["weight_rule"] else "unit"),
             "step": STEP_TEXT.format(passes=passes),
-            "weights": "unit (the reference counts vertices); degree weights in degree_weights",
+            "weights": ("vertex weight = degree; the reference arm and cpu_baseline run the same hypergraph "
+                        "with unit weights (the reference counts vertices)") if w["weight_rule"] else "unit",
             "l2": "inputs larger than L2 (per-instance CSRs and lists exceed 129 MB)" if hg.pins > 8_000_000
                   else "inputs smaller than L2",
             "per_metric_pins_per_s": {m: hg.pins * len(v) / sum(v) for m, v in per_metric.items()},
@@ -390,7 +374,6 @@ def run_ours(args):
             "parallelism": "one instance per metric on one GPU (replicas only across GPUs)",
             "e2e_step": f"per metric: reset_state (host -> device) + refine({passes}) + partition (device -> host)",
         },
-        "degree_weights": degree,
         "e2e": {"value": e2e_value, "unit": "pins/s", "h2d_bytes_per_step": h2d // len(metrics),
                 "d2h_bytes_per_step": d2h // len(metrics)},
         "gpu_launches": launches,
@@ -414,10 +397,10 @@ STEP_TEXT = ("one refinement pass of each metric's resident instance (state carr
              "restart from the initial partition every {passes} steps, untimed)")
 
 
-def workload_text(name, w, nov, noe, pins, passes, metrics):
-    """The workload string, the same on both arms."""
-    return (f"{name}: {nov} vertices, {noe} nets, {pins} pins, unit weights, K={w['K']}, eps factor {w['eps']}, "
-            f"{passes}-pass schedule, metrics {','.join(metrics)}")
+def workload_text(name, w, nov, noe, pins, passes, metrics, weights):
+    """The workload string of either arm (they differ only in the weights)."""
+    return (f"{name}: {nov} vertices, {noe} nets, {pins} pins, {weights} weights, K={w['K']}, eps factor "
+            f"{w['eps']}, {passes}-pass schedule, metrics {','.join(metrics)}")
 
 
 def unique_bytes(hg, K):
@@ -562,7 +545,9 @@ def run_reference_arm(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": tot_t / args.steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
         "data": "synthetic (seeded generator; instance drawn by oracle/fp_oracle_gen.cpp)", "impl": "reference",
-        "config": {"workload": workload_text(args.config, w, nov, noe, pins, passes, metrics),
+        "config": {"workload": workload_text(args.config, w, nov, noe, pins, passes, metrics, "unit"),
+                   "weights": "unit: the reference counts vertices and has no vertex weights; the GPU arm runs "
+                              "the same hypergraph with the workload's weights",
                    "step": STEP_TEXT.format(passes=passes), "threads": threads,
                    "per_metric_pins_per_s": {m: pins * k / t for m, (k, t) in res.items()},
                    "per_metric_refine_s": {m: t for m, (_, t) in res.items()}},
@@ -664,7 +649,6 @@ def main():
     ap.add_argument("--cpu-passes", type=int, default=2,
                     help="cpu_baseline: passes of each metric's schedule (a bounded sample)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-degree", action="store_true", help="skip the degree-weight figure")
     ap.add_argument("--mode", default="refine", choices=["refine", "batch", "serve"],
                     help="refine: the pins/s line; batch / serve: the many-request runners")
     ap.add_argument("--batch-n", type=int, default=64)
