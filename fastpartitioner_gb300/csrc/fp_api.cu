@@ -112,6 +112,10 @@ struct fp_instance {
   int* heavy_pos_d = nullptr;
   std::vector<int> mid_pos;       // CTA-evaluated vertices, by position
   int* mid_pos_d = nullptr;
+  std::vector<int> porder;        // LDG engine positions (SpecBuf::porder)
+  int* porder_d = nullptr;
+  int* iso_list_d = nullptr;
+  int* iso_before_d = nullptr;
   unsigned char* vclass_d = nullptr;
 };
 
@@ -333,6 +337,56 @@ static cudaError_t clear_spec_scratch(const SpecBuf& b, int noe, int K, cudaStre
   return e;
 }
 
+// Positions of the LDG engine (TV / MSV / MSRV).  A vertex without nets and
+// with weight 0 reads only the part sizes and changes nothing that a later
+// decision reads; when every vertex without nets weighs 0 (vertex weight =
+// degree), they are left out of the walked positions and decided after each
+// window from the exact sizes at their place.  Uploads porder, iso_list and
+// iso_before and fills the SpecBuf fields.
+static int build_positions(fp_instance* in) {
+  const HostGraph& g = in->g;
+  const Problem& pb = in->pb;
+  in->porder.clear();
+  std::vector<int> iso, before;
+  bool compact = true, any_iso = false;
+  for (int v = 0; v < g.nov; v++)
+    if (g.vptr[v + 1] == g.vptr[v]) {
+      any_iso = true;
+      if (pb.w[v] != 0) compact = false;
+    }
+  compact = compact && any_iso;
+  for (int z = 0; z < g.nov; z++) {
+    const int v = pb.order[z];
+    if (compact && g.vptr[v + 1] == g.vptr[v]) {
+      iso.push_back(v);
+    } else {
+      in->porder.push_back(v);
+      before.push_back((int)iso.size());
+    }
+  }
+  if (compact && in->porder.empty()) {   // nothing but vertices without nets: walk them all
+    in->porder.assign(pb.order.begin(), pb.order.end());
+    iso.clear();
+    before.clear();
+    compact = false;
+  }
+  before.push_back((int)iso.size());
+  in->sb.porder = in->porder_d;
+  in->sb.npos = (int)in->porder.size();
+  in->sb.iso_list = in->iso_list_d;
+  in->sb.iso_before = in->iso_before_d;
+  in->sb.niso = compact ? (int)iso.size() : 0;
+  cudaStream_t s = in->ctx->stream;
+  cudaError_t e = cudaMemcpyAsync(in->porder_d, in->porder.data(), sizeof(int) * in->porder.size(),
+                                  cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess && !iso.empty())
+    e = cudaMemcpyAsync(in->iso_list_d, iso.data(), sizeof(int) * iso.size(), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess && compact)
+    e = cudaMemcpyAsync(in->iso_before_d, before.data(), sizeof(int) * before.size(), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);   // host vectors are local
+  return cuda_status(e);
+}
+
 // Vertex classes of the LDG engine (see kLightWork) and the position lists of
 // the medium and whole-grid vertices, uploaded to the device.
 static int classify(fp_instance* in, long long light_work, long long super_work) {
@@ -368,8 +422,9 @@ static int classify(fp_instance* in, long long light_work, long long super_work)
   // TM and MSM walk the vertices in id order (TM/partition.cpp:300), the others
   // in the visiting order.
   const bool by_id = pb.metric == FP_METRIC_TM || pb.metric == FP_METRIC_MSM;
-  for (int z = 0; z < g.nov; z++) {
-    const int v = by_id ? z : pb.order[z];
+  const int npos = by_id ? g.nov : (int)in->porder.size();
+  for (int z = 0; z < npos; z++) {
+    const int v = by_id ? z : in->porder[z];
     long long work = 0;
     for (uint32_t k = g.vptr[v]; k < g.vptr[v + 1]; k++) {
       const uint32_t e = g.vnets[k];
@@ -468,6 +523,8 @@ int fp_instance_create(fp_ctx* ctx, const fp_hypergraph* h, int32_t K, int32_t m
         (rc = dalloc(in, &in->sb.hadelta, 2 * kMaxGridVerts * K)) ||
         (rc = dalloc(in, &in->sb.hmisc, 16 * kMaxGridVerts)) || (rc = dalloc(in, &in->sb.mlast, K)) || (rc = dalloc(in, &in->heavy_pos_d, std::max(g.nov, g.noe))) ||
         (rc = dalloc(in, &in->mid_pos_d, std::max(g.nov, g.noe))) ||
+        (rc = dalloc(in, &in->porder_d, ldg ? g.nov : 1)) || (rc = dalloc(in, &in->iso_list_d, ldg ? g.nov : 1)) ||
+        (rc = dalloc(in, &in->iso_before_d, ldg ? g.nov + 1 : 1)) ||
         (rc = dalloc(in, &in->metric_out, 8))) {
       fp_instance_destroy(in);
       return rc;
@@ -496,6 +553,7 @@ int fp_instance_create(fp_ctx* ctx, const fp_hypergraph* h, int32_t K, int32_t m
       if (e == cudaSuccess && cn) e = cudaMemsetAsync(in->sb.cn_wit, 0xff, sizeof(int) * g.nov, s0);   // no witnesses
       if (e == cudaSuccess) e = cudaStreamSynchronize(s0);
       if (e != cudaSuccess) { fp_instance_destroy(in); return cuda_status(e); }
+      if (ldg && (rc = build_positions(in))) { fp_instance_destroy(in); return rc; }
       rc = classify(in, metric == FP_METRIC_CN ? kCnLightPins : kLightWork,
                     metric == FP_METRIC_CN ? kCnGridPins : default_super_work(metric));
       if (rc) { fp_instance_destroy(in); return rc; }
@@ -575,7 +633,9 @@ int fp_instance_footprint(int32_t nov, int32_t noe, int64_t pins, int32_t K, int
     add(E, 4); add(E, 8); add(E, 4); add(E, 4);              // claim_m, claim64, claim_c, mask_c
     add(G2K, 4); add(G2K, 8); add(G2K, 4); add(G2K, 4); add(G2K, 4);
     add(16 * (size_t)kMaxGridVerts, 4); add(K, 8);           // hmisc, mlast
-    add(VE, 4); add(VE, 4); add(8, 8);                       // heavy / medium positions, metric_out
+    add(VE, 4); add(VE, 4);                                  // heavy / medium positions
+    add(ldg ? V : 1, 4); add(ldg ? V : 1, 4); add(ldg ? V + 1 : 1, 4);   // porder, iso_list, iso_before
+    add(8, 8);                                               // metric_out
     b += (long long)metrics_scratch_bytes(K);
     *bytes = b;
     return FP_OK;

@@ -118,6 +118,17 @@ struct SpecBuf {
   int gmax;              // whole-grid vertices one window may hold (1 .. kMaxGridVerts)
   int wgrow;             // LDG window after a cut: this many times the last valid length
   int maxfix;            // in-window decision fixes per window (MSV / MSRV)
+  // LDG engine positions: the vertices walked in windows, in visiting order.
+  // When every vertex without nets weighs 0 they are left out of the
+  // positions (porder holds the others) and decided after each window:
+  // iso_list holds them in visiting order, iso_before[j] counts those before
+  // position j (iso_before[npos] = niso).  Otherwise porder is the visiting
+  // order and niso = 0.
+  const int* porder;
+  int npos;
+  const int* iso_list;
+  const int* iso_before;
+  int niso;
   unsigned long long* stats;  // [kNumStats] round statistics (see fp_get_stats)
   int wmax;              // longest window of the LDG and CN engines
   int wmax_msg;          // longest window of the TM / MSM engine (dec only)

@@ -588,7 +588,7 @@ __device__ void cta_eval_ldg(const DevInstance& I, const SpecBuf& B, const Round
   const int words = (K + 31) >> 5;
   const bool vol = metric != kTV, rv = metric == kMSRV;
   const int o = z - pos;
-  const int v = __ldg(&I.order[z]);
+  const int v = __ldg(&B.porder[z]);
   const int own = lds(&I.part_vec[v]);
   const uint32_t base = __ldg(&I.vptr[v]);
   const int deg = (int)(__ldg(&I.vptr[v + 1]) - base);
@@ -735,7 +735,7 @@ __device__ void cta_validate_ldg(const DevInstance& I, const SpecBuf& B, const R
   const int fl = lds(&B.flag[o]);
   const int pk = lds(&B.dec[o]);
   const int own = pk >> 16, d = pk & 0xffff;
-  const int v = __ldg(&I.order[z]);
+  const int v = __ldg(&B.porder[z]);
   if (wib == 0) {
     // drift before z: earlier CTAs, this CTA's warps before the owner (cw / cv),
     // the owner's positions before z
@@ -794,7 +794,7 @@ __device__ void fix_position(const DevInstance& I, const SpecBuf& B, const Round
   const int lane = threadIdx.x & 31;
   const bool vol = metric != kTV, rv = metric == kMSRV;
   const int K = I.K;
-  const int v = __ldg(&I.order[z]);
+  const int v = __ldg(&B.porder[z]);
   const uint32_t base = __ldg(&I.vptr[v]);
   const int deg = (int)(__ldg(&I.vptr[v + 1]) - base);
   const int fl = lds(&B.flag[o]);
@@ -912,7 +912,7 @@ __global__ void __launch_bounds__(kSThreads, 2) spec_ldg_kernel(DevInstance I, S
     int hidx = 0;
     bool pass_start = true;
     bool prev_maxtouch = false;
-    while (pos < I.nov) {
+    while (pos < B.npos) {
       const int par = round & 1;
       // ------------------------------------------------------------ round state
       for (int p = threadIdx.x; p < K; p += blockDim.x) {
@@ -924,7 +924,7 @@ __global__ void __launch_bounds__(kSThreads, 2) spec_ldg_kernel(DevInstance I, S
           // (block 0 stores it; the others read only parts not scanned there)
           const unsigned long long ml = lds(&B.mlast[p]);
           if (round > 0 && (int)(ml >> 32) == round) {
-            const int mv = __ldg(&I.order[(int)(ml & 0xffffffffu)]);
+            const int mv = __ldg(&B.porder[(int)(ml & 0xffffffffu)]);
             marker_s[p] = mv;
             if (blockIdx.x == 0) I.marker[p] = mv;
           } else {
@@ -1000,7 +1000,7 @@ __global__ void __launch_bounds__(kSThreads, 2) spec_ldg_kernel(DevInstance I, S
       // ================================================================= round
       // A window holds up to gmax whole-grid vertices and ends before the next
       // one.
-      int end_w = min(pos + W, I.nov);
+      int end_w = min(pos + W, B.npos);
       if (hidx + B.gmax < B.nheavy) end_w = min(end_w, (int)__ldg(&B.heavy_pos[hidx + B.gmax]));
       int ns = 0;
       while (ns < B.gmax && hidx + ns < B.nheavy && __ldg(&B.heavy_pos[hidx + ns]) < end_w) ns++;
@@ -1016,7 +1016,7 @@ __global__ void __launch_bounds__(kSThreads, 2) spec_ldg_kernel(DevInstance I, S
       const unsigned long long tR = gtimer();
       if ((int)threadIdx.x < ns) {
         const int z = __ldg(&B.heavy_pos[hidx + threadIdx.x]);
-        const int v = __ldg(&I.order[z]);
+        const int v = __ldg(&B.porder[z]);
         const uint32_t b = __ldg(&I.vptr[v]);
         s_gz[threadIdx.x] = z;
         s_gv[threadIdx.x] = v;
@@ -1065,7 +1065,7 @@ __global__ void __launch_bounds__(kSThreads, 2) spec_ldg_kernel(DevInstance I, S
       int nV = 0;
       for (int z = z0; z < z1; z++) {
         const int o = z - pos;
-        const int v = __ldg(&I.order[z]);
+        const int v = __ldg(&B.porder[z]);
         const uint32_t base = __ldg(&I.vptr[v]);
         const int deg = (int)(__ldg(&I.vptr[v + 1]) - base);
         if (__ldg(&B.vclass[v]) != 0) continue;   // medium vertex: evaluated by the whole CTA below
@@ -1386,7 +1386,7 @@ __global__ void __launch_bounds__(kSThreads, 2) spec_ldg_kernel(DevInstance I, S
           const int fl = lds(&B.flag[o]);
           const int slk = lds(&B.slack[o]), vslk = lds(&B.vslack[o]);
           int pk = lds(&B.dec[o]);
-          const int v = __ldg(&I.order[z]);
+          const int v = __ldg(&B.porder[z]);
           if (z < zfix || (fl & 4)) {      // valid already / medium vertex, validated by the CTA below
             Dw += wz;
             Vw += vz;
@@ -1469,7 +1469,7 @@ __global__ void __launch_bounds__(kSThreads, 2) spec_ldg_kernel(DevInstance I, S
         // a size flip of a light position (MSV / MSRV): fix it and validate again
         bool fix = vfix && nfix < B.maxfix && cutw != kNone && (cutw & 7) == 2;
         const int zc = cutw >> 3;
-        if (fix) fix = zc < end_w && __ldg(&B.vclass[__ldg(&I.order[zc])]) == 0;
+        if (fix) fix = zc < end_w && __ldg(&B.vclass[__ldg(&B.porder[zc])]) == 0;
         if (!fix) break;
         if (gw == (zc - pos) / q)
           fix_position(I, B, R, metric, zc, zc - pos, par, gw, loc, gains, losses, adelta, logp);
@@ -1509,7 +1509,7 @@ __global__ void __launch_bounds__(kSThreads, 2) spec_ldg_kernel(DevInstance I, S
         for (int z = z0 + lane; z < min(z1, cut); z += 32) {
           const int o = z - pos;
           const int fl = lds(&B.flag[o]);
-          I.recs[__ldg(&I.order[z])] =
+          I.recs[__ldg(&B.porder[z])] =
               make_int4(lds(&B.dec[o]) & 0xffff, lds(&B.rgain[o]), lds(&B.rloss[o]), fl & 1);
         }
       }
@@ -1517,7 +1517,7 @@ __global__ void __launch_bounds__(kSThreads, 2) spec_ldg_kernel(DevInstance I, S
         const int o = z - pos;
         const int fl = lds(&B.flag[o]);
         if (!(fl & (1 | 64)) || (fl & 4)) continue;   // claims held: a mover or a replaced mover
-        const int v = __ldg(&I.order[z]);
+        const int v = __ldg(&B.porder[z]);
         const int pk = lds(&B.dec[o]);
         const int own = pk >> 16, d = pk & 0xffff;
         const uint32_t base = __ldg(&I.vptr[v]);
@@ -1542,7 +1542,7 @@ __global__ void __launch_bounds__(kSThreads, 2) spec_ldg_kernel(DevInstance I, S
         const int o = z - pos;
         const int fl = lds(&B.flag[o]);
         if (!(fl & 1)) continue;
-        const int v = __ldg(&I.order[z]);
+        const int v = __ldg(&B.porder[z]);
         const int pk = lds(&B.dec[o]);
         const int own = pk >> 16, d = pk & 0xffff;
         const uint32_t base = __ldg(&I.vptr[v]);
@@ -1584,6 +1584,92 @@ __global__ void __launch_bounds__(kSThreads, 2) spec_ldg_kernel(DevInstance I, S
           }
           unclaim_nets(I, B, vol, base_s, deg_s, gtid, gthreads);
         }
+      }
+      if (B.niso && (metric != kMSRV || logp)) {
+        // Vertices without nets, weight 0 (positions hold only the others):
+        // each takes the least-loaded part at its place in the visiting order
+        // (TV: unless the clamps keep it home) and changes nothing a later
+        // decision reads, so they are decided here, after the cut, from the
+        // exact sizes between the committed positions (MSRV never moves them;
+        // there they are walked only for the decision records).
+        int* dsz = gains_b;   // the committed movers' size changes before this CTA's first position
+        const int cta_o0 = cz0 - pos;
+        for (int p = threadIdx.x; p < K; p += blockDim.x) dsz[p] = 0;
+        __syncthreads();
+        const int nmv = lds(&B.mcnt[par]);
+        for (int i = threadIdx.x; i < nmv; i += blockDim.x) {
+          const int4 m = lds(&B.mlist[i]);
+          if (m.x >= cta_o0 || m.y == 0) continue;
+          atomicAdd(&dsz[m.z & 0xffff], m.y);
+          atomicAdd(&dsz[m.z >> 16], -m.y);
+        }
+        __syncthreads();
+        const int zb = min(z1, cut);
+        if (z0 < zb) {
+          int* sz = cnt;   // this warp's sizes, at its current position
+          for (int p = lane; p < K; p += 32) sz[p] = sizes_s[p] + dsz[p];
+          __syncwarp();
+          for (int o2 = cta_o0 + lane; o2 < z0 - pos; o2 += 32) {
+            const int w = lds(&B.wt[o2]);
+            if (w == 0) continue;
+            const int pk = lds(&B.dec[o2]);
+            atomicAdd(&sz[pk & 0xffff], w);
+            atomicAdd(&sz[pk >> 16], -w);
+          }
+          __syncwarp();
+          int amin = -1;
+          long long nmoved = 0;
+          auto group = [&](int k0, int k1) {
+            if (k0 >= k1) return;
+            if (amin < 0) {
+              unsigned long long mk = ~0ull;
+              for (int p = lane; p < K; p += 32) {
+                const unsigned long long key = ((unsigned long long)((unsigned)sz[p] ^ 0x80000000u) << 32) | (unsigned)p;
+                mk = key < mk ? key : mk;
+              }
+              for (int off = 16; off; off >>= 1) {
+                const unsigned long long x = __shfl_xor_sync(kAll, mk, off);
+                mk = x < mk ? x : mk;
+              }
+              amin = (int)(mk & 0xffffffffu);
+            }
+            const int sa = sz[amin];
+            const bool home = metric == kTV && (sa > I.max_pw || sa < I.min_pw);
+            for (int k = k0 + lane; k < k1; k += 32) {
+              const int v = __ldg(&B.iso_list[k]);
+              const int own = lds(&I.part_vec[v]);
+              const int d = home ? own : amin;
+              const bool mv = d != own && metric != kMSRV;
+              if (mv) {
+                I.part_vec[v] = d;
+                nmoved++;
+              }
+              if (logp) I.recs[v] = make_int4(d, 0, 0, mv ? 1 : 0);
+            }
+          };
+          if (pos == 0 && gw == 0) group(0, __ldg(&B.iso_before[0]));   // before the pass's first position
+          for (int z = z0; z < zb; z++) {
+            const int o = z - pos;
+            const int w = lds(&B.wt[o]);
+            if (w != 0) {
+              __syncwarp();
+              if (lane == 0) {
+                const int pk = lds(&B.dec[o]);
+                sz[pk & 0xffff] += w;
+                sz[pk >> 16] -= w;
+              }
+              __syncwarp();
+              amin = -1;
+            }
+            group(__ldg(&B.iso_before[z]), __ldg(&B.iso_before[z + 1]));
+          }
+          nmoved = warp_sum64(nmoved);
+          if (lane == 0 && nmoved) {
+            atomicAdd((unsigned long long*)&I.moves[it], (unsigned long long)nmoved);
+            atomicAdd(&B.stats[2], (unsigned long long)nmoved);
+          }
+        }
+        __syncthreads();
       }
       if (ns) {
         // the other parity's tallies are cleared for the next window with
@@ -1645,7 +1731,7 @@ __global__ void __launch_bounds__(kSThreads, 2) spec_ldg_kernel(DevInstance I, S
     // markers of the last window (the loop's final barrier made them visible)
     for (int p = threadIdx.x; p < K; p += blockDim.x) {
       const unsigned long long ml = lds(&B.mlast[p]);
-      if (round > 0 && (int)(ml >> 32) == round) I.marker[p] = __ldg(&I.order[(int)(ml & 0xffffffffu)]);
+      if (round > 0 && (int)(ml >> 32) == round) I.marker[p] = __ldg(&B.porder[(int)(ml & 0xffffffffu)]);
     }
   }
 }
