@@ -569,34 +569,40 @@ def same_results(a, b):
 
 
 def run_batch(args):
-    """Mixed batch: requests of uneven size, K and metric (vertices
-    log-uniform in [1e3, 1e6], nets = vertices x U[0.5, 2], Zipf(2.2) net sizes
-    up to 2000 pins, K from {2, 4, ..., 512}, metric uniform over the six,
-    --batch-passes passes), the pipelined runner against the plain
-    per-request loop on the same requests; partitions/s on the wall clock,
-    hypergraph construction and streaming initial partitions included."""
+    """Mixed batch (config: vertices log-uniform in [1e3, 1e6], nets =
+    vertices x U[0.5, 2], Zipf(2.2) net sizes up to 2000 pins, K from {2, 4,
+    ..., 512}, metric uniform over the six, --batch-passes passes, unit
+    weights): --gpu-slots concurrent GPU slots (run_concurrent: own stream, a
+    share of the SMs and a device arena each, host preparation on --workers
+    threads, largest request first) against the plain per-request loop on the
+    same requests; partitions/s on the wall clock, hypergraph construction and
+    streaming initial partitions included."""
     import torch
     import fastpartitioner_gb300 as fp
     from fastpartitioner_gb300 import serving as sv
     torch.cuda.set_device(0)
-    eng = fp.Engine(0)
     mk = lambda: sv.mixed_batch(args.batch_n, seed=args.batch_seed, passes=args.batch_passes)
+    arena = sv.arena_for(mk())
+    slots = sv.gpu_slots(0, args.gpu_slots, arena)
+    eng = fp.Engine(0)
     for _ in range(args.warmup):
-        sv.run_pipelined(eng, mk()[:4], workers=args.workers)
+        sv.run_concurrent(slots, sv.mixed_batch(8, seed=99, vmax=20_000), workers=args.workers)
+    conc = sv.run_concurrent(slots, mk(), workers=args.workers)
     plain = sv.run_plain(eng, mk())
-    pipe = sv.run_pipelined(eng, mk(), workers=args.workers)
-    sp, spp = sv.summary(plain), sv.summary(pipe)
+    sp, sc = sv.summary(plain), sv.summary(conc)
     eng.close()
+    for e in slots:
+        e.close()
     line = {
-        "metric": "partitions/s (mixed batch, pipelined vs plain per-request loop)",
-        "value": spp["partitions_per_s"], "unit": "partitions/s", "n_gpus": 1, "steps": 1,
-        "warmup": args.warmup, "ms_per_step": 1e3 * spp["makespan_s"], "higher_is_better": True,
+        "metric": "partitions/s (mixed batch, concurrent GPU slots vs plain per-request loop)",
+        "value": sc["partitions_per_s"], "unit": "partitions/s", "n_gpus": 1, "steps": 1,
+        "warmup": args.warmup, "ms_per_step": 1e3 * sc["makespan_s"], "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded generator)",
         "config": {"workload": f"mixed batch of {args.batch_n} hypergraphs (seed {args.batch_seed}), "
                                f"{args.batch_passes} passes each", "workers": args.workers,
-                   "plain_loop": sp, "pipelined": spp,
-                   "speedup_vs_plain": spp["partitions_per_s"] / sp["partitions_per_s"],
-                   "same_alone_and_in_the_mix": same_results(plain, pipe)},
+                   "gpu_slots": args.gpu_slots, "arena_bytes": arena, "plain_loop": sp, "concurrent": sc,
+                   "speedup_vs_plain": sc["partitions_per_s"] / sp["partitions_per_s"],
+                   "same_alone_and_in_the_mix": same_results(plain, conc)},
     }
     print(json.dumps(line), flush=True)
 
@@ -605,23 +611,30 @@ def run_serve(args):
     """Continuous serving: Poisson arrivals at --rate per second for
     --duration seconds, each request a hypergraph as in the mixed batch with
     vertices log-uniform in [1e3, --serve-vmax], admission by device footprint
-    under --budget-gb; against a serial queue of plain per-request calls on the
-    same arrivals.  Latency is arrival to result."""
+    under --budget-gb, refinement on --gpu-slots concurrent GPU slots; against a
+    serial queue of plain per-request calls on the same arrivals.  Latency is
+    arrival to result."""
     import torch
     import fastpartitioner_gb300 as fp
     from fastpartitioner_gb300 import serving as sv
     torch.cuda.set_device(0)
-    eng = fp.Engine(0)
     n = max(1, int(round(args.rate * args.duration)))
     mk = lambda: sv.poisson_arrivals(sv.mixed_batch(n, seed=args.batch_seed, vmax=args.serve_vmax,
                                                     passes=args.batch_passes), args.rate, seed=1)
+    arena = sv.arena_for(mk())
+    budget = int(args.budget_gb * 2**30)
+    nslots = max(1, min(args.gpu_slots, budget // arena))
+    slots = sv.gpu_slots(0, nslots, arena)
     for _ in range(args.warmup):
-        sv.run_pipelined(eng, sv.mixed_batch(4, seed=99, vmax=20_000), workers=args.workers)
-    srv = sv.Server(eng, budget_bytes=int(args.budget_gb * 2**30), workers=args.workers, slots=args.slots)
+        sv.run_concurrent(slots, sv.mixed_batch(8, seed=99, vmax=20_000), workers=args.workers)
+    srv = sv.Server(slots, budget_bytes=budget - nslots * arena, workers=args.workers, slots=args.slots)
     served = srv.run(mk())
+    eng = fp.Engine(0)
     serial = sv.run_plain(eng, mk())
     ss, sq = sv.summary(served), sv.summary(serial)
     eng.close()
+    for e in slots:
+        e.close()
     line = {
         "metric": "p99 latency (continuous serving vs a serial plain-GPU queue)",
         "value": ss["p99_latency_s"], "unit": "s", "n_gpus": 1, "steps": 1, "warmup": args.warmup,
@@ -629,7 +642,8 @@ def run_serve(args):
         "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded generator, Poisson arrivals)",
         "config": {"workload": f"{n} requests at {args.rate}/s, vertices log-uniform in [1e3, {args.serve_vmax}], "
                                f"{args.batch_passes} passes", "budget_gb": args.budget_gb,
-                   "workers": args.workers, "slots": args.slots, "served": ss, "serial_queue": sq,
+                   "workers": args.workers, "admission_slots": args.slots, "gpu_slots": nslots,
+                   "arena_bytes": arena, "served": ss, "serial_queue": sq,
                    "peak_reserved_gb": srv.peak_reserved / 2**30,
                    "same_alone_and_in_the_mix": same_results(sorted(serial, key=lambda r: r.rid), served)},
     }
@@ -657,9 +671,10 @@ def main():
     ap.add_argument("--workers", type=int, default=os.cpu_count() or 8)
     ap.add_argument("--rate", type=float, default=20.0)
     ap.add_argument("--duration", type=float, default=5.0)
-    ap.add_argument("--serve-vmax", type=int, default=1_000_000)
+    ap.add_argument("--serve-vmax", type=int, default=4_000_000)
     ap.add_argument("--budget-gb", type=float, default=150.0)
-    ap.add_argument("--slots", type=int, default=32)
+    ap.add_argument("--slots", type=int, default=32, help="serve: requests admitted at once")
+    ap.add_argument("--gpu-slots", type=int, default=4, help="batch / serve: concurrent GPU slots")
     args = ap.parse_args()
     if args.mode == "batch":
         run_batch(args)

@@ -121,6 +121,8 @@ def lib():
             "fp_ctx_create": ([i32, pp], C.c_int),
             "fp_ctx_destroy": ([vp], C.c_int),
             "fp_ctx_set_stream": ([vp, vp], C.c_int),
+            "fp_ctx_set_arena": ([vp, i64], C.c_int),
+            "fp_ctx_set_sm_limit": ([vp, i32], C.c_int),
             "fp_instance_create": ([vp, C.POINTER(_Hypergraph), i32, i32, dbl, pp], C.c_int),
             "fp_instance_destroy": ([vp], C.c_int),
             "fp_instance_device_bytes": ([vp, C.POINTER(i64)], C.c_int),
@@ -374,6 +376,15 @@ class Engine:
         """Runs subsequent work on the given cudaStream_t (e.g. a torch stream's
         ``cuda_stream``); None selects the engine's own stream."""
         _check(lib().fp_ctx_set_stream(self._ctx, stream_handle), "fp_ctx_set_stream")
+
+    def set_arena(self, nbytes: int) -> None:
+        """fp_ctx_set_arena: instances of this engine take their device buffers
+        from one allocation of `nbytes` (one instance at a time); 0 releases it."""
+        _check(lib().fp_ctx_set_arena(self._ctx, int(nbytes)), "fp_ctx_set_arena")
+
+    def set_sm_limit(self, sms: int) -> None:
+        """fp_ctx_set_sm_limit: size this engine's grids for `sms` SMs (0: all)."""
+        _check(lib().fp_ctx_set_sm_limit(self._ctx, int(sms)), "fp_ctx_set_sm_limit")
 
     def instance(self, hg: Hypergraph, K: int, metric, eps_factor: float = 1.05) -> "Instance":
         return Instance(self, hg, K, metric_id(metric), eps_factor)

@@ -79,10 +79,22 @@ using namespace fp;
 
 struct fp_ctx {
   int device = 0;
-  int num_sms = 0;
+  int num_sms = 0;    // SMs the engines size their grids for (fp_ctx_set_sm_limit)
+  int dev_sms = 0;    // SMs of the device
   int max_smem = 0;   // opt-in shared memory per CTA
   cudaStream_t own = nullptr;
   cudaStream_t stream = nullptr;
+  // fp_ctx_set_arena: one device allocation that instances of this context
+  // take their buffers from, and pinned host words they share, so that
+  // creating and releasing an instance calls neither cudaMalloc nor cudaFree
+  // (which waits for the whole device, other contexts' work included)
+  unsigned char* arena = nullptr;
+  size_t arena_bytes = 0;
+  size_t arena_used = 0;
+  bool arena_busy = false;   // an instance holds the arena (one at a time)
+  long long* h_moves = nullptr;     // pinned, with the arena
+  int* h_status = nullptr;
+  long long* h_metrics = nullptr;
 };
 
 struct fp_instance {
@@ -94,6 +106,7 @@ struct fp_instance {
   DevInstance d{};
   std::vector<void*> allocs;
   long long dev_bytes = 0;        // bytes of the device allocations in `allocs`
+  bool in_arena = false;          // buffers taken from ctx->arena (nothing in allocs)
   void* metric_scratch = nullptr;
   long long* metric_out = nullptr;
   long long* h_moves = nullptr;   // pinned
@@ -131,13 +144,26 @@ int cuda_status(cudaError_t e) {
   return FP_ERR_CUDA;
 }
 
+// Arena allocations are 256-byte aligned, like cudaMalloc's.
+constexpr size_t kArenaAlign = 256;
+
 template <class T>
 int dalloc(fp_instance* in, T** p, size_t n) {
+  const size_t bytes = std::max<size_t>(n, 1) * sizeof(T);
+  if (in->in_arena) {
+    fp_ctx* c = in->ctx;
+    const size_t at = (c->arena_used + kArenaAlign - 1) & ~(kArenaAlign - 1);
+    if (at + bytes > c->arena_bytes) return FP_ERR_NOMEM;
+    c->arena_used = at + bytes;
+    in->dev_bytes += (long long)bytes;
+    *p = reinterpret_cast<T*>(c->arena + at);
+    return FP_OK;
+  }
   void* q = nullptr;
-  cudaError_t e = cudaMalloc(&q, std::max<size_t>(n, 1) * sizeof(T));
+  cudaError_t e = cudaMalloc(&q, bytes);
   if (e != cudaSuccess) return cuda_status(e);
   in->allocs.push_back(q);
-  in->dev_bytes += (long long)(std::max<size_t>(n, 1) * sizeof(T));
+  in->dev_bytes += (long long)bytes;
   *p = static_cast<T*>(q);
   return FP_OK;
 }
@@ -283,6 +309,7 @@ int fp_ctx_create(int32_t device, fp_ctx** out) {
     if (!c) return FP_ERR_NOMEM;
     c->device = device;
     cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
+    c->dev_sms = c->num_sms;
     cudaDeviceGetAttribute(&c->max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
     e = cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking);
     if (e != cudaSuccess) { delete c; return cuda_status(e); }
@@ -292,12 +319,55 @@ int fp_ctx_create(int32_t device, fp_ctx** out) {
   });
 }
 
+static void arena_release(fp_ctx* c) {
+  if (c->arena) cudaFree(c->arena);
+  if (c->h_moves) cudaFreeHost(c->h_moves);
+  if (c->h_status) cudaFreeHost(c->h_status);
+  if (c->h_metrics) cudaFreeHost(c->h_metrics);
+  c->arena = nullptr;
+  c->h_moves = nullptr;
+  c->h_status = nullptr;
+  c->h_metrics = nullptr;
+  c->arena_bytes = c->arena_used = 0;
+}
+
 int fp_ctx_destroy(fp_ctx* ctx) {
   return fp::guarded([&]() -> int {
     if (!ctx) return FP_ERR_INVALID;
     cudaSetDevice(ctx->device);
+    arena_release(ctx);
     if (ctx->own) cudaStreamDestroy(ctx->own);
     delete ctx;
+    return FP_OK;
+  });
+}
+
+int fp_ctx_set_arena(fp_ctx* ctx, int64_t bytes) {
+  return fp::guarded([&]() -> int {
+    if (!ctx || bytes < 0) return FP_ERR_INVALID;
+    if (ctx->arena_busy) return FP_ERR_STATE;
+    cudaSetDevice(ctx->device);
+    arena_release(ctx);
+    if (bytes == 0) return FP_OK;
+    void* p = nullptr;
+    cudaError_t e = cudaMalloc(&p, (size_t)bytes);
+    if (e != cudaSuccess) return cuda_status(e);
+    ctx->arena = static_cast<unsigned char*>(p);
+    ctx->arena_bytes = (size_t)bytes;
+    if (cudaMallocHost(&ctx->h_moves, sizeof(long long) * kMaxPasses) != cudaSuccess ||
+        cudaMallocHost(&ctx->h_status, sizeof(int)) != cudaSuccess ||
+        cudaMallocHost(&ctx->h_metrics, sizeof(long long) * 8) != cudaSuccess) {
+      arena_release(ctx);
+      return FP_ERR_NOMEM;
+    }
+    return FP_OK;
+  });
+}
+
+int fp_ctx_set_sm_limit(fp_ctx* ctx, int32_t sms) {
+  return fp::guarded([&]() -> int {
+    if (!ctx || sms < 0) return FP_ERR_INVALID;
+    ctx->num_sms = sms == 0 ? ctx->dev_sms : std::min(sms, ctx->dev_sms);
     return FP_OK;
   });
 }
@@ -467,8 +537,15 @@ int fp_instance_create(fp_ctx* ctx, const fp_hypergraph* h, int32_t K, int32_t m
     if (!in) return FP_ERR_NOMEM;
     made = in;
     in->ctx = ctx;
+    if (ctx->arena) {
+      // the context's arena serves one instance at a time
+      if (ctx->arena_busy) { delete in; made = nullptr; return FP_ERR_STATE; }
+      in->in_arena = true;
+      ctx->arena_busy = true;
+      ctx->arena_used = 0;
+    }
     int rc = make_problem(h, K, metric, eps_factor, in->g, in->pb);   // validates h
-    if (rc) { delete in; return rc; }
+    if (rc) { fp_instance_destroy(in); made = nullptr; return rc; }
     const HostGraph& g = in->g;
     const Problem& pb = in->pb;
 
@@ -535,10 +612,17 @@ int fp_instance_create(fp_ctx* ctx, const fp_hypergraph* h, int32_t K, int32_t m
       return rc;
     }
     void* ms = nullptr;
-    cudaError_t e = cudaMalloc(&ms, metrics_scratch_bytes(K));
-    if (e != cudaSuccess) { fp_instance_destroy(in); return cuda_status(e); }
-    in->allocs.push_back(ms);
-    in->dev_bytes += (long long)metrics_scratch_bytes(K);
+    cudaError_t e = cudaSuccess;
+    if (in->in_arena) {
+      unsigned char* q = nullptr;
+      if ((rc = dalloc(in, &q, metrics_scratch_bytes(K)))) { fp_instance_destroy(in); return rc; }
+      ms = q;
+    } else {
+      e = cudaMalloc(&ms, metrics_scratch_bytes(K));
+      if (e != cudaSuccess) { fp_instance_destroy(in); return cuda_status(e); }
+      in->allocs.push_back(ms);
+      in->dev_bytes += (long long)metrics_scratch_bytes(K);
+    }
     in->metric_scratch = ms;
     in->sb.wmax = kSpecWindow;
     in->sb.ctab_mask = ldg ? (unsigned)(ctab - 1) : 0u;
@@ -563,9 +647,13 @@ int fp_instance_create(fp_ctx* ctx, const fp_hypergraph* h, int32_t K, int32_t m
                     metric == FP_METRIC_CN ? kCnGridPins : default_super_work(metric));
       if (rc) { fp_instance_destroy(in); return rc; }
     }
-    if (cudaMallocHost(&in->h_moves, sizeof(long long) * kMaxPasses) != cudaSuccess ||
-        cudaMallocHost(&in->h_status, sizeof(int)) != cudaSuccess ||
-        cudaMallocHost(&in->h_metrics, sizeof(long long) * 8) != cudaSuccess) {
+    if (in->in_arena) {   // the context's pinned words
+      in->h_moves = ctx->h_moves;
+      in->h_status = ctx->h_status;
+      in->h_metrics = ctx->h_metrics;
+    } else if (cudaMallocHost(&in->h_moves, sizeof(long long) * kMaxPasses) != cudaSuccess ||
+               cudaMallocHost(&in->h_status, sizeof(int)) != cudaSuccess ||
+               cudaMallocHost(&in->h_metrics, sizeof(long long) * 8) != cudaSuccess) {
       fp_instance_destroy(in);
       return FP_ERR_NOMEM;
     }
@@ -653,9 +741,16 @@ int fp_instance_destroy(fp_instance* in) {
     cudaSetDevice(in->ctx->device);
     for (void* p : in->allocs) cudaFree(p);
     if (in->recs) cudaFree(in->recs);
-    if (in->h_moves) cudaFreeHost(in->h_moves);
-    if (in->h_status) cudaFreeHost(in->h_status);
-    if (in->h_metrics) cudaFreeHost(in->h_metrics);
+    if (in->in_arena) {
+      // the buffers stay in the context's arena for the next instance; its
+      // work on the context's stream is ordered after this one's
+      in->ctx->arena_busy = false;
+      in->ctx->arena_used = 0;
+    } else {
+      if (in->h_moves) cudaFreeHost(in->h_moves);
+      if (in->h_status) cudaFreeHost(in->h_status);
+      if (in->h_metrics) cudaFreeHost(in->h_metrics);
+    }
     delete in;
     return FP_OK;
   });

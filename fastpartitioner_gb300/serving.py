@@ -16,10 +16,17 @@ TV/partition.h:19, once per request).
   thread, in request order, on the engine's stream; a request's state enters
   its instance through fp_set_state, which gives the device state that
   fp_initial_partition gives.
+* run_concurrent: as run_pipelined, with several GPU slots.  A slot is an
+  engine of its own (context and stream) whose grids are sized for a share of
+  the SMs (fp_ctx_set_sm_limit) and whose instances live in a device arena
+  (fp_ctx_set_arena, no cudaMalloc / cudaFree per request, which would wait
+  for the other slots' work); one host thread per slot takes the next prepared
+  request, largest first, so small requests run on the device side by side.
 * Server: requests arrive over time (Poisson arrivals); each is admitted when
   a preparation slot is free and its device footprint (fp_instance_footprint)
   fits the device-memory budget, is prepared on the workers and refined on the
-  GPU in arrival order.  Latency is arrival to result.
+  GPU as soon as a GPU slot is free (one slot: in arrival order).  Latency is
+  arrival to result.
 
 Results do not depend on the runner: a request's part vector and metrics are
 those of the request alone.
@@ -222,6 +229,80 @@ def run_pipelined(engine, requests: list, workers: int = 8, lookahead: Optional[
     return out
 
 
+ARENA_SLACK = 1 << 16   # fp_instance_footprint + this always fits an arena (256-byte aligned buffers)
+
+
+def gpu_slots(device: int, slots: int, arena_bytes: int, sm_share: float = 0.8):
+    """`slots` engines on `device` for concurrent refinement: each sized for an
+    equal part of `sm_share` of the SMs (the grid-wide engines need all CTAs of
+    a launch resident; the concurrent grids must fit the device together), each
+    with an arena of `arena_bytes`."""
+    import torch
+    from . import Engine
+    sms = torch.cuda.get_device_properties(device).multi_processor_count
+    per = max(1, int(sms * sm_share) // slots)
+    out = []
+    for _ in range(slots):
+        e = Engine(device)
+        e.set_sm_limit(per)
+        e.set_arena(arena_bytes)
+        out.append(e)
+    return out
+
+
+def arena_for(requests: list) -> int:
+    """An arena size that fits every request of the list."""
+    need = 0
+    for r in requests:
+        hg = r.hypergraph()
+        need = max(need, footprint(hg.nov, hg.noe, hg.pins, r.K, r.metric))
+    return need + ARENA_SLACK
+
+
+def _size_key(r: Request) -> int:
+    if r.hg is not None:
+        return r.hg.pins
+    sp = r.spec
+    return sp.noe * (sp.size_lo + sp.size_hi) // 2 if sp is not None else 0
+
+
+def run_concurrent(engines: list, requests: list, workers: int = 8, lookahead: Optional[int] = None,
+                   largest_first: bool = True, clock: Callable[[], float] = time.perf_counter) -> list:
+    """Host preparation on `workers` threads, GPU work on one thread per engine
+    (gpu_slots): every slot takes the next prepared request, the largest first
+    unless told otherwise.  Results in request-id order."""
+    order = sorted(requests, key=lambda r: -_size_key(r)) if largest_first else list(requests)
+    lookahead = lookahead or 2 * max(workers, len(engines))
+    t0 = clock()
+    out = []
+    lock = threading.Lock()
+    with ThreadPoolExecutor(max_workers=workers) as ex:
+        futs = deque()
+        it = iter(order)
+        for r in it:
+            futs.append(ex.submit(_prepare, r, clock, t0))
+            if len(futs) >= lookahead:
+                break
+
+        def slot(engine):
+            mine = []
+            while True:
+                with lock:
+                    if not futs:
+                        return mine
+                    f = futs.popleft()
+                    nxt = next(it, None)
+                    if nxt is not None:
+                        futs.append(ex.submit(_prepare, nxt, clock, t0))
+                p = f.result()
+                mine.append(_refine_on_gpu(engine, p, clock, t0))
+
+        with ThreadPoolExecutor(max_workers=len(engines)) as gpu:
+            for part in gpu.map(slot, engines):
+                out.extend(part)
+    return sorted(out, key=lambda x: x.rid)
+
+
 class Server:
     """Continuous serving on one GPU.
 
@@ -245,7 +326,11 @@ class Server:
 
     def __init__(self, engine, budget_bytes: int, workers: int = 8, slots: int = 32,
                  clock: Callable[[], float] = time.perf_counter, footprint_fn=footprint):
-        self.engine = engine
+        # one engine (requests refined in admission order on the calling
+        # thread) or a list of GPU slots (gpu_slots: a prepared request goes to
+        # the next free slot, and requests overlap on the device)
+        self.engines = list(engine) if isinstance(engine, (list, tuple)) else [engine]
+        self.engine = self.engines[0]
         self.budget = int(budget_bytes)
         self.workers = workers
         self.slots = slots
@@ -290,33 +375,53 @@ class Server:
             return p, need
 
         out = []
-        with ThreadPoolExecutor(max_workers=self.workers) as ex:
+        free = deque(self.engines)   # GPU slots not refining
+        running = set()              # GPU futures
+
+        def on_gpu(engine, p, need):
+            try:
+                return _refine_on_gpu(engine, p, self.clock, t0)
+            finally:
+                p.hg = p.state = None
+                with cv:
+                    book["reserved"] -= need
+                    cv.notify_all()
+
+        def finish(fs):
+            for f in fs:
+                engine, res = f.result()
+                out.append(res)
+                free.append(engine)
+                running.discard(f)
+
+        with ThreadPoolExecutor(max_workers=self.workers) as ex, \
+                ThreadPoolExecutor(max_workers=len(self.engines)) as gpu:
             queue = deque(reqs)      # not yet admitted
             admitted = deque()       # futures, admission order
             idx = 0
-            while queue or admitted:
+            while queue or admitted or running:
+                finish([f for f in list(running) if f.done()])
                 now = self.clock() - t0
-                while queue and queue[0].arrival <= now and len(admitted) < self.slots:
+                while queue and queue[0].arrival <= now and len(admitted) + len(running) < self.slots:
                     admitted.append(ex.submit(prepare, idx, queue.popleft()))
                     idx += 1
-                    self.peak_admitted = max(self.peak_admitted, len(admitted))
-                if admitted and admitted[0].done():
+                    self.peak_admitted = max(self.peak_admitted, len(admitted) + len(running))
+                if admitted and admitted[0].done() and free:
                     p, need = admitted.popleft().result()
-                    out.append(_refine_on_gpu(self.engine, p, self.clock, t0))
-                    p.hg = p.state = None
-                    with cv:
-                        book["reserved"] -= need
-                        cv.notify_all()
+                    engine = free.popleft()
+                    running.add(gpu.submit(lambda e=engine, q=p, n=need: (e, on_gpu(e, q, n))))
                     continue
-                # wait for the head's preparation, or for the next arrival if
-                # it could be admitted now
+                # wait for the head's preparation, a GPU slot, or the next
+                # arrival if it could be admitted now
                 timeout = None
-                if queue and len(admitted) < self.slots:
+                if queue and len(admitted) + len(running) < self.slots:
                     timeout = max(0.0, queue[0].arrival - (self.clock() - t0))
-                if admitted:
-                    wait([admitted[0]], timeout=timeout)
+                pending = list(running) + ([admitted[0]] if admitted and free else [])
+                if pending:
+                    wait(pending, timeout=timeout, return_when="FIRST_COMPLETED")
                 elif timeout:
                     time.sleep(timeout)
+            finish(list(running))
         return sorted(out, key=lambda x: x.rid)
 
 

@@ -87,6 +87,30 @@ int fp_ctx_destroy(fp_ctx* ctx);
  * selects the context's own stream. */
 int fp_ctx_set_stream(fp_ctx* ctx, void* stream);
 
+/* Serving many requests (no counterpart in the reference, which makes one
+ * call per process).
+ * fp_ctx_set_arena: the context allocates `bytes` of device memory once (and
+ * a few pinned host words); its instances take their buffers from it instead
+ * of cudaMalloc, and releasing one frees nothing.  cudaMalloc and cudaFree
+ * synchronise with the whole device, so a loop that creates and releases an
+ * instance per request on one context would otherwise stall the work that
+ * other contexts (other streams) have in flight.  The arena serves one
+ * instance at a time: fp_instance_create returns FP_ERR_STATE while another
+ * instance of the context exists, FP_ERR_NOMEM if the instance does not fit
+ * (fp_instance_footprint + 64 KiB always fits: each buffer is aligned to 256
+ * bytes).  bytes = 0 releases the arena; FP_ERR_STATE while an instance holds
+ * it.
+ * fp_ctx_set_sm_limit: the refinement and metric kernels of this context size
+ * their grids for `sms` SMs (0: the whole device), so that instances of
+ * several contexts, on their own streams, run on the GPU at the same time --
+ * requests too small to fill the device otherwise leave most of it idle.  The
+ * grid-wide engines need every CTA of a launch resident at once: the grids of
+ * the contexts that run concurrently must fit the device together (their SM
+ * limits summing to at most its SM count); the engine's bounded waits turn a
+ * violation into FP_ERR_DEVICE_TIMEOUT, never a hang. */
+int fp_ctx_set_arena(fp_ctx* ctx, int64_t bytes);
+int fp_ctx_set_sm_limit(fp_ctx* ctx, int32_t sms);
+
 /* Structural check fp_instance_create applies (no device needed): consistent
  * CSRs, distinct pins per net, non-empty nets whose source is one of their
  * pins, a permutation ordering, non-negative weights summing below 2^31. */

@@ -238,3 +238,42 @@ def test_gpu_side_failure_releases_the_request():
             assert r.status == fp.ERR_INVALID and "device lost" in r.error and r.part_vec is None
         else:
             assert r.status == 0
+
+
+def test_concurrent_slots_equal_plain_one_instance_per_slot():
+    """run_concurrent: every slot (engine) makes its calls from one thread of
+    its own and holds one instance at a time; results equal the plain loop's."""
+    reqs = small_batch(30, seed=7)
+    plain = sv.run_plain(FakeEngine(), reqs)
+    engines = [FakeEngine() for _ in range(3)]
+    conc = sv.run_concurrent(engines, reqs, workers=4)
+    assert [r.rid for r in conc] == [r.rid for r in reqs]
+    for a, b in zip(plain, conc):
+        assert a.status == b.status == 0
+        np.testing.assert_array_equal(a.part_vec, b.part_vec)
+        assert a.metrics == b.metrics
+    used = [e for e in engines if e.calls]
+    assert len(used) >= 2
+    for e in used:
+        assert len({tid for _, tid in e.calls}) == 1 and e.max_alive == 1
+    assert len({e.calls[0][1] for e in used}) == len(used)   # one thread per slot
+
+
+def test_server_with_gpu_slots_keeps_budget_and_results():
+    reqs = sv.poisson_arrivals(small_batch(24, seed=9), rate=300.0, seed=3)
+    alone = {r.rid: r for r in sv.run_plain(FakeEngine(), [sv.Request(**{**q.__dict__, "arrival": 0.0})
+                                                             for q in reqs])}
+    foot = [fp.footprint(*(lambda h: (h.nov, h.noe, h.pins))(r.hypergraph()), r.K, r.metric) for r in reqs]
+    budget = 3 * max(foot)
+    engines = [FakeEngine() for _ in range(3)]
+    srv = sv.Server(engines, budget_bytes=budget, workers=4, slots=6)
+    out = srv.run(reqs)
+    assert srv.peak_reserved <= budget
+    assert [r.rid for r in out] == sorted(r.rid for r in reqs)
+    for r in out:
+        assert r.status == 0
+        np.testing.assert_array_equal(r.part_vec, alone[r.rid].part_vec)
+        assert r.metrics == alone[r.rid].metrics
+        assert r.t_arrival <= r.t_start <= r.t_done
+    for e in engines:
+        assert e.max_alive <= 1

@@ -105,14 +105,24 @@ def test_results_same_alone_and_in_the_mix(fp, gpu_engine):
     srv = sv.Server(gpu_engine, budget_bytes=budget, workers=4, slots=4)
     served = srv.run(reqs)
     assert srv.peak_reserved <= budget
-    for a, b, c in zip(alone, mixed, served):
-        assert a.rid == b.rid == c.rid
-        assert a.status == b.status == c.status, a.rid
+    # several requests on the device at once: GPU slots with SM shares and arenas
+    slots = sv.gpu_slots(0, 3, sv.arena_for(batch()))
+    try:
+        conc = sv.run_concurrent(slots, batch(), workers=4)
+        srv2 = sv.Server(slots, budget_bytes=budget, workers=4, slots=6)
+        served2 = srv2.run(sv.poisson_arrivals(batch(), rate=200.0, seed=5))
+    finally:
+        for e in slots:
+            e.close()
+    for a, b, c, d, f in zip(alone, mixed, served, conc, served2):
+        assert a.rid == b.rid == c.rid == d.rid == f.rid
+        assert a.status == b.status == c.status == d.status == f.status, (a.rid, d.error, f.error)
         if a.status:
             continue
-        assert (a.part_vec == b.part_vec).all() and (a.part_vec == c.part_vec).all(), a.rid
-        assert a.metrics == b.metrics == c.metrics, a.rid
-        assert a.device_bytes == b.device_bytes == c.device_bytes
+        for x in (b, c, d, f):
+            assert (a.part_vec == x.part_vec).all(), a.rid
+            assert a.metrics == x.metrics, a.rid
+            assert a.device_bytes == x.device_bytes
 
 
 @pytest.mark.parametrize("metric", METRICS)
