@@ -177,8 +177,9 @@ def test_bench_batch_and_serve_lines(monkeypatch, capsys):
     orig = sv.mixed_batch
     monkeypatch.setattr(sv, "mixed_batch", lambda n, seed=0, vmax=1_000_000, passes=8, **kw:
                         orig(n, seed=seed, vmin=200, vmax=4000, passes=passes, Ks=(2, 4, 8, 16, 32)))
+    monkeypatch.setattr(sv, "gpu_slots", lambda device, n, arena, **kw: [FakeEngine() for _ in range(n)])
     args = bench.argparse.Namespace(batch_n=10, batch_seed=0, batch_passes=2, workers=3, warmup=1, rate=200.0,
-                                    duration=0.05, serve_vmax=4000, budget_gb=1.0, slots=4)
+                                    duration=0.05, serve_vmax=4000, budget_gb=1.0, slots=4, gpu_slots=2)
     bench.run_batch(args)
     bench.run_serve(args)
     lines = [json.loads(x) for x in capsys.readouterr().out.strip().splitlines()]
@@ -188,6 +189,7 @@ def test_bench_batch_and_serve_lines(monkeypatch, capsys):
     assert b["config"]["plain_loop"]["completed"] == 10
     assert v["unit"] == "s" and v["higher_is_better"] is False and v["config"]["same_alone_and_in_the_mix"] is True
     assert v["config"]["served"]["requests"] == 10 and v["config"]["peak_reserved_gb"] <= 1.0
+    assert b["config"]["gpu_slots"] == 2 and v["config"]["gpu_slots"] >= 1
 
 
 class BrokenRequest(sv.Request):
