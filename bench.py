@@ -67,22 +67,28 @@ def metrics_for(w, arg):
     return w["metrics"].split(",") if "metrics" in w else list(METRICS)
 
 
-def measured_traffic(kernel, config, scale):
-    """DRAM bytes per launch of `kernel` on the full-size workload, from an ncu
-    summary under profiles/: a line `traffic: <kernel> <config> <bytes>` (the
-    capture's dram__bytes_read.sum + dram__bytes_write.sum per launch, scaled to
-    full size as that summary states).  None when absent or not full size."""
+def measured_traffic(kernel, config, scale, metrics=None):
+    """DRAM bytes per launch of `kernel` on the full-size workload, from the
+    ncu summaries under profiles/: lines `traffic: <kernel> <config> <metric>
+    <bytes>` (dram__bytes_read.sum + dram__bytes_write.sum of one captured
+    launch of that metric's instance).  The mean over `metrics` (the metrics
+    whose launches the kernel ran, one launch each per step); None when a
+    metric has no line or the run is not full size."""
     if scale != 1:
         return None
+    found = {}
     for md in sorted((ROOT / "profiles").glob("*.md")):
         for line in md.read_text().splitlines():
             f = line.strip().strip("`").split()
-            if len(f) == 4 and f[0] == "traffic:" and f[1] == kernel and f[2] == config:
+            if len(f) == 5 and f[0] == "traffic:" and f[1] == kernel and f[2] == config:
                 try:
-                    return int(float(f[3]))
+                    found[f[3]] = int(float(f[4]))
                 except ValueError:
-                    return None
-    return None
+                    pass
+    want = list(metrics) if metrics else sorted(found)
+    if not want or any(m not in found for m in want):
+        return None
+    return int(sum(found[m] for m in want) / len(want))
 
 
 def spec_for(fp, w, scale=1, unit_weights=False):
@@ -335,7 +341,7 @@ def run_ours(args):
                             "algorithmic_bytes_per_launch": int(k["bytes"] / k["launches"]),
                             "achieved_gbs": ach, "frac": ach / peak}
     dom = max(per_kernel, key=lambda n: per_kernel[n]["share"])
-    traffic = measured_traffic(dom, args.config, args.scale)
+    traffic = measured_traffic(dom, args.config, args.scale, per_kernel[dom]["metrics"])
     unique = unique_bytes(hg, w["K"])
     dom_metrics = per_kernel[dom]["metrics"]
     uniq_per_launch = sum(unique[m] * len(per_metric[m]) for m in dom_metrics) / per_kernel[dom]["launches"]
