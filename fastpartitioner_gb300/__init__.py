@@ -128,6 +128,7 @@ def lib():
             "fp_instance_device_bytes": ([vp, C.POINTER(i64)], C.c_int),
             "fp_instance_footprint": ([i32, i32, i64, i32, i32, C.POINTER(i64)], C.c_int),
             "fp_initial_partition": ([vp], C.c_int),
+            "fp_set_stream_mode": ([vp, i32, C.POINTER(i32)], C.c_int),
             "fp_refine": ([vp, i32], C.c_int),
             "fp_reset_state": ([vp], C.c_int),
             "fp_set_engine": ([vp, i32], C.c_int),
@@ -422,6 +423,21 @@ class Instance:
 
     def initial_partition(self) -> None:
         _check(lib().fp_initial_partition(self._h), "fp_initial_partition")
+
+    def set_stream(self, where: str) -> None:
+        """fp_set_stream_mode: 'auto' (the default: TV / MSV / MSRV stream on
+        the device when the instance qualifies), 'host', or 'device' (TV, MSV,
+        MSRV and CN on the device whenever the instance qualifies)."""
+        modes = {"auto": 0, "host": 1, "device": 2}
+        if where not in modes:
+            raise ValueError(f"stream must be one of {sorted(modes)}")
+        _check(lib().fp_set_stream_mode(self._h, modes[where], None), "fp_set_stream_mode")
+
+    def streamed_on_device(self) -> bool:
+        """True if the last initial_partition ran on the device."""
+        out = C.c_int32()
+        _check(lib().fp_set_stream_mode(self._h, -1, C.byref(out)), "fp_set_stream_mode")
+        return bool(out.value)
 
     def refine(self, passes: int) -> None:
         _check(lib().fp_refine(self._h, passes), "fp_refine")

@@ -24,6 +24,9 @@ cudaError_t launch_spec_msg(const DevInstance& I, const SpecBuf& B, int passes, 
 cudaError_t launch_spec_cn(const DevInstance& I, const SpecBuf& B, int passes, int num_sms, cudaStream_t st,
                            int* grid_out);
 size_t spec_ldg_smem_bytes(int K);
+size_t stream_smem_bytes(int K);
+cudaError_t launch_stream_ldg(const DevInstance& I, const SpecBuf& B, const StreamArgs& S, int num_sms,
+                              cudaStream_t st);
 size_t spec_msg_smem_bytes(int K);
 // The speculative grid-wide engine covers every metric as long as its shared
 // memory fits a CTA (per-warp K-sized arrays) and the walked positions (vertices;
@@ -129,6 +132,17 @@ struct fp_instance {
   int* porder_d = nullptr;
   int* iso_list_d = nullptr;
   int* iso_before_d = nullptr;
+  int* st_porder_d = nullptr;     // device stream positions, vertices without nets, their
+  int* st_iso_d = nullptr;        //   counts before each position, whole-grid positions,
+  int* st_before_d = nullptr;     //   last position that saw each part
+  int* st_heavy_d = nullptr;
+  int* st_mid_d = nullptr;
+  unsigned char* st_class_d = nullptr;
+  int* mark_pos_d = nullptr;
+  StreamArgs sa{};                // device stream (TV / MSV / MSRV), csrc/fp_stream.cu
+  bool stream_dev = false;        // the instance qualifies for the device stream
+  int stream_mode = 0;            // fp_set_stream_mode: 0 auto, 1 host, 2 device where it qualifies
+  bool last_stream_dev = false;   // the last fp_initial_partition ran on the device
   unsigned char* vclass_d = nullptr;
 };
 
@@ -407,6 +421,79 @@ static cudaError_t clear_spec_scratch(const SpecBuf& b, int noe, int K, cudaStre
   return e;
 }
 
+// Positions of the device stream (TV, MSV, MSRV, CN; csrc/fp_stream.cu): the
+// vertices with nets in visiting order, when every vertex without nets weighs
+// 0 (those are placed from the sizes alone), and the positions whose vertex
+// the whole grid places.  Sets stream_dev when the instance qualifies.
+static int build_stream_positions(fp_instance* in) {
+  const HostGraph& g = in->g;
+  const Problem& pb = in->pb;
+  std::vector<int> sp, siso, sbefore, heavy, mid;
+  std::vector<unsigned char> pclass;
+  bool w0 = true;
+  for (int v = 0; v < g.nov; v++)
+    if (g.vptr[v + 1] == g.vptr[v] && pb.w[v] != 0) w0 = false;
+  for (int z = 0; z < g.nov; z++) {
+    const int v = pb.order[z];
+    if (g.vptr[v + 1] == g.vptr[v]) {
+      siso.push_back(v);
+      continue;
+    }
+    // the list entries its evaluation reads at most: sum of min(|e|, K)
+    long long work = 0;
+    for (uint32_t i = g.vptr[v]; i < g.vptr[v + 1]; i++) {
+      const int e = (int)g.vnets[i];
+      work += std::min<long long>(g.nptr[e + 1] - g.nptr[e], pb.K);
+    }
+    unsigned char c = 0;
+    if (g.vptr[v + 1] - g.vptr[v] >= (uint32_t)kStreamHeavy || work >= kStreamGridWork) {
+      c = 2;
+      heavy.push_back((int)sp.size());
+    } else if (work >= kStreamCtaWork) {
+      c = 1;
+      mid.push_back((int)sp.size());
+    }
+    pclass.push_back(c);
+    sp.push_back(v);
+    sbefore.push_back((int)siso.size());
+  }
+  sbefore.push_back((int)siso.size());
+  in->stream_dev = w0 && !sp.empty() && pb.K <= kStreamMaxK &&
+                   stream_smem_bytes(pb.K) + 4096 <= (size_t)in->ctx->max_smem;
+  in->sa.porder = in->st_porder_d;
+  in->sa.npos = (int)sp.size();
+  in->sa.iso_list = in->st_iso_d;
+  in->sa.iso_before = in->st_before_d;
+  in->sa.niso = (int)siso.size();
+  in->sa.heavy_pos = in->st_heavy_d;
+  in->sa.nheavy = (int)heavy.size();
+  in->sa.mid_pos = in->st_mid_d;
+  in->sa.nmid = (int)mid.size();
+  in->sa.pclass = in->st_class_d;
+  in->sa.mark_pos = in->mark_pos_d;
+  // the slot records: CN's refinement scratch of (pin, offset) pairs is free
+  // before the first refinement
+  in->sa.rec = pb.metric == FP_METRIC_CN ? reinterpret_cast<uint32_t*>(in->sb.cn_moved) : in->sb.rec;
+  cudaStream_t s0 = in->ctx->stream;
+  cudaError_t e0 = cudaSuccess;
+  if (in->stream_dev) {
+    e0 = cudaMemcpyAsync(in->st_porder_d, sp.data(), sizeof(int) * sp.size(), cudaMemcpyHostToDevice, s0);
+    if (e0 == cudaSuccess && !siso.empty())
+      e0 = cudaMemcpyAsync(in->st_iso_d, siso.data(), sizeof(int) * siso.size(), cudaMemcpyHostToDevice, s0);
+    if (e0 == cudaSuccess)
+      e0 = cudaMemcpyAsync(in->st_before_d, sbefore.data(), sizeof(int) * sbefore.size(), cudaMemcpyHostToDevice,
+                           s0);
+    if (e0 == cudaSuccess && !heavy.empty())
+      e0 = cudaMemcpyAsync(in->st_heavy_d, heavy.data(), sizeof(int) * heavy.size(), cudaMemcpyHostToDevice, s0);
+    if (e0 == cudaSuccess && !mid.empty())
+      e0 = cudaMemcpyAsync(in->st_mid_d, mid.data(), sizeof(int) * mid.size(), cudaMemcpyHostToDevice, s0);
+    if (e0 == cudaSuccess)
+      e0 = cudaMemcpyAsync(in->st_class_d, pclass.data(), pclass.size(), cudaMemcpyHostToDevice, s0);
+    if (e0 == cudaSuccess) e0 = cudaStreamSynchronize(s0);
+  }
+  return cuda_status(e0);
+}
+
 // Positions of the LDG engine (TV / MSV / MSRV).  A vertex without nets and
 // with weight 0 reads only the part sizes and changes nothing that a later
 // decision reads; for TV, when every vertex without nets weighs 0 (vertex
@@ -607,6 +694,13 @@ int fp_instance_create(fp_ctx* ctx, const fp_hypergraph* h, int32_t K, int32_t m
         (rc = dalloc(in, &in->mid_pos_d, std::max(g.nov, g.noe))) ||
         (rc = dalloc(in, &in->porder_d, ldg ? g.nov : 1)) || (rc = dalloc(in, &in->iso_list_d, ldg ? g.nov : 1)) ||
         (rc = dalloc(in, &in->iso_before_d, ldg ? g.nov + 1 : 1)) ||
+        (rc = dalloc(in, &in->st_porder_d, ldg || cn ? g.nov : 1)) ||
+        (rc = dalloc(in, &in->st_iso_d, ldg || cn ? g.nov : 1)) ||
+        (rc = dalloc(in, &in->st_before_d, ldg || cn ? g.nov + 1 : 1)) ||
+        (rc = dalloc(in, &in->st_heavy_d, ldg || cn ? g.nov : 1)) ||
+        (rc = dalloc(in, &in->st_mid_d, ldg || cn ? g.nov : 1)) ||
+        (rc = dalloc(in, &in->st_class_d, ldg || cn ? g.nov : 1)) ||
+        (rc = dalloc(in, &in->mark_pos_d, ldg || cn ? K : 1)) ||
         (rc = dalloc(in, &in->metric_out, 8))) {
       fp_instance_destroy(in);
       return rc;
@@ -643,6 +737,7 @@ int fp_instance_create(fp_ctx* ctx, const fp_hypergraph* h, int32_t K, int32_t m
       if (e == cudaSuccess) e = cudaStreamSynchronize(s0);
       if (e != cudaSuccess) { fp_instance_destroy(in); return cuda_status(e); }
       if (ldg && (rc = build_positions(in))) { fp_instance_destroy(in); return rc; }
+      if ((ldg || cn) && (rc = build_stream_positions(in))) { fp_instance_destroy(in); return rc; }
       rc = classify(in, metric == FP_METRIC_CN ? kCnLightPins : kLightWork,
                     metric == FP_METRIC_CN ? kCnGridPins : default_super_work(metric));
       if (rc) { fp_instance_destroy(in); return rc; }
@@ -728,6 +823,10 @@ int fp_instance_footprint(int32_t nov, int32_t noe, int64_t pins, int32_t K, int
     add(16 * (size_t)kMaxGridVerts, 4); add(K, 8);           // hmisc, mlast
     add(VE, 4); add(VE, 4);                                  // heavy / medium positions
     add(ldg ? V : 1, 4); add(ldg ? V : 1, 4); add(ldg ? V + 1 : 1, 4);   // porder, iso_list, iso_before
+    add(ldg || cn ? V : 1, 4); add(ldg || cn ? V : 1, 4);   // device stream: positions, iso,
+    add(ldg || cn ? V + 1 : 1, 4); add(ldg || cn ? V : 1, 4);   //   before, whole-grid positions,
+    add(ldg || cn ? V : 1, 4); add(ldg || cn ? V : 1, 1);   //   CTA positions, classes,
+    add(ldg || cn ? (size_t)K : 1, 4);                      //   mark_pos
     add(8, 8);                                               // metric_out
     b += (long long)metrics_scratch_bytes(K);
     *bytes = b;
@@ -756,15 +855,98 @@ int fp_instance_destroy(fp_instance* in) {
   });
 }
 
+// The LDG metrics' stream on the device (csrc/fp_stream.cu); the result is
+// copied back into the host state, which fp_reset_state uploads again.
+static int device_stream(fp_instance* in) {
+  cudaSetDevice(in->ctx->device);
+  cudaStream_t s = in->ctx->stream;
+  const HostGraph& g = in->g;
+  const int K = in->pb.K;
+  DevInstance& d = in->d;
+  static const int none[8] = {0x7fffffff, 0x7fffffff, 0x7fffffff, 0x7fffffff,
+                              0x7fffffff, 0x7fffffff, 0x7fffffff, 0x7fffffff};
+  cudaError_t e = cudaMemsetAsync(d.part_vec, 0xff, sizeof(int) * g.nov, s);
+  auto zero = [&](void* p, size_t bytes, int val) {
+    if (e == cudaSuccess && bytes) e = cudaMemsetAsync(p, val, bytes, s);
+  };
+  zero(d.ep_len, sizeof(int) * g.noe, 0);
+  zero(d.ep_part, sizeof(int) * g.pins, 0xff);
+  zero(d.ep_cnt, sizeof(int) * g.pins, 0);
+  zero(d.part_sizes, sizeof(int) * K, 0);
+  zero(d.marker, sizeof(int) * K, 0xff);
+  zero(d.send, sizeof(int) * K, 0);
+  zero(d.recv, sizeof(int) * K, 0);
+  zero(d.msgs, sizeof(int) * K, 0);
+  zero(d.status, sizeof(int), 0);
+  zero(in->mark_pos_d, sizeof(int) * K, 0xff);
+  zero(in->sb.claim64, sizeof(unsigned long long) * std::max(g.noe, 1), 0);
+  zero(in->sb.bar, sizeof(unsigned) * 4, 0);
+  zero(in->sb.stats, sizeof(unsigned long long) * kNumStats, 0);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(in->sb.ctl, none, sizeof(none), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = clear_spec_scratch(in->sb, g.noe, K, s);
+  if (e == cudaSuccess) e = launch_stream_ldg(d, in->sb, in->sa, in->ctx->num_sms, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(in->h_status, d.status, sizeof(int), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_status(e);
+  if (*in->h_status) return *in->h_status;
+  HostState& st = in->st;
+  st.part_vec.resize(g.nov);
+  st.part_sizes.resize(K);
+  st.ep_start.assign(g.nptr.begin(), g.nptr.end());
+  st.ep_len.resize(g.noe);
+  st.ep_part.resize(g.pins);
+  st.ep_cnt.resize(g.pins);
+  st.marker.resize(K);
+  st.send.resize(K);
+  st.recv.resize(K);
+  st.msgs.assign(K, 0);
+  st.conn.clear();
+  auto back = [&](void* dst, const void* src, size_t bytes) {
+    if (e == cudaSuccess && bytes) e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, s);
+  };
+  back(st.part_vec.data(), d.part_vec, sizeof(int) * g.nov);
+  back(st.part_sizes.data(), d.part_sizes, sizeof(int) * K);
+  back(st.ep_len.data(), d.ep_len, sizeof(int) * g.noe);
+  back(st.ep_part.data(), d.ep_part, sizeof(int) * g.pins);
+  back(st.ep_cnt.data(), d.ep_cnt, sizeof(int) * g.pins);
+  back(st.marker.data(), d.marker, sizeof(int) * K);
+  back(st.send.data(), d.send, sizeof(int) * K);
+  back(st.recv.data(), d.recv, sizeof(int) * K);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  return cuda_status(e);
+}
+
 int fp_initial_partition(fp_instance* in) {
   return fp::guarded([&]() -> int {
     if (!in) return FP_ERR_INVALID;
+    in->has_state = false;
+    in->last_stream_dev = false;
+    // auto: the device stream where it is faster than the host's (TV, MSV,
+    // MSRV; CN's stream cuts its windows at most positions, whose fallback
+    // part moves with every placement)
+    const bool dev = in->stream_mode == 2 || (in->stream_mode == 0 && in->pb.metric != FP_METRIC_CN);
+    if (in->stream_dev && dev) {
+      const int rc = device_stream(in);
+      if (rc) return rc;
+      in->last_stream_dev = true;
+      in->has_state = true;
+      return FP_OK;
+    }
     int rc = initial_partition(in->pb, in->st);
     if (rc) return rc;
     cudaSetDevice(in->ctx->device);
     rc = upload_state(in);
     if (rc) return rc;
     in->has_state = true;
+    return FP_OK;
+  });
+}
+
+int fp_set_stream_mode(fp_instance* in, int32_t mode, int32_t* last_on_device) {
+  return fp::guarded([&]() -> int {
+    if (!in || mode < -1 || mode > 2) return FP_ERR_INVALID;
+    if (mode >= 0) in->stream_mode = mode;
+    if (last_on_device) *last_on_device = in->last_stream_dev ? 1 : 0;
     return FP_OK;
   });
 }

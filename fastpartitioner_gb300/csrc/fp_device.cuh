@@ -50,6 +50,29 @@ struct DevInstance {
   int4* recs;
 };
 
+// The device stream's inputs besides the instance and its speculation buffers
+// (csrc/fp_stream.cu).
+struct StreamArgs {
+  const int* porder;      // vertices with nets (or all vertices), visiting order
+  int npos;
+  const int* iso_list;    // vertices without nets (weight 0), visiting order
+  const int* iso_before;  // [npos + 1] vertices without nets before each position
+  int niso;
+  const int* heavy_pos;   // positions whose vertex the whole grid places, ascending
+  int nheavy;
+  const int* mid_pos;     // positions whose vertex one CTA evaluates, ascending
+  int nmid;
+  const unsigned char* pclass;   // [npos] 0 a warp evaluates, 1 a CTA, 2 the grid
+  int* mark_pos;          // [K] last position whose vertex saw the part, -1: none
+  uint32_t* rec;          // [pins] slot of the chosen part in each (vertex, net) pair
+};
+constexpr int kStreamHeavy = 4096;   // nets of a vertex the whole grid places in the device stream
+// List entries a position's evaluation may read (the sum of min(|e|, K) over
+// its nets) from which one CTA, or the whole grid, evaluates it.
+constexpr long long kStreamCtaWork = 4096;
+constexpr long long kStreamGridWork = 65536;
+constexpr int kStreamMaxK = 1024;    // shared memory of the device stream's CTAs
+
 // Round statistics kept per instance (fp_get_stats).
 constexpr int kNumStats = 48;
 

@@ -1,0 +1,662 @@
+// Streaming initial partitions on the device: the LDG streams of TV
+// (TV/partition.cpp:207-264, LDG2 without a current part), MSV
+// (MGV/partition.cpp:122-189) and MSRV (MSRV/partition.cpp:123-196), and CN's
+// stream (CN/partition.cpp:132-221).
+//
+// The reference places the vertices one by one in visiting order: a vertex
+// scores every part listed on its nets (the number of its nets listing it,
+// times 1 - size / C), takes the best (ties: the smaller part, then the part
+// seen first), or the least-loaded part when none scores, and then adds itself
+// to its nets' lists: a count increment where the part is listed, an append
+// where it is not.  CN scores only the nets with one listed part (uncut nets),
+// by that part.  A later decision reads the part sets of its nets (an
+// increment changes no score and no first sighting) and the part sizes.
+//
+// One cooperative kernel runs the stream in windows of the next positions,
+// like the refinement engine:
+//
+//   A  evaluate  every warp tallies its positions' nets against the lists at
+//                the window start, decides with the window-start sizes, finds
+//                its part's slot in each net and claims the nets it will
+//                append to (round-stamped, never cleared);
+//   B  validate  a position keeps its decision iff no earlier position of the
+//                window appends to one of its nets and the decision taken again
+//                with the exact sizes at its place (the window-start sizes plus
+//                the earlier placements) is the same;
+//   C  commit    the positions before the first invalid one are applied at
+//                once: on any net at most one of them appends (a later reader
+//                of that net is invalid), the others increment counts.
+//
+// Vertices without nets read only the sizes.  When all of them weigh 0 (vertex
+// weight = degree) they are not positions: after each window's commit they take
+// the least-loaded part of the sizes at their place.  A vertex with many nets
+// (kStreamHeavy or more) is a window of its own, evaluated and committed by the
+// whole grid.
+
+#include "fp_spec_common.cuh"
+
+namespace fp {
+
+namespace {
+
+using namespace spec;
+
+constexpr int kCN = 0;
+constexpr int kTV = 1;
+constexpr int kMSV = 4;
+constexpr int kMSRV = 5;
+
+// CN's tally of the nets [nb, min(nb + 32, deg)) of a vertex: the part of
+// every net with exactly one listed part, the number of such nets per part and
+// the first such net (CN/partition.cpp:150-170).
+__device__ __forceinline__ void tally_uncut(const DevInstance& I, uint32_t base, int nb, int deg, int* cnt,
+                                            unsigned long long* first) {
+  const int k = nb + (threadIdx.x & 31);
+  if (k >= deg) return;
+  const int e = (int)__ldg(&I.vnets[base + k]);
+  if (lds(&I.ep_len[e]) != 1) return;
+  const int p = lds(&I.ep_part[__ldg(&I.nptr[e])]);
+  if ((unsigned)p >= (unsigned)I.K) {
+    dev_fail(I.status, kDevErrInvalid);
+    return;
+  }
+  atomicAdd(&cnt[p], 1);
+  atomicMin(&first[p], (unsigned long long)k << 32);
+}
+
+// The stream's tally of nets [nb, min(nb + 32, deg)) into cnt / first.
+__device__ __forceinline__ void tally_stream(const DevInstance& I, bool cn, uint32_t base, int nb, int deg, int* cnt,
+                                             unsigned long long* first) {
+  if (cn) tally_uncut(I, base, nb, deg, cnt, first);
+  else tally_batch(I, -1, base, nb, deg, cnt, first);
+}
+
+__device__ __forceinline__ unsigned long long skey(int round, int pos) {
+  return ((unsigned long long)(unsigned)round << 32) | (0xffffffffu - (unsigned)pos);
+}
+// Did a position before `pos` of this round claim net e (it appends to it)?
+__device__ __forceinline__ bool claimed_before(const SpecBuf& B, int round, int e, int pos) {
+  const unsigned long long c = lds(&B.claim64[e]);
+  return (int)(c >> 32) == round && (int)(0xffffffffu - (unsigned)(c & 0xffffffffu)) < pos;
+}
+
+// Candidate entry: part (12 bits), nets listing it (16), first sighting: net
+// index (16) and slot (20).  Positions hold fewer than kStreamHeavy nets.
+__device__ __forceinline__ unsigned long long sc_entry(int p, int c, unsigned long long f) {
+  return ((unsigned long long)p << 52) | ((unsigned long long)c << 36) | (((f >> 32) & 0xffffull) << 20) |
+         (f & 0xfffffull);
+}
+
+// Exact LDG pick of one warp over candidate entries (part, count, first),
+// sizes sz0[p] + (dsz ? dsz[p] : 0): the best positive score, ties to the
+// smaller part, then the first seen; -1 if no part scores (TV/partition.cpp:
+// 98-117).
+__device__ int pick_entries(const DevInstance& I, const unsigned long long* cl, int nc, const int* sz0,
+                            const int* dsz) {
+  const int lane = threadIdx.x & 31;
+  LdgKey best{-1.0, 0, -1, ~0ull};
+  for (int i = lane; i < nc; i += 32) {
+    const unsigned long long ent = lds(&cl[i]);
+    const int p = (int)(ent >> 52);
+    const int c = (int)((ent >> 36) & 0xffffull);
+    const unsigned long long f = (((ent >> 20) & 0xffffull) << 32) | (ent & 0xfffffull);
+    const int sz = sz0[p] + (dsz ? dsz[p] : 0);
+    const LdgKey k{ldg_score(c, sz, I.C), sz, p, f};
+    if (ldg_better(k, best)) best = k;
+  }
+  best = warp_ldg_argmax(best);
+  return best.part;
+}
+
+// Least-loaded part of sz0 + dsz, lowest index on ties (one warp).
+__device__ int least_loaded(const int* sz0, const int* dsz, int K) {
+  const int lane = threadIdx.x & 31;
+  unsigned long long mk = ~0ull;
+  for (int p = lane; p < K; p += 32) {
+    const int sz = sz0[p] + (dsz ? dsz[p] : 0);
+    const unsigned long long key = ((unsigned long long)((unsigned)sz ^ 0x80000000u) << 32) | (unsigned)p;
+    mk = key < mk ? key : mk;
+  }
+  for (int off = 16; off; off >>= 1) {
+    const unsigned long long x = __shfl_xor_sync(kAll, mk, off);
+    mk = x < mk ? x : mk;
+  }
+  return (int)(mk & 0xffffffffu);
+}
+
+// Slot of part d in each of the nets [nb, min(nb + 32, deg)) of a vertex, -1
+// where d is not listed; lane i gets net nb + i's.  The lists' entries are
+// walked flattened across the warp, kU loads per lane in flight, as in
+// tally_batch.  sd: 32 ints of per-warp scratch.
+__device__ int locate_part(const DevInstance& I, uint32_t base, int nb, int deg, int d, int* sd) {
+  const int lane = threadIdx.x & 31;
+  const int k = nb + lane;
+  int s = 0, n = 0;
+  if (k < deg) {
+    const int e = (int)__ldg(&I.vnets[base + k]);
+    s = (int)__ldg(&I.nptr[e]);
+    const int cap = (int)__ldg(&I.nptr[e + 1]) - s;
+    n = lds(&I.ep_len[e]);
+    if (n < 0 || n > cap) { dev_fail(I.status, kDevErrInvalid); n = 0; }
+  }
+  sd[lane] = -1;
+  int incl = n;
+  for (int off = 1; off < 32; off <<= 1) {
+    const int t = __shfl_up_sync(kAll, incl, off);
+    if (lane >= off) incl += t;
+  }
+  const int total = __shfl_sync(kAll, incl, 31);
+  __syncwarp();
+  constexpr int kU = 4;
+  for (int f0 = 0; f0 < total; f0 += 32 * kU) {
+    int aa[kU], kn[kU], kj[kU];
+#pragma unroll
+    for (int u = 0; u < kU; u++) {
+      const int f = f0 + u * 32 + lane;
+      int lo = 0, hi = 31;
+#pragma unroll
+      for (int it = 0; it < 5; it++) {
+        const int mid = (lo + hi) >> 1;
+        const int val = __shfl_sync(kAll, incl, mid);
+        if (f < val) hi = mid; else lo = mid + 1;
+      }
+      const int sl = __shfl_sync(kAll, s, lo);
+      const int nl = __shfl_sync(kAll, n, lo);
+      const int il = __shfl_sync(kAll, incl, lo);
+      kn[u] = lo;
+      kj[u] = f - (il - nl);
+      aa[u] = f < total ? sl + kj[u] : -1;
+    }
+    int pp[kU];
+#pragma unroll
+    for (int u = 0; u < kU; u++) pp[u] = aa[u] >= 0 ? lds(&I.ep_part[aa[u]]) : -1;
+#pragma unroll
+    for (int u = 0; u < kU; u++)
+      if (aa[u] >= 0 && pp[u] == d) sd[kn[u]] = kj[u];   // d is listed once per net: one writer
+  }
+  __syncwarp();
+  const int j = sd[lane];
+  __syncwarp();
+  return k < deg ? j : -1;
+}
+
+// Adds one pin of part d to net e at slot `slot` (-1 / kNoSlot: append).
+__device__ __forceinline__ void place_net(const DevInstance& I, int e, int d, int slot) {
+  const int s = (int)__ldg(&I.nptr[e]);
+  if (slot >= 0 && slot != (int)kNoSlot) {
+    atomicAdd(&I.ep_cnt[s + slot], 1);
+  } else {
+    const int n = lds(&I.ep_len[e]);
+    const int cap = (int)__ldg(&I.nptr[e + 1]) - s;
+    if (n >= cap) {
+      dev_fail(I.status, kDevErrInvalid);
+      return;
+    }
+    I.ep_part[s + n] = d;
+    I.ep_cnt[s + n] = 1;
+    I.ep_len[e] = n + 1;
+  }
+}
+
+// Candidates of window offset o from a tally (cnt / first over K parts), in
+// ascending part order, and its decision with the window-start sizes (the
+// least-loaded part minpart when no part scores); writes cand, ncand, dec, wt
+// and the weight's mlist entry.  One warp; returns the decision.
+__device__ int decide_position(const DevInstance& I, const SpecBuf& B, const int* sizes_s, int minpart,
+                               const int* cnt, const unsigned long long* first, int o, int wv, int par) {
+  const int lane = threadIdx.x & 31;
+  const int K = I.K;
+  unsigned long long* cl = B.cand + (size_t)o * K;
+  int nc = 0;
+  LdgKey best{-1.0, 0, -1, ~0ull};
+  for (int p0 = 0; p0 < K; p0 += 32) {
+    const int p = p0 + lane;
+    const int c = p < K ? cnt[p] : 0;
+    const unsigned m = __ballot_sync(kAll, c > 0);
+    if (c > 0) {
+      cl[nc + __popc(m & ((1u << lane) - 1u))] = sc_entry(p, c, first[p]);
+      const LdgKey k{ldg_score(c, sizes_s[p], I.C), sizes_s[p], p, first[p]};
+      if (ldg_better(k, best)) best = k;
+    }
+    nc += __popc(m);
+  }
+  best = warp_ldg_argmax(best);
+  const int d = best.part >= 0 ? best.part : minpart;
+  if (lane == 0) {
+    B.ncand[o] = nc;
+    B.dec[o] = d;
+    B.wt[o] = wv;
+    if (wv) {
+      const int i = atomicAdd(&B.mcnt[par], 1);
+      B.mlist[i] = make_int4(o, wv, d, 0);
+    }
+  }
+  __syncwarp();
+  return d;
+}
+
+// The records of d in the nets [n0, n1) of a vertex (one warp) and the claims
+// of the nets d is appended to.
+__device__ void record_slots(const DevInstance& I, const SpecBuf& B, const StreamArgs& S, uint32_t base, int n0,
+                             int n1, int d, int round, int z, int* sd) {
+  const int lane = threadIdx.x & 31;
+  for (int nb = n0; nb < n1; nb += 32) {
+    const int j = locate_part(I, base, nb, n1, d, sd);
+    const int k = nb + lane;
+    if (k < n1) {
+      S.rec[base + k] = j >= 0 ? (uint32_t)j : kNoSlot;
+      if (j < 0) atomicMax(&B.claim64[(int)__ldg(&I.vnets[base + k])], skey(round, z));
+    }
+  }
+}
+
+// The vertices without nets [k0, k1) of the iso list take the least-loaded
+// part of sz (TV: the size of that part above max_pw would make the reference
+// use part -1: unsupported).  One warp; *amin caches the argmin (-1: stale).
+__device__ void place_iso(const DevInstance& I, const StreamArgs& S, const int* sz, int k0, int k1, int* amin) {
+  if (k0 >= k1) return;
+  const int lane = threadIdx.x & 31;
+  if (*amin < 0) *amin = least_loaded(sz, nullptr, I.K);
+  const int d = *amin;
+  if (I.metric == kTV && sz[d] > I.max_pw) {
+    if (lane == 0) dev_fail(I.status, kDevErrUnsupported);
+    return;
+  }
+  for (int k = k0 + lane; k < k1; k += 32) I.part_vec[__ldg(&S.iso_list[k])] = d;
+}
+
+__global__ void __launch_bounds__(kSThreads, 1) stream_ldg_kernel(DevInstance I, SpecBuf B, StreamArgs S) {
+  barrier_start();
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ unsigned long long uscr[kSWarps];
+  __shared__ int s_minpart, s_minsize, s_second, s_dec;
+  const int K = I.K;
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const int gw = blockIdx.x * kSWarps + wib;
+  const int nwarps = gridDim.x * kSWarps;
+  const int gtid = blockIdx.x * blockDim.x + threadIdx.x, gthreads = gridDim.x * blockDim.x;
+  const bool tv = I.metric == kTV;
+  const bool cn = I.metric == kCN;   // no marker and no TV clamp
+  Carve cv{smem_raw};
+  int* sizes_s = cv.take<int>(K);
+  int* dsz_cta = cv.take<int>(K);
+  int* cnt_b = cv.take<int>((size_t)K * kSWarps);
+  unsigned long long* first_b = cv.take<unsigned long long>((size_t)K * kSWarps);
+  int* sd_b = cv.take<int>(32 * kSWarps);
+  int* cnt = cnt_b + (size_t)wib * K;
+  unsigned long long* first = first_b + (size_t)wib * K;
+  int* sd = sd_b + 32 * wib;
+  const bool stats = blockIdx.x == 0 && threadIdx.x == 0;
+  unsigned long long t0 = stats ? gtimer() : 0ull;
+  auto lap = [&](int slot) {   // block 0's time since the last lap into stats[slot]
+    if (stats) {
+      const unsigned long long t = gtimer();
+      B.stats[slot] += t - t0;
+      t0 = t;
+    }
+  };
+
+  int pos = 0, round = 1, hidx = 0;
+  int W = min(nwarps, B.wmax);
+  while (pos < S.npos) {
+    const int par = round & 1;
+    // ------------------------------------------------------------ round state
+    for (int p = threadIdx.x; p < K; p += blockDim.x) sizes_s[p] = lds(&I.part_sizes[p]);
+    __syncthreads();
+    block_min_part(sizes_s, K, uscr, &s_minpart, &s_minsize, &s_second);
+    __syncthreads();
+    while (hidx < S.nheavy && __ldg(&S.heavy_pos[hidx]) < pos) hidx++;
+    if (hidx < S.nheavy && __ldg(&S.heavy_pos[hidx]) == pos) {
+      // ================================================ a vertex with many nets
+      const int v = __ldg(&S.porder[pos]);
+      const uint32_t base = __ldg(&I.vptr[v]);
+      const int deg = (int)(__ldg(&I.vptr[v + 1]) - base);
+      for (int p = lane; p < K; p += 32) { cnt[p] = 0; first[p] = ~0ull; }
+      __syncwarp();
+      {
+        int n0, n1;
+        net_range(deg, gw, nwarps, &n0, &n1);
+        for (int nb = n0; nb < n1; nb += 32) tally_stream(I, cn, base, nb, n1, cnt, first);
+      }
+      __syncthreads();
+      for (int p = threadIdx.x; p < K; p += blockDim.x) {
+        int c = 0;
+        unsigned long long f = ~0ull;
+        for (int x = 0; x < kSWarps; x++) {
+          c += cnt_b[(size_t)x * K + p];
+          const unsigned long long fx = first_b[(size_t)x * K + p];
+          f = fx < f ? fx : f;
+        }
+        if (c) {
+          atomicAdd(&B.hcnt[p], c);
+          atomicMin(&B.hfirst[p], f);
+        }
+      }
+      if (!grid_barrier(B.bar, I.status)) return;
+      if (blockIdx.x == 0) {
+        if (wib == 0) {
+          LdgKey best{-1.0, 0, -1, ~0ull};
+          for (int p = lane; p < K; p += 32) {
+            const int c = lds(&B.hcnt[p]);
+            if (c <= 0) continue;
+            const LdgKey k{ldg_score(c, sizes_s[p], I.C), sizes_s[p], p, lds(&B.hfirst[p])};
+            if (ldg_better(k, best)) best = k;
+          }
+          best = warp_ldg_argmax(best);
+          const int d = best.part >= 0 ? best.part : s_minpart;
+          if (lane == 0) {
+            if (tv && sizes_s[d] > I.max_pw) dev_fail(I.status, kDevErrUnsupported);
+            B.dec[0] = d;
+          }
+        }
+        if (!cn)
+          for (int p = threadIdx.x; p < K; p += blockDim.x)
+            if (lds(&B.hcnt[p]) > 0) atomicMax(&S.mark_pos[p], pos);
+      }
+      if (!grid_barrier(B.bar, I.status)) return;
+      const int d = lds(&B.dec[0]);
+      const int wv = __ldg(&I.w[v]);
+      {
+        int n0, n1;
+        net_range(deg, gw, nwarps, &n0, &n1);
+        for (int nb = n0; nb < n1; nb += 32) {
+          const int j = locate_part(I, base, nb, n1, d, sd);
+          if (nb + lane < n1) place_net(I, (int)__ldg(&I.vnets[base + nb + lane]), d, j);
+        }
+      }
+      if (gtid == 0) {
+        I.part_vec[v] = d;
+        if (wv) atomicAdd(&I.part_sizes[d], wv);
+      }
+      if (S.niso && gw == 0) {
+        // the vertices without nets before and after this one
+        int* sz = cnt;
+        for (int p = lane; p < K; p += 32) sz[p] = sizes_s[p];
+        __syncwarp();
+        int amin = -1;
+        if (pos == 0) place_iso(I, S, sz, 0, __ldg(&S.iso_before[0]), &amin);
+        __syncwarp();
+        if (lane == 0) sz[d] += wv;
+        __syncwarp();
+        amin = wv ? -1 : amin;
+        place_iso(I, S, sz, __ldg(&S.iso_before[pos]), __ldg(&S.iso_before[pos + 1]), &amin);
+      }
+      for (int p = gtid; p < K; p += gthreads) {
+        B.hcnt[p] = 0;
+        B.hfirst[p] = ~0ull;
+      }
+      if (gtid == 0) {   // the next round's cut word and placements, as a window leaves them
+        B.ctl[4 + (par ^ 1)] = kNone;
+        B.mcnt[par ^ 1] = 0;
+      }
+      pos++;
+      round++;
+      if (!grid_barrier(B.bar, I.status)) return;
+      if (stats) B.stats[1]++;
+      lap(19);
+      continue;
+    }
+
+    // ================================================================= window
+    int end_w = min(pos + W, S.npos);
+    if (hidx < S.nheavy) end_w = min(end_w, (int)__ldg(&S.heavy_pos[hidx]));
+    const int span = end_w - pos;
+    const int q = (span + nwarps - 1) / nwarps;
+    const int z0 = min(pos + gw * q, end_w);
+    const int z1 = min(z0 + q, end_w);
+    // ---- A: evaluate: light positions by their warps, medium positions by
+    // CTAs from the end of the grid
+    for (int z = z0; z < z1; z++) {
+      if (__ldg(&S.pclass[z]) != 0) continue;
+      const int o = z - pos;
+      const int v = __ldg(&S.porder[z]);
+      const uint32_t base = __ldg(&I.vptr[v]);
+      const int deg = (int)(__ldg(&I.vptr[v + 1]) - base);
+      for (int p = lane; p < K; p += 32) { cnt[p] = 0; first[p] = ~0ull; }
+      __syncwarp();
+      for (int nb = 0; nb < deg; nb += 32) tally_stream(I, cn, base, nb, deg, cnt, first);
+      __syncwarp();
+      const int d = decide_position(I, B, sizes_s, s_minpart, cnt, first, o, __ldg(&I.w[v]), par);
+      record_slots(I, B, S, base, 0, deg, d, round, z, sd);
+      __syncwarp();
+    }
+    if (S.nmid) {
+      const int i0 = lower_bound_pos(S.mid_pos, S.nmid, pos);
+      const int i1 = lower_bound_pos(S.mid_pos, S.nmid, end_w);
+      for (int i = i0 + (int)(gridDim.x - 1 - blockIdx.x); i < i1; i += gridDim.x) {
+        const int z = __ldg(&S.mid_pos[i]);
+        const int o = z - pos;
+        const int v = __ldg(&S.porder[z]);
+        const uint32_t base = __ldg(&I.vptr[v]);
+        const int deg = (int)(__ldg(&I.vptr[v + 1]) - base);
+        int n0, n1;
+        net_range(deg, wib, kSWarps, &n0, &n1);
+        __syncthreads();   // the tallies of the CTA's previous position are read
+        for (int p = lane; p < K; p += 32) { cnt[p] = 0; first[p] = ~0ull; }
+        __syncwarp();
+        for (int nb = n0; nb < n1; nb += 32) tally_stream(I, cn, base, nb, n1, cnt, first);
+        __syncthreads();
+        for (int p = threadIdx.x; p < K; p += blockDim.x) {   // warp 0's arrays hold the sums
+          int c = 0;
+          unsigned long long f = ~0ull;
+          for (int x = 0; x < kSWarps; x++) {
+            c += cnt_b[(size_t)x * K + p];
+            const unsigned long long fx = first_b[(size_t)x * K + p];
+            f = fx < f ? fx : f;
+          }
+          cnt_b[p] = c;
+          first_b[p] = f;
+        }
+        __syncthreads();
+        if (wib == 0) {
+          const int d = decide_position(I, B, sizes_s, s_minpart, cnt_b, first_b, o, __ldg(&I.w[v]), par);
+          if (lane == 0) s_dec = d;
+        }
+        __syncthreads();
+        record_slots(I, B, S, base, n0, n1, s_dec, round, z, sd);
+      }
+    }
+    if (!grid_barrier(B.bar, I.status)) return;
+    lap(16);
+    // ---- B: validate
+    int* const cut_w = &B.ctl[4 + par];
+    {
+      const int cz0 = min(pos + blockIdx.x * kSWarps * q, end_w);
+      const int cta_o0 = cz0 - pos;
+      for (int p = threadIdx.x; p < K; p += blockDim.x) dsz_cta[p] = 0;
+      __syncthreads();
+      const int nm = lds(&B.mcnt[par]);
+      for (int i = threadIdx.x; i < nm; i += blockDim.x) {
+        const int4 m = lds(&B.mlist[i]);
+        if (m.x < cta_o0) atomicAdd(&dsz_cta[m.z], m.y);
+      }
+      __syncthreads();
+      for (int z = z0; z < z1; z++) {
+        const int o = z - pos;
+        const int v = __ldg(&S.porder[z]);
+        const uint32_t base = __ldg(&I.vptr[v]);
+        const int deg = (int)(__ldg(&I.vptr[v + 1]) - base);
+        bool conf = false;
+        for (int k = lane; k < deg && !conf; k += 32)
+          conf = claimed_before(B, round, (int)__ldg(&I.vnets[base + k]), z);
+        int why = __any_sync(kAll, conf) ? 5 : 0;
+        if (!why) {
+          // the exact sizes here: the window-start sizes, the placements before
+          // this CTA's positions, those of this CTA's positions before z
+          int* dsz = cnt;
+          for (int p = lane; p < K; p += 32) dsz[p] = dsz_cta[p];
+          __syncwarp();
+          for (int o2 = cta_o0 + lane; o2 < o; o2 += 32) {
+            const int w = lds(&B.wt[o2]);
+            if (w) atomicAdd(&dsz[lds(&B.dec[o2])], w);
+          }
+          __syncwarp();
+          int d2 = pick_entries(I, B.cand + (size_t)o * K, lds(&B.ncand[o]), sizes_s, dsz);
+          if (d2 < 0) d2 = least_loaded(sizes_s, dsz, K);
+          if (d2 != lds(&B.dec[o])) {
+            why = 2;   // a size flip: the window commits this position with d2 as its last
+            if (lane == 0) B.dfix[o] = d2;
+          }
+          if (tv && sizes_s[d2] + dsz[d2] > I.max_pw) why = 7;   // unsupported, reported at commit
+          __syncwarp();
+        }
+        if (why) {
+          if (lane == 0) atomicMin(cut_w, (z << 3) | why);
+          break;
+        }
+      }
+    }
+    if (!grid_barrier(B.bar, I.status)) return;
+    lap(17);
+    const int cutw = lds(cut_w);
+    int cut = cutw == kNone ? end_w : min(cutw >> 3, end_w);
+    // a size flip at the cut: its lists are exact (no earlier append to its
+    // nets), so it commits with its exact decision after the others
+    const bool flip = cutw != kNone && (cutw & 7) == 2;
+    const int cutc = flip ? cut + 1 : cut;
+    if (cutw != kNone && (cutw & 7) == 7 && (cutw >> 3) == pos) {
+      // the window's first position needs a part above max_pw: the reference
+      // would place it in part -1
+      if (gtid == 0) dev_fail(I.status, kDevErrUnsupported);
+      return;
+    }
+    if (cut <= pos) {
+      if (gtid == 0) dev_fail(I.status, kDevErrInvalid);
+      return;
+    }
+    // ---- C: commit the positions before the cut (and a flip at the cut)
+    for (int z = z0; z < min(z1, cutc); z++) {
+      const int o = z - pos;
+      const int v = __ldg(&S.porder[z]);
+      const uint32_t base = __ldg(&I.vptr[v]);
+      const int deg = (int)(__ldg(&I.vptr[v + 1]) - base);
+      const int d = z == cut ? lds(&B.dfix[o]) : lds(&B.dec[o]);
+      if (z == cut) {
+        for (int nb = 0; nb < deg; nb += 32) {
+          const int j = locate_part(I, base, nb, deg, d, sd);
+          if (nb + lane < deg) place_net(I, (int)__ldg(&I.vnets[base + nb + lane]), d, j);
+        }
+      } else {
+        for (int k = lane; k < deg; k += 32)
+          place_net(I, (int)__ldg(&I.vnets[base + k]), d, (int)lds(&S.rec[base + k]));
+      }
+      if (!cn) {
+        const unsigned long long* cl = B.cand + (size_t)o * K;
+        const int nc = lds(&B.ncand[o]);
+        for (int i = lane; i < nc; i += 32) atomicMax(&S.mark_pos[(int)(lds(&cl[i]) >> 52)], z);
+      }
+      if (lane == 0) {
+        I.part_vec[v] = d;
+        const int wv = lds(&B.wt[o]);
+        if (wv) atomicAdd(&I.part_sizes[d], wv);
+      }
+    }
+    if (S.niso) {
+      // the vertices without nets between the committed positions: the
+      // least-loaded part of the exact sizes at their place
+      const int zb = min(z1, cutc);
+      if (z0 < zb || (pos == 0 && gw == 0)) {
+        const int cta_o0 = min(pos + blockIdx.x * kSWarps * q, end_w) - pos;
+        int* sz = cnt;
+        for (int p = lane; p < K; p += 32) sz[p] = sizes_s[p] + dsz_cta[p];
+        __syncwarp();
+        for (int o2 = cta_o0 + lane; o2 < z0 - pos; o2 += 32) {
+          const int w = lds(&B.wt[o2]);
+          if (w) atomicAdd(&sz[lds(&B.dec[o2])], w);
+        }
+        __syncwarp();
+        int amin = -1;
+        if (pos == 0 && gw == 0) place_iso(I, S, sz, 0, __ldg(&S.iso_before[0]), &amin);
+        for (int z = z0; z < zb; z++) {
+          const int o = z - pos;
+          const int w = lds(&B.wt[o]);
+          if (w) {
+            __syncwarp();
+            if (lane == 0) sz[z == cut ? lds(&B.dfix[o]) : lds(&B.dec[o])] += w;
+            __syncwarp();
+            amin = -1;
+          }
+          place_iso(I, S, sz, __ldg(&S.iso_before[z]), __ldg(&S.iso_before[z + 1]), &amin);
+        }
+      }
+    }
+    if (gw == 0 && lane == 0) {
+      B.ctl[4 + (par ^ 1)] = kNone;
+      B.mcnt[par ^ 1] = 0;
+    }
+    if (stats) {
+      B.stats[0]++;
+      B.stats[2] += cutc - pos;
+      if (cutw != kNone) B.stats[(cutw & 7) == 2 ? 5 : 8]++;
+    }
+    if (cutc >= end_w) {
+      if (end_w == pos + W) W = min(2 * W, B.wmax);
+    } else {
+      W = max(256, min(B.wmax, 2 * (cutc - pos)));
+    }
+    pos = cutc;
+    round++;
+    if (!grid_barrier(B.bar, I.status)) return;
+    lap(18);
+  }
+  // TV's marker: the last vertex that saw each part (TV/partition.cpp:218-226)
+  if (blockIdx.x == 0 && !cn)
+    for (int p = threadIdx.x; p < K; p += blockDim.x) {
+      const int z = lds(&S.mark_pos[p]);
+      I.marker[p] = z >= 0 ? __ldg(&S.porder[z]) : -1;
+    }
+}
+
+// Send (and, MSRV, received) volumes of the streamed lists: the source's part
+// sends to every other listed part (MGV/partition.cpp:159-184).
+// Nothing is counted after a failed stream (its part vector is incomplete).
+__global__ void stream_volumes_kernel(DevInstance I, int rv) {
+  if (*I.status != 0) return;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < I.noe; e += gridDim.x * blockDim.x) {
+    const int sp = I.part_vec[__ldg(&I.src[e])];
+    if ((unsigned)sp >= (unsigned)I.K) continue;
+    const int s = (int)__ldg(&I.nptr[e]);
+    const int n = I.ep_len[e];
+    for (int j = 0; j < n; j++) {
+      const int p = I.ep_part[s + j];
+      if (p == sp || (unsigned)p >= (unsigned)I.K) continue;
+      atomicAdd(&I.send[sp], 1);
+      if (rv) atomicAdd(&I.recv[p], 1);
+    }
+  }
+}
+
+}  // namespace
+
+size_t stream_smem_bytes(int K) {
+  auto a = [](size_t n) { return (n + 15) & ~size_t(15); };
+  return 2 * a(sizeof(int) * K) + a(sizeof(int) * (size_t)K * kSWarps) +
+         a(sizeof(unsigned long long) * (size_t)K * kSWarps) + a(sizeof(int) * 32 * kSWarps);
+}
+
+cudaError_t launch_stream_ldg(const DevInstance& I, const SpecBuf& B, const StreamArgs& S, int num_sms,
+                              cudaStream_t st) {
+  const size_t smem = stream_smem_bytes(I.K);
+  const void* fn = (const void*)stream_ldg_kernel;
+  cudaError_t err = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (err != cudaSuccess) return err;
+  int per_sm = 0;
+  err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kSThreads, smem);
+  if (err != cudaSuccess) return err;
+  if (per_sm < 1) return cudaErrorInvalidConfiguration;
+  int grid = per_sm * num_sms;
+  if (grid * kSWarps > B.max_warps) grid = B.max_warps / kSWarps;
+  DevInstance Ic = I;
+  SpecBuf Bc = B;
+  StreamArgs Sc = S;
+  void* args[] = {&Ic, &Bc, &Sc};
+  err = cudaLaunchCooperativeKernel(fn, grid, kSThreads, args, smem, st);
+  if (err != cudaSuccess) return err;
+  if (I.metric == kMSV || I.metric == kMSRV) {
+    stream_volumes_kernel<<<num_sms * 4, 256, 0, st>>>(I, I.metric == kMSRV ? 1 : 0);
+    err = cudaGetLastError();
+  }
+  return err;
+}
+
+}  // namespace fp

@@ -131,12 +131,26 @@ int fp_instance_destroy(fp_instance* inst);
 int fp_instance_device_bytes(fp_instance* inst, int64_t* bytes);
 int fp_instance_footprint(int32_t nov, int32_t noe, int64_t pins, int32_t K, int32_t metric, int64_t* bytes);
 
-/* Streaming initial partition of the metric (host, vertex order), uploaded as
- * the refinement state: part vector, per-net ordered part lists, part sizes and
+/* Streaming initial partition of the metric in vertex order, kept as the
+ * refinement state: part vector, per-net ordered part lists, part sizes and
  * the metric's auxiliary state (TV marker, MSV/MSRV volumes, TM/MSM K x K
  * connection counts).  Replaces the initial stream inside partition_gpu(),
- * e.g. TV/partition.cpp:1035-1092. */
+ * e.g. TV/partition.cpp:1035-1092.  The TV, MSV, MSRV and CN streams can run
+ * on the device when every vertex without nets weighs 0 (vertex weight =
+ * degree) and K <= 1024 (fp_set_stream_mode); the other cases, and TM / MSM,
+ * stream on the host and upload.  Both give the same state (the host stream's
+ * result is bit for bit the reference's); the device result is copied back to
+ * the host for fp_reset_state. */
 int fp_initial_partition(fp_instance* inst);
+
+/* Where fp_initial_partition streams: mode 0 (the default) on the device for
+ * TV, MSV and MSRV when the instance qualifies, where it is faster than the
+ * host; 1 always on the host; 2 on the device for TV, MSV, MSRV and CN
+ * whenever the instance qualifies; -1 leaves the mode as it is.
+ * *last_on_device (if not NULL) is set to 1 if the last fp_initial_partition
+ * ran on the device.  No counterpart in the reference (its stream is CPU
+ * code). */
+int fp_set_stream_mode(fp_instance* inst, int32_t mode, int32_t* last_on_device);
 
 /* Copies the host-side result of the last fp_initial_partition to the device
  * again (host -> device), discarding device-side refinement: the upload leg of
