@@ -151,6 +151,9 @@ def lib():
             "fp_graph_from_vertices": ([i32, i32, vp, vp, vp, pp], C.c_int),
             "fp_read_patohlike": ([C.c_char_p, i32, i32, pp], C.c_int),
             "fp_thin_nets": ([C.POINTER(_Hypergraph), i32, i32, pp], C.c_int),
+            "fp_create_inverse": ([vp, i32, i32, i64, vp, vp, vp, vp], C.c_int),
+            "fp_thin_nets_device": ([vp, C.POINTER(_Hypergraph), i32, i32, pp], C.c_int),
+            "fp_bfs_order_device": ([vp, C.POINTER(_Hypergraph), i32, vp, vp], C.c_int),
             "fp_write_patohlike": ([vp, C.c_char_p], C.c_int),
             "fp_graph_view": ([vp, C.POINTER(_Hypergraph)], C.c_int),
             "fp_graph_destroy": ([vp], C.c_int),
@@ -389,6 +392,37 @@ class Engine:
 
     def instance(self, hg: Hypergraph, K: int, metric, eps_factor: float = 1.05) -> "Instance":
         return Instance(self, hg, K, metric_id(metric), eps_factor)
+
+    def create_inverse(self, nov: int, noe: int, row_ptr, col_ind):
+        """fp_create_inverse on this engine's GPU: the net -> pins CSR
+        (row_ptr_inv, col_ind_inv) of a vertex -> nets CSR, pins ascending per
+        net (the reference's createInverse)."""
+        row_ptr = np.ascontiguousarray(row_ptr, dtype=np.uint32)
+        col_ind = np.ascontiguousarray(col_ind, dtype=np.uint32)
+        pins = int(row_ptr[-1]) if len(row_ptr) else 0
+        rp = np.empty(noe + 1, np.uint32)
+        ci = np.empty(max(pins, 1), np.uint32)
+        _check(lib().fp_create_inverse(self._ctx, int(nov), int(noe), pins, _ptr(row_ptr), _ptr(col_ind), _ptr(rp),
+                                       _ptr(ci)), "fp_create_inverse")
+        return rp, ci[:pins]
+
+    def thin(self, hg: Hypergraph, mean_factor: int, min_pins: int) -> Hypergraph:
+        """fp_thin_nets_device: Hypergraph.thin on this engine's GPU."""
+        g = C.c_void_p()
+        v = hg.view()
+        _check(lib().fp_thin_nets_device(self._ctx, C.byref(v), int(mean_factor), int(min_pins), C.byref(g)),
+               "fp_thin_nets_device")
+        return _take_graph(g)
+
+    def bfs_order(self, hg: Hypergraph, start: int, far: Optional[np.ndarray] = None) -> np.ndarray:
+        """fp_bfs_order_device: Hypergraph.bfs_order on this engine's GPU; the
+        two farthest vertices into `far` (2 int32) if given."""
+        out = np.empty(hg.nov, np.int32)
+        f = np.empty(2, np.int32) if far is None else far
+        v = hg.view()
+        _check(lib().fp_bfs_order_device(self._ctx, C.byref(v), int(start), _ptr(out), _ptr(f)),
+               "fp_bfs_order_device")
+        return out
 
     def close(self):
         if self._ctx:

@@ -12,6 +12,7 @@
 #include <new>
 #include <vector>
 #include <algorithm>
+#include <memory>
 
 namespace fp {
 size_t refine_smem_bytes(int metric, int K);
@@ -28,6 +29,12 @@ size_t stream_smem_bytes(int K);
 cudaError_t launch_stream_ldg(const DevInstance& I, const SpecBuf& B, const StreamArgs& S, int num_sms,
                               cudaStream_t st);
 size_t spec_msg_smem_bytes(int K);
+int create_inverse_device(int device, cudaStream_t st, int num_sms, int nov, int noe, long long pins,
+                          const uint32_t* vptr_h, const uint32_t* vnets_h, uint32_t* nptr_h, uint32_t* npins_h);
+int thin_nets_device(int device, cudaStream_t st, int num_sms, const fp_hypergraph* h, double size_lim,
+                     int thin_min, HostGraph& out);
+int bfs_order_device(int device, cudaStream_t st, int num_sms, const fp_hypergraph* h, int start, int* ordering,
+                     int* far_out);
 // The speculative grid-wide engine covers every metric as long as its shared
 // memory fits a CTA (per-warp K-sized arrays) and the walked positions (vertices;
 // nets for CN) stay below 2^28, the range of its cut words (position << 3 |
@@ -1188,6 +1195,42 @@ int fp_get_moves(fp_instance* in, int64_t* moves, int32_t n) {
     if (!in || !moves || n < 0) return FP_ERR_INVALID;
     for (int i = 0; i < n; i++) moves[i] = i < in->last_passes ? in->h_moves[i] : 0;
     return FP_OK;
+  });
+}
+
+int fp_create_inverse(fp_ctx* ctx, int32_t nov, int32_t noe, int64_t pins, const uint32_t* row_ptr,
+                      const uint32_t* col_ind, uint32_t* row_ptr_inv, uint32_t* col_ind_inv) {
+  return fp::guarded([&]() -> int {
+    if (!ctx) return FP_ERR_INVALID;
+    return create_inverse_device(ctx->device, ctx->stream, ctx->num_sms, nov, noe, pins, row_ptr, col_ind,
+                                 row_ptr_inv, col_ind_inv);
+  });
+}
+
+int fp_thin_nets_device(fp_ctx* ctx, const fp_hypergraph* h, int32_t thin_mean, int32_t thin_min, fp_graph** out) {
+  return fp::guarded([&]() -> int {
+    if (!ctx || !h || !out) return FP_ERR_INVALID;
+    *out = nullptr;
+    const int rc = validate(h);
+    if (rc) return rc;
+    // the driver's bound: thin_mean x (pins / (noe + .0f)), in float, then double
+    const double mean = h->noe > 0 ? (double)((float)h->pins / ((float)h->noe + 0.0f)) : 0.0;
+    std::unique_ptr<fp_graph> gg(new (std::nothrow) fp_graph);
+    if (!gg) return FP_ERR_NOMEM;
+    const int r = thin_nets_device(ctx->device, ctx->stream, ctx->num_sms, h, thin_mean * mean, thin_min, gg->g);
+    if (r) return r;
+    *out = gg.release();
+    return FP_OK;
+  });
+}
+
+int fp_bfs_order_device(fp_ctx* ctx, const fp_hypergraph* h, int32_t start, int32_t* ordering, int32_t* far_out) {
+  return fp::guarded([&]() -> int {
+    if (!ctx || !h || !ordering) return FP_ERR_INVALID;
+    const int rc = validate(h);
+    if (rc) return rc;
+    if (start < 0 || start >= h->nov) return FP_ERR_INVALID;
+    return bfs_order_device(ctx->device, ctx->stream, ctx->num_sms, h, start, ordering, far_out);
   });
 }
 

@@ -337,6 +337,26 @@ int fp_read_patohlike(const char* path, int32_t transpose, int32_t write_cache, 
  * (thin_partition, CN/partition.cpp:841-1196, is partition() writing into the
  * caller's part vector) and evaluates the six metrics on the full one. */
 int fp_thin_nets(const fp_hypergraph* h, int32_t thin_mean, int32_t thin_min, fp_graph** out);
+
+/* The same three hypergraph transforms on the context's GPU (csrc/fp_ingest.cu),
+ * with results equal to the host forms' bit for bit:
+ *
+ * fp_create_inverse: the reference's createInverse (shared/utils.cpp:32-56)
+ * with caller-owned host arrays -- from the vertex -> nets CSR (row_ptr[nov+1],
+ * col_ind[pins]) the net -> pins CSR (row_ptr_inv[noe+1], col_ind_inv[pins]),
+ * each net's pins in ascending vertex id.  The per-net counts the reference
+ * takes (net_appearence) are counted on the device.  FP_ERR_INVALID if
+ * row_ptr is not a CSR of `pins` entries or a net id is not below noe.
+ *
+ * fp_thin_nets_device: fp_thin_nets (CN/cn.cpp:201-268) on the device.
+ *
+ * fp_bfs_order_device: fp_bfs_order (shared/utils.cpp:433-536) on the device:
+ * the same three searches, the same ordering and farthest vertices, the same
+ * FP_ERR_UNSUPPORTED when a vertex is not reached. */
+int fp_create_inverse(fp_ctx* ctx, int32_t nov, int32_t noe, int64_t pins, const uint32_t* row_ptr,
+                      const uint32_t* col_ind, uint32_t* row_ptr_inv, uint32_t* col_ind_inv);
+int fp_thin_nets_device(fp_ctx* ctx, const fp_hypergraph* h, int32_t thin_mean, int32_t thin_min, fp_graph** out);
+int fp_bfs_order_device(fp_ctx* ctx, const fp_hypergraph* h, int32_t start, int32_t* ordering, int32_t* far_out);
 int fp_write_patohlike(const fp_graph* g, const char* path);
 int fp_graph_view(const fp_graph* g, fp_hypergraph* view);
 int fp_graph_destroy(fp_graph* g);
