@@ -28,6 +28,9 @@ size_t spec_ldg_smem_bytes(int K);
 size_t stream_smem_bytes(int K);
 cudaError_t launch_stream_ldg(const DevInstance& I, const SpecBuf& B, const StreamArgs& S, int num_sms,
                               cudaStream_t st);
+size_t stream_msg_smem_bytes(int K);
+cudaError_t launch_stream_msg(const DevInstance& I, const SpecBuf& B, const StreamArgs& S, int num_sms,
+                              cudaStream_t st);
 size_t spec_msg_smem_bytes(int K);
 int create_inverse_device(int device, cudaStream_t st, int num_sms, int nov, int noe, long long pins,
                           const uint32_t* vptr_h, const uint32_t* vnets_h, uint32_t* nptr_h, uint32_t* npins_h);
@@ -145,6 +148,15 @@ struct fp_instance {
   int* st_heavy_d = nullptr;
   int* st_mid_d = nullptr;
   unsigned char* st_class_d = nullptr;
+  uint32_t* st_rec_d = nullptr;   // TM / MSM stream: (vertex, net) records
+  uint32_t* st_prow_d = nullptr;  //   conn > 0 by row and by column
+  uint32_t* st_pcol_d = nullptr;
+  int* st_rowpos_d = nullptr;     //   first positions per row / column
+  int* st_colpos_d = nullptr;
+  int* st_saved_d = nullptr;      //   messages saved per part, per window offset
+  uint32_t* st_actm_d = nullptr;  //   active / own-net part masks per window offset
+  uint32_t* st_ownm_d = nullptr;
+  int st_msg_wmax = 0;
   int* mark_pos_d = nullptr;
   StreamArgs sa{};                // device stream (TV / MSV / MSRV), csrc/fp_stream.cu
   bool stream_dev = false;        // the instance qualifies for the device stream
@@ -158,6 +170,9 @@ namespace {
 const int kMaxPasses = 4096;
 const int kSpecWindow = 16384;   // longest speculative window (vertices)
 const int kMsgWindow = 65536;    // longest TM / MSM window
+// Longest window of the TM / MSM device stream: its saved-message rows take K
+// ints per window offset.
+static int msg_stream_window(int nov) { return std::min(kSpecWindow, std::max(256, nov)); }
 
 int cuda_status(cudaError_t e) {
   if (e == cudaSuccess) return FP_OK;
@@ -437,6 +452,9 @@ static int build_stream_positions(fp_instance* in) {
   const Problem& pb = in->pb;
   std::vector<int> sp, siso, sbefore, heavy, mid;
   std::vector<unsigned char> pclass;
+  // TM / MSM: one CTA places a vertex with many nets alone; the others: one
+  // CTA evaluates a position with long lists, the grid places the longest
+  const bool msgm = pb.metric == FP_METRIC_TM || pb.metric == FP_METRIC_MSM;
   bool w0 = true;
   for (int v = 0; v < g.nov; v++)
     if (g.vptr[v + 1] == g.vptr[v] && pb.w[v] != 0) w0 = false;
@@ -446,27 +464,32 @@ static int build_stream_positions(fp_instance* in) {
       siso.push_back(v);
       continue;
     }
-    // the list entries its evaluation reads at most: sum of min(|e|, K)
-    long long work = 0;
-    for (uint32_t i = g.vptr[v]; i < g.vptr[v + 1]; i++) {
-      const int e = (int)g.vnets[i];
-      work += std::min<long long>(g.nptr[e + 1] - g.nptr[e], pb.K);
+    const uint32_t deg = g.vptr[v + 1] - g.vptr[v];
+    if (msgm) {
+      if (deg >= (uint32_t)kMsgStreamCta) heavy.push_back((int)sp.size());
+    } else {
+      // the list entries its evaluation reads at most: sum of min(|e|, K)
+      long long work = 0;
+      for (uint32_t i = g.vptr[v]; i < g.vptr[v + 1]; i++) {
+        const int e = (int)g.vnets[i];
+        work += std::min<long long>(g.nptr[e + 1] - g.nptr[e], pb.K);
+      }
+      unsigned char c = 0;
+      if (deg >= (uint32_t)kStreamHeavy || work >= kStreamGridWork) {
+        c = 2;
+        heavy.push_back((int)sp.size());
+      } else if (work >= kStreamCtaWork) {
+        c = 1;
+        mid.push_back((int)sp.size());
+      }
+      pclass.push_back(c);
     }
-    unsigned char c = 0;
-    if (g.vptr[v + 1] - g.vptr[v] >= (uint32_t)kStreamHeavy || work >= kStreamGridWork) {
-      c = 2;
-      heavy.push_back((int)sp.size());
-    } else if (work >= kStreamCtaWork) {
-      c = 1;
-      mid.push_back((int)sp.size());
-    }
-    pclass.push_back(c);
     sp.push_back(v);
     sbefore.push_back((int)siso.size());
   }
   sbefore.push_back((int)siso.size());
   in->stream_dev = w0 && !sp.empty() && pb.K <= kStreamMaxK &&
-                   stream_smem_bytes(pb.K) + 4096 <= (size_t)in->ctx->max_smem;
+                   (msgm ? stream_msg_smem_bytes(pb.K) : stream_smem_bytes(pb.K)) + 4096 <= (size_t)in->ctx->max_smem;
   in->sa.porder = in->st_porder_d;
   in->sa.npos = (int)sp.size();
   in->sa.iso_list = in->st_iso_d;
@@ -480,7 +503,17 @@ static int build_stream_positions(fp_instance* in) {
   in->sa.mark_pos = in->mark_pos_d;
   // the slot records: CN's refinement scratch of (pin, offset) pairs is free
   // before the first refinement
-  in->sa.rec = pb.metric == FP_METRIC_CN ? reinterpret_cast<uint32_t*>(in->sb.cn_moved) : in->sb.rec;
+  in->sa.rec = pb.metric == FP_METRIC_CN ? reinterpret_cast<uint32_t*>(in->sb.cn_moved)
+               : msgm                       ? in->st_rec_d
+                                            : in->sb.rec;
+  in->sa.prow = in->st_prow_d;
+  in->sa.pcol = in->st_pcol_d;
+  in->sa.rowpos = in->st_rowpos_d;
+  in->sa.colpos = in->st_colpos_d;
+  in->sa.saved = in->st_saved_d;
+  in->sa.actm = in->st_actm_d;
+  in->sa.ownm = in->st_ownm_d;
+  in->sa.msg_wmax = msg_stream_window(g.nov);
   cudaStream_t s0 = in->ctx->stream;
   cudaError_t e0 = cudaSuccess;
   if (in->stream_dev) {
@@ -494,7 +527,7 @@ static int build_stream_positions(fp_instance* in) {
       e0 = cudaMemcpyAsync(in->st_heavy_d, heavy.data(), sizeof(int) * heavy.size(), cudaMemcpyHostToDevice, s0);
     if (e0 == cudaSuccess && !mid.empty())
       e0 = cudaMemcpyAsync(in->st_mid_d, mid.data(), sizeof(int) * mid.size(), cudaMemcpyHostToDevice, s0);
-    if (e0 == cudaSuccess)
+    if (e0 == cudaSuccess && !pclass.empty())
       e0 = cudaMemcpyAsync(in->st_class_d, pclass.data(), pclass.size(), cudaMemcpyHostToDevice, s0);
     if (e0 == cudaSuccess) e0 = cudaStreamSynchronize(s0);
   }
@@ -701,13 +734,17 @@ int fp_instance_create(fp_ctx* ctx, const fp_hypergraph* h, int32_t K, int32_t m
         (rc = dalloc(in, &in->mid_pos_d, std::max(g.nov, g.noe))) ||
         (rc = dalloc(in, &in->porder_d, ldg ? g.nov : 1)) || (rc = dalloc(in, &in->iso_list_d, ldg ? g.nov : 1)) ||
         (rc = dalloc(in, &in->iso_before_d, ldg ? g.nov + 1 : 1)) ||
-        (rc = dalloc(in, &in->st_porder_d, ldg || cn ? g.nov : 1)) ||
-        (rc = dalloc(in, &in->st_iso_d, ldg || cn ? g.nov : 1)) ||
-        (rc = dalloc(in, &in->st_before_d, ldg || cn ? g.nov + 1 : 1)) ||
-        (rc = dalloc(in, &in->st_heavy_d, ldg || cn ? g.nov : 1)) ||
+        (rc = dalloc(in, &in->st_porder_d, g.nov)) || (rc = dalloc(in, &in->st_iso_d, g.nov)) ||
+        (rc = dalloc(in, &in->st_before_d, g.nov + 1)) || (rc = dalloc(in, &in->st_heavy_d, g.nov)) ||
         (rc = dalloc(in, &in->st_mid_d, ldg || cn ? g.nov : 1)) ||
         (rc = dalloc(in, &in->st_class_d, ldg || cn ? g.nov : 1)) ||
-        (rc = dalloc(in, &in->mark_pos_d, ldg || cn ? K : 1)) ||
+        (rc = dalloc(in, &in->mark_pos_d, K)) ||
+        (rc = dalloc(in, &in->st_rec_d, msg ? g.pins : 1)) || (rc = dalloc(in, &in->st_prow_d, msg ? K * words : 1)) ||
+        (rc = dalloc(in, &in->st_pcol_d, msg ? K * words : 1)) ||
+        (rc = dalloc(in, &in->st_rowpos_d, msg ? 2 * K : 1)) || (rc = dalloc(in, &in->st_colpos_d, msg ? 2 * K : 1)) ||
+        (rc = dalloc(in, &in->st_saved_d, msg ? (size_t)msg_stream_window(g.nov) * K : 1)) ||
+        (rc = dalloc(in, &in->st_actm_d, msg ? (size_t)msg_stream_window(g.nov) * words : 1)) ||
+        (rc = dalloc(in, &in->st_ownm_d, msg ? (size_t)msg_stream_window(g.nov) * words : 1)) ||
         (rc = dalloc(in, &in->metric_out, 8))) {
       fp_instance_destroy(in);
       return rc;
@@ -744,7 +781,7 @@ int fp_instance_create(fp_ctx* ctx, const fp_hypergraph* h, int32_t K, int32_t m
       if (e == cudaSuccess) e = cudaStreamSynchronize(s0);
       if (e != cudaSuccess) { fp_instance_destroy(in); return cuda_status(e); }
       if (ldg && (rc = build_positions(in))) { fp_instance_destroy(in); return rc; }
-      if ((ldg || cn) && (rc = build_stream_positions(in))) { fp_instance_destroy(in); return rc; }
+      if ((rc = build_stream_positions(in))) { fp_instance_destroy(in); return rc; }
       rc = classify(in, metric == FP_METRIC_CN ? kCnLightPins : kLightWork,
                     metric == FP_METRIC_CN ? kCnGridPins : default_super_work(metric));
       if (rc) { fp_instance_destroy(in); return rc; }
@@ -830,10 +867,16 @@ int fp_instance_footprint(int32_t nov, int32_t noe, int64_t pins, int32_t K, int
     add(16 * (size_t)kMaxGridVerts, 4); add(K, 8);           // hmisc, mlast
     add(VE, 4); add(VE, 4);                                  // heavy / medium positions
     add(ldg ? V : 1, 4); add(ldg ? V : 1, 4); add(ldg ? V + 1 : 1, 4);   // porder, iso_list, iso_before
-    add(ldg || cn ? V : 1, 4); add(ldg || cn ? V : 1, 4);   // device stream: positions, iso,
-    add(ldg || cn ? V + 1 : 1, 4); add(ldg || cn ? V : 1, 4);   //   before, whole-grid positions,
+    add(V, 4); add(V, 4); add(V + 1, 4); add(V, 4);          // device stream: positions, iso, before,
+                                                             //   whole-grid positions,
     add(ldg || cn ? V : 1, 4); add(ldg || cn ? V : 1, 1);   //   CTA positions, classes,
-    add(ldg || cn ? (size_t)K : 1, 4);                      //   mark_pos
+    add(K, 4);                                              //   mark_pos
+    {
+      const size_t mw = (size_t)msg_stream_window(nov);      //   TM / MSM: records, masks, first
+      add(msg ? P : 1, 4); add(msg ? K * words : 1, 4); add(msg ? K * words : 1, 4);   //   positions,
+      add(msg ? 2 * (size_t)K : 1, 4); add(msg ? 2 * (size_t)K : 1, 4);               //   saved messages,
+      add(msg ? mw * K : 1, 4); add(msg ? mw * words : 1, 4); add(msg ? mw * words : 1, 4);   // part masks
+    }
     add(8, 8);                                               // metric_out
     b += (long long)metrics_scratch_bytes(K);
     *bytes = b;
@@ -891,7 +934,25 @@ static int device_stream(fp_instance* in) {
   zero(in->sb.stats, sizeof(unsigned long long) * kNumStats, 0);
   if (e == cudaSuccess) e = cudaMemcpyAsync(in->sb.ctl, none, sizeof(none), cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess) e = clear_spec_scratch(in->sb, g.noe, K, s);
-  if (e == cudaSuccess) e = launch_stream_ldg(d, in->sb, in->sa, in->ctx->num_sms, s);
+  const bool msg = in->pb.metric == FP_METRIC_TM || in->pb.metric == FP_METRIC_MSM;
+  std::vector<int> conn0;
+  if (msg) {
+    // connection counts start at 0 (MSM: -1 on the diagonal, MSM/partition.cpp:
+    // 150-156); no entry is positive; no first positions
+    const size_t words = (size_t)(K + 31) / 32;
+    conn0.assign((size_t)K * K, 0);
+    if (in->pb.metric == FP_METRIC_MSM)
+      for (int i = 0; i < K; i++) conn0[(size_t)i * K + i] = -1;
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(d.conn, conn0.data(), sizeof(int) * conn0.size(), cudaMemcpyHostToDevice, s);
+    zero(in->st_prow_d, sizeof(uint32_t) * K * words, 0);
+    zero(in->st_pcol_d, sizeof(uint32_t) * K * words, 0);
+    zero(in->st_rowpos_d, sizeof(int) * 2 * K, 0x7f);
+    zero(in->st_colpos_d, sizeof(int) * 2 * K, 0x7f);
+  }
+  if (e == cudaSuccess)
+    e = msg ? launch_stream_msg(d, in->sb, in->sa, in->ctx->num_sms, s)
+            : launch_stream_ldg(d, in->sb, in->sa, in->ctx->num_sms, s);
   if (e == cudaSuccess) e = cudaMemcpyAsync(in->h_status, d.status, sizeof(int), cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return cuda_status(e);
@@ -908,9 +969,14 @@ static int device_stream(fp_instance* in) {
   st.recv.resize(K);
   st.msgs.assign(K, 0);
   st.conn.clear();
+  if (msg) st.conn.resize((size_t)K * K);
   auto back = [&](void* dst, const void* src, size_t bytes) {
     if (e == cudaSuccess && bytes) e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, s);
   };
+  if (msg) {
+    back(st.conn.data(), d.conn, sizeof(int) * st.conn.size());
+    back(st.msgs.data(), d.msgs, sizeof(int) * K);
+  }
   back(st.part_vec.data(), d.part_vec, sizeof(int) * g.nov);
   back(st.part_sizes.data(), d.part_sizes, sizeof(int) * K);
   back(st.ep_len.data(), d.ep_len, sizeof(int) * g.noe);
@@ -931,7 +997,9 @@ int fp_initial_partition(fp_instance* in) {
     // auto: the device stream where it is faster than the host's (TV, MSV,
     // MSRV; CN's stream cuts its windows at most positions, whose fallback
     // part moves with every placement)
-    const bool dev = in->stream_mode == 2 || (in->stream_mode == 0 && in->pb.metric != FP_METRIC_CN);
+    const int m = in->pb.metric;
+    const bool dev = in->stream_mode == 2 ||
+                     (in->stream_mode == 0 && (m == FP_METRIC_TV || m == FP_METRIC_MSV || m == FP_METRIC_MSRV));
     if (in->stream_dev && dev) {
       const int rc = device_stream(in);
       if (rc) return rc;

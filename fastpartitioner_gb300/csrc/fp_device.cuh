@@ -65,6 +65,15 @@ struct StreamArgs {
   const unsigned char* pclass;   // [npos] 0 a warp evaluates, 1 a CTA, 2 the grid
   int* mark_pos;          // [K] last position whose vertex saw the part, -1: none
   uint32_t* rec;          // [pins] slot of the chosen part in each (vertex, net) pair
+  // message-greedy stream (TM, MSM; csrc/fp_stream_msg.cu)
+  uint32_t* prow;         // [K * words] conn > 0: bit b of row a
+  uint32_t* pcol;         // [K * words] conn > 0: bit a of column b
+  int* rowpos;            // [2 * K] by round parity: first position that makes an entry of row a positive
+  int* colpos;            // [2 * K]
+  int* saved;             // [msg_wmax * K] messages each part saves, per window offset
+  uint32_t* actm;         // [msg_wmax * words] source parts active on the position's nets
+  uint32_t* ownm;         // [msg_wmax * words] parts listed on the nets the position is the source of
+  int msg_wmax;
 };
 constexpr int kStreamHeavy = 4096;   // nets of a vertex the whole grid places in the device stream
 // List entries a position's evaluation may read (the sum of min(|e|, K) over
@@ -72,6 +81,7 @@ constexpr int kStreamHeavy = 4096;   // nets of a vertex the whole grid places i
 constexpr long long kStreamCtaWork = 4096;
 constexpr long long kStreamGridWork = 65536;
 constexpr int kStreamMaxK = 1024;    // shared memory of the device stream's CTAs
+constexpr int kMsgStreamCta = 1024;  // nets of a vertex one CTA places alone in the message-greedy stream
 
 // Round statistics kept per instance (fp_get_stats).
 constexpr int kNumStats = 48;

@@ -35,6 +35,8 @@
 
 #include "fp_spec_common.cuh"
 
+#include <algorithm>
+
 namespace fp {
 
 namespace {
@@ -626,12 +628,613 @@ __global__ void stream_volumes_kernel(DevInstance I, int rv) {
   }
 }
 
+// ============================================================== TM / MSM
+// The message-greedy stream (TM/partition.cpp:87-250, MSM/partition.cpp:
+// 146-309).  A vertex v reads: the source parts of its nets whose source is
+// placed (the active parts), the part lists of the nets it is the source of
+// (its own nets), which connection counts are positive in the active parts'
+// rows and in the listed parts' columns, and the part sizes.  It saves, in
+// part k, one message per active part sp with conn[sp][k] > 0 and one per
+// (own net, listed part p) with conn[k][p] > 0; it takes the part below
+// capacity that saves the most (ties: the smaller part, then the lower
+// index), else the least-loaded part.  Placing v appends or increments its
+// nets' lists, makes v's part the source part of its own nets, and raises
+// conn[sp][d] (1 if it was 0, else +1 where d is new on the net) and
+// conn[d][p] (+1 per own net listing p), counting a message where an entry
+// leaves 0.
+//
+// A window position is invalid when an earlier one appends to or is the
+// source of one of its nets (claims), or makes an entry positive in a row or
+// column it reads (first such position per row and per column, by round
+// parity).  Among the committed positions an entry that was 0 at the window
+// start is therefore raised by one position only, so its first-event rule is
+// applied by that position alone; the other entries only add.
+
+// Record of a (vertex, net) pair: the chosen part's slot (13 bits; kNoSlot:
+// appended), the net's source part at the window start plus one (11 bits; 0:
+// the source is not placed), the vertex is the net's source (bit 24).
+__device__ __forceinline__ uint32_t mrec(int slot, int sp, bool own) {
+  return (uint32_t)(slot < 0 ? (int)kNoSlot : slot) | ((uint32_t)(sp + 1) << 13) | (own ? 1u << 24 : 0u);
+}
+__device__ __forceinline__ int mrec_slot(uint32_t r) { return (int)(r & 0x1fffu); }
+__device__ __forceinline__ int mrec_sp(uint32_t r) { return (int)((r >> 13) & 0x7ffu) - 1; }
+__device__ __forceinline__ bool mrec_own(uint32_t r) { return (r >> 24) & 1u; }
+
+__device__ __forceinline__ bool bit_of(const uint32_t* m, int b) { return (m[b >> 5] >> (b & 31)) & 1u; }
+
+struct MsgKey {
+  int sv, sz, k;   // k = -1: none
+};
+__device__ __forceinline__ bool msg_better(const MsgKey& a, const MsgKey& b) {
+  if (a.k < 0) return false;
+  if (b.k < 0) return true;
+  if (a.sv != b.sv) return a.sv > b.sv;
+  if (a.sz != b.sz) return a.sz < b.sz;
+  return a.k < b.k;
+}
+__device__ __forceinline__ MsgKey warp_msg_best(MsgKey x) {
+  for (int off = 16; off; off >>= 1) {
+    MsgKey o;
+    o.sv = __shfl_xor_sync(kAll, x.sv, off);
+    o.sz = __shfl_xor_sync(kAll, x.sz, off);
+    o.k = __shfl_xor_sync(kAll, x.k, off);
+    if (msg_better(o, x)) x = o;
+  }
+  return x;
+}
+
+// Messages part k saves for the active parts `act` and the own-net parts
+// `own` with multiplicities `mult` (conn > 0 masks prow / pcol).
+__device__ __forceinline__ int msg_saved(const StreamArgs& S, int K, int words, int k, const uint32_t* act,
+                                         const uint32_t* own, const int* mult) {
+  int sv = 0;
+  const uint32_t* col = S.pcol + (size_t)k * words;
+  const uint32_t* row = S.prow + (size_t)k * words;
+  for (int w = 0; w < words; w++) {
+    sv += __popc(act[w] & __ldcg(&col[w]));
+    uint32_t x = own[w] & __ldcg(&row[w]);
+    while (x) {
+      const int b = __ffs(x) - 1;
+      x &= x - 1;
+      sv += mult[w * 32 + b];
+    }
+  }
+  return sv;
+}
+
+// Nets [n0, n1) of v: active source parts into act, own nets' listed parts
+// into own / mult (one warp; act, own, mult shared by the warps that call it).
+__device__ void msg_scan_nets(const DevInstance& I, int v, uint32_t base, int n0, int n1, uint32_t* act,
+                              uint32_t* own, int* mult) {
+  const int lane = threadIdx.x & 31;
+  for (int k = n0 + lane; k < n1; k += 32) {
+    const int e = (int)__ldg(&I.vnets[base + k]);
+    const int s = __ldg(&I.src[e]);
+    if (s == v) {
+      const int sl = (int)__ldg(&I.nptr[e]);
+      const int n = lds(&I.ep_len[e]);
+      for (int j = 0; j < n; j++) {
+        const int p = lds(&I.ep_part[sl + j]);
+        if ((unsigned)p >= (unsigned)I.K) { dev_fail(I.status, kDevErrInvalid); continue; }
+        atomicAdd(&mult[p], 1);
+        atomicOr(&own[p >> 5], 1u << (p & 31));
+      }
+    } else {
+      const int sp = lds(&I.part_vec[s]);
+      if (sp >= 0) atomicOr(&act[sp >> 5], 1u << (sp & 31));
+    }
+  }
+}
+
+// Records of v's nets [n0, n1) for decision d (slot, source part, own net)
+// and, with claim, the claims of the nets v appends to or is the source of.
+__device__ void msg_records(const DevInstance& I, const SpecBuf& B, const StreamArgs& S, int v, uint32_t base,
+                            int n0, int n1, int d, bool claim, int round, int z, int* sd) {
+  const int lane = threadIdx.x & 31;
+  for (int nb = n0; nb < n1; nb += 32) {
+    const int j = locate_part(I, base, nb, n1, d, sd);
+    const int k = nb + lane;
+    if (k < n1) {
+      const int e = (int)__ldg(&I.vnets[base + k]);
+      const int s = __ldg(&I.src[e]);
+      const bool own = s == v;
+      const int sp = own ? -1 : lds(&I.part_vec[s]);
+      S.rec[base + k] = mrec(j, sp, own);
+      if (claim && (j < 0 || own)) atomicMax(&B.claim64[e], skey(round, z));
+    }
+  }
+}
+
+// The entries position z (decision d) makes positive, by the window-start
+// masks: (sp, d) for active sp != d, (d, p) for own-net parts p != d; their
+// rows and columns' first positions (one warp).
+__device__ void msg_mark_new(const StreamArgs& S, int K, int words, int par, int z, int d, const uint32_t* act,
+                             const uint32_t* own) {
+  const int lane = threadIdx.x & 31;
+  bool any_d_col = false, any_d_row = false;
+  for (int k = lane; k < K; k += 32) {
+    if (k == d) continue;
+    if (bit_of(act, k) && !((__ldcg(&S.prow[(size_t)k * words + (d >> 5)]) >> (d & 31)) & 1u)) {
+      atomicMin(&S.rowpos[par * K + k], z);
+      any_d_col = true;
+    }
+    if (bit_of(own, k) && !((__ldcg(&S.prow[(size_t)d * words + (k >> 5)]) >> (k & 31)) & 1u)) {
+      atomicMin(&S.colpos[par * K + k], z);
+      any_d_row = true;
+    }
+  }
+  if (__any_sync(kAll, any_d_col) && lane == 0) atomicMin(&S.colpos[par * K + d], z);
+  if (__any_sync(kAll, any_d_row) && lane == 0) atomicMin(&S.rowpos[par * K + d], z);
+}
+
+__device__ __forceinline__ void set_pos_bit(const StreamArgs& S, int words, int a, int b) {
+  atomicOr(&S.prow[(size_t)a * words + (b >> 5)], 1u << (b & 31));
+  atomicOr(&S.pcol[(size_t)b * words + (a >> 5)], 1u << (a & 31));
+}
+
+// Commit of v's connection updates for decision d over nets [n0, n1) of the
+// warp, before v's lists change.  first[K]: first net index per active part
+// (filled by the caller over all of v's nets), zs[K]: conn[sp][d] was 0.
+__device__ void msg_commit_act(const DevInstance& I, const StreamArgs& S, int words, int d, uint32_t base, int n0,
+                               int n1, const int* first, const int* zs, int slot_override_d, int* sd) {
+  const int lane = threadIdx.x & 31;
+  const int K = I.K;
+  for (int nb = n0; nb < n1; nb += 32) {
+    // d's slot: the record's, or located again (a flip committed with another part)
+    const int jl = slot_override_d ? locate_part(I, base, nb, n1, d, sd) : 0;
+    const int k = nb + lane;
+    if (k >= n1) continue;
+    const uint32_t r = lds(&S.rec[base + k]);
+    const int sp = mrec_sp(r);
+    if (sp < 0 || sp == d) continue;
+    const bool dc1 = slot_override_d ? jl < 0 : mrec_slot(r) == (int)kNoSlot;   // d is new on the net
+    const bool is_first = first[sp] == k;
+    const int add = is_first ? (zs[sp] ? 1 : (dc1 ? 1 : 0)) : (dc1 ? 1 : 0);
+    if (add) atomicAdd(&I.conn[(size_t)sp * K + d], add);
+    if (is_first && zs[sp]) {
+      atomicAdd(&I.msgs[sp], 1);
+      set_pos_bit(S, words, sp, d);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kSThreads, 2) stream_msg_kernel(DevInstance I, SpecBuf B, StreamArgs S) {
+  barrier_start();
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ unsigned long long uscr[kSWarps];
+  __shared__ int s_minpart, s_minsize, s_second, s_dec;
+  __shared__ MsgKey s_best[kSWarps];
+  const int K = I.K;
+  const int words = (K + 31) >> 5;
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const int gw = blockIdx.x * kSWarps + wib;
+  const int nwarps = gridDim.x * kSWarps;
+  const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
+  Carve cv{smem_raw};
+  int* sizes_s = cv.take<int>(K);
+  int* dsz_cta = cv.take<int>(K);
+  int* a_b = cv.take<int>((size_t)K * kSWarps);        // per warp: multiplicities / sizes / first nets
+  int* b_b = cv.take<int>((size_t)K * kSWarps);        // per warp: zero-start flags
+  uint32_t* act_b = cv.take<uint32_t>((size_t)words * kSWarps);
+  uint32_t* own_b = cv.take<uint32_t>((size_t)words * kSWarps);
+  int* sd_b = cv.take<int>(32 * kSWarps);
+  int* ca = cv.take<int>(K);                           // CTA: multiplicities, then first nets
+  int* cb = cv.take<int>(K);                           // CTA: zero-start flags
+  uint32_t* cact = cv.take<uint32_t>(words);
+  uint32_t* cown = cv.take<uint32_t>(words);
+  int* wa = a_b + (size_t)wib * K;
+  int* wb = b_b + (size_t)wib * K;
+  uint32_t* wact = act_b + (size_t)wib * words;
+  uint32_t* wown = own_b + (size_t)wib * words;
+  int* sd = sd_b + 32 * wib;
+  const bool stats = blockIdx.x == 0 && threadIdx.x == 0;
+  unsigned long long t0 = stats ? gtimer() : 0ull;
+  auto lap = [&](int slot) {
+    if (stats) {
+      const unsigned long long t = gtimer();
+      B.stats[slot] += t - t0;
+      t0 = t;
+    }
+  };
+
+  int pos = 0, round = 1, hidx = 0;
+  int W = min(nwarps, S.msg_wmax);
+  while (pos < S.npos) {
+    const int par = round & 1;
+    for (int p = threadIdx.x; p < K; p += blockDim.x) sizes_s[p] = lds(&I.part_sizes[p]);
+    __syncthreads();
+    block_min_part(sizes_s, K, uscr, &s_minpart, &s_minsize, &s_second);
+    __syncthreads();
+    while (hidx < S.nheavy && __ldg(&S.heavy_pos[hidx]) < pos) hidx++;
+    if (hidx < S.nheavy && __ldg(&S.heavy_pos[hidx]) == pos) {
+      // ======================= a vertex with many nets: CTA 0 places it alone
+      if (blockIdx.x == 0) {
+        const int v = __ldg(&S.porder[pos]);
+        const uint32_t base = __ldg(&I.vptr[v]);
+        const int deg = (int)(__ldg(&I.vptr[v + 1]) - base);
+        int n0, n1;
+        net_range(deg, wib, kSWarps, &n0, &n1);
+        for (int p = threadIdx.x; p < K; p += blockDim.x) ca[p] = 0;
+        for (int x = threadIdx.x; x < words; x += blockDim.x) { cact[x] = 0; cown[x] = 0; }
+        __syncthreads();
+        msg_scan_nets(I, v, base, n0, n1, cact, cown, ca);
+        __syncthreads();
+        MsgKey best{0, 0, -1};
+        for (int k = threadIdx.x; k < K; k += blockDim.x) {
+          const int sv = msg_saved(S, K, words, k, cact, cown, ca);
+          if ((double)sizes_s[k] < I.C) {
+            const MsgKey c{sv, sizes_s[k], k};
+            if (msg_better(c, best)) best = c;
+          }
+        }
+        best = warp_msg_best(best);
+        if (lane == 0) s_best[wib] = best;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+          MsgKey b = s_best[0];
+          for (int x = 1; x < kSWarps; x++)
+            if (msg_better(s_best[x], b)) b = s_best[x];
+          s_dec = b.k >= 0 ? b.k : s_minpart;
+        }
+        __syncthreads();
+        const int d = s_dec;
+        // own-net messages: conn[d][p] += multiplicity, a message where it was 0
+        for (int p = threadIdx.x; p < K; p += blockDim.x) {
+          const int m = ca[p];
+          if (m > 0 && p != d) {
+            const bool z0 = !((__ldcg(&S.prow[(size_t)d * words + (p >> 5)]) >> (p & 31)) & 1u);
+            atomicAdd(&I.conn[(size_t)d * K + p], m);
+            if (z0) {
+              atomicAdd(&I.msgs[d], 1);
+              set_pos_bit(S, words, d, p);
+            }
+          }
+        }
+        // records (no claims: the window holds this position alone)
+        msg_records(I, B, S, v, base, n0, n1, d, false, round, pos, sd);
+        __syncthreads();
+        for (int p = threadIdx.x; p < K; p += blockDim.x) {
+          ca[p] = 0x7fffffff;
+          cb[p] = p != d && !((__ldcg(&S.prow[(size_t)p * words + (d >> 5)]) >> (d & 31)) & 1u);
+        }
+        __syncthreads();
+        for (int k = n0 + lane; k < n1; k += 32) {
+          const int sp = mrec_sp(lds(&S.rec[base + k]));
+          if (sp >= 0 && sp != d) atomicMin(&ca[sp], k);
+        }
+        __syncthreads();
+        msg_commit_act(I, S, words, d, base, n0, n1, ca, cb, 0, sd);
+        __syncthreads();
+        for (int k = n0 + lane; k < n1; k += 32)
+          place_net(I, (int)__ldg(&I.vnets[base + k]), d, mrec_slot(lds(&S.rec[base + k])));
+        if (threadIdx.x == 0) {
+          I.part_vec[v] = d;
+          const int wv = __ldg(&I.w[v]);
+          if (wv) atomicAdd(&I.part_sizes[d], wv);
+        }
+        if (S.niso && wib == 0) {
+          int* sz = wa;
+          for (int p = lane; p < K; p += 32) sz[p] = sizes_s[p];
+          __syncwarp();
+          int amin = -1;
+          if (pos == 0) place_iso(I, S, sz, 0, __ldg(&S.iso_before[0]), &amin);
+          __syncwarp();
+          const int wv = __ldg(&I.w[v]);
+          if (lane == 0) sz[d] += wv;
+          __syncwarp();
+          amin = wv ? -1 : amin;
+          place_iso(I, S, sz, __ldg(&S.iso_before[pos]), __ldg(&S.iso_before[pos + 1]), &amin);
+        }
+      }
+      if (gtid == 0) {
+        B.ctl[4 + (par ^ 1)] = kNone;
+        B.mcnt[par ^ 1] = 0;
+      }
+      for (int p = gtid; p < K; p += gridDim.x * blockDim.x) {
+        S.rowpos[(par ^ 1) * K + p] = kNone;
+        S.colpos[(par ^ 1) * K + p] = kNone;
+      }
+      pos++;
+      round++;
+      if (!grid_barrier(B.bar, I.status)) return;
+      if (stats) B.stats[1]++;
+      lap(19);
+      continue;
+    }
+
+    // ================================================================= window
+    int end_w = min(pos + W, S.npos);
+    if (hidx < S.nheavy) end_w = min(end_w, (int)__ldg(&S.heavy_pos[hidx]));
+    const int span = end_w - pos;
+    const int q = (span + nwarps - 1) / nwarps;
+    const int z0 = min(pos + gw * q, end_w);
+    const int z1 = min(z0 + q, end_w);
+    // ---- A: evaluate
+    for (int z = z0; z < z1; z++) {
+      const int o = z - pos;
+      const int v = __ldg(&S.porder[z]);
+      const uint32_t base = __ldg(&I.vptr[v]);
+      const int deg = (int)(__ldg(&I.vptr[v + 1]) - base);
+      for (int p = lane; p < K; p += 32) wa[p] = 0;
+      for (int x = lane; x < words; x += 32) { wact[x] = 0; wown[x] = 0; }
+      __syncwarp();
+      msg_scan_nets(I, v, base, 0, deg, wact, wown, wa);
+      __syncwarp();
+      MsgKey best{0, 0, -1};
+      int* sv_out = S.saved + (size_t)o * K;
+      for (int k = lane; k < K; k += 32) {
+        const int sv = msg_saved(S, K, words, k, wact, wown, wa);
+        sv_out[k] = sv;
+        if ((double)sizes_s[k] < I.C) {
+          const MsgKey c{sv, sizes_s[k], k};
+          if (msg_better(c, best)) best = c;
+        }
+      }
+      best = warp_msg_best(best);
+      const int d = best.k >= 0 ? best.k : s_minpart;
+      msg_records(I, B, S, v, base, 0, deg, d, true, round, z, sd);
+      msg_mark_new(S, K, words, par, z, d, wact, wown);
+      for (int x = lane; x < words; x += 32) {
+        S.actm[(size_t)o * words + x] = wact[x];
+        S.ownm[(size_t)o * words + x] = wown[x];
+      }
+      const int wv = __ldg(&I.w[v]);
+      if (lane == 0) {
+        B.dec[o] = d;
+        B.wt[o] = wv;
+        if (wv) B.mlist[atomicAdd(&B.mcnt[par], 1)] = make_int4(o, wv, d, 0);
+      }
+      __syncwarp();
+    }
+    if (!grid_barrier(B.bar, I.status)) return;
+    lap(16);
+    // ---- B: validate
+    int* const cut_w = &B.ctl[4 + par];
+    {
+      const int cz0 = min(pos + blockIdx.x * kSWarps * q, end_w);
+      const int cta_o0 = cz0 - pos;
+      for (int p = threadIdx.x; p < K; p += blockDim.x) dsz_cta[p] = 0;
+      __syncthreads();
+      const int nm = lds(&B.mcnt[par]);
+      for (int i = threadIdx.x; i < nm; i += blockDim.x) {
+        const int4 m = lds(&B.mlist[i]);
+        if (m.x < cta_o0) atomicAdd(&dsz_cta[m.z], m.y);
+      }
+      __syncthreads();
+      for (int z = z0; z < z1; z++) {
+        const int o = z - pos;
+        const int v = __ldg(&S.porder[z]);
+        const uint32_t base = __ldg(&I.vptr[v]);
+        const int deg = (int)(__ldg(&I.vptr[v + 1]) - base);
+        bool conf = false;
+        for (int k = lane; k < deg && !conf; k += 32)
+          conf = claimed_before(B, round, (int)__ldg(&I.vnets[base + k]), z);
+        for (int k = lane; k < K && !conf; k += 32) {
+          if (bit_of(S.actm + (size_t)o * words, k) && lds(&S.rowpos[par * K + k]) < z) conf = true;
+          if (bit_of(S.ownm + (size_t)o * words, k) && lds(&S.colpos[par * K + k]) < z) conf = true;
+        }
+        int why = __any_sync(kAll, conf) ? 5 : 0;
+        if (!why) {
+          int* dsz = wa;
+          for (int p = lane; p < K; p += 32) dsz[p] = dsz_cta[p];
+          __syncwarp();
+          for (int o2 = cta_o0 + lane; o2 < o; o2 += 32) {
+            const int w = lds(&B.wt[o2]);
+            if (w) atomicAdd(&dsz[lds(&B.dec[o2])], w);
+          }
+          __syncwarp();
+          MsgKey best{0, 0, -1};
+          const int* sv_in = S.saved + (size_t)o * K;
+          for (int k = lane; k < K; k += 32) {
+            const int sz = sizes_s[k] + dsz[k];
+            if ((double)sz < I.C) {
+              const MsgKey c{lds(&sv_in[k]), sz, k};
+              if (msg_better(c, best)) best = c;
+            }
+          }
+          best = warp_msg_best(best);
+          const int d2 = best.k >= 0 ? best.k : least_loaded(sizes_s, dsz, K);
+          if (d2 != lds(&B.dec[o])) {
+            why = 2;
+            if (lane == 0) B.dfix[o] = d2;
+          }
+          __syncwarp();
+        }
+        if (why) {
+          if (lane == 0) atomicMin(cut_w, (z << 3) | why);
+          break;
+        }
+      }
+    }
+    if (!grid_barrier(B.bar, I.status)) return;
+    lap(17);
+    const int cutw = lds(cut_w);
+    const int cut = cutw == kNone ? end_w : min(cutw >> 3, end_w);
+    const bool flip = cutw != kNone && (cutw & 7) == 2;
+    const int cutc = flip ? cut + 1 : cut;
+    if (cut <= pos) {
+      if (gtid == 0) dev_fail(I.status, kDevErrInvalid);
+      return;
+    }
+    // ---- C: commit
+    for (int z = z0; z < min(z1, cutc); z++) {
+      const int o = z - pos;
+      const int v = __ldg(&S.porder[z]);
+      const uint32_t base = __ldg(&I.vptr[v]);
+      const int deg = (int)(__ldg(&I.vptr[v + 1]) - base);
+      const bool fl = z == cut;
+      const int d = fl ? lds(&B.dfix[o]) : lds(&B.dec[o]);
+      // own-net messages from the window-start lists (before v's placement)
+      for (int p = lane; p < K; p += 32) wa[p] = 0;
+      for (int x = lane; x < words; x += 32) { wact[x] = 0; wown[x] = 0; }
+      __syncwarp();
+      for (int k = lane; k < deg; k += 32) {
+        const uint32_t r = lds(&S.rec[base + k]);
+        if (!mrec_own(r)) continue;
+        const int e = (int)__ldg(&I.vnets[base + k]);
+        const int sl = (int)__ldg(&I.nptr[e]);
+        const int n = lds(&I.ep_len[e]);
+        for (int j = 0; j < n; j++) {
+          const int pp = lds(&I.ep_part[sl + j]);
+          if ((unsigned)pp < (unsigned)K) atomicAdd(&wa[pp], 1);
+        }
+      }
+      __syncwarp();
+      for (int p = lane; p < K; p += 32) {
+        const int m = wa[p];
+        if (m > 0 && p != d) {
+          const bool z0b = !((__ldcg(&S.prow[(size_t)d * words + (p >> 5)]) >> (p & 31)) & 1u);
+          atomicAdd(&I.conn[(size_t)d * K + p], m);
+          if (z0b) {
+            atomicAdd(&I.msgs[d], 1);
+            set_pos_bit(S, words, d, p);
+          }
+        }
+      }
+      __syncwarp();
+      // active-source messages: first net per source part, zero-start flags
+      for (int p = lane; p < K; p += 32) {
+        wa[p] = 0x7fffffff;
+        wb[p] = p != d && !((__ldcg(&S.prow[(size_t)p * words + (d >> 5)]) >> (d & 31)) & 1u);
+      }
+      __syncwarp();
+      for (int k = lane; k < deg; k += 32) {
+        const int sp = mrec_sp(lds(&S.rec[base + k]));
+        if (sp >= 0 && sp != d) atomicMin(&wa[sp], k);
+      }
+      __syncwarp();
+      msg_commit_act(I, S, words, d, base, 0, deg, wa, wb, fl ? 1 : 0, sd);
+      __syncwarp();
+      if (fl) {
+        for (int nb = 0; nb < deg; nb += 32) {
+          const int j = locate_part(I, base, nb, deg, d, sd);
+          if (nb + lane < deg) place_net(I, (int)__ldg(&I.vnets[base + nb + lane]), d, j);
+        }
+      } else {
+        for (int k = lane; k < deg; k += 32)
+          place_net(I, (int)__ldg(&I.vnets[base + k]), d, mrec_slot(lds(&S.rec[base + k])));
+      }
+      if (lane == 0) {
+        I.part_vec[v] = d;
+        const int wv = lds(&B.wt[o]);
+        if (wv) atomicAdd(&I.part_sizes[d], wv);
+      }
+      __syncwarp();
+    }
+    if (S.niso) {
+      const int zb = min(z1, cutc);
+      if (z0 < zb || (pos == 0 && gw == 0)) {
+        const int cta_o0 = min(pos + blockIdx.x * kSWarps * q, end_w) - pos;
+        int* sz = wa;
+        for (int p = lane; p < K; p += 32) sz[p] = sizes_s[p] + dsz_cta[p];
+        __syncwarp();
+        for (int o2 = cta_o0 + lane; o2 < z0 - pos; o2 += 32) {
+          const int w = lds(&B.wt[o2]);
+          if (w) atomicAdd(&sz[lds(&B.dec[o2])], w);
+        }
+        __syncwarp();
+        int amin = -1;
+        if (pos == 0 && gw == 0) place_iso(I, S, sz, 0, __ldg(&S.iso_before[0]), &amin);
+        for (int z = z0; z < zb; z++) {
+          const int o = z - pos;
+          const int w = lds(&B.wt[o]);
+          if (w) {
+            __syncwarp();
+            if (lane == 0) sz[z == cut ? lds(&B.dfix[o]) : lds(&B.dec[o])] += w;
+            __syncwarp();
+            amin = -1;
+          }
+          place_iso(I, S, sz, __ldg(&S.iso_before[z]), __ldg(&S.iso_before[z + 1]), &amin);
+        }
+      }
+    }
+    if (gtid == 0) {
+      B.ctl[4 + (par ^ 1)] = kNone;
+      B.mcnt[par ^ 1] = 0;
+    }
+    for (int p = gtid; p < K; p += gridDim.x * blockDim.x) {
+      S.rowpos[(par ^ 1) * K + p] = kNone;
+      S.colpos[(par ^ 1) * K + p] = kNone;
+    }
+    if (stats) {
+      B.stats[0]++;
+      B.stats[2] += cutc - pos;
+      if (cutw != kNone) B.stats[(cutw & 7) == 2 ? 5 : 8]++;
+    }
+    if (cutc >= end_w) {
+      if (end_w == pos + W) W = min(2 * W, S.msg_wmax);
+    } else {
+      W = min(S.msg_wmax, max(256, 2 * (cutc - pos)));
+    }
+    pos = cutc;
+    round++;
+    if (!grid_barrier(B.bar, I.status)) return;
+    lap(18);
+  }
+}
+
+// The refinement's masks of the streamed connection counts: zero and one, by
+// row and by column.
+__global__ void stream_conn_masks_kernel(DevInstance I) {
+  const int K = I.K;
+  const int words = (K + 31) >> 5;
+  for (long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x; x < (long long)K * words;
+       x += (long long)gridDim.x * blockDim.x) {
+    const int a = (int)(x / words), w = (int)(x % words);
+    uint32_t zr = 0, zc = 0, c1r = 0, c1c = 0;
+    for (int b = 0; b < 32; b++) {
+      const int k = w * 32 + b;
+      if (k >= K) break;
+      const int r = I.conn[(size_t)a * K + k];   // row a, column k
+      const int c = I.conn[(size_t)k * K + a];   // column a, row k
+      if (r == 0) zr |= 1u << b;
+      if (r == 1) c1r |= 1u << b;
+      if (c == 0) zc |= 1u << b;
+      if (c == 1) c1c |= 1u << b;
+    }
+    I.zrow[x] = zr;
+    I.zcol[x] = zc;
+    I.c1row[x] = c1r;
+    I.c1col[x] = c1c;
+  }
+}
+
 }  // namespace
 
 size_t stream_smem_bytes(int K) {
   auto a = [](size_t n) { return (n + 15) & ~size_t(15); };
   return 2 * a(sizeof(int) * K) + a(sizeof(int) * (size_t)K * kSWarps) +
          a(sizeof(unsigned long long) * (size_t)K * kSWarps) + a(sizeof(int) * 32 * kSWarps);
+}
+
+size_t stream_msg_smem_bytes(int K) {
+  auto a = [](size_t n) { return (n + 15) & ~size_t(15); };
+  const size_t words = (size_t)(K + 31) / 32;
+  return 2 * a(sizeof(int) * K) + 2 * a(sizeof(int) * (size_t)K * kSWarps) + 2 * a(sizeof(uint32_t) * words * kSWarps) +
+         a(sizeof(int) * 32 * kSWarps) + 2 * a(sizeof(int) * K) + 2 * a(sizeof(uint32_t) * words);
+}
+
+cudaError_t launch_stream_msg(const DevInstance& I, const SpecBuf& B, const StreamArgs& S, int num_sms,
+                              cudaStream_t st) {
+  const size_t smem = stream_msg_smem_bytes(I.K);
+  const void* fn = (const void*)stream_msg_kernel;
+  cudaError_t err = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (err != cudaSuccess) return err;
+  int per_sm = 0;
+  err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kSThreads, smem);
+  if (err != cudaSuccess) return err;
+  if (per_sm < 1) return cudaErrorInvalidConfiguration;
+  int grid = per_sm * num_sms;
+  if (grid * kSWarps > B.max_warps) grid = B.max_warps / kSWarps;
+  DevInstance Ic = I;
+  SpecBuf Bc = B;
+  StreamArgs Sc = S;
+  void* args[] = {&Ic, &Bc, &Sc};
+  err = cudaLaunchCooperativeKernel(fn, grid, kSThreads, args, smem, st);
+  if (err != cudaSuccess) return err;
+  const long long n = (long long)I.K * ((I.K + 31) / 32);
+  stream_conn_masks_kernel<<<(int)std::min<long long>((n + 255) / 256, (long long)num_sms * 8), 256, 0, st>>>(I);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_stream_ldg(const DevInstance& I, const SpecBuf& B, const StreamArgs& S, int num_sms,

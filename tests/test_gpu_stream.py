@@ -1,10 +1,11 @@
-"""The streaming initial partition of TV, MSV, MSRV and CN on the device
-(csrc/fp_stream.cu) against the host stream (fp_stream_partition, the
-restatement of TV/partition.cpp:207-264, MGV/partition.cpp:122-189,
-MSRV/partition.cpp:123-196 and CN/partition.cpp:132-221 that the oracle and the
-reference's own outputs pin): the whole fp_state -- part vector, every net's
-ordered (part, count) list, part sizes, TV's marker, the MSV / MSRV volumes --
-bit for bit.
+"""The streaming initial partitions on the device (csrc/fp_stream.cu) against
+the host streams (fp_stream_partition, the restatement of
+TV/partition.cpp:207-264, MGV/partition.cpp:122-189, MSRV/partition.cpp:
+123-196, CN/partition.cpp:132-221, TM/partition.cpp:87-250 and
+MSM/partition.cpp:146-309 that the oracle and the reference's own outputs
+pin): the whole fp_state -- part vector, every net's ordered (part, count)
+list, part sizes, TV's marker, the MSV / MSRV volumes, the TM / MSM K x K
+connection counts and messages -- bit for bit.
 
 The device stream runs when every vertex without nets weighs 0 (vertex weight =
 degree) and K <= 1024; the cases cover vertices without nets before, between
@@ -16,8 +17,13 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-STREAMED = ("TV", "MSV", "MSRV", "CN")
+STREAMED = ("TV", "MSV", "MSRV", "CN", "TM", "MSM")
 FIELDS = ("part_vec", "ep_ends", "ep_parts", "ep_cnt", "part_sizes", "marker", "send", "recv")
+MSG_FIELDS = ("conn", "msgs")
+
+
+def fields(metric):
+    return FIELDS + (MSG_FIELDS if metric in ("TM", "MSM") else ())
 
 
 def degree_weighted(hg):
@@ -69,12 +75,12 @@ def test_device_stream_matches_host_stream(fp, gpu_engine, name, mk, K, metric):
     want = fp.stream_partition(hg, K, metric)
     on_dev, got = device_state(gpu_engine, hg, K, metric)
     assert on_dev, "the instance qualifies for the device stream"
-    for f in FIELDS:
+    for f in fields(metric):
         np.testing.assert_array_equal(got[f], want[f], err_msg=f"{name} {metric} {f}")
     np.testing.assert_array_equal(got["ep_starts"], hg.nptr[:-1].astype(np.int32))
     host_dev, host = device_state(gpu_engine, hg, K, metric, where="host")
     assert not host_dev
-    for f in FIELDS:
+    for f in fields(metric):
         np.testing.assert_array_equal(host[f], want[f], err_msg=f"host {name} {metric} {f}")
 
 
@@ -101,14 +107,15 @@ def test_refinement_after_the_device_stream(fp, orc, gpu_engine, metric):
 
 
 def test_device_stream_only_where_it_qualifies(fp, gpu_engine):
-    """Unit weights with vertices without nets, K above 1024 and TM / MSM
-    stream on the host; by default CN does too (its device stream is slower)."""
+    """Unit weights with vertices without nets and K above 1024 stream on the
+    host; by default CN, TM and MSM do too."""
     unit = fp.generate(fp.GenSpec.zipf(5000, 4000, 2.0, 2, 200, beta=1.0, seed=88))
     assert (np.diff(unit.vptr) == 0).any()
     degw = fp.generate(fp.GenSpec.zipf(5000, 4000, 2.0, 2, 200, beta=1.0, weight_rule=1, seed=88))
     for hg, K, metric, dev, where in ((unit, 8, "TV", False, "device"), (degw, 2048, "MSV", False, "device"),
                                       (degw, 8, "CN", True, "device"), (degw, 8, "CN", False, "auto"),
-                                      (degw, 8, "TM", False, "device"), (degw, 8, "MSRV", True, "auto")):
+                                      (degw, 8, "TM", True, "device"), (degw, 8, "TM", False, "auto"),
+                                      (degw, 16, "MSM", True, "device"), (degw, 8, "MSRV", True, "auto")):
         with gpu_engine.instance(hg, K, metric) as inst:
             inst.set_stream(where)
             inst.initial_partition()
@@ -117,5 +124,5 @@ def test_device_stream_only_where_it_qualifies(fp, gpu_engine):
                 continue
             st = inst.get_state()
         want = fp.stream_partition(hg, K, metric)
-        for f in FIELDS:
+        for f in fields(metric):
             np.testing.assert_array_equal(st[f], want[f], err_msg=f)
