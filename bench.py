@@ -656,6 +656,116 @@ def run_serve(args):
     print(json.dumps(line), flush=True)
 
 
+def run_stream(args):
+    """Streaming initial partitions of the workload: the device stream
+    (fp_set_stream_mode device: csrc/fp_stream.cu) against the host stream on
+    the same instance, per metric (--metrics; default TV, MSV, MSRV, the ones
+    that stream on the device by default).  Seconds of fp_initial_partition on
+    the wall clock, the state's copy to the host included; every state array
+    compared."""
+    import torch
+    import fastpartitioner_gb300 as fp
+    torch.cuda.set_device(0)
+    w = WORKLOADS[args.config]
+    metrics = args.metrics.split(",") if args.metrics else ["TV", "MSV", "MSRV"]
+    hg = fp.generate(spec_for(fp, w, args.scale))
+    fields = ("part_vec", "ep_ends", "ep_parts", "ep_cnt", "part_sizes", "marker", "send", "recv", "conn", "msgs")
+    per = {}
+    with fp.Engine(0) as eng:
+        for m in metrics:
+            with eng.instance(hg, w["K"], m, w["eps"]) as inst:
+                t = {}
+                st = {}
+                for where in ["device"] * (args.warmup + 1) + ["host"]:
+                    inst.set_stream(where)
+                    torch.cuda.synchronize()
+                    t0 = time.perf_counter()
+                    inst.initial_partition()
+                    torch.cuda.synchronize()
+                    t[where] = time.perf_counter() - t0
+                    if where == "device" and not inst.streamed_on_device():
+                        raise RuntimeError(f"{m}: the instance does not qualify for the device stream")
+                    st[where] = inst.get_state()
+                x = inst.stats()
+                per[m] = {"device_s": t["device"], "host_s": t["host"],
+                          "same": all(np.array_equal(st["device"][f], st["host"][f]) for f in fields),
+                          "windows": x["windows"], "whole_grid_windows": x["heavy_rounds"],
+                          "cut_size_flip": x["cut_size"], "cut_conflict": x["cut_conflict"]}
+    dev = sum(v["device_s"] for v in per.values())
+    host = sum(v["host_s"] for v in per.values())
+    line = {
+        "metric": "initial partition seconds (device stream; host stream beside it)", "value": dev, "unit": "s",
+        "n_gpus": 1, "steps": 1, "warmup": args.warmup, "ms_per_step": 1e3 * dev, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded generator)",
+        "config": {"workload": workload_text(args.config, w, hg.nov, hg.noe, hg.pins, 0, metrics, "degree"),
+                   "host_s": host, "per_metric": per,
+                   "same_as_host": all(v["same"] for v in per.values())},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_transforms(args):
+    """The hypergraph transforms on the device against their host forms:
+    createInverse (fp_create_inverse) and CN thinning (fp_thin_nets_device,
+    mean factor 2, 100 pins) on the workload, the BFS visiting order
+    (fp_bfs_order_device) on a 1 M-vertex Zipf hypergraph (the host BFS walks
+    every (vertex, net, pin) triple: hours at the workload's size).  Seconds on
+    the wall clock, host <-> device copies included; results compared."""
+    import torch
+    import fastpartitioner_gb300 as fp
+    torch.cuda.set_device(0)
+    w = WORKLOADS[args.config]
+    hg = fp.generate(spec_for(fp, w, args.scale))
+    g2 = fp.generate(fp.GenSpec.zipf(1_000_000 // args.scale, 1_000_000 // args.scale, 2.1, 2, 2000, beta=1.2,
+                                     seed=31))
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = fn()
+        torch.cuda.synchronize()
+        return r, time.perf_counter() - t0
+
+    def bfs(fn, *a):
+        """Raw call (a vertex left unreached is FP_ERR_UNSUPPORTED, with the
+        reached prefix of the ordering still written): (status, ordering)."""
+        import ctypes as C
+        out = np.empty(g2.nov, np.int32)
+        far = np.empty(2, np.int32)
+        v = g2.view()
+        rc = fn(*a, C.byref(v), 7, out.ctypes.data, far.ctypes.data)
+        return rc, out, far
+
+    out = {}
+    with fp.Engine(0) as eng:
+        for _ in range(args.warmup):
+            eng.create_inverse(hg.nov, hg.noe, hg.vptr, hg.vnets)
+        (rp, ci), td = timed(lambda: eng.create_inverse(hg.nov, hg.noe, hg.vptr, hg.vnets))
+        hv, th = timed(lambda: fp.Hypergraph.from_vertices(hg.nov, hg.noe, hg.vptr, hg.vnets))
+        out["create_inverse"] = {"device_s": td, "host_s": th, "pins": int(hg.pins),
+                                 "same": bool(np.array_equal(rp, hv.nptr) and np.array_equal(ci, hv.npins))}
+        a, td = timed(lambda: eng.thin(hg, 2, 100))
+        b, th = timed(lambda: hg.thin(2, 100))
+        out["thin_nets"] = {"device_s": td, "host_s": th, "kept_nets": int(a.noe),
+                            "same": all(np.array_equal(getattr(a, f), getattr(b, f))
+                                        for f in ("vptr", "vnets", "nptr", "npins", "src"))}
+        from fastpartitioner_gb300 import lib
+        (rd, od, fd), td = timed(lambda: bfs(lib().fp_bfs_order_device, eng._ctx))
+        (rh, oh, fh), th = timed(lambda: bfs(lib().fp_bfs_order))
+        out["bfs_order"] = {"device_s": td, "host_s": th, "nov": g2.nov, "pins": int(g2.pins),
+                            "reached": int((oh >= 0).sum()), "status": int(rh),
+                            "same": bool(rd == rh and np.array_equal(od, oh) and np.array_equal(fd, fh))}
+    line = {
+        "metric": "createInverse pins/s on the device (thinning and BFS ordering beside it)",
+        "value": hg.pins / out["create_inverse"]["device_s"], "unit": "pins/s", "n_gpus": 1, "steps": 1,
+        "warmup": args.warmup, "ms_per_step": 1e3 * out["create_inverse"]["device_s"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "uint32", "data": "synthetic (seeded generator)",
+        "config": {"workload": workload_text(args.config, w, hg.nov, hg.noe, hg.pins, 0, [], "degree"),
+                   "per_transform": out, "same_as_host": all(v["same"] for v in out.values())},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -669,8 +779,9 @@ def main():
     ap.add_argument("--cpu-passes", type=int, default=2,
                     help="cpu_baseline: passes of each metric's schedule (a bounded sample)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--mode", default="refine", choices=["refine", "batch", "serve"],
-                    help="refine: the pins/s line; batch / serve: the many-request runners")
+    ap.add_argument("--mode", default="refine", choices=["refine", "batch", "serve", "stream", "transforms"],
+                    help="refine: the pins/s line; batch / serve: the many-request runners; stream: device vs "
+                         "host initial partitions; transforms: device createInverse, thinning, BFS order")
     ap.add_argument("--batch-n", type=int, default=64)
     ap.add_argument("--batch-seed", type=int, default=0)
     ap.add_argument("--batch-passes", type=int, default=8)
@@ -686,6 +797,10 @@ def main():
         run_batch(args)
     elif args.mode == "serve":
         run_serve(args)
+    elif args.mode == "stream":
+        run_stream(args)
+    elif args.mode == "transforms":
+        run_transforms(args)
     elif args.impl == "reference":
         run_reference_arm(args)
     else:

@@ -136,6 +136,7 @@ def lib():
             "fp_set_decision_log": ([vp, i32], C.c_int),
             "fp_get_decisions": ([vp, vp, vp, vp, vp], C.c_int),
             "fp_set_classes": ([vp, i64, i64], C.c_int),
+            "fp_set_window": ([vp, i32, i32], C.c_int),
             "fp_metrics": ([vp, vp], C.c_int),
             "fp_get_partition": ([vp, vp], C.c_int),
             "fp_get_lists": ([vp, vp, vp, vp], C.c_int),
@@ -480,6 +481,10 @@ class Instance:
         """'auto' (speculative grid-wide engine where available) or 'sequential'
         (single-CTA walk); both give identical results."""
         _check(lib().fp_set_engine(self._h, {"auto": 0, "sequential": 1}[engine]), "fp_set_engine")
+
+    def set_window(self, min_len: int, grow: int) -> None:
+        """fp_set_window: window length after an early end (tuning only)."""
+        _check(lib().fp_set_window(self._h, int(min_len), int(grow)), "fp_set_window")
 
     def reset_state(self) -> None:
         """Uploads the host-side stream result again (host -> device)."""

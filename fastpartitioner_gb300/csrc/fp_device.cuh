@@ -74,6 +74,7 @@ struct StreamArgs {
   uint32_t* actm;         // [msg_wmax * words] source parts active on the position's nets
   uint32_t* ownm;         // [msg_wmax * words] parts listed on the nets the position is the source of
   int msg_wmax;
+  int walk;               // walk the changed decisions in the window (else cut at the first)
 };
 constexpr int kStreamHeavy = 4096;   // nets of a vertex the whole grid places in the device stream
 // List entries a position's evaluation may read (the sum of min(|e|, K) over
@@ -149,7 +150,8 @@ struct SpecBuf {
   int* hmisc;            // [2 * kMaxGridVerts * 8]
   unsigned long long* mlast;  // [K] TV: (window stamp << 32) | last position whose scan holds the part
   int gmax;              // whole-grid vertices one window may hold (1 .. kMaxGridVerts)
-  int wgrow;             // LDG window after a cut: this many times the last valid length
+  int wgrow;             // LDG window after a cut: this many times the last valid length,
+  int wmin;              //   at least this many positions
   int maxfix;            // in-window decision fixes per window (MSV / MSRV)
   // LDG engine positions: the vertices walked in windows, in visiting order.
   // When every vertex without nets weighs 0 they are left out of the

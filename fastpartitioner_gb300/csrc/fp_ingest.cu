@@ -196,37 +196,100 @@ __device__ __forceinline__ int lower_bound_items(const T* t, int n, T x) {
   return lo;
 }
 
+// Long segments: the chunks (kSortTile items) of all of them and then all
+// their items are spread over the grid.  lpre[i] / ipre[i]: chunks / items of
+// the long segments before list entry i (one thread fills them; the long
+// segments are few).
+__global__ void sort_long_prefix_kernel(const uint32_t* off, const int* lng, const int* cnt, int* lpre,
+                                        long long* ipre) {
+  const int nl = cnt[1];
+  int c = 0;
+  long long it = 0;
+  for (int i = 0; i < nl; i++) {
+    lpre[i] = c;
+    ipre[i] = it;
+    const uint32_t n = off[lng[i] + 1] - off[lng[i]];
+    c += (int)((n + kSortTile - 1) / kSortTile);
+    it += n;
+  }
+  lpre[nl] = c;
+  ipre[nl] = it;
+}
+
+// The list entry i with pre[i] <= x < pre[i + 1].
+template <class P>
+__device__ __forceinline__ int entry_of(const P* pre, int n, P x) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int m = (lo + hi + 1) >> 1;
+    if (pre[m] <= x) lo = m; else hi = m - 1;
+  }
+  return lo;
+}
+
 template <class T>
-__global__ void __launch_bounds__(kSortThreads) sort_long_kernel(T* a, T* tmp, const uint32_t* off, const int* lng,
-                                                                 const int* cnt) {
+__global__ void __launch_bounds__(kSortThreads) sort_long_chunks_kernel(T* a, const uint32_t* off, const int* lng,
+                                                                        const int* cnt, const int* lpre) {
   __shared__ T buf[kSortTile];
   const int nl = cnt[1];
-  for (int i = blockIdx.x; i < nl; i += gridDim.x) {
-    const int s = lng[i];
-    const uint32_t b = off[s];
-    const int n = (int)(off[s + 1] - b);
-    T* seg = a + b;
-    T* out = tmp + b;
-    for (int c0 = 0; c0 < n; c0 += kSortTile) {
-      const int m = min(kSortTile, n - c0);
-      for (int k = threadIdx.x; k < m; k += blockDim.x) buf[k] = seg[c0 + k];
-      cta_sort(buf, m);
-      for (int k = threadIdx.x; k < m; k += blockDim.x) seg[c0 + k] = buf[k];
-      __syncthreads();
-    }
-    for (int k = threadIdx.x; k < n; k += blockDim.x) {
-      const T x = seg[k];
-      const int c = k / kSortTile;
-      int r = k - c * kSortTile;
-      for (int c0 = 0; c0 < n; c0 += kSortTile)
-        if (c0 != c * kSortTile) r += lower_bound_items(seg + c0, min(kSortTile, n - c0), x);
-      out[r] = x;
-    }
-    __syncthreads();
-    for (int k = threadIdx.x; k < n; k += blockDim.x) seg[k] = out[k];
+  if (nl == 0) return;
+  const int nch = lpre[nl];
+  for (int g = blockIdx.x; g < nch; g += gridDim.x) {
+    const int i = entry_of(lpre, nl, g);
+    const uint32_t b = off[lng[i]];
+    const int n = (int)(off[lng[i] + 1] - b);
+    const int c0 = (g - lpre[i]) * kSortTile;
+    const int m = min(kSortTile, n - c0);
+    for (int k = threadIdx.x; k < m; k += blockDim.x) buf[k] = a[b + c0 + k];
+    cta_sort(buf, m);
+    for (int k = threadIdx.x; k < m; k += blockDim.x) a[b + c0 + k] = buf[k];
     __syncthreads();
   }
 }
+
+// Every item of a long segment to its rank: its index in its chunk plus the
+// items below it in each other chunk (binary searches; items are distinct).
+template <class T>
+__global__ void sort_long_rank_kernel(const T* a, T* tmp, const uint32_t* off, const int* lng, const int* cnt,
+                                      const long long* ipre) {
+  const int nl = cnt[1];
+  if (nl == 0) return;
+  const long long tot = ipre[nl];
+  for (long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x; x < tot;
+       x += (long long)gridDim.x * blockDim.x) {
+    const int i = entry_of(ipre, nl, x);
+    const uint32_t b = off[lng[i]];
+    const int n = (int)(off[lng[i] + 1] - b);
+    const int k = (int)(x - ipre[i]);
+    const T* seg = a + b;
+    const T v = seg[k];
+    const int c = k / kSortTile;
+    int r = k - c * kSortTile;
+    for (int c0 = 0; c0 < n; c0 += kSortTile)
+      if (c0 != c * kSortTile) r += lower_bound_items(seg + c0, min(kSortTile, n - c0), v);
+    tmp[b + r] = v;
+  }
+}
+
+template <class T>
+__global__ void sort_long_copy_kernel(T* a, const T* tmp, const uint32_t* off, const int* lng, const int* cnt,
+                                      const long long* ipre) {
+  const int nl = cnt[1];
+  if (nl == 0) return;
+  const long long tot = ipre[nl];
+  for (long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x; x < tot;
+       x += (long long)gridDim.x * blockDim.x) {
+    const int i = entry_of(ipre, nl, x);
+    const uint32_t b = off[lng[i]] + (uint32_t)(x - ipre[i]);
+    a[b] = tmp[b];
+  }
+}
+
+// List scratch of segmented_sort for nseg segments, in ints: the mid and long
+// lists, the long segments' chunk prefix (nseg + 1) and, 8-byte aligned, their
+// item prefix (nseg + 1 long longs).
+size_t sort_ipre_at(int nseg) { return (3 * (size_t)std::max(nseg, 1) + 2 + 1) & ~size_t(1); }
+size_t sort_list_ints(int nseg) { return sort_ipre_at(nseg) + 2 * ((size_t)std::max(nseg, 1) + 1); }
 
 template <class T>
 cudaError_t segmented_sort(T* a, T* tmp, const uint32_t* off, int nseg, int* lists, int* cnt, int num_sms,
@@ -234,12 +297,19 @@ cudaError_t segmented_sort(T* a, T* tmp, const uint32_t* off, int nseg, int* lis
   if (nseg <= 0) return cudaSuccess;
   cudaError_t e = cudaMemsetAsync(cnt, 0, sizeof(int) * 2, st);
   if (e != cudaSuccess) return e;
+  int* mid = lists;
+  int* lng = lists + nseg;
+  int* lpre = lists + 2 * (size_t)nseg;                                 // nseg + 1
+  long long* ipre = reinterpret_cast<long long*>(lists + sort_ipre_at(nseg));
   const int blocks = std::max(1, std::min((nseg + 7) / 8, num_sms * 16));
-  sort_small_kernel<T><<<blocks, 256, 0, st>>>(a, off, nseg, lists, lists + nseg, cnt);
+  sort_small_kernel<T><<<blocks, 256, 0, st>>>(a, off, nseg, mid, lng, cnt);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  sort_mid_kernel<T><<<num_sms * 2, kSortThreads, 0, st>>>(a, off, lists, cnt);
+  sort_mid_kernel<T><<<num_sms * 2, kSortThreads, 0, st>>>(a, off, mid, cnt);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  sort_long_kernel<T><<<num_sms * 2, kSortThreads, 0, st>>>(a, tmp, off, lists + nseg, cnt);
+  sort_long_prefix_kernel<<<1, 1, 0, st>>>(off, lng, cnt, lpre, ipre);
+  sort_long_chunks_kernel<T><<<num_sms * 2, kSortThreads, 0, st>>>(a, off, lng, cnt, lpre);
+  sort_long_rank_kernel<T><<<num_sms * 8, 256, 0, st>>>(a, tmp, off, lng, cnt, ipre);
+  sort_long_copy_kernel<T><<<num_sms * 8, 256, 0, st>>>(a, tmp, off, lng, cnt, ipre);
   return cudaGetLastError();
 }
 
@@ -295,36 +365,24 @@ __global__ void thin_nets_kernel(const uint32_t* nptr, const uint32_t* npins, co
   }
 }
 
-__global__ void thin_vcount_kernel(const uint32_t* vptr, const uint32_t* vnets, int nov, const uint32_t* keep,
-                                   uint32_t* vcnt) {
-  const int lane = threadIdx.x & 31;
-  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
-  for (int v = w; v < nov; v += nw) {
-    uint32_t c = 0;
-    for (uint32_t k = vptr[v] + lane; k < vptr[v + 1]; k += 32) c += keep[vnets[k]];
-    for (int off = 16; off; off >>= 1) c += __shfl_xor_sync(kAllLanes, c, off);
-    if (lane == 0) vcnt[v] = c;
+// Each vertex's kept nets, renumbered, in its own order: slot k of the
+// vertex -> nets CSR goes to the scan of the kept slots before it.
+__global__ void thin_slot_flags_kernel(const uint32_t* vnets, long long pins, const uint32_t* keep, uint32_t* sflag) {
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < pins; k += (long long)gridDim.x * blockDim.x)
+    sflag[k] = keep[vnets[k]];
+}
+
+__global__ void thin_slot_write_kernel(const uint32_t* vnets, long long pins, const uint32_t* keep,
+                                       const uint32_t* renum, const uint32_t* sscan, uint32_t* tvnets) {
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < pins;
+       k += (long long)gridDim.x * blockDim.x) {
+    const uint32_t e = vnets[k];
+    if (keep[e]) tvnets[sscan[k]] = renum[e];
   }
 }
 
-// Each vertex's kept nets, renumbered, in its own order (one warp per vertex,
-// ballot-compacted 32 nets at a time).
-__global__ void thin_vnets_kernel(const uint32_t* vptr, const uint32_t* vnets, int nov, const uint32_t* keep,
-                                  const uint32_t* renum, const uint32_t* tvptr, uint32_t* tvnets) {
-  const int lane = threadIdx.x & 31;
-  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
-  for (int v = w; v < nov; v += nw) {
-    uint32_t at = tvptr[v];
-    for (uint32_t k0 = vptr[v]; k0 < vptr[v + 1]; k0 += 32) {
-      const uint32_t k = k0 + lane;
-      const bool in = k < vptr[v + 1];
-      const uint32_t e = in ? vnets[k] : 0u;
-      const bool kp = in && keep[e];
-      const unsigned m = __ballot_sync(kAllLanes, kp);
-      if (kp) tvnets[at + __popc(m & ((1u << lane) - 1u))] = renum[e];
-      at += __popc(m);
-    }
-  }
+__global__ void thin_vptr_kernel(const uint32_t* vptr, int nov, const uint32_t* sscan, uint32_t* tvptr) {
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v <= nov; v += gridDim.x * blockDim.x) tvptr[v] = sscan[vptr[v]];
 }
 
 // ------------------------------------------------------------------------ BFS
@@ -343,7 +401,8 @@ struct BfsBuf {
   unsigned long long* sort_tmp;  // [nov]
   uint32_t* bucket;              // [nov + 1] reached vertices per frontier position, then offsets
   uint32_t* cursor;              // [nov]
-  int* lists;                    // [2 * nov]
+  uint32_t* foff;                // [nov + 1] nets of the frontier positions before each
+  int* lists;                    // [sort_list_ints(nov)]
   int* cnt;                      // [8]: [0,1] sort lists, [2] nets this level, [3] reached, [4] min id
   uint32_t* scan_tmp;
 };
@@ -362,34 +421,35 @@ __global__ void bfs_start_kernel(BfsBuf B, int nov, int noe, int s) {
   if (blockIdx.x == 0 && threadIdx.x == 0) B.frontier[0] = s;
 }
 
-// (a) every (frontier position i, net index k) pair bids for its net.
+// Nets per frontier position, scanned into foff (nf + 1) by the caller.
+__global__ void bfs_fdeg_kernel(BfsBuf B, const uint32_t* vptr, int nf) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i <= nf; i += gridDim.x * blockDim.x)
+    B.foff[i] = i < nf ? vptr[B.frontier[i] + 1] - vptr[B.frontier[i]] : 0u;
+}
+
+// (a) every (frontier position i, net index k) pair bids for its net; the
+// pairs are spread over the grid (a vertex may have millions of nets).
 __global__ void bfs_bid_kernel(BfsBuf B, const uint32_t* vptr, const uint32_t* vnets, int nf) {
-  const int lane = threadIdx.x & 31;
-  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
-  for (int i = w; i < nf; i += nw) {
-    const int v = B.frontier[i];
-    const uint32_t b = vptr[v], d = vptr[v + 1] - b;
-    for (uint32_t k = lane; k < d; k += 32) {
-      const uint32_t e = vnets[b + k];
-      if (!B.net_done[e]) atomicMin(&B.net_key[e], ((unsigned long long)i << 32) | k);
-    }
+  const uint32_t tot = B.foff[nf];
+  for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < tot; t += gridDim.x * blockDim.x) {
+    const int i = entry_of(B.foff, nf, t);
+    const uint32_t k = t - B.foff[i];
+    const uint32_t e = vnets[vptr[B.frontier[i]] + k];
+    if (!B.net_done[e]) atomicMin(&B.net_key[e], ((unsigned long long)i << 32) | k);
   }
 }
 
 // (b) the nets bid for this level, listed once: the bid of (i, k) for net e
 // wins iff net_key[e] == (i, k).
 __global__ void bfs_list_nets_kernel(BfsBuf B, const uint32_t* vptr, const uint32_t* vnets, int nf) {
-  const int lane = threadIdx.x & 31;
-  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
-  for (int i = w; i < nf; i += nw) {
-    const int v = B.frontier[i];
-    const uint32_t b = vptr[v], d = vptr[v + 1] - b;
-    for (uint32_t k = lane; k < d; k += 32) {
-      const uint32_t e = vnets[b + k];
-      if (!B.net_done[e] && B.net_key[e] == (((unsigned long long)i << 32) | k)) {
-        B.next_nets[atomicAdd(&B.cnt[2], 1)] = (int)e;
-        B.net_done[e] = 1;
-      }
+  const uint32_t tot = B.foff[nf];
+  for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < tot; t += gridDim.x * blockDim.x) {
+    const int i = entry_of(B.foff, nf, t);
+    const uint32_t k = t - B.foff[i];
+    const uint32_t e = vnets[vptr[B.frontier[i]] + k];
+    if (!B.net_done[e] && B.net_key[e] == (((unsigned long long)i << 32) | k)) {
+      B.next_nets[atomicAdd(&B.cnt[2], 1)] = (int)e;
+      B.net_done[e] = 1;
     }
   }
 }
@@ -548,7 +608,7 @@ int create_inverse_device(int device, cudaStream_t st, int num_sms, int nov, int
   uint32_t* npins = M.get<uint32_t>(pins);
   uint32_t* cursor = M.get<uint32_t>(noe);
   uint32_t* stmp = M.get<uint32_t>(scan_scratch((long long)noe + 1));
-  int* lists = M.get<int>(2 * (size_t)std::max(noe, 1));
+  int* lists = M.get<int>(sort_list_ints(noe));
   int* cnt = M.get<int>(8);
   uint32_t* sort_tmp = M.get<uint32_t>(pins);
   if (M.err != cudaSuccess) return status_of(M.err);
@@ -584,7 +644,8 @@ int thin_nets_device(int device, cudaStream_t st, int num_sms, const fp_hypergra
   int* tsrc = M.get<int>(noe);
   uint32_t* tvptr = M.get<uint32_t>((size_t)nov + 1);
   uint32_t* tvnets = M.get<uint32_t>(pins);
-  uint32_t* stmp = M.get<uint32_t>(scan_scratch((long long)std::max(noe, nov) + 1));
+  uint32_t* sscan = M.get<uint32_t>((size_t)pins + 1);   // kept slots of the vertex -> nets CSR, scanned
+  uint32_t* stmp = M.get<uint32_t>(scan_scratch(std::max<long long>(std::max(noe, nov), pins) + 1));
   if (M.err != cudaSuccess) return status_of(M.err);
   auto up = [&](void* d, const void* s, size_t bytes) {
     if (e == cudaSuccess && bytes) e = cudaMemcpyAsync(d, s, bytes, cudaMemcpyHostToDevice, st);
@@ -610,15 +671,18 @@ int thin_nets_device(int device, cudaStream_t st, int num_sms, const fp_hypergra
                                                                              toff, tpins, tsrc);
     e = cudaGetLastError();
   }
-  if (e == cudaSuccess) {
-    thin_vcount_kernel<<<grid_for((long long)nov * 32, num_sms), 256, 0, st>>>(vptr, vnets, nov, keep, tvptr);
+  if (e == cudaSuccess) e = cudaMemsetAsync(sscan + pins, 0, sizeof(uint32_t), st);
+  if (e == cudaSuccess && pins > 0) {
+    thin_slot_flags_kernel<<<grid_for(pins, num_sms), 256, 0, st>>>(vnets, pins, keep, sscan);
     e = cudaGetLastError();
   }
-  if (e == cudaSuccess) e = cudaMemsetAsync(tvptr + nov, 0, sizeof(uint32_t), st);
-  if (e == cudaSuccess) e = scan_exclusive(tvptr, tvptr, (long long)nov + 1, stmp, st);
+  if (e == cudaSuccess) e = scan_exclusive(sscan, sscan, pins + 1, stmp, st);
+  if (e == cudaSuccess && pins > 0) {
+    thin_slot_write_kernel<<<grid_for(pins, num_sms), 256, 0, st>>>(vnets, pins, keep, renum, sscan, tvnets);
+    e = cudaGetLastError();
+  }
   if (e == cudaSuccess) {
-    thin_vnets_kernel<<<grid_for((long long)nov * 32, num_sms), 256, 0, st>>>(vptr, vnets, nov, keep, renum, tvptr,
-                                                                              tvnets);
+    thin_vptr_kernel<<<grid_for((long long)nov + 1, num_sms), 256, 0, st>>>(vptr, nov, sscan, tvptr);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
@@ -668,7 +732,7 @@ int bfs_order_device(int device, cudaStream_t st, int num_sms, const fp_hypergra
   const size_t nmax = (size_t)std::max(nov, noe);
   uint32_t* cursor = M.get<uint32_t>(nmax);
   uint32_t* stmp = M.get<uint32_t>(scan_scratch((long long)nmax + 1));
-  int* lists = M.get<int>(2 * nmax);
+  int* lists = M.get<int>(sort_list_ints((int)nmax));
   uint32_t* sort32 = M.get<uint32_t>(pins);
   int* order = M.get<int>(nov);
   BfsBuf B{};
@@ -682,6 +746,7 @@ int bfs_order_device(int device, cudaStream_t st, int num_sms, const fp_hypergra
   B.items = M.get<unsigned long long>(nov);
   B.sort_tmp = M.get<unsigned long long>(nov);
   B.bucket = M.get<uint32_t>((size_t)nov + 1);
+  B.foff = M.get<uint32_t>((size_t)nov + 1);
   B.cursor = cursor;
   B.lists = lists;
   B.cnt = M.get<int>(8);
@@ -731,8 +796,11 @@ int bfs_order_device(int device, cudaStream_t st, int num_sms, const fp_hypergra
       if ((x = cudaMemsetAsync(B.bucket, 0, sizeof(uint32_t) * ((size_t)nf + 1), st)) != cudaSuccess) return x;
       if ((x = cudaMemsetAsync(B.cursor, 0, sizeof(uint32_t) * nf, st)) != cudaSuccess) return x;
       bfs_set_kernel<<<1, 1, 0, st>>>(B.cnt);
-      bfs_bid_kernel<<<grid_for((long long)nf * 32, num_sms), 256, 0, st>>>(B, vptr, vnets, nf);
-      bfs_list_nets_kernel<<<grid_for((long long)nf * 32, num_sms), 256, 0, st>>>(B, vptr, vnets, nf);
+      bfs_fdeg_kernel<<<grid_for((long long)nf + 1, num_sms), 256, 0, st>>>(B, vptr, nf);
+      if ((x = cudaGetLastError()) != cudaSuccess) return x;
+      if ((x = scan_exclusive(B.foff, B.foff, (long long)nf + 1, B.scan_tmp, st)) != cudaSuccess) return x;
+      bfs_bid_kernel<<<num_sms * 16, 256, 0, st>>>(B, vptr, vnets, nf);
+      bfs_list_nets_kernel<<<num_sms * 16, 256, 0, st>>>(B, vptr, vnets, nf);
       bfs_walk_kernel<<<num_sms * 8, 256, 0, st>>>(B, vptr, nptr, npins);
       bfs_reached_kernel<<<grid_for(nov, num_sms), 256, 0, st>>>(B, nov, level);
       if ((x = cudaGetLastError()) != cudaSuccess) return x;

@@ -1715,7 +1715,7 @@ __global__ void __launch_bounds__(kSThreads, 2) spec_ldg_kernel(DevInstance I, S
         if (end_w == pos + W) W = min(2 * W, B.wmax);
       } else {
         // regrow from the last valid length
-        W = max(256, min(B.wmax, B.wgrow * (cut - pos)));
+        W = min(B.wmax, max(B.wmin > 0 ? B.wmin : nwarps, B.wgrow * (cut - pos)));
       }
       pos = cut;
       round++;

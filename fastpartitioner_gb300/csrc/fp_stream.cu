@@ -205,7 +205,8 @@ __device__ __forceinline__ void place_net(const DevInstance& I, int e, int d, in
 // least-loaded part minpart when no part scores); writes cand, ncand, dec, wt
 // and the weight's mlist entry.  One warp; returns the decision.
 __device__ int decide_position(const DevInstance& I, const SpecBuf& B, const int* sizes_s, int minpart,
-                               const int* cnt, const unsigned long long* first, int o, int wv, int par) {
+                               const int* cnt, const unsigned long long* first, int o, int wv, int par,
+                               int* nc_out) {
   const int lane = threadIdx.x & 31;
   const int K = I.K;
   unsigned long long* cl = B.cand + (size_t)o * K;
@@ -224,13 +225,16 @@ __device__ int decide_position(const DevInstance& I, const SpecBuf& B, const int
   }
   best = warp_ldg_argmax(best);
   const int d = best.part >= 0 ? best.part : minpart;
+  *nc_out = nc;
   if (lane == 0) {
     B.ncand[o] = nc;
     B.dec[o] = d;
     B.wt[o] = wv;
+    B.flag[o] = 0;
     if (wv) {
       const int i = atomicAdd(&B.mcnt[par], 1);
       B.mlist[i] = make_int4(o, wv, d, 0);
+      B.midx[o] = i;
     }
   }
   __syncwarp();
@@ -239,17 +243,37 @@ __device__ int decide_position(const DevInstance& I, const SpecBuf& B, const int
 
 // The records of d in the nets [n0, n1) of a vertex (one warp) and the claims
 // of the nets d is appended to.
-__device__ void record_slots(const DevInstance& I, const SpecBuf& B, const StreamArgs& S, uint32_t base, int n0,
-                             int n1, int d, int round, int z, int* sd) {
+// With claim_all every net is claimed (and counted as appended to): any
+// other decision's appends are then a subset.
+__device__ int record_slots(const DevInstance& I, const SpecBuf& B, const StreamArgs& S, uint32_t base, int n0,
+                            int n1, int d, int round, int z, int* sd, bool claim_all) {
   const int lane = threadIdx.x & 31;
+  int napp = 0;
   for (int nb = n0; nb < n1; nb += 32) {
     const int j = locate_part(I, base, nb, n1, d, sd);
     const int k = nb + lane;
+    const bool app = k < n1 && (j < 0 || claim_all);
     if (k < n1) {
       S.rec[base + k] = j >= 0 ? (uint32_t)j : kNoSlot;
-      if (j < 0) atomicMax(&B.claim64[(int)__ldg(&I.vnets[base + k])], skey(round, z));
+      if (app) atomicMax(&B.claim64[(int)__ldg(&I.vnets[base + k])], skey(round, z));
     }
+    napp += __popc(__ballot_sync(kAll, app));
   }
+  return napp;   // every lane
+}
+
+// Nets of window offset o listing part d (its candidate entry's count; 0 if d
+// is not a candidate).  One warp.
+__device__ int cand_count(const SpecBuf& B, int K, int o, int d) {
+  const int lane = threadIdx.x & 31;
+  const unsigned long long* cl = B.cand + (size_t)o * K;
+  const int nc = lds(&B.ncand[o]);
+  int c = 0;
+  for (int i = lane; i < nc; i += 32) {
+    const unsigned long long ent = lds(&cl[i]);
+    if ((int)(ent >> 52) == d) c = (int)((ent >> 36) & 0xffffull);
+  }
+  return warp_max(c);
 }
 
 // The vertices without nets [k0, k1) of the iso list take the least-loaded
@@ -271,7 +295,7 @@ __global__ void __launch_bounds__(kSThreads, 1) stream_ldg_kernel(DevInstance I,
   barrier_start();
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ unsigned long long uscr[kSWarps];
-  __shared__ int s_minpart, s_minsize, s_second, s_dec;
+  __shared__ int s_minpart, s_minsize, s_second, s_dec, s_napp, s_nc;
   const int K = I.K;
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int gw = blockIdx.x * kSWarps + wib;
@@ -387,8 +411,9 @@ __global__ void __launch_bounds__(kSThreads, 1) stream_ldg_kernel(DevInstance I,
         B.hcnt[p] = 0;
         B.hfirst[p] = ~0ull;
       }
-      if (gtid == 0) {   // the next round's cut word and placements, as a window leaves them
+      if (gtid == 0) {   // the next round's cut words and placements, as a window leaves them
         B.ctl[4 + (par ^ 1)] = kNone;
+        B.ctl[2 + (par ^ 1)] = kNone;
         B.mcnt[par ^ 1] = 0;
       }
       pos++;
@@ -418,8 +443,12 @@ __global__ void __launch_bounds__(kSThreads, 1) stream_ldg_kernel(DevInstance I,
       __syncwarp();
       for (int nb = 0; nb < deg; nb += 32) tally_stream(I, cn, base, nb, deg, cnt, first);
       __syncwarp();
-      const int d = decide_position(I, B, sizes_s, s_minpart, cnt, first, o, __ldg(&I.w[v]), par);
-      record_slots(I, B, S, base, 0, deg, d, round, z, sd);
+      int nc;
+      const int d = decide_position(I, B, sizes_s, s_minpart, cnt, first, o, __ldg(&I.w[v]), par, &nc);
+      // CN: a position without candidates decides by the sizes alone; it
+      // claims all its nets, so that a changed decision adds no claim
+      const int napp = record_slots(I, B, S, base, 0, deg, d, round, z, sd, cn && nc == 0);
+      if (lane == 0) B.slack[o] = napp;   // nets the decision appends to
       __syncwarp();
     }
     if (S.nmid) {
@@ -451,20 +480,36 @@ __global__ void __launch_bounds__(kSThreads, 1) stream_ldg_kernel(DevInstance I,
         }
         __syncthreads();
         if (wib == 0) {
-          const int d = decide_position(I, B, sizes_s, s_minpart, cnt_b, first_b, o, __ldg(&I.w[v]), par);
-          if (lane == 0) s_dec = d;
+          int nc;
+          const int d = decide_position(I, B, sizes_s, s_minpart, cnt_b, first_b, o, __ldg(&I.w[v]), par, &nc);
+          if (lane == 0) {
+            s_dec = d;
+            s_nc = nc;
+          }
         }
+        if (threadIdx.x == 0) s_napp = 0;
         __syncthreads();
-        record_slots(I, B, S, base, n0, n1, s_dec, round, z, sd);
+        const int napp = record_slots(I, B, S, base, n0, n1, s_dec, round, z, sd, cn && s_nc == 0);
+        if (lane == 0) atomicAdd(&s_napp, napp);
+        __syncthreads();
+        if (threadIdx.x == 0) B.slack[o] = s_napp;
       }
     }
     if (!grid_barrier(B.bar, I.status)) return;
     lap(16);
-    // ---- B: validate
+    // ---- B: validate.  B1 (every warp): the first position with a claim
+    // conflict, and the first whose decision changes with the exact sizes
+    // (or needs a TV part above max_pw) if every earlier one keeps its own.
+    // B2 (one warp, only if such a change comes before the first conflict):
+    // walk the positions from it in order with exact sizes, taking each
+    // changed decision whose appends are a subset of the old one's (no new
+    // claims), and end the window at the first change that is not -- that
+    // position commits last, with its exact decision -- or at the conflict.
     int* const cut_w = &B.ctl[4 + par];
+    int* const flip_w = &B.ctl[2 + par];
+    const int cz0 = min(pos + blockIdx.x * kSWarps * q, end_w);
+    const int cta_o0 = cz0 - pos;
     {
-      const int cz0 = min(pos + blockIdx.x * kSWarps * q, end_w);
-      const int cta_o0 = cz0 - pos;
       for (int p = threadIdx.x; p < K; p += blockDim.x) dsz_cta[p] = 0;
       __syncthreads();
       const int nm = lds(&B.mcnt[par]);
@@ -473,6 +518,7 @@ __global__ void __launch_bounds__(kSThreads, 1) stream_ldg_kernel(DevInstance I,
         if (m.x < cta_o0) atomicAdd(&dsz_cta[m.z], m.y);
       }
       __syncthreads();
+      bool decided = false;   // this warp found its first change: later ones only check conflicts
       for (int z = z0; z < z1; z++) {
         const int o = z - pos;
         const int v = __ldg(&S.porder[z]);
@@ -481,49 +527,151 @@ __global__ void __launch_bounds__(kSThreads, 1) stream_ldg_kernel(DevInstance I,
         bool conf = false;
         for (int k = lane; k < deg && !conf; k += 32)
           conf = claimed_before(B, round, (int)__ldg(&I.vnets[base + k]), z);
-        int why = __any_sync(kAll, conf) ? 5 : 0;
-        if (!why) {
-          // the exact sizes here: the window-start sizes, the placements before
-          // this CTA's positions, those of this CTA's positions before z
-          int* dsz = cnt;
-          for (int p = lane; p < K; p += 32) dsz[p] = dsz_cta[p];
-          __syncwarp();
-          for (int o2 = cta_o0 + lane; o2 < o; o2 += 32) {
-            const int w = lds(&B.wt[o2]);
-            if (w) atomicAdd(&dsz[lds(&B.dec[o2])], w);
-          }
-          __syncwarp();
-          int d2 = pick_entries(I, B.cand + (size_t)o * K, lds(&B.ncand[o]), sizes_s, dsz);
-          if (d2 < 0) d2 = least_loaded(sizes_s, dsz, K);
-          if (d2 != lds(&B.dec[o])) {
-            why = 2;   // a size flip: the window commits this position with d2 as its last
-            if (lane == 0) B.dfix[o] = d2;
-          }
-          if (tv && sizes_s[d2] + dsz[d2] > I.max_pw) why = 7;   // unsupported, reported at commit
-          __syncwarp();
-        }
-        if (why) {
-          if (lane == 0) atomicMin(cut_w, (z << 3) | why);
+        if (__any_sync(kAll, conf)) {
+          if (lane == 0) atomicMin(cut_w, (z << 3) | 5);
           break;
         }
+        if (decided) continue;
+        // the exact sizes here if no earlier decision changes: the window-start
+        // sizes, the placements before this CTA's positions, those of this
+        // CTA's positions before z
+        int* dsz = cnt;
+        for (int p = lane; p < K; p += 32) dsz[p] = dsz_cta[p];
+        __syncwarp();
+        for (int o2 = cta_o0 + lane; o2 < o; o2 += 32) {
+          const int w = lds(&B.wt[o2]);
+          if (w) atomicAdd(&dsz[lds(&B.dec[o2])], w);
+        }
+        __syncwarp();
+        int d2 = pick_entries(I, B.cand + (size_t)o * K, lds(&B.ncand[o]), sizes_s, dsz);
+        if (d2 < 0) d2 = least_loaded(sizes_s, dsz, K);
+        const bool clamp = tv && sizes_s[d2] + dsz[d2] > I.max_pw;
+        if (d2 != lds(&B.dec[o]) || clamp) {
+          if (lane == 0) {
+            B.dfix[o] = d2;
+            atomicMin(flip_w, (z << 3) | (clamp ? 7 : 2));
+          }
+          decided = true;
+        }
+        __syncwarp();
       }
     }
     if (!grid_barrier(B.bar, I.status)) return;
     lap(17);
-    const int cutw = lds(cut_w);
-    int cut = cutw == kNone ? end_w : min(cutw >> 3, end_w);
-    // a size flip at the cut: its lists are exact (no earlier append to its
-    // nets), so it commits with its exact decision after the others
-    const bool flip = cutw != kNone && (cutw & 7) == 2;
-    const int cutc = flip ? cut + 1 : cut;
-    if (cutw != kNone && (cutw & 7) == 7 && (cutw >> 3) == pos) {
-      // the window's first position needs a part above max_pw: the reference
-      // would place it in part -1
-      if (gtid == 0) dev_fail(I.status, kDevErrUnsupported);
-      return;
+    const int cutw = lds(cut_w), flipw = lds(flip_w);
+    const int zc = cutw == kNone ? end_w : min(cutw >> 3, end_w);
+    const int zf = flipw == kNone ? end_w : min(flipw >> 3, end_w);
+    int cut = zc, cutc = zc;
+    if (zf < zc && !S.walk) {
+      // the first change ends the window: it commits last with its exact
+      // decision (a TV clamp does not commit)
+      cut = zf;
+      cutc = (flipw & 7) == 2 ? zf + 1 : zf;
+    } else if (zf < zc) {
+      if (blockIdx.x == 0 && wib == 0) {
+        int* sz = cnt;
+        for (int p = lane; p < K; p += 32) sz[p] = sizes_s[p];
+        __syncwarp();
+        const int nm = lds(&B.mcnt[par]);
+        for (int i = lane; i < nm; i += 32) {
+          const int4 m = lds(&B.mlist[i]);
+          if (m.x < zf - pos) atomicAdd(&sz[m.z], m.y);
+        }
+        __syncwarp();
+        int c1 = zc, c2 = zc;
+        bool stop = false;
+        // 32 positions at a time: their scalar words one per lane, and the
+        // next position's first 32 candidates loaded while one is decided
+        for (int zb = zf; zb < zc && !stop; zb += 32) {
+          const int zl = zb + lane, ol = zl - pos;
+          const bool in = zl < zc;
+          const int nc_l = in ? lds(&B.ncand[ol]) : 0;
+          const int d_l = in ? lds(&B.dec[ol]) : 0;
+          const int w_l = in ? lds(&B.wt[ol]) : 0;
+          const int na_l = in ? lds(&B.slack[ol]) : 0;
+          int deg_l = 0;
+          if (in) {
+            const int v = __ldg(&S.porder[zl]);
+            deg_l = (int)(__ldg(&I.vptr[v + 1]) - __ldg(&I.vptr[v]));
+          }
+          const int nb = min(32, zc - zb);
+          unsigned long long ent = 0;
+          {
+            const int nc0 = __shfl_sync(kAll, nc_l, 0);
+            if (lane < nc0) ent = lds(&B.cand[(size_t)(zb - pos) * K + lane]);
+          }
+          for (int j = 0; j < nb; j++) {
+            const int z = zb + j, o = z - pos;
+            const int nc = __shfl_sync(kAll, nc_l, j);
+            const int d = __shfl_sync(kAll, d_l, j);
+            const int w = __shfl_sync(kAll, w_l, j);
+            const int napp = __shfl_sync(kAll, na_l, j);
+            const int deg = __shfl_sync(kAll, deg_l, j);
+            const int ncn = __shfl_sync(kAll, nc_l, (j + 1) & 31);
+            unsigned long long ent_next = 0;
+            if (j + 1 < nb && lane < ncn) ent_next = lds(&B.cand[(size_t)(o + 1) * K + lane]);
+            LdgKey best{-1.0, 0, -1, ~0ull};
+            for (int i = lane; i < nc; i += 32) {
+              const unsigned long long e = i < 32 ? ent : lds(&B.cand[(size_t)o * K + i]);
+              const int p = (int)(e >> 52);
+              const int c = (int)((e >> 36) & 0xffffull);
+              const unsigned long long f = (((e >> 20) & 0xffffull) << 32) | (e & 0xfffffull);
+              const LdgKey k{ldg_score(c, sz[p], I.C), sz[p], p, f};
+              if (ldg_better(k, best)) best = k;
+            }
+            best = warp_ldg_argmax(best);
+            const int d2 = best.part >= 0 ? best.part : least_loaded(sz, nullptr, K);
+            ent = ent_next;
+            if (tv && sz[d2] > I.max_pw) {   // the reference would use part -1
+              c1 = c2 = z;
+              stop = true;
+              break;
+            }
+            if (d2 != d) {
+              // the old decision appended to every net, or the new one to none
+              const bool safe = napp == deg || (!cn && cand_count(B, K, o, d2) == deg);
+              if (!safe) {
+                if (lane == 0) B.dfix[o] = d2;
+                c1 = z;
+                c2 = z + 1;
+                stop = true;
+                break;
+              }
+              if (lane == 0) {
+                B.dec[o] = d2;
+                B.flag[o] = 1;   // its records are d's: located again at commit
+                if (w) B.mlist[lds(&B.midx[o])].z = d2;
+                B.stats[9]++;
+              }
+            }
+            __syncwarp();
+            if (lane == 0 && w) sz[d2] += w;
+            __syncwarp();
+          }
+        }
+        if (lane == 0) {
+          B.ctl[6] = c1;
+          B.ctl[7] = c2;
+        }
+      }
+      if (!grid_barrier(B.bar, I.status)) return;
+      lap(20);
+      cut = lds(&B.ctl[6]);
+      cutc = lds(&B.ctl[7]);
+      // the placements before each CTA's positions, with the changed decisions
+      for (int p = threadIdx.x; p < K; p += blockDim.x) dsz_cta[p] = 0;
+      __syncthreads();
+      const int nm = lds(&B.mcnt[par]);
+      for (int i = threadIdx.x; i < nm; i += blockDim.x) {
+        const int4 m = lds(&B.mlist[i]);
+        if (m.x < cta_o0) atomicAdd(&dsz_cta[m.z], m.y);
+      }
+      __syncthreads();
     }
     if (cut <= pos) {
-      if (gtid == 0) dev_fail(I.status, kDevErrInvalid);
+      // the window's first position needs a part above max_pw: the reference
+      // would place it in part -1
+      if (gtid == 0) dev_fail(I.status, tv ? kDevErrUnsupported : kDevErrInvalid);
       return;
     }
     // ---- C: commit the positions before the cut (and a flip at the cut)
@@ -533,7 +681,7 @@ __global__ void __launch_bounds__(kSThreads, 1) stream_ldg_kernel(DevInstance I,
       const uint32_t base = __ldg(&I.vptr[v]);
       const int deg = (int)(__ldg(&I.vptr[v + 1]) - base);
       const int d = z == cut ? lds(&B.dfix[o]) : lds(&B.dec[o]);
-      if (z == cut) {
+      if (z == cut || lds(&B.flag[o])) {
         for (int nb = 0; nb < deg; nb += 32) {
           const int j = locate_part(I, base, nb, deg, d, sd);
           if (nb + lane < deg) place_net(I, (int)__ldg(&I.vnets[base + nb + lane]), d, j);
@@ -584,12 +732,14 @@ __global__ void __launch_bounds__(kSThreads, 1) stream_ldg_kernel(DevInstance I,
     }
     if (gw == 0 && lane == 0) {
       B.ctl[4 + (par ^ 1)] = kNone;
+      B.ctl[2 + (par ^ 1)] = kNone;
       B.mcnt[par ^ 1] = 0;
     }
     if (stats) {
       B.stats[0]++;
       B.stats[2] += cutc - pos;
-      if (cutw != kNone) B.stats[(cutw & 7) == 2 ? 5 : 8]++;
+      if (cutc > cut) B.stats[5]++;                       // a change with new appends
+      else if (cut < end_w) B.stats[8]++;                 // a conflict
     }
     if (cutc >= end_w) {
       if (end_w == pos + W) W = min(2 * W, B.wmax);
@@ -685,14 +835,21 @@ __device__ __forceinline__ MsgKey warp_msg_best(MsgKey x) {
 
 // Messages part k saves for the active parts `act` and the own-net parts
 // `own` with multiplicities `mult` (conn > 0 masks prow / pcol).
-__device__ __forceinline__ int msg_saved(const StreamArgs& S, int K, int words, int k, const uint32_t* act,
-                                         const uint32_t* own, const int* mult) {
+// The masks are read from shared memory (a copy staged at the round start)
+// when kStaged, else from global memory past L1.
+constexpr int kMsgStageK = 256;
+template <bool kStaged>
+__device__ __forceinline__ uint32_t mask_word(const uint32_t* p) { return kStaged ? *p : __ldcg(p); }
+
+template <bool kStaged>
+__device__ __forceinline__ int msg_saved(const uint32_t* prow, const uint32_t* pcol, int words, int k,
+                                         const uint32_t* act, const uint32_t* own, const int* mult) {
   int sv = 0;
-  const uint32_t* col = S.pcol + (size_t)k * words;
-  const uint32_t* row = S.prow + (size_t)k * words;
+  const uint32_t* col = pcol + (size_t)k * words;
+  const uint32_t* row = prow + (size_t)k * words;
   for (int w = 0; w < words; w++) {
-    sv += __popc(act[w] & __ldcg(&col[w]));
-    uint32_t x = own[w] & __ldcg(&row[w]);
+    sv += __popc(act[w] & mask_word<kStaged>(&col[w]));
+    uint32_t x = own[w] & mask_word<kStaged>(&row[w]);
     while (x) {
       const int b = __ffs(x) - 1;
       x &= x - 1;
@@ -728,9 +885,10 @@ __device__ void msg_scan_nets(const DevInstance& I, int v, uint32_t base, int n0
 
 // Records of v's nets [n0, n1) for decision d (slot, source part, own net)
 // and, with claim, the claims of the nets v appends to or is the source of.
-__device__ void msg_records(const DevInstance& I, const SpecBuf& B, const StreamArgs& S, int v, uint32_t base,
-                            int n0, int n1, int d, bool claim, int round, int z, int* sd) {
+__device__ int msg_records(const DevInstance& I, const SpecBuf& B, const StreamArgs& S, int v, uint32_t base,
+                           int n0, int n1, int d, bool claim, int round, int z, int* sd) {
   const int lane = threadIdx.x & 31;
+  int napp = 0;
   for (int nb = n0; nb < n1; nb += 32) {
     const int j = locate_part(I, base, nb, n1, d, sd);
     const int k = nb + lane;
@@ -742,7 +900,9 @@ __device__ void msg_records(const DevInstance& I, const SpecBuf& B, const Stream
       S.rec[base + k] = mrec(j, sp, own);
       if (claim && (j < 0 || own)) atomicMax(&B.claim64[e], skey(round, z));
     }
+    napp += __popc(__ballot_sync(kAll, k < n1 && j < 0));
   }
+  return napp;   // nets d is appended to, every lane
 }
 
 // The entries position z (decision d) makes positive, by the window-start
@@ -822,6 +982,9 @@ __global__ void __launch_bounds__(kSThreads, 2) stream_msg_kernel(DevInstance I,
   int* cb = cv.take<int>(K);                           // CTA: zero-start flags
   uint32_t* cact = cv.take<uint32_t>(words);
   uint32_t* cown = cv.take<uint32_t>(words);
+  const bool staged = K <= kMsgStageK;
+  uint32_t* sprow = cv.take<uint32_t>(staged ? (size_t)K * words : 0);   // the round's conn > 0 masks
+  uint32_t* spcol = cv.take<uint32_t>(staged ? (size_t)K * words : 0);
   int* wa = a_b + (size_t)wib * K;
   int* wb = b_b + (size_t)wib * K;
   uint32_t* wact = act_b + (size_t)wib * words;
@@ -842,6 +1005,11 @@ __global__ void __launch_bounds__(kSThreads, 2) stream_msg_kernel(DevInstance I,
   while (pos < S.npos) {
     const int par = round & 1;
     for (int p = threadIdx.x; p < K; p += blockDim.x) sizes_s[p] = lds(&I.part_sizes[p]);
+    if (staged)
+      for (int x = threadIdx.x; x < K * words; x += blockDim.x) {
+        sprow[x] = __ldcg(&S.prow[x]);
+        spcol[x] = __ldcg(&S.pcol[x]);
+      }
     __syncthreads();
     block_min_part(sizes_s, K, uscr, &s_minpart, &s_minsize, &s_second);
     __syncthreads();
@@ -861,7 +1029,8 @@ __global__ void __launch_bounds__(kSThreads, 2) stream_msg_kernel(DevInstance I,
         __syncthreads();
         MsgKey best{0, 0, -1};
         for (int k = threadIdx.x; k < K; k += blockDim.x) {
-          const int sv = msg_saved(S, K, words, k, cact, cown, ca);
+          const int sv = staged ? msg_saved<true>(sprow, spcol, words, k, cact, cown, ca)
+                                : msg_saved<false>(S.prow, S.pcol, words, k, cact, cown, ca);
           if ((double)sizes_s[k] < I.C) {
             const MsgKey c{sv, sizes_s[k], k};
             if (msg_better(c, best)) best = c;
@@ -928,6 +1097,7 @@ __global__ void __launch_bounds__(kSThreads, 2) stream_msg_kernel(DevInstance I,
       }
       if (gtid == 0) {
         B.ctl[4 + (par ^ 1)] = kNone;
+        B.ctl[2 + (par ^ 1)] = kNone;
         B.mcnt[par ^ 1] = 0;
       }
       for (int p = gtid; p < K; p += gridDim.x * blockDim.x) {
@@ -963,7 +1133,8 @@ __global__ void __launch_bounds__(kSThreads, 2) stream_msg_kernel(DevInstance I,
       MsgKey best{0, 0, -1};
       int* sv_out = S.saved + (size_t)o * K;
       for (int k = lane; k < K; k += 32) {
-        const int sv = msg_saved(S, K, words, k, wact, wown, wa);
+        const int sv = staged ? msg_saved<true>(sprow, spcol, words, k, wact, wown, wa)
+                              : msg_saved<false>(S.prow, S.pcol, words, k, wact, wown, wa);
         sv_out[k] = sv;
         if ((double)sizes_s[k] < I.C) {
           const MsgKey c{sv, sizes_s[k], k};
@@ -972,7 +1143,7 @@ __global__ void __launch_bounds__(kSThreads, 2) stream_msg_kernel(DevInstance I,
       }
       best = warp_msg_best(best);
       const int d = best.k >= 0 ? best.k : s_minpart;
-      msg_records(I, B, S, v, base, 0, deg, d, true, round, z, sd);
+      const int napp = msg_records(I, B, S, v, base, 0, deg, d, true, round, z, sd);
       msg_mark_new(S, K, words, par, z, d, wact, wown);
       for (int x = lane; x < words; x += 32) {
         S.actm[(size_t)o * words + x] = wact[x];
@@ -982,17 +1153,29 @@ __global__ void __launch_bounds__(kSThreads, 2) stream_msg_kernel(DevInstance I,
       if (lane == 0) {
         B.dec[o] = d;
         B.wt[o] = wv;
-        if (wv) B.mlist[atomicAdd(&B.mcnt[par], 1)] = make_int4(o, wv, d, 0);
+        B.flag[o] = 0;
+        B.slack[o] = napp;
+        if (wv) {
+          const int i = atomicAdd(&B.mcnt[par], 1);
+          B.mlist[i] = make_int4(o, wv, d, 0);
+          B.midx[o] = i;
+        }
       }
       __syncwarp();
     }
     if (!grid_barrier(B.bar, I.status)) return;
     lap(16);
-    // ---- B: validate
+    // ---- B: validate, as in the LDG stream: B1 finds the first conflict
+    // (claims, or a row / column an earlier position makes positive) and the
+    // first decision that changes with the exact sizes; B2 walks from that
+    // change to the conflict on one warp, taking each change whose appends are
+    // a subset of the old decision's, and stopping at a position that reads a
+    // row or column a taken change makes positive.
     int* const cut_w = &B.ctl[4 + par];
+    int* const flip_w = &B.ctl[2 + par];
+    const int cz0 = min(pos + blockIdx.x * kSWarps * q, end_w);
+    const int cta_o0 = cz0 - pos;
     {
-      const int cz0 = min(pos + blockIdx.x * kSWarps * q, end_w);
-      const int cta_o0 = cz0 - pos;
       for (int p = threadIdx.x; p < K; p += blockDim.x) dsz_cta[p] = 0;
       __syncthreads();
       const int nm = lds(&B.mcnt[par]);
@@ -1001,6 +1184,7 @@ __global__ void __launch_bounds__(kSThreads, 2) stream_msg_kernel(DevInstance I,
         if (m.x < cta_o0) atomicAdd(&dsz_cta[m.z], m.y);
       }
       __syncthreads();
+      bool decided = false;
       for (int z = z0; z < z1; z++) {
         const int o = z - pos;
         const int v = __ldg(&S.porder[z]);
@@ -1013,45 +1197,178 @@ __global__ void __launch_bounds__(kSThreads, 2) stream_msg_kernel(DevInstance I,
           if (bit_of(S.actm + (size_t)o * words, k) && lds(&S.rowpos[par * K + k]) < z) conf = true;
           if (bit_of(S.ownm + (size_t)o * words, k) && lds(&S.colpos[par * K + k]) < z) conf = true;
         }
-        int why = __any_sync(kAll, conf) ? 5 : 0;
-        if (!why) {
-          int* dsz = wa;
-          for (int p = lane; p < K; p += 32) dsz[p] = dsz_cta[p];
-          __syncwarp();
-          for (int o2 = cta_o0 + lane; o2 < o; o2 += 32) {
-            const int w = lds(&B.wt[o2]);
-            if (w) atomicAdd(&dsz[lds(&B.dec[o2])], w);
-          }
-          __syncwarp();
-          MsgKey best{0, 0, -1};
-          const int* sv_in = S.saved + (size_t)o * K;
-          for (int k = lane; k < K; k += 32) {
-            const int sz = sizes_s[k] + dsz[k];
-            if ((double)sz < I.C) {
-              const MsgKey c{lds(&sv_in[k]), sz, k};
-              if (msg_better(c, best)) best = c;
-            }
-          }
-          best = warp_msg_best(best);
-          const int d2 = best.k >= 0 ? best.k : least_loaded(sizes_s, dsz, K);
-          if (d2 != lds(&B.dec[o])) {
-            why = 2;
-            if (lane == 0) B.dfix[o] = d2;
-          }
-          __syncwarp();
-        }
-        if (why) {
-          if (lane == 0) atomicMin(cut_w, (z << 3) | why);
+        if (__any_sync(kAll, conf)) {
+          if (lane == 0) atomicMin(cut_w, (z << 3) | 5);
           break;
         }
+        if (decided) continue;
+        int* dsz = wa;
+        for (int p = lane; p < K; p += 32) dsz[p] = dsz_cta[p];
+        __syncwarp();
+        for (int o2 = cta_o0 + lane; o2 < o; o2 += 32) {
+          const int w = lds(&B.wt[o2]);
+          if (w) atomicAdd(&dsz[lds(&B.dec[o2])], w);
+        }
+        __syncwarp();
+        MsgKey best{0, 0, -1};
+        const int* sv_in = S.saved + (size_t)o * K;
+        for (int k = lane; k < K; k += 32) {
+          const int sz = sizes_s[k] + dsz[k];
+          if ((double)sz < I.C) {
+            const MsgKey c{lds(&sv_in[k]), sz, k};
+            if (msg_better(c, best)) best = c;
+          }
+        }
+        best = warp_msg_best(best);
+        const int d2 = best.k >= 0 ? best.k : least_loaded(sizes_s, dsz, K);
+        if (d2 != lds(&B.dec[o])) {
+          if (lane == 0) atomicMin(flip_w, (z << 3) | 2);
+          decided = true;
+        }
+        __syncwarp();
       }
     }
     if (!grid_barrier(B.bar, I.status)) return;
     lap(17);
-    const int cutw = lds(cut_w);
-    const int cut = cutw == kNone ? end_w : min(cutw >> 3, end_w);
-    const bool flip = cutw != kNone && (cutw & 7) == 2;
-    const int cutc = flip ? cut + 1 : cut;
+    const int cutw = lds(cut_w), flipw = lds(flip_w);
+    const int zc = cutw == kNone ? end_w : min(cutw >> 3, end_w);
+    const int zf = flipw == kNone ? end_w : min(flipw >> 3, end_w);
+    int cut = zc, cutc = zc;
+    if (zf < zc) {
+      if (blockIdx.x == 0 && wib == 0) {
+        int* sz = wa;
+        uint32_t* rows_new = wact;   // rows / columns a taken change makes positive
+        uint32_t* cols_new = wown;
+        for (int p = lane; p < K; p += 32) sz[p] = sizes_s[p];
+        for (int x = lane; x < words; x += 32) { rows_new[x] = 0; cols_new[x] = 0; }
+        __syncwarp();
+        const int nm = lds(&B.mcnt[par]);
+        for (int i = lane; i < nm; i += 32) {
+          const int4 m = lds(&B.mlist[i]);
+          if (m.x < zf - pos) atomicAdd(&sz[m.z], m.y);
+        }
+        __syncwarp();
+        int c1 = zc, c2 = zc;
+        bool stop = false;
+        constexpr int kSv = kMsgStageK / 32;   // saved values a lane prefetches (K <= kMsgStageK)
+        // 32 positions at a time: their scalar words one per lane; the next
+        // position's saved messages loaded while one is decided (K <= 256)
+        for (int zb = zf; zb < zc && !stop; zb += 32) {
+          const int zl = zb + lane, ol = zl - pos;
+          const bool in = zl < zc;
+          const int d_l = in ? lds(&B.dec[ol]) : 0;
+          const int w_l = in ? lds(&B.wt[ol]) : 0;
+          const int na_l = in ? lds(&B.slack[ol]) : 0;
+          int deg_l = 0;
+          if (in) {
+            const int v = __ldg(&S.porder[zl]);
+            deg_l = (int)(__ldg(&I.vptr[v + 1]) - __ldg(&I.vptr[v]));
+          }
+          const int nb = min(32, zc - zb);
+          int sv[kSv], svn[kSv];
+#pragma unroll
+          for (int u = 0; u < kSv; u++) {
+            const int k = lane + 32 * u;
+            sv[u] = staged && k < K ? lds(&S.saved[(size_t)(zb - pos) * K + k]) : 0;
+          }
+          for (int j = 0; j < nb; j++) {
+            const int z = zb + j, o = z - pos;
+            const int d = __shfl_sync(kAll, d_l, j);
+            const int w = __shfl_sync(kAll, w_l, j);
+            const int napp = __shfl_sync(kAll, na_l, j);
+            const int deg = __shfl_sync(kAll, deg_l, j);
+#pragma unroll
+            for (int u = 0; u < kSv; u++) {
+              const int k = lane + 32 * u;
+              svn[u] = staged && k < K && j + 1 < nb ? lds(&S.saved[(size_t)(o + 1) * K + k]) : 0;
+            }
+            const uint32_t* am = S.actm + (size_t)o * words;
+            const uint32_t* om = S.ownm + (size_t)o * words;
+            bool conf = false;
+            for (int x = lane; x < words; x += 32)
+              if ((lds(&am[x]) & rows_new[x]) || (lds(&om[x]) & cols_new[x])) conf = true;
+            if (__any_sync(kAll, conf)) {
+              c1 = c2 = z;
+              stop = true;
+              break;
+            }
+            MsgKey best{0, 0, -1};
+            if (staged) {
+#pragma unroll
+              for (int u = 0; u < kSv; u++) {
+                const int k = lane + 32 * u;
+                if (k < K && (double)sz[k] < I.C) {
+                  const MsgKey c{sv[u], sz[k], k};
+                  if (msg_better(c, best)) best = c;
+                }
+              }
+            } else {
+              const int* sv_in = S.saved + (size_t)o * K;
+              for (int k = lane; k < K; k += 32)
+                if ((double)sz[k] < I.C) {
+                  const MsgKey c{lds(&sv_in[k]), sz[k], k};
+                  if (msg_better(c, best)) best = c;
+                }
+            }
+            best = warp_msg_best(best);
+            const int d2 = best.k >= 0 ? best.k : least_loaded(sz, nullptr, K);
+#pragma unroll
+            for (int u = 0; u < kSv; u++) sv[u] = svn[u];
+            if (d2 != d) {
+              if (napp != deg) {   // new appends: commit last, with d2
+                if (lane == 0) B.dfix[o] = d2;
+                c1 = z;
+                c2 = z + 1;
+                stop = true;
+                break;
+              }
+              bool ncol = false, nrow = false;
+              for (int k = lane; k < K; k += 32) {
+                if (k == d2) continue;
+                if (((lds(&am[k >> 5]) >> (k & 31)) & 1u) &&
+                    !((__ldcg(&S.prow[(size_t)k * words + (d2 >> 5)]) >> (d2 & 31)) & 1u)) {
+                  atomicOr(&rows_new[k >> 5], 1u << (k & 31));
+                  ncol = true;
+                }
+                if (((lds(&om[k >> 5]) >> (k & 31)) & 1u) &&
+                    !((__ldcg(&S.prow[(size_t)d2 * words + (k >> 5)]) >> (k & 31)) & 1u)) {
+                  atomicOr(&cols_new[k >> 5], 1u << (k & 31));
+                  nrow = true;
+                }
+              }
+              const bool any_c = __any_sync(kAll, ncol), any_r = __any_sync(kAll, nrow);
+              if (lane == 0) {
+                if (any_c) atomicOr(&cols_new[d2 >> 5], 1u << (d2 & 31));
+                if (any_r) atomicOr(&rows_new[d2 >> 5], 1u << (d2 & 31));
+                B.dec[o] = d2;
+                B.flag[o] = 1;
+                if (w) B.mlist[lds(&B.midx[o])].z = d2;
+                B.stats[9]++;
+              }
+            }
+            __syncwarp();
+            if (lane == 0 && w) sz[d2] += w;
+            __syncwarp();
+          }
+        }
+        if (lane == 0) {
+          B.ctl[6] = c1;
+          B.ctl[7] = c2;
+        }
+      }
+      if (!grid_barrier(B.bar, I.status)) return;
+      lap(20);
+      cut = lds(&B.ctl[6]);
+      cutc = lds(&B.ctl[7]);
+      for (int p = threadIdx.x; p < K; p += blockDim.x) dsz_cta[p] = 0;
+      __syncthreads();
+      const int nm = lds(&B.mcnt[par]);
+      for (int i = threadIdx.x; i < nm; i += blockDim.x) {
+        const int4 m = lds(&B.mlist[i]);
+        if (m.x < cta_o0) atomicAdd(&dsz_cta[m.z], m.y);
+      }
+      __syncthreads();
+    }
     if (cut <= pos) {
       if (gtid == 0) dev_fail(I.status, kDevErrInvalid);
       return;
@@ -1062,8 +1379,8 @@ __global__ void __launch_bounds__(kSThreads, 2) stream_msg_kernel(DevInstance I,
       const int v = __ldg(&S.porder[z]);
       const uint32_t base = __ldg(&I.vptr[v]);
       const int deg = (int)(__ldg(&I.vptr[v + 1]) - base);
-      const bool fl = z == cut;
-      const int d = fl ? lds(&B.dfix[o]) : lds(&B.dec[o]);
+      const bool fl = z == cut || lds(&B.flag[o]);   // records of another part: located again
+      const int d = z == cut ? lds(&B.dfix[o]) : lds(&B.dec[o]);
       // own-net messages from the window-start lists (before v's placement)
       for (int p = lane; p < K; p += 32) wa[p] = 0;
       for (int x = lane; x < words; x += 32) { wact[x] = 0; wown[x] = 0; }
@@ -1150,6 +1467,7 @@ __global__ void __launch_bounds__(kSThreads, 2) stream_msg_kernel(DevInstance I,
     }
     if (gtid == 0) {
       B.ctl[4 + (par ^ 1)] = kNone;
+      B.ctl[2 + (par ^ 1)] = kNone;
       B.mcnt[par ^ 1] = 0;
     }
     for (int p = gtid; p < K; p += gridDim.x * blockDim.x) {
@@ -1159,7 +1477,8 @@ __global__ void __launch_bounds__(kSThreads, 2) stream_msg_kernel(DevInstance I,
     if (stats) {
       B.stats[0]++;
       B.stats[2] += cutc - pos;
-      if (cutw != kNone) B.stats[(cutw & 7) == 2 ? 5 : 8]++;
+      if (cutc > cut) B.stats[5]++;
+      else if (cut < end_w) B.stats[8]++;
     }
     if (cutc >= end_w) {
       if (end_w == pos + W) W = min(2 * W, S.msg_wmax);
@@ -1211,7 +1530,8 @@ size_t stream_msg_smem_bytes(int K) {
   auto a = [](size_t n) { return (n + 15) & ~size_t(15); };
   const size_t words = (size_t)(K + 31) / 32;
   return 2 * a(sizeof(int) * K) + 2 * a(sizeof(int) * (size_t)K * kSWarps) + 2 * a(sizeof(uint32_t) * words * kSWarps) +
-         a(sizeof(int) * 32 * kSWarps) + 2 * a(sizeof(int) * K) + 2 * a(sizeof(uint32_t) * words);
+         a(sizeof(int) * 32 * kSWarps) + 2 * a(sizeof(int) * K) + 2 * a(sizeof(uint32_t) * words) +
+         (K <= kMsgStageK ? 2 * a(sizeof(uint32_t) * K * words) : 0);
 }
 
 cudaError_t launch_stream_msg(const DevInstance& I, const SpecBuf& B, const StreamArgs& S, int num_sms,

@@ -180,6 +180,11 @@ int fp_set_engine(fp_instance* inst, int32_t engine);
  * by one CTA, with more than super_work pins by the whole grid (defaults 128
  * and 1024). */
 int fp_set_classes(fp_instance* inst, int64_t light_work, int64_t super_work);
+/* Tuning of the speculative engine's window lengths (no effect on results;
+ * TV / MSV / MSRV): after a window ends early, the next one is `grow` times
+ * the committed length, at least `min_len` positions (0: one per warp of the
+ * grid).  Defaults 0 and 2 (MSV) or 4 (TV, MSRV). */
+int fp_set_window(fp_instance* inst, int32_t min_len, int32_t grow);
 int fp_metrics(fp_instance* inst, int64_t out[6]);
 
 /* Copies of the current device state (caller-allocated host buffers). */
