@@ -65,8 +65,10 @@ constexpr int kCnGridPins = 1024;   //     with more than this by the whole grid
 int default_super_work(int metric) {
   switch (metric) {
     case FP_METRIC_MSV: return 16384;
-    case FP_METRIC_MSRV:
-    case FP_METRIC_TM: return 32768;
+    case FP_METRIC_MSRV: return 32768;
+    // measured on the 4M-vertex Zipf workload: passes 2-3 at 84 / 77 ms
+    // against 94 / 90 with 32768 (pass 1 152 against 140)
+    case FP_METRIC_TM: return 65536;
     default: return 262144;
   }
 }

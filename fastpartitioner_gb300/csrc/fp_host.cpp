@@ -574,13 +574,19 @@ int fp_partition_gpu(int32_t metric, const uint32_t* row_ptr, const uint32_t* co
     g.pins = pins;
     g.vptr.assign(row_ptr, row_ptr + nov + 1);
     g.vnets.assign(col_ind, col_ind + pins);
+    fp_ctx* ctx = nullptr;
+    int rc = fp_ctx_create(0, &ctx);
+    if (rc) return rc;
     if (row_ptr_inv && col_ind_inv) {
       g.nptr.assign(row_ptr_inv, row_ptr_inv + noe + 1);
       g.npins.assign(col_ind_inv, col_ind_inv + pins);
     } else {
-      for (long long k = 0; k < pins; k++)
-        if (g.vnets[k] >= (uint32_t)noe) return FP_ERR_INVALID;
-      build_net_csr(g);
+      // the reference's createInverse, on the device (fp_create_inverse)
+      g.nptr.resize((size_t)noe + 1);
+      g.npins.resize((size_t)std::max<long long>(pins, 1));
+      rc = fp_create_inverse(ctx, nov, noe, pins, row_ptr, col_ind, g.nptr.data(), g.npins.data());
+      g.npins.resize(pins);
+      if (rc) { fp_ctx_destroy(ctx); return rc; }
     }
     g.src.assign(src_nodes, src_nodes + noe);
     fp_hypergraph h;
@@ -595,10 +601,7 @@ int fp_partition_gpu(int32_t metric, const uint32_t* row_ptr, const uint32_t* co
     h.weights = nullptr;
     h.ordering = ordering;
 
-    fp_ctx* ctx = nullptr;
     fp_instance* inst = nullptr;
-    int rc = fp_ctx_create(0, &ctx);
-    if (rc) return rc;
     rc = fp_instance_create(ctx, &h, K, metric, 1.05, &inst);
     if (rc) { fp_ctx_destroy(ctx); return rc; }
     int64_t before[6] = {0}, after[6] = {-1, -1, -1, -1, -1, -1};

@@ -176,7 +176,7 @@ int fp_set_engine(fp_instance* inst, int32_t engine);
  * TM / MSM: a vertex whose work -- the sum over its nets of min(net size, K) --
  * is at most light_work is evaluated by one warp, at most super_work by one
  * CTA, above it by the whole grid.  Defaults: 2048 and 262144 (MSV 16384,
- * MSRV and TM 32768).  CN: a net with more than light_work pins is evaluated
+ * MSRV 32768, TM 65536).  CN: a net with more than light_work pins is evaluated
  * by one CTA, with more than super_work pins by the whole grid (defaults 128
  * and 1024). */
 int fp_set_classes(fp_instance* inst, int64_t light_work, int64_t super_work);
