@@ -262,6 +262,32 @@ __device__ int record_slots(const DevInstance& I, const SpecBuf& B, const Stream
   return napp;   // every lane
 }
 
+// The walk takes a changed decision d of position z that appends where the old
+// one did not: the nets d is appended to are claimed for z (the earliest
+// claim wins), and the walk checks every later position against the claims
+// again.  One warp.
+__device__ void claim_appends(const DevInstance& I, const SpecBuf& B, int v, int round, int z, int d, int* sd) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t base = __ldg(&I.vptr[v]);
+  const int deg = (int)(__ldg(&I.vptr[v + 1]) - base);
+  for (int nb = 0; nb < deg; nb += 32) {
+    const int j = locate_part(I, base, nb, deg, d, sd);
+    const int k = nb + lane;
+    if (k < deg && j < 0) atomicMax(&B.claim64[(int)__ldg(&I.vnets[base + k])], skey(round, z));
+  }
+}
+
+// Does an earlier position of the round claim one of position z's nets (v's)?
+// One warp; every lane gets the answer.
+__device__ bool conflicts_now(const DevInstance& I, const SpecBuf& B, int v, int round, int z) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t base = __ldg(&I.vptr[v]);
+  const int deg = (int)(__ldg(&I.vptr[v + 1]) - base);
+  bool conf = false;
+  for (int k = lane; k < deg && !conf; k += 32) conf = claimed_before(B, round, (int)__ldg(&I.vnets[base + k]), z);
+  return __any_sync(kAll, conf);
+}
+
 // Nets of window offset o listing part d (its candidate entry's count; 0 if d
 // is not a candidate).  One warp.
 __device__ int cand_count(const SpecBuf& B, int K, int o, int d) {
@@ -291,7 +317,7 @@ __device__ void place_iso(const DevInstance& I, const StreamArgs& S, const int* 
   for (int k = k0 + lane; k < k1; k += 32) I.part_vec[__ldg(&S.iso_list[k])] = d;
 }
 
-__global__ void __launch_bounds__(kSThreads, 1) stream_ldg_kernel(DevInstance I, SpecBuf B, StreamArgs S) {
+__global__ void __launch_bounds__(kSThreads, 2) stream_ldg_kernel(DevInstance I, SpecBuf B, StreamArgs S) {
   barrier_start();
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ unsigned long long uscr[kSWarps];
@@ -579,7 +605,7 @@ __global__ void __launch_bounds__(kSThreads, 1) stream_ldg_kernel(DevInstance I,
         }
         __syncwarp();
         int c1 = zc, c2 = zc;
-        bool stop = false;
+        bool stop = false, reclaim = false;
         // 32 positions at a time: their scalar words one per lane, and the
         // next position's first 32 candidates loaded while one is decided
         for (int zb = zf; zb < zc && !stop; zb += 32) {
@@ -589,10 +615,10 @@ __global__ void __launch_bounds__(kSThreads, 1) stream_ldg_kernel(DevInstance I,
           const int d_l = in ? lds(&B.dec[ol]) : 0;
           const int w_l = in ? lds(&B.wt[ol]) : 0;
           const int na_l = in ? lds(&B.slack[ol]) : 0;
-          int deg_l = 0;
+          int deg_l = 0, v_l = 0;
           if (in) {
-            const int v = __ldg(&S.porder[zl]);
-            deg_l = (int)(__ldg(&I.vptr[v + 1]) - __ldg(&I.vptr[v]));
+            v_l = __ldg(&S.porder[zl]);
+            deg_l = (int)(__ldg(&I.vptr[v_l + 1]) - __ldg(&I.vptr[v_l]));
           }
           const int nb = min(32, zc - zb);
           unsigned long long ent = 0;
@@ -607,7 +633,13 @@ __global__ void __launch_bounds__(kSThreads, 1) stream_ldg_kernel(DevInstance I,
             const int w = __shfl_sync(kAll, w_l, j);
             const int napp = __shfl_sync(kAll, na_l, j);
             const int deg = __shfl_sync(kAll, deg_l, j);
+            const int vz = __shfl_sync(kAll, v_l, j);
             const int ncn = __shfl_sync(kAll, nc_l, (j + 1) & 31);
+            if (reclaim && conflicts_now(I, B, vz, round, z)) {   // a taken change appends to one of its nets
+              c1 = c2 = z;
+              stop = true;
+              break;
+            }
             unsigned long long ent_next = 0;
             if (j + 1 < nb && lane < ncn) ent_next = lds(&B.cand[(size_t)(o + 1) * K + lane]);
             LdgKey best{-1.0, 0, -1, ~0ull};
@@ -628,14 +660,12 @@ __global__ void __launch_bounds__(kSThreads, 1) stream_ldg_kernel(DevInstance I,
               break;
             }
             if (d2 != d) {
-              // the old decision appended to every net, or the new one to none
+              // the old decision appended to every net, or the new one to none:
+              // no new claim; else the new appends are claimed
               const bool safe = napp == deg || (!cn && cand_count(B, K, o, d2) == deg);
               if (!safe) {
-                if (lane == 0) B.dfix[o] = d2;
-                c1 = z;
-                c2 = z + 1;
-                stop = true;
-                break;
+                claim_appends(I, B, vz, round, z, d2, sd);
+                reclaim = true;
               }
               if (lane == 0) {
                 B.dec[o] = d2;
@@ -1249,7 +1279,7 @@ __global__ void __launch_bounds__(kSThreads, 2) stream_msg_kernel(DevInstance I,
         }
         __syncwarp();
         int c1 = zc, c2 = zc;
-        bool stop = false;
+        bool stop = false, reclaim = false;
         constexpr int kSv = kMsgStageK / 32;   // saved values a lane prefetches (K <= kMsgStageK)
         // 32 positions at a time: their scalar words one per lane; the next
         // position's saved messages loaded while one is decided (K <= 256)
@@ -1259,10 +1289,10 @@ __global__ void __launch_bounds__(kSThreads, 2) stream_msg_kernel(DevInstance I,
           const int d_l = in ? lds(&B.dec[ol]) : 0;
           const int w_l = in ? lds(&B.wt[ol]) : 0;
           const int na_l = in ? lds(&B.slack[ol]) : 0;
-          int deg_l = 0;
+          int deg_l = 0, v_l = 0;
           if (in) {
-            const int v = __ldg(&S.porder[zl]);
-            deg_l = (int)(__ldg(&I.vptr[v + 1]) - __ldg(&I.vptr[v]));
+            v_l = __ldg(&S.porder[zl]);
+            deg_l = (int)(__ldg(&I.vptr[v_l + 1]) - __ldg(&I.vptr[v_l]));
           }
           const int nb = min(32, zc - zb);
           int sv[kSv], svn[kSv];
@@ -1277,6 +1307,7 @@ __global__ void __launch_bounds__(kSThreads, 2) stream_msg_kernel(DevInstance I,
             const int w = __shfl_sync(kAll, w_l, j);
             const int napp = __shfl_sync(kAll, na_l, j);
             const int deg = __shfl_sync(kAll, deg_l, j);
+            const int vz = __shfl_sync(kAll, v_l, j);
 #pragma unroll
             for (int u = 0; u < kSv; u++) {
               const int k = lane + 32 * u;
@@ -1287,7 +1318,7 @@ __global__ void __launch_bounds__(kSThreads, 2) stream_msg_kernel(DevInstance I,
             bool conf = false;
             for (int x = lane; x < words; x += 32)
               if ((lds(&am[x]) & rows_new[x]) || (lds(&om[x]) & cols_new[x])) conf = true;
-            if (__any_sync(kAll, conf)) {
+            if (__any_sync(kAll, conf) || (reclaim && conflicts_now(I, B, vz, round, z))) {
               c1 = c2 = z;
               stop = true;
               break;
@@ -1315,12 +1346,9 @@ __global__ void __launch_bounds__(kSThreads, 2) stream_msg_kernel(DevInstance I,
 #pragma unroll
             for (int u = 0; u < kSv; u++) sv[u] = svn[u];
             if (d2 != d) {
-              if (napp != deg) {   // new appends: commit last, with d2
-                if (lane == 0) B.dfix[o] = d2;
-                c1 = z;
-                c2 = z + 1;
-                stop = true;
-                break;
+              if (napp != deg) {   // new appends: claimed; later positions check them
+                claim_appends(I, B, vz, round, z, d2, sd);
+                reclaim = true;
               }
               bool ncol = false, nrow = false;
               for (int k = lane; k < K; k += 32) {
