@@ -674,6 +674,8 @@ def run_stream(args):
     with fp.Engine(0) as eng:
         for m in metrics:
             with eng.instance(hg, w["K"], m, w["eps"]) as inst:
+                if args.stream_walk >= 0:
+                    inst.set_stream_walk(bool(args.stream_walk))
                 t = {}
                 st = {}
                 for where in ["device"] * (args.warmup + 1) + ["host"]:
@@ -698,7 +700,7 @@ def run_stream(args):
         "n_gpus": 1, "steps": 1, "warmup": args.warmup, "ms_per_step": 1e3 * dev, "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded generator)",
         "config": {"workload": workload_text(args.config, w, hg.nov, hg.noe, hg.pins, 0, metrics, "degree"),
-                   "host_s": host, "per_metric": per,
+                   "stream_walk": args.stream_walk, "host_s": host, "per_metric": per,
                    "same_as_host": all(v["same"] for v in per.values())},
     }
     print(json.dumps(line), flush=True)
@@ -792,6 +794,9 @@ def main():
     ap.add_argument("--budget-gb", type=float, default=150.0)
     ap.add_argument("--slots", type=int, default=32, help="serve: requests admitted at once")
     ap.add_argument("--gpu-slots", type=int, default=4, help="batch / serve: concurrent GPU slots")
+    ap.add_argument("--stream-walk", type=int, default=-1,
+                    help="stream: 1 / 0 walks changed decisions in the device stream's windows or not "
+                         "(default: the library's per-metric choice)")
     args = ap.parse_args()
     if args.mode == "batch":
         run_batch(args)

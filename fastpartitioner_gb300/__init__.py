@@ -129,6 +129,7 @@ def lib():
             "fp_instance_footprint": ([i32, i32, i64, i32, i32, C.POINTER(i64)], C.c_int),
             "fp_initial_partition": ([vp], C.c_int),
             "fp_set_stream_mode": ([vp, i32, C.POINTER(i32)], C.c_int),
+            "fp_set_stream_walk": ([vp, i32], C.c_int),
             "fp_refine": ([vp, i32], C.c_int),
             "fp_reset_state": ([vp], C.c_int),
             "fp_set_engine": ([vp, i32], C.c_int),
@@ -467,6 +468,11 @@ class Instance:
         if where not in modes:
             raise ValueError(f"stream must be one of {sorted(modes)}")
         _check(lib().fp_set_stream_mode(self._h, modes[where], None), "fp_set_stream_mode")
+
+    def set_stream_walk(self, on: bool) -> None:
+        """fp_set_stream_walk: the device stream walks changed decisions
+        inside its windows (tuning only)."""
+        _check(lib().fp_set_stream_walk(self._h, int(bool(on))), "fp_set_stream_walk")
 
     def streamed_on_device(self) -> bool:
         """True if the last initial_partition ran on the device."""

@@ -1028,6 +1028,14 @@ int fp_initial_partition(fp_instance* in) {
   });
 }
 
+int fp_set_stream_walk(fp_instance* in, int32_t walk) {
+  return fp::guarded([&]() -> int {
+    if (!in || walk < 0 || walk > 1) return FP_ERR_INVALID;
+    in->sa.walk = walk;
+    return FP_OK;
+  });
+}
+
 int fp_set_stream_mode(fp_instance* in, int32_t mode, int32_t* last_on_device) {
   return fp::guarded([&]() -> int {
     if (!in || mode < -1 || mode > 2) return FP_ERR_INVALID;

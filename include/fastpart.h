@@ -151,6 +151,11 @@ int fp_initial_partition(fp_instance* inst);
  * ran on the device.  No counterpart in the reference (its stream is CPU
  * code). */
 int fp_set_stream_mode(fp_instance* inst, int32_t mode, int32_t* last_on_device);
+/* Tuning of the device stream (no effect on results): walk = 1 lets a window
+ * continue past the decisions that change with the exact sizes (one warp
+ * takes them in order), 0 ends the window at the first.  Defaults: 1 for CN,
+ * TM and MSM, 0 for TV, MSV and MSRV.  TM / MSM always walk. */
+int fp_set_stream_walk(fp_instance* inst, int32_t walk);
 
 /* Copies the host-side result of the last fp_initial_partition to the device
  * again (host -> device), discarding device-side refinement: the upload leg of

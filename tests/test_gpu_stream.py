@@ -126,3 +126,36 @@ def test_device_stream_only_where_it_qualifies(fp, gpu_engine):
         want = fp.stream_partition(hg, K, metric)
         for f in fields(metric):
             np.testing.assert_array_equal(st[f], want[f], err_msg=f)
+
+
+@pytest.mark.parametrize("metric", ("TV", "CN", "MSRV"))
+def test_stream_walk_setting_leaves_the_result(fp, gpu_engine, metric):
+    """fp_set_stream_walk (walk the changed decisions in a window, or end the
+    window at the first) is tuning only: the same state either way."""
+    hg = heavy_case(fp, 89)
+    states = []
+    for walk in (0, 1):
+        with gpu_engine.instance(hg, 16, metric) as inst:
+            inst.set_stream("device")
+            inst.set_stream_walk(bool(walk))
+            inst.initial_partition()
+            assert inst.streamed_on_device()
+            states.append(inst.get_state())
+    for f in fields(metric):
+        np.testing.assert_array_equal(states[0][f], states[1][f], err_msg=f"{metric} {f}")
+
+
+@pytest.mark.parametrize("metric", ("TV", "MSV", "MSRV"))
+def test_window_setting_leaves_the_refinement(fp, orc, gpu_engine, metric):
+    """fp_set_window (window length after a cut) is tuning only."""
+    hg = fp.generate(fp.GenSpec.zipf(20000, 15000, 2.0, 2, 400, beta=1.0, weight_rule=1, seed=90))
+    o = orc.run_oracle(hg, 64, metric, 3)
+    assert o["status"] == 0
+    with gpu_engine.instance(hg, 64, metric) as inst:
+        inst.initial_partition()
+        for wmin, grow in ((0, 2), (256, 4), (4096, 1)):
+            inst.reset_state()
+            inst.set_window(wmin, grow)
+            inst.refine(3)
+            np.testing.assert_array_equal(inst.partition(), o["part_vec"], err_msg=f"{metric} {wmin} {grow}")
+            assert inst.metrics() == o["metrics_final"], (metric, wmin, grow)
