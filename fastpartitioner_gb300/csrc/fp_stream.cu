@@ -1,7 +1,9 @@
 // Streaming initial partitions on the device: the LDG streams of TV
 // (TV/partition.cpp:207-264, LDG2 without a current part), MSV
 // (MGV/partition.cpp:122-189) and MSRV (MSRV/partition.cpp:123-196), and CN's
-// stream (CN/partition.cpp:132-221).
+// stream (CN/partition.cpp:132-221), in stream_ldg_kernel; the
+// message-greedy streams of TM and MSM (TM/partition.cpp:87-250,
+// MSM/partition.cpp:146-309) in stream_msg_kernel, further down.
 //
 // The reference places the vertices one by one in visiting order: a vertex
 // scores every part listed on its nets (the number of its nets listing it,
@@ -22,16 +24,24 @@
 //   B  validate  a position keeps its decision iff no earlier position of the
 //                window appends to one of its nets and the decision taken again
 //                with the exact sizes at its place (the window-start sizes plus
-//                the earlier placements) is the same;
-//   C  commit    the positions before the first invalid one are applied at
-//                once: on any net at most one of them appends (a later reader
-//                of that net is invalid), the others increment counts.
+//                the earlier placements) is the same.  The window ends at the
+//                first conflict; at the first changed decision it either ends
+//                too (that position commits last, with its exact decision) or,
+//                with StreamArgs::walk, one warp walks on in order with exact
+//                sizes, taking every change (a change that appends where the
+//                old decision did not claims those nets, and the later
+//                positions are checked against the claims again);
+//   C  commit    the positions before the cut are applied at once: on any net
+//                at most one of them appends (a later reader of that net is
+//                invalid), the others increment counts at their recorded slots
+//                (changed decisions locate theirs again).
 //
 // Vertices without nets read only the sizes.  When all of them weigh 0 (vertex
 // weight = degree) they are not positions: after each window's commit they take
-// the least-loaded part of the sizes at their place.  A vertex with many nets
-// (kStreamHeavy or more) is a window of its own, evaluated and committed by the
-// whole grid.
+// the least-loaded part of the sizes at their place.  A position is evaluated
+// by a warp, by a CTA when its lists are long (kStreamCtaWork entries or more),
+// and a vertex with many nets (kStreamHeavy or more, or kStreamGridWork list
+// entries) is a window of its own, evaluated and committed by the whole grid.
 
 #include "fp_spec_common.cuh"
 
